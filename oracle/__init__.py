@@ -1,0 +1,338 @@
+"""ctypes binding of the CPU restatement of partapp's inference hot path.
+
+TEST INFRASTRUCTURE ONLY.  The product (the ``partapp_gb300`` package and its
+CUDA library) never imports this module.  It is used by ``tests/``, by
+``__graft_entry__.smoke()`` as the checker, and by ``bench.py`` for the timed
+CPU baseline / reference arm.
+
+The C++ sources next to this file restate the reference functions cited in
+``oracle.h``; ``build()`` compiles them with the committed Makefile into
+``oracle/_build/liboracle.so``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+_lock = threading.Lock()
+
+LOG_ZERO = -1e6
+NO_CLASS_VALUE = 0.0
+
+
+class OrcExp(C.Structure):
+    _fields_ = [
+        ("num_rotation_steps", C.c_int),
+        ("min_part_rotation", C.c_float),
+        ("max_part_rotation", C.c_float),
+        ("min_object_scale", C.c_float),
+        ("max_object_scale", C.c_float),
+        ("strip_border_detections", C.c_float),
+        ("max_local_max", C.c_int),
+        ("use_pairwise", C.c_int),
+    ]
+
+
+class OrcTree(C.Structure):
+    _fields_ = [
+        ("n_parts", C.c_int),
+        ("root", C.c_int),
+        ("is_upright", C.POINTER(C.c_int)),
+        ("n_joints", C.c_int),
+        ("child", C.POINTER(C.c_int)),
+        ("parent", C.POINTER(C.c_int)),
+        ("offset_c", C.POINTER(C.c_double)),
+        ("offset_p", C.POINTER(C.c_double)),
+        ("C", C.POINTER(C.c_double)),
+        ("rot_mean", C.POINTER(C.c_double)),
+        ("rot_sigma", C.POINTER(C.c_double)),
+    ]
+
+
+class OrcModels(C.Structure):
+    _fields_ = [
+        ("n_parts", C.c_int),
+        ("n_stumps", C.c_int),
+        ("f", C.POINTER(C.c_int32)),
+        ("p", C.POINTER(C.c_float)),
+        ("theta", C.POINTER(C.c_float)),
+        ("alpha", C.POINTER(C.c_float)),
+        ("sum_alpha", C.POINTER(C.c_float)),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the Makefile beside this file."""
+    with _lock:
+        if force or not os.path.exists(_LIB_PATH) or _stale():
+            subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def _stale() -> bool:
+    t = os.path.getmtime(_LIB_PATH)
+    return any(os.path.getmtime(os.path.join(_HERE, f)) > t for f in ("oracle.cpp", "oracle.h"))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(_LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+def _declare(L):
+    fp, ip, dp = C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.orc_adaboost_eval.argtypes = [C.POINTER(C.c_int32), fp, fp, fp, C.c_int, C.c_float, fp,
+                                    C.c_int64, C.c_int, C.c_int, fp]
+    L.orc_adaboost_eval.restype = None
+    L.orc_sum_alpha.argtypes = [fp, C.c_int]
+    L.orc_sum_alpha.restype = C.c_float
+    L.orc_score_grid_window.argtypes = [C.POINTER(C.c_int32), fp, fp, fp, C.c_int, C.c_float, fp,
+                                        C.POINTER(C.c_uint8), C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_int, C.c_double, C.c_int, fp]
+    L.orc_score_grid_window.restype = None
+    L.orc_squeeze_bbox.argtypes = [fp, C.c_int, C.c_int, ip]
+    L.orc_squeeze_bbox.restype = C.c_int
+    L.orc_transform_grid.argtypes = [fp, C.c_int, C.c_int, fp, C.c_int, C.c_int, dp, C.c_float,
+                                     C.c_int]
+    L.orc_transform_grid.restype = None
+    L.orc_clip_log.argtypes = [fp, C.c_int64]
+    L.orc_clip_log.restype = None
+    L.orc_gaussian_filter.argtypes = [C.c_double, dp]
+    L.orc_gaussian_filter.restype = C.c_int
+    for suf, t in (("f32", fp), ("f64", dp)):
+        fn = getattr(L, "orc_rot_joint_marginal_" + suf)
+        fn.argtypes = [C.POINTER(OrcExp), t, t, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.c_double,
+                       C.c_double, C.c_double]
+        fn.restype = C.c_int
+        fn = getattr(L, "orc_ps_infer_" + suf)
+        fn.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree), t, C.c_int, C.c_int, t, fp, t, fp, ip,
+                       fp, ip]
+        fn.restype = C.c_int
+    L.orc_find_local_max.argtypes = [fp, C.c_int, C.c_int, C.c_int, C.c_int, dp]
+    L.orc_find_local_max.restype = C.c_int
+    L.orc_find_obj_f32.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree), C.POINTER(OrcModels), fp,
+                                   C.c_int, C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, fp, fp,
+                                   fp, fp, fp, ip, fp, ip]
+    L.orc_find_obj_f32.restype = C.c_int
+    L.orc_find_obj_batch_f32.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree),
+                                         C.POINTER(OrcModels), C.c_int, C.POINTER(fp), C.c_int,
+                                         C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, fp,
+                                         C.c_int]
+    L.orc_find_obj_batch_f32.restype = C.c_int
+
+
+# ---------------------------------------------------------------------------
+# Python-facing helpers.  Arrays are numpy, C-contiguous.
+# ---------------------------------------------------------------------------
+
+def make_exp(R=24, min_rot=-180.0, max_rot=180.0, scale=1.0, strip=0.0, max_local_max=1000,
+             use_pairwise=True) -> OrcExp:
+    return OrcExp(int(R), float(min_rot), float(max_rot), float(scale), float(scale), float(strip),
+                  int(max_local_max), int(bool(use_pairwise)))
+
+
+class _TreeHolder:
+    """Keeps the numpy arrays behind an OrcTree alive."""
+
+    def __init__(self, tree):
+        P = int(tree["n_parts"])
+        self.is_upright = np.ascontiguousarray(tree["is_upright"], dtype=np.int32)
+        self.child = np.ascontiguousarray(tree["child"], dtype=np.int32)
+        self.parent = np.ascontiguousarray(tree["parent"], dtype=np.int32)
+        self.offset_c = np.ascontiguousarray(tree["offset_c"], dtype=np.float64)
+        self.offset_p = np.ascontiguousarray(tree["offset_p"], dtype=np.float64)
+        self.C = np.ascontiguousarray(tree["C"], dtype=np.float64)
+        self.rot_mean = np.ascontiguousarray(tree["rot_mean"], dtype=np.float64)
+        self.rot_sigma = np.ascontiguousarray(tree["rot_sigma"], dtype=np.float64)
+        self.s = OrcTree(P, int(tree["root"]), _p(self.is_upright, C.c_int), len(self.child),
+                         _p(self.child, C.c_int), _p(self.parent, C.c_int),
+                         _p(self.offset_c, C.c_double), _p(self.offset_p, C.c_double),
+                         _p(self.C, C.c_double), _p(self.rot_mean, C.c_double),
+                         _p(self.rot_sigma, C.c_double))
+
+
+class _ModelsHolder:
+    def __init__(self, models):
+        self.f = np.ascontiguousarray(models["f"], dtype=np.int32)
+        self.p = np.ascontiguousarray(models["p"], dtype=np.float32)
+        self.theta = np.ascontiguousarray(models["theta"], dtype=np.float32)
+        self.alpha = np.ascontiguousarray(models["alpha"], dtype=np.float32)
+        P, S = self.f.shape
+        self.sum_alpha = np.array([sum_alpha(self.alpha[i]) for i in range(P)], dtype=np.float32)
+        self.s = OrcModels(P, S, _p(self.f, C.c_int32), _p(self.p, C.c_float),
+                           _p(self.theta, C.c_float), _p(self.alpha, C.c_float),
+                           _p(self.sum_alpha, C.c_float))
+
+
+def sum_alpha(alpha) -> float:
+    a = np.ascontiguousarray(alpha, dtype=np.float32)
+    return float(lib().orc_sum_alpha(_p(a, C.c_float), len(a)))
+
+
+def adaboost_eval(f, p, theta, alpha, desc, normalize=True, sum_alpha_value=None):
+    f = np.ascontiguousarray(f, dtype=np.int32)
+    p = np.ascontiguousarray(p, dtype=np.float32)
+    theta = np.ascontiguousarray(theta, dtype=np.float32)
+    alpha = np.ascontiguousarray(alpha, dtype=np.float32)
+    desc = np.ascontiguousarray(desc, dtype=np.float32)
+    D = desc.shape[-1]
+    n = desc.size // D
+    sa = sum_alpha(alpha) if sum_alpha_value is None else float(sum_alpha_value)
+    out = np.empty(desc.shape[:-1], dtype=np.float32)
+    lib().orc_adaboost_eval(_p(f, C.c_int32), _p(p, C.c_float), _p(theta, C.c_float),
+                            _p(alpha, C.c_float), len(f), sa, _p(desc, C.c_float), n, D,
+                            int(normalize), _p(out, C.c_float))
+    return out
+
+
+def score_grid_window(f, p, theta, alpha, cells, valid, gx, gy, grid_step, normalize=True):
+    f = np.ascontiguousarray(f, dtype=np.int32)
+    p = np.ascontiguousarray(p, dtype=np.float32)
+    theta = np.ascontiguousarray(theta, dtype=np.float32)
+    alpha = np.ascontiguousarray(alpha, dtype=np.float32)
+    cells = np.ascontiguousarray(cells, dtype=np.float32)
+    valid = np.ascontiguousarray(valid, dtype=np.uint8)
+    ny, nx, Dc = cells.shape
+    out = np.empty((ny, nx), dtype=np.float32)
+    lib().orc_score_grid_window(_p(f, C.c_int32), _p(p, C.c_float), _p(theta, C.c_float),
+                                _p(alpha, C.c_float), len(f), sum_alpha(alpha),
+                                _p(cells, C.c_float), _p(valid, C.c_uint8), ny, nx, Dc, int(gx),
+                                int(gy), float(grid_step), int(normalize), _p(out, C.c_float))
+    return out
+
+
+def squeeze_bbox(grid):
+    g = np.ascontiguousarray(grid, dtype=np.float32)
+    bbox = np.zeros(4, dtype=np.int32)
+    crop = lib().orc_squeeze_bbox(_p(g, C.c_float), g.shape[0], g.shape[1], _p(bbox, C.c_int))
+    return bool(crop), bbox
+
+
+def transform_grid(grid_in, out_shape, T21, default=0.0, method=1):
+    g = np.ascontiguousarray(grid_in, dtype=np.float32)
+    T = np.ascontiguousarray(T21, dtype=np.float64).reshape(9)
+    out = np.empty(out_shape, dtype=np.float32)
+    lib().orc_transform_grid(_p(g, C.c_float), g.shape[0], g.shape[1], _p(out, C.c_float),
+                             out_shape[0], out_shape[1], _p(T, C.c_double), float(default),
+                             int(method))
+    return out
+
+
+def clip_log(grid):
+    g = np.array(grid, dtype=np.float32, copy=True, order="C")
+    lib().orc_clip_log(_p(g, C.c_float), g.size)
+    return g
+
+
+def gaussian_filter(sigma):
+    buf = np.zeros(int(2 * np.floor(3 * sigma + 0.5) + 1) + 8, dtype=np.float64)
+    n = lib().orc_gaussian_filter(float(sigma), _p(buf, C.c_double))
+    return buf[:n].copy()
+
+
+def rot_joint_marginal(exp: OrcExp, child, offset_c, offset_p, Cmat, rot_mean, rot_sigma,
+                       scale=1.0, f64=False):
+    dt, ct = (np.float64, C.c_double) if f64 else (np.float32, C.c_float)
+    child = np.ascontiguousarray(child, dtype=dt)
+    R, H, W = child.shape
+    out = np.empty_like(child)
+    oc = np.ascontiguousarray(offset_c, dtype=np.float64)
+    op = np.ascontiguousarray(offset_p, dtype=np.float64)
+    Cm = np.ascontiguousarray(Cmat, dtype=np.float64).reshape(4)
+    fn = lib().orc_rot_joint_marginal_f64 if f64 else lib().orc_rot_joint_marginal_f32
+    rc = fn(C.byref(exp), _p(child, ct), _p(out, ct), R, H, W, _p(oc, C.c_double),
+            _p(op, C.c_double), _p(Cm, C.c_double), float(rot_mean), float(rot_sigma),
+            float(scale))
+    if rc:
+        raise ValueError(f"orc_rot_joint_marginal failed: {rc}")
+    return out
+
+
+def ps_infer(exp: OrcExp, tree, log_unary, f64=False, want_marg=True, want_hyps=True):
+    """Returns dict(log_marg, best_conf, root_post, part_hyps, n_part_hyps, root_hyps,
+    n_root_hyps)."""
+    dt, ct = (np.float64, C.c_double) if f64 else (np.float32, C.c_float)
+    u = np.ascontiguousarray(log_unary, dtype=dt)
+    P, R, H, W = u.shape
+    th = _TreeHolder(tree)
+    K = exp.max_local_max
+    marg = np.empty_like(u) if want_marg else None
+    best = np.zeros((P, 7), dtype=np.float32)
+    rp = np.empty((H, W), dtype=dt)
+    ph = np.zeros((P, K, 7), dtype=np.float32) if want_hyps else None
+    nph = np.zeros(P, dtype=np.int32)
+    rh = np.zeros((1000, 4), dtype=np.float32) if want_hyps else None
+    nrh = np.zeros(1, dtype=np.int32)
+    fn = lib().orc_ps_infer_f64 if f64 else lib().orc_ps_infer_f32
+    rc = fn(C.byref(exp), C.byref(th.s), _p(u, ct), H, W, _p(marg, ct), _p(best, C.c_float),
+            _p(rp, ct), _p(ph, C.c_float), _p(nph, C.c_int), _p(rh, C.c_float), _p(nrh, C.c_int))
+    if rc:
+        raise ValueError(f"orc_ps_infer failed: {rc}")
+    return dict(log_marg=marg, best_conf=best, root_post=rp, part_hyps=ph, n_part_hyps=nph,
+                root_hyps=rh, n_root_hyps=int(nrh[0]))
+
+
+def find_local_max(grid, max_n):
+    g = np.ascontiguousarray(grid, dtype=np.float32)
+    S, H, W = g.shape
+    out = np.zeros((max(max_n, 1), 4), dtype=np.float64)
+    n = lib().orc_find_local_max(_p(g, C.c_float), S, H, W, int(max_n), _p(out, C.c_double))
+    return out[:n].copy()
+
+
+def find_obj(exp: OrcExp, tree, models, desc, Tig, H, W, interpolate=True):
+    """Whole --find_obj path for one image; desc is [R][ny][nx][D]."""
+    desc = np.ascontiguousarray(desc, dtype=np.float32)
+    R, ny, nx, D = desc.shape
+    th, mh = _TreeHolder(tree), _ModelsHolder(models)
+    P = th.s.n_parts
+    K = exp.max_local_max
+    T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(9)
+    lu = np.empty((P, R, H, W), dtype=np.float32)
+    marg = np.empty((P, R, H, W), dtype=np.float32)
+    best = np.zeros((P, 7), dtype=np.float32)
+    rp = np.empty((H, W), dtype=np.float32)
+    ph = np.zeros((P, K, 7), dtype=np.float32)
+    nph = np.zeros(P, dtype=np.int32)
+    rh = np.zeros((1000, 4), dtype=np.float32)
+    nrh = np.zeros(1, dtype=np.int32)
+    fp = C.c_float
+    rc = lib().orc_find_obj_f32(C.byref(exp), C.byref(th.s), C.byref(mh.s), _p(desc, fp), ny, nx,
+                                D, _p(T, C.c_double), int(interpolate), H, W, _p(lu, fp),
+                                _p(marg, fp), _p(best, fp), _p(rp, fp), _p(ph, fp),
+                                _p(nph, C.c_int), _p(rh, fp), _p(nrh, C.c_int))
+    if rc:
+        raise ValueError(f"orc_find_obj failed: {rc}")
+    return dict(log_unary=lu, log_marg=marg, best_conf=best, root_post=rp, part_hyps=ph,
+                n_part_hyps=nph, root_hyps=rh, n_root_hyps=int(nrh[0]))
+
+
+def find_obj_batch(exp: OrcExp, tree, models, descs, Tig, H, W, interpolate=True, n_threads=1):
+    """CPU baseline: many images over n_threads threads; returns best_conf [n][P][7]."""
+    th, mh = _TreeHolder(tree), _ModelsHolder(models)
+    descs = [np.ascontiguousarray(d, dtype=np.float32) for d in descs]
+    R, ny, nx, D = descs[0].shape
+    arr = (C.POINTER(C.c_float) * len(descs))(*[_p(d, C.c_float) for d in descs])
+    best = np.zeros((len(descs), th.s.n_parts, 7), dtype=np.float32)
+    T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(9)
+    rc = lib().orc_find_obj_batch_f32(C.byref(exp), C.byref(th.s), C.byref(mh.s), len(descs), arr,
+                                      ny, nx, D, _p(T, C.c_double), int(interpolate), H, W,
+                                      _p(best, C.c_float), int(n_threads))
+    if rc:
+        raise ValueError(f"orc_find_obj_batch failed: {rc}")
+    return best
