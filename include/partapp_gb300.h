@@ -1,0 +1,241 @@
+/*
+ * partapp_gb300.h -- C-ABI of the GB300 implementation of partapp's
+ * inference hot path (dense AdaBoost part unaries + rotation-aware
+ * pictorial-structures sum-product with marginals).
+ *
+ * The reference has no plugin/FFI layer: its boundary is the in-process C++
+ * call surface of libPartDetect / libPictStruct.  Each entry point below names
+ * the reference function(s) it replaces (paths relative to the reference
+ * tree).  Conventions:
+ *   - every call returns a pa_status and never aborts (the reference reports
+ *     errors only through assert());
+ *   - maps use the reference's FloatGrid3 layout, C order [rot][y][x], float;
+ *     per-part stacks are [part][rot][y][x];
+ *   - buffers are caller-owned; `mem` says whether the data pointers of a call
+ *     are device (PA_MEM_DEVICE) or host (PA_MEM_HOST) memory.  Host buffers
+ *     are staged through the context's device workspace;
+ *   - a context is bound to one device and one CUDA stream; calls on one
+ *     context must not run concurrently from several host threads.
+ */
+#ifndef PARTAPP_GB300_H_
+#define PARTAPP_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int pa_status;
+#define PA_OK 0
+#define PA_ERR_INVALID 1      /* argument the reference would assert on */
+#define PA_ERR_UNSUPPORTED 2  /* valid for the reference, not built here */
+#define PA_ERR_CUDA 3         /* CUDA runtime error (message in pa_last_error) */
+#define PA_ERR_NOMEM 4        /* device or host allocation failed */
+#define PA_ERR_NUMERIC 5      /* exp() overflow: the reference asserts here */
+
+#define PA_MEM_DEVICE 0
+#define PA_MEM_HOST 1
+
+#define PA_NO_CLASS_VALUE 0.0f /* libPartDetect/partdetect.h:45 */
+#define PA_LOG_ZERO (-1e6f)    /* libBoostMath/boost_math.h:23 */
+
+typedef struct pa_ctx pa_ctx;
+typedef struct pa_classifier pa_classifier;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on `device` with its own non-blocking stream. */
+pa_status pa_ctx_create(int device, pa_ctx **out);
+pa_status pa_ctx_destroy(pa_ctx *ctx);
+/* Makes the context issue its work on `stream` (a cudaStream_t). */
+pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream);
+pa_status pa_ctx_synchronize(pa_ctx *ctx);
+/* Message of the last failing call on this context (never NULL). */
+const char *pa_last_error(const pa_ctx *ctx);
+const char *pa_status_string(pa_status s);
+/* Number of kernels this context has launched so far. */
+uint64_t pa_ctx_kernel_launches(const pa_ctx *ctx);
+
+/* ------------------------------------------------------ experiment params */
+
+/* The ExpParam fields the path reads (libPartApp/ExpParam.proto:160,
+ * 189-195, 229, 282; defaults in brackets). */
+typedef struct {
+  int num_rotation_steps;        /* R [48] */
+  float min_part_rotation;       /* degrees [-180] */
+  float max_part_rotation;       /* degrees [180] */
+  float min_object_scale;        /* [1]; num_scale_steps is 1 */
+  float max_object_scale;        /* [1] */
+  float strip_border_detections; /* fraction of the width [0] */
+  int roi_save_num_samples;      /* local maxima kept per part [1000] */
+  int use_pairwise;              /* [1] */
+  int interpolate;               /* grid->image TM_BILINEAR if 1, else TM_DIRECT [0] */
+} pa_exp_param;
+
+void pa_exp_param_default(pa_exp_param *p);
+
+/* ------------------------------------------------------ AdaBoost unaries */
+
+/* One decision stump: DecisionStump (libAdaBoost/AdaBoost.h:30-38) without
+ * the training-only fields. */
+typedef struct {
+  int32_t f;   /* feature index */
+  float p;     /* polarity */
+  float theta; /* threshold */
+  float alpha; /* weight */
+} pa_stump;
+
+/* Uploads a classifier; sum_alpha is accumulated in stump order as
+ * operator>> does (libAdaBoost/AdaBoost.cc:311-338). */
+pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps,
+                               int n_stumps, pa_classifier **out);
+/* Parses the text model format of AdaBoostClassifier::loadClassifier
+ * (AdaBoost.cc:295-338): "D\n ns\n (f p alpha J_wse theta)*ns". */
+pa_status pa_classifier_parse(pa_ctx *ctx, const char *text, size_t len,
+                              pa_classifier **out);
+pa_status pa_classifier_destroy(pa_ctx *ctx, pa_classifier *cls);
+pa_status pa_classifier_info(const pa_classifier *cls, int *dim, int *n_stumps,
+                             float *sum_alpha);
+
+/* Dense part detection: score[p][k][iy][ix] =
+ * AdaBoostClassifier::evaluateFeaturePoint(desc[k][iy][ix][:], normalize)
+ * for every location of every field k (AdaBoost.h:131-160 called from
+ * computeScoreGrid, libPartDetect/partdetect_test.cpp:366-377).  Each
+ * location holds its complete dim-long window vector.  Decisions and the
+ * float sum follow the reference's stump order bit for bit.
+ *   desc    [n_fields][ny][nx][dim]
+ *   scores  [n_parts][n_fields][ny][nx] */
+pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
+                         const float *desc, int n_fields, int ny, int nx, int dim,
+                         int normalize, float *scores, int mem);
+
+/* computeScoreGrid over a grid of per-cell descriptors: each window vector is
+ * the reverse-order concatenation of gx*gy cell descriptors taken every
+ * round(k*grid_step) cells (FeatureGrid::concatenate,
+ * libPartDetect/FeatureGrid.cpp:137-181); windows past last_valid_grid_pos
+ * (FeatureGrid.h:71-75) or touching a cell with valid == 0 get
+ * NO_CLASS_VALUE.  dim of every classifier must be gx*gy*dc.
+ *   cells   [n_fields][ny][nx][dc], valid [n_fields][ny][nx] (uint8)
+ *   scores  [n_parts][n_fields][ny][nx] */
+pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls,
+                                int n_parts, const float *cells, const uint8_t *valid,
+                                int n_fields, int ny, int nx, int dc, int gx, int gy,
+                                double grid_step, int normalize, float *scores, int mem);
+
+/* Score grids -> log unary maps: transform_grid_fixed_size(grid -> image,
+ * Tig, NO_CLASS_VALUE, TM_BILINEAR or TM_DIRECT) as in PartApp::loadScoreGrid
+ * (libPartApp/partapp.cpp:876-899) / partdetect_dense
+ * (partdetect_test.cpp:268-292), then clip_scores_fill + computeLogGrid
+ * (objectdetect_findrot.cpp:834-845).  Tig is [n_parts][R][9] (row-major
+ * 3x3, grid -> image), or one shared [9] matrix if tig_shared.
+ *   scores    [n_parts][R][ny][nx]
+ *   log_unary [n_parts][R][H][W] */
+pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, int ny,
+                        int nx, const double *Tig, int tig_shared, int interpolate, int H,
+                        int W, float *log_unary, int mem);
+
+/* -------------------------------------------------- pictorial structures */
+
+/* Tree and joints in host memory: struct Joint
+ * (libPictStruct/objectdetect.h:54-86) after loadJoints
+ * (objectdetect_aux.cpp:54-141), i.e. 0-based part indices, radians. */
+typedef struct {
+  int n_parts;
+  int root;                /* the part with is_root && is_detect */
+  const int *is_upright;   /* [n_parts] PartDef.is_upright */
+  int n_joints;            /* must be n_parts - 1 */
+  const int *child;        /* [n_joints] */
+  const int *parent;       /* [n_joints] */
+  const double *offset_c;  /* [n_joints][2] */
+  const double *offset_p;  /* [n_joints][2] */
+  const double *C;         /* [n_joints][4] row-major 2x2 covariance */
+  const double *rot_mean;  /* [n_joints] radians */
+  const double *rot_sigma; /* [n_joints] radians */
+} pa_tree;
+
+/* PartHyp::toVect order (objectdetect.h:139-159). */
+typedef struct {
+  float scaleidx, scale, rotidx, rot, x, y, score;
+} pa_part_hyp;
+
+/* Outputs of one image.  Every pointer may be NULL.  Map outputs live in the
+ * call's `mem` space, the rest in host memory.
+ *   log_marg     [P][R][H][W] final log marginals (log_part_posterior)
+ *   root_post    [H][W]       log root posterior over the kept rotations
+ *   best         [P]          first-maximum argmax of each marginal
+ *   part_hyps    [P][roi_save_num_samples] local maxima, n_part_hyps [P]
+ *   root_hyps    [1000][4]    (scale, x, y, score), n_root_hyps [1]
+ *   log_z        [P]          FP64 log(sum exp(log_marg[p])) per part; the
+ *                             root's entry is the log-partition function
+ *   msg_max      [2*(P-1)]    FP64 copy of the per-message normaliser in_M:
+ *                             [j] upward message over joint j, [P-1+j] the
+ *                             downward message over joint j */
+typedef struct {
+  float *log_marg;
+  float *root_post;
+  pa_part_hyp *best;
+  pa_part_hyp *part_hyps;
+  int *n_part_hyps;
+  float *root_hyps;
+  int *n_root_hyps;
+  double *log_z;
+  double *msg_max;
+} pa_ps_outputs;
+
+/* computeRootPosteriorRot + computePartMarginals + root rotation
+ * marginalisation + findLocalMax (libPictStruct/objectdetect_findrot.cpp:
+ * 73-286, 470-727; objectdetect_aux.cpp:193-320) on log unaries that went
+ * through clip_scores_fill + computeLogGrid.  The upright mask and the root
+ * border strip are applied inside, as in the reference.  `flip` applies
+ * loadJoints' mirroring (objectdetect_aux.cpp:98-116) to the joints.
+ * Supported trees: the root may have any number of children, every other
+ * part at most one (the reference asserts this at :210); covariances must be
+ * diagonal (gaussFilterDiag2d); PA_ERR_UNSUPPORTED otherwise.
+ *   log_unary [P][R][H][W] */
+pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                      const float *log_unary, int H, int W, const pa_ps_outputs *out,
+                      int mem);
+
+/* computeRotJointMarginal (objectdetect_findrot.cpp:292-456): one message
+ * child -> parent frame.  child, parent [R][H][W]. */
+pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float *child,
+                                float *parent, int R, int H, int W, const double *offset_c,
+                                const double *offset_p, const double *C, double rot_mean,
+                                double rot_sigma, double scale, int mem);
+
+/* ---------------------------------------------------- the --find_obj path */
+
+/* One image of `partapp --find_obj` with freshly computed scores
+ * (findObjectDataset, objectdetect_aux.cpp:368-403 -> partdetect_dense ->
+ * findObjectImageRotJoints, objectdetect_findrot.cpp:729-1058):
+ * pa_score_grids + pa_unary_maps + pa_ps_infer in one call.  All n_cls
+ * classifiers are evaluated (partdetect_dense scores every classifier it
+ * loads); the first tree->n_parts of them are the part detectors the tree
+ * uses.
+ *   desc       [R][ny][nx][dim]
+ *   Tig        as pa_unary_maps for the first n_parts classifiers
+ *   scores_out [n_cls][R][ny][nx] score grids (may be NULL), in `mem` */
+pa_status pa_find_obj(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                      const pa_classifier *const *cls, int n_cls, const float *desc, int ny,
+                      int nx, int dim, const double *Tig, int tig_shared, int H, int W,
+                      float *scores_out, const pa_ps_outputs *out, int mem);
+
+/* A batch of images sharing sizes and classifiers, each with its own tree
+ * parameters (the per-image pairwise terms of poselet-conditioned models),
+ * processed together: one launch per pipeline phase covers every image.
+ *   desc       [n_images][R][ny][nx][dim] in `mem`
+ *   trees      [n_images] host structs (same topology, own joint parameters)
+ *   scores_out [n_cls][n_images*R][ny][nx] (may be NULL), in `mem`
+ *   out        [n_images] output sets as pa_find_obj */
+pa_status pa_find_obj_batch(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
+                            const pa_tree *trees, int flip, const pa_classifier *const *cls,
+                            int n_cls, const float *desc, int ny, int nx, int dim,
+                            const double *Tig, int tig_shared, int H, int W, float *scores_out,
+                            const pa_ps_outputs *out, int mem);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARTAPP_GB300_H_ */

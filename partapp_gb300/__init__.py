@@ -1,0 +1,394 @@
+"""partapp_gb300 -- GB300 implementation of partapp's --find_obj hot path.
+
+Python binding of the C-ABI in include/partapp_gb300.h (libpartapp_gb300.so,
+built by partapp_gb300.build).  The names mirror the reference's C++ entry
+points:
+
+  Context.score_grids          computeScoreGrid + evaluateFeaturePoint
+                               (libPartDetect/partdetect_test.cpp:344-405,
+                                libAdaBoost/AdaBoost.h:131-160)
+  Context.score_grids_window   the FeatureGrid::concatenate form
+  Context.unary_maps           grid -> image + clip_scores_fill + computeLogGrid
+  Context.rot_joint_marginal   computeRotJointMarginal
+                               (libPictStruct/objectdetect_findrot.cpp:292-456)
+  Context.compute_root_posterior_rot
+                               computeRootPosteriorRot + computePartMarginals
+                               (objectdetect_findrot.cpp:124-286, 470-727)
+  Context.find_obj             findObjectImageRotJoints with fresh scores
+  Context.find_obj_batch       many images per call
+
+Arrays: numpy arrays are host memory (copied through the device workspace);
+torch CUDA tensors are used in place as device memory.  There is no CPU
+fallback: without the built library or a GPU every compute call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libpartapp_gb300.so")
+
+PA_OK, PA_ERR_INVALID, PA_ERR_UNSUPPORTED, PA_ERR_CUDA, PA_ERR_NOMEM, PA_ERR_NUMERIC = range(6)
+PA_MEM_DEVICE, PA_MEM_HOST = 0, 1
+LOG_ZERO = -1e6
+NO_CLASS_VALUE = 0.0
+
+# every symbol include/partapp_gb300.h declares
+EXPORTS = (
+    "pa_ctx_create", "pa_ctx_destroy", "pa_ctx_set_stream", "pa_ctx_synchronize",
+    "pa_last_error", "pa_status_string", "pa_ctx_kernel_launches", "pa_exp_param_default",
+    "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
+    "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
+    "pa_ps_infer", "pa_rot_joint_marginal", "pa_find_obj", "pa_find_obj_batch",
+)
+
+
+class PaError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class ExpParam(C.Structure):
+    _fields_ = [("num_rotation_steps", C.c_int), ("min_part_rotation", C.c_float),
+                ("max_part_rotation", C.c_float), ("min_object_scale", C.c_float),
+                ("max_object_scale", C.c_float), ("strip_border_detections", C.c_float),
+                ("roi_save_num_samples", C.c_int), ("use_pairwise", C.c_int),
+                ("interpolate", C.c_int)]
+
+
+class Stump(C.Structure):
+    _fields_ = [("f", C.c_int32), ("p", C.c_float), ("theta", C.c_float), ("alpha", C.c_float)]
+
+
+class Tree(C.Structure):
+    _fields_ = [("n_parts", C.c_int), ("root", C.c_int), ("is_upright", C.POINTER(C.c_int)),
+                ("n_joints", C.c_int), ("child", C.POINTER(C.c_int)),
+                ("parent", C.POINTER(C.c_int)), ("offset_c", C.POINTER(C.c_double)),
+                ("offset_p", C.POINTER(C.c_double)), ("C", C.POINTER(C.c_double)),
+                ("rot_mean", C.POINTER(C.c_double)), ("rot_sigma", C.POINTER(C.c_double))]
+
+
+class PartHyp(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("scaleidx", "scale", "rotidx", "rot", "x", "y", "score")]
+
+
+class PsOutputs(C.Structure):
+    _fields_ = [("log_marg", C.c_void_p), ("root_post", C.c_void_p),
+                ("best", C.POINTER(PartHyp)), ("part_hyps", C.POINTER(PartHyp)),
+                ("n_part_hyps", C.POINTER(C.c_int)), ("root_hyps", C.POINTER(C.c_float)),
+                ("n_root_hyps", C.POINTER(C.c_int)), ("log_z", C.POINTER(C.c_double)),
+                ("msg_max", C.POINTER(C.c_double))]
+
+
+_lib = None
+
+
+def load_library():
+    """Load libpartapp_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"partapp_gb300: native library missing at {LIB_PATH}; "
+                          "build it with `python -m partapp_gb300.build`")
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp, fp = C.c_void_p, C.c_int, C.c_double, C.c_float
+    P = C.POINTER
+    L.pa_ctx_create.argtypes = [ip, P(vp)]
+    L.pa_ctx_destroy.argtypes = [vp]
+    L.pa_ctx_set_stream.argtypes = [vp, vp]
+    L.pa_ctx_synchronize.argtypes = [vp]
+    L.pa_last_error.argtypes = [vp]
+    L.pa_last_error.restype = C.c_char_p
+    L.pa_status_string.argtypes = [ip]
+    L.pa_status_string.restype = C.c_char_p
+    L.pa_ctx_kernel_launches.argtypes = [vp]
+    L.pa_ctx_kernel_launches.restype = C.c_uint64
+    L.pa_exp_param_default.argtypes = [P(ExpParam)]
+    L.pa_exp_param_default.restype = None
+    L.pa_classifier_create.argtypes = [vp, ip, P(Stump), ip, P(vp)]
+    L.pa_classifier_parse.argtypes = [vp, C.c_char_p, C.c_size_t, P(vp)]
+    L.pa_classifier_destroy.argtypes = [vp, vp]
+    L.pa_classifier_info.argtypes = [vp, P(ip), P(ip), P(fp)]
+    L.pa_score_grids.argtypes = [vp, P(vp), ip, vp, ip, ip, ip, ip, ip, vp, ip]
+    L.pa_score_grids_window.argtypes = [vp, P(vp), ip, vp, vp, ip, ip, ip, ip, ip, ip, dp, ip,
+                                        vp, ip]
+    L.pa_unary_maps.argtypes = [vp, vp, ip, ip, ip, ip, P(dp), ip, ip, ip, ip, vp, ip]
+    L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, vp, ip, ip, P(PsOutputs), ip]
+    L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
+                                        dp, dp, dp, ip]
+    L.pa_find_obj.argtypes = [vp, P(ExpParam), P(Tree), ip, P(vp), ip, vp, ip, ip, ip, P(dp), ip,
+                              ip, ip, vp, P(PsOutputs), ip]
+    L.pa_find_obj_batch.argtypes = [vp, P(ExpParam), ip, P(Tree), ip, P(vp), ip, vp, ip, ip, ip,
+                                    P(dp), ip, ip, ip, vp, P(PsOutputs), ip]
+    for name in EXPORTS:
+        getattr(L, name)  # every declared entry point must resolve
+    _lib = L
+    return L
+
+
+def exp_param(R=24, min_rot=-180.0, max_rot=180.0, scale=1.0, strip=0.0, local_max=1000,
+              use_pairwise=True, interpolate=True) -> ExpParam:
+    return ExpParam(int(R), float(min_rot), float(max_rot), float(scale), float(scale),
+                    float(strip), int(local_max), int(bool(use_pairwise)), int(bool(interpolate)))
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+class _Buf:
+    """Holds a numpy or torch buffer and its pointer + memory space."""
+
+    def __init__(self, a, dtype):
+        if _is_torch(a):
+            import torch
+
+            tdt = {np.float32: torch.float32, np.uint8: torch.uint8}[dtype]
+            if not a.is_cuda:
+                raise ValueError("torch tensors must live on the GPU")
+            if a.dtype != tdt or not a.is_contiguous():
+                raise ValueError(f"expected a contiguous {tdt} CUDA tensor")
+            self.arr, self.ptr, self.mem = a, a.data_ptr(), PA_MEM_DEVICE
+        else:
+            arr = np.ascontiguousarray(a, dtype=dtype)
+            self.arr, self.ptr, self.mem = arr, arr.ctypes.data, PA_MEM_HOST
+
+
+def _empty_like_space(shape, mem, like=None):
+    if mem == PA_MEM_DEVICE:
+        import torch
+
+        return torch.empty(shape, dtype=torch.float32, device=like.device)
+    return np.empty(shape, dtype=np.float32)
+
+
+class _TreeHolder:
+    def __init__(self, tree):
+        self.is_upright = np.ascontiguousarray(tree["is_upright"], dtype=np.int32)
+        self.child = np.ascontiguousarray(tree["child"], dtype=np.int32)
+        self.parent = np.ascontiguousarray(tree["parent"], dtype=np.int32)
+        self.offset_c = np.ascontiguousarray(tree["offset_c"], dtype=np.float64).reshape(-1)
+        self.offset_p = np.ascontiguousarray(tree["offset_p"], dtype=np.float64).reshape(-1)
+        self.C = np.ascontiguousarray(tree["C"], dtype=np.float64).reshape(-1)
+        self.rot_mean = np.ascontiguousarray(tree["rot_mean"], dtype=np.float64)
+        self.rot_sigma = np.ascontiguousarray(tree["rot_sigma"], dtype=np.float64)
+        pi = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+        pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self.s = Tree(int(tree["n_parts"]), int(tree["root"]), pi(self.is_upright),
+                      len(self.child), pi(self.child), pi(self.parent), pd(self.offset_c),
+                      pd(self.offset_p), pd(self.C), pd(self.rot_mean), pd(self.rot_sigma))
+
+
+class Classifier:
+    """An AdaBoost classifier resident on the device (pa_classifier)."""
+
+    def __init__(self, ctx: "Context", handle, keep=None):
+        self.ctx, self.h, self._keep = ctx, handle, keep
+
+    @classmethod
+    def from_stumps(cls, ctx, f, p, theta, alpha, dim):
+        n = len(f)
+        arr = (Stump * n)()
+        for i in range(n):
+            arr[i] = Stump(int(f[i]), float(p[i]), float(theta[i]), float(alpha[i]))
+        h = C.c_void_p()
+        ctx._check(ctx.L.pa_classifier_create(ctx.h, int(dim), arr, n, C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def parse(cls, ctx, text: str):
+        b = text.encode()
+        h = C.c_void_p()
+        ctx._check(ctx.L.pa_classifier_parse(ctx.h, b, len(b), C.byref(h)))
+        return cls(ctx, h)
+
+    def info(self):
+        d, n, s = C.c_int(), C.c_int(), C.c_float()
+        self.ctx.L.pa_classifier_info(self.h, C.byref(d), C.byref(n), C.byref(s))
+        return d.value, n.value, s.value
+
+    def close(self):
+        if self.h:
+            self.ctx.L.pa_classifier_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """A pa_ctx: one device, one stream, its own workspace."""
+
+    def __init__(self, device: int = 0):
+        self.L = load_library()
+        h = C.c_void_p()
+        st = self.L.pa_ctx_create(int(device), C.byref(h))
+        if st != PA_OK:
+            raise PaError(st, "pa_ctx_create failed (no CUDA device?)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pa_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != PA_OK:
+            raise PaError(st, self.L.pa_last_error(self.h).decode())
+
+    def set_stream(self, stream_ptr: int):
+        self._check(self.L.pa_ctx_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def synchronize(self):
+        self._check(self.L.pa_ctx_synchronize(self.h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.pa_ctx_kernel_launches(self.h))
+
+    # ---------------------------------------------------------- unaries
+    def classifiers(self, models) -> list:
+        """Upload {f, p, theta, alpha} arrays of shape [n_parts][n_stumps]."""
+        D = int(models.get("D", int(np.max(models["f"])) + 1))
+        return [Classifier.from_stumps(self, models["f"][i], models["p"][i], models["theta"][i],
+                                       models["alpha"][i], D) for i in range(len(models["f"]))]
+
+    @staticmethod
+    def _cls_array(cls_list):
+        return (C.c_void_p * len(cls_list))(*[c.h for c in cls_list])
+
+    def score_grids(self, cls_list, desc, normalize=True):
+        """desc [n_fields][ny][nx][dim] -> scores [n_parts][n_fields][ny][nx]."""
+        d = _Buf(desc, np.float32)
+        nf, ny, nx, dim = d.arr.shape
+        out = _empty_like_space((len(cls_list), nf, ny, nx), d.mem, d.arr)
+        o = _Buf(out, np.float32)
+        self._check(self.L.pa_score_grids(self.h, self._cls_array(cls_list), len(cls_list), d.ptr,
+                                          nf, ny, nx, dim, int(normalize), o.ptr, d.mem))
+        return out
+
+    def score_grids_window(self, cls_list, cells, valid, gx, gy, grid_step, normalize=True):
+        c = _Buf(cells, np.float32)
+        v = _Buf(valid, np.uint8)
+        nf, ny, nx, dc = c.arr.shape
+        out = _empty_like_space((len(cls_list), nf, ny, nx), c.mem, c.arr)
+        o = _Buf(out, np.float32)
+        self._check(self.L.pa_score_grids_window(self.h, self._cls_array(cls_list),
+                                                 len(cls_list), c.ptr, v.ptr, nf, ny, nx, dc,
+                                                 int(gx), int(gy), float(grid_step),
+                                                 int(normalize), o.ptr, c.mem))
+        return out
+
+    def unary_maps(self, scores, Tig, H, W, interpolate=True):
+        """scores [P][R][ny][nx] -> log unaries [P][R][H][W]."""
+        s = _Buf(scores, np.float32)
+        P, R, ny, nx = s.arr.shape
+        T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(-1)
+        shared = int(T.size == 9)
+        out = _empty_like_space((P, R, H, W), s.mem, s.arr)
+        o = _Buf(out, np.float32)
+        self._check(self.L.pa_unary_maps(self.h, s.ptr, P, R, ny, nx,
+                                         T.ctypes.data_as(C.POINTER(C.c_double)), shared,
+                                         int(interpolate), H, W, o.ptr, s.mem))
+        return out
+
+    # ---------------------------------------------------------- messages
+    def rot_joint_marginal(self, exp: ExpParam, child, offset_c, offset_p, Cmat, rot_mean,
+                           rot_sigma, scale=1.0):
+        c = _Buf(child, np.float32)
+        R, H, W = c.arr.shape
+        out = _empty_like_space((R, H, W), c.mem, c.arr)
+        o = _Buf(out, np.float32)
+        dp = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        oc, op, Cm = dp(offset_c), dp(offset_p), dp(Cmat)
+        pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._check(self.L.pa_rot_joint_marginal(self.h, C.byref(exp), c.ptr, o.ptr, R, H, W,
+                                                 pd(oc), pd(op), pd(Cm), float(rot_mean),
+                                                 float(rot_sigma), float(scale), c.mem))
+        return out
+
+    def _outputs(self, P, R, H, W, K, mem, like, want_marg=True, want_root=True):
+        res = dict(best=(PartHyp * P)(), log_z=np.zeros(P), msg_max=np.zeros(max(1, 2 * (P - 1))),
+                   n_part_hyps=np.zeros(P, dtype=np.int32), n_root_hyps=np.zeros(1, np.int32),
+                   part_hyps=(PartHyp * max(1, P * K))(), root_hyps=np.zeros((1000, 4), np.float32))
+        res["log_marg"] = _empty_like_space((P, R, H, W), mem, like) if want_marg else None
+        res["root_post"] = _empty_like_space((H, W), mem, like) if want_root else None
+        ptr = lambda a: None if a is None else _Buf(a, np.float32).ptr
+        o = PsOutputs(ptr(res["log_marg"]), ptr(res["root_post"]), res["best"], res["part_hyps"],
+                      res["n_part_hyps"].ctypes.data_as(C.POINTER(C.c_int)),
+                      res["root_hyps"].ctypes.data_as(C.POINTER(C.c_float)),
+                      res["n_root_hyps"].ctypes.data_as(C.POINTER(C.c_int)),
+                      res["log_z"].ctypes.data_as(C.POINTER(C.c_double)),
+                      res["msg_max"].ctypes.data_as(C.POINTER(C.c_double)))
+        return res, o
+
+    @staticmethod
+    def _finish(res, P):
+        res["best_conf"] = np.array([[h.scaleidx, h.scale, h.rotidx, h.rot, h.x, h.y, h.score]
+                                     for h in res.pop("best")], dtype=np.float32)
+        return res
+
+    def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,
+                                   want_marg=True):
+        """log_unary [P][R][H][W] (after clip_scores_fill + computeLogGrid)."""
+        u = _Buf(log_unary, np.float32)
+        P, R, H, W = u.arr.shape
+        th = _TreeHolder(tree)
+        res, o = self._outputs(P, R, H, W, exp.roi_save_num_samples, u.mem, u.arr, want_marg)
+        self._check(self.L.pa_ps_infer(self.h, C.byref(exp), C.byref(th.s), int(flip), u.ptr, H,
+                                       W, C.byref(o), u.mem))
+        return self._finish(res, P)
+
+    def find_obj(self, exp: ExpParam, tree, cls_list, desc, Tig, H, W, flip=False,
+                 want_marg=True):
+        """desc [R][ny][nx][dim] -> marginals, argmax, root posterior of one image."""
+        d = _Buf(desc, np.float32)
+        R, ny, nx, dim = d.arr.shape
+        th = _TreeHolder(tree)
+        P = th.s.n_parts
+        T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(-1)
+        res, o = self._outputs(P, R, H, W, exp.roi_save_num_samples, d.mem, d.arr, want_marg)
+        self._check(self.L.pa_find_obj(self.h, C.byref(exp), C.byref(th.s), int(flip),
+                                       self._cls_array(cls_list), len(cls_list), d.ptr, ny, nx,
+                                       dim, T.ctypes.data_as(C.POINTER(C.c_double)),
+                                       int(T.size == 9), H, W, None, C.byref(o), d.mem))
+        return self._finish(res, P)
+
+    def find_obj_batch(self, exp: ExpParam, trees, cls_list, desc, Tig, H, W, flip=False,
+                       want_marg=False, want_root=False, scores_out=None):
+        """desc [B][R][ny][nx][dim]; trees: list of B tree dicts (same topology).
+        cls_list may hold more classifiers than the tree has parts; the first
+        n_parts feed the tree, all are evaluated (scores_out, if given, is
+        [n_cls][B*R][ny][nx] in the same memory space as desc)."""
+        d = _Buf(desc, np.float32)
+        B, R, ny, nx, dim = d.arr.shape
+        ths = [_TreeHolder(t) for t in trees]
+        arr = (Tree * B)(*[t.s for t in ths])
+        P = ths[0].s.n_parts
+        T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(-1)
+        results, outs = [], (PsOutputs * B)()
+        for i in range(B):
+            res, o = self._outputs(P, R, H, W, exp.roi_save_num_samples, d.mem, d.arr, want_marg,
+                                   want_root)
+            results.append(res)
+            outs[i] = o
+        so = None if scores_out is None else _Buf(scores_out, np.float32).ptr
+        self._check(self.L.pa_find_obj_batch(self.h, C.byref(exp), B, arr, int(flip),
+                                             self._cls_array(cls_list), len(cls_list), d.ptr, ny,
+                                             nx, dim, T.ctypes.data_as(C.POINTER(C.c_double)),
+                                             int(T.size == 9), H, W, so, outs, d.mem))
+        return [self._finish(r, P) for r in results]

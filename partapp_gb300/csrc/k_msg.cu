@@ -1,0 +1,438 @@
+// k_msg.cu -- pictorial-structures messages on GB300.
+//
+// One message is computeRotJointMarginal (libPictStruct/
+// objectdetect_findrot.cpp:292-456):
+//   M    = max(child)                                   (getMinMax, :301-302)
+//   J10  = per-rotation nearest shift of child by R(a_r) s offset_c into
+//          rotation r + rot_mean_idx, LOG_ZERO outside        (:342-359)
+//   E    = exp(J10 - M)                                     (:362-365)
+//   E'   = circular rotation filter, clipped taps           (:373-420)
+//   J01  = separable truncated Gaussian (x pass, y pass)    (:423-429)
+//   out  = nearest shift of log(J01) + M by -R(a_r) s offset_p (:432-448)
+// followed by what the caller does with `out` (addGrid2 into the parent
+// belief, :637-654; computePartMarginals, :163-236).
+//
+// Two kernels per batch of independent messages:
+//   k_msg_rows  one CTA per (image row y, message): stages all R rotations of
+//               the row as exp(J10 - M) in shared memory, applies the rotation
+//               filter per column in registers and the x pass along the row,
+//               and writes the exp-domain intermediate E2.
+//   k_msg_cols  one CTA per (32-column strip, row band, rotation, message):
+//               y pass over the staged strip, log, + M, the shift back into
+//               the parent frame and the epilogue (store / add / marginal).
+// The nearest-shift source indices come from per-message tables computed
+// with the reference's double-precision rounding (k_shift_tables).
+#include "pa_internal.cuh"
+
+namespace pa {
+namespace {
+
+constexpr int kThreadsRows = 256;
+constexpr int kThreadsCols = 256;
+constexpr int kNO = 11;   // outputs per lane in the row/column passes (odd: conflict-free)
+constexpr int kU = 8;     // taps per unrolled block
+constexpr int kTX = 32;   // parent columns per k_msg_cols CTA
+constexpr int kCW = 33;   // staged source columns (one spare for rounding glitches)
+
+__device__ __forceinline__ int wrap(int r, int R) { return r < 0 ? r + R : (r >= R ? r - R : r); }
+
+// ---------------------------------------------------------------------------
+// Rotation filter on one column held in registers: out[r] = sum_j t[j] *
+// e[(r - NR + j) mod R] (grid_filter_1d_blas_wraparound,
+// libMultiArray/multi_array_filter.hpp:116-155).
+// ---------------------------------------------------------------------------
+template <int R, int NR>
+__device__ __forceinline__ void rot_filter_fixed(const float (&e)[R], float *out, int stride,
+                                                 const float *t) {
+  float tv[2 * NR + 1];
+#pragma unroll
+  for (int j = 0; j < 2 * NR + 1; ++j) tv[j] = t[j];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    float acc = 0.f;
+#pragma unroll
+    for (int j = 0; j < 2 * NR + 1; ++j) acc = fmaf(tv[j], e[((r - NR + j) % R + R) % R], acc);
+    out[r * stride] = acc;
+  }
+}
+
+template <int R, int NR>
+__device__ __forceinline__ bool rot_filter_dispatch(int nr, const float (&e)[R], float *out,
+                                                    int stride, const float *t) {
+  if constexpr (NR < 0) {
+    return false;
+  } else {
+    if (nr == NR) {
+      rot_filter_fixed<R, NR>(e, out, stride, t);
+      return true;
+    }
+    return rot_filter_dispatch<R, NR - 1>(nr, e, out, stride, t);
+  }
+}
+
+// Row stride of the staged rows: left pad covers the widest x kernel, the
+// right pad also covers the unrolled tail of the x pass (kU + kNO extra
+// reads past the last tap), so every read stays inside zero padding.
+__host__ __device__ __forceinline__ int rows_stride(int W, int padx) {
+  return W + 2 * padx + kU + kNO;
+}
+
+// Shared-memory regions start on 16-byte boundaries (float4 tap loads).
+__host__ __device__ __forceinline__ int align4(int n) { return (n + 3) & ~3; }
+
+// ---------------------------------------------------------------------------
+// k_msg_rows
+// ---------------------------------------------------------------------------
+template <int RT>
+__global__ void __launch_bounds__(kThreadsRows) k_msg_rows(const MsgDesc *__restrict__ msgs,
+                                                           int Rrt, int H, int W, int padx,
+                                                           int *err) {
+  const int R = RT > 0 ? RT : Rrt;
+  const MsgDesc md = msgs[blockIdx.y];
+  const int y = blockIdx.x;
+  const int WP = rows_stride(W, padx);
+  extern __shared__ __align__(16) float sm[];
+  float *E = sm;                       // [R][WP]
+  float *tx = E + align4(R * WP);      // x taps, zero-padded to a multiple of kU (16B aligned)
+  const int xpad = ((md.xlen + kU - 1) / kU) * kU;
+  float *tr = tx + ((2 * padx + 1 + kU - 1) / kU) * kU;  // rotation taps
+  const int tid = threadIdx.x;
+
+  for (int i = tid; i < xpad; i += blockDim.x) tx[i] = i < md.xlen ? md.xtaps[i] : 0.f;
+  for (int i = tid; i < md.rlen; i += blockDim.x) tr[i] = md.rtaps[i];
+
+  // (1) stage exp(J10 - M) for all rotations of row y; zero padding.
+  const float negM = -fkey_decode(*md.in_max);
+  const int HW = H * W;
+  for (int idx = tid; idx < R * WP; idx += blockDim.x) {
+    const int r = idx / WP;
+    const int x = idx - r * WP - padx;
+    float v = 0.f;
+    if (x >= 0 && x < W) {
+      const int sy = md.ty_in[r * H + y];
+      const int sx = md.tx_in[r * W + x];
+      float lv = kLogZero;
+      if (sy >= 0 && sx >= 0) lv = __ldg(md.in + (int64_t)(r - md.kidx) * HW + sy * W + sx);
+      v = expf(__fadd_rn(lv, negM));
+      if (v == INFINITY) atomicOr(err, 1);
+    }
+    E[idx] = v;
+  }
+  __syncthreads();
+
+  // (2) rotation filter, column by column, in place.
+  if (md.rlen == 0) {
+    for (int idx = tid; idx < R * W; idx += blockDim.x) {
+      const int r = idx / W, x = idx - r * W;
+      E[r * WP + padx + x] = 0.f;
+    }
+  } else if (md.rlen > 0) {
+    const int nr = (md.rlen - 1) / 2;
+    if constexpr (RT > 0) {
+      for (int x = tid; x < W; x += blockDim.x) {
+        float e[RT];
+#pragma unroll
+        for (int r = 0; r < RT; ++r) e[r] = E[r * WP + padx + x];
+        if (!rot_filter_dispatch<RT, (RT - 1) / 2>(nr, e, E + padx + x, WP, tr)) atomicOr(err, 2);
+      }
+    } else {
+      float *col = tr + kMaxRot;  // [blockDim.x][R] scratch
+      for (int x = tid; x < W; x += blockDim.x) {
+        float *c = col + tid * R;
+        for (int r = 0; r < R; ++r) c[r] = E[r * WP + padx + x];
+        for (int r = 0; r < R; ++r) {
+          float acc = 0.f;
+          for (int j = 0; j < md.rlen; ++j) acc = fmaf(tr[j], c[wrap(r - nr + j, R)], acc);
+          E[r * WP + padx + x] = acc;
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // (3) x pass: lane l owns outputs [l*kNO, l*kNO + kNO) of a row.
+  const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int kx = (md.xlen - 1) / 2;
+  float *e2 = md.e2;
+  for (int r = warp; r < R; r += nwarps) {
+    const float *row = E + r * WP + padx - kx;
+    for (int x0 = lane * kNO; x0 < W; x0 += 32 * kNO) {
+      float acc[kNO];
+#pragma unroll
+      for (int i = 0; i < kNO; ++i) acc[i] = 0.f;
+      for (int kb = 0; kb < xpad; kb += kU) {
+        float v[kNO + kU - 1];
+#pragma unroll
+        for (int i = 0; i < kNO + kU - 1; ++i) v[i] = row[x0 + kb + i];
+        const float4 ta = *reinterpret_cast<const float4 *>(tx + kb);
+        const float4 tb = *reinterpret_cast<const float4 *>(tx + kb + 4);
+        const float t[kU] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+#pragma unroll
+        for (int u = 0; u < kU; ++u)
+#pragma unroll
+          for (int i = 0; i < kNO; ++i) acc[i] = fmaf(t[u], v[i + u], acc[i]);
+      }
+      float *o = e2 + (int64_t)r * HW + (int64_t)y * W;
+#pragma unroll
+      for (int i = 0; i < kNO; ++i)
+        if (x0 + i < W) o[x0 + i] = acc[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_msg_cols
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void block_reduce_commit(int key, int *slot, int *sbuf) {
+  key = __reduce_max_sync(0xFFFFFFFFu, key);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sbuf[warp] = key;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = sbuf[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, sbuf[w]);
+    atomicMax(slot, m);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__restrict__ msgs,
+                                                           int R, int H, int W, int band,
+                                                           int pady, int *err) {
+  const MsgDesc md = msgs[blockIdx.z];
+  const int r = blockIdx.y % R;
+  const int yb = blockIdx.y / R;
+  const int y0 = yb * band, y1 = min(H, y0 + band);
+  const int x0 = blockIdx.x * kTX, x1 = min(W, x0 + kTX);
+  const int tid = threadIdx.x;
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int lim[4];
+  __shared__ int red[kThreadsCols / 32];
+  __shared__ unsigned long long redu[kThreadsCols / 32];
+
+  const int16_t *txo = md.tx_out + r * W;
+  const int16_t *tyo = md.ty_out + r * H;
+  if (tid == 0) {
+    lim[0] = 1 << 30; lim[1] = -1; lim[2] = 1 << 30; lim[3] = -1;
+  }
+  __syncthreads();
+  for (int i = tid; i < (x1 - x0) + (y1 - y0); i += blockDim.x) {
+    if (i < x1 - x0) {
+      const int c = txo[x0 + i];
+      if (c >= 0) { atomicMin(&lim[0], c); atomicMax(&lim[1], c); }
+    } else {
+      const int rr = tyo[y0 + i - (x1 - x0)];
+      if (rr >= 0) { atomicMin(&lim[2], rr); atomicMax(&lim[3], rr); }
+    }
+  }
+  __syncthreads();
+  const int cmin = lim[0], cmax = lim[1], rmin = lim[2], rmax = lim[3];
+  const bool any = (cmax >= 0 && rmax >= 0);
+  const int ky = (md.ylen - 1) / 2;
+  const int nrows = any ? rmax - rmin + 1 : 0;      // F rows
+  const int srows = nrows + 2 * ky;                  // staged rows
+  if (any && (cmax - cmin + 1 > kCW || nrows > band + 2)) {
+    if (tid == 0) atomicOr(err, 4);
+    return;
+  }
+  float *S = sm;                                          // [srows][kCW]
+  float *F = S + align4((band + 2 + 2 * pady) * kCW);     // [nrows][kCW]
+  float *ty = F + align4((band + 2) * kCW);               // y taps padded, 16B aligned
+  const int ypad = ((md.ylen + kU - 1) / kU) * kU;
+  for (int i = tid; i < ypad; i += blockDim.x) ty[i] = i < md.ylen ? md.ytaps[i] : 0.f;
+
+  const int64_t HW = (int64_t)H * W;
+  const float *e2 = md.e2 + (int64_t)r * HW;
+  if (any) {
+    // stage E2 rows [rmin - ky, rmax + ky] x columns [cmin, cmin + kCW), zero outside
+    for (int i = tid; i < srows * kCW; i += blockDim.x) {
+      const int sr = i / kCW, c = i - sr * kCW;
+      const int yy = rmin - ky + sr, xx = cmin + c;
+      float v = 0.f;
+      if (yy >= 0 && yy < H && xx < W && xx <= cmax) v = e2[(int64_t)yy * W + xx];
+      S[i] = v;
+    }
+  }
+  __syncthreads();
+  if (any) {
+    // y pass: lane = column, kNO consecutive rows per lane-task.
+    const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int ncol = cmax - cmin + 1;
+    const int nchunks = (nrows + kNO - 1) / kNO;
+    for (int task = warp; task < 2 * nchunks; task += nwarps) {
+      const int rr0 = (task >> 1) * kNO;
+      const int c = lane + 32 * (task & 1);
+      if (c < ncol) {
+        float acc[kNO];
+#pragma unroll
+        for (int i = 0; i < kNO; ++i) acc[i] = 0.f;
+        const float *col = S + c;
+        for (int kb = 0; kb < ypad; kb += kU) {
+          float v[kNO + kU - 1];
+#pragma unroll
+          for (int i = 0; i < kNO + kU - 1; ++i) {
+            const int sr = rr0 + kb + i;
+            v[i] = sr < srows ? col[sr * kCW] : 0.f;
+          }
+          const float4 ta = *reinterpret_cast<const float4 *>(ty + kb);
+          const float4 tb = *reinterpret_cast<const float4 *>(ty + kb + 4);
+          const float t[kU] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+#pragma unroll
+          for (int u = 0; u < kU; ++u)
+#pragma unroll
+            for (int i = 0; i < kNO; ++i) acc[i] = fmaf(t[u], v[i + u], acc[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < kNO; ++i)
+          if (rr0 + i < nrows) F[(rr0 + i) * kCW + c] = acc[i];
+      }
+    }
+  }
+  __syncthreads();
+
+  // epilogue: log, + M, shift back, combine with the caller's accumulation.
+  const float M = fkey_decode(*md.in_max);
+  if (md.in_max_f64 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) *md.in_max_f64 = (double)M;
+  const int tw = x1 - x0;
+  int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
+  unsigned long long am = 0ull;
+  for (int i = tid; i < (y1 - y0) * tw; i += blockDim.x) {
+    const int yy = y0 + i / tw, xx = x0 + (i - (i / tw) * tw);
+    const int sy = tyo[yy], sx = txo[xx];
+    float m = kLogZero;
+    if (sy >= 0 && sx >= 0) {
+      const float f = F[(sy - rmin) * kCW + (sx - cmin)];
+      m = __fadd_rn(f == 0.f ? kLogZero : logf(f), M);
+    }
+    const int64_t idx = (int64_t)r * HW + (int64_t)yy * W + xx;
+    if (md.mode == EPI_STORE) {
+      md.dst0[idx] = m;
+    } else if (md.mode == EPI_ADD) {
+      const float o = __fadd_rn(m, md.src0[idx]);
+      md.dst0[idx] = o;
+      k0 = max(k0, (o == o) ? fkey(o) : kFkeyNegInf);
+    } else {
+      const float o = __fadd_rn(md.src0[idx], m);
+      md.dst0[idx] = o;
+      const unsigned long long a = akey(o, (uint32_t)idx);
+      am = a > am ? a : am;
+      if (md.dst1) {
+        const float o1 = __fadd_rn(md.src1[idx], m);
+        md.dst1[idx] = o1;
+        k1 = max(k1, (o1 == o1) ? fkey(o1) : kFkeyNegInf);
+      }
+    }
+  }
+  if (md.mode == EPI_ADD && md.max0) block_reduce_commit(k0, md.max0, red);
+  if (md.mode == EPI_DOWN) {
+    if (md.max1) block_reduce_commit(k1, md.max1, red);
+    if (md.amax0) {
+      am = warp_max_u64(am);
+      const int lane = tid & 31, warp = tid >> 5;
+      if (lane == 0) redu[warp] = am;
+      __syncthreads();
+      if (tid == 0) {
+        unsigned long long b = redu[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = redu[w] > b ? redu[w] : b;
+        atomicMax(md.amax0, b);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shift tables: the nearest-neighbour source index of
+// transform_grid_fixed_size with a pure translation
+// (multi_array_transform.hpp:194-215): floor((x3 + a) + 0.5), -1 outside.
+// shifts[msg][4][R] = {a_x_in, a_y_in, a_x_out, a_y_out}; NaN in a_*_in marks
+// a log_joint_10 rotation without a source rotation.
+// tables[msg] = tx_in[R][W], ty_in[R][H], tx_out[R][W], ty_out[R][H].
+// ---------------------------------------------------------------------------
+__global__ void k_shift_tables(const double *__restrict__ shifts, int R, int H, int W,
+                               int16_t *__restrict__ tables) {
+  const int msg = blockIdx.y;
+  const double *sh = shifts + (size_t)msg * 4 * R;
+  int16_t *tb = tables + (size_t)msg * 2 * R * (W + H);
+  const int per = R * (W + H);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * per; i += gridDim.x * blockDim.x) {
+    const int side = i / per;  // 0: in, 1: out
+    int j = i - side * per;
+    int r, pos, n, axis;
+    if (j < R * W) {
+      r = j / W; pos = j - r * W; n = W; axis = 0;
+    } else {
+      j -= R * W;
+      r = j / H; pos = j - r * H; n = H; axis = 1;
+    }
+    const double a = sh[(side * 2 + axis) * R + r];
+    int16_t v = -1;
+    if (a == a) {
+      const double p = __dadd_rn(__dadd_rn((double)pos, a), 0.5);
+      const double f = floor(p);
+      if (f >= 0.0 && f < (double)n) v = (int16_t)f;
+    }
+    // layout: side 0 -> [tx_in | ty_in], side 1 -> [tx_out | ty_out]
+    tb[side * per + (axis == 0 ? r * W + pos : R * W + r * H + pos)] = v;
+  }
+}
+
+template <int RT>
+cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
+                          int *err, cudaStream_t s) {
+  const int WP = rows_stride(W, padx);
+  size_t smem = ((size_t)align4(R * WP) + ((2 * padx + 1 + kU - 1) / kU) * kU + kMaxRot) * sizeof(float);
+  if (RT == 0) smem += (size_t)kThreadsRows * R * sizeof(float);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  cudaFuncSetAttribute(k_msg_rows<RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid((unsigned)H, (unsigned)n_msgs);
+  k_msg_rows<RT><<<grid, kThreadsRows, smem, s>>>(msgs, R, H, W, padx, err);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,
+                                int16_t *tables, cudaStream_t s) {
+  dim3 grid((unsigned)((2 * R * (W + H) + 255) / 256), (unsigned)n_msgs);
+  k_shift_tables<<<grid, 256, 0, s>>>(shifts, R, H, W, tables);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
+                            int *err, cudaStream_t s) {
+  switch (R) {
+    case 12: return launch_rows_t<12>(msgs, n_msgs, R, H, W, padx, err, s);
+    case 24: return launch_rows_t<24>(msgs, n_msgs, R, H, W, padx, err, s);
+    case 48: return launch_rows_t<48>(msgs, n_msgs, R, H, W, padx, err, s);
+    default: return launch_rows_t<0>(msgs, n_msgs, R, H, W, padx, err, s);
+  }
+}
+
+cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int pady,
+                            int *err, cudaStream_t s) {
+  // Row band: the whole column when it fits, else bands of 256 rows.
+  int band = H;
+  auto smem_for = [&](int b) {
+    return ((size_t)align4((b + 2 + 2 * pady) * kCW) + (size_t)align4((b + 2) * kCW) +
+            ((2 * pady + 1 + kU - 1) / kU) * kU) * sizeof(float);
+  };
+  while (smem_for(band) > 100 * 1024 && band > 32) band = (band + 1) / 2;
+  const size_t smem = smem_for(band);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  cudaFuncSetAttribute(k_msg_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int nb = (H + band - 1) / band;
+  dim3 grid((unsigned)((W + kTX - 1) / kTX), (unsigned)(R * nb), (unsigned)n_msgs);
+  k_msg_cols<<<grid, kThreadsCols, smem, s>>>(msgs, R, H, W, band, pady, err);
+  return cudaGetLastError();
+}
+
+}  // namespace pa

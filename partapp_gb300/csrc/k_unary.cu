@@ -1,0 +1,212 @@
+// k_unary.cu -- score grids -> masked log unary maps.
+//
+// Per (part, rotation) map this fuses, in the reference's order:
+//   transform_grid_fixed_size(grid -> image, Tig, NO_CLASS_VALUE, method)
+//       (libMultiArray/multi_array_transform.hpp:123-257, called from
+//        PartApp::loadScoreGrid, libPartApp/partapp.cpp:887-896, and
+//        partdetect_dense, libPartDetect/partdetect_test.cpp:283-289)
+//   clip_scores_fill          (libPictStruct/objectdetect_aux.hpp:42-60)
+//   computeLogGrid            (libMultiArray/multi_array_op.hpp:154-167)
+//   upright mask, root strip  (libPictStruct/objectdetect_findrot.cpp:509-551)
+// and folds the map's maximum (getMinMax of the first message,
+// multi_array_op.hpp:61-77) into one atomic per CTA.
+//
+// Grid coordinates are evaluated in double with the reference's rounding
+// (explicit __dmul_rn/__dadd_rn: no fused multiply-add); for axis-aligned Tig
+// the per-column / per-row coordinates come from host-built tables.
+#include "pa_internal.cuh"
+
+namespace pa {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float clip_log(float v) {
+  if (v < 0.f) v = kClipMin;
+  return v == 0.f ? kLogZero : logf(v);
+}
+
+__device__ __forceinline__ void block_max_commit(int key, int *slot) {
+  key = __reduce_max_sync(0xFFFFFFFFu, key);
+  __shared__ int wmax[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) wmax[warp] = key;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = wmax[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, wmax[w]);
+    atomicMax(slot, m);
+  }
+}
+
+__device__ __forceinline__ int key_of(float v) { return (v == v) ? fkey(v) : kFkeyNegInf; }
+
+// TM_BILINEAR: one CTA per (map, band of rows).
+__global__ void __launch_bounds__(kThreads) k_unary_bilinear(const UnaryMap *__restrict__ maps,
+                                                             int ny, int nx, int H, int W,
+                                                             int rows_per_cta) {
+  const UnaryMap m = maps[blockIdx.x];
+  const int y0 = blockIdx.y * rows_per_cta;
+  const int y1e = min(H, y0 + rows_per_cta);
+  const float eps10 = 10.0f * 1.1920928955078125e-07f;  // 10 * FLT_EPSILON
+  int kmax = kFkeyNegInf;
+  const int npix = (y1e - y0) * W;
+  for (int i = threadIdx.x; i < npix; i += blockDim.x) {
+    const int y3 = y0 + i / W, x3 = i - (i / W) * W;
+    float v = kNoClassValue;
+    int ix1, iy1;
+    float a, b;
+    if (m.separable) {
+      ix1 = m.colx[x3];
+      a = m.cola[x3];
+      iy1 = m.rowy[y3];
+      b = m.rowb[y3];
+    } else {
+      const double x1 = __dadd_rn(__dadd_rn(__dmul_rn(m.T13[0], (double)x3), __dmul_rn(m.T13[1], (double)y3)), m.T13[2]);
+      const double yy = __dadd_rn(__dadd_rn(__dmul_rn(m.T13[3], (double)x3), __dmul_rn(m.T13[4], (double)y3)), m.T13[5]);
+      ix1 = (int)floor(x1);
+      iy1 = (int)floor(yy);
+      a = __double2float_rn(__dsub_rn(x1, (double)ix1));
+      b = __double2float_rn(__dsub_rn(yy, (double)iy1));
+    }
+    if (ix1 >= 0 && ix1 < nx && iy1 >= 0 && iy1 < ny) {
+      const float *g0 = m.grid + (int64_t)iy1 * nx + ix1;
+      if (a < eps10 && b < eps10) {
+        v = __ldg(g0);
+      } else if (ix1 < nx - 1 && iy1 < ny - 1) {
+        const float *g1 = g0 + nx;
+        const float omb = __fsub_rn(1.0f, b), oma = __fsub_rn(1.0f, a);
+        const float t0 = __fmul_rn(__fmul_rn(omb, oma), __ldg(g0));
+        const float t1 = __fmul_rn(__fmul_rn(omb, a), __ldg(g0 + 1));
+        const float t2 = __fmul_rn(__fmul_rn(b, oma), __ldg(g1));
+        const float t3 = __fmul_rn(__fmul_rn(b, a), __ldg(g1 + 1));
+        v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+      }
+    }
+    float o = clip_log(v);
+    if (m.masked_all || (m.strip > 0 && (x3 < m.strip || x3 >= W - m.strip))) o = kLogZero;
+    m.out[(int64_t)y3 * W + x3] = o;
+    kmax = max(kmax, key_of(o));
+  }
+  if (m.max_slot) block_max_commit(kmax, m.max_slot);
+}
+
+// TM_DIRECT, pass 1: every pixel starts at NO_CLASS_VALUE -> LOG_ZERO.
+__global__ void __launch_bounds__(kThreads) k_unary_direct_fill(const UnaryMap *__restrict__ maps,
+                                                                int H, int W, int rows_per_cta) {
+  const UnaryMap m = maps[blockIdx.x];
+  const int y0 = blockIdx.y * rows_per_cta;
+  const int y1e = min(H, y0 + rows_per_cta);
+  const int npix = (y1e - y0) * W;
+  float *out = m.out + (int64_t)y0 * W;
+  for (int i = threadIdx.x; i < npix; i += blockDim.x) out[i] = kLogZero;
+  if (m.max_slot && blockIdx.y == 0) block_max_commit(fkey(kLogZero), m.max_slot);
+}
+
+// TM_DIRECT, pass 2: forward-map every grid cell != NO_CLASS_VALUE
+// (multi_array_transform.hpp:173-193).  The host guarantees the map is
+// injective, so the reference's "last write wins" order never matters.
+__global__ void __launch_bounds__(kThreads) k_unary_direct_scatter(const UnaryMap *__restrict__ maps,
+                                                                   int ny, int nx, int H, int W) {
+  const UnaryMap m = maps[blockIdx.x];
+  int kmax = kFkeyNegInf;
+  for (int i = threadIdx.x; i < ny * nx; i += blockDim.x) {
+    const int y1 = i / nx, x1 = i - y1 * nx;
+    const float v = __ldg(m.grid + i);
+    if (v == kNoClassValue) continue;
+    int ix3, iy3;
+    if (m.separable) {
+      ix3 = m.colx[x1];
+      iy3 = m.rowy[y1];
+    } else {
+      const double x3 = __dadd_rn(__dadd_rn(__dmul_rn(m.T31[0], (double)x1), __dmul_rn(m.T31[1], (double)y1)), m.T31[2]);
+      const double y3 = __dadd_rn(__dadd_rn(__dmul_rn(m.T31[3], (double)x1), __dmul_rn(m.T31[4], (double)y1)), m.T31[5]);
+      ix3 = (int)floor(__dadd_rn(x3, 0.5));
+      iy3 = (int)floor(__dadd_rn(y3, 0.5));
+    }
+    if (ix3 < 0 || ix3 >= W || iy3 < 0 || iy3 >= H) continue;
+    float o = clip_log(v);
+    if (m.masked_all || (m.strip > 0 && (ix3 < m.strip || ix3 >= W - m.strip))) o = kLogZero;
+    m.out[(int64_t)iy3 * W + ix3] = o;
+    kmax = max(kmax, key_of(o));
+  }
+  if (m.max_slot) block_max_commit(kmax, m.max_slot);
+}
+
+// Upright mask + root strip applied to caller-provided log unaries, with the
+// part maximum.  masked_rot[r] != 0 marks a rotation the upright rule drops.
+__global__ void __launch_bounds__(kThreads) k_prepare_unary(const float *__restrict__ in,
+                                                            float *__restrict__ out,
+                                                            const int *__restrict__ masked_rot,
+                                                            int strip, int R, int H, int W,
+                                                            int *max_slot) {
+  const int64_t HW = (int64_t)H * W;
+  const int64_t N = HW * R;
+  int kmax = kFkeyNegInf;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / HW);
+    const int x = (int)(i % W);
+    float o = in[i];
+    if ((masked_rot && masked_rot[r]) || (strip > 0 && (x < strip || x >= W - strip))) o = kLogZero;
+    out[i] = o;
+    kmax = max(kmax, key_of(o));
+  }
+  if (max_slot) block_max_commit(kmax, max_slot);
+}
+
+__global__ void __launch_bounds__(kThreads) k_map_max(const float *__restrict__ x, int64_t N,
+                                                      int *max_slot) {
+  int kmax = kFkeyNegInf;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x)
+    kmax = max(kmax, key_of(__ldg(x + i)));
+  block_max_commit(kmax, max_slot);
+}
+
+__global__ void k_fill_int(int *p, int v, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+}  // namespace
+
+cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, int H, int W,
+                              int direct, cudaStream_t s) {
+  const int rows = 16;
+  dim3 grid((unsigned)n_maps, (unsigned)((H + rows - 1) / rows));
+  if (!direct) {
+    k_unary_bilinear<<<grid, kThreads, 0, s>>>(maps, ny, nx, H, W, rows);
+  } else {
+    k_unary_direct_fill<<<grid, kThreads, 0, s>>>(maps, H, W, rows);
+    k_unary_direct_scatter<<<(unsigned)n_maps, kThreads, 0, s>>>(maps, ny, nx, H, W);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prepare_unary(const float *in, float *out, const int *masked_rot, int strip,
+                                 int R, int H, int W, int *max_slot, cudaStream_t s) {
+  const int64_t N = (int64_t)R * H * W;
+  int blocks = (int)((N + kThreads - 1) / kThreads);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_prepare_unary<<<blocks, kThreads, 0, s>>>(in, out, masked_rot, strip, R, H, W, max_slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_map_max(const float *x, int64_t N, int *max_slot, cudaStream_t s) {
+  int blocks = (int)((N + kThreads - 1) / kThreads);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_map_max<<<blocks, kThreads, 0, s>>>(x, N, max_slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_int(int *p, int v, int64_t n, cudaStream_t s) {
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 1024) blocks = 1024;
+  if (blocks < 1) blocks = 1;
+  k_fill_int<<<blocks, 256, 0, s>>>(p, v, n);
+  return cudaGetLastError();
+}
+
+}  // namespace pa

@@ -1,0 +1,1442 @@
+// pa_api.cu -- host side of the C-ABI (include/partapp_gb300.h).
+//
+// Builds, for every call, the device-side descriptors of the pipeline
+// (stump tables, unary-map transforms, the message schedule of the tree with
+// per-message filter taps and shift tables) in one parameter blob, uploads
+// it with a single copy, and launches the kernels of k_*.cu on the context's
+// stream.  All host-side parameter math (rotation offsets, Gaussian taps,
+// index rounding, matrix inverse) repeats the reference's double-precision
+// operations in the same order; this file is compiled with FMA contraction
+// off so the host rounds exactly as the reference did.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pa_internal.cuh"
+
+using namespace pa;
+
+struct pa_classifier {
+  int dim = 0;
+  int n = 0;
+  float sum_alpha = 0.f;
+  float4 *d = nullptr;
+};
+
+struct pa_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  uint64_t launches = 0;
+  char *arena = nullptr;
+  size_t arena_cap = 0;
+  char *pinned = nullptr;
+  size_t pinned_cap = 0;
+};
+
+namespace {
+
+pa_status fail(pa_ctx *ctx, pa_status st, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return st;
+}
+
+#define PA_CK(call)                                                                 \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(ctx, PA_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));        \
+  } while (0)
+
+#define PA_LAUNCH(call)    \
+  do {                     \
+    PA_CK(call);           \
+    ++ctx->launches;       \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// ------------------------------------------------------------------------
+// Two-pass layout builder.  Pass 1 (dry) only measures the parameter blob
+// and the device scratch; pass 2 fills the blob with final device pointers.
+// The arena holds [parameter blob | scratch].
+// ------------------------------------------------------------------------
+struct Builder {
+  bool dry = true;
+  char *base = nullptr;         // device arena (pass 2)
+  size_t blob_size = 0;         // pass-2 size of the blob region (from pass 1)
+  std::vector<char> blob;
+  size_t scratch_off = 0;
+
+  static size_t al(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+  template <class T>
+  T *param(const T *src, size_t n) {
+    const size_t o = al(blob.size(), 256);
+    blob.resize(o + n * sizeof(T));
+    if (n && src) std::memcpy(blob.data() + o, src, n * sizeof(T));
+    return dry ? nullptr : reinterpret_cast<T *>(base + o);
+  }
+  template <class T>
+  T *scratch(size_t n) {
+    const size_t o = al(scratch_off, 256);
+    scratch_off = o + n * sizeof(T);
+    return dry ? nullptr : reinterpret_cast<T *>(base + al(blob_size, 256) + o);
+  }
+  size_t total() const { return al(blob_size, 256) + al(scratch_off, 256) + 256; }
+};
+
+pa_status ensure_arena(pa_ctx *ctx, size_t bytes) {
+  if (ctx->arena_cap >= bytes) return PA_OK;
+  PA_CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->arena) cudaFree(ctx->arena);
+  ctx->arena = nullptr;
+  ctx->arena_cap = 0;
+  size_t cap = bytes + bytes / 8;
+  if (cudaMalloc(&ctx->arena, cap) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->arena = nullptr;
+    return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes of device workspace", cap);
+  }
+  ctx->arena_cap = cap;
+  return PA_OK;
+}
+
+pa_status upload_blob(pa_ctx *ctx, const Builder &b) {
+  if (b.blob.empty()) return PA_OK;
+  if (ctx->pinned_cap < b.blob.size()) {
+    PA_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    ctx->pinned = nullptr;
+    ctx->pinned_cap = 0;
+    const size_t cap = b.blob.size() + b.blob.size() / 4 + 4096;
+    if (cudaMallocHost(&ctx->pinned, cap) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes of pinned staging", cap);
+    }
+    ctx->pinned_cap = cap;
+  }
+  PA_CK(cudaStreamSynchronize(ctx->stream));  // staging buffer is reused
+  std::memcpy(ctx->pinned, b.blob.data(), b.blob.size());
+  PA_CK(cudaMemcpyAsync(ctx->arena, ctx->pinned, b.blob.size(), cudaMemcpyHostToDevice,
+                        ctx->stream));
+  return PA_OK;
+}
+
+pa_status copy_in(pa_ctx *ctx, void *dst, const void *src, size_t bytes, int mem) {
+  if (!bytes) return PA_OK;
+  PA_CK(cudaMemcpyAsync(dst, src, bytes,
+                        mem == PA_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                        ctx->stream));
+  return PA_OK;
+}
+
+// ------------------------------------------------------------------------
+// Reference parameter math (host, double precision, reference op order).
+// ------------------------------------------------------------------------
+double value_from_index(double minval, double maxval, double num_steps, int idx) {
+  if (minval == maxval) return minval;                 // partapp_aux.hpp:45-58
+  double step_size = (maxval - minval) / num_steps;
+  return minval + step_size * (0.5 + idx);
+}
+int index_from_value(double minval, double maxval, double num_steps, double val) {
+  if (minval == maxval) return 0;                      // partapp_aux.hpp:23-43
+  double step_size = (maxval - minval) / num_steps;
+  return (int)std::floor((val - minval) / step_size);
+}
+double rot_from_index(const pa_exp_param *e, int idx) {
+  return value_from_index(e->min_part_rotation, e->max_part_rotation,
+                          (double)(unsigned)e->num_rotation_steps, idx);
+}
+int index_from_rot(const pa_exp_param *e, double rot) {
+  return index_from_value(e->min_part_rotation, e->max_part_rotation,
+                          (double)(unsigned)e->num_rotation_steps, rot);
+}
+double scale_from_index(const pa_exp_param *e, int idx) {
+  return value_from_index(e->min_object_scale, e->max_object_scale, 1.0, idx);
+}
+
+// rotation bin width in radians, objectdetect_findrot.cpp:319-321
+double rot_step_rad(const pa_exp_param *e) {
+  float step_f = (e->max_part_rotation - e->min_part_rotation) /
+                 (float)(unsigned)e->num_rotation_steps;
+  double s = step_f;
+  s *= M_PI / 180.0;
+  return s;
+}
+
+// get_gaussian_filter, boost_math.cpp:104-117 (unnormalised)
+std::vector<double> gaussian_taps(double sigma) {
+  int ksize = (int)std::floor(3 * sigma + 0.5);
+  std::vector<double> f(2 * ksize + 1);
+  f[ksize] = 1.0;
+  for (int i = 1; i <= ksize; ++i) {
+    f[ksize + i] = std::exp(-i * i / (2 * sigma * sigma));
+    f[ksize - i] = f[ksize + i];
+  }
+  return f;
+}
+
+// prod(prod(R(alpha), S(scale)), (ox, oy, 0)), objectdetect_findrot.cpp:348-351
+void rotate_offset(const pa_exp_param *e, int r, double scale, const double *o, double &dx,
+                   double &dy) {
+  float alpha = (float)(rot_from_index(e, r) * M_PI / 180.0);
+  double ca = std::cos((double)alpha), sa = std::sin((double)alpha);
+  double t00 = ca * scale, t01 = (-sa) * scale;
+  double t10 = sa * scale, t11 = ca * scale;
+  dx = t00 * o[0] + t01 * o[1];
+  dy = t10 * o[0] + t11 * o[1];
+}
+
+// hc::inverse, homogeneous_coord.cpp:49-69
+void hc_inverse(const double *T, double *I) {
+  double D = T[0] * T[4] - T[3] * T[1];
+  I[0] = T[4] / D;
+  I[1] = -T[1] / D;
+  I[3] = -T[3] / D;
+  I[4] = T[0] / D;
+  double t0 = I[0] * T[2] + I[1] * T[5];
+  double t1 = I[3] * T[2] + I[4] * T[5];
+  I[2] = -t0;
+  I[5] = -t1;
+  I[6] = 0;
+  I[7] = 0;
+  I[8] = 1;
+}
+
+bool exp_ok(const pa_exp_param *e) {
+  return e && e->num_rotation_steps >= 2 && e->num_rotation_steps <= kMaxRot &&
+         e->max_part_rotation > e->min_part_rotation &&
+         e->strip_border_detections >= 0 && e->strip_border_detections < 0.5f &&
+         e->roi_save_num_samples >= 0;
+}
+
+// ------------------------------------------------------------------------
+// Tree schedule (computeRootPosteriorRot / computePartMarginals order).
+// ------------------------------------------------------------------------
+struct Joint {
+  double oc[2], op[2], C[4], rot_mean, rot_sigma;
+};
+
+struct Sched {
+  int P = 0, root = 0, maxdepth = 0;
+  std::vector<std::vector<int>> ch, chj;  // children per part, joint order
+  std::vector<int> pj, depth, rslot;      // parent joint, depth, slot among root children
+  std::vector<int> upright;
+};
+
+pa_status build_sched(pa_ctx *ctx, const pa_tree *t, Sched &s) {
+  if (!t || t->n_parts < 1 || t->root < 0 || t->root >= t->n_parts)
+    return fail(ctx, PA_ERR_INVALID, "invalid tree: n_parts/root");
+  const int P = t->n_parts;
+  if (t->n_joints != P - 1)
+    return fail(ctx, PA_ERR_INVALID, "tree needs n_parts-1 joints (loadJoints asserts this)");
+  s.P = P;
+  s.root = t->root;
+  s.ch.assign(P, {});
+  s.chj.assign(P, {});
+  s.pj.assign(P, -1);
+  s.depth.assign(P, -1);
+  s.rslot.assign(P, -1);
+  s.upright.assign(P, 0);
+  for (int p = 0; p < P; ++p) s.upright[p] = t->is_upright ? (t->is_upright[p] != 0) : 0;
+  for (int j = 0; j < t->n_joints; ++j) {
+    const int c = t->child[j], q = t->parent[j];
+    if (c < 0 || c >= P || q < 0 || q >= P || c == q)
+      return fail(ctx, PA_ERR_INVALID, "joint %d: part index out of range", j);
+    if (s.pj[c] >= 0 || c == t->root)
+      return fail(ctx, PA_ERR_INVALID, "joint %d: part %d has two parents", j, c);
+    s.pj[c] = j;
+    s.ch[q].push_back(c);
+    s.chj[q].push_back(j);
+  }
+  s.depth[s.root] = 0;
+  std::vector<int> order{s.root};
+  for (size_t i = 0; i < order.size(); ++i)
+    for (int c : s.ch[order[i]]) {
+      s.depth[c] = s.depth[order[i]] + 1;
+      s.maxdepth = std::max(s.maxdepth, s.depth[c]);
+      order.push_back(c);
+    }
+  if ((int)order.size() != P) return fail(ctx, PA_ERR_INVALID, "joints do not form a tree");
+  for (int p = 0; p < P; ++p)
+    if (p != s.root && s.ch[p].size() > 1)
+      return fail(ctx, PA_ERR_UNSUPPORTED,
+                  "part %d has %zu children; the reference supports one child below the root",
+                  p, s.ch[p].size());
+  if ((int)s.ch[s.root].size() > kMaxRootChildren)
+    return fail(ctx, PA_ERR_UNSUPPORTED, "root has more than %d children", kMaxRootChildren);
+  for (size_t i = 0; i < s.ch[s.root].size(); ++i) s.rslot[s.ch[s.root][i]] = (int)i;
+  return PA_OK;
+}
+
+bool same_topology(const pa_tree *a, const pa_tree *b) {
+  if (a->n_parts != b->n_parts || a->root != b->root || a->n_joints != b->n_joints) return false;
+  for (int j = 0; j < a->n_joints; ++j)
+    if (a->child[j] != b->child[j] || a->parent[j] != b->parent[j]) return false;
+  for (int p = 0; p < a->n_parts; ++p) {
+    const int ua = a->is_upright ? a->is_upright[p] != 0 : 0;
+    const int ub = b->is_upright ? b->is_upright[p] != 0 : 0;
+    if (ua != ub) return false;
+  }
+  return true;
+}
+
+pa_status load_joints(pa_ctx *ctx, const pa_tree *t, int flip, std::vector<Joint> &js) {
+  js.resize(t->n_joints);
+  for (int j = 0; j < t->n_joints; ++j) {
+    Joint &J = js[j];
+    for (int k = 0; k < 2; ++k) {
+      J.oc[k] = t->offset_c[2 * j + k];
+      J.op[k] = t->offset_p[2 * j + k];
+    }
+    for (int k = 0; k < 4; ++k) J.C[k] = t->C[4 * j + k];
+    J.rot_mean = t->rot_mean[j];
+    J.rot_sigma = t->rot_sigma[j];
+    if (flip) {  // loadJoints, objectdetect_aux.cpp:98-116
+      J.oc[0] = -J.oc[0];
+      J.op[0] = -J.op[0];
+      J.C[1] = -J.C[1];
+      J.C[2] = -J.C[2];
+      J.rot_mean = -J.rot_mean;
+    }
+    if (J.C[1] != 0 || J.C[2] != 0)
+      return fail(ctx, PA_ERR_UNSUPPORTED,
+                  "joint %d: non-diagonal covariance (gaussFilter2dOffset) is not built", j);
+    if (!(J.C[0] > 0 && J.C[3] > 0))
+      return fail(ctx, PA_ERR_INVALID, "joint %d: covariance diagonal must be > 0", j);
+    if (!(std::isfinite(J.rot_mean) && std::isfinite(J.rot_sigma)))
+      return fail(ctx, PA_ERR_INVALID, "joint %d: rotation parameters not finite", j);
+  }
+  return PA_OK;
+}
+
+// Per-message host parameters of computeRotJointMarginal(child -> parent,
+// offset_c_10 = oc, offset_p_01 = op, rot_mean, rot_sigma).
+struct MsgParams {
+  int kidx = 0, rlen = -1, xlen = 1, ylen = 1;
+  std::vector<float> rtaps, xtaps, ytaps;
+  std::vector<double> shifts;  // [4][R]
+};
+
+void msg_params(const pa_exp_param *e, double scale, const double *oc, const double *op,
+                const double *C, double rot_mean, double rot_sigma, MsgParams &m) {
+  const int R = e->num_rotation_steps;
+  const double step = rot_step_rad(e);
+  const double rot_sigma_idx = rot_sigma / step;
+  m.kidx = (int)std::floor(-rot_mean / step + 0.5);
+  m.rtaps.clear();
+  if (rot_sigma > 0) {  // objectdetect_findrot.cpp:377-404
+    std::vector<double> f = gaussian_taps(rot_sigma_idx);
+    int first = 0, fs = (int)f.size();
+    if (fs >= R) {
+      int crot = fs / 2;
+      fs = (R % 2 == 1) ? R - 2 : R - 1;
+      first = crot - fs / 2;
+    }
+    for (int i = first; i < first + fs; ++i) m.rtaps.push_back((float)f[i]);
+    m.rlen = fs;
+  } else if (rot_sigma == 0) {
+    m.rlen = -1;
+  } else {
+    m.rlen = 0;
+  }
+  const double sc2 = scale * scale;  // gaussFilterDiag2d, multi_array_filter.hpp:232-236
+  std::vector<double> fx = gaussian_taps(std::sqrt(sc2 * C[0]));
+  std::vector<double> fy = gaussian_taps(std::sqrt(sc2 * C[3]));
+  m.xtaps.assign(fx.begin(), fx.end());
+  m.ytaps.assign(fy.begin(), fy.end());
+  m.xlen = (int)fx.size();
+  m.ylen = (int)fy.size();
+  m.shifts.assign(4 * (size_t)R, 0.0);
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+  for (int r = 0; r < R; ++r) {
+    const int rs = r - m.kidx;
+    if (rs >= 0 && rs < R) {
+      double dx, dy;
+      rotate_offset(e, rs, scale, oc, dx, dy);
+      m.shifts[0 * R + r] = -dx;
+      m.shifts[1 * R + r] = -dy;
+    } else {
+      m.shifts[0 * R + r] = nan;
+      m.shifts[1 * R + r] = nan;
+    }
+    double dx, dy;
+    rotate_offset(e, r, scale, op, dx, dy);
+    m.shifts[2 * R + r] = dx;
+    m.shifts[3 * R + r] = dy;
+  }
+}
+
+// ------------------------------------------------------------------------
+// PS plan for a batch of images (shared topology and sizes).
+// ------------------------------------------------------------------------
+struct ImgMaps {
+  std::vector<float *> U, POST, MARG, TMP, MSGR, FR;
+  float *root_post = nullptr;
+};
+
+struct PsPlan {
+  int B = 0, P = 0, R = 0, H = 0, W = 0;
+  int64_t N = 0;
+  Sched sc;
+  std::vector<ImgMaps> im;
+  int *umax = nullptr, *pmax = nullptr, *frmax = nullptr, *tmax = nullptr;  // [B][P]
+  unsigned long long *amax = nullptr;                                         // [B][P]
+  double *msgmax = nullptr;                                                   // [B][2(P-1)]
+  double *logz = nullptr, *logz_part = nullptr;                               // [B][P]
+  int *err = nullptr;
+  struct Phase {
+    MsgDesc *msgs = nullptr;
+    int n = 0, padx = 0, pady = 0;
+  };
+  std::vector<Phase> up, down;
+  RootDesc *roots = nullptr;
+  int16_t *tables = nullptr;
+  double *shifts = nullptr;
+  int n_msgs_total = 0;
+  const float **marg_ptrs = nullptr;
+  const float **post_root_ptrs = nullptr;
+  float **root_post_ptrs = nullptr;
+  int *keep = nullptr;
+  int n_keep = 0;
+};
+
+// Builds the device-side plan.  unary maps U are scratch unless `unary_in`
+// gives their final location.  marg_out/root_post_out: per image device
+// outputs (nullptr -> scratch).
+void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
+             const std::vector<std::vector<Joint>> &joints, float *const *marg_out,
+             float *const *root_post_out) {
+  const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
+  const int64_t N = pl.N;
+  const Sched &s = pl.sc;
+  const double scale = scale_from_index(e, 0);
+  pl.im.assign(B, {});
+  for (int i = 0; i < B; ++i) {
+    ImgMaps &m = pl.im[i];
+    m.U.assign(P, nullptr);
+    m.POST.assign(P, nullptr);
+    m.MARG.assign(P, nullptr);
+    m.TMP.assign(P, nullptr);
+    m.MSGR.assign(s.ch[s.root].size(), nullptr);
+    m.FR.assign(s.ch[s.root].size(), nullptr);
+    for (int p = 0; p < P; ++p) {
+      m.U[p] = b.scratch<float>(N);
+      const bool inner = (p != s.root && !s.ch[p].empty());
+      m.POST[p] = inner ? b.scratch<float>(N) : m.U[p];
+      m.TMP[p] = inner ? b.scratch<float>(N) : nullptr;
+      m.MARG[p] = marg_out && marg_out[i] ? marg_out[i] + (int64_t)p * N : b.scratch<float>(N);
+    }
+    m.POST[s.root] = m.MARG[s.root];
+    for (size_t k = 0; k < m.MSGR.size(); ++k) {
+      m.MSGR[k] = b.scratch<float>(N);
+      m.FR[k] = b.scratch<float>(N);
+    }
+    m.root_post = root_post_out && root_post_out[i] ? root_post_out[i]
+                                                    : b.scratch<float>((size_t)H * W);
+  }
+  pl.umax = b.scratch<int>((size_t)B * P);
+  pl.pmax = b.scratch<int>((size_t)B * P);
+  pl.frmax = b.scratch<int>((size_t)B * P);
+  pl.tmax = b.scratch<int>((size_t)B * P);
+  pl.amax = b.scratch<unsigned long long>((size_t)B * P);
+  pl.msgmax = b.scratch<double>((size_t)B * 2 * std::max(1, P - 1));
+  pl.logz = b.scratch<double>((size_t)B * P);
+  pl.logz_part = b.scratch<double>((size_t)B * P * kLogZBlocks);
+  pl.err = b.scratch<int>(1);
+
+  if (!e->use_pairwise) return;
+
+  // message list: upward by decreasing depth, downward by increasing depth
+  struct M {
+    int img, child, parent, joint;
+    bool up;
+  };
+  std::vector<std::vector<M>> upph, dnph;
+  std::vector<int> parent_of(P, -1);
+  for (int p = 0; p < P; ++p)
+    for (int c : s.ch[p]) parent_of[c] = p;
+  for (int d = s.maxdepth; d >= 1; --d) {
+    std::vector<M> ph;
+    for (int i = 0; i < B; ++i)
+      for (int c = 0; c < P; ++c)
+        if (s.depth[c] == d) ph.push_back({i, c, parent_of[c], s.pj[c], true});
+    upph.push_back(ph);
+  }
+  for (int d = 1; d <= s.maxdepth; ++d) {
+    std::vector<M> ph;
+    for (int i = 0; i < B; ++i)
+      for (int c = 0; c < P; ++c)
+        if (s.depth[c] == d) ph.push_back({i, c, parent_of[c], s.pj[c], false});
+    dnph.push_back(ph);
+  }
+  size_t maxph = 0;
+  for (auto &ph : upph) maxph = std::max(maxph, ph.size());
+  for (auto &ph : dnph) maxph = std::max(maxph, ph.size());
+  std::vector<float *> e2(maxph);
+  for (size_t k = 0; k < maxph; ++k) e2[k] = b.scratch<float>(N);
+
+  pl.n_msgs_total = 0;
+  for (auto &ph : upph) pl.n_msgs_total += (int)ph.size();
+  for (auto &ph : dnph) pl.n_msgs_total += (int)ph.size();
+  const size_t tbl_per = (size_t)2 * R * (W + H);
+  std::vector<double> all_shifts;
+  all_shifts.reserve((size_t)pl.n_msgs_total * 4 * R);
+
+  int msg_counter = 0;
+  auto build_phase = [&](const std::vector<M> &ph, PsPlan::Phase &out) {
+    std::vector<MsgDesc> descs(ph.size());
+    out.n = (int)ph.size();
+    out.padx = out.pady = 0;
+    for (size_t k = 0; k < ph.size(); ++k) {
+      const M &mm = ph[k];
+      const Joint &J = joints[mm.img][mm.joint];
+      const int c = mm.child;
+      const int par = mm.parent;
+      MsgParams mp;
+      if (mm.up)
+        msg_params(e, scale, J.oc, J.op, J.C, J.rot_mean, J.rot_sigma, mp);
+      else
+        msg_params(e, scale, J.op, J.oc, J.C, -J.rot_mean, J.rot_sigma, mp);
+      ImgMaps &im = pl.im[mm.img];
+      MsgDesc &d = descs[k];
+      std::memset(&d, 0, sizeof d);
+      const int ib = mm.img * P;
+      const int gidx = msg_counter++;
+      const size_t toff = (size_t)gidx * tbl_per;
+      d.tx_in = b.dry ? nullptr : pl.tables + toff;
+      d.ty_in = b.dry ? nullptr : pl.tables + toff + (size_t)R * W;
+      d.tx_out = b.dry ? nullptr : pl.tables + toff + (size_t)R * (W + H);
+      d.ty_out = b.dry ? nullptr : pl.tables + toff + (size_t)R * (W + H) + (size_t)R * W;
+      all_shifts.insert(all_shifts.end(), mp.shifts.begin(), mp.shifts.end());
+      d.rtaps = mp.rtaps.empty() ? nullptr : b.param(mp.rtaps.data(), mp.rtaps.size());
+      d.xtaps = b.param(mp.xtaps.data(), mp.xtaps.size());
+      d.ytaps = b.param(mp.ytaps.data(), mp.ytaps.size());
+      d.kidx = mp.kidx;
+      d.rlen = mp.rlen;
+      d.xlen = mp.xlen;
+      d.ylen = mp.ylen;
+      d.e2 = e2[k];
+      out.padx = std::max(out.padx, (mp.xlen - 1) / 2);
+      out.pady = std::max(out.pady, (mp.ylen - 1) / 2);
+      if (mm.up) {
+        const bool inner = !s.ch[c].empty();
+        d.in = inner ? im.POST[c] : im.U[c];
+        d.in_max = b.dry ? nullptr : (inner ? pl.pmax : pl.umax) + ib + c;
+        if (par == s.root) {
+          d.mode = EPI_STORE;
+          d.dst0 = im.MSGR[s.rslot[c]];
+        } else {
+          d.mode = EPI_ADD;
+          d.dst0 = im.POST[par];
+          d.src0 = im.U[par];
+          d.max0 = b.dry ? nullptr : pl.pmax + ib + par;
+        }
+      } else {
+        if (par == s.root) {
+          d.in = im.FR[s.rslot[c]];
+          d.in_max = b.dry ? nullptr : pl.frmax + ib + s.rslot[c];
+        } else {
+          d.in = im.TMP[par];
+          d.in_max = b.dry ? nullptr : pl.tmax + ib + par;
+        }
+        d.mode = EPI_DOWN;
+        d.dst0 = im.MARG[c];
+        d.src0 = im.POST[c];
+        d.amax0 = b.dry ? nullptr : pl.amax + ib + c;
+        if (!s.ch[c].empty()) {
+          d.dst1 = im.TMP[c];
+          d.src1 = im.U[c];
+          d.max1 = b.dry ? nullptr : pl.tmax + ib + c;
+        }
+      }
+      // in_M in schedule order: joint index (upward), P-1 + joint index (downward)
+      d.in_max_f64 = b.dry ? nullptr
+                           : pl.msgmax + (size_t)mm.img * 2 * (P - 1) + (mm.up ? 0 : P - 1) + mm.joint;
+    }
+    out.msgs = b.param(descs.data(), descs.size());
+  };
+  // tables first so descriptors can point into them
+  pl.tables = b.scratch<int16_t>((size_t)pl.n_msgs_total * tbl_per);
+  pl.up.assign(upph.size(), {});
+  pl.down.assign(dnph.size(), {});
+  for (size_t k = 0; k < upph.size(); ++k) build_phase(upph[k], pl.up[k]);
+  for (size_t k = 0; k < dnph.size(); ++k) build_phase(dnph[k], pl.down[k]);
+  pl.shifts = b.param(all_shifts.data(), all_shifts.size());
+
+  std::vector<RootDesc> rds(B);
+  for (int i = 0; i < B; ++i) {
+    RootDesc &rd = rds[i];
+    std::memset(&rd, 0, sizeof rd);
+    ImgMaps &im = pl.im[i];
+    rd.k = (int)s.ch[s.root].size();
+    for (int k = 0; k < rd.k; ++k) {
+      rd.msg[k] = im.MSGR[k];
+      rd.from_root[k] = im.FR[k];
+      rd.fr_max[k] = b.dry ? nullptr : pl.frmax + i * P + k;
+    }
+    rd.unary = im.U[s.root];
+    rd.post = im.MARG[s.root];
+    rd.amax = b.dry ? nullptr : pl.amax + i * P + s.root;
+  }
+  pl.roots = b.param(rds.data(), rds.size());
+
+  std::vector<int> keep;
+  if (s.upright[s.root]) {  // objectdetect_findrot.cpp:698-707
+    int k1 = index_from_rot(e, -1e-6), k2 = index_from_rot(e, 1e-6);
+    keep.push_back(k1);
+    if (k2 != k1) keep.push_back(k2);
+  } else {
+    for (int r = 0; r < R; ++r) keep.push_back(r);
+  }
+  pl.n_keep = (int)keep.size();
+  pl.keep = b.param(keep.data(), keep.size());
+  std::vector<const float *> pr(B);
+  std::vector<float *> rp(B);
+  for (int i = 0; i < B; ++i) {
+    pr[i] = pl.im[i].MARG[s.root];
+    rp[i] = pl.im[i].root_post;
+  }
+  pl.post_root_ptrs = b.param(pr.data(), pr.size());
+  pl.root_post_ptrs = b.param(rp.data(), rp.size());
+}
+
+void plan_marg_ptrs(Builder &b, PsPlan &pl) {
+  std::vector<const float *> mp;
+  for (int i = 0; i < pl.B; ++i)
+    for (int p = 0; p < pl.P; ++p) mp.push_back(pl.im[i].MARG[p]);
+  pl.marg_ptrs = b.param(mp.data(), mp.size());
+}
+
+pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
+  cudaStream_t st = ctx->stream;
+  const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
+  if (e->use_pairwise) {
+    if (pl.n_msgs_total > 0)
+      PA_LAUNCH(launch_shift_tables(pl.shifts, pl.n_msgs_total, R, H, W, pl.tables, st));
+    for (auto &ph : pl.up) {
+      if (!ph.n) continue;
+      PA_LAUNCH(launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
+      PA_LAUNCH(launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+    }
+    PA_LAUNCH(launch_root_combine(pl.roots, B, pl.N, st));
+    for (auto &ph : pl.down) {
+      if (!ph.n) continue;
+      PA_LAUNCH(launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
+      PA_LAUNCH(launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+    }
+    PA_LAUNCH(launch_root_posterior(pl.post_root_ptrs, pl.root_post_ptrs, pl.keep, pl.n_keep, B,
+                                    R, H, W, st));
+    // leaves without a downward message (a root without children) keep the
+    // upward belief; their argmax comes from the combine kernel (root) only.
+  } else {
+    PA_LAUNCH(launch_argmax(pl.marg_ptrs, B * P, pl.N, pl.amax, st));
+  }
+  PA_LAUNCH(launch_log_z(pl.marg_ptrs, pl.amax, B * P, pl.N, pl.logz_part, pl.logz, st));
+  return PA_OK;
+}
+
+pa_status init_slots(pa_ctx *ctx, PsPlan &pl) {
+  cudaStream_t st = ctx->stream;
+  const int n = pl.B * pl.P;
+  PA_LAUNCH(launch_fill_int(pl.umax, kFkeyNegInf, n, st));
+  PA_LAUNCH(launch_fill_int(pl.pmax, kFkeyNegInf, n, st));
+  PA_LAUNCH(launch_fill_int(pl.frmax, kFkeyNegInf, n, st));
+  PA_LAUNCH(launch_fill_int(pl.tmax, kFkeyNegInf, n, st));
+  PA_CK(cudaMemsetAsync(pl.amax, 0, sizeof(unsigned long long) * n, st));
+  PA_CK(cudaMemsetAsync(pl.err, 0, sizeof(int), st));
+  return PA_OK;
+}
+
+void decode_hyp(const pa_exp_param *e, unsigned long long key, int H, int W, pa_part_hyp *h) {
+  const float v = ukey_decode((uint32_t)(key >> 32));
+  const uint32_t flat = 0xFFFFFFFFu - (uint32_t)(key & 0xFFFFFFFFu);
+  const int64_t HW = (int64_t)H * W;
+  const int r = (int)(flat / HW);
+  const int64_t rem = flat % HW;
+  h->scaleidx = 0.f;
+  h->scale = (float)scale_from_index(e, 0);
+  h->rotidx = (float)r;
+  h->rot = (float)rot_from_index(e, r);
+  h->x = (float)(rem % W);
+  h->y = (float)(rem / W);
+  h->score = v;
+}
+
+// Reads back the small per-image results and writes host outputs.
+pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_outputs *outs,
+                    int mem) {
+  const int B = pl.B, P = pl.P, H = pl.H, W = pl.W;
+  std::vector<unsigned long long> am((size_t)B * P);
+  std::vector<double> lz((size_t)B * P), mm((size_t)B * 2 * std::max(1, P - 1));
+  int errflag = 0;
+  cudaStream_t st = ctx->stream;
+  PA_CK(cudaMemcpyAsync(am.data(), pl.amax, am.size() * 8, cudaMemcpyDeviceToHost, st));
+  PA_CK(cudaMemcpyAsync(lz.data(), pl.logz, lz.size() * 8, cudaMemcpyDeviceToHost, st));
+  PA_CK(cudaMemcpyAsync(mm.data(), pl.msgmax, mm.size() * 8, cudaMemcpyDeviceToHost, st));
+  PA_CK(cudaMemcpyAsync(&errflag, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  for (int i = 0; i < B; ++i) {
+    const pa_ps_outputs &o = outs[i];
+    if (mem == PA_MEM_HOST) {
+      if (o.log_marg)
+        for (int p = 0; p < P; ++p)
+          PA_CK(cudaMemcpyAsync(o.log_marg + (int64_t)p * pl.N, pl.im[i].MARG[p],
+                                pl.N * sizeof(float), cudaMemcpyDeviceToHost, st));
+      if (o.root_post && e->use_pairwise)
+        PA_CK(cudaMemcpyAsync(o.root_post, pl.im[i].root_post, (size_t)H * W * sizeof(float),
+                              cudaMemcpyDeviceToHost, st));
+    }
+  }
+  PA_CK(cudaStreamSynchronize(st));
+  for (int i = 0; i < B; ++i) {
+    const pa_ps_outputs &o = outs[i];
+    for (int p = 0; p < P; ++p) {
+      if (o.best) decode_hyp(e, am[(size_t)i * P + p], H, W, &o.best[p]);
+      if (o.log_z) o.log_z[p] = lz[(size_t)i * P + p];
+      if (o.n_part_hyps) o.n_part_hyps[p] = 0;
+    }
+    if (o.msg_max)
+      for (int k = 0; k < 2 * (P - 1); ++k) o.msg_max[k] = mm[(size_t)i * 2 * (P - 1) + k];
+    if (o.n_root_hyps) *o.n_root_hyps = 0;
+  }
+  if (errflag & 1)
+    return fail(ctx, PA_ERR_NUMERIC, "exp() overflowed in a message (the reference asserts here)");
+  if (errflag & ~1)
+    return fail(ctx, PA_ERR_UNSUPPORTED, "message kernel rejected its input (code %d)", errflag);
+  return PA_OK;
+}
+
+// Unary-map descriptors for B images x P parts x R rotations.
+struct UnaryTables {
+  std::vector<int> colx, rowy;
+  std::vector<float> cola, rowb;
+  bool separable = false;
+  double T13[9], T31[9];
+};
+
+pa_status unary_tables(pa_ctx *ctx, const double *Tig, int ny, int nx, int H, int W, int direct,
+                       UnaryTables &t) {
+  for (int k = 0; k < 9; ++k) t.T31[k] = Tig[k];
+  if (Tig[6] != 0 || Tig[7] != 0 || Tig[8] != 1)
+    return fail(ctx, PA_ERR_INVALID, "Tig must be affine (last row 0 0 1)");
+  hc_inverse(Tig, t.T13);
+  if (!std::isfinite(t.T13[0]) || !std::isfinite(t.T13[4]))
+    return fail(ctx, PA_ERR_INVALID, "Tig is singular");
+  if (!direct) {
+    t.separable = (t.T13[1] == 0 && t.T13[3] == 0);
+    if (t.separable) {
+      t.colx.resize(W);
+      t.cola.resize(W);
+      t.rowy.resize(H);
+      t.rowb.resize(H);
+      for (int x3 = 0; x3 < W; ++x3) {
+        double x1 = t.T13[0] * x3 + t.T13[2];
+        int ix = (int)std::floor(x1);
+        t.colx[x3] = ix;
+        t.cola[x3] = (float)(x1 - ix);
+      }
+      for (int y3 = 0; y3 < H; ++y3) {
+        double y1 = t.T13[4] * y3 + t.T13[5];
+        int iy = (int)std::floor(y1);
+        t.rowy[y3] = iy;
+        t.rowb[y3] = (float)(y1 - iy);
+      }
+    }
+  } else {
+    t.separable = (Tig[1] == 0 && Tig[3] == 0);
+    if (t.separable) {
+      t.colx.resize(nx);
+      t.rowy.resize(ny);
+      for (int x1 = 0; x1 < nx; ++x1) t.colx[x1] = (int)std::floor(Tig[0] * x1 + Tig[2] + 0.5);
+      for (int y1 = 0; y1 < ny; ++y1) t.rowy[y1] = (int)std::floor(Tig[4] * y1 + Tig[5] + 0.5);
+      for (int x1 = 1; x1 < nx; ++x1)
+        if (t.colx[x1] == t.colx[x1 - 1])
+          return fail(ctx, PA_ERR_UNSUPPORTED, "TM_DIRECT map is not injective (grid step < 1)");
+      for (int y1 = 1; y1 < ny; ++y1)
+        if (t.rowy[y1] == t.rowy[y1 - 1])
+          return fail(ctx, PA_ERR_UNSUPPORTED, "TM_DIRECT map is not injective (grid step < 1)");
+    } else {
+      // smallest singular value of the linear part must exceed sqrt(2)
+      const double a = Tig[0], b = Tig[1], c = Tig[3], d = Tig[4];
+      const double s1 = a * a + b * b + c * c + d * d, det = std::fabs(a * d - b * c);
+      const double smin2 = 0.5 * (s1 - std::sqrt(std::max(0.0, s1 * s1 - 4 * det * det)));
+      if (smin2 <= 2.0)
+        return fail(ctx, PA_ERR_UNSUPPORTED, "rotated TM_DIRECT map may collide (scale < sqrt 2)");
+    }
+  }
+  return PA_OK;
+}
+
+pa_status plan_unary(pa_ctx *ctx, Builder &b, const double *Tig, int tig_shared, int n_img, int P,
+                     int R, int ny, int nx, int H, int W, int direct, const float *scores,
+                     int64_t scores_field_stride, const std::vector<std::vector<float *>> &outs,
+                     const std::vector<int> &upright, int root, float strip_frac, int *umax,
+                     const pa_exp_param *e, UnaryMap **maps_dev, int apply_masks) {
+  const int n_tig = tig_shared ? 1 : P * R;
+  std::vector<UnaryTables> tabs(n_tig);
+  std::vector<const int *> dcolx(n_tig), drowy(n_tig);
+  std::vector<const float *> dcola(n_tig), drowb(n_tig);
+  for (int k = 0; k < n_tig; ++k) {
+    pa_status st = unary_tables(ctx, Tig + 9 * k, ny, nx, H, W, direct, tabs[k]);
+    if (st) return st;
+    if (tabs[k].separable) {
+      dcolx[k] = b.param(tabs[k].colx.data(), tabs[k].colx.size());
+      drowy[k] = b.param(tabs[k].rowy.data(), tabs[k].rowy.size());
+      if (!direct) {
+        dcola[k] = b.param(tabs[k].cola.data(), tabs[k].cola.size());
+        drowb[k] = b.param(tabs[k].rowb.data(), tabs[k].rowb.size());
+      }
+    }
+  }
+  const int strip = (int)(strip_frac * W);
+  std::vector<UnaryMap> maps((size_t)n_img * P * R);
+  for (int i = 0; i < n_img; ++i)
+    for (int p = 0; p < P; ++p)
+      for (int r = 0; r < R; ++r) {
+        UnaryMap &m = maps[((size_t)i * P + p) * R + r];
+        std::memset(&m, 0, sizeof m);
+        const int k = tig_shared ? 0 : p * R + r;
+        m.grid = b.dry ? nullptr : scores + ((int64_t)p * scores_field_stride + (int64_t)i * R + r) * ny * nx;
+        m.out = b.dry ? nullptr : outs[i][p] + (int64_t)r * H * W;
+        m.separable = tabs[k].separable;
+        m.colx = dcolx[k];
+        m.cola = dcola[k];
+        m.rowy = drowy[k];
+        m.rowb = drowb[k];
+        for (int q = 0; q < 6; ++q) {
+          m.T13[q] = tabs[k].T13[q];
+          m.T31[q] = tabs[k].T31[q];
+        }
+        if (apply_masks) {
+          m.masked_all = upright[p] && !(std::fabs(rot_from_index(e, r)) < 15.0);
+          m.strip = (p == root) ? strip : 0;
+        }
+        m.max_slot = (b.dry || !umax) ? nullptr : umax + i * P + p;
+      }
+  *maps_dev = b.param(maps.data(), maps.size());
+  return PA_OK;
+}
+
+pa_status check_classifiers(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts, int dim) {
+  if (!cls || n_parts < 1) return fail(ctx, PA_ERR_INVALID, "no classifiers");
+  for (int p = 0; p < n_parts; ++p) {
+    if (!cls[p]) return fail(ctx, PA_ERR_INVALID, "classifier %d is NULL", p);
+    if (cls[p]->dim != dim)
+      return fail(ctx, PA_ERR_INVALID, "classifier %d has dim %d, descriptors have %d", p,
+                  cls[p]->dim, dim);
+  }
+  return PA_OK;
+}
+
+StumpPart *plan_stumps(Builder &b, const pa_classifier *const *cls, int n_parts) {
+  std::vector<StumpPart> sp(n_parts);
+  for (int p = 0; p < n_parts; ++p) sp[p] = {cls[p]->d, cls[p]->n, cls[p]->sum_alpha};
+  return b.param(sp.data(), sp.size());
+}
+
+// The whole --find_obj pipeline for n_img images.
+pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
+                        int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
+                        int ny, int nx, int dim, const double *Tig, int tig_shared, int H, int W,
+                        float *scores_out, const pa_ps_outputs *outs, int mem) {
+  if (!exp_ok(e)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (n_img < 1 || !trees || !desc || !Tig || !outs || ny < 1 || nx < 1 || dim < 1 || H < 1 ||
+      W < 1 || H > 32767 || W > 32767)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  PsPlan pl;
+  pa_status st = build_sched(ctx, &trees[0], pl.sc);
+  if (st) return st;
+  for (int i = 1; i < n_img; ++i)
+    if (!same_topology(&trees[0], &trees[i]))
+      return fail(ctx, PA_ERR_INVALID, "image %d: tree topology differs from image 0", i);
+  const int P = pl.sc.P, R = e->num_rotation_steps;
+  if (n_cls < P) return fail(ctx, PA_ERR_INVALID, "need at least n_parts classifiers");
+  st = check_classifiers(ctx, cls, n_cls, dim);
+  if (st) return st;
+  std::vector<std::vector<Joint>> joints(n_img);
+  for (int i = 0; i < n_img; ++i) {
+    st = load_joints(ctx, &trees[i], flip, joints[i]);
+    if (st) return st;
+  }
+  pl.B = n_img;
+  pl.P = P;
+  pl.R = R;
+  pl.H = H;
+  pl.W = W;
+  pl.N = (int64_t)R * H * W;
+  const int64_t G = (int64_t)ny * nx;
+  const int64_t n_fields = (int64_t)n_img * R;
+
+  std::vector<float *> marg_out(n_img, nullptr), rp_out(n_img, nullptr);
+  if (mem == PA_MEM_DEVICE)
+    for (int i = 0; i < n_img; ++i) {
+      marg_out[i] = outs[i].log_marg;
+      rp_out[i] = outs[i].root_post;
+    }
+
+  DeviceGuard dg(ctx->device);
+  // pass 1 (dry): measure
+  Builder b1;
+  b1.dry = true;
+  const bool scores_dev_out = (mem == PA_MEM_DEVICE && scores_out);
+  StumpPart *sp = plan_stumps(b1, cls, n_cls);
+  const float *desc_dev = (mem == PA_MEM_DEVICE) ? desc : b1.scratch<float>(n_fields * G * dim);
+  float *scores = scores_dev_out ? scores_out : b1.scratch<float>((size_t)n_cls * n_fields * G);
+  plan_ps(b1, pl, e, joints, marg_out.data(), rp_out.data());
+  plan_marg_ptrs(b1, pl);
+  UnaryMap *umaps = nullptr;
+  std::vector<std::vector<float *>> uouts(n_img, std::vector<float *>(P, nullptr));
+  st = plan_unary(ctx, b1, Tig, tig_shared, n_img, P, R, ny, nx, H, W, !e->interpolate, scores,
+                  n_fields, uouts, pl.sc.upright, pl.sc.root, e->strip_border_detections,
+                  pl.umax, e, &umaps, 1);
+  if (st) return st;
+  // pass 2: real
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  b.base = ctx->arena;
+  PsPlan pl2 = pl;
+  sp = plan_stumps(b, cls, n_cls);
+  desc_dev = (mem == PA_MEM_DEVICE) ? desc : b.scratch<float>(n_fields * G * dim);
+  scores = scores_dev_out ? scores_out : b.scratch<float>((size_t)n_cls * n_fields * G);
+  plan_ps(b, pl2, e, joints, marg_out.data(), rp_out.data());
+  plan_marg_ptrs(b, pl2);
+  for (int i = 0; i < n_img; ++i)
+    for (int p = 0; p < P; ++p) uouts[i][p] = pl2.im[i].U[p];
+  st = plan_unary(ctx, b, Tig, tig_shared, n_img, P, R, ny, nx, H, W, !e->interpolate, scores,
+                  n_fields, uouts, pl2.sc.upright, pl2.sc.root, e->strip_border_detections,
+                  pl2.umax, e, &umaps, 1);
+  if (st) return st;
+  if (b.blob.size() != b1.blob.size() || b.scratch_off != b1.scratch_off)
+    return fail(ctx, PA_ERR_INVALID, "internal: plan size mismatch");
+
+  st = upload_blob(ctx, b);
+  if (st) return st;
+  if (mem == PA_MEM_HOST) {
+    st = copy_in(ctx, (void *)desc_dev, desc, (size_t)n_fields * G * dim * sizeof(float), mem);
+    if (st) return st;
+  }
+  st = init_slots(ctx, pl2);
+  if (st) return st;
+  cudaStream_t s = ctx->stream;
+  PA_LAUNCH(launch_score_grids(sp, n_cls, desc_dev, G, (int)n_fields, dim, 1, scores, s));
+  if (scores_out && mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(scores_out, scores, (size_t)n_cls * n_fields * G * sizeof(float),
+                          cudaMemcpyDeviceToHost, s));
+  PA_LAUNCH(launch_unary_maps(umaps, n_img * P * R, ny, nx, H, W, !e->interpolate, s));
+  if (!e->use_pairwise) {
+    // getMaxStates: the marginals are the masked unaries
+    for (int i = 0; i < n_img; ++i)
+      for (int p = 0; p < P; ++p)
+        PA_CK(cudaMemcpyAsync(pl2.im[i].MARG[p], pl2.im[i].U[p], pl2.N * sizeof(float),
+                              cudaMemcpyDeviceToDevice, s));
+  }
+  st = run_ps(ctx, e, pl2);
+  if (st) return st;
+  return finish_ps(ctx, e, pl2, outs, mem);
+}
+
+}  // namespace
+
+// ==========================================================================
+// C-ABI
+// ==========================================================================
+extern "C" {
+
+const char *pa_status_string(pa_status s) {
+  switch (s) {
+    case PA_OK: return "ok";
+    case PA_ERR_INVALID: return "invalid argument";
+    case PA_ERR_UNSUPPORTED: return "unsupported";
+    case PA_ERR_CUDA: return "CUDA error";
+    case PA_ERR_NOMEM: return "out of memory";
+    case PA_ERR_NUMERIC: return "numeric overflow";
+    default: return "unknown status";
+  }
+}
+
+void pa_exp_param_default(pa_exp_param *p) {
+  if (!p) return;
+  p->num_rotation_steps = 48;
+  p->min_part_rotation = -180.f;
+  p->max_part_rotation = 180.f;
+  p->min_object_scale = 1.f;
+  p->max_object_scale = 1.f;
+  p->strip_border_detections = 0.f;
+  p->roi_save_num_samples = 1000;
+  p->use_pairwise = 1;
+  p->interpolate = 0;
+}
+
+pa_status pa_ctx_create(int device, pa_ctx **out) {
+  if (!out) return PA_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return PA_ERR_CUDA;
+  }
+  std::unique_ptr<pa_ctx> c(new pa_ctx);
+  c->device = device;
+  DeviceGuard dg(device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return PA_ERR_CUDA;
+  }
+  c->own_stream = true;
+  *out = c.release();
+  return PA_OK;
+}
+
+pa_status pa_ctx_destroy(pa_ctx *ctx) {
+  if (!ctx) return PA_OK;
+  {
+    DeviceGuard dg(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return PA_OK;
+}
+
+pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream) {
+  if (!ctx) return PA_ERR_INVALID;
+  DeviceGuard dg(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  ctx->stream = (cudaStream_t)stream;
+  ctx->own_stream = false;
+  return PA_OK;
+}
+
+pa_status pa_ctx_synchronize(pa_ctx *ctx) {
+  if (!ctx) return PA_ERR_INVALID;
+  DeviceGuard dg(ctx->device);
+  PA_CK(cudaStreamSynchronize(ctx->stream));
+  return PA_OK;
+}
+
+const char *pa_last_error(const pa_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+uint64_t pa_ctx_kernel_launches(const pa_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int n_stumps,
+                               pa_classifier **out) {
+  if (!ctx || !out) return PA_ERR_INVALID;
+  *out = nullptr;
+  if (dim < 1 || n_stumps < 1 || !stumps)
+    return fail(ctx, PA_ERR_INVALID, "classifier needs dim >= 1 and stumps");
+  std::vector<float4> host(n_stumps);
+  float sum_alpha = 0.f;  // operator>>, AdaBoost.cc:327-331
+  for (int i = 0; i < n_stumps; ++i) {
+    if (stumps[i].f < 0 || stumps[i].f >= dim)
+      return fail(ctx, PA_ERR_INVALID, "stump %d: feature %d outside [0,%d)", i, stumps[i].f, dim);
+    float fbits;
+    std::memcpy(&fbits, &stumps[i].f, 4);
+    host[i] = make_float4(fbits, stumps[i].p, stumps[i].theta, stumps[i].alpha);
+    sum_alpha += stumps[i].alpha;
+  }
+  DeviceGuard dg(ctx->device);
+  std::unique_ptr<pa_classifier> c(new pa_classifier);
+  c->dim = dim;
+  c->n = n_stumps;
+  c->sum_alpha = sum_alpha;
+  if (cudaMalloc(&c->d, sizeof(float4) * n_stumps) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, PA_ERR_NOMEM, "cannot allocate stump table");
+  }
+  PA_CK(cudaMemcpy(c->d, host.data(), sizeof(float4) * n_stumps, cudaMemcpyHostToDevice));
+  *out = c.release();
+  return PA_OK;
+}
+
+pa_status pa_classifier_parse(pa_ctx *ctx, const char *text, size_t len, pa_classifier **out) {
+  if (!ctx || !text || !out) return PA_ERR_INVALID;
+  std::string s(text, len);
+  const char *p = s.c_str();
+  char *end = nullptr;
+  auto next_num = [&](double &v) -> bool {
+    v = std::strtod(p, &end);
+    if (end == p) return false;
+    p = end;
+    return true;
+  };
+  double dv, nv;
+  if (!next_num(dv) || !next_num(nv) || dv < 1 || nv < 1)
+    return fail(ctx, PA_ERR_INVALID, "classifier text: missing D / number of stumps");
+  const int D = (int)dv, ns = (int)nv;
+  std::vector<pa_stump> st(ns);
+  for (int i = 0; i < ns; ++i) {
+    double f, pp, a, j, th;
+    if (!next_num(f) || !next_num(pp) || !next_num(a) || !next_num(j) || !next_num(th))
+      return fail(ctx, PA_ERR_INVALID, "classifier text: stump %d truncated", i);
+    st[i].f = (int32_t)f;
+    st[i].p = (float)pp;
+    st[i].alpha = (float)a;
+    st[i].theta = (float)th;
+  }
+  return pa_classifier_create(ctx, D, st.data(), ns, out);
+}
+
+pa_status pa_classifier_destroy(pa_ctx *ctx, pa_classifier *cls) {
+  if (!cls) return PA_OK;
+  if (ctx) {
+    DeviceGuard dg(ctx->device);
+    cudaFree(cls->d);
+  } else {
+    cudaFree(cls->d);
+  }
+  delete cls;
+  return PA_OK;
+}
+
+pa_status pa_classifier_info(const pa_classifier *cls, int *dim, int *n_stumps, float *sum_alpha) {
+  if (!cls) return PA_ERR_INVALID;
+  if (dim) *dim = cls->dim;
+  if (n_stumps) *n_stumps = cls->n;
+  if (sum_alpha) *sum_alpha = cls->sum_alpha;
+  return PA_OK;
+}
+
+pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
+                         const float *desc, int n_fields, int ny, int nx, int dim, int normalize,
+                         float *scores, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!desc || !scores || n_fields < 1 || ny < 1 || nx < 1 || dim < 1)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  pa_status st = check_classifiers(ctx, cls, n_parts, dim);
+  if (st) return st;
+  DeviceGuard dg(ctx->device);
+  const int64_t G = (int64_t)ny * nx;
+  const size_t din = (size_t)n_fields * G * dim, dout = (size_t)n_parts * n_fields * G;
+  Builder b1;
+  plan_stumps(b1, cls, n_parts);
+  if (mem == PA_MEM_HOST) {
+    b1.scratch<float>(din);
+    b1.scratch<float>(dout);
+  }
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  b.base = ctx->arena;
+  StumpPart *sp = plan_stumps(b, cls, n_parts);
+  const float *d_in = desc;
+  float *d_out = scores;
+  if (mem == PA_MEM_HOST) {
+    d_in = b.scratch<float>(din);
+    d_out = b.scratch<float>(dout);
+  }
+  st = upload_blob(ctx, b);
+  if (st) return st;
+  if (mem == PA_MEM_HOST) {
+    st = copy_in(ctx, (void *)d_in, desc, din * sizeof(float), mem);
+    if (st) return st;
+  }
+  PA_LAUNCH(launch_score_grids(sp, n_parts, d_in, G, n_fields, dim, normalize, d_out, ctx->stream));
+  if (mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  PA_CK(cudaStreamSynchronize(ctx->stream));
+  return PA_OK;
+}
+
+pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
+                                const float *cells, const uint8_t *valid, int n_fields, int ny,
+                                int nx, int dc, int gx, int gy, double grid_step, int normalize,
+                                float *scores, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!cells || !valid || !scores || n_fields < 1 || ny < 1 || nx < 1 || dc < 1 || gx < 1 ||
+      gy < 1 || !(grid_step > 0))
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  const int D = gx * gy * dc;
+  pa_status st = check_classifiers(ctx, cls, n_parts, D);
+  if (st) return st;
+  DeviceGuard dg(ctx->device);
+  const int64_t G = (int64_t)ny * nx;
+  const size_t ncell = (size_t)n_fields * G * dc, nval = (size_t)n_fields * G;
+  const size_t ndense = (size_t)n_fields * G * D, dout = (size_t)n_parts * n_fields * G;
+  Builder b1;
+  plan_stumps(b1, cls, n_parts);
+  b1.scratch<float>(ndense);
+  b1.scratch<uint8_t>(nval);
+  if (mem == PA_MEM_HOST) {
+    b1.scratch<float>(ncell);
+    b1.scratch<uint8_t>(nval);
+    b1.scratch<float>(dout);
+  }
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  b.base = ctx->arena;
+  StumpPart *sp = plan_stumps(b, cls, n_parts);
+  float *dense = b.scratch<float>(ndense);
+  uint8_t *ok = b.scratch<uint8_t>(nval);
+  const float *d_cells = cells;
+  const uint8_t *d_valid = valid;
+  float *d_out = scores;
+  if (mem == PA_MEM_HOST) {
+    d_cells = b.scratch<float>(ncell);
+    d_valid = b.scratch<uint8_t>(nval);
+    d_out = b.scratch<float>(dout);
+  }
+  st = upload_blob(ctx, b);
+  if (st) return st;
+  if (mem == PA_MEM_HOST) {
+    if ((st = copy_in(ctx, (void *)d_cells, cells, ncell * sizeof(float), mem))) return st;
+    if ((st = copy_in(ctx, (void *)d_valid, valid, nval, mem))) return st;
+  }
+  cudaStream_t s = ctx->stream;
+  PA_LAUNCH(launch_window_gather(d_cells, d_valid, n_fields, ny, nx, dc, gx, gy, grid_step, dense,
+                                 ok, s));
+  PA_LAUNCH(launch_score_grids(sp, n_parts, dense, G, n_fields, D, normalize, d_out, s));
+  PA_LAUNCH(launch_mask_no_class(d_out, ok, n_parts, (int64_t)n_fields * G, s));
+  if (mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, s));
+  PA_CK(cudaStreamSynchronize(s));
+  return PA_OK;
+}
+
+pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, int ny, int nx,
+                        const double *Tig, int tig_shared, int interpolate, int H, int W,
+                        float *log_unary, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!scores || !Tig || !log_unary || n_parts < 1 || R < 1 || ny < 1 || nx < 1 || H < 1 || W < 1)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  DeviceGuard dg(ctx->device);
+  const size_t nin = (size_t)n_parts * R * ny * nx, nout = (size_t)n_parts * R * H * W;
+  pa_exp_param e;
+  pa_exp_param_default(&e);
+  e.num_rotation_steps = R;
+  std::vector<int> upright(n_parts, 0);
+  std::vector<std::vector<float *>> outs(1, std::vector<float *>(n_parts, nullptr));
+  UnaryMap *maps = nullptr;
+  Builder b1;
+  const float *d_in = scores;
+  float *d_out = log_unary;
+  if (mem == PA_MEM_HOST) {
+    b1.scratch<float>(nin);
+    b1.scratch<float>(nout);
+  }
+  pa_status st = plan_unary(ctx, b1, Tig, tig_shared, 1, n_parts, R, ny, nx, H, W, !interpolate,
+                            d_in, R, outs, upright, 0, 0.f, nullptr, &e, &maps, 0);
+  if (st) return st;
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  if ((st = ensure_arena(ctx, b1.total()))) return st;
+  b.base = ctx->arena;
+  if (mem == PA_MEM_HOST) {
+    d_in = b.scratch<float>(nin);
+    d_out = b.scratch<float>(nout);
+  }
+  for (int p = 0; p < n_parts; ++p) outs[0][p] = d_out + (size_t)p * R * H * W;
+  st = plan_unary(ctx, b, Tig, tig_shared, 1, n_parts, R, ny, nx, H, W, !interpolate, d_in, R,
+                  outs, upright, 0, 0.f, nullptr, &e, &maps, 0);
+  if (st) return st;
+  if ((st = upload_blob(ctx, b))) return st;
+  if (mem == PA_MEM_HOST)
+    if ((st = copy_in(ctx, (void *)d_in, scores, nin * sizeof(float), mem))) return st;
+  PA_LAUNCH(launch_unary_maps(maps, n_parts * R, ny, nx, H, W, !interpolate, ctx->stream));
+  if (mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(log_unary, d_out, nout * sizeof(float), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  PA_CK(cudaStreamSynchronize(ctx->stream));
+  return PA_OK;
+}
+
+pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                      const float *log_unary, int H, int W, const pa_ps_outputs *out, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (!tree || !log_unary || !out || H < 1 || W < 1 || H > 32767 || W > 32767)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  PsPlan pl;
+  pa_status st = build_sched(ctx, tree, pl.sc);
+  if (st) return st;
+  std::vector<std::vector<Joint>> joints(1);
+  if ((st = load_joints(ctx, tree, flip, joints[0]))) return st;
+  const int P = pl.sc.P, R = ep->num_rotation_steps;
+  pl.B = 1;
+  pl.P = P;
+  pl.R = R;
+  pl.H = H;
+  pl.W = W;
+  pl.N = (int64_t)R * H * W;
+  DeviceGuard dg(ctx->device);
+  float *marg_out = (mem == PA_MEM_DEVICE) ? out->log_marg : nullptr;
+  float *rp_out = (mem == PA_MEM_DEVICE) ? out->root_post : nullptr;
+  std::vector<int> masked((size_t)P * R, 0);
+  for (int p = 0; p < P; ++p)
+    if (pl.sc.upright[p])
+      for (int r = 0; r < R; ++r) masked[(size_t)p * R + r] = !(std::fabs(rot_from_index(ep, r)) < 15.0);
+  auto plan = [&](Builder &b, PsPlan &p2, int **masked_dev, const float **unary_dev) {
+    *masked_dev = b.param(masked.data(), masked.size());
+    *unary_dev = (mem == PA_MEM_HOST) ? b.scratch<float>((size_t)P * pl.N) : log_unary;
+    plan_ps(b, p2, ep, joints, &marg_out, &rp_out);
+    plan_marg_ptrs(b, p2);
+  };
+  Builder b1;
+  PsPlan pl1 = pl;
+  int *mk = nullptr;
+  const float *ud = nullptr;
+  plan(b1, pl1, &mk, &ud);
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  if ((st = ensure_arena(ctx, b1.total()))) return st;
+  b.base = ctx->arena;
+  PsPlan pl2 = pl;
+  plan(b, pl2, &mk, &ud);
+  if ((st = upload_blob(ctx, b))) return st;
+  if (mem == PA_MEM_HOST)
+    if ((st = copy_in(ctx, (void *)ud, log_unary, (size_t)P * pl.N * sizeof(float), mem))) return st;
+  if ((st = init_slots(ctx, pl2))) return st;
+  cudaStream_t s = ctx->stream;
+  const int strip = (int)(ep->strip_border_detections * W);
+  for (int p = 0; p < P; ++p) {
+    float *dst = ep->use_pairwise ? pl2.im[0].U[p] : pl2.im[0].MARG[p];
+    PA_LAUNCH(launch_prepare_unary(ud + (size_t)p * pl.N, dst, pl2.sc.upright[p] ? mk + (size_t)p * R : nullptr,
+                                   p == pl2.sc.root ? strip : 0, R, H, W, pl2.umax + p, s));
+  }
+  if ((st = run_ps(ctx, ep, pl2))) return st;
+  return finish_ps(ctx, ep, pl2, out, mem);
+}
+
+pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float *child,
+                                float *parent, int R, int H, int W, const double *offset_c,
+                                const double *offset_p, const double *C, double rot_mean,
+                                double rot_sigma, double scale, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!ep || !child || !parent || !offset_c || !offset_p || !C || H < 1 || W < 1 ||
+      H > 32767 || W > 32767 || R != ep->num_rotation_steps || !exp_ok(ep))
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes, parameters or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  if (C[1] != 0 || C[2] != 0)
+    return fail(ctx, PA_ERR_UNSUPPORTED, "non-diagonal covariance (gaussFilter2dOffset) is not built");
+  if (!(C[0] > 0 && C[3] > 0)) return fail(ctx, PA_ERR_INVALID, "covariance diagonal must be > 0");
+  DeviceGuard dg(ctx->device);
+  const int64_t N = (int64_t)R * H * W;
+  MsgParams mp;
+  msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, mp);
+  auto plan = [&](Builder &b, MsgDesc **md, int16_t **tables, double **shifts, int **slot,
+                  int **err, const float **din, float **dout, float **e2) {
+    MsgDesc d;
+    std::memset(&d, 0, sizeof d);
+    *tables = b.scratch<int16_t>((size_t)2 * R * (W + H));
+    *slot = b.scratch<int>(1);
+    *err = b.scratch<int>(1);
+    *e2 = b.scratch<float>(N);
+    *din = (mem == PA_MEM_HOST) ? b.scratch<float>(N) : child;
+    *dout = (mem == PA_MEM_HOST) ? b.scratch<float>(N) : parent;
+    d.in = *din;
+    d.in_max = *slot;
+    d.e2 = *e2;
+    d.tx_in = *tables;
+    d.ty_in = b.dry ? nullptr : *tables + (size_t)R * W;
+    d.tx_out = b.dry ? nullptr : *tables + (size_t)R * (W + H);
+    d.ty_out = b.dry ? nullptr : *tables + (size_t)R * (W + H) + (size_t)R * W;
+    d.rtaps = mp.rtaps.empty() ? nullptr : b.param(mp.rtaps.data(), mp.rtaps.size());
+    d.xtaps = b.param(mp.xtaps.data(), mp.xtaps.size());
+    d.ytaps = b.param(mp.ytaps.data(), mp.ytaps.size());
+    d.kidx = mp.kidx;
+    d.rlen = mp.rlen;
+    d.xlen = mp.xlen;
+    d.ylen = mp.ylen;
+    d.mode = EPI_STORE;
+    d.dst0 = *dout;
+    *shifts = b.param(mp.shifts.data(), mp.shifts.size());
+    *md = b.param(&d, 1);
+  };
+  MsgDesc *md;
+  int16_t *tables;
+  double *shifts;
+  int *slot, *err;
+  const float *din;
+  float *dout, *e2;
+  Builder b1;
+  plan(b1, &md, &tables, &shifts, &slot, &err, &din, &dout, &e2);
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  b.base = ctx->arena;
+  plan(b, &md, &tables, &shifts, &slot, &err, &din, &dout, &e2);
+  if ((st = upload_blob(ctx, b))) return st;
+  cudaStream_t s = ctx->stream;
+  if (mem == PA_MEM_HOST)
+    if ((st = copy_in(ctx, (void *)din, child, N * sizeof(float), mem))) return st;
+  PA_LAUNCH(launch_fill_int(slot, kFkeyNegInf, 1, s));
+  PA_CK(cudaMemsetAsync(err, 0, sizeof(int), s));
+  PA_LAUNCH(launch_map_max(din, N, slot, s));
+  PA_LAUNCH(launch_shift_tables(shifts, 1, R, H, W, tables, s));
+  PA_LAUNCH(launch_msg_rows(md, 1, R, H, W, (mp.xlen - 1) / 2, err, s));
+  PA_LAUNCH(launch_msg_cols(md, 1, R, H, W, (mp.ylen - 1) / 2, err, s));
+  if (mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(parent, dout, N * sizeof(float), cudaMemcpyDeviceToHost, s));
+  int errflag = 0;
+  PA_CK(cudaMemcpyAsync(&errflag, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PA_CK(cudaStreamSynchronize(s));
+  if (errflag & 1)
+    return fail(ctx, PA_ERR_NUMERIC, "exp() overflowed in the message (the reference asserts here)");
+  if (errflag) return fail(ctx, PA_ERR_UNSUPPORTED, "message kernel rejected its input (code %d)", errflag);
+  return PA_OK;
+}
+
+pa_status pa_find_obj(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                      const pa_classifier *const *cls, int n_cls, const float *desc, int ny,
+                      int nx, int dim, const double *Tig, int tig_shared, int H, int W,
+                      float *scores_out, const pa_ps_outputs *out, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  return find_obj_impl(ctx, ep, 1, tree, flip, cls, n_cls, desc, ny, nx, dim, Tig, tig_shared, H,
+                       W, scores_out, out, mem);
+}
+
+pa_status pa_find_obj_batch(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
+                            const pa_tree *trees, int flip, const pa_classifier *const *cls,
+                            int n_cls, const float *desc, int ny, int nx, int dim,
+                            const double *Tig, int tig_shared, int H, int W, float *scores_out,
+                            const pa_ps_outputs *out, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  return find_obj_impl(ctx, ep, n_images, trees, flip, cls, n_cls, desc, ny, nx, dim, Tig,
+                       tig_shared, H, W, scores_out, out, mem);
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+// pa_internal.cuh -- declarations shared by the CUDA kernels and the host
+// orchestration of libpartapp_gb300.  Not part of the public C-ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "partapp_gb300.h"
+
+namespace pa {
+
+constexpr float kLogZero = -1e6f;         // libBoostMath/boost_math.h:23
+constexpr float kNoClassValue = 0.0f;     // libPartDetect/partdetect.h:45
+constexpr float kClipMin = 0.0001f;       // clip_scores_fill default min_val
+constexpr int kMaxRot = 64;               // rotation bins a message kernel handles
+constexpr int kMaxRootChildren = 16;
+constexpr int kLogZBlocks = 152;          // partial sums per map in launch_log_z
+
+// ---------------------------------------------------------------------------
+// Order-preserving integer keys for float max/argmax with atomics.
+// fkey: signed-int key, a > b  <=>  fkey(a) > fkey(b) for non-NaN floats.
+// akey: 64-bit argmax key: high word orders the value (-0 folded onto +0,
+// NaN lowest), low word prefers the smaller flat index (first maximum).
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int fkey(float f) {
+  union { float f; int i; } u;
+  u.f = f;
+  return u.i >= 0 ? u.i : (u.i ^ 0x7FFFFFFF);
+}
+__host__ __device__ inline float fkey_decode(int k) {
+  union { float f; int i; } u;
+  u.i = k >= 0 ? k : (k ^ 0x7FFFFFFF);
+  return u.f;
+}
+constexpr int kFkeyNegInf = (int)(0xFF800000u ^ 0x7FFFFFFFu);  // fkey(-inf)
+
+__host__ __device__ inline uint32_t ukey(float f) {
+  union { float f; uint32_t u; } v;
+  v.f = f;
+  if (f != f) return 0u;            // NaN never wins (reference: '>' is false)
+  if (v.u == 0x80000000u) v.u = 0;  // -0 == +0
+  return (v.u & 0x80000000u) ? ~v.u : (v.u | 0x80000000u);
+}
+__host__ __device__ inline float ukey_decode(uint32_t k) {
+  union { float f; uint32_t u; } v;
+  v.u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+  return v.f;
+}
+__host__ __device__ inline unsigned long long akey(float v, uint32_t flat) {
+  return ((unsigned long long)ukey(v) << 32) | (unsigned long long)(0xFFFFFFFFu - flat);
+}
+
+// ---------------------------------------------------------------------------
+// AdaBoost stump table in device memory: {f, p, theta, alpha} per stump,
+// plus the per-classifier metadata used by the score-grid kernel.
+// ---------------------------------------------------------------------------
+struct StumpPart {
+  const float4 *stumps;  // .x = f (int bits), .y = p, .z = theta, .w = alpha
+  int n;
+  float sum_alpha;
+};
+
+// ---------------------------------------------------------------------------
+// Unary-map descriptor: one (part, rotation) score grid -> log map.
+// ---------------------------------------------------------------------------
+struct UnaryMap {
+  const float *grid;     // [ny][nx]
+  float *out;            // [H][W]
+  const int *colx;       // separable path: [W] ix1 (TM_BILINEAR) / [nx] ix3 (TM_DIRECT)
+  const float *cola;     // [W] bilinear weight a
+  const int *rowy;       // [H] iy1 / [ny] iy3
+  const float *rowb;     // [H] weight b
+  double T13[6];         // general path: grid coords of image pixel (rows 0-1)
+  double T31[6];         // general DIRECT path: image coords of grid cell
+  int separable;
+  int masked_all;        // upright part and this rotation is not kept
+  int strip;             // root border strip width in pixels (0 if none)
+  int *max_slot;         // fkey of max over the part's masked map
+};
+
+// ---------------------------------------------------------------------------
+// Message descriptor: one computeRotJointMarginal plus the accumulation the
+// reference performs with its result.
+// ---------------------------------------------------------------------------
+enum EpiMode : int {
+  EPI_STORE = 0,  // dst0 = m
+  EPI_ADD = 1,    // dst0 = m + src0              (post[u] = (0 + m) + unary[u])
+  EPI_DOWN = 2,   // dst0 = src0 + m, argmax;      (post[c] += from_root[c])
+                  // dst1 = src1 + m, max          (tmp = unary[c] + from_root[c])
+};
+
+struct MsgDesc {
+  const float *in;        // [R][H][W]
+  const int *in_max;      // fkey of max(in)
+  float *e2;              // [R][H][W] row-filtered exp-domain intermediate
+  const int16_t *tx_in;   // [R][W] source column in `in` for log_joint_10 column (or -1)
+  const int16_t *ty_in;   // [R][H] source row (or -1; all -1 if rotation has no source)
+  const int16_t *tx_out;  // [R][W] source column in log_joint_01 for parent column
+  const int16_t *ty_out;  // [R][H]
+  const float *rtaps;     // rotation taps (clipped), rlen of them
+  const float *xtaps;     // spatial x taps, xlen (odd)
+  const float *ytaps;     // spatial y taps, ylen (odd)
+  int kidx;               // rot_mean_idx: log_joint_10 rotation = source rotation + kidx
+  int rlen;               // -1: rot_sigma == 0 (identity); 0: rot_sigma < 0 (zeros)
+  int xlen, ylen;
+  int mode;
+  float *dst0;
+  const float *src0;
+  float *dst1;
+  const float *src1;
+  int *max0;
+  int *max1;
+  unsigned long long *amax0;
+  double *in_max_f64;     // optional FP64 copy of in_M
+};
+
+struct RootDesc {
+  const float *msg[kMaxRootChildren];   // root children's messages, joint order
+  float *from_root[kMaxRootChildren];
+  int *fr_max[kMaxRootChildren];
+  int k;
+  const float *unary;                   // masked unary of the root
+  float *post;                          // post[root] == root marginal
+  unsigned long long *amax;
+};
+
+// Kernel launchers (defined in the .cu files).  All return cudaGetLastError().
+cudaError_t launch_score_grids(const StumpPart *parts_dev, int n_parts, const float *desc,
+                               int64_t n_loc_per_field, int n_fields, int dim, int normalize,
+                               float *scores, cudaStream_t s);
+cudaError_t launch_window_gather(const float *cells, const uint8_t *valid, int n_fields, int ny,
+                                 int nx, int dc, int gx, int gy, double grid_step, float *dense,
+                                 uint8_t *ok, cudaStream_t s);
+cudaError_t launch_mask_no_class(float *scores, const uint8_t *ok, int n_parts, int64_t n_per_part,
+                                 cudaStream_t s);
+cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, int H, int W,
+                              int direct, cudaStream_t s);
+cudaError_t launch_prepare_unary(const float *in, float *out, const int *masked_rot, int strip,
+                                 int R, int H, int W, int *max_slot, cudaStream_t s);
+cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,
+                                int16_t *tables, cudaStream_t s);
+cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
+                            int *err_flag, cudaStream_t s);
+cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int pady,
+                            int *err_flag, cudaStream_t s);
+cudaError_t launch_root_combine(const RootDesc *rd, int n_roots, int64_t N, cudaStream_t s);
+cudaError_t launch_root_posterior(const float *const *post_root, float *const *root_post,
+                                  const int *keep, int n_keep, int n_images, int R, int H, int W,
+                                  cudaStream_t s);
+cudaError_t launch_fill_int(int *p, int v, int64_t n, cudaStream_t s);
+cudaError_t launch_map_max(const float *x, int64_t N, int *max_slot, cudaStream_t s);
+cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
+                          unsigned long long *amax, cudaStream_t s);
+cudaError_t launch_log_z(const float *const *maps, const unsigned long long *amax, int n_maps,
+                         int64_t N, double *partials, double *log_z, cudaStream_t s);
+
+}  // namespace pa

@@ -1,0 +1,294 @@
+"""Parity of the CUDA path (through the C-ABI) with the CPU oracle.
+
+Tolerances:
+  * AdaBoost scores, feature indexing, NO_CLASS_VALUE masks: bit-exact;
+  * log unary maps: the same grid cells and float bilinear weights as the
+    reference; the log differs from log(double) by at most a few ulp:
+    |d| <= 4e-7 * max(1, |v|);
+  * messages / marginals: per cell after max-normalisation,
+    |exp(a - max a) - exp(b - max b)| <= 1e-4 against the FP32 oracle
+    (TOL_F32) and <= 1e-3 against the FP64 oracle (TOL_F64);
+  * argmax (rotation, x, y) per part: identical.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as orc_mod
+from partapp_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+TOL_F32 = 1e-4
+TOL_F64 = 1e-3
+LOG_ZERO = np.float32(-1e6)
+
+
+@pytest.fixture(scope="module")
+def pa():
+    from partapp_gb300 import build
+
+    build.build()
+    import partapp_gb300
+
+    return partapp_gb300
+
+
+@pytest.fixture(scope="module")
+def ctx(pa):
+    import torch
+
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    c = pa.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def orc():
+    orc_mod.build()
+    return orc_mod
+
+
+def maxnorm_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    pa_ = np.exp(a - a.max())
+    pb_ = np.exp(b - b.max())
+    return float(np.abs(pa_ - pb_).max())
+
+
+def small_tree(rng, R):
+    return synth.make_tree(rng, R=R, offset_range=(3.0, 10.0), sigma_range=(1.0, 3.0))
+
+
+# --------------------------------------------------------------- AdaBoost
+def test_score_grids_bit_exact(ctx, orc):
+    rng = np.random.default_rng(1)
+    R, ny, nx, D = 3, 7, 33, 200
+    desc = synth.make_descriptors(rng, R, ny, nx, D)
+    m = synth.make_models(rng, n_parts=4, n_stumps=150, D=D)
+    # plant exact ties v == theta on both polarities
+    for p in range(4):
+        for i in range(0, 150, 7):
+            m["theta"][p, i] = desc[i % R, i % ny, i % nx, m["f"][p, i]]
+    cls = ctx.classifiers(m)
+    got = ctx.score_grids(cls, desc)
+    for p in range(4):
+        want = orc.adaboost_eval(m["f"][p], m["p"][p], m["theta"][p], m["alpha"][p], desc)
+        assert np.array_equal(got[p], want), f"part {p}"
+        assert cls[p].info()[2] == orc.sum_alpha(m["alpha"][p])
+
+
+def test_classifier_text_format(ctx, orc):
+    text = "4\n3\t\n0\t1\t0.5\t0.1\t0.25\t\n2\t-1\t0.75\t0.2\t0.6\t\n3\t1\t0.125\t0.3\t0.9\t\n"
+    from partapp_gb300 import Classifier
+
+    cl = Classifier.parse(ctx, text)
+    assert cl.info() == (4, 3, np.float32(0.5 + 0.75 + 0.125))
+    v = np.array([[[[0.2, 0.0, 0.7, 0.95]]]], dtype=np.float32)
+    got = ctx.score_grids([cl], v, normalize=False)
+    want = orc.adaboost_eval([0, 2, 3], [1, -1, 1], [0.25, 0.6, 0.9], [0.5, 0.75, 0.125], v,
+                             normalize=False)
+    assert got[0, 0, 0, 0] == want[0, 0, 0]
+
+
+@pytest.mark.parametrize("grid_step", [1.0, 2.0])
+def test_score_grids_window_bit_exact(ctx, orc, grid_step):
+    rng = np.random.default_rng(2)
+    F, ny, nx, dc, gx, gy = 2, 11, 13, 16, 3, 2
+    cells = synth.make_descriptors(rng, F, ny, nx, dc)
+    valid = (rng.random((F, ny, nx)) > 0.05).astype(np.uint8)
+    m = synth.make_models(rng, n_parts=3, n_stumps=80, D=gx * gy * dc)
+    cls = ctx.classifiers(m)
+    got = ctx.score_grids_window(cls, cells, valid, gx, gy, grid_step)
+    for p in range(3):
+        for k in range(F):
+            want = orc.score_grid_window(m["f"][p], m["p"][p], m["theta"][p], m["alpha"][p],
+                                         cells[k], valid[k], gx, gy, grid_step)
+            assert np.array_equal(got[p, k], want), (p, k)
+
+
+# -------------------------------------------------------------- unary maps
+@pytest.mark.parametrize("interpolate", [True, False])
+@pytest.mark.parametrize("Tig", [synth.grid_to_image(4.0), synth.grid_to_image(4.0, 1.5, 2.25)])
+def test_unary_maps(ctx, orc, interpolate, Tig):
+    rng = np.random.default_rng(3)
+    P, R, ny, nx, H, W = 2, 3, 15, 20, 60, 80
+    s = rng.uniform(-1, 1, (P, R, ny, nx)).astype(np.float32)
+    s[:, :, 3, 4] = 0.0
+    got = ctx.unary_maps(s, Tig, H, W, interpolate=interpolate)
+    for p in range(P):
+        for r in range(R):
+            img = orc.transform_grid(s[p, r], (H, W), Tig, 0.0, 1 if interpolate else 2)
+            want = orc.clip_log(img)
+            z = want == LOG_ZERO
+            assert np.array_equal(got[p, r] == LOG_ZERO, z)
+            d = np.abs(got[p, r][~z] - want[~z])
+            assert np.all(d <= 4e-7 * np.maximum(1.0, np.abs(want[~z])))
+
+
+def test_unary_maps_rotated_grid(ctx, orc):
+    rng = np.random.default_rng(4)
+    a = math.radians(22.5)
+    Tig = np.array([[4 * math.cos(a), -4 * math.sin(a), 30.0],
+                    [4 * math.sin(a), 4 * math.cos(a), 5.0], [0, 0, 1]])
+    s = rng.uniform(-1, 1, (1, 2, 14, 18)).astype(np.float32)
+    got = ctx.unary_maps(s, Tig, 64, 72, interpolate=True)
+    for r in range(2):
+        want = orc.clip_log(orc.transform_grid(s[0, r], (64, 72), Tig, 0.0, 1))
+        z = want == LOG_ZERO
+        assert np.array_equal(got[0, r] == LOG_ZERO, z)
+        assert np.max(np.abs(got[0, r][~z] - want[~z])) <= 4e-6
+
+
+# ---------------------------------------------------------------- messages
+@pytest.mark.parametrize("R", [24, 12, 8, 48])
+def test_rot_joint_marginal(ctx, orc, R):
+    rng = np.random.default_rng(10 + R)
+    H, W = 50, 70
+    child = synth.random_log_unary(rng, 1, R, H, W, zero_frac=0.02)[0]
+    step = synth.rot_step_rad(R)
+    for k, rs, oc, op, sig in [(0, 1.3, (4.2, -3.1), (-2.6, 5.7), (1.5, 2.5)),
+                               (2, 2.9, (-9.5, 7.25), (6.0, -4.5), (3.0, 1.2)),
+                               (-1, 0.0, (0.5, 0.5), (-0.5, 0.5), (0.7, 0.9))]:
+        e = orc.make_exp(R=R)
+        args = (np.array(oc), np.array(op), np.diag([sig[0] ** 2, sig[1] ** 2]), k * step, rs * step)
+        want = orc.rot_joint_marginal(e, child, *args)
+        got = ctx.rot_joint_marginal(_pa_exp(R), child, *args)
+        oob = want == LOG_ZERO
+        assert np.array_equal(got[oob], want[oob])
+        assert maxnorm_err(got, want) <= 1e-5
+        want64 = orc.rot_joint_marginal(e, child.astype(np.float64), *args, f64=True)
+        assert maxnorm_err(got, want64) <= 1e-4
+
+
+def _pa_exp(R, **kw):
+    import partapp_gb300
+
+    return partapp_gb300.exp_param(R=R, **kw)
+
+
+def compare_ps(got, want, want64=None, check_argmax=True):
+    P = want["log_marg"].shape[0]
+    for p in range(P):
+        err = maxnorm_err(got["log_marg"][p], want["log_marg"][p])
+        assert err <= TOL_F32, (p, err)
+        if want64 is not None:
+            assert maxnorm_err(got["log_marg"][p], want64["log_marg"][p]) <= TOL_F64
+    if check_argmax:
+        assert np.array_equal(got["best_conf"][:, [2, 4, 5]], want["best_conf"][:, [2, 4, 5]])
+        np.testing.assert_allclose(got["best_conf"][:, 6], want["best_conf"][:, 6], rtol=1e-5,
+                                   atol=1e-4)
+
+
+@pytest.mark.parametrize("R", [24, 16])
+def test_ps_infer_matches_oracle(ctx, orc, R):
+    rng = np.random.default_rng(20 + R)
+    H, W = 60, 80
+    tree = small_tree(rng, R)
+    u = synth.random_log_unary(rng, 10, R, H, W)
+    e = orc.make_exp(R=R)
+    want = orc.ps_infer(e, tree, u)
+    want64 = orc.ps_infer(e, tree, u.astype(np.float64), f64=True)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R), tree, u)
+    compare_ps(got, want, want64)
+    assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
+    # FP64 log-partition of every marginal
+    for p in range(10):
+        m = want64["log_marg"][p]
+        lz = m.max() + math.log(np.exp(m - m.max()).sum())
+        assert abs(got["log_z"][p] - lz) <= 1e-3 * max(1.0, abs(lz))
+
+
+@pytest.mark.parametrize("variant", ["flip", "upright", "strip", "no_pairwise", "interp_direct"])
+def test_ps_variants(ctx, orc, variant):
+    rng = np.random.default_rng(sum(map(ord, variant)))
+    R, H, W = 24, 48, 64
+    tree = small_tree(rng, R)
+    u = synth.random_log_unary(rng, 10, R, H, W)
+    kw, flip = {}, False
+    if variant == "flip":
+        flip = True
+    if variant == "upright":
+        tree["is_upright"][[8, 9]] = 1
+    if variant == "strip":
+        kw["strip"] = 0.1
+    if variant == "no_pairwise":
+        kw["use_pairwise"] = False
+    e = orc.make_exp(R=R, **kw)
+    t_or = dict(tree)
+    if flip:  # loadJoints mirroring, objectdetect_aux.cpp:98-116
+        t_or = dict(tree, offset_c=tree["offset_c"] * [-1, 1], offset_p=tree["offset_p"] * [-1, 1],
+                    rot_mean=-tree["rot_mean"])
+    want = orc.ps_infer(e, t_or, u)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R, **kw), tree, u, flip=flip)
+    compare_ps(got, want)
+    if kw.get("use_pairwise", True):
+        assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
+
+
+# ---------------------------------------------------------- --find_obj path
+@pytest.mark.parametrize("interpolate", [True, False])
+def test_find_obj_pipeline(ctx, orc, interpolate):
+    img = synth.make_image(7, R=12, H=64, W=96, n_stumps=120, D=96, offset_range=(3, 10),
+                           sigma_range=(1, 3))
+    e = orc.make_exp(R=12)
+    want = orc.find_obj(e, img["tree"], img["models"], img["desc"], img["Tig"], 64, 96,
+                        interpolate=interpolate)
+    cls = ctx.classifiers(img["models"])
+    got = ctx.find_obj(_pa_exp(12, interpolate=interpolate), img["tree"], cls, img["desc"],
+                       img["Tig"], 64, 96)
+    compare_ps(got, want)
+    assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
+
+
+def test_find_obj_batch_device_resident(ctx, orc):
+    import torch
+
+    imgs = [synth.make_image(100 + i, R=12, H=48, W=64, n_stumps=60, D=96, offset_range=(3, 8),
+                             sigma_range=(1, 2.5)) for i in range(3)]
+    models = imgs[0]["models"]
+    e = orc.make_exp(R=12)
+    desc = torch.from_numpy(np.stack([im["desc"] for im in imgs])).cuda()
+    cls = ctx.classifiers(models)
+    got = ctx.find_obj_batch(_pa_exp(12), [im["tree"] for im in imgs], cls, desc, imgs[0]["Tig"],
+                             48, 64, want_marg=True, want_root=True)
+    for i, im in enumerate(imgs):
+        want = orc.find_obj(e, im["tree"], models, im["desc"], im["Tig"], 48, 64)
+        g = dict(got[i], log_marg=got[i]["log_marg"].cpu().numpy())
+        compare_ps(g, want)
+        assert maxnorm_err(got[i]["root_post"].cpu().numpy(), want["root_post"]) <= TOL_F32
+
+
+def test_config0_full_size_one_image(ctx, orc):
+    """The BASELINE config-0 workload: 320x240, 24 rotations, 10 parts x 500
+    stumps over 960-dim descriptors at stride 4, bilinear upsampling."""
+    img = synth.make_image(2024)
+    e = orc.make_exp(R=24)
+    want = orc.find_obj(e, img["tree"], img["models"], img["desc"], img["Tig"], 240, 320)
+    cls = ctx.classifiers(img["models"])
+    got = ctx.find_obj(_pa_exp(24), img["tree"], cls, img["desc"], img["Tig"], 240, 320)
+    compare_ps(got, want)
+
+
+# ------------------------------------------------------------------ errors
+def test_errors_are_statuses(ctx, pa):
+    rng = np.random.default_rng(5)
+    R = 12
+    u = synth.random_log_unary(rng, 10, R, 20, 24)
+    tree = small_tree(rng, R)
+    bad = dict(tree, C=tree["C"].copy())
+    bad["C"][0, 1] = bad["C"][0, 2] = 0.5
+    with pytest.raises(pa.PaError) as ei:
+        ctx.compute_root_posterior_rot(_pa_exp(R), bad, u)
+    assert ei.value.status == pa.PA_ERR_UNSUPPORTED
+    two = dict(tree, parent=tree["parent"].copy())
+    two["parent"][3] = 1  # part 1 (an upper leg) now has two children
+    with pytest.raises(pa.PaError) as ei:
+        ctx.compute_root_posterior_rot(_pa_exp(R), two, u)
+    assert ei.value.status == pa.PA_ERR_UNSUPPORTED
+    with pytest.raises(pa.PaError) as ei:
+        ctx.compute_root_posterior_rot(_pa_exp(1), tree, u[:, :1])
+    assert ei.value.status == pa.PA_ERR_INVALID
