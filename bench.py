@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""Throughput of the partapp --find_obj hot path (AdaBoost part unaries + PS
+marginals) on GB300, in images/s.
+
+Workload (the "full local-appearance scale" configuration): 640x480 images,
+24 rotations, 22 AdaBoost classifiers of 500 stumps over 960-dim descriptors
+at stride 4 (one 160x120 descriptor field per rotation, Gamma(0.5,1) values
+L2-normalised per location), the 10-part tree with per-image pairwise terms
+(offsets U(10,60) px, sigma U(2,12) px, rotation sigma U(1,3) bins), score
+maps bilinearly upsampled.  Inputs are synthetic (seeded); no dataset.
+
+  python bench.py [--gpus N --steps K --warmup W --batch B]
+  python bench.py --impl reference ...   # the reference's CPU algorithm
+
+One step = one pa_find_obj_batch call over B images.  `value` is measured
+with descriptors resident in HBM; `e2e` through the same C-ABI call with
+pinned host descriptors (host->device copy inside the timed region).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+R, H, W = 24, 480, 640
+STRIDE, D = 4, 960
+NY, NX = H // STRIDE, W // STRIDE
+N_CLS, N_STUMPS, P = 22, 500, 10
+WORKLOAD = "find_obj 640x480, R=24, 22x500-stump AdaBoost over 960-d descriptors, 10-part PS"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=4, help="images per step")
+    ap.add_argument("--e2e-batch", type=int, default=2)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=1234)
+    return ap.parse_args()
+
+
+def make_models(seed):
+    from partapp_gb300 import synth
+
+    return synth.make_models(np.random.default_rng(seed), n_parts=N_CLS, n_stumps=N_STUMPS, D=D)
+
+
+def make_trees(seed, n):
+    from partapp_gb300 import synth
+
+    rng = np.random.default_rng(seed + 1)
+    return [synth.make_tree(rng, R=R, offset_range=(10.0, 60.0), sigma_range=(2.0, 12.0))
+            for _ in range(n)]
+
+
+def device_descriptors(n_img, seed, device):
+    """[n][R][NY][NX][D] Gamma(0.5,1) = z^2/2, L2-normalised per location."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    out = torch.empty((n_img, R, NY, NX, D), dtype=torch.float32, device=device)
+    for i in range(n_img):
+        for r in range(R):
+            z = torch.randn((NY, NX, D), generator=g, device=device, dtype=torch.float32)
+            z.mul_(z).mul_(0.5)
+            z.div_(torch.linalg.vector_norm(z, dim=-1, keepdim=True))
+            out[i, r].copy_(z)
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 5 + k and r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def algorithmic_bytes(trees, batch):
+    """Per-kernel algorithmic bytes of one step (one batch), FP32 maps.
+    score_grids: every descriptor read once + every score written.
+    msg_rows:    per message, input map read + exp-domain intermediate written.
+    msg_cols:    per message, intermediate read + the epilogue's reads/writes
+                 (store: 1 write; add: 1 read + 1 write; marginal: 1 read +
+                 1 write, +1 read +1 write when the child has a child).
+    """
+    N = R * H * W * 4
+    t = trees[0]
+    ch = {p: [] for p in range(P)}
+    for c, q in zip(t["child"], t["parent"]):
+        ch[int(q)].append(int(c))
+    root = int(t["root"])
+    cols = 0
+    for c, q in zip(t["child"], t["parent"]):
+        c, q = int(c), int(q)
+        cols += N * (2 if q == root else 3)            # upward
+        cols += N * (5 if ch[c] else 3)                # downward
+    n_msg = 2 * (P - 1)
+    return {
+        "score_grids": batch * (R * NY * NX * D * 4 + N_CLS * R * NY * NX * 4),
+        "msg_rows": batch * n_msg * 2 * N,
+        "msg_cols": batch * cols,
+    }
+
+
+def traffic_from_profiles(kernel):
+    """dram read+write bytes per launch of `kernel` from the committed ncu
+    summary, if present (profiles/traffic.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            d = json.load(f)
+        v = d.get(kernel)
+        return None if v is None else float(v["bytes_per_launch"])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
+def cpu_baseline_run(models, trees, desc0, n_threads):
+    """The oracle port on the host cores: n_threads images, one per thread,
+    each single-threaded like the reference; all share one descriptor field
+    set (timing does not depend on the descriptor values)."""
+    import oracle
+    from partapp_gb300 import synth
+
+    oracle.build()
+    e = oracle.make_exp(R=R)
+    descs = [desc0] * n_threads
+    t0 = time.perf_counter()
+    # per-image trees: run one batch call per distinct tree via threads
+    import concurrent.futures as cf
+
+    with cf.ThreadPoolExecutor(max_workers=n_threads) as ex:
+        futs = [ex.submit(oracle.find_obj_batch, e, trees[i % len(trees)], models, [descs[i]],
+                          synth.grid_to_image(STRIDE), H, W, True, 1) for i in range(n_threads)]
+        for f in futs:
+            f.result()
+    dt = time.perf_counter() - t0
+    return n_threads / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from partapp_gb300 import synth
+
+    n_threads = args.cpu_threads or os.cpu_count() or 1
+    models = make_models(args.seed)
+    trees = make_trees(args.seed, n_threads)
+    desc0 = synth.make_descriptors(np.random.default_rng(args.seed), R, NY, NX, D)
+    # one step ~ one image per host thread; bounded so K+W steps end in minutes
+    steps = max(1, min(args.steps, 3))
+    warm = min(args.warmup, 1)
+    for _ in range(warm):
+        cpu_baseline_run(models, trees, desc0, n_threads)
+    vals, tot = [], 0.0
+    for _ in range(steps):
+        v, dt = cpu_baseline_run(models, trees, desc0, n_threads)
+        vals.append(v)
+        tot += dt
+    value = n_threads * steps / tot
+    sample = (f"{n_threads} images per step, one per host thread, single-threaded per image "
+              f"(oracle port of the reference CPU path, 22 classifiers + 10-part PS)")
+    line = {
+        "impl": "reference", "metric": "images/s (unary+PS marginals)", "value": value,
+        "unit": "images/s", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+        "ms_per_step": 1e3 * tot / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "images_per_step": n_threads},
+        "cpu_baseline": {"value": value, "unit": "images/s", "cores": n_threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build, synth
+
+    build.build()
+    ctx = pa.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    B = args.batch
+    models = make_models(args.seed)
+    trees = make_trees(args.seed + 97 * rank, B)
+    cls = ctx.classifiers(models)
+    desc = device_descriptors(B, args.seed + 7919 * rank, dev)
+    Tig = synth.grid_to_image(STRIDE)
+    e = pa.exp_param(R=R, interpolate=True)
+
+    def step():
+        return ctx.find_obj_batch(e, trees, cls, desc, Tig, H, W)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    ctx.reset_timing()
+    ctx.enable_timing(True)
+    l0 = ctx.kernel_launches
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        t_start.record(stream)
+        for _ in range(args.steps):
+            res = step()
+        t_end.record(stream)
+        torch.cuda.synchronize(dev)
+    ctx.enable_timing(False)
+    launches = ctx.kernel_launches - l0
+    ms = t_start.elapsed_time(t_end)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ktimes = ctx.kernel_times()
+    images = B * args.steps * world
+    value = images / (ms / 1e3)
+
+    # roofline of the dominant kernel
+    peaks, peak_kind = measured_peaks()
+    alg = algorithmic_bytes(trees, B)
+    dom = max(ktimes, key=lambda k: ktimes[k][0])
+    dom_ms, dom_n = ktimes[dom]
+    roof = None
+    if dom in alg:
+        per_launch_bytes = alg[dom] * args.steps / dom_n
+        avg_ms = dom_ms / dom_n
+        achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
+                "traffic": traffic_from_profiles(dom), "alg_bytes_per_launch": per_launch_bytes,
+                "avg_launch_ms": avg_ms}
+    kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps}
+               for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][0])}
+    for k in kernels:
+        if k in alg:
+            kernels[k]["GB/s"] = alg[k] / (ktimes[k][0] / args.steps / 1e3) / 1e9
+
+    # end to end through the same C-ABI call with pinned host buffers
+    Be = min(args.e2e_batch, B)
+    host = torch.empty((Be, R, NY, NX, D), dtype=torch.float32, pin_memory=True)
+    host.copy_(desc[:Be])
+    host_np = host.numpy()
+
+    def step_e2e():
+        return ctx.find_obj_batch(e, trees[:Be], cls, host_np, Tig, H, W)
+
+    for _ in range(3):
+        step_e2e()
+    torch.cuda.synchronize(dev)
+    e2e_steps = max(2, args.steps // 2)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(e2e_steps):
+        r = step_e2e()
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = t0.elapsed_time(t1)
+    e2e_val = Be * e2e_steps / (e2e_ms / 1e3) * world
+    h2d = Be * R * NY * NX * D * 4
+    d2h = Be * P * (7 * 4 + 8) + Be * 2 * (P - 1) * 8
+
+    cpu = None
+    if rank == 0 and args.cpu_baseline:
+        n_thr = args.cpu_threads or os.cpu_count() or 1
+        desc0 = desc[0].cpu().numpy()
+        v, dt = cpu_baseline_run(models, make_trees(args.seed + 5, n_thr), desc0, n_thr)
+        cpu = {"value": v, "unit": "images/s", "cores": n_thr, "kind": "port",
+               "sample": f"{n_thr} images, one per host thread ({dt:.1f} s), oracle port of the "
+                         f"reference CPU path on this workload"}
+
+    if rank == 0:
+        best = res[0]["best_conf"]
+        line = {
+            "metric": "images/s (unary+PS marginals)", "value": value, "unit": "images/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "images_per_step": B, "parallelism": "replicas",
+                       "l2": "inputs larger than L2 (%.1f GB of descriptors per step)"
+                             % (B * R * NY * NX * D * 4 / 1e9)},
+            "e2e": {"value": e2e_val, "unit": "images/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "images_per_step": Be},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "gpu_launches": launches, "kernels": kernels,
+            "sample_best_conf_part0": [float(x) for x in best[0]],
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

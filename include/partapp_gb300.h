@@ -57,6 +57,17 @@ const char *pa_last_error(const pa_ctx *ctx);
 const char *pa_status_string(pa_status s);
 /* Number of kernels this context has launched so far. */
 uint64_t pa_ctx_kernel_launches(const pa_ctx *ctx);
+/* Per-kernel device timing, the GPU counterpart of the reference's
+ * get_runtime() prints (objectdetect_findrot.cpp:52-57, 995-998): while
+ * enabled, every launch is bracketed by CUDA events on the context's stream
+ * and the elapsed times are accumulated per kernel at each call's
+ * synchronisation point.  pa_ctx_timing_count snapshots the kernel names;
+ * pa_ctx_timing_get reads entry i of that snapshot. */
+pa_status pa_ctx_enable_timing(pa_ctx *ctx, int on);
+pa_status pa_ctx_timing_reset(pa_ctx *ctx);
+int pa_ctx_timing_count(pa_ctx *ctx);
+pa_status pa_ctx_timing_get(pa_ctx *ctx, int i, const char **name, double *total_ms,
+                            uint64_t *launches);
 
 /* ------------------------------------------------------ experiment params */
 

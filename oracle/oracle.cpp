@@ -663,16 +663,19 @@ int orc_find_obj_f32(const orc_exp *e, const orc_tree *t, const orc_models *m, c
                      float *log_unary, float *log_marg, float *best_conf, float *root_post,
                      float *part_hyps, int *n_part_hyps, float *root_hyps, int *n_root_hyps) {
   const int P = t->n_parts, R = e->num_rotation_steps;
-  if (m->n_parts != P) return -1;
+  if (m->n_parts < P) return -1;
   const size_t HW = (size_t)H * W, N = HW * R, G = (size_t)ny * nx;
   std::vector<float> unary((size_t)P * N);
   std::vector<float> grid(G);
   const int S = m->n_stumps;
-  for (int p = 0; p < P; ++p)
+  /* partdetect_dense scores every loaded classifier; the first P are the
+   * part detectors of the tree (partdetect_test.cpp:197-228) */
+  for (int p = 0; p < m->n_parts; ++p)
     for (int r = 0; r < R; ++r) {
       orc_adaboost_eval(m->f + (size_t)p * S, m->p + (size_t)p * S, m->theta + (size_t)p * S,
                         m->alpha + (size_t)p * S, S, m->sum_alpha[p], desc + (size_t)r * G * D,
                         (int64_t)G, D, 1, grid.data());
+      if (p >= P) continue;
       float *u = unary.data() + (size_t)p * N + (size_t)r * HW;
       orc_transform_grid(grid.data(), ny, nx, u, H, W, Tig, NO_CLASS_VALUE, interpolate ? 1 : 2);
       orc_clip_log(u, (int64_t)HW);

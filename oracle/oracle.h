@@ -143,9 +143,10 @@ int orc_find_local_max(const float *grid, int S, int H, int W, int max_n,
                        double *out);
 
 
-/* AdaBoost models of all parts (one classifier per part, n_stumps each). */
+/* AdaBoost classifiers (n_stumps each); the first tree->n_parts of them are
+ * the part detectors the tree uses, any further ones are evaluated only. */
 typedef struct {
-  int n_parts;
+  int n_parts;                /* number of classifiers */
   int n_stumps;               /* stumps per classifier */
   const int32_t *f;           /* [n_parts][n_stumps] feature index */
   const float *p;             /* polarity */

@@ -39,7 +39,8 @@ NO_CLASS_VALUE = 0.0
 # every symbol include/partapp_gb300.h declares
 EXPORTS = (
     "pa_ctx_create", "pa_ctx_destroy", "pa_ctx_set_stream", "pa_ctx_synchronize",
-    "pa_last_error", "pa_status_string", "pa_ctx_kernel_launches", "pa_exp_param_default",
+    "pa_last_error", "pa_status_string", "pa_ctx_kernel_launches", "pa_ctx_enable_timing",
+    "pa_ctx_timing_reset", "pa_ctx_timing_count", "pa_ctx_timing_get", "pa_exp_param_default",
     "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
     "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
     "pa_ps_infer", "pa_rot_joint_marginal", "pa_find_obj", "pa_find_obj_batch",
@@ -108,6 +109,10 @@ def load_library():
     L.pa_status_string.restype = C.c_char_p
     L.pa_ctx_kernel_launches.argtypes = [vp]
     L.pa_ctx_kernel_launches.restype = C.c_uint64
+    L.pa_ctx_enable_timing.argtypes = [vp, ip]
+    L.pa_ctx_timing_reset.argtypes = [vp]
+    L.pa_ctx_timing_count.argtypes = [vp]
+    L.pa_ctx_timing_get.argtypes = [vp, ip, P(C.c_char_p), P(dp), P(C.c_uint64)]
     L.pa_exp_param_default.argtypes = [P(ExpParam)]
     L.pa_exp_param_default.restype = None
     L.pa_classifier_create.argtypes = [vp, ip, P(Stump), ip, P(vp)]
@@ -259,6 +264,21 @@ class Context:
     @property
     def kernel_launches(self) -> int:
         return int(self.L.pa_ctx_kernel_launches(self.h))
+
+    def enable_timing(self, on: bool = True):
+        self._check(self.L.pa_ctx_enable_timing(self.h, int(on)))
+
+    def reset_timing(self):
+        self._check(self.L.pa_ctx_timing_reset(self.h))
+
+    def kernel_times(self) -> dict:
+        """{kernel: (total_ms, launches)} accumulated while timing was on."""
+        out = {}
+        for i in range(self.L.pa_ctx_timing_count(self.h)):
+            nm, ms, n = C.c_char_p(), C.c_double(), C.c_uint64()
+            self._check(self.L.pa_ctx_timing_get(self.h, i, C.byref(nm), C.byref(ms), C.byref(n)))
+            out[nm.value.decode()] = (ms.value, int(n.value))
+        return out
 
     # ---------------------------------------------------------- unaries
     def classifiers(self, models) -> list:

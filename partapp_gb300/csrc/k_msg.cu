@@ -84,7 +84,7 @@ __host__ __device__ __forceinline__ int align4(int n) { return (n + 3) & ~3; }
 // k_msg_rows
 // ---------------------------------------------------------------------------
 template <int RT>
-__global__ void __launch_bounds__(kThreadsRows) k_msg_rows(const MsgDesc *__restrict__ msgs,
+__global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 3) k_msg_rows(const MsgDesc *__restrict__ msgs,
                                                            int Rrt, int H, int W, int padx,
                                                            int *err) {
   const int R = RT > 0 ? RT : Rrt;
@@ -104,19 +104,39 @@ __global__ void __launch_bounds__(kThreadsRows) k_msg_rows(const MsgDesc *__rest
   // (1) stage exp(J10 - M) for all rotations of row y; zero padding.
   const float negM = -fkey_decode(*md.in_max);
   const int HW = H * W;
-  for (int idx = tid; idx < R * WP; idx += blockDim.x) {
-    const int r = idx / WP;
-    const int x = idx - r * WP - padx;
-    float v = 0.f;
-    if (x >= 0 && x < W) {
-      const int sy = md.ty_in[r * H + y];
-      const int sx = md.tx_in[r * W + x];
-      float lv = kLogZero;
-      if (sy >= 0 && sx >= 0) lv = __ldg(md.in + (int64_t)(r - md.kidx) * HW + sy * W + sx);
-      v = expf(__fadd_rn(lv, negM));
-      if (v == INFINITY) atomicOr(err, 1);
+  const int pad_r = WP - padx - W;
+  for (int idx = tid; idx < R * (padx + pad_r); idx += blockDim.x) {
+    const int r = idx / (padx + pad_r), k = idx - r * (padx + pad_r);
+    E[r * WP + (k < padx ? k : padx + W + (k - padx))] = 0.f;
+  }
+  {
+    // four independent gathers in flight per thread
+    constexpr int U = 4;
+    const int n = R * W;
+    for (int base = tid; base < n; base += U * blockDim.x) {
+      float lv[U];
+      int dst[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int idx = base + u * blockDim.x;
+        lv[u] = kLogZero;
+        dst[u] = -1;
+        if (idx < n) {
+          const int r = idx / W, x = idx - r * W;
+          dst[u] = r * WP + padx + x;
+          const int sy = md.ty_in[r * H + y];
+          const int sx = md.tx_in[r * W + x];
+          if (sy >= 0 && sx >= 0) lv[u] = __ldg(md.in + (int64_t)(r - md.kidx) * HW + sy * W + sx);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (dst[u] < 0) continue;
+        const float v = expf(__fadd_rn(lv[u], negM));
+        if (v == INFINITY) atomicOr(err, 1);
+        E[dst[u]] = v;
+      }
     }
-    E[idx] = v;
   }
   __syncthreads();
 
@@ -225,13 +245,24 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
     lim[0] = 1 << 30; lim[1] = -1; lim[2] = 1 << 30; lim[3] = -1;
   }
   __syncthreads();
-  for (int i = tid; i < (x1 - x0) + (y1 - y0); i += blockDim.x) {
-    if (i < x1 - x0) {
-      const int c = txo[x0 + i];
-      if (c >= 0) { atomicMin(&lim[0], c); atomicMax(&lim[1], c); }
-    } else {
-      const int rr = tyo[y0 + i - (x1 - x0)];
-      if (rr >= 0) { atomicMin(&lim[2], rr); atomicMax(&lim[3], rr); }
+  {
+    int cmn = 1 << 30, cmx = -1, rmn = 1 << 30, rmx = -1;
+    for (int i = tid; i < (x1 - x0) + (y1 - y0); i += blockDim.x) {
+      if (i < x1 - x0) {
+        const int c = txo[x0 + i];
+        if (c >= 0) { cmn = min(cmn, c); cmx = max(cmx, c); }
+      } else {
+        const int rr = tyo[y0 + i - (x1 - x0)];
+        if (rr >= 0) { rmn = min(rmn, rr); rmx = max(rmx, rr); }
+      }
+    }
+    cmn = __reduce_min_sync(0xFFFFFFFFu, cmn);
+    cmx = __reduce_max_sync(0xFFFFFFFFu, cmx);
+    rmn = __reduce_min_sync(0xFFFFFFFFu, rmn);
+    rmx = __reduce_max_sync(0xFFFFFFFFu, rmx);
+    if ((tid & 31) == 0) {
+      atomicMin(&lim[0], cmn); atomicMax(&lim[1], cmx);
+      atomicMin(&lim[2], rmn); atomicMax(&lim[3], rmx);
     }
   }
   __syncthreads();
@@ -254,12 +285,25 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
   const float *e2 = md.e2 + (int64_t)r * HW;
   if (any) {
     // stage E2 rows [rmin - ky, rmax + ky] x columns [cmin, cmin + kCW), zero outside
-    for (int i = tid; i < srows * kCW; i += blockDim.x) {
-      const int sr = i / kCW, c = i - sr * kCW;
-      const int yy = rmin - ky + sr, xx = cmin + c;
-      float v = 0.f;
-      if (yy >= 0 && yy < H && xx < W && xx <= cmax) v = e2[(int64_t)yy * W + xx];
-      S[i] = v;
+    constexpr int U = 4;
+    const int n = srows * kCW;
+    for (int base = tid; base < n; base += U * blockDim.x) {
+      float v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = base + u * blockDim.x;
+        v[u] = 0.f;
+        if (i < n) {
+          const int sr = i / kCW, c = i - sr * kCW;
+          const int yy = rmin - ky + sr, xx = cmin + c;
+          if (yy >= 0 && yy < H && xx < W && xx <= cmax) v[u] = __ldg(e2 + (int64_t)yy * W + xx);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = base + u * blockDim.x;
+        if (i < n) S[i] = v[u];
+      }
     }
   }
   __syncthreads();
@@ -305,30 +349,52 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
   const int tw = x1 - x0;
   int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
   unsigned long long am = 0ull;
-  for (int i = tid; i < (y1 - y0) * tw; i += blockDim.x) {
-    const int yy = y0 + i / tw, xx = x0 + (i - (i / tw) * tw);
-    const int sy = tyo[yy], sx = txo[xx];
-    float m = kLogZero;
-    if (sy >= 0 && sx >= 0) {
-      const float f = F[(sy - rmin) * kCW + (sx - cmin)];
-      m = __fadd_rn(f == 0.f ? kLogZero : logf(f), M);
+  const int n_out = (y1 - y0) * tw;
+  const int mode = md.mode;
+  const float *src0 = md.src0, *src1 = md.src1;
+  float *dst0 = md.dst0, *dst1 = md.dst1;
+  constexpr int U = 4;
+  for (int base = tid; base < n_out; base += U * blockDim.x) {
+    float m[U], a0[U], a1[U];
+    int64_t idx[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = base + u * blockDim.x;
+      idx[u] = -1;
+      m[u] = kLogZero;
+      a0[u] = 0.f;
+      a1[u] = 0.f;
+      if (i < n_out) {
+        const int yy = y0 + i / tw, xx = x0 + (i - (i / tw) * tw);
+        const int sy = tyo[yy], sx = txo[xx];
+        if (sy >= 0 && sx >= 0) {
+          const float f = F[(sy - rmin) * kCW + (sx - cmin)];
+          m[u] = __fadd_rn(f == 0.f ? kLogZero : logf(f), M);
+        }
+        idx[u] = (int64_t)r * HW + (int64_t)yy * W + xx;
+        if (mode != EPI_STORE) a0[u] = __ldg(src0 + idx[u]);
+        if (mode == EPI_DOWN && dst1) a1[u] = __ldg(src1 + idx[u]);
+      }
     }
-    const int64_t idx = (int64_t)r * HW + (int64_t)yy * W + xx;
-    if (md.mode == EPI_STORE) {
-      md.dst0[idx] = m;
-    } else if (md.mode == EPI_ADD) {
-      const float o = __fadd_rn(m, md.src0[idx]);
-      md.dst0[idx] = o;
-      k0 = max(k0, (o == o) ? fkey(o) : kFkeyNegInf);
-    } else {
-      const float o = __fadd_rn(md.src0[idx], m);
-      md.dst0[idx] = o;
-      const unsigned long long a = akey(o, (uint32_t)idx);
-      am = a > am ? a : am;
-      if (md.dst1) {
-        const float o1 = __fadd_rn(md.src1[idx], m);
-        md.dst1[idx] = o1;
-        k1 = max(k1, (o1 == o1) ? fkey(o1) : kFkeyNegInf);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (idx[u] < 0) continue;
+      if (mode == EPI_STORE) {
+        dst0[idx[u]] = m[u];
+      } else if (mode == EPI_ADD) {
+        const float o = __fadd_rn(m[u], a0[u]);
+        dst0[idx[u]] = o;
+        k0 = max(k0, (o == o) ? fkey(o) : kFkeyNegInf);
+      } else {
+        const float o = __fadd_rn(a0[u], m[u]);
+        dst0[idx[u]] = o;
+        const unsigned long long k = akey(o, (uint32_t)idx[u]);
+        am = k > am ? k : am;
+        if (dst1) {
+          const float o1 = __fadd_rn(a1[u], m[u]);
+          dst1[idx[u]] = o1;
+          k1 = max(k1, (o1 == o1) ? fkey(o1) : kFkeyNegInf);
+        }
       }
     }
   }

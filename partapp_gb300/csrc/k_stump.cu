@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(512) k_score_grids(const StumpPart *__restrict
   for (int i = 0; i < sp.n; ++i) {
     const float4 q = __ldg(st + i);
     const float val = v[__float_as_int(q.x) ^ lane];
-    s += (__fmul_rn(val, q.y) < __fmul_rn(q.z, q.y)) ? q.w : -q.w;
+    s += (__fmul_rn(val, q.y) < q.z) ? q.w : -q.w;
   }
   if (normalize) s = __fdiv_rn(s, sp.sum_alpha);
   scores[((int64_t)part * n_fields + field) * n_loc + loc0 + lane] = s;
@@ -107,11 +107,160 @@ __global__ void k_mask_no_class(float *__restrict__ scores, const uint8_t *__res
     for (int p = 0; p < n_parts; ++p) scores[(int64_t)p * n_per_part + i] = kNoClassValue;
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined variant for 960-dim descriptors.
+//
+// The classifiers are split into G groups of at most kMaxWarps; a CTA serves
+// one group and keeps that group's stump tables resident in shared memory
+// for the whole launch.  The CTAs of the G groups walk the tiles in the same
+// order, so the second read of a tile is an L2 hit.
+//
+// Persistent CTAs walk the tiles; while a tile is being evaluated, the next
+// tile is already in flight into registers (kChunks float4 per thread).
+// Rows are stored with a stride of DIM + 1 floats, so the 32 lanes (32
+// locations) reading one feature hit 32 banks, and a warp's staging store of
+// 4 rows x 8 float4 chunks hits bank (l + 4q + j) mod 32, again all 32 banks.
+//
+// Stump records are {f, t, a, -}: for a polarity p = +1 the test
+// v*p < theta*p is v < theta; for p = -1 it is v > theta, i.e.
+// !(v < nextafter(theta, +inf)).  With t = theta or nextafter(theta, +inf)
+// and a = p*alpha the reference's vote (v*p < theta*p) ? alpha : -alpha is
+// (v < t) ? a : -a for every finite v -- one compare, one select, one add.
+// Classifiers with other polarities use the literal form (k_score_grids).
+// ---------------------------------------------------------------------------
+constexpr int kChunks = 24;
+constexpr int kMaxWarps = 11;
+
+template <int DIM>
+__global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
+    const StumpPart *__restrict__ parts, int n_parts, int n_groups, int group_size,
+    const float *__restrict__ desc, int64_t n_loc, int normalize, float *__restrict__ scores,
+    int n_fields) {
+  static_assert(DIM % 32 == 0, "DIM must be a multiple of 32");
+  constexpr int kCpr = DIM / 4;          // float4 chunks per row
+  constexpr int kBlk = 8 * (kCpr / 8);   // 4-row x 8-chunk blocks per tile
+  constexpr int kStride = DIM + 1;       // padded shared-memory row
+  extern __shared__ __align__(16) float sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int group = blockIdx.x % n_groups;
+  const int cta_in_group = blockIdx.x / n_groups;
+  const int ctas_per_group = gridDim.x / n_groups;
+  // this warp's classifier (warps past the group size only stage tiles)
+  const int part = warp < group_size ? group * group_size + warp : n_parts;
+  const int64_t blocks_per_field = (n_loc + kLoc - 1) / kLoc;
+  const int64_t n_tiles = blocks_per_field * n_fields;
+  const int lrow = lane >> 3, lchunk = lane & 7;
+
+  // resident stump tables of the group: warp w's table at stumps_sm[w]
+  float4 *stab = reinterpret_cast<float4 *>(sm + 32 * kStride + ((32 * kStride) & 3 ? 4 - ((32 * kStride) & 3) : 0));
+  int my_n = 0;
+  float my_sum_alpha = 1.f;
+  const float4 *my_tab = stab;
+  {
+    int off = 0;
+    for (int w = 0; w < group_size && w < nwarps; ++w) {
+      const int pw = group * group_size + w;
+      if (pw >= n_parts) break;
+      const StumpPart sp = parts[pw];
+      if (w == warp) {
+        my_n = sp.n;
+        my_sum_alpha = sp.sum_alpha;
+        my_tab = stab + off;
+        for (int i = lane; i < sp.n; i += 32) stab[off + i] = __ldg(sp.fast + i);
+      }
+      off += sp.n;
+    }
+  }
+
+  float4 st[kChunks];
+  auto load_tile = [&](int64_t tt) {
+    const int field = (int)(tt / blocks_per_field);
+    const int64_t loc0 = (tt - (int64_t)field * blocks_per_field) * kLoc;
+    const int nl = (n_loc - loc0) < kLoc ? (int)(n_loc - loc0) : kLoc;
+    const float4 *src = reinterpret_cast<const float4 *>(desc + ((int64_t)field * n_loc + loc0) * DIM) +
+                        lrow * kCpr + 24 * warp + lchunk;
+#pragma unroll
+    for (int k = 0; k < kChunks; ++k) {
+      const int g = warp * kChunks + k;
+      const int l = 4 * (k & 7) + lrow;
+      if (g < kBlk && l < nl) st[k] = __ldg(src + (4 * (k & 7)) * kCpr + 8 * (k >> 3));
+      else st[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+
+  int64_t t = cta_in_group;
+  if (t < n_tiles) load_tile(t);
+  for (; t < n_tiles; t += ctas_per_group) {
+    __syncthreads();  // the previous tile is no longer read (first pass: stump tables staged)
+#pragma unroll
+    for (int k = 0; k < kChunks; ++k) {
+      const int g = warp * kChunks + k;
+      if (g < kBlk) {
+        const int l = 4 * (k & 7) + lrow;
+        float *dst = sm + l * kStride + 4 * (8 * (3 * warp + (k >> 3)) + lchunk);
+        dst[0] = st[k].x;
+        dst[1] = st[k].y;
+        dst[2] = st[k].z;
+        dst[3] = st[k].w;
+      }
+    }
+    __syncthreads();
+    if (t + ctas_per_group < n_tiles) load_tile(t + ctas_per_group);
+    if (part < n_parts) {
+      const int field = (int)(t / blocks_per_field);
+      const int64_t loc0 = (t - (int64_t)field * blocks_per_field) * kLoc;
+      const int nl = (n_loc - loc0) < kLoc ? (int)(n_loc - loc0) : kLoc;
+      const float *v = sm + lane * kStride;
+      float s = 0.f;
+#pragma unroll 8
+      for (int i = 0; i < my_n; ++i) {
+        const float4 q = my_tab[i];  // {f, t, a, -}
+        const float val = v[__float_as_int(q.x)];
+        s += (val < q.y) ? q.z : -q.z;
+      }
+      if (normalize) s = __fdiv_rn(s, my_sum_alpha);
+      if (lane < nl) scores[((int64_t)part * n_fields + field) * n_loc + loc0 + lane] = s;
+    }
+  }
+}
+
 }  // namespace
 
-cudaError_t launch_score_grids(const StumpPart *parts_dev, int n_parts, const float *desc,
+cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
+                               const int *n_stumps, int n_parts, const float *desc,
                                int64_t n_loc, int n_fields, int dim, int normalize,
                                float *scores, cudaStream_t s) {
+  // pipelined kernel: groups of <= kMaxWarps classifiers with resident
+  // stump tables; needs 960-dim descriptors, unit polarities and room for
+  // the tables next to the 32 x 961 tile.
+  const bool aligned = ((uintptr_t)desc & 15) == 0;
+  bool all_fast = true;
+  for (int p = 0; p < n_parts; ++p) all_fast = all_fast && fast_ok[p];
+  const int n_groups = (n_parts + kMaxWarps - 1) / kMaxWarps;
+  const int nw = (n_parts + n_groups - 1) / n_groups;
+  size_t max_group_stumps = 0;
+  for (int g = 0; g < n_groups; ++g) {
+    size_t tot = 0;
+    for (int p = g * nw; p < n_parts && p < (g + 1) * nw; ++p) tot += (size_t)n_stumps[p];
+    max_group_stumps = tot > max_group_stumps ? tot : max_group_stumps;
+  }
+  const size_t tile_bytes = ((size_t)kLoc * 961 + 3) / 4 * 4 * sizeof(float);
+  const size_t smem_pipe = tile_bytes + max_group_stumps * sizeof(float4);
+  const int launch_warps = nw < 10 ? 10 : nw;  // ten warps stage a 960-wide tile
+  if (dim == 960 && aligned && all_fast && smem_pipe <= 227 * 1024) {
+    cudaFuncSetAttribute(k_score_grids_pipe<960>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_pipe);
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t n_tiles = ((n_loc + kLoc - 1) / kLoc) * n_fields;
+    int64_t per_group = sms / n_groups;
+    if (per_group < 1) per_group = 1;
+    if (per_group > n_tiles) per_group = n_tiles;
+    k_score_grids_pipe<960><<<(unsigned)(per_group * n_groups), 32 * launch_warps, smem_pipe, s>>>(
+        parts_dev, n_parts, n_groups, nw, desc, n_loc, normalize, scores, n_fields);
+    return cudaGetLastError();
+  }
   const int dp = (dim + 31) & ~31;
   const size_t smem = (size_t)kLoc * dp * sizeof(float);
   if (smem > 227 * 1024) return cudaErrorInvalidValue;

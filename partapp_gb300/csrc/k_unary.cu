@@ -91,6 +91,69 @@ __global__ void __launch_bounds__(kThreads) k_unary_bilinear(const UnaryMap *__r
   if (m.max_slot) block_max_commit(kmax, m.max_slot);
 }
 
+// TM_BILINEAR with axis-aligned Tig: per (map, band of rows) the column
+// table and the few grid rows the band reads are staged in shared memory.
+__global__ void __launch_bounds__(kThreads) k_unary_bilinear_sep(const UnaryMap *__restrict__ maps,
+                                                                 int ny, int nx, int H, int W,
+                                                                 int rows_per_cta) {
+  extern __shared__ __align__(16) float sm[];
+  const UnaryMap &mg = maps[blockIdx.x];
+  const float *grid = mg.grid;
+  float *out = mg.out;
+  const int *colx = mg.colx, *rowy = mg.rowy;
+  const float *cola = mg.cola, *rowb = mg.rowb;
+  const int masked_all = mg.masked_all, strip = mg.strip;
+  int *max_slot = mg.max_slot;
+  const int y0 = blockIdx.y * rows_per_cta;
+  const int y1e = min(H, y0 + rows_per_cta);
+  const float eps10 = 10.0f * 1.1920928955078125e-07f;  // 10 * FLT_EPSILON
+  int *sx = reinterpret_cast<int *>(sm);          // [W] ix1
+  float *sa = sm + W;                             // [W] a
+  float *sg = sm + 2 * W;                         // [nrows][nx] grid rows
+  // grid rows read by this band: [rlo, rhi] (rows are monotone in y3)
+  int rlo = rowy[y0], rhi = rowy[y1e - 1];
+  if (rlo > rhi) { const int t = rlo; rlo = rhi; rhi = t; }
+  rlo = max(rlo, 0);
+  rhi = min(rhi + 1, ny - 1);
+  const int nrows = rhi >= rlo ? rhi - rlo + 1 : 0;
+  for (int i = threadIdx.x; i < W; i += blockDim.x) {
+    sx[i] = colx[i];
+    sa[i] = cola[i];
+  }
+  for (int i = threadIdx.x; i < nrows * nx; i += blockDim.x) sg[i] = __ldg(grid + (int64_t)rlo * nx + i);
+  __syncthreads();
+  int kmax = kFkeyNegInf;
+  for (int y3 = y0; y3 < y1e; ++y3) {
+    const int iy1 = rowy[y3];
+    const float b = rowb[y3];
+    const bool yin = (iy1 >= 0 && iy1 < ny);
+    for (int x3 = threadIdx.x; x3 < W; x3 += blockDim.x) {
+      float v = kNoClassValue;
+      const int ix1 = sx[x3];
+      const float a = sa[x3];
+      if (yin && ix1 >= 0 && ix1 < nx) {
+        const float *g0 = sg + (iy1 - rlo) * nx + ix1;
+        if (a < eps10 && b < eps10) {
+          v = g0[0];
+        } else if (ix1 < nx - 1 && iy1 < ny - 1) {
+          const float *g1 = g0 + nx;
+          const float omb = __fsub_rn(1.0f, b), oma = __fsub_rn(1.0f, a);
+          const float t0 = __fmul_rn(__fmul_rn(omb, oma), g0[0]);
+          const float t1 = __fmul_rn(__fmul_rn(omb, a), g0[1]);
+          const float t2 = __fmul_rn(__fmul_rn(b, oma), g1[0]);
+          const float t3 = __fmul_rn(__fmul_rn(b, a), g1[1]);
+          v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+        }
+      }
+      float o = clip_log(v);
+      if (masked_all || (strip > 0 && (x3 < strip || x3 >= W - strip))) o = kLogZero;
+      out[(int64_t)y3 * W + x3] = o;
+      kmax = max(kmax, key_of(o));
+    }
+  }
+  if (max_slot) block_max_commit(kmax, max_slot);
+}
+
 // TM_DIRECT, pass 1: every pixel starts at NO_CLASS_VALUE -> LOG_ZERO.
 __global__ void __launch_bounds__(kThreads) k_unary_direct_fill(const UnaryMap *__restrict__ maps,
                                                                 int H, int W, int rows_per_cta) {
@@ -173,11 +236,19 @@ __global__ void k_fill_int(int *p, int v, int64_t n) {
 }  // namespace
 
 cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, int H, int W,
-                              int direct, cudaStream_t s) {
+                              int direct, int separable, cudaStream_t s) {
   const int rows = 16;
   dim3 grid((unsigned)n_maps, (unsigned)((H + rows - 1) / rows));
   if (!direct) {
-    k_unary_bilinear<<<grid, kThreads, 0, s>>>(maps, ny, nx, H, W, rows);
+    // rows of the grid one band reads: at most rows * |dy1/dy3| + 2
+    const size_t smem = (size_t)(2 * W + (size_t)(rows + 2) * nx) * sizeof(float);
+    if (separable && smem <= 96 * 1024) {
+      cudaFuncSetAttribute(k_unary_bilinear_sep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      k_unary_bilinear_sep<<<grid, kThreads, smem, s>>>(maps, ny, nx, H, W, rows);
+    } else {
+      k_unary_bilinear<<<grid, kThreads, 0, s>>>(maps, ny, nx, H, W, rows);
+    }
   } else {
     k_unary_direct_fill<<<grid, kThreads, 0, s>>>(maps, H, W, rows);
     k_unary_direct_scatter<<<(unsigned)n_maps, kThreads, 0, s>>>(maps, ny, nx, H, W);

@@ -10,6 +10,7 @@
 // off so the host rounds exactly as the reference did.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -27,7 +28,8 @@ struct pa_classifier {
   int dim = 0;
   int n = 0;
   float sum_alpha = 0.f;
-  float4 *d = nullptr;
+  float4 *d = nullptr;     // {f, p, theta*p, alpha}
+  float4 *fast = nullptr;  // {f, t, p*alpha, 0}, only when every p is +1 or -1
 };
 
 struct pa_ctx {
@@ -40,6 +42,21 @@ struct pa_ctx {
   size_t arena_cap = 0;
   char *pinned = nullptr;
   size_t pinned_cap = 0;
+  // per-kernel device timing (CUDA events around each launch)
+  bool timing = false;
+  struct Pending {
+    const char *name;
+    cudaEvent_t a, b;
+    int n;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  struct Acc {
+    double ms = 0;
+    uint64_t n = 0;
+  };
+  std::map<std::string, Acc> times;
+  std::vector<std::string> names;  // stable storage for pa_ctx_timing_get
 };
 
 namespace {
@@ -61,11 +78,58 @@ pa_status fail(pa_ctx *ctx, pa_status st, const char *fmt, ...) {
       return fail(ctx, PA_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));        \
   } while (0)
 
-#define PA_LAUNCH(call)    \
-  do {                     \
-    PA_CK(call);           \
-    ++ctx->launches;       \
+// Launches `nk` kernels through `call`, timed when the context records
+// timing.  Every launch is counted in pa_ctx_kernel_launches.
+#define PA_LAUNCH_N(name, nk, call)                                \
+  do {                                                             \
+    cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;                  \
+    if (ctx->timing) {                                             \
+      ev_a_ = take_event(ctx);                                     \
+      ev_b_ = take_event(ctx);                                     \
+      cudaEventRecord(ev_a_, ctx->stream);                         \
+    }                                                              \
+    PA_CK(call);                                                   \
+    if (ctx->timing) {                                             \
+      cudaEventRecord(ev_b_, ctx->stream);                         \
+      ctx->pending.push_back({name, ev_a_, ev_b_, (nk)});          \
+    }                                                              \
+    ctx->launches += (nk);                                         \
   } while (0)
+#define PA_LAUNCH(name, call) PA_LAUNCH_N(name, 1, call)
+
+cudaEvent_t take_event(pa_ctx *ctx) {
+  if (!ctx->pool.empty()) {
+    cudaEvent_t e = ctx->pool.back();
+    ctx->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Called after the stream has been synchronised.
+void resolve_timing(pa_ctx *ctx) {
+  for (auto &p : ctx->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      auto &acc = ctx->times[p.name];
+      acc.ms += ms;
+      acc.n += (uint64_t)p.n;
+    } else {
+      cudaGetLastError();
+    }
+    ctx->pool.push_back(p.a);
+    ctx->pool.push_back(p.b);
+  }
+  ctx->pending.clear();
+}
+
+pa_status sync_ctx(pa_ctx *ctx) {
+  PA_CK(cudaStreamSynchronize(ctx->stream));
+  resolve_timing(ctx);
+  return PA_OK;
+}
 
 struct DeviceGuard {
   int prev = -1;
@@ -107,7 +171,10 @@ struct Builder {
     scratch_off = o + n * sizeof(T);
     return dry ? nullptr : reinterpret_cast<T *>(base + al(blob_size, 256) + o);
   }
-  size_t total() const { return al(blob_size, 256) + al(scratch_off, 256) + 256; }
+  // Pass 1 measures the blob as it grows; pass 2 places scratch after the
+  // blob size measured in pass 1.  Both must agree on where scratch starts.
+  size_t blob_region() const { return al(dry ? blob.size() : blob_size, 256); }
+  size_t total() const { return blob_region() + al(scratch_off, 256) + 256; }
 };
 
 pa_status ensure_arena(pa_ctx *ctx, size_t bytes) {
@@ -127,6 +194,10 @@ pa_status ensure_arena(pa_ctx *ctx, size_t bytes) {
 }
 
 pa_status upload_blob(pa_ctx *ctx, const Builder &b) {
+  // every pointer the plan hands to a kernel lies inside the arena
+  if (b.dry || b.blob.size() > b.blob_size ||
+      b.blob_region() + Builder::al(b.scratch_off, 256) > ctx->arena_cap)
+    return fail(ctx, PA_ERR_INVALID, "internal: plan does not fit the workspace");
   if (b.blob.empty()) return PA_OK;
   if (ctx->pinned_cap < b.blob.size()) {
     PA_CK(cudaStreamSynchronize(ctx->stream));
@@ -638,36 +709,36 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
   if (e->use_pairwise) {
     if (pl.n_msgs_total > 0)
-      PA_LAUNCH(launch_shift_tables(pl.shifts, pl.n_msgs_total, R, H, W, pl.tables, st));
+      PA_LAUNCH("shift_tables", launch_shift_tables(pl.shifts, pl.n_msgs_total, R, H, W, pl.tables, st));
     for (auto &ph : pl.up) {
       if (!ph.n) continue;
-      PA_LAUNCH(launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
-      PA_LAUNCH(launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+      PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
+      PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
     }
-    PA_LAUNCH(launch_root_combine(pl.roots, B, pl.N, st));
+    PA_LAUNCH("root_combine", launch_root_combine(pl.roots, B, pl.N, st));
     for (auto &ph : pl.down) {
       if (!ph.n) continue;
-      PA_LAUNCH(launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
-      PA_LAUNCH(launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+      PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
+      PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
     }
-    PA_LAUNCH(launch_root_posterior(pl.post_root_ptrs, pl.root_post_ptrs, pl.keep, pl.n_keep, B,
+    PA_LAUNCH("root_posterior", launch_root_posterior(pl.post_root_ptrs, pl.root_post_ptrs, pl.keep, pl.n_keep, B,
                                     R, H, W, st));
     // leaves without a downward message (a root without children) keep the
     // upward belief; their argmax comes from the combine kernel (root) only.
   } else {
-    PA_LAUNCH(launch_argmax(pl.marg_ptrs, B * P, pl.N, pl.amax, st));
+    PA_LAUNCH("argmax", launch_argmax(pl.marg_ptrs, B * P, pl.N, pl.amax, st));
   }
-  PA_LAUNCH(launch_log_z(pl.marg_ptrs, pl.amax, B * P, pl.N, pl.logz_part, pl.logz, st));
+  PA_LAUNCH_N("log_z", 2, launch_log_z(pl.marg_ptrs, pl.amax, B * P, pl.N, pl.logz_part, pl.logz, st));
   return PA_OK;
 }
 
 pa_status init_slots(pa_ctx *ctx, PsPlan &pl) {
   cudaStream_t st = ctx->stream;
   const int n = pl.B * pl.P;
-  PA_LAUNCH(launch_fill_int(pl.umax, kFkeyNegInf, n, st));
-  PA_LAUNCH(launch_fill_int(pl.pmax, kFkeyNegInf, n, st));
-  PA_LAUNCH(launch_fill_int(pl.frmax, kFkeyNegInf, n, st));
-  PA_LAUNCH(launch_fill_int(pl.tmax, kFkeyNegInf, n, st));
+  PA_LAUNCH("fill", launch_fill_int(pl.umax, kFkeyNegInf, n, st));
+  PA_LAUNCH("fill", launch_fill_int(pl.pmax, kFkeyNegInf, n, st));
+  PA_LAUNCH("fill", launch_fill_int(pl.frmax, kFkeyNegInf, n, st));
+  PA_LAUNCH("fill", launch_fill_int(pl.tmax, kFkeyNegInf, n, st));
   PA_CK(cudaMemsetAsync(pl.amax, 0, sizeof(unsigned long long) * n, st));
   PA_CK(cudaMemsetAsync(pl.err, 0, sizeof(int), st));
   return PA_OK;
@@ -712,7 +783,10 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
                               cudaMemcpyDeviceToHost, st));
     }
   }
-  PA_CK(cudaStreamSynchronize(st));
+  {
+    pa_status ss = sync_ctx(ctx);
+    if (ss) return ss;
+  }
   for (int i = 0; i < B; ++i) {
     const pa_ps_outputs &o = outs[i];
     for (int p = 0; p < P; ++p) {
@@ -796,7 +870,8 @@ pa_status plan_unary(pa_ctx *ctx, Builder &b, const double *Tig, int tig_shared,
                      int R, int ny, int nx, int H, int W, int direct, const float *scores,
                      int64_t scores_field_stride, const std::vector<std::vector<float *>> &outs,
                      const std::vector<int> &upright, int root, float strip_frac, int *umax,
-                     const pa_exp_param *e, UnaryMap **maps_dev, int apply_masks) {
+                     const pa_exp_param *e, UnaryMap **maps_dev, int apply_masks,
+                     int *all_separable) {
   const int n_tig = tig_shared ? 1 : P * R;
   std::vector<UnaryTables> tabs(n_tig);
   std::vector<const int *> dcolx(n_tig), drowy(n_tig);
@@ -814,6 +889,9 @@ pa_status plan_unary(pa_ctx *ctx, Builder &b, const double *Tig, int tig_shared,
     }
   }
   const int strip = (int)(strip_frac * W);
+  *all_separable = 1;
+  for (int k = 0; k < n_tig; ++k)
+    if (!tabs[k].separable || std::fabs(tabs[k].T13[4]) > 1.0) *all_separable = 0;
   std::vector<UnaryMap> maps((size_t)n_img * P * R);
   for (int i = 0; i < n_img; ++i)
     for (int p = 0; p < P; ++p)
@@ -855,8 +933,20 @@ pa_status check_classifiers(pa_ctx *ctx, const pa_classifier *const *cls, int n_
 
 StumpPart *plan_stumps(Builder &b, const pa_classifier *const *cls, int n_parts) {
   std::vector<StumpPart> sp(n_parts);
-  for (int p = 0; p < n_parts; ++p) sp[p] = {cls[p]->d, cls[p]->n, cls[p]->sum_alpha};
+  for (int p = 0; p < n_parts; ++p) sp[p] = {cls[p]->d, cls[p]->fast, cls[p]->n, cls[p]->sum_alpha};
   return b.param(sp.data(), sp.size());
+}
+
+std::vector<char> fast_flags(const pa_classifier *const *cls, int n) {
+  std::vector<char> f(n);
+  for (int p = 0; p < n; ++p) f[p] = cls[p]->fast != nullptr;
+  return f;
+}
+
+std::vector<int> stump_counts(const pa_classifier *const *cls, int n) {
+  std::vector<int> c(n);
+  for (int p = 0; p < n; ++p) c[p] = cls[p]->n;
+  return c;
 }
 
 // The whole --find_obj pipeline for n_img images.
@@ -911,10 +1001,11 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   plan_ps(b1, pl, e, joints, marg_out.data(), rp_out.data());
   plan_marg_ptrs(b1, pl);
   UnaryMap *umaps = nullptr;
+  int usep = 0;
   std::vector<std::vector<float *>> uouts(n_img, std::vector<float *>(P, nullptr));
   st = plan_unary(ctx, b1, Tig, tig_shared, n_img, P, R, ny, nx, H, W, !e->interpolate, scores,
                   n_fields, uouts, pl.sc.upright, pl.sc.root, e->strip_border_detections,
-                  pl.umax, e, &umaps, 1);
+                  pl.umax, e, &umaps, 1, &usep);
   if (st) return st;
   // pass 2: real
   Builder b;
@@ -933,7 +1024,7 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
     for (int p = 0; p < P; ++p) uouts[i][p] = pl2.im[i].U[p];
   st = plan_unary(ctx, b, Tig, tig_shared, n_img, P, R, ny, nx, H, W, !e->interpolate, scores,
                   n_fields, uouts, pl2.sc.upright, pl2.sc.root, e->strip_border_detections,
-                  pl2.umax, e, &umaps, 1);
+                  pl2.umax, e, &umaps, 1, &usep);
   if (st) return st;
   if (b.blob.size() != b1.blob.size() || b.scratch_off != b1.scratch_off)
     return fail(ctx, PA_ERR_INVALID, "internal: plan size mismatch");
@@ -947,11 +1038,14 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   st = init_slots(ctx, pl2);
   if (st) return st;
   cudaStream_t s = ctx->stream;
-  PA_LAUNCH(launch_score_grids(sp, n_cls, desc_dev, G, (int)n_fields, dim, 1, scores, s));
+  const std::vector<char> ff = fast_flags(cls, n_cls);
+  const std::vector<int> ns = stump_counts(cls, n_cls);
+  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_cls, desc_dev, G,
+                                              (int)n_fields, dim, 1, scores, s));
   if (scores_out && mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores_out, scores, (size_t)n_cls * n_fields * G * sizeof(float),
                           cudaMemcpyDeviceToHost, s));
-  PA_LAUNCH(launch_unary_maps(umaps, n_img * P * R, ny, nx, H, W, !e->interpolate, s));
+  PA_LAUNCH_N("unary_maps", e->interpolate ? 1 : 2, launch_unary_maps(umaps, n_img * P * R, ny, nx, H, W, !e->interpolate, usep, s));
   if (!e->use_pairwise) {
     // getMaxStates: the marginals are the masked unaries
     for (int i = 0; i < n_img; ++i)
@@ -1021,6 +1115,8 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) {
   {
     DeviceGuard dg(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    resolve_timing(ctx);
+    for (cudaEvent_t e : ctx->pool) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1050,21 +1146,65 @@ const char *pa_last_error(const pa_ctx *ctx) { return ctx ? ctx->err.c_str() : "
 
 uint64_t pa_ctx_kernel_launches(const pa_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+pa_status pa_ctx_enable_timing(pa_ctx *ctx, int on) {
+  if (!ctx) return PA_ERR_INVALID;
+  DeviceGuard dg(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  resolve_timing(ctx);
+  ctx->timing = on != 0;
+  return PA_OK;
+}
+
+pa_status pa_ctx_timing_reset(pa_ctx *ctx) {
+  if (!ctx) return PA_ERR_INVALID;
+  DeviceGuard dg(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  resolve_timing(ctx);
+  ctx->times.clear();
+  return PA_OK;
+}
+
+int pa_ctx_timing_count(pa_ctx *ctx) {
+  if (!ctx) return 0;
+  ctx->names.clear();
+  for (auto &kv : ctx->times) ctx->names.push_back(kv.first);
+  return (int)ctx->names.size();
+}
+
+pa_status pa_ctx_timing_get(pa_ctx *ctx, int i, const char **name, double *total_ms,
+                            uint64_t *launches) {
+  if (!ctx || i < 0 || i >= (int)ctx->names.size()) return PA_ERR_INVALID;
+  const auto &acc = ctx->times[ctx->names[i]];
+  if (name) *name = ctx->names[i].c_str();
+  if (total_ms) *total_ms = acc.ms;
+  if (launches) *launches = acc.n;
+  return PA_OK;
+}
+
 pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int n_stumps,
                                pa_classifier **out) {
   if (!ctx || !out) return PA_ERR_INVALID;
   *out = nullptr;
   if (dim < 1 || n_stumps < 1 || !stumps)
     return fail(ctx, PA_ERR_INVALID, "classifier needs dim >= 1 and stumps");
-  std::vector<float4> host(n_stumps);
+  std::vector<float4> host(n_stumps), fast(n_stumps);
   float sum_alpha = 0.f;  // operator>>, AdaBoost.cc:327-331
+  bool unit_polarity = true;
   for (int i = 0; i < n_stumps; ++i) {
     if (stumps[i].f < 0 || stumps[i].f >= dim)
       return fail(ctx, PA_ERR_INVALID, "stump %d: feature %d outside [0,%d)", i, stumps[i].f, dim);
     float fbits;
     std::memcpy(&fbits, &stumps[i].f, 4);
-    host[i] = make_float4(fbits, stumps[i].p, stumps[i].theta, stumps[i].alpha);
-    sum_alpha += stumps[i].alpha;
+    const float p = stumps[i].p, th = stumps[i].theta, a = stumps[i].alpha;
+    // theta * p is the right-hand side of the stump test (AdaBoost.h:156);
+    // the device compares v * p against this same float product.
+    host[i] = make_float4(fbits, p, th * p, a);
+    // p = +1: v < theta; p = -1: v > theta == !(v < nextafter(theta, +inf))
+    if (std::isnan(th)) unit_polarity = false;
+    else if (p == 1.0f) fast[i] = make_float4(fbits, th, a, 0.f);
+    else if (p == -1.0f) fast[i] = make_float4(fbits, std::nextafter(th, INFINITY), -a, 0.f);
+    else unit_polarity = false;
+    sum_alpha += a;
   }
   DeviceGuard dg(ctx->device);
   std::unique_ptr<pa_classifier> c(new pa_classifier);
@@ -1076,6 +1216,14 @@ pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int
     return fail(ctx, PA_ERR_NOMEM, "cannot allocate stump table");
   }
   PA_CK(cudaMemcpy(c->d, host.data(), sizeof(float4) * n_stumps, cudaMemcpyHostToDevice));
+  if (unit_polarity) {
+    if (cudaMalloc(&c->fast, sizeof(float4) * n_stumps) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(c->d);
+      return fail(ctx, PA_ERR_NOMEM, "cannot allocate stump table");
+    }
+    PA_CK(cudaMemcpy(c->fast, fast.data(), sizeof(float4) * n_stumps, cudaMemcpyHostToDevice));
+  }
   *out = c.release();
   return PA_OK;
 }
@@ -1113,8 +1261,10 @@ pa_status pa_classifier_destroy(pa_ctx *ctx, pa_classifier *cls) {
   if (ctx) {
     DeviceGuard dg(ctx->device);
     cudaFree(cls->d);
+    if (cls->fast) cudaFree(cls->fast);
   } else {
     cudaFree(cls->d);
+    if (cls->fast) cudaFree(cls->fast);
   }
   delete cls;
   return PA_OK;
@@ -1165,11 +1315,13 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
     st = copy_in(ctx, (void *)d_in, desc, din * sizeof(float), mem);
     if (st) return st;
   }
-  PA_LAUNCH(launch_score_grids(sp, n_parts, d_in, G, n_fields, dim, normalize, d_out, ctx->stream));
+  const std::vector<char> ff = fast_flags(cls, n_parts);
+  const std::vector<int> ns = stump_counts(cls, n_parts);
+  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, d_in, G,
+                                              n_fields, dim, normalize, d_out, ctx->stream));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-  PA_CK(cudaStreamSynchronize(ctx->stream));
-  return PA_OK;
+  return sync_ctx(ctx);
 }
 
 pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
@@ -1221,14 +1373,16 @@ pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, in
     if ((st = copy_in(ctx, (void *)d_valid, valid, nval, mem))) return st;
   }
   cudaStream_t s = ctx->stream;
-  PA_LAUNCH(launch_window_gather(d_cells, d_valid, n_fields, ny, nx, dc, gx, gy, grid_step, dense,
+  PA_LAUNCH("window_gather", launch_window_gather(d_cells, d_valid, n_fields, ny, nx, dc, gx, gy, grid_step, dense,
                                  ok, s));
-  PA_LAUNCH(launch_score_grids(sp, n_parts, dense, G, n_fields, D, normalize, d_out, s));
-  PA_LAUNCH(launch_mask_no_class(d_out, ok, n_parts, (int64_t)n_fields * G, s));
+  const std::vector<char> ff = fast_flags(cls, n_parts);
+  const std::vector<int> ns = stump_counts(cls, n_parts);
+  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, dense, G,
+                                              n_fields, D, normalize, d_out, s));
+  PA_LAUNCH("mask_no_class", launch_mask_no_class(d_out, ok, n_parts, (int64_t)n_fields * G, s));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, s));
-  PA_CK(cudaStreamSynchronize(s));
-  return PA_OK;
+  return sync_ctx(ctx);
 }
 
 pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, int ny, int nx,
@@ -1253,8 +1407,9 @@ pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, in
     b1.scratch<float>(nin);
     b1.scratch<float>(nout);
   }
+  int usep = 0;
   pa_status st = plan_unary(ctx, b1, Tig, tig_shared, 1, n_parts, R, ny, nx, H, W, !interpolate,
-                            d_in, R, outs, upright, 0, 0.f, nullptr, &e, &maps, 0);
+                            d_in, R, outs, upright, 0, 0.f, nullptr, &e, &maps, 0, &usep);
   if (st) return st;
   Builder b;
   b.dry = false;
@@ -1267,17 +1422,16 @@ pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, in
   }
   for (int p = 0; p < n_parts; ++p) outs[0][p] = d_out + (size_t)p * R * H * W;
   st = plan_unary(ctx, b, Tig, tig_shared, 1, n_parts, R, ny, nx, H, W, !interpolate, d_in, R,
-                  outs, upright, 0, 0.f, nullptr, &e, &maps, 0);
+                  outs, upright, 0, 0.f, nullptr, &e, &maps, 0, &usep);
   if (st) return st;
   if ((st = upload_blob(ctx, b))) return st;
   if (mem == PA_MEM_HOST)
     if ((st = copy_in(ctx, (void *)d_in, scores, nin * sizeof(float), mem))) return st;
-  PA_LAUNCH(launch_unary_maps(maps, n_parts * R, ny, nx, H, W, !interpolate, ctx->stream));
+  PA_LAUNCH_N("unary_maps", interpolate ? 1 : 2, launch_unary_maps(maps, n_parts * R, ny, nx, H, W, !interpolate, usep, ctx->stream));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(log_unary, d_out, nout * sizeof(float), cudaMemcpyDeviceToHost,
                           ctx->stream));
-  PA_CK(cudaStreamSynchronize(ctx->stream));
-  return PA_OK;
+  return sync_ctx(ctx);
 }
 
 pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
@@ -1332,7 +1486,7 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
   const int strip = (int)(ep->strip_border_detections * W);
   for (int p = 0; p < P; ++p) {
     float *dst = ep->use_pairwise ? pl2.im[0].U[p] : pl2.im[0].MARG[p];
-    PA_LAUNCH(launch_prepare_unary(ud + (size_t)p * pl.N, dst, pl2.sc.upright[p] ? mk + (size_t)p * R : nullptr,
+    PA_LAUNCH("prepare_unary", launch_prepare_unary(ud + (size_t)p * pl.N, dst, pl2.sc.upright[p] ? mk + (size_t)p * R : nullptr,
                                    p == pl2.sc.root ? strip : 0, R, H, W, pl2.umax + p, s));
   }
   if ((st = run_ps(ctx, ep, pl2))) return st;
@@ -1403,17 +1557,17 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
   cudaStream_t s = ctx->stream;
   if (mem == PA_MEM_HOST)
     if ((st = copy_in(ctx, (void *)din, child, N * sizeof(float), mem))) return st;
-  PA_LAUNCH(launch_fill_int(slot, kFkeyNegInf, 1, s));
+  PA_LAUNCH("fill", launch_fill_int(slot, kFkeyNegInf, 1, s));
   PA_CK(cudaMemsetAsync(err, 0, sizeof(int), s));
-  PA_LAUNCH(launch_map_max(din, N, slot, s));
-  PA_LAUNCH(launch_shift_tables(shifts, 1, R, H, W, tables, s));
-  PA_LAUNCH(launch_msg_rows(md, 1, R, H, W, (mp.xlen - 1) / 2, err, s));
-  PA_LAUNCH(launch_msg_cols(md, 1, R, H, W, (mp.ylen - 1) / 2, err, s));
+  PA_LAUNCH("map_max", launch_map_max(din, N, slot, s));
+  PA_LAUNCH("shift_tables", launch_shift_tables(shifts, 1, R, H, W, tables, s));
+  PA_LAUNCH("msg_rows", launch_msg_rows(md, 1, R, H, W, (mp.xlen - 1) / 2, err, s));
+  PA_LAUNCH("msg_cols", launch_msg_cols(md, 1, R, H, W, (mp.ylen - 1) / 2, err, s));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(parent, dout, N * sizeof(float), cudaMemcpyDeviceToHost, s));
   int errflag = 0;
   PA_CK(cudaMemcpyAsync(&errflag, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  PA_CK(cudaStreamSynchronize(s));
+  if (pa_status ss = sync_ctx(ctx)) return ss;
   if (errflag & 1)
     return fail(ctx, PA_ERR_NUMERIC, "exp() overflowed in the message (the reference asserts here)");
   if (errflag) return fail(ctx, PA_ERR_UNSUPPORTED, "message kernel rejected its input (code %d)", errflag);

@@ -55,7 +55,8 @@ __host__ __device__ inline unsigned long long akey(float v, uint32_t flat) {
 // plus the per-classifier metadata used by the score-grid kernel.
 // ---------------------------------------------------------------------------
 struct StumpPart {
-  const float4 *stumps;  // .x = f (int bits), .y = p, .z = theta, .w = alpha
+  const float4 *stumps;  // .x = f (int bits), .y = p, .z = theta * p, .w = alpha
+  const float4 *fast;    // .x = f (int bits), .y = t, .z = p * alpha (p = +-1 only)
   int n;
   float sum_alpha;
 };
@@ -125,7 +126,9 @@ struct RootDesc {
 };
 
 // Kernel launchers (defined in the .cu files).  All return cudaGetLastError().
-cudaError_t launch_score_grids(const StumpPart *parts_dev, int n_parts, const float *desc,
+// fast_ok[p] / n_stumps[p] are host arrays describing the classifiers.
+cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
+                               const int *n_stumps, int n_parts, const float *desc,
                                int64_t n_loc_per_field, int n_fields, int dim, int normalize,
                                float *scores, cudaStream_t s);
 cudaError_t launch_window_gather(const float *cells, const uint8_t *valid, int n_fields, int ny,
@@ -133,8 +136,10 @@ cudaError_t launch_window_gather(const float *cells, const uint8_t *valid, int n
                                  uint8_t *ok, cudaStream_t s);
 cudaError_t launch_mask_no_class(float *scores, const uint8_t *ok, int n_parts, int64_t n_per_part,
                                  cudaStream_t s);
+// separable != 0 promises every map uses the column/row tables and that a
+// band of 16 image rows reads at most 18 grid rows (|Tig y scale| >= 1).
 cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, int H, int W,
-                              int direct, cudaStream_t s);
+                              int direct, int separable, cudaStream_t s);
 cudaError_t launch_prepare_unary(const float *in, float *out, const int *masked_rot, int strip,
                                  int R, int H, int W, int *max_slot, cudaStream_t s);
 cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,

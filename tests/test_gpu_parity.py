@@ -81,6 +81,29 @@ def test_score_grids_bit_exact(ctx, orc):
         assert cls[p].info()[2] == orc.sum_alpha(m["alpha"][p])
 
 
+@pytest.mark.parametrize("polarity,n_parts", [("unit", 22), ("unit", 13), ("unit", 10),
+                                              ("general", 22)])
+def test_score_grids_960_pipelined_bit_exact(ctx, orc, polarity, n_parts):
+    """The 960-dim path (staged tiles, sign-folded stump test) on a ragged
+    tile count, 22 classifiers and planted v == theta ties; a classifier with
+    a non-unit polarity exercises the literal v*p < theta*p form."""
+    rng = np.random.default_rng(9)
+    R, ny, nx, D = 2, 7, 33, 960
+    desc = synth.make_descriptors(rng, R, ny, nx, D)
+    m = synth.make_models(rng, n_parts=n_parts, n_stumps=120, D=D)
+    for p in range(n_parts):
+        for i in range(0, 120, 5):
+            m["theta"][p, i] = desc[i % R, (i // 3) % ny, i % nx, m["f"][p, i]]
+    if polarity == "general":
+        m["p"][3, ::7] = 0.5
+        m["p"][4, ::9] = -2.0
+    cls = ctx.classifiers(m)
+    got = ctx.score_grids(cls, desc)
+    for p in range(n_parts):
+        want = orc.adaboost_eval(m["f"][p], m["p"][p], m["theta"][p], m["alpha"][p], desc)
+        assert np.array_equal(got[p], want), f"part {p}"
+
+
 def test_classifier_text_format(ctx, orc):
     text = "4\n3\t\n0\t1\t0.5\t0.1\t0.25\t\n2\t-1\t0.75\t0.2\t0.6\t\n3\t1\t0.125\t0.3\t0.9\t\n"
     from partapp_gb300 import Classifier
