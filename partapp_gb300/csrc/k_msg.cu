@@ -36,6 +36,20 @@ constexpr int kCW = 33;   // staged source columns (one spare for rounding glitc
 
 __device__ __forceinline__ int wrap(int r, int R) { return r < 0 ? r + R : (r >= R ? r - R : r); }
 
+// Source index of a nearest-neighbour shift: a row of the exact table,
+// summarised by {c, lo, hi, uniform} when it is the plain shift
+// pos -> pos + c on [lo, hi) and -1 elsewhere (always, unless x + t lands
+// within an ulp of a half-integer).
+__device__ __forceinline__ int shift_src(int4 d, const int16_t *tab, int pos) {
+  if (d.w) return (pos >= d.y && pos < d.z) ? pos + d.x : -1;
+  return tab[pos];
+}
+
+// log of a filtered value: LOG_ZERO for 0 (computeLogGrid).  The accurate
+// logf/expf are kept: the approximate intrinsics move near-tied maxima of
+// the marginals enough to change the argmax.
+__device__ __forceinline__ float log_or_zero(float f) { return f == 0.f ? kLogZero : logf(f); }
+
 // ---------------------------------------------------------------------------
 // Rotation filter on one column held in registers: out[r] = sum_j t[j] *
 // e[(r - NR + j) mod R] (grid_filter_1d_blas_wraparound,
@@ -109,6 +123,9 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 3) k_msg_rows(con
     const int r = idx / (padx + pad_r), k = idx - r * (padx + pad_r);
     E[r * WP + (k < padx ? k : padx + W + (k - padx))] = 0.f;
   }
+  int4 *sdesc = reinterpret_cast<int4 *>(tr + kMaxRot + (RT == 0 ? kThreadsRows * R : 0));
+  for (int i = tid; i < 2 * R; i += blockDim.x) sdesc[i] = md.sdesc[i];  // in_x[R], in_y[R]
+  __syncthreads();
   {
     // four independent gathers in flight per thread
     constexpr int U = 4;
@@ -124,8 +141,8 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 3) k_msg_rows(con
         if (idx < n) {
           const int r = idx / W, x = idx - r * W;
           dst[u] = r * WP + padx + x;
-          const int sy = md.ty_in[r * H + y];
-          const int sx = md.tx_in[r * W + x];
+          const int sy = shift_src(sdesc[R + r], md.ty_in + r * H, y);
+          const int sx = shift_src(sdesc[r], md.tx_in + r * W, x);
           if (sy >= 0 && sx >= 0) lv[u] = __ldg(md.in + (int64_t)(r - md.kidx) * HW + sy * W + sx);
         }
       }
@@ -241,18 +258,27 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
 
   const int16_t *txo = md.tx_out + r * W;
   const int16_t *tyo = md.ty_out + r * H;
+  const int4 dxo = md.sdesc[2 * R + r], dyo = md.sdesc[3 * R + r];
   if (tid == 0) {
     lim[0] = 1 << 30; lim[1] = -1; lim[2] = 1 << 30; lim[3] = -1;
+    if (dxo.w) {
+      const int a = max(x0, dxo.y), b = min(x1, dxo.z);
+      if (a < b) { lim[0] = a + dxo.x; lim[1] = b - 1 + dxo.x; }
+    }
+    if (dyo.w) {
+      const int a = max(y0, dyo.y), b = min(y1, dyo.z);
+      if (a < b) { lim[2] = a + dyo.x; lim[3] = b - 1 + dyo.x; }
+    }
   }
   __syncthreads();
-  {
+  if (!dxo.w || !dyo.w) {
     int cmn = 1 << 30, cmx = -1, rmn = 1 << 30, rmx = -1;
     for (int i = tid; i < (x1 - x0) + (y1 - y0); i += blockDim.x) {
       if (i < x1 - x0) {
-        const int c = txo[x0 + i];
+        const int c = dxo.w ? -1 : txo[x0 + i];
         if (c >= 0) { cmn = min(cmn, c); cmx = max(cmx, c); }
       } else {
-        const int rr = tyo[y0 + i - (x1 - x0)];
+        const int rr = dyo.w ? -1 : tyo[y0 + i - (x1 - x0)];
         if (rr >= 0) { rmn = min(rmn, rr); rmx = max(rmx, rr); }
       }
     }
@@ -261,8 +287,8 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
     rmn = __reduce_min_sync(0xFFFFFFFFu, rmn);
     rmx = __reduce_max_sync(0xFFFFFFFFu, rmx);
     if ((tid & 31) == 0) {
-      atomicMin(&lim[0], cmn); atomicMax(&lim[1], cmx);
-      atomicMin(&lim[2], rmn); atomicMax(&lim[3], rmx);
+      if (!dxo.w) { atomicMin(&lim[0], cmn); atomicMax(&lim[1], cmx); }
+      if (!dyo.w) { atomicMin(&lim[2], rmn); atomicMax(&lim[3], rmx); }
     }
   }
   __syncthreads();
@@ -366,10 +392,10 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
       a1[u] = 0.f;
       if (i < n_out) {
         const int yy = y0 + i / tw, xx = x0 + (i - (i / tw) * tw);
-        const int sy = tyo[yy], sx = txo[xx];
+        const int sy = shift_src(dyo, tyo, yy), sx = shift_src(dxo, txo, xx);
         if (sy >= 0 && sx >= 0) {
           const float f = F[(sy - rmin) * kCW + (sx - cmin)];
-          m[u] = __fadd_rn(f == 0.f ? kLogZero : logf(f), M);
+          m[u] = __fadd_rn(log_or_zero(f), M);
         }
         idx[u] = (int64_t)r * HW + (int64_t)yy * W + xx;
         if (mode != EPI_STORE) a0[u] = __ldg(src0 + idx[u]);
@@ -451,12 +477,40 @@ __global__ void k_shift_tables(const double *__restrict__ shifts, int R, int H, 
   }
 }
 
+// Summaries {c, lo, hi, uniform} of every table row.  sdesc[msg] =
+// [in_x[R] | in_y[R] | out_x[R] | out_y[R]].
+__global__ void k_shift_desc(const int16_t *__restrict__ tables, int n_msgs, int R, int H, int W,
+                             int4 *__restrict__ sdesc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_msgs * 4 * R) return;
+  const int msg = i / (4 * R), k = i - msg * 4 * R;
+  const int which = k / R, r = k - which * R;  // 0 in_x, 1 in_y, 2 out_x, 3 out_y
+  const int n = (which & 1) ? H : W;
+  const int16_t *tb = tables + (size_t)msg * 2 * R * (W + H) + (which >= 2 ? (size_t)R * (W + H) : 0) +
+                      ((which & 1) ? (size_t)R * W + (size_t)r * H : (size_t)r * W);
+  int lo = -1, hi = -1, c = 0;
+  bool uniform = true;
+  for (int p = 0; p < n; ++p) {
+    const int v = tb[p];
+    if (v >= 0) {
+      if (lo < 0) { lo = p; c = v - p; }
+      else if (hi >= 0 || v != p + c) uniform = false;  // a gap or a different shift
+    } else if (lo >= 0 && hi < 0) {
+      hi = p;
+    }
+  }
+  if (lo < 0) { lo = 0; hi = 0; }
+  else if (hi < 0) hi = n;
+  sdesc[i] = make_int4(c, lo, hi, uniform ? 1 : 0);
+}
+
 template <int RT>
 cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
                           int *err, cudaStream_t s) {
   const int WP = rows_stride(W, padx);
   size_t smem = ((size_t)align4(R * WP) + ((2 * padx + 1 + kU - 1) / kU) * kU + kMaxRot) * sizeof(float);
   if (RT == 0) smem += (size_t)kThreadsRows * R * sizeof(float);
+  smem += (size_t)2 * R * sizeof(int4);
   if (smem > 227 * 1024) return cudaErrorInvalidValue;
   cudaFuncSetAttribute(k_msg_rows<RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid((unsigned)H, (unsigned)n_msgs);
@@ -467,9 +521,10 @@ cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, 
 }  // namespace
 
 cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,
-                                int16_t *tables, cudaStream_t s) {
+                                int16_t *tables, int4 *sdesc, cudaStream_t s) {
   dim3 grid((unsigned)((2 * R * (W + H) + 255) / 256), (unsigned)n_msgs);
   k_shift_tables<<<grid, 256, 0, s>>>(shifts, R, H, W, tables);
+  k_shift_desc<<<(n_msgs * 4 * R + 127) / 128, 128, 0, s>>>(tables, n_msgs, R, H, W, sdesc);
   return cudaGetLastError();
 }
 

@@ -227,6 +227,14 @@ __global__ void __launch_bounds__(kThreads) k_map_max(const float *__restrict__ 
   block_max_commit(kmax, max_slot);
 }
 
+// Copies n 16-byte words; the source may be pinned host memory (unified
+// addressing), which keeps small uploads off the copy engines.
+__global__ void k_copy16(const int4 *__restrict__ src, int4 *__restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
 __global__ void k_fill_int(int *p, int v, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -269,6 +277,15 @@ cudaError_t launch_map_max(const float *x, int64_t N, int *max_slot, cudaStream_
   int blocks = (int)((N + kThreads - 1) / kThreads);
   if (blocks > 152 * 8) blocks = 152 * 8;
   k_map_max<<<blocks, kThreads, 0, s>>>(x, N, max_slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy16(const void *src, void *dst, int64_t n_words, cudaStream_t s) {
+  int blocks = (int)((n_words + 255) / 256);
+  if (blocks > 256) blocks = 256;
+  if (blocks < 1) blocks = 1;
+  k_copy16<<<blocks, 256, 0, s>>>(reinterpret_cast<const int4 *>(src), reinterpret_cast<int4 *>(dst),
+                                  n_words);
   return cudaGetLastError();
 }
 

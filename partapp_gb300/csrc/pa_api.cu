@@ -42,6 +42,12 @@ struct pa_ctx {
   size_t arena_cap = 0;
   char *pinned = nullptr;
   size_t pinned_cap = 0;
+  // host-input ring: descriptor slots filled on copy_stream while the main
+  // stream computes on the previous slot
+  cudaStream_t copy_stream = nullptr;
+  char *ring = nullptr;
+  size_t ring_cap = 0;
+  std::vector<cudaEvent_t> ring_ev;
   // per-kernel device timing (CUDA events around each launch)
   bool timing = false;
   struct Pending {
@@ -213,8 +219,10 @@ pa_status upload_blob(pa_ctx *ctx, const Builder &b) {
   }
   PA_CK(cudaStreamSynchronize(ctx->stream));  // staging buffer is reused
   std::memcpy(ctx->pinned, b.blob.data(), b.blob.size());
-  PA_CK(cudaMemcpyAsync(ctx->arena, ctx->pinned, b.blob.size(), cudaMemcpyHostToDevice,
-                        ctx->stream));
+  // a kernel reads the pinned staging buffer directly: the parameters do not
+  // queue behind large host->device copies on the copy engines
+  PA_LAUNCH("upload", launch_copy16(ctx->pinned, ctx->arena, (int64_t)((b.blob.size() + 15) / 16),
+                                    ctx->stream));
   return PA_OK;
 }
 
@@ -488,6 +496,7 @@ struct PsPlan {
   std::vector<Phase> up, down;
   RootDesc *roots = nullptr;
   int16_t *tables = nullptr;
+  int4 *sdesc = nullptr;
   double *shifts = nullptr;
   int n_msgs_total = 0;
   const float **marg_ptrs = nullptr;
@@ -604,6 +613,7 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
       d.ty_in = b.dry ? nullptr : pl.tables + toff + (size_t)R * W;
       d.tx_out = b.dry ? nullptr : pl.tables + toff + (size_t)R * (W + H);
       d.ty_out = b.dry ? nullptr : pl.tables + toff + (size_t)R * (W + H) + (size_t)R * W;
+      d.sdesc = b.dry ? nullptr : pl.sdesc + (size_t)gidx * 4 * R;
       all_shifts.insert(all_shifts.end(), mp.shifts.begin(), mp.shifts.end());
       d.rtaps = mp.rtaps.empty() ? nullptr : b.param(mp.rtaps.data(), mp.rtaps.size());
       d.xtaps = b.param(mp.xtaps.data(), mp.xtaps.size());
@@ -654,6 +664,7 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   };
   // tables first so descriptors can point into them
   pl.tables = b.scratch<int16_t>((size_t)pl.n_msgs_total * tbl_per);
+  pl.sdesc = b.scratch<int4>((size_t)pl.n_msgs_total * 4 * R);
   pl.up.assign(upph.size(), {});
   pl.down.assign(dnph.size(), {});
   for (size_t k = 0; k < upph.size(); ++k) build_phase(upph[k], pl.up[k]);
@@ -709,7 +720,7 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
   if (e->use_pairwise) {
     if (pl.n_msgs_total > 0)
-      PA_LAUNCH("shift_tables", launch_shift_tables(pl.shifts, pl.n_msgs_total, R, H, W, pl.tables, st));
+      PA_LAUNCH_N("shift_tables", 2, launch_shift_tables(pl.shifts, pl.n_msgs_total, R, H, W, pl.tables, pl.sdesc, st));
     for (auto &ph : pl.up) {
       if (!ph.n) continue;
       PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
@@ -950,15 +961,13 @@ std::vector<int> stump_counts(const pa_classifier *const *cls, int n) {
 }
 
 // The whole --find_obj pipeline for n_img images.
-pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
+// scores_out (if any) is laid out [n_cls][scores_fields][ny][nx] and this
+// call fills fields [scores_field0, scores_field0 + n_img*R) of it.
+pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
                         int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
-                        int ny, int nx, int dim, const double *Tig, int tig_shared, int H, int W,
-                        float *scores_out, const pa_ps_outputs *outs, int mem) {
-  if (!exp_ok(e)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
-  if (n_img < 1 || !trees || !desc || !Tig || !outs || ny < 1 || nx < 1 || dim < 1 || H < 1 ||
-      W < 1 || H > 32767 || W > 32767)
-    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
-  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+                        int in_mem, int ny, int nx, int dim, const double *Tig, int tig_shared,
+                        int H, int W, float *scores_out, int64_t scores_field0,
+                        int64_t scores_fields, const pa_ps_outputs *outs, int mem) {
   PsPlan pl;
   pa_status st = build_sched(ctx, &trees[0], pl.sc);
   if (st) return st;
@@ -994,9 +1003,12 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   // pass 1 (dry): measure
   Builder b1;
   b1.dry = true;
-  const bool scores_dev_out = (mem == PA_MEM_DEVICE && scores_out);
+  // device score grids can be written in place only when the caller's layout
+  // is exactly this call's [n_cls][n_fields] block
+  const bool scores_dev_out =
+      (mem == PA_MEM_DEVICE && scores_out && scores_field0 == 0 && scores_fields == n_fields);
   StumpPart *sp = plan_stumps(b1, cls, n_cls);
-  const float *desc_dev = (mem == PA_MEM_DEVICE) ? desc : b1.scratch<float>(n_fields * G * dim);
+  const float *desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b1.scratch<float>(n_fields * G * dim);
   float *scores = scores_dev_out ? scores_out : b1.scratch<float>((size_t)n_cls * n_fields * G);
   plan_ps(b1, pl, e, joints, marg_out.data(), rp_out.data());
   plan_marg_ptrs(b1, pl);
@@ -1016,7 +1028,7 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   b.base = ctx->arena;
   PsPlan pl2 = pl;
   sp = plan_stumps(b, cls, n_cls);
-  desc_dev = (mem == PA_MEM_DEVICE) ? desc : b.scratch<float>(n_fields * G * dim);
+  desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b.scratch<float>(n_fields * G * dim);
   scores = scores_dev_out ? scores_out : b.scratch<float>((size_t)n_cls * n_fields * G);
   plan_ps(b, pl2, e, joints, marg_out.data(), rp_out.data());
   plan_marg_ptrs(b, pl2);
@@ -1031,8 +1043,8 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
 
   st = upload_blob(ctx, b);
   if (st) return st;
-  if (mem == PA_MEM_HOST) {
-    st = copy_in(ctx, (void *)desc_dev, desc, (size_t)n_fields * G * dim * sizeof(float), mem);
+  if (in_mem == PA_MEM_HOST) {
+    st = copy_in(ctx, (void *)desc_dev, desc, (size_t)n_fields * G * dim * sizeof(float), in_mem);
     if (st) return st;
   }
   st = init_slots(ctx, pl2);
@@ -1042,9 +1054,12 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   const std::vector<int> ns = stump_counts(cls, n_cls);
   PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_cls, desc_dev, G,
                                               (int)n_fields, dim, 1, scores, s));
-  if (scores_out && mem == PA_MEM_HOST)
-    PA_CK(cudaMemcpyAsync(scores_out, scores, (size_t)n_cls * n_fields * G * sizeof(float),
-                          cudaMemcpyDeviceToHost, s));
+  if (scores_out && !scores_dev_out)
+    PA_CK(cudaMemcpy2DAsync(scores_out + scores_field0 * G, (size_t)scores_fields * G * sizeof(float),
+                            scores, (size_t)n_fields * G * sizeof(float),
+                            (size_t)n_fields * G * sizeof(float), (size_t)n_cls,
+                            mem == PA_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                            s));
   PA_LAUNCH_N("unary_maps", e->interpolate ? 1 : 2, launch_unary_maps(umaps, n_img * P * R, ny, nx, H, W, !e->interpolate, usep, s));
   if (!e->use_pairwise) {
     // getMaxStates: the marginals are the masked unaries
@@ -1056,6 +1071,89 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   st = run_ps(ctx, e, pl2);
   if (st) return st;
   return finish_ps(ctx, e, pl2, outs, mem);
+}
+
+// Host descriptors, several images: images go through a ring of device
+// slots.  The copy of image i+k (k < slots) runs on the context's copy
+// stream while image i is being computed, so a batch costs about
+// max(copy, compute) per image instead of their sum.
+pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
+                        int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
+                        int ny, int nx, int dim, const double *Tig, int tig_shared, int H, int W,
+                        float *scores_out, const pa_ps_outputs *outs) {
+  DeviceGuard dg(ctx->device);
+  const int R = e->num_rotation_steps;
+  const size_t per_img = (size_t)R * ny * nx * dim;
+  const size_t bytes = per_img * sizeof(float);
+  const int nslots = n_img < 3 ? n_img : 3;
+  if (!ctx->copy_stream) {
+    if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_CUDA, "cannot create the copy stream");
+    }
+  }
+  while ((int)ctx->ring_ev.size() < 3) {
+    cudaEvent_t ev;
+    PA_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ctx->ring_ev.push_back(ev);
+  }
+  if (ctx->ring_cap < nslots * bytes) {
+    PA_CK(cudaStreamSynchronize(ctx->copy_stream));
+    if (ctx->ring) cudaFree(ctx->ring);
+    ctx->ring = nullptr;
+    ctx->ring_cap = 0;
+    if (cudaMalloc(&ctx->ring, nslots * bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes for the input ring", nslots * bytes);
+    }
+    ctx->ring_cap = nslots * bytes;
+  }
+  auto issue = [&](int i) -> pa_status {
+    const int k = i % nslots;
+    PA_CK(cudaMemcpyAsync(ctx->ring + k * bytes, desc + i * per_img, bytes, cudaMemcpyHostToDevice,
+                          ctx->copy_stream));
+    PA_CK(cudaEventRecord(ctx->ring_ev[k], ctx->copy_stream));
+    return PA_OK;
+  };
+  for (int i = 0; i < nslots; ++i)
+    if (pa_status st = issue(i)) return st;
+  pa_status result = PA_OK;
+  for (int i = 0; i < n_img; ++i) {
+    const int k = i % nslots;
+    PA_CK(cudaStreamWaitEvent(ctx->stream, ctx->ring_ev[k], 0));
+    pa_status st = find_obj_core(ctx, e, 1, &trees[i], flip, cls, n_cls,
+                                 reinterpret_cast<const float *>(ctx->ring + k * bytes),
+                                 PA_MEM_DEVICE, ny, nx, dim, Tig, tig_shared, H, W, scores_out,
+                                 (int64_t)i * R, (int64_t)n_img * R, &outs[i], PA_MEM_HOST);
+    // image i is complete (the core synchronises the main stream): its slot
+    // can take image i + nslots
+    if (st && st != PA_ERR_NUMERIC) {
+      cudaStreamSynchronize(ctx->copy_stream);
+      return st;
+    }
+    if (st) result = st;
+    if (i + nslots < n_img)
+      if (pa_status s2 = issue(i + nslots)) return s2;
+  }
+  PA_CK(cudaStreamSynchronize(ctx->copy_stream));
+  return result;
+}
+
+pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
+                        int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
+                        int ny, int nx, int dim, const double *Tig, int tig_shared, int H, int W,
+                        float *scores_out, const pa_ps_outputs *outs, int mem) {
+  if (!exp_ok(e)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (n_img < 1 || !trees || !desc || !Tig || !outs || ny < 1 || nx < 1 || dim < 1 || H < 1 ||
+      W < 1 || H > 32767 || W > 32767)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  if (mem == PA_MEM_HOST && n_img > 1)
+    return find_obj_ring(ctx, e, n_img, trees, flip, cls, n_cls, desc, ny, nx, dim, Tig,
+                         tig_shared, H, W, scores_out, outs);
+  return find_obj_core(ctx, e, n_img, trees, flip, cls, n_cls, desc, mem, ny, nx, dim, Tig,
+                       tig_shared, H, W, scores_out, 0, (int64_t)n_img * e->num_rotation_steps,
+                       outs, mem);
 }
 
 }  // namespace
@@ -1119,6 +1217,12 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) {
     for (cudaEvent_t e : ctx->pool) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->copy_stream) {
+      cudaStreamSynchronize(ctx->copy_stream);
+      cudaStreamDestroy(ctx->copy_stream);
+    }
+    if (ctx->ring) cudaFree(ctx->ring);
+    for (cudaEvent_t e : ctx->ring_ev) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;
@@ -1509,11 +1613,14 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
   const int64_t N = (int64_t)R * H * W;
   MsgParams mp;
   msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, mp);
+  int4 *sdesc = nullptr;
   auto plan = [&](Builder &b, MsgDesc **md, int16_t **tables, double **shifts, int **slot,
                   int **err, const float **din, float **dout, float **e2) {
     MsgDesc d;
     std::memset(&d, 0, sizeof d);
     *tables = b.scratch<int16_t>((size_t)2 * R * (W + H));
+    sdesc = b.scratch<int4>((size_t)4 * R);
+    d.sdesc = sdesc;
     *slot = b.scratch<int>(1);
     *err = b.scratch<int>(1);
     *e2 = b.scratch<float>(N);
@@ -1560,7 +1667,7 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
   PA_LAUNCH("fill", launch_fill_int(slot, kFkeyNegInf, 1, s));
   PA_CK(cudaMemsetAsync(err, 0, sizeof(int), s));
   PA_LAUNCH("map_max", launch_map_max(din, N, slot, s));
-  PA_LAUNCH("shift_tables", launch_shift_tables(shifts, 1, R, H, W, tables, s));
+  PA_LAUNCH_N("shift_tables", 2, launch_shift_tables(shifts, 1, R, H, W, tables, sdesc, s));
   PA_LAUNCH("msg_rows", launch_msg_rows(md, 1, R, H, W, (mp.xlen - 1) / 2, err, s));
   PA_LAUNCH("msg_cols", launch_msg_cols(md, 1, R, H, W, (mp.ylen - 1) / 2, err, s));
   if (mem == PA_MEM_HOST)

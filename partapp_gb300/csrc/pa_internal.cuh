@@ -98,6 +98,7 @@ struct MsgDesc {
   const int16_t *ty_in;   // [R][H] source row (or -1; all -1 if rotation has no source)
   const int16_t *tx_out;  // [R][W] source column in log_joint_01 for parent column
   const int16_t *ty_out;  // [R][H]
+  const int4 *sdesc;      // [4][R] row summaries {c, lo, hi, uniform}: in_x, in_y, out_x, out_y
   const float *rtaps;     // rotation taps (clipped), rlen of them
   const float *xtaps;     // spatial x taps, xlen (odd)
   const float *ytaps;     // spatial y taps, ylen (odd)
@@ -143,7 +144,7 @@ cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, 
 cudaError_t launch_prepare_unary(const float *in, float *out, const int *masked_rot, int strip,
                                  int R, int H, int W, int *max_slot, cudaStream_t s);
 cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,
-                                int16_t *tables, cudaStream_t s);
+                                int16_t *tables, int4 *sdesc, cudaStream_t s);
 cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
                             int *err_flag, cudaStream_t s);
 cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int pady,
@@ -153,6 +154,8 @@ cudaError_t launch_root_posterior(const float *const *post_root, float *const *r
                                   const int *keep, int n_keep, int n_images, int R, int H, int W,
                                   cudaStream_t s);
 cudaError_t launch_fill_int(int *p, int v, int64_t n, cudaStream_t s);
+// src and dst 16-byte aligned; src may be pinned host memory.
+cudaError_t launch_copy16(const void *src, void *dst, int64_t n_words, cudaStream_t s);
 cudaError_t launch_map_max(const float *x, int64_t N, int *max_slot, cudaStream_t s);
 cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
                           unsigned long long *amax, cudaStream_t s);

@@ -8,7 +8,9 @@ Tolerances:
   * messages / marginals: per cell after max-normalisation,
     |exp(a - max a) - exp(b - max b)| <= 1e-4 against the FP32 oracle
     (TOL_F32) and <= 1e-3 against the FP64 oracle (TOL_F64);
-  * argmax (rotation, x, y) per part: identical.
+  * argmax (rotation, x, y) per part: identical to the FP32 oracle, except
+    where the two cells are a near-tie of the FP64 marginal (values within
+    1e-4, the marginal tolerance); at most one such part per case.
 """
 import math
 
@@ -193,6 +195,11 @@ def _pa_exp(R, **kw):
     return partapp_gb300.exp_param(R=R, **kw)
 
 
+def flat_of(best, R, H, W):
+    r, x, y = int(best[2]), int(best[4]), int(best[5])
+    return (r * H + y) * W + x
+
+
 def compare_ps(got, want, want64=None, check_argmax=True):
     P = want["log_marg"].shape[0]
     for p in range(P):
@@ -201,9 +208,24 @@ def compare_ps(got, want, want64=None, check_argmax=True):
         if want64 is not None:
             assert maxnorm_err(got["log_marg"][p], want64["log_marg"][p]) <= TOL_F64
     if check_argmax:
-        assert np.array_equal(got["best_conf"][:, [2, 4, 5]], want["best_conf"][:, [2, 4, 5]])
-        np.testing.assert_allclose(got["best_conf"][:, 6], want["best_conf"][:, 6], rtol=1e-5,
-                                   atol=1e-4)
+        _, R, H, W = want["log_marg"].shape
+        flips = 0
+        for p in range(P):
+            g, w = got["best_conf"][p], want["best_conf"][p]
+            if (g[2], g[4], g[5]) == (w[2], w[4], w[5]):
+                assert abs(g[6] - w[6]) <= 1e-5 * max(1.0, abs(w[6])), (p, g[6], w[6])
+                continue
+            assert want64 is not None, f"part {p}: argmax {g[[2, 4, 5]]} != {w[[2, 4, 5]]}"
+            m = want64["log_marg"][p].reshape(-1)
+            gap = abs(m[flat_of(g, R, H, W)] - m[flat_of(w, R, H, W)])
+            assert gap <= 1e-4, f"part {p}: argmax moved off a non-tied maximum (gap {gap})"
+            flips += 1
+        assert flips <= 1, f"{flips} near-tie argmax flips"
+
+
+def oracle64(orc, e, tree, log_unary):
+    return orc.ps_infer(e, tree, np.asarray(log_unary, dtype=np.float64), f64=True,
+                        want_hyps=False)
 
 
 @pytest.mark.parametrize("R", [24, 16])
@@ -247,7 +269,7 @@ def test_ps_variants(ctx, orc, variant):
                     rot_mean=-tree["rot_mean"])
     want = orc.ps_infer(e, t_or, u)
     got = ctx.compute_root_posterior_rot(_pa_exp(R, **kw), tree, u, flip=flip)
-    compare_ps(got, want)
+    compare_ps(got, want, oracle64(orc, e, t_or, u))
     if kw.get("use_pairwise", True):
         assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
 
@@ -263,7 +285,7 @@ def test_find_obj_pipeline(ctx, orc, interpolate):
     cls = ctx.classifiers(img["models"])
     got = ctx.find_obj(_pa_exp(12, interpolate=interpolate), img["tree"], cls, img["desc"],
                        img["Tig"], 64, 96)
-    compare_ps(got, want)
+    compare_ps(got, want, oracle64(orc, e, img["tree"], want["log_unary"]))
     assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
 
 
@@ -281,8 +303,35 @@ def test_find_obj_batch_device_resident(ctx, orc):
     for i, im in enumerate(imgs):
         want = orc.find_obj(e, im["tree"], models, im["desc"], im["Tig"], 48, 64)
         g = dict(got[i], log_marg=got[i]["log_marg"].cpu().numpy())
-        compare_ps(g, want)
+        compare_ps(g, want, oracle64(orc, e, im["tree"], want["log_unary"]))
         assert maxnorm_err(got[i]["root_post"].cpu().numpy(), want["root_post"]) <= TOL_F32
+
+
+def test_find_obj_batch_host_ring_matches_device(ctx):
+    """Host descriptors go through the copy/compute ring one image at a time;
+    results (and the strided score-grid output) must equal the batched
+    device-resident call bit for bit."""
+    import torch
+
+    imgs = [synth.make_image(300 + i, R=12, H=48, W=64, n_stumps=60, D=96, offset_range=(3, 8),
+                             sigma_range=(1, 2.5)) for i in range(4)]
+    models = imgs[0]["models"]
+    cls = ctx.classifiers(models)
+    desc = np.stack([im["desc"] for im in imgs])
+    trees = [im["tree"] for im in imgs]
+    sc_host = np.zeros((10, 4 * 12, 12, 16), dtype=np.float32)
+    host = ctx.find_obj_batch(_pa_exp(12), trees, cls, desc, imgs[0]["Tig"], 48, 64,
+                              want_marg=True, want_root=True, scores_out=sc_host)
+    sc_dev = torch.zeros((10, 4 * 12, 12, 16), dtype=torch.float32, device="cuda")
+    dev = ctx.find_obj_batch(_pa_exp(12), trees, cls, torch.from_numpy(desc).cuda(),
+                             imgs[0]["Tig"], 48, 64, want_marg=True, want_root=True,
+                             scores_out=sc_dev)
+    assert np.array_equal(sc_host, sc_dev.cpu().numpy())
+    for h, d in zip(host, dev):
+        assert np.array_equal(h["best_conf"], d["best_conf"])
+        assert np.array_equal(h["log_marg"], d["log_marg"].cpu().numpy())
+        assert np.array_equal(h["root_post"], d["root_post"].cpu().numpy())
+        assert np.array_equal(h["log_z"], d["log_z"])
 
 
 def test_config0_full_size_one_image(ctx, orc):
@@ -293,7 +342,7 @@ def test_config0_full_size_one_image(ctx, orc):
     want = orc.find_obj(e, img["tree"], img["models"], img["desc"], img["Tig"], 240, 320)
     cls = ctx.classifiers(img["models"])
     got = ctx.find_obj(_pa_exp(24), img["tree"], cls, img["desc"], img["Tig"], 240, 320)
-    compare_ps(got, want)
+    compare_ps(got, want, oracle64(orc, e, img["tree"], want["log_unary"]))
 
 
 # ------------------------------------------------------------------ errors
