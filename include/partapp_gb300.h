@@ -216,6 +216,26 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
                                 const double *offset_p, const double *C, double rot_mean,
                                 double rot_sigma, double scale, int mem);
 
+/* No counterpart in the reference.  pa_rot_joint_marginal for callers that
+ * cannot allocate device memory on their call path (a host application that
+ * keeps all device memory in its own pool, or a loop that must not hit
+ * cudaMalloc/cudaFree because they can synchronise the device).  It allocates
+ * nothing: its scratch is one static device array of fixed size in the
+ * library, held by every GPU that loads it.  child and parent are device
+ * pointers; `stream` is a cudaStream_t (NULL: the legacy default stream) and
+ * the call returns after the work on it has finished.
+ * Limits: R*H*W <= PA_NOALLOC_MAX_CELLS, R <= 64, H + W <= 4096, at most
+ * 1024 spatial taps per axis; larger sizes return PA_ERR_NOMEM.
+ * Calls share the array: calls whose GPU work overlaps race.  The first call
+ * on a device looks up the array's address; make it before any stream
+ * capture. */
+#define PA_NOALLOC_MAX_CELLS 2097152
+pa_status pa_rot_joint_marginal_noalloc(const pa_exp_param *ep, const float *child,
+                                        float *parent, int R, int H, int W,
+                                        const double *offset_c, const double *offset_p,
+                                        const double *C, double rot_mean, double rot_sigma,
+                                        double scale, void *stream);
+
 /* ---------------------------------------------------- the --find_obj path */
 
 /* One image of `partapp --find_obj` with freshly computed scores

@@ -35,6 +35,7 @@ PA_OK, PA_ERR_INVALID, PA_ERR_UNSUPPORTED, PA_ERR_CUDA, PA_ERR_NOMEM, PA_ERR_NUM
 PA_MEM_DEVICE, PA_MEM_HOST = 0, 1
 LOG_ZERO = -1e6
 NO_CLASS_VALUE = 0.0
+NOALLOC_MAX_CELLS = 2097152  # PA_NOALLOC_MAX_CELLS
 
 # every symbol include/partapp_gb300.h declares
 EXPORTS = (
@@ -43,7 +44,8 @@ EXPORTS = (
     "pa_ctx_timing_reset", "pa_ctx_timing_count", "pa_ctx_timing_get", "pa_exp_param_default",
     "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
     "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
-    "pa_ps_infer", "pa_rot_joint_marginal", "pa_find_obj", "pa_find_obj_batch",
+    "pa_ps_infer", "pa_rot_joint_marginal", "pa_rot_joint_marginal_noalloc", "pa_find_obj",
+    "pa_find_obj_batch",
 )
 
 
@@ -126,6 +128,8 @@ def load_library():
     L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, vp, ip, ip, P(PsOutputs), ip]
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
                                         dp, dp, dp, ip]
+    L.pa_rot_joint_marginal_noalloc.argtypes = [P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp),
+                                                 P(dp), dp, dp, dp, vp]
     L.pa_find_obj.argtypes = [vp, P(ExpParam), P(Tree), ip, P(vp), ip, vp, ip, ip, ip, P(dp), ip,
                               ip, ip, vp, P(PsOutputs), ip]
     L.pa_find_obj_batch.argtypes = [vp, P(ExpParam), ip, P(Tree), ip, P(vp), ip, vp, ip, ip, ip,

@@ -414,13 +414,12 @@ pa_status load_joints(pa_ctx *ctx, const pa_tree *t, int flip, std::vector<Joint
   return PA_OK;
 }
 
+}  // namespace
+
+namespace pa {
+
 // Per-message host parameters of computeRotJointMarginal(child -> parent,
 // offset_c_10 = oc, offset_p_01 = op, rot_mean, rot_sigma).
-struct MsgParams {
-  int kidx = 0, rlen = -1, xlen = 1, ylen = 1;
-  std::vector<float> rtaps, xtaps, ytaps;
-  std::vector<double> shifts;  // [4][R]
-};
 
 void msg_params(const pa_exp_param *e, double scale, const double *oc, const double *op,
                 const double *C, double rot_mean, double rot_sigma, MsgParams &m) {
@@ -470,6 +469,10 @@ void msg_params(const pa_exp_param *e, double scale, const double *oc, const dou
     m.shifts[3 * R + r] = dy;
   }
 }
+
+}  // namespace pa
+
+namespace {
 
 // ------------------------------------------------------------------------
 // PS plan for a batch of images (shared topology and sizes).

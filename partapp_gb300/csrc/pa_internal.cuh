@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "partapp_gb300.h"
 
 namespace pa {
@@ -125,6 +127,18 @@ struct RootDesc {
   float *post;                          // post[root] == root marginal
   unsigned long long *amax;
 };
+
+// Host-side parameters of one computeRotJointMarginal(child -> parent,
+// offset_c_10 = oc, offset_p_01 = op, rot_mean, rot_sigma): rotation-mean bin
+// shift, clipped rotation taps, spatial taps and the per-rotation shift
+// amounts in the reference's double-precision rounding (pa_api.cu).
+struct MsgParams {
+  int kidx = 0, rlen = -1, xlen = 1, ylen = 1;
+  std::vector<float> rtaps, xtaps, ytaps;
+  std::vector<double> shifts;  // [4][R]: a_x_in, a_y_in, a_x_out, a_y_out
+};
+void msg_params(const pa_exp_param *e, double scale, const double *oc, const double *op,
+                const double *C, double rot_mean, double rot_sigma, MsgParams &m);
 
 // Kernel launchers (defined in the .cu files).  All return cudaGetLastError().
 // fast_ok[p] / n_stumps[p] are host arrays describing the classifiers.
