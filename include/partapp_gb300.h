@@ -80,7 +80,7 @@ typedef struct {
   float min_object_scale;        /* [1]; num_scale_steps is 1 */
   float max_object_scale;        /* [1] */
   float strip_border_detections; /* fraction of the width [0] */
-  int roi_save_num_samples;      /* local maxima kept per part [1000] */
+  int roi_save_num_samples;      /* local maxima kept per part [1000], <= 2048 */
   int use_pairwise;              /* [1] */
   int interpolate;               /* grid->image TM_BILINEAR if 1, else TM_DIRECT [0] */
 } pa_exp_param;

@@ -364,6 +364,9 @@ class Context:
     def _finish(res, P):
         res["best_conf"] = np.array([[h.scaleidx, h.scale, h.rotidx, h.rot, h.x, h.y, h.score]
                                      for h in res.pop("best")], dtype=np.float32)
+        ph = np.frombuffer(res["part_hyps"], dtype=np.float32)
+        res["part_hyps"] = ph.reshape(P, -1, 7).copy() if ph.size >= 7 * P else ph.reshape(0, 7)
+        res["root_hyps"] = res["root_hyps"][: int(res["n_root_hyps"][0])]
         return res
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,

@@ -21,7 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpartapp_gb300.so")
-SOURCES = ["k_stump.cu", "k_unary.cu", "k_msg.cu", "k_reduce.cu", "pa_api.cu", "pa_noalloc.cu"]
+SOURCES = ["k_stump.cu", "k_unary.cu", "k_msg.cu", "k_reduce.cu", "k_localmax.cu", "pa_api.cu",
+           "pa_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -311,7 +311,7 @@ bool exp_ok(const pa_exp_param *e) {
   return e && e->num_rotation_steps >= 2 && e->num_rotation_steps <= kMaxRot &&
          e->max_part_rotation > e->min_part_rotation &&
          e->strip_border_detections >= 0 && e->strip_border_detections < 0.5f &&
-         e->roi_save_num_samples >= 0;
+         e->roi_save_num_samples >= 0 && e->roi_save_num_samples <= 2048;
 }
 
 // ------------------------------------------------------------------------
@@ -507,7 +507,17 @@ struct PsPlan {
   float **root_post_ptrs = nullptr;
   int *keep = nullptr;
   int n_keep = 0;
+  // findLocalMax outputs (objectdetect_aux.cpp:193-320)
+  bool want_part_hyps = false, want_root_hyps = false;
+  int hyp_k = 0;
+  void *lm_scratch = nullptr;
+  float *part_hyps = nullptr;   // [B*P][hyp_k][4] (s, x, y, value)
+  int *n_part_hyps = nullptr;   // [B*P]
+  float *root_hyps = nullptr;   // [B][1000][4]
+  int *n_root_hyps = nullptr;   // [B]
 };
+
+constexpr int kRootHyps = 1000;  // max_hypothesis_number, objectdetect_findrot.cpp:1037
 
 // Builds the device-side plan.  unary maps U are scratch unless `unary_in`
 // gives their final location.  marg_out/root_post_out: per image device
@@ -718,6 +728,30 @@ void plan_marg_ptrs(Builder &b, PsPlan &pl) {
   pl.marg_ptrs = b.param(mp.data(), mp.size());
 }
 
+// Local maxima are computed only when some output asks for them.
+void plan_localmax(Builder &b, PsPlan &pl, const pa_exp_param *e, const pa_ps_outputs *outs) {
+  pl.want_part_hyps = pl.want_root_hyps = false;
+  for (int i = 0; i < pl.B; ++i) {
+    if (outs[i].part_hyps || outs[i].n_part_hyps) pl.want_part_hyps = true;
+    if (outs[i].root_hyps || outs[i].n_root_hyps) pl.want_root_hyps = true;
+  }
+  pl.hyp_k = e->roi_save_num_samples;
+  if (pl.hyp_k < 1) pl.want_part_hyps = false;
+  if (!e->use_pairwise) pl.want_root_hyps = false;
+  size_t sb = 0;
+  if (pl.want_part_hyps) {
+    sb = std::max(sb, local_max_scratch_bytes(pl.B * pl.P, pl.N, pl.hyp_k));
+    pl.part_hyps = b.scratch<float>((size_t)pl.B * pl.P * pl.hyp_k * 4);
+    pl.n_part_hyps = b.scratch<int>((size_t)pl.B * pl.P);
+  }
+  if (pl.want_root_hyps) {
+    sb = std::max(sb, local_max_scratch_bytes(pl.B, (int64_t)pl.H * pl.W, kRootHyps));
+    pl.root_hyps = b.scratch<float>((size_t)pl.B * kRootHyps * 4);
+    pl.n_root_hyps = b.scratch<int>((size_t)pl.B);
+  }
+  pl.lm_scratch = sb ? (void *)b.scratch<char>(sb) : nullptr;
+}
+
 pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   cudaStream_t st = ctx->stream;
   const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
@@ -743,6 +777,15 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
     PA_LAUNCH("argmax", launch_argmax(pl.marg_ptrs, B * P, pl.N, pl.amax, st));
   }
   PA_LAUNCH_N("log_z", 2, launch_log_z(pl.marg_ptrs, pl.amax, B * P, pl.N, pl.logz_part, pl.logz, st));
+  if (pl.want_part_hyps)
+    PA_LAUNCH_N("local_max", local_max_kernels(pl.N, pl.hyp_k),
+                launch_local_max(pl.marg_ptrs, B * P, R, H, W, pl.hyp_k, pl.lm_scratch,
+                                 pl.part_hyps, pl.n_part_hyps, st, nullptr));
+  if (pl.want_root_hyps)
+    PA_LAUNCH_N("local_max", local_max_kernels((int64_t)H * W, kRootHyps),
+                launch_local_max(reinterpret_cast<const float *const *>(pl.root_post_ptrs), B, 1,
+                                 H, W, kRootHyps, pl.lm_scratch, pl.root_hyps, pl.n_root_hyps, st,
+                                 nullptr));
   return PA_OK;
 }
 
@@ -785,6 +828,20 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
   PA_CK(cudaMemcpyAsync(lz.data(), pl.logz, lz.size() * 8, cudaMemcpyDeviceToHost, st));
   PA_CK(cudaMemcpyAsync(mm.data(), pl.msgmax, mm.size() * 8, cudaMemcpyDeviceToHost, st));
   PA_CK(cudaMemcpyAsync(&errflag, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  std::vector<float> ph, rh;
+  std::vector<int> nph, nrh;
+  if (pl.want_part_hyps) {
+    ph.resize((size_t)B * P * pl.hyp_k * 4);
+    nph.resize((size_t)B * P);
+    PA_CK(cudaMemcpyAsync(ph.data(), pl.part_hyps, ph.size() * 4, cudaMemcpyDeviceToHost, st));
+    PA_CK(cudaMemcpyAsync(nph.data(), pl.n_part_hyps, nph.size() * 4, cudaMemcpyDeviceToHost, st));
+  }
+  if (pl.want_root_hyps) {
+    rh.resize((size_t)B * kRootHyps * 4);
+    nrh.resize((size_t)B);
+    PA_CK(cudaMemcpyAsync(rh.data(), pl.root_hyps, rh.size() * 4, cudaMemcpyDeviceToHost, st));
+    PA_CK(cudaMemcpyAsync(nrh.data(), pl.n_root_hyps, nrh.size() * 4, cudaMemcpyDeviceToHost, st));
+  }
   for (int i = 0; i < B; ++i) {
     const pa_ps_outputs &o = outs[i];
     if (mem == PA_MEM_HOST) {
@@ -806,11 +863,35 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
     for (int p = 0; p < P; ++p) {
       if (o.best) decode_hyp(e, am[(size_t)i * P + p], H, W, &o.best[p]);
       if (o.log_z) o.log_z[p] = lz[(size_t)i * P + p];
-      if (o.n_part_hyps) o.n_part_hyps[p] = 0;
+      const int n = pl.want_part_hyps ? nph[(size_t)i * P + p] : 0;
+      if (o.n_part_hyps) o.n_part_hyps[p] = n;
+      if (o.part_hyps)
+        for (int k = 0; k < n; ++k) {
+          // PartHyp(exp_param, 0, rotidx, x, y, score).toVect(), objectdetect.h:95-159
+          const float *r = &ph[(((size_t)i * P + p) * pl.hyp_k + k) * 4];
+          pa_part_hyp &h = o.part_hyps[(size_t)p * pl.hyp_k + k];
+          h.scaleidx = 0.f;
+          h.scale = (float)scale_from_index(e, 0);
+          h.rotidx = r[0];
+          h.rot = (float)rot_from_index(e, (int)r[0]);
+          h.x = r[1];
+          h.y = r[2];
+          h.score = r[3];
+        }
     }
     if (o.msg_max)
       for (int k = 0; k < 2 * (P - 1); ++k) o.msg_max[k] = mm[(size_t)i * 2 * (P - 1) + k];
-    if (o.n_root_hyps) *o.n_root_hyps = 0;
+    const int nr = pl.want_root_hyps ? nrh[i] : 0;
+    if (o.n_root_hyps) *o.n_root_hyps = nr;
+    if (o.root_hyps)
+      for (int k = 0; k < nr; ++k) {
+        // ObjectHypothesis (scale, x, y, score), objectdetect_aux.cpp:279-290
+        const float *r = &rh[((size_t)i * kRootHyps + k) * 4];
+        o.root_hyps[4 * k + 0] = (float)scale_from_index(e, (int)r[0]);
+        o.root_hyps[4 * k + 1] = r[1];
+        o.root_hyps[4 * k + 2] = r[2];
+        o.root_hyps[4 * k + 3] = r[3];
+      }
   }
   if (errflag & 1)
     return fail(ctx, PA_ERR_NUMERIC, "exp() overflowed in a message (the reference asserts here)");
@@ -1015,6 +1096,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   float *scores = scores_dev_out ? scores_out : b1.scratch<float>((size_t)n_cls * n_fields * G);
   plan_ps(b1, pl, e, joints, marg_out.data(), rp_out.data());
   plan_marg_ptrs(b1, pl);
+  plan_localmax(b1, pl, e, outs);
   UnaryMap *umaps = nullptr;
   int usep = 0;
   std::vector<std::vector<float *>> uouts(n_img, std::vector<float *>(P, nullptr));
@@ -1035,6 +1117,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   scores = scores_dev_out ? scores_out : b.scratch<float>((size_t)n_cls * n_fields * G);
   plan_ps(b, pl2, e, joints, marg_out.data(), rp_out.data());
   plan_marg_ptrs(b, pl2);
+  plan_localmax(b, pl2, e, outs);
   for (int i = 0; i < n_img; ++i)
     for (int p = 0; p < P; ++p) uouts[i][p] = pl2.im[i].U[p];
   st = plan_unary(ctx, b, Tig, tig_shared, n_img, P, R, ny, nx, H, W, !e->interpolate, scores,
@@ -1572,6 +1655,7 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
     *unary_dev = (mem == PA_MEM_HOST) ? b.scratch<float>((size_t)P * pl.N) : log_unary;
     plan_ps(b, p2, ep, joints, &marg_out, &rp_out);
     plan_marg_ptrs(b, p2);
+    plan_localmax(b, p2, ep, out);
   };
   Builder b1;
   PsPlan pl1 = pl;

@@ -171,6 +171,13 @@ cudaError_t launch_fill_int(int *p, int v, int64_t n, cudaStream_t s);
 // src and dst 16-byte aligned; src may be pinned host memory.
 cudaError_t launch_copy16(const void *src, void *dst, int64_t n_words, cudaStream_t s);
 cudaError_t launch_map_max(const float *x, int64_t N, int *max_slot, cudaStream_t s);
+// findLocalMax of n_maps [S][H][W] grids: up to k (1..2048) maxima per map as
+// (s, x, y, value) rows in hyps[map][k][4], their number in n_hyps[map].
+size_t local_max_scratch_bytes(int n_maps, int64_t cells, int k);
+int local_max_kernels(int64_t cells, int k);
+cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H, int W, int k,
+                             void *scratch, float *hyps, int *n_hyps, cudaStream_t s,
+                             int *n_kernels);
 cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
                           unsigned long long *amax, cudaStream_t s);
 cudaError_t launch_log_z(const float *const *maps, const unsigned long long *amax, int n_maps,

@@ -345,6 +345,58 @@ def test_config0_full_size_one_image(ctx, orc):
     compare_ps(got, want, oracle64(orc, e, img["tree"], want["log_unary"]))
 
 
+# ----------------------------------------------------------- local maxima
+@pytest.mark.parametrize("K,levels", [(50, 9), (1000, 2)])
+def test_local_max_exact_on_unaries(ctx, orc, K, levels):
+    """findLocalMax (objectdetect_aux.cpp:193-264) on maps with many ties and
+    plateaus: with use_pairwise off the marginals are the masked unaries, so
+    the GPU lists must equal the oracle's exactly -- the K largest values in
+    stable order when there are more than K maxima (K=50), and enumeration
+    order (rotation, then x, then y) otherwise (few maxima, K=1000)."""
+    rng = np.random.default_rng(K)
+    R, H, W = 6, 40, 52
+    if levels > 2:  # noisy, heavily tied: thousands of maxima
+        u = np.floor(rng.uniform(0, levels, (10, R, H, W))).astype(np.float32) - 5.0
+    else:  # a few quantised bumps: few maxima, including tied plateaus
+        r, y, x = np.meshgrid(np.arange(R), np.arange(H), np.arange(W), indexing="ij")
+        u = np.zeros((10, R, H, W), dtype=np.float32)
+        for p in range(10):
+            for _ in range(3):
+                cr, cy, cx = rng.integers(0, R), rng.uniform(0, H), rng.uniform(0, W)
+                u[p] += np.exp(-((y - cy) ** 2 + (x - cx) ** 2) / 60.0 - (r - cr) ** 2 / 4.0)
+        u = np.floor(u * 4.0).astype(np.float32)
+    tree = small_tree(rng, R)
+    e = orc.make_exp(R=R, use_pairwise=False, max_local_max=K)
+    want = orc.ps_infer(e, tree, u)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R, use_pairwise=False, local_max=K), tree, u)
+    assert np.array_equal(got["n_part_hyps"], want["n_part_hyps"])
+    for p in range(10):
+        n = int(want["n_part_hyps"][p])
+        assert np.array_equal(got["part_hyps"][p, :n], want["part_hyps"][p, :n]), p
+    if levels == 2:
+        assert (want["n_part_hyps"] < K).any()  # the enumeration-order branch ran
+    else:
+        assert (want["n_part_hyps"] == K).all()
+
+
+def test_local_max_with_pairwise_overlaps_oracle(ctx, orc):
+    rng = np.random.default_rng(44)
+    R, H, W = 12, 48, 64
+    tree = small_tree(rng, R)
+    u = synth.random_log_unary(rng, 10, R, H, W)
+    e = orc.make_exp(R=R, max_local_max=200)
+    want = orc.ps_infer(e, tree, u)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R, local_max=200), tree, u)
+    for p in range(10):
+        g = {tuple(r) for r in got["part_hyps"][p, :20, 2:6:1][:, [0, 2, 3]].tolist()}
+        w = {tuple(r) for r in want["part_hyps"][p, :20, 2:6:1][:, [0, 2, 3]].tolist()}
+        assert len(g & w) >= 18, p
+    assert abs(int(got["n_root_hyps"][0]) - want["n_root_hyps"]) <= 2
+    g = {tuple(r) for r in got["root_hyps"][:20, 1:3].tolist()}
+    w = {tuple(r) for r in want["root_hyps"][:20, 1:3].tolist()}
+    assert len(g & w) >= 18
+
+
 # ------------------------------------------------------------------ errors
 def test_errors_are_statuses(ctx, pa):
     rng = np.random.default_rng(5)
