@@ -151,24 +151,30 @@ __global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
   const int64_t n_tiles = blocks_per_field * n_fields;
   const int lrow = lane >> 3, lchunk = lane & 7;
 
-  // resident stump tables of the group: warp w's table at stumps_sm[w]
-  float4 *stab = reinterpret_cast<float4 *>(sm + 32 * kStride + ((32 * kStride) & 3 ? 4 - ((32 * kStride) & 3) : 0));
-  int my_n = 0;
+  // resident packed stump tables of the group: per classifier
+  // f8[npad/8] (uint4) followed by ta2[npad/2] (float4)
+  char *stab = reinterpret_cast<char *>(sm + 32 * kStride);
+  int my_npad = 0;
   float my_sum_alpha = 1.f;
-  const float4 *my_tab = stab;
+  const uint4 *my_f8 = nullptr;
+  const float4 *my_ta = nullptr;
   {
-    int off = 0;
+    size_t off = 0;
     for (int w = 0; w < group_size && w < nwarps; ++w) {
       const int pw = group * group_size + w;
       if (pw >= n_parts) break;
       const StumpPart sp = parts[pw];
+      uint4 *f8 = reinterpret_cast<uint4 *>(stab + off);
+      float4 *ta = reinterpret_cast<float4 *>(stab + off + (size_t)sp.npad * 2);
       if (w == warp) {
-        my_n = sp.n;
+        my_npad = sp.npad;
         my_sum_alpha = sp.sum_alpha;
-        my_tab = stab + off;
-        for (int i = lane; i < sp.n; i += 32) stab[off + i] = __ldg(sp.fast + i);
+        my_f8 = f8;
+        my_ta = ta;
+        for (int i = lane; i < sp.npad / 8; i += 32) f8[i] = __ldg(sp.f8 + i);
+        for (int i = lane; i < sp.npad / 2; i += 32) ta[i] = __ldg(sp.ta2 + i);
       }
-      off += sp.n;
+      off += (size_t)sp.npad * 10;
     }
   }
 
@@ -212,11 +218,19 @@ __global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
       const int nl = (n_loc - loc0) < kLoc ? (int)(n_loc - loc0) : kLoc;
       const float *v = sm + lane * kStride;
       float s = 0.f;
-#pragma unroll 8
-      for (int i = 0; i < my_n; ++i) {
-        const float4 q = my_tab[i];  // {f, t, a, -}
-        const float val = v[__float_as_int(q.x)];
-        s += (val < q.y) ? q.z : -q.z;
+#pragma unroll 2
+      for (int j = 0; j < my_npad / 8; ++j) {
+        const uint4 fq = my_f8[j];
+        const float4 q0 = my_ta[4 * j], q1 = my_ta[4 * j + 1];
+        const float4 q2 = my_ta[4 * j + 2], q3 = my_ta[4 * j + 3];
+        s += (v[fq.x & 0xFFFFu] < q0.x) ? q0.y : -q0.y;
+        s += (v[fq.x >> 16] < q0.z) ? q0.w : -q0.w;
+        s += (v[fq.y & 0xFFFFu] < q1.x) ? q1.y : -q1.y;
+        s += (v[fq.y >> 16] < q1.z) ? q1.w : -q1.w;
+        s += (v[fq.z & 0xFFFFu] < q2.x) ? q2.y : -q2.y;
+        s += (v[fq.z >> 16] < q2.z) ? q2.w : -q2.w;
+        s += (v[fq.w & 0xFFFFu] < q3.x) ? q3.y : -q3.y;
+        s += (v[fq.w >> 16] < q3.z) ? q3.w : -q3.w;
       }
       if (normalize) s = __fdiv_rn(s, my_sum_alpha);
       if (lane < nl) scores[((int64_t)part * n_fields + field) * n_loc + loc0 + lane] = s;
@@ -245,7 +259,7 @@ cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
     max_group_stumps = tot > max_group_stumps ? tot : max_group_stumps;
   }
   const size_t tile_bytes = ((size_t)kLoc * 961 + 3) / 4 * 4 * sizeof(float);
-  const size_t smem_pipe = tile_bytes + max_group_stumps * sizeof(float4);
+  const size_t smem_pipe = tile_bytes + max_group_stumps * 10;  // 2 B index + 8 B {t, a}
   const int launch_warps = nw < 10 ? 10 : nw;  // ten warps stage a 960-wide tile
   if (dim == 960 && aligned && all_fast && smem_pipe <= 227 * 1024) {
     cudaFuncSetAttribute(k_score_grids_pipe<960>, cudaFuncAttributeMaxDynamicSharedMemorySize,

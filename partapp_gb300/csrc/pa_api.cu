@@ -27,9 +27,11 @@ using namespace pa;
 struct pa_classifier {
   int dim = 0;
   int n = 0;
+  int npad = 0;
   float sum_alpha = 0.f;
   float4 *d = nullptr;     // {f, p, theta*p, alpha}
   float4 *fast = nullptr;  // {f, t, p*alpha, 0}, only when every p is +1 or -1
+  char *packed = nullptr;  // f8[npad/8] (uint4) then ta2[npad/2] (float4)
 };
 
 struct pa_ctx {
@@ -1028,19 +1030,28 @@ pa_status check_classifiers(pa_ctx *ctx, const pa_classifier *const *cls, int n_
 
 StumpPart *plan_stumps(Builder &b, const pa_classifier *const *cls, int n_parts) {
   std::vector<StumpPart> sp(n_parts);
-  for (int p = 0; p < n_parts; ++p) sp[p] = {cls[p]->d, cls[p]->fast, cls[p]->n, cls[p]->sum_alpha};
+  for (int p = 0; p < n_parts; ++p) {
+    const pa_classifier *c = cls[p];
+    sp[p].stumps = c->d;
+    sp[p].fast = c->fast;
+    sp[p].f8 = c->packed ? reinterpret_cast<const uint4 *>(c->packed) : nullptr;
+    sp[p].ta2 = c->packed ? reinterpret_cast<const float4 *>(c->packed + (size_t)c->npad * 2) : nullptr;
+    sp[p].n = c->n;
+    sp[p].npad = c->npad;
+    sp[p].sum_alpha = c->sum_alpha;
+  }
   return b.param(sp.data(), sp.size());
 }
 
 std::vector<char> fast_flags(const pa_classifier *const *cls, int n) {
   std::vector<char> f(n);
-  for (int p = 0; p < n; ++p) f[p] = cls[p]->fast != nullptr;
+  for (int p = 0; p < n; ++p) f[p] = cls[p]->packed != nullptr;
   return f;
 }
 
 std::vector<int> stump_counts(const pa_classifier *const *cls, int n) {
   std::vector<int> c(n);
-  for (int p = 0; p < n; ++p) c[p] = cls[p]->n;
+  for (int p = 0; p < n; ++p) c[p] = cls[p]->npad ? cls[p]->npad : cls[p]->n;
   return c;
 }
 
@@ -1413,6 +1424,33 @@ pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int
       return fail(ctx, PA_ERR_NOMEM, "cannot allocate stump table");
     }
     PA_CK(cudaMemcpy(c->fast, fast.data(), sizeof(float4) * n_stumps, cudaMemcpyHostToDevice));
+    // packed copy; stumps past n are {t = -inf, a = +0}: their vote -0 leaves
+    // the running sum (which starts at +0 and is never -0) unchanged
+    if (dim <= 65536) {
+      const int npad = (n_stumps + 7) / 8 * 8;
+      std::vector<uint16_t> f16(npad, 0);
+      std::vector<float> ta(2 * (size_t)npad);
+      for (int i = 0; i < npad; ++i) {
+        if (i < n_stumps) {
+          f16[i] = (uint16_t)stumps[i].f;
+          ta[2 * i] = fast[i].y;
+          ta[2 * i + 1] = fast[i].z;
+        } else {
+          ta[2 * i] = -INFINITY;
+          ta[2 * i + 1] = 0.f;
+        }
+      }
+      const size_t fb = (size_t)npad * 2, tb = (size_t)npad * 8;
+      if (cudaMalloc(&c->packed, fb + tb) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(c->d);
+        cudaFree(c->fast);
+        return fail(ctx, PA_ERR_NOMEM, "cannot allocate stump table");
+      }
+      PA_CK(cudaMemcpy(c->packed, f16.data(), fb, cudaMemcpyHostToDevice));
+      PA_CK(cudaMemcpy(c->packed + fb, ta.data(), tb, cudaMemcpyHostToDevice));
+      c->npad = npad;
+    }
   }
   *out = c.release();
   return PA_OK;
@@ -1452,9 +1490,11 @@ pa_status pa_classifier_destroy(pa_ctx *ctx, pa_classifier *cls) {
     DeviceGuard dg(ctx->device);
     cudaFree(cls->d);
     if (cls->fast) cudaFree(cls->fast);
+    if (cls->packed) cudaFree(cls->packed);
   } else {
     cudaFree(cls->d);
     if (cls->fast) cudaFree(cls->fast);
+    if (cls->packed) cudaFree(cls->packed);
   }
   delete cls;
   return PA_OK;

@@ -59,7 +59,11 @@ __host__ __device__ inline unsigned long long akey(float v, uint32_t flat) {
 struct StumpPart {
   const float4 *stumps;  // .x = f (int bits), .y = p, .z = theta * p, .w = alpha
   const float4 *fast;    // .x = f (int bits), .y = t, .z = p * alpha (p = +-1 only)
+  // packed form of `fast` for the 960-dim kernel, npad = n rounded up to 8:
+  const uint4 *f8;       // [npad/8] eight uint16 feature indices
+  const float4 *ta2;     // [npad/2] {t0, a0, t1, a1}
   int n;
+  int npad;
   float sum_alpha;
 };
 
