@@ -252,7 +252,7 @@ def run_ours(args):
     dev = torch.device(f"cuda:{local}")
 
     import partapp_gb300 as pa
-    from partapp_gb300 import build, synth
+    from partapp_gb300 import build, replicas, synth
 
     build.build()
     ctx = pa.Context(local)
@@ -287,14 +287,10 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
     ctx.enable_timing(False)
     launches = ctx.kernel_launches - l0
-    ms = t_start.elapsed_time(t_end)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(t_start.elapsed_time(t_end), dist, dev)
     ktimes = ctx.kernel_times()
-    images = B * args.steps * world
-    value = images / (ms / 1e3)
+    images = replicas.sum_over_ranks(B * args.steps, dist, dev)
+    value = replicas.throughput(images, ms)
 
     # roofline of the dominant kernel
     peaks, peak_kind = measured_peaks()
@@ -335,8 +331,8 @@ def run_ours(args):
         r = step_e2e()
     t1.record(stream)
     torch.cuda.synchronize(dev)
-    e2e_ms = t0.elapsed_time(t1)
-    e2e_val = Be * e2e_steps / (e2e_ms / 1e3) * world
+    e2e_ms = replicas.max_over_ranks(t0.elapsed_time(t1), dist, dev)
+    e2e_val = replicas.throughput(replicas.sum_over_ranks(Be * e2e_steps, dist, dev), e2e_ms)
     h2d = Be * R * NY * NX * D * 4
     d2h = Be * P * (7 * 4 + 8) + Be * 2 * (P - 1) * 8
 

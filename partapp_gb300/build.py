@@ -21,6 +21,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpartapp_gb300.so")
+HOST = os.path.join(HERE, "host")
+CLI = os.path.join(OUT, "partapp_find_obj")
+HOST_SOURCES = ["objectdetect_gpu.cpp", "find_obj_main.cpp"]
 SOURCES = ["k_stump.cu", "k_unary.cu", "k_msg.cu", "k_reduce.cu", "k_localmax.cu", "pa_api.cu",
            "pa_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -90,9 +93,26 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}\n{r.stdout}")
+    build_host()
     if verbose:
         print(LIB)
     return LIB
+
+
+def build_host() -> str:
+    """The C++ host layer (partapp_gpu.hpp) and the partapp_find_obj CLI,
+    linked against the C-ABI library (rpath $ORIGIN)."""
+    srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
+    deps = srcs + [os.path.join(HOST, "partapp_gpu.hpp"), LIB,
+                   os.path.join(ROOT, "include", "partapp_gb300.h")]
+    if _stale(CLI, deps):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), "-I", HOST] + \
+            srcs + ["-L", OUT, "-lpartapp_gb300", "-Wl,-rpath,$ORIGIN", "-o", CLI]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host build failed:\n{r.stderr}\n{r.stdout}")
+    return CLI
 
 
 def ptxas_report() -> str:

@@ -9,10 +9,11 @@
 //
 // GPU form: every local maximum becomes a 64-bit key whose high word orders
 // the value and whose low word is ~enumeration index, so "larger key" is
-// "larger value, then earlier in enumeration".  Chunks of kChunk keys are
-// sorted in shared memory and cut to their top max_n; repeated levels shrink
-// the candidate list until one chunk remains, which is ordered by key (more
-// than max_n maxima) or by enumeration index (at most max_n maxima).
+// "larger value, then earlier in enumeration" and keys are unique.  A radix
+// select over 8-bit digits finds the max_n-th largest key; the keys at or
+// above its bin (at most kChunk) are gathered, sorted in shared memory and
+// ordered by key (more than max_n maxima) or by enumeration index (at most
+// max_n maxima).
 #include "pa_internal.cuh"
 
 namespace pa {
@@ -95,46 +96,137 @@ __device__ void bitonic_desc(unsigned long long *a) {
     }
 }
 
-// One level: chunk c of map m (its first n_in[m] keys are valid) -> its top
-// k keys, sorted, zero-padded to exactly k, at out[m][c*k ...].
-__global__ void __launch_bounds__(kThreads) k_lm_level(const unsigned long long *__restrict__ in,
-                                                       const int *__restrict__ n_in,
-                                                       int64_t in_cap,
-                                                       unsigned long long *__restrict__ out,
-                                                       int *__restrict__ n_out, int64_t out_cap,
-                                                       int k) {
-  __shared__ unsigned long long a[kChunk];
+// Radix select of the top k keys of every map (keys are unique: the low
+// word is the enumeration index).  Pass d looks at bits [56 - 8d, 64 - 8d) of
+// the keys that share the bits above with `prefix`: every CTA histograms a
+// stride of the keys, and the last CTA to finish (arrival counter; no CTA
+// waits on another) picks the bin b that holds the k_rem-th largest key.
+// Keys in higher bins are selected for sure; the pass ends the search when
+// bin b holds at most `room` keys, so the final gather collects at most
+// k + room <= kChunk keys.
+struct LmState {
+  unsigned long long prefix;
+  int k_rem;
+  int shift;    // bits below the decided prefix when done
+  int done;     // 1: prefix decided; 2: every candidate is selected
+  int arrive;
+  int pad[2];
+};
+
+__global__ void __launch_bounds__(256) k_lm_radix(const unsigned long long *__restrict__ keys,
+                                                  const int *__restrict__ counts, int64_t cap,
+                                                  int pass, int room,
+                                                  unsigned int *__restrict__ hist,
+                                                  LmState *__restrict__ state) {
+  __shared__ unsigned int h[256];
+  __shared__ int last;
   const int map = blockIdx.y;
-  const int64_t n = min((int64_t)n_in[map], in_cap);
-  const int64_t start = (int64_t)blockIdx.x * kChunk;
-  if (blockIdx.x == 0 && threadIdx.x == 0) n_out[map] = (int)(((n + kChunk - 1) / kChunk) * k);
-  if (start >= n) return;
-  const int m = (int)min((int64_t)kChunk, n - start);
-  for (int t = threadIdx.x; t < kChunk; t += blockDim.x)
-    a[t] = t < m ? in[(int64_t)map * in_cap + start + t] : 0ull;
+  LmState *st = state + map;
+  if (st->done) return;  // decided by an earlier pass (uniform for the CTA)
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
   __syncthreads();
-  bitonic_desc(a);
-  unsigned long long *o = out + (int64_t)map * out_cap + (int64_t)blockIdx.x * k;
-  for (int t = threadIdx.x; t < k; t += blockDim.x) o[t] = a[t];
+  const int64_t n = min((int64_t)counts[map], cap);
+  const int shift = 56 - 8 * pass;
+  const unsigned long long prefix = st->prefix;
+  const unsigned long long *k = keys + (int64_t)map * cap;
+  // lanes that fall into the same bin add once (bins are crowded: most
+  // marginal values share their top bits)
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n_pad = (n + 31) / 32 * 32;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += stride) {
+    int bin = -1;
+    if (i < n) {
+      const unsigned long long key = k[i];
+      if (pass == 0 || (key >> (shift + 8)) == (prefix >> (shift + 8)))
+        bin = (int)((key >> shift) & 255u);
+    }
+    const unsigned same = __match_any_sync(0xFFFFFFFFu, bin);
+    if (bin >= 0 && (threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&h[bin], (unsigned)__popc(same));
+  }
+  __syncthreads();
+  unsigned int *g = hist + (int64_t)map * 256;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i]) atomicAdd(&g[i], h[i]);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(&st->arrive, 1) == (int)gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // the last CTA: read the complete histogram (through L2) and decide
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    h[i] = __ldcg(&g[i]);
+    g[i] = 0;  // ready for the next pass
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    st->arrive = 0;
+    const int k_rem = st->k_rem;
+    unsigned int total = 0;
+    for (int b = 0; b < 256; ++b) total += h[b];
+    if (pass == 0 && total <= (unsigned)k_rem) {
+      st->done = 2;
+    } else {
+      unsigned int cum = 0;
+      int b = 255;
+      for (; b > 0; --b) {
+        if (cum + h[b] >= (unsigned)k_rem) break;
+        cum += h[b];
+      }
+      st->prefix = prefix | ((unsigned long long)b << shift);
+      st->k_rem = k_rem - (int)cum;
+      if (h[b] <= (unsigned)room || shift == 0) {
+        st->shift = shift;
+        st->done = 1;
+      }
+    }
+  }
 }
 
-// Final: at most kChunk keys left.  With total maxima <= k the reference
-// lists them in enumeration order, else the k largest by value.
-__global__ void __launch_bounds__(kThreads) k_lm_final(const unsigned long long *__restrict__ in,
-                                                       const int *__restrict__ n_in,
-                                                       int64_t in_cap,
-                                                       const int *__restrict__ total, int k,
+__global__ void k_lm_init(LmState *__restrict__ state, int n_maps, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_maps) return;
+  LmState s;
+  s.prefix = 0ull;
+  s.k_rem = k;
+  s.shift = 0;
+  s.done = 0;
+  s.arrive = 0;
+  s.pad[0] = s.pad[1] = 0;
+  state[i] = s;
+}
+
+// Final: gather the selected keys (all candidates, or those at or above the
+// decided prefix: at most kChunk), sort them, keep k.  With total maxima
+// <= k the reference lists them in enumeration order, else the k largest by
+// value.
+__global__ void __launch_bounds__(kThreads) k_lm_final(const unsigned long long *__restrict__ keys,
+                                                       const int *__restrict__ counts, int64_t cap,
+                                                       const LmState *__restrict__ state, int k,
                                                        int S, int H, int W,
                                                        float *__restrict__ hyps,
                                                        int *__restrict__ n_hyps) {
   __shared__ unsigned long long a[kChunk];
+  __shared__ int na;
   const int map = blockIdx.x;
-  const int64_t n = min((int64_t)n_in[map], min(in_cap, (int64_t)kChunk));
-  const int tot = total[map];
-  for (int t = threadIdx.x; t < kChunk; t += blockDim.x)
-    a[t] = t < n ? in[(int64_t)map * in_cap + t] : 0ull;
+  const int64_t n = min((int64_t)counts[map], cap);
+  const LmState st = state[map];
+  for (int t = threadIdx.x; t < kChunk; t += blockDim.x) a[t] = 0ull;
+  if (threadIdx.x == 0) na = 0;
+  __syncthreads();
+  const unsigned long long *src = keys + (int64_t)map * cap;
+  const bool all = st.done == 2;
+  const unsigned long long lo = st.prefix;  // keys >= lo: selected or in the boundary bin
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const unsigned long long key = src[i];
+    if (all || (key >> st.shift) >= (lo >> st.shift)) {
+      const int p = atomicAdd(&na, 1);
+      if (p < kChunk) a[p] = key;
+    }
+  }
   __syncthreads();
   bitonic_desc(a);
+  const int tot = (int)n;
   const int keep = tot < k ? tot : k;
   if (tot <= k) {
     // enumeration order: ascending index == descending low word
@@ -175,25 +267,22 @@ struct LmLayout {
   }
 };
 
+constexpr int kRadixPasses = 8;  // 8-bit digits of the 64-bit keys
+constexpr int kRadixCtas = 8;    // CTAs per map in a histogram pass
+
 int local_max_kernels(int64_t cells, int k) {
-  int n = 2;  // candidates + final
-  int64_t cap = cells;
-  while (cap > kChunk) {
-    cap = ((cap + kChunk - 1) / kChunk) * k;
-    ++n;
-  }
-  return n;
+  (void)cells;
+  (void)k;
+  return 3 + kRadixPasses;  // counts, init, candidates + passes + final
 }
 
 size_t local_max_scratch_bytes(int n_maps, int64_t cells, int k) {
+  (void)k;
   LmLayout L;
-  L.take((size_t)n_maps * 3 * sizeof(int));
+  L.take((size_t)n_maps * sizeof(int));
+  L.take((size_t)n_maps * sizeof(LmState));
+  L.take((size_t)n_maps * 256 * sizeof(unsigned int));
   L.take((size_t)n_maps * (size_t)cells * 8);
-  int64_t cap = cells;
-  while (cap > kChunk) {
-    cap = ((cap + kChunk - 1) / kChunk) * k;
-    L.take((size_t)n_maps * (size_t)cap * 8);
-  }
   return L.off;
 }
 
@@ -202,41 +291,29 @@ cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H,
                              int *n_kernels) {
   if (k < 1 || k > kChunk / 2) return cudaErrorInvalidValue;
   const int64_t cells = (int64_t)S * H * W;
+  if (cells > 0xFFFFFFFFll) return cudaErrorInvalidValue;  // 32-bit enumeration index
   char *base = static_cast<char *>(scratch);
   LmLayout L;
-  int *counts = reinterpret_cast<int *>(base + L.take((size_t)n_maps * 3 * sizeof(int)));
-  int *total = counts;                 // candidates per map (level-0 size)
-  int *cnt_a = counts + n_maps;        // ping-pong level sizes
-  int *cnt_b = counts + 2 * n_maps;
+  int *counts = reinterpret_cast<int *>(base + L.take((size_t)n_maps * sizeof(int)));
+  LmState *state = reinterpret_cast<LmState *>(base + L.take((size_t)n_maps * sizeof(LmState)));
+  unsigned int *hist =
+      reinterpret_cast<unsigned int *>(base + L.take((size_t)n_maps * 256 * sizeof(unsigned int)));
   unsigned long long *keys =
       reinterpret_cast<unsigned long long *>(base + L.take((size_t)n_maps * cells * 8));
-  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * 3 * n_maps, s);
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * n_maps, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * 256 * n_maps, s);
   if (e != cudaSuccess) return e;
+  k_lm_init<<<(n_maps + 127) / 128, 128, 0, s>>>(state, n_maps, k);
   const int tiles = ((H + kTY - 1) / kTY) * ((W + kTX - 1) / kTX);
   k_lm_cand<<<dim3((unsigned)tiles, (unsigned)S, (unsigned)n_maps), kTY * kTX, 0, s>>>(
-      maps, S, H, W, keys, cells, total);
-  int nk = 1;
-  const unsigned long long *cur = keys;
-  const int *cur_n = total;
-  int64_t cur_cap = cells;
-  int *next_n = cnt_a;
-  while (cur_cap > kChunk) {
-    const int64_t chunks = (cur_cap + kChunk - 1) / kChunk;
-    const int64_t out_cap = chunks * k;
-    unsigned long long *out =
-        reinterpret_cast<unsigned long long *>(base + L.take((size_t)n_maps * out_cap * 8));
-    k_lm_level<<<dim3((unsigned)chunks, (unsigned)n_maps), kThreads, 0, s>>>(cur, cur_n, cur_cap, out,
-                                                                           next_n, out_cap, k);
-    ++nk;
-    cur = out;
-    cur_n = next_n;
-    next_n = (next_n == cnt_a) ? cnt_b : cnt_a;
-    cur_cap = out_cap;
-  }
-  k_lm_final<<<(unsigned)n_maps, kThreads, 0, s>>>(cur, cur_n, cur_cap, total, k, S, H, W, hyps,
+      maps, S, H, W, keys, cells, counts);
+  const int room = kChunk - k;
+  for (int pass = 0; pass < kRadixPasses; ++pass)
+    k_lm_radix<<<dim3(kRadixCtas, (unsigned)n_maps), 256, 0, s>>>(keys, counts, cells, pass, room,
+                                                                   hist, state);
+  k_lm_final<<<(unsigned)n_maps, kThreads, 0, s>>>(keys, counts, cells, state, k, S, H, W, hyps,
                                                    n_hyps);
-  ++nk;
-  if (n_kernels) *n_kernels = nk;
+  if (n_kernels) *n_kernels = 3 + kRadixPasses;
   return cudaGetLastError();
 }
 

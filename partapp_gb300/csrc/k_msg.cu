@@ -27,7 +27,7 @@
 namespace pa {
 namespace {
 
-constexpr int kThreadsRows = 256;
+constexpr int kThreadsRows = 384;
 constexpr int kThreadsCols = 256;
 constexpr int kNO = 11;   // outputs per lane in the row/column passes (odd: conflict-free)
 constexpr int kU = 8;     // taps per unrolled block
@@ -35,6 +35,20 @@ constexpr int kTX = 32;   // parent columns per k_msg_cols CTA
 constexpr int kCW = 33;   // staged source columns (one spare for rounding glitches)
 
 __device__ __forceinline__ int wrap(int r, int R) { return r < 0 ? r + R : (r >= R ? r - R : r); }
+
+// Packed FP32 FMA (two IEEE fmaf in one instruction, round to nearest, no
+// flush to zero): d = a * b + c lane-wise.  The spatial passes accumulate two
+// independent output streams per thread with it, so each stream keeps the
+// tap order and rounding of a scalar fmaf chain.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
 
 // Source index of a nearest-neighbour shift: a row of the exact table,
 // summarised by {c, lo, hi, uniform} when it is the plain shift
@@ -56,22 +70,26 @@ __device__ __forceinline__ float log_or_zero(float f) { return f == 0.f ? kLogZe
 // libMultiArray/multi_array_filter.hpp:116-155).
 // ---------------------------------------------------------------------------
 template <int R, int NR>
-__device__ __forceinline__ void rot_filter_fixed(const float (&e)[R], float *out, int stride,
+__device__ __forceinline__ void rot_filter_fixed(const float (&e)[R], float2 *out, int stride,
                                                  const float *t) {
+  static_assert(R % 2 == 0, "rotation pairs");
   float tv[2 * NR + 1];
 #pragma unroll
   for (int j = 0; j < 2 * NR + 1; ++j) tv[j] = t[j];
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    float acc = 0.f;
+  for (int q = 0; q < R / 2; ++q) {
+    float a0 = 0.f, a1 = 0.f;
 #pragma unroll
-    for (int j = 0; j < 2 * NR + 1; ++j) acc = fmaf(tv[j], e[((r - NR + j) % R + R) % R], acc);
-    out[r * stride] = acc;
+    for (int j = 0; j < 2 * NR + 1; ++j) {
+      a0 = fmaf(tv[j], e[((2 * q - NR + j) % R + R) % R], a0);
+      a1 = fmaf(tv[j], e[((2 * q + 1 - NR + j) % R + R) % R], a1);
+    }
+    out[q * stride] = make_float2(a0, a1);
   }
 }
 
 template <int R, int NR>
-__device__ __forceinline__ bool rot_filter_dispatch(int nr, const float (&e)[R], float *out,
+__device__ __forceinline__ bool rot_filter_dispatch(int nr, const float (&e)[R], float2 *out,
                                                     int stride, const float *t) {
   if constexpr (NR < 0) {
     return false;
@@ -96,62 +114,94 @@ __host__ __device__ __forceinline__ int align4(int n) { return (n + 3) & ~3; }
 
 // ---------------------------------------------------------------------------
 // k_msg_rows
+//
+// Shared layout: rotations are staged in pairs, E2v[p][col] = {E[2p][col],
+// E[2p+1][col]} (float2), so one 64-bit load feeds both halves of a packed
+// FMA in the x pass.  An odd R gets a zero dummy rotation.
 // ---------------------------------------------------------------------------
 template <int RT>
-__global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 3) k_msg_rows(const MsgDesc *__restrict__ msgs,
+__global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(const MsgDesc *__restrict__ msgs,
                                                            int Rrt, int H, int W, int padx,
                                                            int *err) {
   const int R = RT > 0 ? RT : Rrt;
+  const int RP = (R + 1) / 2;  // rotation pairs
   const MsgDesc md = msgs[blockIdx.y];
   const int y = blockIdx.x;
   const int WP = rows_stride(W, padx);
   extern __shared__ __align__(16) float sm[];
-  float *E = sm;                       // [R][WP]
-  float *tx = E + align4(R * WP);      // x taps, zero-padded to a multiple of kU (16B aligned)
+  float2 *E = reinterpret_cast<float2 *>(sm);  // [RP][WP] rotation pairs
+  const int xpmax = ((2 * padx + 1 + kU - 1) / kU) * kU;
+  float2 *tx = E + ((RP * WP + 1) & ~1);     // x taps {t, t}, zero-padded, 16B aligned
   const int xpad = ((md.xlen + kU - 1) / kU) * kU;
-  float *tr = tx + ((2 * padx + 1 + kU - 1) / kU) * kU;  // rotation taps
+  float *tr = reinterpret_cast<float *>(tx + xpmax);  // rotation taps
   const int tid = threadIdx.x;
 
-  for (int i = tid; i < xpad; i += blockDim.x) tx[i] = i < md.xlen ? md.xtaps[i] : 0.f;
+  for (int i = tid; i < xpad; i += blockDim.x) {
+    const float t = i < md.xlen ? md.xtaps[i] : 0.f;
+    tx[i] = make_float2(t, t);
+  }
   for (int i = tid; i < md.rlen; i += blockDim.x) tr[i] = md.rtaps[i];
 
   // (1) stage exp(J10 - M) for all rotations of row y; zero padding.
   const float negM = -fkey_decode(*md.in_max);
   const int HW = H * W;
   const int pad_r = WP - padx - W;
-  for (int idx = tid; idx < R * (padx + pad_r); idx += blockDim.x) {
-    const int r = idx / (padx + pad_r), k = idx - r * (padx + pad_r);
-    E[r * WP + (k < padx ? k : padx + W + (k - padx))] = 0.f;
+  for (int idx = tid; idx < RP * (padx + pad_r); idx += blockDim.x) {
+    const int p = idx / (padx + pad_r), k = idx - p * (padx + pad_r);
+    E[p * WP + (k < padx ? k : padx + W + (k - padx))] = make_float2(0.f, 0.f);
   }
   int4 *sdesc = reinterpret_cast<int4 *>(tr + kMaxRot + (RT == 0 ? kThreadsRows * R : 0));
+  int *rowoff = reinterpret_cast<int *>(sdesc + 2 * R);  // [R] source row of rotation r, or -1
+  float *ostage = reinterpret_cast<float *>(rowoff + align4(R));  // [warps][32 * kNO] output rows
   for (int i = tid; i < 2 * R; i += blockDim.x) sdesc[i] = md.sdesc[i];  // in_x[R], in_y[R]
   __syncthreads();
+  for (int r = tid; r < R; r += blockDim.x) {
+    const int sy = shift_src(sdesc[R + r], md.ty_in + r * H, y);
+    rowoff[r] = sy >= 0 ? (r - md.kidx) * HW + sy * W : -1;
+  }
+  __syncthreads();
   {
-    // four independent gathers in flight per thread
+    // Thread tid stages word h = tid & 1 of pair-cells (p, x), walking the
+    // pair-cells in steps of blockDim.x / 2 (neighbouring threads write
+    // neighbouring words); four independent gathers in flight per thread.
     constexpr int U = 4;
-    const int n = R * W;
-    for (int base = tid; base < n; base += U * blockDim.x) {
+    float *Ef = reinterpret_cast<float *>(E);
+    const int h = tid & 1, step = blockDim.x >> 1;
+    int p = (tid >> 1) / W, x = (tid >> 1) - ((tid >> 1) / W) * W;
+    while (p < RP) {
       float lv[U];
       int dst[U];
+      bool live[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int idx = base + u * blockDim.x;
         lv[u] = kLogZero;
         dst[u] = -1;
-        if (idx < n) {
-          const int r = idx / W, x = idx - r * W;
-          dst[u] = r * WP + padx + x;
-          const int sy = shift_src(sdesc[R + r], md.ty_in + r * H, y);
-          const int sx = shift_src(sdesc[r], md.tx_in + r * W, x);
-          if (sy >= 0 && sx >= 0) lv[u] = __ldg(md.in + (int64_t)(r - md.kidx) * HW + sy * W + sx);
+        live[u] = false;
+        if (p < RP) {
+          const int r = 2 * p + h;
+          dst[u] = (p * WP + padx + x) * 2 + h;
+          if (r < R) {
+            live[u] = true;
+            const int ro = rowoff[r];
+            const int sx = ro >= 0 ? shift_src(sdesc[r], md.tx_in + r * W, x) : -1;
+            if (sx >= 0) lv[u] = __ldg(md.in + (int64_t)ro + sx);
+          }
+          x += step;
+          while (x >= W) {
+            x -= W;
+            ++p;
+          }
         }
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if (dst[u] < 0) continue;
-        const float v = expf(__fadd_rn(lv[u], negM));
-        if (v == INFINITY) atomicOr(err, 1);
-        E[dst[u]] = v;
+        float v = 0.f;
+        if (live[u]) {
+          v = expf(__fadd_rn(lv[u], negM));
+          if (v == INFINITY) atomicOr(err, 1);
+        }
+        Ef[dst[u]] = v;
       }
     }
   }
@@ -159,9 +209,9 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 3) k_msg_rows(con
 
   // (2) rotation filter, column by column, in place.
   if (md.rlen == 0) {
-    for (int idx = tid; idx < R * W; idx += blockDim.x) {
-      const int r = idx / W, x = idx - r * W;
-      E[r * WP + padx + x] = 0.f;
+    for (int idx = tid; idx < RP * W; idx += blockDim.x) {
+      const int p = idx / W, x = idx - p * W;
+      E[p * WP + padx + x] = make_float2(0.f, 0.f);
     }
   } else if (md.rlen > 0) {
     const int nr = (md.rlen - 1) / 2;
@@ -169,50 +219,72 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 3) k_msg_rows(con
       for (int x = tid; x < W; x += blockDim.x) {
         float e[RT];
 #pragma unroll
-        for (int r = 0; r < RT; ++r) e[r] = E[r * WP + padx + x];
+        for (int p = 0; p < RT / 2; ++p) {
+          const float2 v = E[p * WP + padx + x];
+          e[2 * p] = v.x;
+          e[2 * p + 1] = v.y;
+        }
         if (!rot_filter_dispatch<RT, (RT - 1) / 2>(nr, e, E + padx + x, WP, tr)) atomicOr(err, 2);
       }
     } else {
       float *col = tr + kMaxRot;  // [blockDim.x][R] scratch
+      float *Ef = reinterpret_cast<float *>(E);
       for (int x = tid; x < W; x += blockDim.x) {
         float *c = col + tid * R;
-        for (int r = 0; r < R; ++r) c[r] = E[r * WP + padx + x];
+        for (int r = 0; r < R; ++r) c[r] = Ef[((r >> 1) * WP + padx + x) * 2 + (r & 1)];
         for (int r = 0; r < R; ++r) {
           float acc = 0.f;
           for (int j = 0; j < md.rlen; ++j) acc = fmaf(tr[j], c[wrap(r - nr + j, R)], acc);
-          E[r * WP + padx + x] = acc;
+          Ef[((r >> 1) * WP + padx + x) * 2 + (r & 1)] = acc;
         }
       }
     }
   }
   __syncthreads();
 
-  // (3) x pass: lane l owns outputs [l*kNO, l*kNO + kNO) of a row.
+  // (3) x pass: a task is (rotation pair, strip of 32 * kNO columns); lane l
+  // owns outputs [l*kNO, l*kNO + kNO) of the strip for both rotations.  The
+  // results go through a per-warp shared row so that each store instruction
+  // writes 32 consecutive floats.
   const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int kx = (md.xlen - 1) / 2;
   float *e2 = md.e2;
-  for (int r = warp; r < R; r += nwarps) {
-    const float *row = E + r * WP + padx - kx;
-    for (int x0 = lane * kNO; x0 < W; x0 += 32 * kNO) {
-      float acc[kNO];
+  float *ws = ostage + warp * (32 * kNO);
+  const int nstrips = (W + 32 * kNO - 1) / (32 * kNO);
+  for (int task = warp; task < RP * nstrips; task += nwarps) {
+    const int p = task / nstrips;
+    const int xs = (task - p * nstrips) * 32 * kNO;
+    const int x0 = xs + lane * kNO;
+    float2 acc[kNO];
 #pragma unroll
-      for (int i = 0; i < kNO; ++i) acc[i] = 0.f;
+    for (int i = 0; i < kNO; ++i) acc[i] = make_float2(0.f, 0.f);
+    if (x0 < W) {
+      const float2 *row = E + p * WP + padx - kx + x0;
       for (int kb = 0; kb < xpad; kb += kU) {
-        float v[kNO + kU - 1];
+        float2 v[kNO + kU - 1];
 #pragma unroll
-        for (int i = 0; i < kNO + kU - 1; ++i) v[i] = row[x0 + kb + i];
-        const float4 ta = *reinterpret_cast<const float4 *>(tx + kb);
-        const float4 tb = *reinterpret_cast<const float4 *>(tx + kb + 4);
-        const float t[kU] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+        for (int i = 0; i < kNO + kU - 1; ++i) v[i] = row[kb + i];
 #pragma unroll
-        for (int u = 0; u < kU; ++u)
+        for (int u = 0; u < kU; ++u) {
+          const float2 t = tx[kb + u];
 #pragma unroll
-          for (int i = 0; i < kNO; ++i) acc[i] = fmaf(t[u], v[i + u], acc[i]);
+          for (int i = 0; i < kNO; ++i) acc[i] = ffma2(t, v[i + u], acc[i]);
+        }
       }
-      float *o = e2 + (int64_t)r * HW + (int64_t)y * W;
+    }
+    const int nx = min(32 * kNO, W - xs);
+    float *o = e2 + (int64_t)(2 * p) * HW + (int64_t)y * W + xs;
 #pragma unroll
-      for (int i = 0; i < kNO; ++i)
-        if (x0 + i < W) o[x0 + i] = acc[i];
+    for (int i = 0; i < kNO; ++i) ws[lane * kNO + i] = acc[i].x;  // odd kNO: conflict-free
+    __syncwarp();
+    for (int j = lane; j < nx; j += 32) o[j] = ws[j];
+    __syncwarp();
+    if (2 * p + 1 < R) {
+#pragma unroll
+      for (int i = 0; i < kNO; ++i) ws[lane * kNO + i] = acc[i].y;
+      __syncwarp();
+      for (int j = lane; j < nx; j += 32) o[HW + j] = ws[j];
+      __syncwarp();
     }
   }
 }
@@ -375,24 +447,26 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
   const int tw = x1 - x0;
   int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
   unsigned long long am = 0ull;
-  const int n_out = (y1 - y0) * tw;
   const int mode = md.mode;
   const float *src0 = md.src0, *src1 = md.src1;
   float *dst0 = md.dst0, *dst1 = md.dst1;
+  // lane = parent column (coalesced row segments), warps step over rows
+  const int lx = tid & 31, wy = tid >> 5, nwy = blockDim.x >> 5;
+  const int xx = x0 + lx;
+  const int sx = lx < tw ? shift_src(dxo, txo, xx) : -1;
   constexpr int U = 4;
-  for (int base = tid; base < n_out; base += U * blockDim.x) {
+  for (int yb = y0 + wy; yb < y1; yb += U * nwy) {
     float m[U], a0[U], a1[U];
     int64_t idx[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int i = base + u * blockDim.x;
+      const int yy = yb + u * nwy;
       idx[u] = -1;
       m[u] = kLogZero;
       a0[u] = 0.f;
       a1[u] = 0.f;
-      if (i < n_out) {
-        const int yy = y0 + i / tw, xx = x0 + (i - (i / tw) * tw);
-        const int sy = shift_src(dyo, tyo, yy), sx = shift_src(dxo, txo, xx);
+      if (lx < tw && yy < y1) {
+        const int sy = shift_src(dyo, tyo, yy);
         if (sy >= 0 && sx >= 0) {
           const float f = F[(sy - rmin) * kCW + (sx - cmin)];
           m[u] = __fadd_rn(log_or_zero(f), M);
@@ -508,10 +582,13 @@ template <int RT>
 cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
                           int *err, cudaStream_t s) {
   const int WP = rows_stride(W, padx);
-  size_t smem = ((size_t)align4(R * WP) + ((2 * padx + 1 + kU - 1) / kU) * kU + kMaxRot) * sizeof(float);
+  const int RP = (R + 1) / 2;
+  size_t smem = ((size_t)2 * ((RP * WP + 1) & ~1) + 2 * ((2 * padx + 1 + kU - 1) / kU) * kU + kMaxRot) *
+                sizeof(float);
   if (RT == 0) smem += (size_t)kThreadsRows * R * sizeof(float);
-  smem += (size_t)2 * R * sizeof(int4);
-  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  smem += (size_t)2 * R * sizeof(int4) + (size_t)align4(R) * sizeof(int) +
+          (size_t)(kThreadsRows / 32) * 32 * kNO * sizeof(float);
+  if (smem > 227 * 1024 || (int64_t)R * H * W >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
   cudaFuncSetAttribute(k_msg_rows<RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid((unsigned)H, (unsigned)n_msgs);
   k_msg_rows<RT><<<grid, kThreadsRows, smem, s>>>(msgs, R, H, W, padx, err);

@@ -1,0 +1,194 @@
+// find_obj_main.cpp -- `partapp_find_obj --find_obj`: the --find_obj mode of
+// the reference's partapp binary (apps/partapp/main.cpp, findObjectDataset)
+// over an experiment directory of plain files:
+//
+//   exp.txt        "key value" lines: num_rotation_steps, min_part_rotation,
+//                  max_part_rotation, object_scale, strip_border_detections,
+//                  roi_save_num_samples, use_pairwise, interpolate, height,
+//                  width, grid_ny, grid_nx, dim, n_classifiers, n_images
+//   tig.txt        9 numbers: grid -> image transform, row-major 3x3
+//   joints.txt     "n_parts root", then n_parts is_upright flags, then one
+//                  line per joint: child parent ocx ocy opx opy C00 C01 C10
+//                  C11 rot_mean rot_sigma (radians; joints_<i>.txt if present
+//                  overrides it for image i)
+//   class_<c>.txt  AdaBoost classifier c in the reference's text format
+//                  (libAdaBoost/AdaBoost.cc:295-338)
+//   desc_<i>.bin   float32 [R][grid_ny][grid_nx][dim] descriptors of image i
+//
+// Writes best_conf_<i>.txt (one PartHyp::toVect line per part, as the
+// reference's best_conf), log_z_<i>.txt and part_hyps_<i>.txt into --outdir.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "partapp_gpu.hpp"
+
+using namespace partapp_gpu;
+
+namespace {
+
+std::string read_file(const std::string &path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  std::ostringstream ss;
+  ss << f.rdbuf();
+  return ss.str();
+}
+
+bool exists(const std::string &path) { return std::ifstream(path).good(); }
+
+std::map<std::string, double> read_kv(const std::string &path) {
+  std::map<std::string, double> kv;
+  std::istringstream in(read_file(path));
+  std::string k;
+  double v;
+  while (in >> k >> v) kv[k] = v;
+  return kv;
+}
+
+double need(const std::map<std::string, double> &kv, const std::string &k) {
+  auto it = kv.find(k);
+  if (it == kv.end()) throw std::runtime_error("exp.txt: missing " + k);
+  return it->second;
+}
+
+void read_joints(const std::string &path, PartConfig &pc, std::vector<Joint> &js) {
+  std::istringstream in(read_file(path));
+  int P = 0;
+  in >> P >> pc.rootpart_idx;
+  if (!in || P < 1) throw std::runtime_error(path + ": bad header");
+  pc.is_upright.assign(P, 0);
+  for (int p = 0; p < P; ++p) in >> pc.is_upright[p];
+  js.clear();
+  for (int j = 0; j < P - 1; ++j) {
+    Joint J;
+    in >> J.child_idx >> J.parent_idx >> J.offset_c[0] >> J.offset_c[1] >> J.offset_p[0] >>
+        J.offset_p[1] >> J.C[0] >> J.C[1] >> J.C[2] >> J.C[3] >> J.rot_mean >> J.rot_sigma;
+    if (!in) throw std::runtime_error(path + ": bad joint line");
+    js.push_back(J);
+  }
+}
+
+void usage() {
+  std::cout << "usage: partapp_find_obj --find_obj --expdir DIR [--outdir DIR] [--first i]\n"
+               "                        [--numimgs n] [--batch b] [--flip] [--device d]\n";
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  std::string expdir, outdir;
+  int first = 0, numimgs = -1, batch = 1, device = 0;
+  bool find_obj = false, flip = false;
+  for (int i = 1; i < argc; ++i) {
+    const std::string a = argv[i];
+    auto next = [&]() -> std::string {
+      if (i + 1 >= argc) throw std::runtime_error("missing value after " + a);
+      return argv[++i];
+    };
+    if (a == "--find_obj") find_obj = true;
+    else if (a == "--expdir") expdir = next();
+    else if (a == "--outdir") outdir = next();
+    else if (a == "--first") first = std::atoi(next().c_str());
+    else if (a == "--numimgs") numimgs = std::atoi(next().c_str());
+    else if (a == "--batch") batch = std::atoi(next().c_str());
+    else if (a == "--device") device = std::atoi(next().c_str());
+    else if (a == "--flip") flip = true;
+    else if (a == "--help" || a == "-h") { usage(); return 0; }
+    else { std::cerr << "unknown option " << a << "\n"; usage(); return 2; }
+  }
+  if (!find_obj || expdir.empty()) {
+    usage();
+    return find_obj ? 2 : 0;
+  }
+  if (outdir.empty()) outdir = expdir;
+  try {
+    const auto kv = read_kv(expdir + "/exp.txt");
+    PartApp app;
+    ExpParam &e = app.m_exp_param;
+    e.num_rotation_steps = (int)need(kv, "num_rotation_steps");
+    e.min_part_rotation = (float)need(kv, "min_part_rotation");
+    e.max_part_rotation = (float)need(kv, "max_part_rotation");
+    e.min_object_scale = e.max_object_scale = (float)need(kv, "object_scale");
+    e.strip_border_detections = (float)need(kv, "strip_border_detections");
+    e.roi_save_num_samples = (int)need(kv, "roi_save_num_samples");
+    e.use_pairwise = need(kv, "use_pairwise") != 0;
+    e.interpolate = need(kv, "interpolate") != 0;
+    const int H = (int)need(kv, "height"), W = (int)need(kv, "width");
+    const int ny = (int)need(kv, "grid_ny"), nx = (int)need(kv, "grid_nx");
+    const int dim = (int)need(kv, "dim"), n_cls = (int)need(kv, "n_classifiers");
+    const int n_images = (int)need(kv, "n_images");
+    const int R = e.num_rotation_steps;
+    if (numimgs < 0) numimgs = n_images - first;
+    if (first < 0 || first + numimgs > n_images || batch < 1)
+      throw std::runtime_error("image range outside the experiment");
+
+    double Tig[9];
+    {
+      std::istringstream in(read_file(expdir + "/tig.txt"));
+      for (double &t : Tig) in >> t;
+      if (!in) throw std::runtime_error("tig.txt: need 9 numbers");
+    }
+    read_joints(expdir + "/joints.txt", app.m_part_conf, app.m_joints);
+
+    Context ctx(device);
+    std::vector<std::unique_ptr<AdaBoostClassifier>> abc;
+    for (int c = 0; c < n_cls; ++c) {
+      abc.emplace_back(new AdaBoostClassifier(ctx, read_file(expdir + "/class_" + std::to_string(c) + ".txt")));
+      app.m_abc.push_back(abc.back().get());
+    }
+
+    const size_t per_img = (size_t)R * ny * nx * dim;
+    for (int i0 = first; i0 < first + numimgs; i0 += batch) {
+      const int nb = std::min(batch, first + numimgs - i0);
+      std::vector<float> desc(per_img * nb);
+      std::vector<std::vector<Joint>> joints;
+      for (int b = 0; b < nb; ++b) {
+        const int img = i0 + b;
+        const std::string d = read_file(expdir + "/desc_" + std::to_string(img) + ".bin");
+        if (d.size() != per_img * sizeof(float))
+          throw std::runtime_error("desc_" + std::to_string(img) + ".bin: wrong size");
+        std::memcpy(desc.data() + per_img * b, d.data(), d.size());
+        const std::string jp = expdir + "/joints_" + std::to_string(img) + ".txt";
+        if (exists(jp)) {
+          PartConfig pc;
+          std::vector<Joint> js;
+          read_joints(jp, pc, js);
+          joints.push_back(js);
+        } else {
+          joints.push_back(app.m_joints);
+        }
+      }
+      const auto res = findObjectDataset(ctx, app, flip, joints, desc.data(), nb, ny, nx, dim, Tig, H, W);
+      for (int b = 0; b < nb; ++b) {
+        const std::string tag = std::to_string(i0 + b);
+        std::ofstream bc(outdir + "/best_conf_" + tag + ".txt");
+        bc.precision(9);
+        for (const PartHyp &h : res[b].best_conf) {
+          const auto v = h.toVect();
+          for (size_t k = 0; k < v.size(); ++k) bc << (k ? " " : "") << v[k];
+          bc << "\n";
+        }
+        std::ofstream lz(outdir + "/log_z_" + tag + ".txt");
+        lz.precision(17);
+        for (double z : res[b].log_z) lz << z << "\n";
+        std::ofstream ph(outdir + "/part_hyps_" + tag + ".txt");
+        ph.precision(9);
+        for (size_t p = 0; p < res[b].part_hyps.size(); ++p)
+          for (const PartHyp &h : res[b].part_hyps[p])
+            ph << p << " " << h.m_rotidx << " " << h.m_x << " " << h.m_y << " " << h.m_score << "\n";
+      }
+      std::cout << "find_obj: images " << i0 << ".." << i0 + nb - 1 << " done\n";
+    }
+  } catch (const std::exception &ex) {
+    std::cerr << "partapp_find_obj: " << ex.what() << "\n";
+    return 1;
+  }
+  return 0;
+}

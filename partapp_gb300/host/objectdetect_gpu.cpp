@@ -1,0 +1,274 @@
+// objectdetect_gpu.cpp -- the reference-shaped host functions of
+// partapp_gpu.hpp, each a thin adapter onto include/partapp_gb300.h.
+#include "partapp_gpu.hpp"
+
+#include <cstring>
+
+namespace partapp_gpu {
+
+namespace {
+
+// The C-ABI view of a tree: arrays kept alive by the holder.
+struct TreeHolder {
+  std::vector<int> is_upright, child, parent;
+  std::vector<double> oc, op, C, rot_mean, rot_sigma;
+  pa_tree t{};
+
+  TreeHolder(const PartConfig &pc, int root, const std::vector<Joint> &joints) {
+    is_upright = pc.is_upright;
+    for (const Joint &j : joints) {
+      child.push_back(j.child_idx);
+      parent.push_back(j.parent_idx);
+      oc.insert(oc.end(), j.offset_c, j.offset_c + 2);
+      op.insert(op.end(), j.offset_p, j.offset_p + 2);
+      C.insert(C.end(), j.C, j.C + 4);
+      rot_mean.push_back(j.rot_mean);
+      rot_sigma.push_back(j.rot_sigma);
+    }
+    t.n_parts = pc.part_size();
+    t.root = root;
+    t.is_upright = is_upright.data();
+    t.n_joints = (int)joints.size();
+    t.child = child.data();
+    t.parent = parent.data();
+    t.offset_c = oc.data();
+    t.offset_p = op.data();
+    t.C = C.data();
+    t.rot_mean = rot_mean.data();
+    t.rot_sigma = rot_sigma.data();
+  }
+};
+
+PartHyp to_hyp(const pa_part_hyp &h) {
+  PartHyp p;
+  p.m_scaleidx = (int)h.scaleidx;
+  p.m_scale = h.scale;
+  p.m_rotidx = (int)h.rotidx;
+  p.m_rot = h.rot;
+  p.m_x = (int)h.x;
+  p.m_y = (int)h.y;
+  p.m_score = h.score;
+  return p;
+}
+
+void require(bool ok, const char *what) {
+  if (!ok) throw Error(PA_ERR_INVALID, what);
+}
+
+// Output buffers of one image.
+struct ImageOut {
+  std::vector<pa_part_hyp> best, part_hyps;
+  std::vector<int> n_part_hyps;
+  std::vector<float> root_hyps;
+  int n_root_hyps = 0;
+  std::vector<double> log_z;
+  pa_ps_outputs o{};
+
+  ImageOut(int P, int K) : best(P), part_hyps((size_t)P * K), n_part_hyps(P), root_hyps(1000 * 4),
+                           log_z(P) {
+    o.best = best.data();
+    o.part_hyps = part_hyps.data();
+    o.n_part_hyps = n_part_hyps.data();
+    o.root_hyps = root_hyps.data();
+    o.n_root_hyps = &n_root_hyps;
+    o.log_z = log_z.data();
+  }
+
+  FindObjResult result(int P, int K) const {
+    FindObjResult r;
+    for (int p = 0; p < P; ++p) r.best_conf.push_back(to_hyp(best[p]));
+    r.part_hyps.resize(P);
+    for (int p = 0; p < P; ++p)
+      for (int k = 0; k < n_part_hyps[p]; ++k) r.part_hyps[p].push_back(to_hyp(part_hyps[(size_t)p * K + k]));
+    for (int k = 0; k < n_root_hyps; ++k)
+      r.root_hyps.push_back(std::vector<float>(root_hyps.begin() + 4 * k, root_hyps.begin() + 4 * k + 4));
+    r.log_z = log_z;
+    return r;
+  }
+};
+
+}  // namespace
+
+pa_exp_param ExpParam::c() const {
+  pa_exp_param e;
+  pa_exp_param_default(&e);
+  e.num_rotation_steps = num_rotation_steps;
+  e.min_part_rotation = min_part_rotation;
+  e.max_part_rotation = max_part_rotation;
+  e.min_object_scale = min_object_scale;
+  e.max_object_scale = max_object_scale;
+  e.strip_border_detections = strip_border_detections;
+  e.roi_save_num_samples = roi_save_num_samples;
+  e.use_pairwise = use_pairwise ? 1 : 0;
+  e.interpolate = interpolate ? 1 : 0;
+  return e;
+}
+
+std::vector<float> PartHyp::toVect() const {
+  return {(float)m_scaleidx, (float)m_scale, (float)m_rotidx, (float)m_rot,
+          (float)m_x,        (float)m_y,     m_score};
+}
+
+Context::Context(int device) {
+  const pa_status s = pa_ctx_create(device, &ctx_);
+  if (s != PA_OK) throw Error(s, std::string("pa_ctx_create: ") + pa_status_string(s));
+}
+
+Context::~Context() {
+  if (ctx_) pa_ctx_destroy(ctx_);
+}
+
+void Context::check(pa_status s) const {
+  if (s != PA_OK) throw Error(s, std::string(pa_status_string(s)) + ": " + pa_last_error(ctx_));
+}
+
+AdaBoostClassifier::AdaBoostClassifier(Context &ctx, const std::string &text) : ctx_(ctx) {
+  ctx.check(pa_classifier_parse(ctx.get(), text.data(), text.size(), &cls_));
+}
+
+AdaBoostClassifier::AdaBoostClassifier(Context &ctx, int dim, const std::vector<pa_stump> &stumps)
+    : ctx_(ctx) {
+  ctx.check(pa_classifier_create(ctx.get(), dim, stumps.data(), (int)stumps.size(), &cls_));
+}
+
+AdaBoostClassifier::~AdaBoostClassifier() {
+  if (cls_) pa_classifier_destroy(ctx_.get(), cls_);
+}
+
+int AdaBoostClassifier::dim() const {
+  int d = 0;
+  pa_classifier_info(cls_, &d, nullptr, nullptr);
+  return d;
+}
+
+int AdaBoostClassifier::size() const {
+  int n = 0;
+  pa_classifier_info(cls_, nullptr, &n, nullptr);
+  return n;
+}
+
+float AdaBoostClassifier::sum_alpha() const {
+  float s = 0;
+  pa_classifier_info(cls_, nullptr, nullptr, &s);
+  return s;
+}
+
+void computeRotJointMarginal(Context &ctx, const ExpParam &exp_param, FloatGrid3 &log_prob_child,
+                             FloatGrid3 &log_prob_parent, const double offset_c_10[2],
+                             const double offset_p_01[2], const double C[4], double rot_mean,
+                             double rot_sigma, double scale, bool bIsSparse) {
+  require(!bIsSparse, "computeRotJointMarginal: only the dense path (bIsSparse = false) is built");
+  const size_t *s = log_prob_child.shape();
+  if (log_prob_parent.num_elements() != log_prob_child.num_elements())
+    log_prob_parent = FloatGrid3(s[0], s[1], s[2]);
+  const pa_exp_param e = exp_param.c();
+  ctx.check(pa_rot_joint_marginal(ctx.get(), &e, log_prob_child.data(), log_prob_parent.data(),
+                                  (int)s[0], (int)s[1], (int)s[2], offset_c_10, offset_p_01, C,
+                                  rot_mean, rot_sigma, scale, PA_MEM_HOST));
+}
+
+void computeRootPosteriorRot(Context &ctx, const PartApp &part_app,
+                             std::vector<std::vector<FloatGrid3>> &log_part_detections,
+                             FloatGrid3 &root_part_posterior, int rootpart_idx,
+                             std::vector<Joint> joints, bool flip, bool bIsSparse, int imgidx,
+                             std::vector<std::vector<PartHyp>> &best_part_hyp,
+                             bool bSaveMarginals, std::vector<FloatGrid3> *log_marginals,
+                             std::vector<double> *log_z) {
+  (void)flip;  // the joints are already mirrored by loadJoints; flip only names output files
+  (void)imgidx;
+  (void)bSaveMarginals;
+  require(!bIsSparse, "computeRootPosteriorRot: only the dense path (bIsSparse = false) is built");
+  const int P = (int)log_part_detections.size();
+  require(P == part_app.m_part_conf.part_size(), "one detection stack per part");
+  require(P > 0 && !log_part_detections[0].empty(), "empty detections");
+  const size_t *s = log_part_detections[0][0].shape();
+  const int R = (int)s[0], H = (int)s[1], W = (int)s[2];
+  const size_t N = (size_t)R * H * W;
+  std::vector<float> unary((size_t)P * N);
+  for (int p = 0; p < P; ++p) {
+    require(!log_part_detections[p].empty() && log_part_detections[p][0].num_elements() == N,
+            "all parts need [R][H][W] maps of one size (one scale)");
+    std::memcpy(unary.data() + (size_t)p * N, log_part_detections[p][0].data(), N * sizeof(float));
+  }
+  const TreeHolder th(part_app.m_part_conf, rootpart_idx, joints);
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int K = e.roi_save_num_samples;
+  ImageOut out(P, K > 0 ? K : 1);
+  root_part_posterior = FloatGrid3(1, H, W);
+  out.o.root_post = root_part_posterior.data();
+  std::vector<float> marg;
+  if (log_marginals) {
+    marg.resize((size_t)P * N);
+    out.o.log_marg = marg.data();
+  }
+  ctx.check(pa_ps_infer(ctx.get(), &e, &th.t, 0, unary.data(), H, W, &out.o, PA_MEM_HOST));
+  const FindObjResult r = out.result(P, K > 0 ? K : 1);
+  best_part_hyp = r.part_hyps;
+  if (log_marginals) {
+    log_marginals->clear();
+    for (int p = 0; p < P; ++p) {
+      FloatGrid3 g(R, H, W);
+      std::memcpy(g.data(), marg.data() + (size_t)p * N, N * sizeof(float));
+      log_marginals->push_back(std::move(g));
+    }
+  }
+  if (log_z) *log_z = r.log_z;
+}
+
+void computeScoreGrids(Context &ctx, const std::vector<const AdaBoostClassifier *> &abc,
+                       const float *desc, int n_fields, int ny, int nx, int dim,
+                       bool bNormalizeBoost, std::vector<FloatGrid3> &scores) {
+  std::vector<const pa_classifier *> cls;
+  for (const AdaBoostClassifier *a : abc) cls.push_back(a->get());
+  const size_t per = (size_t)n_fields * ny * nx;
+  std::vector<float> buf(cls.size() * per);
+  ctx.check(pa_score_grids(ctx.get(), cls.data(), (int)cls.size(), desc, n_fields, ny, nx, dim,
+                           bNormalizeBoost ? 1 : 0, buf.data(), PA_MEM_HOST));
+  scores.clear();
+  for (size_t c = 0; c < cls.size(); ++c) {
+    FloatGrid3 g(n_fields, ny, nx);
+    std::memcpy(g.data(), buf.data() + c * per, per * sizeof(float));
+    scores.push_back(std::move(g));
+  }
+}
+
+FindObjResult findObjectImageRotJoints(Context &ctx, const PartApp &part_app, bool flip,
+                                       const float *desc, int ny, int nx, int dim,
+                                       const double Tig[9], int H, int W) {
+  return findObjectDataset(ctx, part_app, flip, {part_app.m_joints}, desc, 1, ny, nx, dim, Tig, H,
+                           W)[0];
+}
+
+std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_app, bool flip,
+                                             const std::vector<std::vector<Joint>> &joints,
+                                             const float *desc, int n_images, int ny, int nx,
+                                             int dim, const double Tig[9], int H, int W) {
+  require(n_images >= 1 && (int)joints.size() == n_images, "one joint set per image");
+  const int P = part_app.m_part_conf.part_size();
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int K = e.roi_save_num_samples > 0 ? e.roi_save_num_samples : 1;
+  std::vector<TreeHolder> holders;
+  holders.reserve(n_images);
+  std::vector<pa_tree> trees;
+  for (int i = 0; i < n_images; ++i) {
+    holders.emplace_back(part_app.m_part_conf, part_app.m_part_conf.rootpart_idx, joints[i]);
+    trees.push_back(holders.back().t);
+  }
+  std::vector<ImageOut> outs;
+  outs.reserve(n_images);
+  std::vector<pa_ps_outputs> o;
+  for (int i = 0; i < n_images; ++i) {
+    outs.emplace_back(P, K);
+    o.push_back(outs.back().o);
+  }
+  std::vector<const pa_classifier *> cls;
+  for (const AdaBoostClassifier *a : part_app.m_abc) cls.push_back(a->get());
+  ctx.check(pa_find_obj_batch(ctx.get(), &e, n_images, trees.data(), flip ? 1 : 0, cls.data(),
+                              (int)cls.size(), desc, ny, nx, dim, Tig, 1, H, W, nullptr, o.data(),
+                              PA_MEM_HOST));
+  std::vector<FindObjResult> res;
+  for (int i = 0; i < n_images; ++i) res.push_back(outs[i].result(P, K));
+  return res;
+}
+
+}  // namespace partapp_gpu

@@ -1,0 +1,185 @@
+// partapp_gpu.hpp -- C++ host layer of partapp_gb300 with the reference's
+// call surface for the --find_obj hot path.
+//
+// The reference's functions take boost::multi_array grids and its own
+// ExpParam / PartConfig / Joint / PartHyp types (libPictStruct/objectdetect.h,
+// libPartApp).  This header keeps those shapes -- FloatGrid3 in C order
+// [rot][y][x], per-part stacks [part][scale], joints as after loadJoints --
+// and forwards every call to the C-ABI of include/partapp_gb300.h, so a
+// caller of the reference can switch with a type alias.  Errors that the
+// reference asserts on throw partapp_gpu::Error here.
+#ifndef PARTAPP_GPU_HPP_
+#define PARTAPP_GPU_HPP_
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "partapp_gb300.h"
+
+namespace partapp_gpu {
+
+struct Error : std::runtime_error {
+  Error(pa_status s, const std::string &what) : std::runtime_error(what), status(s) {}
+  pa_status status;
+};
+
+// boost::multi_array<float, 3> stand-in (libMultiArray/multi_array_def.h:36):
+// contiguous, C order, shape()[0] = rotations, [1] = rows, [2] = columns.
+class FloatGrid3 {
+ public:
+  FloatGrid3() = default;
+  FloatGrid3(size_t n0, size_t n1, size_t n2, float fill = 0.f)
+      : shape_{n0, n1, n2}, data_(n0 * n1 * n2, fill) {}
+  const size_t *shape() const { return shape_; }
+  size_t num_elements() const { return data_.size(); }
+  float *data() { return data_.data(); }
+  const float *data() const { return data_.data(); }
+  float &operator()(size_t r, size_t y, size_t x) { return data_[(r * shape_[1] + y) * shape_[2] + x]; }
+  float operator()(size_t r, size_t y, size_t x) const {
+    return data_[(r * shape_[1] + y) * shape_[2] + x];
+  }
+
+ private:
+  size_t shape_[3] = {0, 0, 0};
+  std::vector<float> data_;
+};
+
+// The ExpParam fields the path reads (libPartApp/ExpParam.proto).
+struct ExpParam {
+  int num_rotation_steps = 48;
+  float min_part_rotation = -180.f, max_part_rotation = 180.f;
+  float min_object_scale = 1.f, max_object_scale = 1.f;
+  float strip_border_detections = 0.f;
+  int roi_save_num_samples = 1000;
+  bool use_pairwise = true;
+  bool interpolate = false;
+  pa_exp_param c() const;
+};
+
+// PartConfig: which part is the root, which parts are upright.
+struct PartConfig {
+  int rootpart_idx = 0;
+  std::vector<int> is_upright;
+  int part_size() const { return (int)is_upright.size(); }
+};
+
+// struct Joint (libPictStruct/objectdetect.h:54-86) after loadJoints
+// (objectdetect_aux.cpp:54-141): 0-based part indices, radians.
+struct Joint {
+  int child_idx = -1, parent_idx = -1;
+  double offset_c[2] = {0, 0};  // parent_pos - child_pos (pixels)
+  double offset_p[2] = {0, 0};  // child_pos - parent_pos (pixels)
+  double C[4] = {1, 0, 0, 1};   // row-major 2x2 covariance
+  double rot_mean = 0, rot_sigma = 0;
+};
+
+// struct PartHyp (objectdetect.h:88-195).
+struct PartHyp {
+  int m_scaleidx = -1;
+  double m_scale = 0;
+  int m_rotidx = -1;
+  double m_rot = 0;  // degrees
+  int m_x = -1, m_y = -1;
+  float m_score = -1e6f;
+  std::vector<float> toVect() const;  // objectdetect.h:139-159
+};
+
+// One GPU context (device + stream + workspace).
+class Context {
+ public:
+  explicit Context(int device = 0);
+  ~Context();
+  Context(const Context &) = delete;
+  Context &operator=(const Context &) = delete;
+  pa_ctx *get() const { return ctx_; }
+  void check(pa_status s) const;  // throws Error with pa_last_error
+
+ private:
+  pa_ctx *ctx_ = nullptr;
+};
+
+// AdaBoostClassifier (libAdaBoost/AdaBoost.h) on the GPU: loaded from the
+// reference's text format (AdaBoost.cc:295-338) or from stump arrays.
+class AdaBoostClassifier {
+ public:
+  AdaBoostClassifier(Context &ctx, const std::string &text);
+  AdaBoostClassifier(Context &ctx, int dim, const std::vector<pa_stump> &stumps);
+  ~AdaBoostClassifier();
+  AdaBoostClassifier(const AdaBoostClassifier &) = delete;
+  AdaBoostClassifier &operator=(const AdaBoostClassifier &) = delete;
+  const pa_classifier *get() const { return cls_; }
+  int dim() const;
+  int size() const;
+  float sum_alpha() const;
+
+ private:
+  Context &ctx_;
+  pa_classifier *cls_ = nullptr;
+};
+
+// What the reference's PartApp carries for this path.
+struct PartApp {
+  ExpParam m_exp_param;
+  PartConfig m_part_conf;
+  std::vector<Joint> m_joints;                    // loadJoints output
+  std::vector<const AdaBoostClassifier *> m_abc;  // part detectors first
+};
+
+// computeRotJointMarginal (objectdetect_findrot.cpp:292-456): child ->
+// parent frame message.  bIsSparse must be false (the dense path).
+void computeRotJointMarginal(Context &ctx, const ExpParam &exp_param, FloatGrid3 &log_prob_child,
+                             FloatGrid3 &log_prob_parent, const double offset_c_10[2],
+                             const double offset_p_01[2], const double C[4], double rot_mean,
+                             double rot_sigma, double scale, bool bIsSparse);
+
+// computeRootPosteriorRot (objectdetect_findrot.cpp:470-727) including
+// computePartMarginals and findLocalMax.  log_part_detections[part][0] are
+// the log unaries (after clip_scores_fill + computeLogGrid); they are not
+// modified.  best_part_hyp[part] receives the local maxima of the part's
+// marginal (best first when more than roi_save_num_samples); if
+// log_marginals is given it receives the final log marginals per part.
+void computeRootPosteriorRot(Context &ctx, const PartApp &part_app,
+                             std::vector<std::vector<FloatGrid3>> &log_part_detections,
+                             FloatGrid3 &root_part_posterior, int rootpart_idx,
+                             std::vector<Joint> joints, bool flip, bool bIsSparse, int imgidx,
+                             std::vector<std::vector<PartHyp>> &best_part_hyp,
+                             bool bSaveMarginals,
+                             std::vector<FloatGrid3> *log_marginals = nullptr,
+                             std::vector<double> *log_z = nullptr);
+
+// computeScoreGrid (libPartDetect/partdetect_test.cpp:344-405) for every
+// classifier over dense window descriptors desc[field][ny][nx][dim]:
+// scores[c] = FloatGrid3(n_fields, ny, nx).
+void computeScoreGrids(Context &ctx, const std::vector<const AdaBoostClassifier *> &abc,
+                       const float *desc, int n_fields, int ny, int nx, int dim,
+                       bool bNormalizeBoost, std::vector<FloatGrid3> &scores);
+
+// Result of one image of findObjectImageRotJoints.
+struct FindObjResult {
+  std::vector<PartHyp> best_conf;                 // argmax per part
+  std::vector<std::vector<PartHyp>> part_hyps;    // local maxima per part
+  std::vector<std::vector<float>> root_hyps;      // (scale, x, y, score)
+  std::vector<double> log_z;                      // FP64 log-partition per part
+};
+
+// findObjectImageRotJoints (objectdetect_findrot.cpp:729-1058) with freshly
+// computed scores: unaries from descriptors desc[R][ny][nx][dim], grid ->
+// image transform Tig (3x3, row-major), PS, marginals, local maxima.
+FindObjResult findObjectImageRotJoints(Context &ctx, const PartApp &part_app, bool flip,
+                                       const float *desc, int ny, int nx, int dim,
+                                       const double Tig[9], int H, int W);
+
+// findObjectDataset (objectdetect_aux.cpp:322-406) over a batch of images
+// with the same sizes; joints[i] are image i's joints (per-image pairwise).
+std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_app, bool flip,
+                                             const std::vector<std::vector<Joint>> &joints,
+                                             const float *desc, int n_images, int ny, int nx,
+                                             int dim, const double Tig[9], int H, int W);
+
+}  // namespace partapp_gpu
+
+#endif  // PARTAPP_GPU_HPP_

@@ -1,0 +1,113 @@
+"""The C++ host layer (partapp_gb300/host) and its `partapp_find_obj
+--find_obj` CLI: the reference-shaped entry points over the C-ABI."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from partapp_gb300 import build, synth
+
+R, H, W, STRIDE, D = 12, 48, 64, 4, 96
+
+
+def cli():
+    build.build()
+    return build.CLI
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+
+    import partapp_gb300 as pa
+
+    build.build()
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    c = pa.Context(0)
+    yield c
+    c.close()
+
+
+def write_classifier(path, models, c):
+    """The reference's text model format (AdaBoost.cc:295-338)."""
+    n = models["f"].shape[1]
+    with open(path, "w") as fh:
+        fh.write(f"{models['D']}\n{n}\n")
+        for i in range(n):
+            fh.write("%d %.9g %.9g %.9g %.9g\n" % (models["f"][c, i], models["p"][c, i],
+                                                   models["alpha"][c, i], 0.0,
+                                                   models["theta"][c, i]))
+
+
+def write_joints(path, tree):
+    P = int(tree["n_parts"])
+    with open(path, "w") as fh:
+        fh.write(f"{P} {int(tree['root'])}\n")
+        fh.write(" ".join(str(int(u)) for u in tree["is_upright"]) + "\n")
+        for j in range(P - 1):
+            vals = [tree["offset_c"][j][0], tree["offset_c"][j][1], tree["offset_p"][j][0],
+                    tree["offset_p"][j][1], *tree["C"][j], tree["rot_mean"][j],
+                    tree["rot_sigma"][j]]
+            fh.write(f"{int(tree['child'][j])} {int(tree['parent'][j])} " +
+                     " ".join("%.17g" % v for v in vals) + "\n")
+
+
+def make_experiment(d, n_images=3):
+    imgs = [synth.make_image(500 + i, R=R, H=H, W=W, n_stumps=60, D=D, offset_range=(3, 8),
+                             sigma_range=(1, 2.5)) for i in range(n_images)]
+    models = imgs[0]["models"]
+    with open(os.path.join(d, "exp.txt"), "w") as fh:
+        for k, v in (("num_rotation_steps", R), ("min_part_rotation", -180),
+                     ("max_part_rotation", 180), ("object_scale", 1),
+                     ("strip_border_detections", 0), ("roi_save_num_samples", 50),
+                     ("use_pairwise", 1), ("interpolate", 1), ("height", H), ("width", W),
+                     ("grid_ny", H // STRIDE), ("grid_nx", W // STRIDE), ("dim", D),
+                     ("n_classifiers", models["f"].shape[0]), ("n_images", n_images)):
+            fh.write(f"{k} {v}\n")
+    with open(os.path.join(d, "tig.txt"), "w") as fh:
+        fh.write(" ".join("%.17g" % t for t in imgs[0]["Tig"].reshape(9)) + "\n")
+    write_joints(os.path.join(d, "joints.txt"), imgs[0]["tree"])
+    for i, im in enumerate(imgs):
+        write_joints(os.path.join(d, f"joints_{i}.txt"), im["tree"])
+        im["desc"].astype(np.float32).tofile(os.path.join(d, f"desc_{i}.bin"))
+    for c in range(models["f"].shape[0]):
+        write_classifier(os.path.join(d, f"class_{c}.txt"), models, c)
+    return imgs
+
+
+def test_cli_builds_and_prints_usage():
+    r = subprocess.run([cli(), "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "--find_obj" in r.stdout
+
+
+def test_cli_reports_a_missing_experiment(tmp_path):
+    r = subprocess.run([cli(), "--find_obj", "--expdir", str(tmp_path / "none")],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batch", [1, 3])
+def test_cli_find_obj_matches_c_abi(tmp_path, ctx, orc, batch):
+    """best_conf and log Z from the C++ CLI equal the C-ABI call through the
+    Python mirror bit for bit, and match the oracle's argmax."""
+    import partapp_gb300 as pa
+
+    imgs = make_experiment(str(tmp_path))
+    r = subprocess.run([cli(), "--find_obj", "--expdir", str(tmp_path), "--batch", str(batch)],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    cls = ctx.classifiers(imgs[0]["models"])
+    e = pa.exp_param(R=R, local_max=50, interpolate=True)
+    ref = ctx.find_obj_batch(e, [im["tree"] for im in imgs], cls,
+                             np.stack([im["desc"] for im in imgs]), imgs[0]["Tig"], H, W)
+    oe = orc.make_exp(R=R, max_local_max=50)
+    for i, im in enumerate(imgs):
+        got = np.loadtxt(tmp_path / f"best_conf_{i}.txt", dtype=np.float64).astype(np.float32)
+        assert np.array_equal(got, ref[i]["best_conf"])
+        lz = np.loadtxt(tmp_path / f"log_z_{i}.txt", dtype=np.float64)
+        assert np.array_equal(lz, np.asarray(ref[i]["log_z"], dtype=np.float64))
+        want = orc.find_obj(oe, im["tree"], imgs[0]["models"], im["desc"], im["Tig"], H, W)
+        for p in range(got.shape[0]):
+            assert tuple(got[p, [2, 4, 5]]) == tuple(want["best_conf"][p, [2, 4, 5]]), (i, p)
