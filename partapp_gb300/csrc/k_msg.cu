@@ -50,6 +50,17 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
   return d;
 }
 
+// Asynchronous 4-byte global -> shared copy; `valid` false writes a zero
+// and reads nothing (cp.async zero-fill).  All copies of a thread are in
+// flight until cp_async_wait_all.
+__device__ __forceinline__ void cp_async4(float *smem, const float *gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem),
+               "r"(valid ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Source index of a nearest-neighbour shift: a row of the exact table,
 // summarised by {c, lo, hi, uniform} when it is the plain shift
 // pos -> pos + c on [lo, hi) and -1 elsewhere (always, unless x + t lands
@@ -161,69 +172,61 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   }
   __syncthreads();
   {
-    // Thread tid stages word h = tid & 1 of pair-cells (p, x), walking the
-    // pair-cells in steps of blockDim.x / 2 (neighbouring threads write
-    // neighbouring words); four independent gathers in flight per thread.
-    constexpr int U = 4;
+    // Raw child values of the shifted rows land in E by asynchronous copies
+    // (all of a thread's copies in flight at once).  Cells without a source
+    // get LOG_ZERO, the dummy rotation of an odd R gets -inf (exp -> 0); the
+    // exp is taken when the rotation filter reads the column.  Thread tid
+    // stages word h = tid & 1 of pair-cells (p, x), walking the pair-cells in
+    // steps of blockDim.x / 2.
     float *Ef = reinterpret_cast<float *>(E);
     const int h = tid & 1, step = blockDim.x >> 1;
     int p = (tid >> 1) / W, x = (tid >> 1) - ((tid >> 1) / W) * W;
     while (p < RP) {
-      float lv[U];
-      int dst[U];
-      bool live[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        lv[u] = kLogZero;
-        dst[u] = -1;
-        live[u] = false;
-        if (p < RP) {
-          const int r = 2 * p + h;
-          dst[u] = (p * WP + padx + x) * 2 + h;
-          if (r < R) {
-            live[u] = true;
-            const int ro = rowoff[r];
-            const int sx = ro >= 0 ? shift_src(sdesc[r], md.tx_in + r * W, x) : -1;
-            if (sx >= 0) lv[u] = __ldg(md.in + (int64_t)ro + sx);
-          }
-          x += step;
-          while (x >= W) {
-            x -= W;
-            ++p;
-          }
-        }
+      const int r = 2 * p + h;
+      float *dst = Ef + (p * WP + padx + x) * 2 + h;
+      if (r >= R) {
+        *dst = -INFINITY;
+      } else {
+        const int ro = rowoff[r];
+        const int sx = ro >= 0 ? shift_src(sdesc[r], md.tx_in + r * W, x) : -1;
+        if (sx >= 0) cp_async4(dst, md.in + (int64_t)ro + sx, true);
+        else *dst = kLogZero;
       }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (dst[u] < 0) continue;
-        float v = 0.f;
-        if (live[u]) {
-          v = expf(__fadd_rn(lv[u], negM));
-          if (v == INFINITY) atomicOr(err, 1);
-        }
-        Ef[dst[u]] = v;
+      x += step;
+      while (x >= W) {
+        x -= W;
+        ++p;
       }
     }
+    cp_async_wait_all();
   }
   __syncthreads();
 
-  // (2) rotation filter, column by column, in place.
-  if (md.rlen == 0) {
+  // (2) E = exp(J10 - M), then the rotation filter, column by column, in place.
+  // rlen < 0: no rotation filter (rot_sigma == 0); rlen == 0: all-zero filter.
+  if (md.rlen <= 0) {
     for (int idx = tid; idx < RP * W; idx += blockDim.x) {
       const int p = idx / W, x = idx - p * W;
-      E[p * WP + padx + x] = make_float2(0.f, 0.f);
+      const float2 v = E[p * WP + padx + x];
+      const float2 ev = make_float2(expf(__fadd_rn(v.x, negM)), expf(__fadd_rn(v.y, negM)));
+      if (ev.x == INFINITY || ev.y == INFINITY) atomicOr(err, 1);
+      E[p * WP + padx + x] = md.rlen == 0 ? make_float2(0.f, 0.f) : ev;
     }
-  } else if (md.rlen > 0) {
+  }
+  if (md.rlen > 0) {
     const int nr = (md.rlen - 1) / 2;
     if constexpr (RT > 0) {
       for (int x = tid; x < W; x += blockDim.x) {
         float e[RT];
+        bool inf = false;
 #pragma unroll
         for (int p = 0; p < RT / 2; ++p) {
           const float2 v = E[p * WP + padx + x];
-          e[2 * p] = v.x;
-          e[2 * p + 1] = v.y;
+          e[2 * p] = expf(__fadd_rn(v.x, negM));
+          e[2 * p + 1] = expf(__fadd_rn(v.y, negM));
+          inf = inf || e[2 * p] == INFINITY || e[2 * p + 1] == INFINITY;
         }
+        if (inf) atomicOr(err, 1);
         if (!rot_filter_dispatch<RT, (RT - 1) / 2>(nr, e, E + padx + x, WP, tr)) atomicOr(err, 2);
       }
     } else {
@@ -231,7 +234,10 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
       float *Ef = reinterpret_cast<float *>(E);
       for (int x = tid; x < W; x += blockDim.x) {
         float *c = col + tid * R;
-        for (int r = 0; r < R; ++r) c[r] = Ef[((r >> 1) * WP + padx + x) * 2 + (r & 1)];
+        for (int r = 0; r < R; ++r) {
+          c[r] = expf(__fadd_rn(Ef[((r >> 1) * WP + padx + x) * 2 + (r & 1)], negM));
+          if (c[r] == INFINITY) atomicOr(err, 1);
+        }
         for (int r = 0; r < R; ++r) {
           float acc = 0.f;
           for (int j = 0; j < md.rlen; ++j) acc = fmaf(tr[j], c[wrap(r - nr + j, R)], acc);
@@ -382,27 +388,16 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
   const int64_t HW = (int64_t)H * W;
   const float *e2 = md.e2 + (int64_t)r * HW;
   if (any) {
-    // stage E2 rows [rmin - ky, rmax + ky] x columns [cmin, cmin + kCW), zero outside
-    constexpr int U = 4;
+    // stage E2 rows [rmin - ky, rmax + ky] x columns [cmin, cmin + kCW), zero
+    // outside, by asynchronous copies (all in flight at once)
     const int n = srows * kCW;
-    for (int base = tid; base < n; base += U * blockDim.x) {
-      float v[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int i = base + u * blockDim.x;
-        v[u] = 0.f;
-        if (i < n) {
-          const int sr = i / kCW, c = i - sr * kCW;
-          const int yy = rmin - ky + sr, xx = cmin + c;
-          if (yy >= 0 && yy < H && xx < W && xx <= cmax) v[u] = __ldg(e2 + (int64_t)yy * W + xx);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int i = base + u * blockDim.x;
-        if (i < n) S[i] = v[u];
-      }
+    for (int i = tid; i < n; i += blockDim.x) {
+      const int sr = i / kCW, c = i - sr * kCW;
+      const int yy = rmin - ky + sr, xx = cmin + c;
+      const bool ok = yy >= 0 && yy < H && xx < W && xx <= cmax;
+      cp_async4(S + i, ok ? e2 + (int64_t)yy * W + xx : e2, ok);
     }
+    cp_async_wait_all();
   }
   __syncthreads();
   if (any) {
