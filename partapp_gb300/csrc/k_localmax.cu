@@ -22,58 +22,78 @@ namespace {
 constexpr int kChunk = 4096;
 constexpr int kThreads = 1024;
 
-// Candidates of one (slice, 8-row x 32-column tile): the tile and a one-cell
-// halo of the slice are staged in shared memory, the adjacent slices are
-// read only at the cells that survive the in-slice test.
-constexpr int kTY = 8, kTX = 32;
+// Candidates of one slice: a warp walks kRowsPerWarp rows of a 32-column
+// strip with lane = column, holding the rows above, at and below the current
+// row in registers (each row is read once, coalesced); the left and right
+// neighbours come from the adjacent lanes, the strip's edge columns from two
+// extra loads.  Cells outside the grid read -inf, which never beats the
+// centre.  The adjacent slices are read only at cells that pass the in-slice
+// test.
+constexpr int kRowsPerWarp = 16;
+constexpr int kCandWarps = 8;
 
-__global__ void __launch_bounds__(256) k_lm_cand(const float *const *__restrict__ maps, int S,
-                                                 int H, int W,
-                                                 unsigned long long *__restrict__ keys,
-                                                 int64_t cap, int *__restrict__ counts) {
-  __shared__ float t[kTY + 2][kTX + 2];
-  const int map = blockIdx.z;
+struct LmRow {
+  float c, l, r;  // this lane's cell and its left / right neighbours
+};
+
+__device__ __forceinline__ LmRow lm_load_row(const float *gs, int y, int H, int W, int x,
+                                             int x0, int lane) {
+  LmRow o;
+  const bool in_row = y >= 0 && y < H;
+  const float *row = gs + (int64_t)y * W;
+  o.c = (in_row && x < W) ? __ldg(row + x) : -INFINITY;
+  float l = __shfl_up_sync(0xFFFFFFFFu, o.c, 1);
+  float r = __shfl_down_sync(0xFFFFFFFFu, o.c, 1);
+  if (lane == 0) l = (in_row && x0 > 0) ? __ldg(row + x0 - 1) : -INFINITY;
+  if (lane == 31) r = (in_row && x0 + 32 < W) ? __ldg(row + x0 + 32) : -INFINITY;
+  o.l = l;
+  o.r = (x + 1 < W) ? r : -INFINITY;
+  return o;
+}
+
+__global__ void __launch_bounds__(32 * kCandWarps) k_lm_cand(const float *const *__restrict__ maps,
+                                                             int S, int H, int W,
+                                                             unsigned long long *__restrict__ keys,
+                                                             int64_t cap, int *__restrict__ counts) {
+  const int map = blockIdx.z / S, s = blockIdx.z - (blockIdx.z / S) * S;
   const float *g = maps[map];
   const int64_t HW = (int64_t)H * W;
-  const int tiles_x = (W + kTX - 1) / kTX;
-  const int s = blockIdx.y;
-  const int ty0 = (blockIdx.x / tiles_x) * kTY, tx0 = (blockIdx.x % tiles_x) * kTX;
   const float *gs = g + (int64_t)s * HW;
-  for (int i = threadIdx.x; i < (kTY + 2) * (kTX + 2); i += blockDim.x) {
-    const int yy = ty0 - 1 + i / (kTX + 2), xx = tx0 - 1 + i % (kTX + 2);
-    // outside the grid: -inf never beats the centre (no strict neighbour test)
-    t[i / (kTX + 2)][i % (kTX + 2)] =
-        (yy >= 0 && yy < H && xx >= 0 && xx < W) ? __ldg(gs + (int64_t)yy * W + xx) : -INFINITY;
-  }
-  __syncthreads();
-  const int ly = threadIdx.x / kTX, lx = threadIdx.x % kTX;
-  const int y = ty0 + ly, x = tx0 + lx;
-  bool lm = false;
-  unsigned long long key = 0ull;
-  if (y < H && x < W) {
-    const float v = t[ly + 1][lx + 1];
-    lm = !(t[ly][lx] > v) && !(t[ly][lx + 1] > v) && !(t[ly][lx + 2] > v) &&
-         !(t[ly + 1][lx] > v) && !(t[ly + 1][lx + 2] > v) && !(t[ly + 2][lx] > v) &&
-         !(t[ly + 2][lx + 1] > v) && !(t[ly + 2][lx + 2] > v);
-    const int64_t i = (int64_t)s * HW + (int64_t)y * W + x;
-    if (lm && s > 0) lm = g[i - HW] < v;
-    if (lm && s < S - 1) lm = g[i + HW] < v;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x0 = blockIdx.x * 32, x = x0 + lane;
+  const int ya = (blockIdx.y * kCandWarps + warp) * kRowsPerWarp;
+  if (ya >= H) return;  // whole warp
+  const int yb = min(H, ya + kRowsPerWarp);
+  LmRow up = lm_load_row(gs, ya - 1, H, W, x, x0, lane);
+  LmRow cur = lm_load_row(gs, ya, H, W, x, x0, lane);
+  for (int y = ya; y < yb; ++y) {
+    const LmRow dn = lm_load_row(gs, y + 1, H, W, x, x0, lane);
+    const float v = cur.c;
+    bool lm = x < W && !(up.l > v) && !(up.c > v) && !(up.r > v) && !(cur.l > v) &&
+              !(cur.r > v) && !(dn.l > v) && !(dn.c > v) && !(dn.r > v);
+    unsigned long long key = 0ull;
     if (lm) {
-      const uint32_t e = (uint32_t)((int64_t)s * HW + (int64_t)x * H + y);
-      key = ((unsigned long long)ukey(v) << 32) | (unsigned long long)(0xFFFFFFFFu - e);
-      if (key == 0ull) lm = false;  // NaN: never ranked (reference comparisons are false)
+      const int64_t i = (int64_t)s * HW + (int64_t)y * W + x;
+      if (s > 0) lm = g[i - HW] < v;
+      if (lm && s < S - 1) lm = g[i + HW] < v;
+      if (lm) {
+        const uint32_t e = (uint32_t)((int64_t)s * HW + (int64_t)x * H + y);
+        key = ((unsigned long long)ukey(v) << 32) | (unsigned long long)(0xFFFFFFFFu - e);
+        if (key == 0ull) lm = false;  // NaN: never ranked (reference comparisons are false)
+      }
     }
-  }
-  const unsigned mask = __ballot_sync(0xFFFFFFFFu, lm);
-  if (mask) {
-    const int lane = threadIdx.x & 31;
-    int pos0 = 0;
-    if (lane == __ffs(mask) - 1) pos0 = atomicAdd(&counts[map], __popc(mask));
-    pos0 = __shfl_sync(0xFFFFFFFFu, pos0, __ffs(mask) - 1);
-    if (lm) {
-      const int64_t p = pos0 + __popc(mask & ((1u << lane) - 1u));
-      if (p < cap) keys[(int64_t)map * cap + p] = key;
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, lm);
+    if (mask) {
+      int pos0 = 0;
+      if (lane == __ffs(mask) - 1) pos0 = atomicAdd(&counts[map], __popc(mask));
+      pos0 = __shfl_sync(0xFFFFFFFFu, pos0, __ffs(mask) - 1);
+      if (lm) {
+        const int64_t q = pos0 + __popc(mask & ((1u << lane) - 1u));
+        if (q < cap) keys[(int64_t)map * cap + q] = key;
+      }
     }
+    up = cur;
+    cur = dn;
   }
 }
 
@@ -304,9 +324,11 @@ cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H,
   if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * 256 * n_maps, s);
   if (e != cudaSuccess) return e;
   k_lm_init<<<(n_maps + 127) / 128, 128, 0, s>>>(state, n_maps, k);
-  const int tiles = ((H + kTY - 1) / kTY) * ((W + kTX - 1) / kTX);
-  k_lm_cand<<<dim3((unsigned)tiles, (unsigned)S, (unsigned)n_maps), kTY * kTX, 0, s>>>(
-      maps, S, H, W, keys, cells, counts);
+  const int rows_per_cta = kCandWarps * kRowsPerWarp;
+  if ((int64_t)S * n_maps > 65535) return cudaErrorInvalidValue;
+  k_lm_cand<<<dim3((unsigned)((W + 31) / 32), (unsigned)((H + rows_per_cta - 1) / rows_per_cta),
+                   (unsigned)(S * n_maps)),
+              32 * kCandWarps, 0, s>>>(maps, S, H, W, keys, cells, counts);
   const int room = kChunk - k;
   for (int pass = 0; pass < kRadixPasses; ++pass)
     k_lm_radix<<<dim3(kRadixCtas, (unsigned)n_maps), 256, 0, s>>>(keys, counts, cells, pass, room,
