@@ -22,78 +22,85 @@ namespace {
 constexpr int kChunk = 4096;
 constexpr int kThreads = 1024;
 
-// Candidates of one slice: a warp walks kRowsPerWarp rows of a 32-column
-// strip with lane = column, holding the rows above, at and below the current
-// row in registers (each row is read once, coalesced); the left and right
-// neighbours come from the adjacent lanes, the strip's edge columns from two
-// extra loads.  Cells outside the grid read -inf, which never beats the
-// centre.  The adjacent slices are read only at cells that pass the in-slice
-// test.
-constexpr int kRowsPerWarp = 16;
-constexpr int kCandWarps = 8;
+// Candidates: a warp owns a block of kLmRows rows x 30 columns and walks all
+// S slices of it.  Lane l holds column x0 - 1 + l (lanes 0 and 31 are the
+// halo columns), so the left/right neighbours are lane shuffles; the rows
+// above and below are neighbouring registers.  Slices s - 1, s, s + 1 are in
+// registers while slice s + 2 is loaded, so every cell is read once and the
+// loads of the next slice are in flight while the current one is tested.
+// Cells outside the grid read -inf, which never beats the centre.
+constexpr int kLmRows = 12;            // output rows per warp
+constexpr int kLmCols = 30;            // output columns per warp
+constexpr int kLmWarps = 8;
+constexpr int kLmR = kLmRows + 2;      // rows held per slice (with halo)
 
-struct LmRow {
-  float c, l, r;  // this lane's cell and its left / right neighbours
-};
-
-__device__ __forceinline__ LmRow lm_load_row(const float *gs, int y, int H, int W, int x,
-                                             int x0, int lane) {
-  LmRow o;
-  const bool in_row = y >= 0 && y < H;
-  const float *row = gs + (int64_t)y * W;
-  o.c = (in_row && x < W) ? __ldg(row + x) : -INFINITY;
-  float l = __shfl_up_sync(0xFFFFFFFFu, o.c, 1);
-  float r = __shfl_down_sync(0xFFFFFFFFu, o.c, 1);
-  if (lane == 0) l = (in_row && x0 > 0) ? __ldg(row + x0 - 1) : -INFINITY;
-  if (lane == 31) r = (in_row && x0 + 32 < W) ? __ldg(row + x0 + 32) : -INFINITY;
-  o.l = l;
-  o.r = (x + 1 < W) ? r : -INFINITY;
-  return o;
+__device__ __forceinline__ void lm_load_slice(float (&v)[kLmR], const float *gs, int ya, int H,
+                                              int W, int x, bool on) {
+#pragma unroll
+  for (int j = 0; j < kLmR; ++j) {
+    const int y = ya - 1 + j;
+    v[j] = (on && y >= 0 && y < H && x >= 0 && x < W) ? __ldg(gs + (int64_t)y * W + x) : -INFINITY;
+  }
 }
 
-__global__ void __launch_bounds__(32 * kCandWarps) k_lm_cand(const float *const *__restrict__ maps,
-                                                             int S, int H, int W,
-                                                             unsigned long long *__restrict__ keys,
-                                                             int64_t cap, int *__restrict__ counts) {
-  const int map = blockIdx.z / S, s = blockIdx.z - (blockIdx.z / S) * S;
+__global__ void __launch_bounds__(32 * kLmWarps, 2) k_lm_cand(const float *const *__restrict__ maps,
+                                                           int S, int H, int W,
+                                                           unsigned long long *__restrict__ keys,
+                                                           int64_t cap, int *__restrict__ counts) {
+  const int map = blockIdx.z;
   const float *g = maps[map];
   const int64_t HW = (int64_t)H * W;
-  const float *gs = g + (int64_t)s * HW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int x0 = blockIdx.x * 32, x = x0 + lane;
-  const int ya = (blockIdx.y * kCandWarps + warp) * kRowsPerWarp;
-  if (ya >= H) return;  // whole warp
-  const int yb = min(H, ya + kRowsPerWarp);
-  LmRow up = lm_load_row(gs, ya - 1, H, W, x, x0, lane);
-  LmRow cur = lm_load_row(gs, ya, H, W, x, x0, lane);
-  for (int y = ya; y < yb; ++y) {
-    const LmRow dn = lm_load_row(gs, y + 1, H, W, x, x0, lane);
-    const float v = cur.c;
-    bool lm = x < W && !(up.l > v) && !(up.c > v) && !(up.r > v) && !(cur.l > v) &&
-              !(cur.r > v) && !(dn.l > v) && !(dn.c > v) && !(dn.r > v);
-    unsigned long long key = 0ull;
-    if (lm) {
-      const int64_t i = (int64_t)s * HW + (int64_t)y * W + x;
-      if (s > 0) lm = g[i - HW] < v;
-      if (lm && s < S - 1) lm = g[i + HW] < v;
+  const int x0 = blockIdx.x * kLmCols;
+  const int x = x0 - 1 + lane;
+  const int ya = (blockIdx.y * kLmWarps + warp) * kLmRows;
+  if (ya >= H) return;  // whole warp; no block-level synchronisation below
+  const bool out_lane = lane >= 1 && lane <= kLmCols && x < W;
+  float A[kLmR], B[kLmR], C[kLmR], D[kLmR];
+#pragma unroll
+  for (int j = 0; j < kLmR; ++j) A[j] = -INFINITY;
+  lm_load_slice(B, g, ya, H, W, x, true);
+  lm_load_slice(C, g + HW, ya, H, W, x, S > 1);
+  for (int s = 0; s < S; ++s) {
+    lm_load_slice(D, g + (int64_t)(s + 2) * HW, ya, H, W, x, s + 2 < S);
+    float bl[kLmR], br[kLmR];
+#pragma unroll
+    for (int j = 0; j < kLmR; ++j) {
+      bl[j] = __shfl_up_sync(0xFFFFFFFFu, B[j], 1);
+      br[j] = __shfl_down_sync(0xFFFFFFFFu, B[j], 1);
+    }
+#pragma unroll
+    for (int j = 1; j <= kLmRows; ++j) {
+      const int y = ya - 1 + j;
+      const float v = B[j];
+      bool lm = out_lane && y < H && !(B[j - 1] > v) && !(bl[j - 1] > v) && !(br[j - 1] > v) &&
+                !(bl[j] > v) && !(br[j] > v) && !(B[j + 1] > v) && !(bl[j + 1] > v) &&
+                !(br[j + 1] > v);
+      if (s > 0) lm = lm && A[j] < v;
+      if (s < S - 1) lm = lm && C[j] < v;
+      unsigned long long key = 0ull;
       if (lm) {
         const uint32_t e = (uint32_t)((int64_t)s * HW + (int64_t)x * H + y);
         key = ((unsigned long long)ukey(v) << 32) | (unsigned long long)(0xFFFFFFFFu - e);
-        if (key == 0ull) lm = false;  // NaN: never ranked (reference comparisons are false)
+        if (key == 0ull) lm = false;
+      }
+      const unsigned mask = __ballot_sync(0xFFFFFFFFu, lm);
+      if (mask) {
+        int pos0 = 0;
+        if (lane == __ffs(mask) - 1) pos0 = atomicAdd(&counts[map], __popc(mask));
+        pos0 = __shfl_sync(0xFFFFFFFFu, pos0, __ffs(mask) - 1);
+        if (lm) {
+          const int64_t q = pos0 + __popc(mask & ((1u << lane) - 1u));
+          if (q < cap) keys[(int64_t)map * cap + q] = key;
+        }
       }
     }
-    const unsigned mask = __ballot_sync(0xFFFFFFFFu, lm);
-    if (mask) {
-      int pos0 = 0;
-      if (lane == __ffs(mask) - 1) pos0 = atomicAdd(&counts[map], __popc(mask));
-      pos0 = __shfl_sync(0xFFFFFFFFu, pos0, __ffs(mask) - 1);
-      if (lm) {
-        const int64_t q = pos0 + __popc(mask & ((1u << lane) - 1u));
-        if (q < cap) keys[(int64_t)map * cap + q] = key;
-      }
+#pragma unroll
+    for (int j = 0; j < kLmR; ++j) {
+      A[j] = B[j];
+      B[j] = C[j];
+      C[j] = D[j];
     }
-    up = cur;
-    cur = dn;
   }
 }
 
@@ -324,11 +331,11 @@ cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H,
   if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * 256 * n_maps, s);
   if (e != cudaSuccess) return e;
   k_lm_init<<<(n_maps + 127) / 128, 128, 0, s>>>(state, n_maps, k);
-  const int rows_per_cta = kCandWarps * kRowsPerWarp;
-  if ((int64_t)S * n_maps > 65535) return cudaErrorInvalidValue;
-  k_lm_cand<<<dim3((unsigned)((W + 31) / 32), (unsigned)((H + rows_per_cta - 1) / rows_per_cta),
-                   (unsigned)(S * n_maps)),
-              32 * kCandWarps, 0, s>>>(maps, S, H, W, keys, cells, counts);
+  const int rows_per_cta = kLmWarps * kLmRows;
+  if (n_maps > 65535) return cudaErrorInvalidValue;
+  k_lm_cand<<<dim3((unsigned)((W + kLmCols - 1) / kLmCols),
+                   (unsigned)((H + rows_per_cta - 1) / rows_per_cta), (unsigned)n_maps),
+              32 * kLmWarps, 0, s>>>(maps, S, H, W, keys, cells, counts);
   const int room = kChunk - k;
   for (int pass = 0; pass < kRadixPasses; ++pass)
     k_lm_radix<<<dim3(kRadixCtas, (unsigned)n_maps), 256, 0, s>>>(keys, counts, cells, pass, room,

@@ -401,13 +401,16 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
   }
   __syncthreads();
   if (any) {
-    // y pass: lane = column, kNO consecutive rows per lane-task.
+    // y pass: lane = column, kNO consecutive rows per lane-task; the row
+    // chunks of the 32 strip columns are spread over all warps, the spare
+    // column (a strip that needs 33 source columns) gets a second round.
     const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int ncol = cmax - cmin + 1;
     const int nchunks = (nrows + kNO - 1) / kNO;
-    for (int task = warp; task < 2 * nchunks; task += nwarps) {
-      const int rr0 = (task >> 1) * kNO;
-      const int c = lane + 32 * (task & 1);
+    const int ntask = ncol > 32 ? 2 * nchunks : nchunks;
+    for (int task = warp; task < ntask; task += nwarps) {
+      const int rr0 = (task < nchunks ? task : task - nchunks) * kNO;
+      const int c = lane + (task < nchunks ? 0 : 32);
       if (c < ncol) {
         float acc[kNO];
 #pragma unroll
