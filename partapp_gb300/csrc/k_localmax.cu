@@ -29,10 +29,11 @@ constexpr int kThreads = 1024;
 // registers while slice s + 2 is loaded, so every cell is read once and the
 // loads of the next slice are in flight while the current one is tested.
 // Cells outside the grid read -inf, which never beats the centre.
-constexpr int kLmRows = 12;            // output rows per warp
+constexpr int kLmRows = 8;             // output rows per warp
 constexpr int kLmCols = 30;            // output columns per warp
 constexpr int kLmWarps = 8;
 constexpr int kLmR = kLmRows + 2;      // rows held per slice (with halo)
+constexpr int kLmBuf = 256;            // keys buffered per warp before a global append
 
 __device__ __forceinline__ void lm_load_slice(float (&v)[kLmR], const float *gs, int ya, int H,
                                               int W, int x, bool on) {
@@ -43,14 +44,29 @@ __device__ __forceinline__ void lm_load_slice(float (&v)[kLmR], const float *gs,
   }
 }
 
-__global__ void __launch_bounds__(32 * kLmWarps, 2) k_lm_cand(const float *const *__restrict__ maps,
+__global__ void __launch_bounds__(32 * kLmWarps, 3) k_lm_cand(const float *const *__restrict__ maps,
                                                            int S, int H, int W,
                                                            unsigned long long *__restrict__ keys,
                                                            int64_t cap, int *__restrict__ counts) {
+  __shared__ unsigned long long kbuf[kLmWarps][kLmBuf];
   const int map = blockIdx.z;
   const float *g = maps[map];
   const int64_t HW = (int64_t)H * W;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long *buf = kbuf[warp];
+  int nbuf = 0;  // warp-uniform
+  unsigned long long *dst = keys + (int64_t)map * cap;
+  // one global reservation for the warp's buffered keys, coalesced writes
+  auto flush = [&]() {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&counts[map], nbuf);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    __syncwarp();
+    for (int i = lane; i < nbuf; i += 32)
+      if ((int64_t)base + i < cap) dst[(int64_t)base + i] = buf[i];
+    __syncwarp();
+    nbuf = 0;
+  };
   const int x0 = blockIdx.x * kLmCols;
   const int x = x0 - 1 + lane;
   const int ya = (blockIdx.y * kLmWarps + warp) * kLmRows;
@@ -86,13 +102,9 @@ __global__ void __launch_bounds__(32 * kLmWarps, 2) k_lm_cand(const float *const
       }
       const unsigned mask = __ballot_sync(0xFFFFFFFFu, lm);
       if (mask) {
-        int pos0 = 0;
-        if (lane == __ffs(mask) - 1) pos0 = atomicAdd(&counts[map], __popc(mask));
-        pos0 = __shfl_sync(0xFFFFFFFFu, pos0, __ffs(mask) - 1);
-        if (lm) {
-          const int64_t q = pos0 + __popc(mask & ((1u << lane) - 1u));
-          if (q < cap) keys[(int64_t)map * cap + q] = key;
-        }
+        if (nbuf + 32 > kLmBuf) flush();
+        if (lm) buf[nbuf + __popc(mask & ((1u << lane) - 1u))] = key;
+        nbuf += __popc(mask);
       }
     }
 #pragma unroll
@@ -102,6 +114,8 @@ __global__ void __launch_bounds__(32 * kLmWarps, 2) k_lm_cand(const float *const
       C[j] = D[j];
     }
   }
+  __syncwarp();
+  if (nbuf) flush();
 }
 
 // Bitonic sort of kChunk keys in shared memory, descending.

@@ -133,12 +133,19 @@ __host__ __device__ __forceinline__ int align4(int n) { return (n + 3) & ~3; }
 template <int RT>
 __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(const MsgDesc *__restrict__ msgs,
                                                            int Rrt, int H, int W, int padx,
-                                                           int *err) {
+                                                           int cw, int *err) {
   const int R = RT > 0 ? RT : Rrt;
   const int RP = (R + 1) / 2;  // rotation pairs
   const MsgDesc md = msgs[blockIdx.y];
   const int y = blockIdx.x;
-  const int WP = rows_stride(W, padx);
+  // column chunk [xc0, xc0 + ncw) of the outputs; E holds its columns plus a
+  // padx halo on each side (local column lx <-> image column xc0 - padx + lx)
+  const int xc0 = blockIdx.z * cw;
+  const int ncw = min(cw, W - xc0);
+  const int WP = rows_stride(cw, padx);
+  const int gx0 = max(0, xc0 - padx), gx1 = min(W, xc0 + ncw + padx);  // gathered columns
+  const int lg0 = gx0 - xc0 + padx, lg1 = gx1 - xc0 + padx;            // their local range
+  const int gw = gx1 - gx0;
   extern __shared__ __align__(16) float sm[];
   float2 *E = reinterpret_cast<float2 *>(sm);  // [RP][WP] rotation pairs
   const int xpmax = ((2 * padx + 1 + kU - 1) / kU) * kU;
@@ -153,13 +160,14 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   }
   for (int i = tid; i < md.rlen; i += blockDim.x) tr[i] = md.rtaps[i];
 
-  // (1) stage exp(J10 - M) for all rotations of row y; zero padding.
+  // (1) stage exp(J10 - M) for all rotations of row y; zero outside the
+  // image (the reference's filter truncates at the border).
   const float negM = -fkey_decode(*md.in_max);
   const int HW = H * W;
-  const int pad_r = WP - padx - W;
-  for (int idx = tid; idx < RP * (padx + pad_r); idx += blockDim.x) {
-    const int p = idx / (padx + pad_r), k = idx - p * (padx + pad_r);
-    E[p * WP + (k < padx ? k : padx + W + (k - padx))] = make_float2(0.f, 0.f);
+  const int npad = WP - gw;
+  for (int idx = tid; idx < RP * npad; idx += blockDim.x) {
+    const int p = idx / npad, k = idx - p * npad;
+    E[p * WP + (k < lg0 ? k : lg1 + (k - lg0))] = make_float2(0.f, 0.f);
   }
   int4 *sdesc = reinterpret_cast<int4 *>(tr + kMaxRot + (RT == 0 ? kThreadsRows * R : 0));
   int *rowoff = reinterpret_cast<int *>(sdesc + 2 * R);  // [R] source row of rotation r, or -1
@@ -176,25 +184,26 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
     // (all of a thread's copies in flight at once).  Cells without a source
     // get LOG_ZERO, the dummy rotation of an odd R gets -inf (exp -> 0); the
     // exp is taken when the rotation filter reads the column.  Thread tid
-    // stages word h = tid & 1 of pair-cells (p, x), walking the pair-cells in
-    // steps of blockDim.x / 2.
+    // stages word h = tid & 1 of pair-cells (p, gx), walking the pair-cells
+    // in steps of blockDim.x / 2.
     float *Ef = reinterpret_cast<float *>(E);
     const int h = tid & 1, step = blockDim.x >> 1;
-    int p = (tid >> 1) / W, x = (tid >> 1) - ((tid >> 1) / W) * W;
+    int p = (tid >> 1) / gw, c = (tid >> 1) - ((tid >> 1) / gw) * gw;
     while (p < RP) {
       const int r = 2 * p + h;
-      float *dst = Ef + (p * WP + padx + x) * 2 + h;
+      const int gx = gx0 + c;
+      float *dst = Ef + (p * WP + lg0 + c) * 2 + h;
       if (r >= R) {
         *dst = -INFINITY;
       } else {
         const int ro = rowoff[r];
-        const int sx = ro >= 0 ? shift_src(sdesc[r], md.tx_in + r * W, x) : -1;
+        const int sx = ro >= 0 ? shift_src(sdesc[r], md.tx_in + r * W, gx) : -1;
         if (sx >= 0) cp_async4(dst, md.in + (int64_t)ro + sx, true);
         else *dst = kLogZero;
       }
-      x += step;
-      while (x >= W) {
-        x -= W;
+      c += step;
+      while (c >= gw) {
+        c -= gw;
         ++p;
       }
     }
@@ -205,66 +214,66 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   // (2) E = exp(J10 - M), then the rotation filter, column by column, in place.
   // rlen < 0: no rotation filter (rot_sigma == 0); rlen == 0: all-zero filter.
   if (md.rlen <= 0) {
-    for (int idx = tid; idx < RP * W; idx += blockDim.x) {
-      const int p = idx / W, x = idx - p * W;
-      const float2 v = E[p * WP + padx + x];
+    for (int idx = tid; idx < RP * gw; idx += blockDim.x) {
+      const int p = idx / gw, x = lg0 + idx - p * gw;
+      const float2 v = E[p * WP + x];
       const float2 ev = make_float2(expf(__fadd_rn(v.x, negM)), expf(__fadd_rn(v.y, negM)));
       if (ev.x == INFINITY || ev.y == INFINITY) atomicOr(err, 1);
-      E[p * WP + padx + x] = md.rlen == 0 ? make_float2(0.f, 0.f) : ev;
+      E[p * WP + x] = md.rlen == 0 ? make_float2(0.f, 0.f) : ev;
     }
   }
   if (md.rlen > 0) {
     const int nr = (md.rlen - 1) / 2;
     if constexpr (RT > 0) {
-      for (int x = tid; x < W; x += blockDim.x) {
+      for (int x = lg0 + tid; x < lg1; x += blockDim.x) {
         float e[RT];
         bool inf = false;
 #pragma unroll
         for (int p = 0; p < RT / 2; ++p) {
-          const float2 v = E[p * WP + padx + x];
+          const float2 v = E[p * WP + x];
           e[2 * p] = expf(__fadd_rn(v.x, negM));
           e[2 * p + 1] = expf(__fadd_rn(v.y, negM));
           inf = inf || e[2 * p] == INFINITY || e[2 * p + 1] == INFINITY;
         }
         if (inf) atomicOr(err, 1);
-        if (!rot_filter_dispatch<RT, (RT - 1) / 2>(nr, e, E + padx + x, WP, tr)) atomicOr(err, 2);
+        if (!rot_filter_dispatch<RT, (RT - 1) / 2>(nr, e, E + x, WP, tr)) atomicOr(err, 2);
       }
     } else {
       float *col = tr + kMaxRot;  // [blockDim.x][R] scratch
       float *Ef = reinterpret_cast<float *>(E);
-      for (int x = tid; x < W; x += blockDim.x) {
+      for (int x = lg0 + tid; x < lg1; x += blockDim.x) {
         float *c = col + tid * R;
         for (int r = 0; r < R; ++r) {
-          c[r] = expf(__fadd_rn(Ef[((r >> 1) * WP + padx + x) * 2 + (r & 1)], negM));
+          c[r] = expf(__fadd_rn(Ef[((r >> 1) * WP + x) * 2 + (r & 1)], negM));
           if (c[r] == INFINITY) atomicOr(err, 1);
         }
         for (int r = 0; r < R; ++r) {
           float acc = 0.f;
           for (int j = 0; j < md.rlen; ++j) acc = fmaf(tr[j], c[wrap(r - nr + j, R)], acc);
-          Ef[((r >> 1) * WP + padx + x) * 2 + (r & 1)] = acc;
+          Ef[((r >> 1) * WP + x) * 2 + (r & 1)] = acc;
         }
       }
     }
   }
   __syncthreads();
 
-  // (3) x pass: a task is (rotation pair, strip of 32 * kNO columns); lane l
-  // owns outputs [l*kNO, l*kNO + kNO) of the strip for both rotations.  The
-  // results go through a per-warp shared row so that each store instruction
-  // writes 32 consecutive floats.
+  // (3) x pass over the chunk's outputs: a task is (rotation pair, strip of
+  // 32 * kNO columns); lane l owns outputs [l*kNO, l*kNO + kNO) of the strip
+  // for both rotations.  The results go through a per-warp shared row so that
+  // each store instruction writes 32 consecutive floats.
   const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int kx = (md.xlen - 1) / 2;
   float *e2 = md.e2;
   float *ws = ostage + warp * (32 * kNO);
-  const int nstrips = (W + 32 * kNO - 1) / (32 * kNO);
+  const int nstrips = (ncw + 32 * kNO - 1) / (32 * kNO);
   for (int task = warp; task < RP * nstrips; task += nwarps) {
     const int p = task / nstrips;
-    const int xs = (task - p * nstrips) * 32 * kNO;
+    const int xs = (task - p * nstrips) * 32 * kNO;  // chunk-relative
     const int x0 = xs + lane * kNO;
     float2 acc[kNO];
 #pragma unroll
     for (int i = 0; i < kNO; ++i) acc[i] = make_float2(0.f, 0.f);
-    if (x0 < W) {
+    if (x0 < ncw) {
       const float2 *row = E + p * WP + padx - kx + x0;
       for (int kb = 0; kb < xpad; kb += kU) {
         float2 v[kNO + kU - 1];
@@ -278,8 +287,8 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
         }
       }
     }
-    const int nx = min(32 * kNO, W - xs);
-    float *o = e2 + (int64_t)(2 * p) * HW + (int64_t)y * W + xs;
+    const int nx = min(32 * kNO, ncw - xs);
+    float *o = e2 + (int64_t)(2 * p) * HW + (int64_t)y * W + xc0 + xs;
 #pragma unroll
     for (int i = 0; i < kNO; ++i) ws[lane * kNO + i] = acc[i].x;  // odd kNO: conflict-free
     __syncwarp();
@@ -577,19 +586,42 @@ __global__ void k_shift_desc(const int16_t *__restrict__ tables, int n_msgs, int
 }
 
 template <int RT>
-cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
-                          int *err, cudaStream_t s) {
-  const int WP = rows_stride(W, padx);
+size_t rows_smem(int R, int cw, int padx) {
+  const int WP = rows_stride(cw, padx);
   const int RP = (R + 1) / 2;
   size_t smem = ((size_t)2 * ((RP * WP + 1) & ~1) + 2 * ((2 * padx + 1 + kU - 1) / kU) * kU + kMaxRot) *
                 sizeof(float);
   if (RT == 0) smem += (size_t)kThreadsRows * R * sizeof(float);
   smem += (size_t)2 * R * sizeof(int4) + (size_t)align4(R) * sizeof(int) +
           (size_t)(kThreadsRows / 32) * 32 * kNO * sizeof(float);
-  if (smem > 227 * 1024 || (int64_t)R * H * W >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
+  return smem;
+}
+
+// Column chunk of the row kernel: the whole row when two CTAs fit on an SM
+// (one for R = 48), else the widest chunk that does (a multiple of 32 * kNO
+// outputs, at least one strip), else the widest that fits at all.
+template <int RT>
+int rows_chunk(int R, int W, int padx) {
+  const size_t target = (RT == 48 ? 227 : 113) * 1024;
+  if (rows_smem<RT>(R, W, padx) <= target) return W;
+  for (size_t lim : {target, (size_t)227 * 1024}) {
+    int best = 0;
+    for (int cw = 32 * kNO; cw < W; cw += 32 * kNO)
+      if (rows_smem<RT>(R, cw, padx) <= lim) best = cw;
+    if (best) return best;
+  }
+  return 0;
+}
+
+template <int RT>
+cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
+                          int *err, cudaStream_t s) {
+  const int cw = rows_chunk<RT>(R, W, padx);
+  if (cw <= 0 || (int64_t)R * H * W >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
+  const size_t smem = rows_smem<RT>(R, cw, padx);
   cudaFuncSetAttribute(k_msg_rows<RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 grid((unsigned)H, (unsigned)n_msgs);
-  k_msg_rows<RT><<<grid, kThreadsRows, smem, s>>>(msgs, R, H, W, padx, err);
+  dim3 grid((unsigned)H, (unsigned)n_msgs, (unsigned)((W + cw - 1) / cw));
+  k_msg_rows<RT><<<grid, kThreadsRows, smem, s>>>(msgs, R, H, W, padx, cw, err);
   return cudaGetLastError();
 }
 

@@ -189,6 +189,27 @@ def test_rot_joint_marginal(ctx, orc, R):
         assert maxnorm_err(got, want64) <= 1e-4
 
 
+@pytest.mark.parametrize("R,W", [(48, 1100), (16, 1500)])
+def test_rot_joint_marginal_wide_rows(ctx, orc, R, W):
+    """Rows too wide for one shared-memory row (wide x kernels, sigma up to
+    24 px as in the 1024x1024 workload): the row pass runs in column chunks
+    with a halo and must equal the oracle as the single-chunk path does."""
+    rng = np.random.default_rng(77 + R)
+    H = 20
+    child = synth.random_log_unary(rng, 1, R, H, W, zero_frac=0.01)[0]
+    step = synth.rot_step_rad(R)
+    for k, rs, oc, op, sig in [(1, 1.7, (31.0, -12.5), (-20.25, 7.5), (24.0, 3.0)),
+                               (0, 2.2, (-55.5, 4.0), (40.0, -2.0), (9.0, 1.5))]:
+        e = orc.make_exp(R=R)
+        args = (np.array(oc), np.array(op), np.diag([sig[0] ** 2, sig[1] ** 2]), k * step,
+                rs * step)
+        want = orc.rot_joint_marginal(e, child, *args)
+        got = ctx.rot_joint_marginal(_pa_exp(R), child, *args)
+        oob = want == LOG_ZERO
+        assert np.array_equal(got[oob], want[oob])
+        assert maxnorm_err(got, want) <= 1e-5
+
+
 def _pa_exp(R, **kw):
     import partapp_gb300
 
