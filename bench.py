@@ -42,10 +42,11 @@ WORKLOAD = "find_obj 640x480, R=24, 22x500-stump AdaBoost over 960-d descriptors
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=4, help="images per step")
-    ap.add_argument("--e2e-batch", type=int, default=4)
+    ap.add_argument("--e2e-batch", type=int, default=8,
+                    help="images per end-to-end call (host descriptors through the copy ring)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -101,6 +102,10 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()  # the sampler is running before the timed region starts
+            while not self.rows and time.time() - t0 < 5.0:
+                time.sleep(0.02)
+            self.rows.clear()
         except OSError:
             self.proc = None
         return self
@@ -260,14 +265,14 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     B = args.batch
     models = make_models(args.seed)
-    trees = make_trees(args.seed + 97 * rank, B)
+    trees = make_trees(args.seed + 97 * rank, max(B, args.e2e_batch))
     cls = ctx.classifiers(models)
     desc = device_descriptors(B, args.seed + 7919 * rank, dev)
     Tig = synth.grid_to_image(STRIDE)
     e = pa.exp_param(R=R, interpolate=True)
 
     def step():
-        return ctx.find_obj_batch(e, trees, cls, desc, Tig, H, W)
+        return ctx.find_obj_batch(e, trees[:B], cls, desc, Tig, H, W)
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -313,9 +318,10 @@ def run_ours(args):
             kernels[k]["GB/s"] = alg[k] / (ktimes[k][0] / args.steps / 1e3) / 1e9
 
     # end to end through the same C-ABI call with pinned host buffers
-    Be = min(args.e2e_batch, B)
+    Be = args.e2e_batch
     host = torch.empty((Be, R, NY, NX, D), dtype=torch.float32, pin_memory=True)
-    host.copy_(desc[:Be])
+    for i in range(Be):  # the device images, repeated: the copy is what is timed
+        host[i].copy_(desc[i % B])
     host_np = host.numpy()
 
     def step_e2e():

@@ -202,15 +202,18 @@ typedef struct {
  * border strip are applied inside, as in the reference.  `flip` applies
  * loadJoints' mirroring (objectdetect_aux.cpp:98-116) to the joints.
  * Supported trees: the root may have any number of children, every other
- * part at most one (the reference asserts this at :210); covariances must be
- * diagonal (gaussFilterDiag2d); PA_ERR_UNSUPPORTED otherwise.
+ * part at most one (the reference asserts this at :210); PA_ERR_UNSUPPORTED
+ * otherwise.  Covariances must be symmetric positive definite: diagonal ones
+ * take gaussFilterDiag2d, others gaussFilter2dOffset (rotation into the
+ * eigenbasis, libMultiArray/multi_array_filter.hpp:335-369).
  *   log_unary [P][R][H][W] */
 pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
                       const float *log_unary, int H, int W, const pa_ps_outputs *out,
                       int mem);
 
 /* computeRotJointMarginal (objectdetect_findrot.cpp:292-456): one message
- * child -> parent frame.  child, parent [R][H][W]. */
+ * child -> parent frame, dense path (bIsSparse = false).  child, parent
+ * [R][H][W]; C as in pa_ps_infer. */
 pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float *child,
                                 float *parent, int R, int H, int W, const double *offset_c,
                                 const double *offset_p, const double *C, double rot_mean,
@@ -225,7 +228,9 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
  * pointers; `stream` is a cudaStream_t (NULL: the legacy default stream) and
  * the call returns after the work on it has finished.
  * Limits: R*H*W <= PA_NOALLOC_MAX_CELLS, R <= 64, H + W <= 4096, at most
- * 1024 spatial taps per axis; larger sizes return PA_ERR_NOMEM.
+ * 1024 spatial taps per axis; larger sizes return PA_ERR_NOMEM.  C must be
+ * diagonal (PA_ERR_UNSUPPORTED otherwise: the rotated-grid path of a full
+ * covariance needs scratch sized by the rotation).
  * Calls share the array: calls whose GPU work overlaps race.  The first call
  * on a device looks up the array's address; make it before any stream
  * capture. */

@@ -114,6 +114,8 @@ def _declare(L):
     L.orc_clip_log.restype = None
     L.orc_gaussian_filter.argtypes = [C.c_double, dp]
     L.orc_gaussian_filter.restype = C.c_int
+    L.orc_eig2d.argtypes = [dp, dp, dp]
+    L.orc_eig2d.restype = None
     for suf, t in (("f32", fp), ("f64", dp)):
         fn = getattr(L, "orc_rot_joint_marginal_" + suf)
         fn.argtypes = [C.POINTER(OrcExp), t, t, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.c_double,
@@ -237,6 +239,16 @@ def clip_log(grid):
     g = np.array(grid, dtype=np.float32, copy=True, order="C")
     lib().orc_clip_log(_p(g, C.c_float), g.size)
     return g
+
+
+def eig2d(M):
+    """boost_math::eig2d of a symmetric 2x2 matrix: (V, E) with V's columns
+    the eigenvectors and E = (smallest, largest) eigenvalue."""
+    m = np.ascontiguousarray(M, dtype=np.float64).reshape(4)
+    V = np.zeros(4)
+    E = np.zeros(2)
+    lib().orc_eig2d(_p(m, C.c_double), _p(V, C.c_double), _p(E, C.c_double))
+    return V.reshape(2, 2), E
 
 
 def gaussian_filter(sigma):

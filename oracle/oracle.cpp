@@ -135,7 +135,152 @@ template <class T> void log_grid(T *d, size_t n) {
   for (size_t i = 0; i < n; ++i) d[i] = (d[i] == 0) ? (T)LOG_ZERO : Num<T>::lg(d[i]);
 }
 
-/* computeRotJointMarginal, objectdetect_findrot.cpp:292-456 (diagonal C). */
+/* hc::inverse, libBoostMath/homogeneous_coord.cpp:49-69 */
+void hc_inverse3(const double *T, double *I) {
+  double D = T[0] * T[4] - T[3] * T[1];
+  I[0] = T[4] / D;
+  I[1] = -T[1] / D;
+  I[3] = -T[3] / D;
+  I[4] = T[0] / D;
+  double t0 = I[0] * T[2] + I[1] * T[5];
+  double t1 = I[3] * T[2] + I[4] * T[5];
+  I[2] = -t0;
+  I[5] = -t1;
+  I[6] = 0;
+  I[7] = 0;
+  I[8] = 1;
+}
+
+/* ublas prod of two 3x3 matrices (row-major): C(i,j) = sum_k A(i,k) B(k,j),
+ * accumulated k = 0, 1, 2. */
+void prod3(const double *A, const double *B, double *Cm) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double t = 0;
+      for (int k = 0; k < 3; ++k) t += A[3 * i + k] * B[3 * k + j];
+      Cm[3 * i + j] = t;
+    }
+}
+
+/* boost_math::eig2d, libBoostMath/boost_math.cpp:40-99: E = (smallest,
+ * largest) eigenvalue, V columns = eigenvectors, V(0,0) = v11. */
+void eig2d(const double *M, double *V, double *E) {
+  double m11 = M[0], m12 = M[1], m22 = M[3];
+  double e1, e2, v11, v21;
+  if (m12 != 0) {
+    double sqrtD = std::sqrt((m11 - m22) * (m11 - m22) + 4 * m12 * m12);
+    e1 = 0.5 * (m11 + m22 - sqrtD);
+    e2 = 0.5 * (m11 + m22 + sqrtD);
+    v11 = 0.5 * (m11 - m22 - sqrtD) / m12;
+    v21 = 1;
+  } else if (m11 < m22) {
+    e1 = m11; e2 = m22; v11 = 1; v21 = 0;
+  } else {
+    e1 = m22; e2 = m11; v11 = 0; v21 = 1;
+  }
+  double norm_v1 = std::sqrt(v11 * v11 + v21 * v21);
+  v11 /= norm_v1;
+  v21 /= norm_v1;
+  V[0] = v11;   /* V(0,0) */
+  V[1] = -v21;  /* V(0,1) = v12 */
+  V[2] = v21;   /* V(1,0) */
+  V[3] = v11;   /* V(1,1) = v22 */
+  E[0] = e1;
+  E[1] = e2;
+}
+
+/* hc::get_transformed_bbox, homogeneous_coord.cpp:140-156 */
+void transformed_bbox(const double *T21, int in_w, int in_h, double &minx, double &miny,
+                      double &maxx, double &maxy) {
+  const double px[4] = {0, (double)(in_w - 1), 0, (double)(in_w - 1)};
+  const double py[4] = {0, 0, (double)(in_h - 1), (double)(in_h - 1)};
+  double xs[4], ys[4];
+  for (int c = 0; c < 4; ++c) {
+    xs[c] = T21[0] * px[c] + T21[1] * py[c] + T21[2] * 1.0;
+    ys[c] = T21[3] * px[c] + T21[4] * py[c] + T21[5] * 1.0;
+  }
+  minx = *std::min_element(xs, xs + 4);
+  maxx = *std::max_element(xs, xs + 4);
+  miny = *std::min_element(ys, ys + 4);
+  maxy = *std::max_element(ys, ys + 4);
+}
+
+/* The bilinear branch of transform_grid_helper
+ * (multi_array_transform.hpp:194-238) with the output -> input map T13
+ * given: exact-hit shortcut, last row/column left at the default. */
+template <class T>
+void bilinear_map(const T *gin, int in_h, int in_w, T *gout, int out_h, int out_w,
+                  const double *T13, T def) {
+  const T eps10 = 10 * std::numeric_limits<T>::epsilon();
+  for (int x3 = 0; x3 < out_w; ++x3)
+    for (int y3 = 0; y3 < out_h; ++y3) {
+      T o = def;
+      double x1 = T13[0] * x3 + T13[1] * y3 + T13[2];
+      double y1 = T13[3] * x3 + T13[4] * y3 + T13[5];
+      int ix1 = (int)std::floor(x1), iy1 = (int)std::floor(y1);
+      if (ix1 >= 0 && ix1 < in_w && iy1 >= 0 && iy1 < in_h) {
+        T a = (T)(x1 - ix1), b = (T)(y1 - iy1);
+        if (a < eps10 && b < eps10) {
+          o = gin[(size_t)iy1 * in_w + ix1];
+        } else if (ix1 < in_w - 1 && iy1 < in_h - 1) {
+          const T *g0 = gin + (size_t)iy1 * in_w + ix1, *g1 = g0 + in_w;
+          const T one = 1;
+          o = (one - b) * (one - a) * g0[0] + (one - b) * a * g0[1] + b * (one - a) * g1[0] +
+              b * a * g1[1];
+        }
+      }
+      gout[(size_t)y3 * out_w + x3] = o;
+    }
+}
+
+/* gaussFilterDiag2d, multi_array_filter.hpp:212-321: x pass then y pass,
+ * taps truncated at the border, sequential float dots. */
+template <class T>
+void gauss_diag(const T *in, T *out, int H, int W, double sigma_x, double sigma_y) {
+  std::vector<double> fxd = gaussian_filter(sigma_x), fyd = gaussian_filter(sigma_y);
+  std::vector<T> fx(fxd.begin(), fxd.end()), fy(fyd.begin(), fyd.end());
+  const int kx = ((int)fx.size() - 1) / 2, ky = ((int)fy.size() - 1) / 2;
+  std::vector<T> sm((size_t)H * W);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      int n1 = std::max(0, x - kx), n2 = std::min(W - 1, x + kx);
+      sm[(size_t)y * W + x] = dot(n2 - n1 + 1, in + (size_t)y * W + n1, 1, fx.data() + (n1 - (x - kx)));
+    }
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      int n1 = std::max(0, y - ky), n2 = std::min(H - 1, y + ky);
+      out[(size_t)y * W + x] = dot(n2 - n1 + 1, sm.data() + (size_t)n1 * W + x, W, fy.data() + (n1 - (y - ky)));
+    }
+}
+
+/* gaussFilter2dOffset with a zero offset, multi_array_filter.hpp:335-369
+ * (the dense path: bilinear forward rotation). */
+template <class T>
+void gauss_full(const T *in, T *out, int H, int W, const double *Cs) {
+  double V[4], E[2];
+  eig2d(Cs, V, E);
+  const double T21[9] = {V[0], V[2], 0, V[1], V[3], 0, 0, 0, 1};  /* [trans(V) | 0] */
+  double minx, miny, maxx, maxy;
+  transformed_bbox(T21, W, H, minx, miny, maxx, maxy);
+  const int ow = (int)std::ceil(maxx - minx), oh = (int)std::ceil(maxy - miny);
+  const double T23[9] = {1, 0, minx, 0, 1, miny, 0, 0, 1};
+  double T12[9], T13[9];
+  hc_inverse3(T21, T12);
+  prod3(T12, T23, T13);
+  std::vector<T> g((size_t)oh * ow), gs((size_t)oh * ow);
+  bilinear_map(in, H, W, g.data(), oh, ow, T13, (T)0);
+  gauss_diag(g.data(), gs.data(), oh, ow, std::sqrt(E[0]), std::sqrt(E[1]));
+  const double mz = -0.0;
+  const double T42[9] = {V[0], V[1], mz, V[2], V[3], mz, 0, 0, 1};
+  double T43[9], Tb[9], Tbb[9];
+  prod3(T42, T23, T43);
+  hc_inverse3(T43, Tb);
+  const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  prod3(Tb, I3, Tbb);
+  bilinear_map(gs.data(), oh, ow, out, H, W, Tbb, (T)0);
+}
+
+/* computeRotJointMarginal, objectdetect_findrot.cpp:292-456. */
 template <class T>
 int rot_joint_marginal(const orc_exp *e, const T *child, T *parent, int R, int H,
                        int W, const double *oc, const double *op,
@@ -143,8 +288,9 @@ int rot_joint_marginal(const orc_exp *e, const T *child, T *parent, int R, int H
                        double scale) {
   const size_t HW = (size_t)H * W, N = HW * R;
   if (R < 2 || H < 1 || W < 1) return -1;
-  if (C[1] != 0 || C[2] != 0) return -2; /* full covariance: gaussFilter2dOffset */
-  if (!(C[0] > 0 && C[3] > 0)) return -1;
+  const bool diag = (C[1] == 0 && C[2] == 0);
+  if (!diag && C[1] != C[2]) return -1; /* eig2d asserts symmetry */
+  if (diag && !(C[0] > 0 && C[3] > 0)) return -1;
 
   /* getMinMax, multi_array_op.hpp:61-77 */
   T in_M = -std::numeric_limits<T>::infinity();
@@ -206,25 +352,14 @@ int rot_joint_marginal(const orc_exp *e, const T *child, T *parent, int R, int H
   /* x/y dimensions: gaussFilter2d -> gaussFilterDiag2d, :423-429 and
    * multi_array_filter.hpp:212-321, 375-388 */
   const double sc2 = scale * scale;
-  const double sigma_x = std::sqrt(sc2 * C[0]);
-  const double sigma_y = std::sqrt(sc2 * C[3]);
-  std::vector<double> fxd = gaussian_filter(sigma_x), fyd = gaussian_filter(sigma_y);
-  std::vector<T> fx(fxd.begin(), fxd.end()), fy(fyd.begin(), fyd.end());
-  const int kx = ((int)fx.size() - 1) / 2, ky = ((int)fy.size() - 1) / 2;
-  std::vector<T> sm(HW);
+  const double Cs[4] = {sc2 * C[0], sc2 * C[1], sc2 * C[2], sc2 * C[3]};  /* square(scale)*C */
   for (int r = 0; r < R; ++r) {
     const T *in = rot_res.data() + r * HW;
     T *out = j01.data() + r * HW;
-    for (int y = 0; y < H; ++y)
-      for (int x = 0; x < W; ++x) {
-        int n1 = std::max(0, x - kx), n2 = std::min(W - 1, x + kx);
-        sm[(size_t)y * W + x] = dot(n2 - n1 + 1, in + (size_t)y * W + n1, 1, fx.data() + (n1 - (x - kx)));
-      }
-    for (int y = 0; y < H; ++y)
-      for (int x = 0; x < W; ++x) {
-        int n1 = std::max(0, y - ky), n2 = std::min(H - 1, y + ky);
-        out[(size_t)y * W + x] = dot(n2 - n1 + 1, sm.data() + (size_t)n1 * W + x, W, fy.data() + (n1 - (y - ky)));
-      }
+    if (diag)
+      gauss_diag(in, out, H, W, std::sqrt(Cs[0]), std::sqrt(Cs[3]));
+    else
+      gauss_full(in, out, H, W, Cs);
   }
 
   /* computeLogGrid + addGrid1(in_M), :432-435 */
@@ -620,6 +755,8 @@ void orc_clip_log(float *grid, int64_t n) {
     if (grid[i] < 0) grid[i] = (float)0.0001;
   log_grid(grid, (size_t)n);
 }
+
+void orc_eig2d(const double *M, double *V, double *E) { eig2d(M, V, E); }
 
 int orc_gaussian_filter(double sigma, double *out) {
   std::vector<double> f = gaussian_filter(sigma);

@@ -100,6 +100,9 @@ void orc_clip_log(float *grid, int64_t n);
  * Writes 2*ksize+1 taps (ksize = floor(3*sigma+0.5)) and returns their
  * count; out must hold at least that many. */
 int orc_gaussian_filter(double sigma, double *out);
+/* boost_math::eig2d (libBoostMath/boost_math.cpp:40-99): V row-major 2x2,
+ * E = (smallest, largest) eigenvalue. */
+void orc_eig2d(const double *M, double *V, double *E);
 
 /* computeRotJointMarginal (libPictStruct/objectdetect_findrot.cpp:292-456). */
 int orc_rot_joint_marginal_f32(const orc_exp *e, const float *child,

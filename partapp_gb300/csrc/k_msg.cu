@@ -33,6 +33,7 @@ constexpr int kNO = 11;   // outputs per lane in the row/column passes (odd: con
 constexpr int kU = 8;     // taps per unrolled block
 constexpr int kTX = 32;   // parent columns per k_msg_cols CTA
 constexpr int kCW = 33;   // staged source columns (one spare for rounding glitches)
+constexpr int kMaxFullTaps = 2048;  // spatial taps of a full-covariance message (sigma <= 341 px)
 
 __device__ __forceinline__ int wrap(int r, int R) { return r < 0 ? r + R : (r >= R ? r - R : r); }
 
@@ -150,7 +151,9 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   float2 *E = reinterpret_cast<float2 *>(sm);  // [RP][WP] rotation pairs
   const int xpmax = ((2 * padx + 1 + kU - 1) / kU) * kU;
   float2 *tx = E + ((RP * WP + 1) & ~1);     // x taps {t, t}, zero-padded, 16B aligned
-  const int xpad = ((md.xlen + kU - 1) / kU) * kU;
+  // x taps (none for a full-covariance message: its spatial filter runs on
+  // the rotated grid, and the phase's padx does not cover its kernel)
+  const int xpad = md.full ? 0 : ((md.xlen + kU - 1) / kU) * kU;
   float *tr = reinterpret_cast<float *>(tx + xpmax);  // rotation taps
   const int tid = threadIdx.x;
 
@@ -257,6 +260,17 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   }
   __syncthreads();
 
+  if (md.full) {
+    // full covariance: the rotation-filtered exp map of the chunk goes out
+    // as is; the spatial filter runs on the rotated grid (k_full_*)
+    const float *Ef = reinterpret_cast<const float *>(E);
+    for (int idx = tid; idx < R * ncw; idx += blockDim.x) {
+      const int r = idx / ncw, j = idx - r * ncw;
+      md.e2[(int64_t)r * HW + (int64_t)y * W + xc0 + j] = Ef[((r >> 1) * WP + padx + j) * 2 + (r & 1)];
+    }
+    return;
+  }
+
   // (3) x pass over the chunk's outputs: a task is (rotation pair, strip of
   // 32 * kNO columns); lane l owns outputs [l*kNO, l*kNO + kNO) of the strip
   // for both rotations.  The results go through a per-warp shared row so that
@@ -329,10 +343,97 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return v;
 }
 
+// ---------------------------------------------------------------------------
+// Epilogue of a message over the parent cells [y0, y1) x [x0, x1) of
+// rotation r: m = log(J01 at the shift-back source) + M, then the caller's
+// accumulation (store / add into the parent belief with its max / marginal
+// formation with the first-maximum argmax).  getf(sy, sx) returns the
+// exp-domain J01 value at source cell (sy, sx).  All threads of the CTA call
+// it (block reductions).
+// ---------------------------------------------------------------------------
+template <class GetF>
+__device__ __forceinline__ void msg_epilogue(const MsgDesc &md, int r, int H, int W, int x0,
+                                             int x1, int y0, int y1, int4 dxo, int4 dyo,
+                                             const int16_t *txo, const int16_t *tyo,
+                                             bool first_block, GetF getf, int *red,
+                                             unsigned long long *redu) {
+  const int tid = threadIdx.x;
+  const int64_t HW = (int64_t)H * W;
+  const float M = fkey_decode(*md.in_max);
+  if (md.in_max_f64 && first_block && tid == 0) *md.in_max_f64 = (double)M;
+  const int tw = x1 - x0;
+  int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
+  unsigned long long am = 0ull;
+  const int mode = md.mode;
+  const float *src0 = md.src0, *src1 = md.src1;
+  float *dst0 = md.dst0, *dst1 = md.dst1;
+  // lane = parent column (coalesced row segments), warps step over rows
+  const int lx = tid & 31, wy = tid >> 5, nwy = blockDim.x >> 5;
+  const int xx = x0 + lx;
+  const int sx = lx < tw ? shift_src(dxo, txo, xx) : -1;
+  constexpr int U = 4;
+  for (int yb = y0 + wy; yb < y1; yb += U * nwy) {
+    float m[U], a0[U], a1[U];
+    int64_t idx[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int yy = yb + u * nwy;
+      idx[u] = -1;
+      m[u] = kLogZero;
+      a0[u] = 0.f;
+      a1[u] = 0.f;
+      if (lx < tw && yy < y1) {
+        const int sy = shift_src(dyo, tyo, yy);
+        if (sy >= 0 && sx >= 0) m[u] = __fadd_rn(log_or_zero(getf(sy, sx)), M);
+        idx[u] = (int64_t)r * HW + (int64_t)yy * W + xx;
+        if (mode != EPI_STORE) a0[u] = __ldg(src0 + idx[u]);
+        if (mode == EPI_DOWN && dst1) a1[u] = __ldg(src1 + idx[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (idx[u] < 0) continue;
+      if (mode == EPI_STORE) {
+        dst0[idx[u]] = m[u];
+      } else if (mode == EPI_ADD) {
+        const float o = __fadd_rn(m[u], a0[u]);
+        dst0[idx[u]] = o;
+        k0 = max(k0, (o == o) ? fkey(o) : kFkeyNegInf);
+      } else {
+        const float o = __fadd_rn(a0[u], m[u]);
+        dst0[idx[u]] = o;
+        const unsigned long long k = akey(o, (uint32_t)idx[u]);
+        am = k > am ? k : am;
+        if (dst1) {
+          const float o1 = __fadd_rn(a1[u], m[u]);
+          dst1[idx[u]] = o1;
+          k1 = max(k1, (o1 == o1) ? fkey(o1) : kFkeyNegInf);
+        }
+      }
+    }
+  }
+  if (md.mode == EPI_ADD && md.max0) block_reduce_commit(k0, md.max0, red);
+  if (md.mode == EPI_DOWN) {
+    if (md.max1) block_reduce_commit(k1, md.max1, red);
+    if (md.amax0) {
+      am = warp_max_u64(am);
+      const int lane = tid & 31, warp = tid >> 5;
+      if (lane == 0) redu[warp] = am;
+      __syncthreads();
+      if (tid == 0) {
+        unsigned long long bm = redu[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bm = redu[w] > bm ? redu[w] : bm;
+        atomicMax(md.amax0, bm);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__restrict__ msgs,
                                                            int R, int H, int W, int band,
                                                            int pady, int *err) {
   const MsgDesc md = msgs[blockIdx.z];
+  if (md.full) return;  // k_full_* (uniform for the CTA)
   const int r = blockIdx.y % R;
   const int yb = blockIdx.y / R;
   const int y0 = yb * band, y1 = min(H, y0 + band);
@@ -449,77 +550,136 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
   __syncthreads();
 
   // epilogue: log, + M, shift back, combine with the caller's accumulation.
-  const float M = fkey_decode(*md.in_max);
-  if (md.in_max_f64 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) *md.in_max_f64 = (double)M;
-  const int tw = x1 - x0;
-  int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
-  unsigned long long am = 0ull;
-  const int mode = md.mode;
-  const float *src0 = md.src0, *src1 = md.src1;
-  float *dst0 = md.dst0, *dst1 = md.dst1;
-  // lane = parent column (coalesced row segments), warps step over rows
-  const int lx = tid & 31, wy = tid >> 5, nwy = blockDim.x >> 5;
-  const int xx = x0 + lx;
-  const int sx = lx < tw ? shift_src(dxo, txo, xx) : -1;
-  constexpr int U = 4;
-  for (int yb = y0 + wy; yb < y1; yb += U * nwy) {
-    float m[U], a0[U], a1[U];
-    int64_t idx[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int yy = yb + u * nwy;
-      idx[u] = -1;
-      m[u] = kLogZero;
-      a0[u] = 0.f;
-      a1[u] = 0.f;
-      if (lx < tw && yy < y1) {
-        const int sy = shift_src(dyo, tyo, yy);
-        if (sy >= 0 && sx >= 0) {
-          const float f = F[(sy - rmin) * kCW + (sx - cmin)];
-          m[u] = __fadd_rn(log_or_zero(f), M);
-        }
-        idx[u] = (int64_t)r * HW + (int64_t)yy * W + xx;
-        if (mode != EPI_STORE) a0[u] = __ldg(src0 + idx[u]);
-        if (mode == EPI_DOWN && dst1) a1[u] = __ldg(src1 + idx[u]);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (idx[u] < 0) continue;
-      if (mode == EPI_STORE) {
-        dst0[idx[u]] = m[u];
-      } else if (mode == EPI_ADD) {
-        const float o = __fadd_rn(m[u], a0[u]);
-        dst0[idx[u]] = o;
-        k0 = max(k0, (o == o) ? fkey(o) : kFkeyNegInf);
-      } else {
-        const float o = __fadd_rn(a0[u], m[u]);
-        dst0[idx[u]] = o;
-        const unsigned long long k = akey(o, (uint32_t)idx[u]);
-        am = k > am ? k : am;
-        if (dst1) {
-          const float o1 = __fadd_rn(a1[u], m[u]);
-          dst1[idx[u]] = o1;
-          k1 = max(k1, (o1 == o1) ? fkey(o1) : kFkeyNegInf);
-        }
-      }
-    }
+  msg_epilogue(md, r, H, W, x0, x1, y0, y1, dxo, dyo, txo, tyo,
+               blockIdx.x == 0 && blockIdx.y == 0,
+               [&](int sy, int sx) { return F[(sy - rmin) * kCW + (sx - cmin)]; }, red, redu);
+}
+
+// ---------------------------------------------------------------------------
+// Full-covariance messages: gaussFilter2dOffset with a zero offset
+// (libMultiArray/multi_array_filter.hpp:335-369) on every rotation of the
+// rotation-filtered exp map e2: bilinear rotation into the eigenbasis of C
+// (transform_grid_resize), unnormalised truncated Gaussians along the eigen
+// axes (gaussFilterDiag2d), bilinear rotation back
+// (transform_grid_fixed_size), then the usual log / + M / shift-back
+// epilogue.  Coordinates are evaluated in double with the reference's
+// rounding, bilinear weights in float (explicit _rn operations: no fused
+// multiply-add).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void map_pt(const double *T, int x, int y, double &ox, double &oy) {
+  ox = __dadd_rn(__dadd_rn(__dmul_rn(T[0], (double)x), __dmul_rn(T[1], (double)y)), T[2]);
+  oy = __dadd_rn(__dadd_rn(__dmul_rn(T[3], (double)x), __dmul_rn(T[4], (double)y)), T[5]);
+}
+
+// TM_BILINEAR sample of g [in_h][in_w] (multi_array_transform.hpp:216-236):
+// exact-hit shortcut, last row/column and outside left at 0.
+__device__ __forceinline__ float bilinear_at(const float *g, int in_h, int in_w, double x1,
+                                             double y1) {
+  const double fx = floor(x1), fy = floor(y1);
+  if (!(fx >= 0.0 && fx < (double)in_w && fy >= 0.0 && fy < (double)in_h)) return 0.f;
+  const int ix1 = (int)fx, iy1 = (int)fy;
+  const float a = __double2float_rn(__dsub_rn(x1, fx));
+  const float b = __double2float_rn(__dsub_rn(y1, fy));
+  const float eps10 = 10.0f * 1.1920928955078125e-07f;  // 10 * FLT_EPSILON
+  const float *g0 = g + (int64_t)iy1 * in_w + ix1;
+  if (a < eps10 && b < eps10) return __ldg(g0);
+  if (ix1 >= in_w - 1 || iy1 >= in_h - 1) return 0.f;
+  const float *g1 = g0 + in_w;
+  const float omb = __fsub_rn(1.0f, b), oma = __fsub_rn(1.0f, a);
+  const float t0 = __fmul_rn(__fmul_rn(omb, oma), __ldg(g0));
+  const float t1 = __fmul_rn(__fmul_rn(omb, a), __ldg(g0 + 1));
+  const float t2 = __fmul_rn(__fmul_rn(b, oma), __ldg(g1));
+  const float t3 = __fmul_rn(__fmul_rn(b, a), __ldg(g1 + 1));
+  return __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+}
+
+// e2 [R][H][W] -> g0 [R][oh][ow]
+__global__ void __launch_bounds__(256) k_full_fwd(const MsgDesc *__restrict__ msgs, int R, int H,
+                                                  int W) {
+  const int msg = blockIdx.z / R, r = blockIdx.z - (blockIdx.z / R) * R;
+  const MsgDesc *md = msgs + msg;
+  if (!md->full) return;
+  const int oh = md->oh, ow = md->ow;
+  const int x3 = blockIdx.x * 32 + threadIdx.x, y3 = blockIdx.y * 8 + threadIdx.y;
+  if (x3 >= ow || y3 >= oh) return;
+  double x1, y1;
+  map_pt(md->tf, x3, y3, x1, y1);
+  md->g0[((int64_t)r * oh + y3) * ow + x3] =
+      bilinear_at(md->e2 + (int64_t)r * H * W, H, W, x1, y1);
+}
+
+// x pass along the rotated rows: g0 -> g1 (truncated at the border)
+__global__ void __launch_bounds__(256) k_full_gx(const MsgDesc *__restrict__ msgs, int R) {
+  const MsgDesc *md = msgs + blockIdx.z;
+  if (!md->full) return;
+  const int oh = md->oh, ow = md->ow, r = blockIdx.y, y = blockIdx.x;
+  if (y >= oh) return;  // uniform for the CTA
+  const int xlen = md->xlen, kx = (xlen - 1) / 2;
+  extern __shared__ __align__(16) float sm[];
+  float *t = sm;                 // [xlen]
+  float *row = sm + align4(xlen);  // [ow + 2 kx], zero outside the grid
+  for (int i = threadIdx.x; i < xlen; i += blockDim.x) t[i] = md->xtaps[i];
+  const float *src = md->g0 + ((int64_t)r * oh + y) * ow;
+  for (int i = threadIdx.x; i < ow + 2 * kx; i += blockDim.x) {
+    const int x = i - kx;
+    row[i] = (x >= 0 && x < ow) ? __ldg(src + x) : 0.f;
   }
-  if (md.mode == EPI_ADD && md.max0) block_reduce_commit(k0, md.max0, red);
-  if (md.mode == EPI_DOWN) {
-    if (md.max1) block_reduce_commit(k1, md.max1, red);
-    if (md.amax0) {
-      am = warp_max_u64(am);
-      const int lane = tid & 31, warp = tid >> 5;
-      if (lane == 0) redu[warp] = am;
-      __syncthreads();
-      if (tid == 0) {
-        unsigned long long b = redu[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = redu[w] > b ? redu[w] : b;
-        atomicMax(md.amax0, b);
-      }
-    }
+  __syncthreads();
+  float *dst = md->g1 + ((int64_t)r * oh + y) * ow;
+  for (int x = threadIdx.x; x < ow; x += blockDim.x) {
+    float acc = 0.f;
+    for (int k = 0; k < xlen; ++k) acc = fmaf(t[k], row[x + k], acc);
+    dst[x] = acc;
   }
+}
+
+// y pass along the rotated columns: g1 -> g0 (truncated at the border)
+constexpr int kFullRows = 32;
+__global__ void __launch_bounds__(256) k_full_gy(const MsgDesc *__restrict__ msgs, int R) {
+  const int msg = blockIdx.z / R, r = blockIdx.z - (blockIdx.z / R) * R;
+  const MsgDesc *md = msgs + msg;
+  if (!md->full) return;
+  const int oh = md->oh, ow = md->ow;
+  const int ylen = md->ylen, ky = (ylen - 1) / 2;
+  __shared__ float t[kMaxFullTaps];
+  for (int i = threadIdx.y * 32 + threadIdx.x; i < ylen; i += 256) t[i] = md->ytaps[i];
+  __syncthreads();
+  const int x = blockIdx.x * 32 + threadIdx.x;
+  if (x >= ow) return;
+  const float *src = md->g1 + (int64_t)r * oh * ow + x;
+  float *dst = md->g0 + (int64_t)r * oh * ow + x;
+  const int yend = min(oh, (blockIdx.y + 1) * kFullRows);
+  for (int y = blockIdx.y * kFullRows + threadIdx.y; y < yend; y += 8) {
+    const int k0 = max(0, ky - y), k1 = min(ylen, oh - y + ky);
+    float acc = 0.f;
+    for (int k = k0; k < k1; ++k) acc = fmaf(t[k], __ldg(src + (int64_t)(y - ky + k) * ow), acc);
+    dst[(int64_t)y * ow] = acc;
+  }
+}
+
+// rotate back (bilinear from g0 at tb * (x, y)), log, + M, shift back, epilogue
+constexpr int kFullBand = 64;
+__global__ void __launch_bounds__(kThreadsCols) k_full_epi(const MsgDesc *__restrict__ msgs, int R,
+                                                          int H, int W) {
+  __shared__ int red[kThreadsCols / 32];
+  __shared__ unsigned long long redu[kThreadsCols / 32];
+  const MsgDesc md = msgs[blockIdx.z];
+  if (!md.full) return;
+  const int r = blockIdx.y % R, yb = blockIdx.y / R;
+  const int y0 = yb * kFullBand, y1 = min(H, y0 + kFullBand);
+  const int x0 = blockIdx.x * kTX, x1 = min(W, x0 + kTX);
+  const int16_t *txo = md.tx_out + r * W;
+  const int16_t *tyo = md.ty_out + r * H;
+  const int4 dxo = md.sdesc[2 * R + r], dyo = md.sdesc[3 * R + r];
+  const float *g = md.g0 + (int64_t)r * md.oh * md.ow;
+  const int oh = md.oh, ow = md.ow;
+  msg_epilogue(md, r, H, W, x0, x1, y0, y1, dxo, dyo, txo, tyo, blockIdx.x == 0 && blockIdx.y == 0,
+               [&](int sy, int sx) {
+                 double px, py;
+                 map_pt(md.tb, sx, sy, px, py);
+                 return bilinear_at(g, oh, ow, px, py);
+               },
+               red, redu);
 }
 
 // ---------------------------------------------------------------------------
@@ -643,6 +803,27 @@ cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W
     case 48: return launch_rows_t<48>(msgs, n_msgs, R, H, W, padx, err, s);
     default: return launch_rows_t<0>(msgs, n_msgs, R, H, W, padx, err, s);
   }
+}
+
+cudaError_t launch_msg_full(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int ohmax,
+                            int owmax, int kxmax, int kymax, int *err, cudaStream_t s) {
+  (void)err;
+  if (ohmax < 1 || owmax < 1 || 2 * kymax + 1 > kMaxFullTaps || (int64_t)R * n_msgs > 65535)
+    return cudaErrorInvalidValue;
+  const size_t gx_smem = ((size_t)align4(2 * kxmax + 1) + owmax + 2 * kxmax) * sizeof(float);
+  if (gx_smem > 227 * 1024) return cudaErrorInvalidValue;
+  k_full_fwd<<<dim3((unsigned)((owmax + 31) / 32), (unsigned)((ohmax + 7) / 8),
+                    (unsigned)(R * n_msgs)),
+               dim3(32, 8), 0, s>>>(msgs, R, H, W);
+  cudaFuncSetAttribute(k_full_gx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gx_smem);
+  k_full_gx<<<dim3((unsigned)ohmax, (unsigned)R, (unsigned)n_msgs), 256, gx_smem, s>>>(msgs, R);
+  k_full_gy<<<dim3((unsigned)((owmax + 31) / 32), (unsigned)((ohmax + kFullRows - 1) / kFullRows),
+                   (unsigned)(R * n_msgs)),
+              dim3(32, 8), 0, s>>>(msgs, R);
+  k_full_epi<<<dim3((unsigned)((W + kTX - 1) / kTX), (unsigned)(R * ((H + kFullBand - 1) / kFullBand)),
+                    (unsigned)n_msgs),
+               kThreadsCols, 0, s>>>(msgs, R, H, W);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int pady,

@@ -309,6 +309,15 @@ void hc_inverse(const double *T, double *I) {
   I[8] = 1;
 }
 
+// The covariances eig2d and gaussFilterDiag2d accept: symmetric, positive
+// definite (both eigenvalues > 0).
+bool cov_ok(const double *C) {
+  if (!(std::isfinite(C[0]) && std::isfinite(C[1]) && std::isfinite(C[2]) && std::isfinite(C[3])))
+    return false;
+  if (C[1] != C[2]) return false;
+  return C[0] > 0 && C[3] > 0 && C[0] * C[3] - C[1] * C[2] > 0;
+}
+
 bool exp_ok(const pa_exp_param *e) {
   return e && e->num_rotation_steps >= 2 && e->num_rotation_steps <= kMaxRot &&
          e->max_part_rotation > e->min_part_rotation &&
@@ -405,11 +414,8 @@ pa_status load_joints(pa_ctx *ctx, const pa_tree *t, int flip, std::vector<Joint
       J.C[2] = -J.C[2];
       J.rot_mean = -J.rot_mean;
     }
-    if (J.C[1] != 0 || J.C[2] != 0)
-      return fail(ctx, PA_ERR_UNSUPPORTED,
-                  "joint %d: non-diagonal covariance (gaussFilter2dOffset) is not built", j);
-    if (!(J.C[0] > 0 && J.C[3] > 0))
-      return fail(ctx, PA_ERR_INVALID, "joint %d: covariance diagonal must be > 0", j);
+    if (!cov_ok(J.C))
+      return fail(ctx, PA_ERR_INVALID, "joint %d: covariance must be symmetric positive definite", j);
     if (!(std::isfinite(J.rot_mean) && std::isfinite(J.rot_sigma)))
       return fail(ctx, PA_ERR_INVALID, "joint %d: rotation parameters not finite", j);
   }
@@ -423,8 +429,83 @@ namespace pa {
 // Per-message host parameters of computeRotJointMarginal(child -> parent,
 // offset_c_10 = oc, offset_p_01 = op, rot_mean, rot_sigma).
 
+// boost_math::eig2d (libBoostMath/boost_math.cpp:40-99): E = (smallest,
+// largest) eigenvalue, V (row-major) holds the eigenvectors as columns.
+void eig2d(const double *M, double *V, double *E) {
+  const double m11 = M[0], m12 = M[1], m22 = M[3];
+  double e1, e2, v11, v21;
+  if (m12 != 0) {
+    const double sqrtD = std::sqrt((m11 - m22) * (m11 - m22) + 4 * m12 * m12);
+    e1 = 0.5 * (m11 + m22 - sqrtD);
+    e2 = 0.5 * (m11 + m22 + sqrtD);
+    v11 = 0.5 * (m11 - m22 - sqrtD) / m12;
+    v21 = 1;
+  } else if (m11 < m22) {
+    e1 = m11; e2 = m22; v11 = 1; v21 = 0;
+  } else {
+    e1 = m22; e2 = m11; v11 = 0; v21 = 1;
+  }
+  const double norm_v1 = std::sqrt(v11 * v11 + v21 * v21);
+  v11 /= norm_v1;
+  v21 /= norm_v1;
+  V[0] = v11;
+  V[1] = -v21;
+  V[2] = v21;
+  V[3] = v11;
+  E[0] = e1;
+  E[1] = e2;
+}
+
+// ublas prod of 3x3 matrices (row-major), accumulated k = 0, 1, 2.
+void prod3(const double *A, const double *B, double *Cm) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double t = 0;
+      for (int k = 0; k < 3; ++k) t += A[3 * i + k] * B[3 * k + j];
+      Cm[3 * i + j] = t;
+    }
+}
+
+// The transforms of gaussFilter2dOffset with a zero offset
+// (libMultiArray/multi_array_filter.hpp:335-369): rotate the [H][W] map into
+// the eigenbasis of C (transform_grid_resize, adaptive size from
+// hc::get_transformed_bbox, homogeneous_coord.cpp:140-156), filter along the
+// eigen axes, rotate back (transform_grid_fixed_size).
+void full_cov_params(const double *Cs, int H, int W, MsgParams &m, double *E) {
+  double V[4];
+  eig2d(Cs, V, E);
+  const double T21[9] = {V[0], V[2], 0, V[1], V[3], 0, 0, 0, 1};  // [trans(V) | 0]
+  const double px[4] = {0, (double)(W - 1), 0, (double)(W - 1)};
+  const double py[4] = {0, 0, (double)(H - 1), (double)(H - 1)};
+  double xs[4], ys[4];
+  for (int c = 0; c < 4; ++c) {
+    xs[c] = T21[0] * px[c] + T21[1] * py[c] + T21[2] * 1.0;
+    ys[c] = T21[3] * px[c] + T21[4] * py[c] + T21[5] * 1.0;
+  }
+  const double minx = *std::min_element(xs, xs + 4), maxx = *std::max_element(xs, xs + 4);
+  const double miny = *std::min_element(ys, ys + 4), maxy = *std::max_element(ys, ys + 4);
+  m.ow = (int)std::ceil(maxx - minx);
+  m.oh = (int)std::ceil(maxy - miny);
+  const double T23[9] = {1, 0, minx, 0, 1, miny, 0, 0, 1};
+  double T12[9], T13[9];
+  hc_inverse(T21, T12);
+  prod3(T12, T23, T13);
+  const double mz = -0.0;
+  const double T42[9] = {V[0], V[1], mz, V[2], V[3], mz, 0, 0, 1};
+  double T43[9], Tb[9], Tbb[9];
+  prod3(T42, T23, T43);
+  hc_inverse(T43, Tb);
+  const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  prod3(Tb, I3, Tbb);
+  for (int k = 0; k < 6; ++k) {
+    m.tf[k] = T13[k];
+    m.tb[k] = Tbb[k];
+  }
+  m.full = true;
+}
+
 void msg_params(const pa_exp_param *e, double scale, const double *oc, const double *op,
-                const double *C, double rot_mean, double rot_sigma, MsgParams &m) {
+                const double *C, double rot_mean, double rot_sigma, int H, int W, MsgParams &m) {
   const int R = e->num_rotation_steps;
   const double step = rot_step_rad(e);
   const double rot_sigma_idx = rot_sigma / step;
@@ -446,8 +527,17 @@ void msg_params(const pa_exp_param *e, double scale, const double *oc, const dou
     m.rlen = 0;
   }
   const double sc2 = scale * scale;  // gaussFilterDiag2d, multi_array_filter.hpp:232-236
-  std::vector<double> fx = gaussian_taps(std::sqrt(sc2 * C[0]));
-  std::vector<double> fy = gaussian_taps(std::sqrt(sc2 * C[3]));
+  const double Cs[4] = {sc2 * C[0], sc2 * C[1], sc2 * C[2], sc2 * C[3]};  // square(scale)*C
+  double sx2 = Cs[0], sy2 = Cs[3];
+  m.full = false;
+  if (Cs[1] != 0 || Cs[2] != 0) {  // gaussFilter2d -> gaussFilter2dOffset
+    double E[2];
+    full_cov_params(Cs, H, W, m, E);
+    sx2 = E[0];
+    sy2 = E[1];
+  }
+  std::vector<double> fx = gaussian_taps(std::sqrt(sx2));
+  std::vector<double> fy = gaussian_taps(std::sqrt(sy2));
   m.xtaps.assign(fx.begin(), fx.end());
   m.ytaps.assign(fy.begin(), fy.end());
   m.xlen = (int)fx.size();
@@ -497,6 +587,7 @@ struct PsPlan {
   struct Phase {
     MsgDesc *msgs = nullptr;
     int n = 0, padx = 0, pady = 0;
+    int n_full = 0, ohmax = 0, owmax = 0, kxf = 0, kyf = 0;  // full-covariance messages
   };
   std::vector<Phase> up, down;
   RootDesc *roots = nullptr;
@@ -595,6 +686,33 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   for (auto &ph : dnph) maxph = std::max(maxph, ph.size());
   std::vector<float *> e2(maxph);
   for (size_t k = 0; k < maxph; ++k) e2[k] = b.scratch<float>(N);
+  // message parameters; rotated-grid buffers of full-covariance messages are
+  // shared by the messages that take slot k in their phase
+  auto params_of = [&](const M &mm) {
+    const Joint &J = joints[mm.img][mm.joint];
+    MsgParams mp;
+    if (mm.up)
+      msg_params(e, scale, J.oc, J.op, J.C, J.rot_mean, J.rot_sigma, H, W, mp);
+    else
+      msg_params(e, scale, J.op, J.oc, J.C, -J.rot_mean, J.rot_sigma, H, W, mp);
+    return mp;
+  };
+  std::vector<std::vector<MsgParams>> upmp(upph.size()), dnmp(dnph.size());
+  std::vector<size_t> slot_cells(maxph, 0);
+  for (size_t k = 0; k < upph.size(); ++k)
+    for (const M &mm : upph[k]) upmp[k].push_back(params_of(mm));
+  for (size_t k = 0; k < dnph.size(); ++k)
+    for (const M &mm : dnph[k]) dnmp[k].push_back(params_of(mm));
+  for (auto *all : {&upmp, &dnmp})
+    for (auto &v : *all)
+      for (size_t k = 0; k < v.size(); ++k)
+        if (v[k].full) slot_cells[k] = std::max(slot_cells[k], (size_t)v[k].oh * v[k].ow);
+  std::vector<float *> g0(maxph, nullptr), g1(maxph, nullptr);
+  for (size_t k = 0; k < maxph; ++k)
+    if (slot_cells[k]) {
+      g0[k] = b.scratch<float>((size_t)R * slot_cells[k]);
+      g1[k] = b.scratch<float>((size_t)R * slot_cells[k]);
+    }
 
   pl.n_msgs_total = 0;
   for (auto &ph : upph) pl.n_msgs_total += (int)ph.size();
@@ -604,20 +722,16 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   all_shifts.reserve((size_t)pl.n_msgs_total * 4 * R);
 
   int msg_counter = 0;
-  auto build_phase = [&](const std::vector<M> &ph, PsPlan::Phase &out) {
+  auto build_phase = [&](const std::vector<M> &ph, const std::vector<MsgParams> &mps,
+                         PsPlan::Phase &out) {
     std::vector<MsgDesc> descs(ph.size());
     out.n = (int)ph.size();
     out.padx = out.pady = 0;
     for (size_t k = 0; k < ph.size(); ++k) {
       const M &mm = ph[k];
-      const Joint &J = joints[mm.img][mm.joint];
       const int c = mm.child;
       const int par = mm.parent;
-      MsgParams mp;
-      if (mm.up)
-        msg_params(e, scale, J.oc, J.op, J.C, J.rot_mean, J.rot_sigma, mp);
-      else
-        msg_params(e, scale, J.op, J.oc, J.C, -J.rot_mean, J.rot_sigma, mp);
+      const MsgParams &mp = mps[k];
       ImgMaps &im = pl.im[mm.img];
       MsgDesc &d = descs[k];
       std::memset(&d, 0, sizeof d);
@@ -638,8 +752,25 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
       d.xlen = mp.xlen;
       d.ylen = mp.ylen;
       d.e2 = e2[k];
-      out.padx = std::max(out.padx, (mp.xlen - 1) / 2);
-      out.pady = std::max(out.pady, (mp.ylen - 1) / 2);
+      if (mp.full) {
+        d.full = 1;
+        d.oh = mp.oh;
+        d.ow = mp.ow;
+        d.g0 = g0[k];
+        d.g1 = g1[k];
+        for (int q = 0; q < 6; ++q) {
+          d.tf[q] = mp.tf[q];
+          d.tb[q] = mp.tb[q];
+        }
+        ++out.n_full;
+        out.ohmax = std::max(out.ohmax, mp.oh);
+        out.owmax = std::max(out.owmax, mp.ow);
+        out.kxf = std::max(out.kxf, (mp.xlen - 1) / 2);
+        out.kyf = std::max(out.kyf, (mp.ylen - 1) / 2);
+      } else {
+        out.padx = std::max(out.padx, (mp.xlen - 1) / 2);
+        out.pady = std::max(out.pady, (mp.ylen - 1) / 2);
+      }
       if (mm.up) {
         const bool inner = !s.ch[c].empty();
         d.in = inner ? im.POST[c] : im.U[c];
@@ -682,8 +813,8 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   pl.sdesc = b.scratch<int4>((size_t)pl.n_msgs_total * 4 * R);
   pl.up.assign(upph.size(), {});
   pl.down.assign(dnph.size(), {});
-  for (size_t k = 0; k < upph.size(); ++k) build_phase(upph[k], pl.up[k]);
-  for (size_t k = 0; k < dnph.size(); ++k) build_phase(dnph[k], pl.down[k]);
+  for (size_t k = 0; k < upph.size(); ++k) build_phase(upph[k], upmp[k], pl.up[k]);
+  for (size_t k = 0; k < dnph.size(); ++k) build_phase(dnph[k], dnmp[k], pl.down[k]);
   pl.shifts = b.param(all_shifts.data(), all_shifts.size());
 
   std::vector<RootDesc> rds(B);
@@ -763,13 +894,21 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
     for (auto &ph : pl.up) {
       if (!ph.n) continue;
       PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
-      PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+      if (ph.n_full < ph.n)
+        PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+      if (ph.n_full)
+        PA_LAUNCH_N("msg_full", 4, launch_msg_full(ph.msgs, ph.n, R, H, W, ph.ohmax, ph.owmax,
+                                                   ph.kxf, ph.kyf, pl.err, st));
     }
     PA_LAUNCH("root_combine", launch_root_combine(pl.roots, B, pl.N, st));
     for (auto &ph : pl.down) {
       if (!ph.n) continue;
       PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
-      PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+      if (ph.n_full < ph.n)
+        PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+      if (ph.n_full)
+        PA_LAUNCH_N("msg_full", 4, launch_msg_full(ph.msgs, ph.n, R, H, W, ph.ohmax, ph.owmax,
+                                                   ph.kxf, ph.kyf, pl.err, st));
     }
     PA_LAUNCH("root_posterior", launch_root_posterior(pl.post_root_ptrs, pl.root_post_ptrs, pl.keep, pl.n_keep, B,
                                     R, H, W, st));
@@ -1733,13 +1872,11 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
       H > 32767 || W > 32767 || R != ep->num_rotation_steps || !exp_ok(ep))
     return fail(ctx, PA_ERR_INVALID, "invalid sizes, parameters or NULL input");
   if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
-  if (C[1] != 0 || C[2] != 0)
-    return fail(ctx, PA_ERR_UNSUPPORTED, "non-diagonal covariance (gaussFilter2dOffset) is not built");
-  if (!(C[0] > 0 && C[3] > 0)) return fail(ctx, PA_ERR_INVALID, "covariance diagonal must be > 0");
+  if (!cov_ok(C)) return fail(ctx, PA_ERR_INVALID, "covariance must be symmetric positive definite");
   DeviceGuard dg(ctx->device);
   const int64_t N = (int64_t)R * H * W;
   MsgParams mp;
-  msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, mp);
+  msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, H, W, mp);
   int4 *sdesc = nullptr;
   auto plan = [&](Builder &b, MsgDesc **md, int16_t **tables, double **shifts, int **slot,
                   int **err, const float **din, float **dout, float **e2) {
@@ -1751,6 +1888,17 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
     *slot = b.scratch<int>(1);
     *err = b.scratch<int>(1);
     *e2 = b.scratch<float>(N);
+    if (mp.full) {
+      d.full = 1;
+      d.oh = mp.oh;
+      d.ow = mp.ow;
+      d.g0 = b.scratch<float>((size_t)R * mp.oh * mp.ow);
+      d.g1 = b.scratch<float>((size_t)R * mp.oh * mp.ow);
+      for (int q = 0; q < 6; ++q) {
+        d.tf[q] = mp.tf[q];
+        d.tb[q] = mp.tb[q];
+      }
+    }
     *din = (mem == PA_MEM_HOST) ? b.scratch<float>(N) : child;
     *dout = (mem == PA_MEM_HOST) ? b.scratch<float>(N) : parent;
     d.in = *din;
@@ -1796,7 +1944,11 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
   PA_LAUNCH("map_max", launch_map_max(din, N, slot, s));
   PA_LAUNCH_N("shift_tables", 2, launch_shift_tables(shifts, 1, R, H, W, tables, sdesc, s));
   PA_LAUNCH("msg_rows", launch_msg_rows(md, 1, R, H, W, (mp.xlen - 1) / 2, err, s));
-  PA_LAUNCH("msg_cols", launch_msg_cols(md, 1, R, H, W, (mp.ylen - 1) / 2, err, s));
+  if (mp.full)
+    PA_LAUNCH_N("msg_full", 4, launch_msg_full(md, 1, R, H, W, mp.oh, mp.ow, (mp.xlen - 1) / 2,
+                                               (mp.ylen - 1) / 2, err, s));
+  else
+    PA_LAUNCH("msg_cols", launch_msg_cols(md, 1, R, H, W, (mp.ylen - 1) / 2, err, s));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(parent, dout, N * sizeof(float), cudaMemcpyDeviceToHost, s));
   int errflag = 0;

@@ -120,6 +120,15 @@ struct MsgDesc {
   int *max1;
   unsigned long long *amax0;
   double *in_max_f64;     // optional FP64 copy of in_M
+  // full covariance (gaussFilter2dOffset): the row pass writes the
+  // rotation-filtered exp map to e2; it is rotated into the eigenbasis of C
+  // (g0 [R][oh][ow]), filtered along the eigen axes (g1, then g0), rotated
+  // back bilinearly and logged by the full-covariance epilogue
+  int full;
+  int oh, ow;
+  float *g0, *g1;
+  double tf[6];           // rotated-grid cell (x3, y3) -> e2 position (x1, y1)
+  double tb[6];           // image cell (x3, y3) -> rotated-grid position
 };
 
 struct RootDesc {
@@ -140,9 +149,12 @@ struct MsgParams {
   int kidx = 0, rlen = -1, xlen = 1, ylen = 1;
   std::vector<float> rtaps, xtaps, ytaps;
   std::vector<double> shifts;  // [4][R]: a_x_in, a_y_in, a_x_out, a_y_out
+  bool full = false;           // non-diagonal covariance: taps along the eigen axes
+  int oh = 0, ow = 0;          // rotated-grid size (transform_grid_resize)
+  double tf[6] = {0, 0, 0, 0, 0, 0}, tb[6] = {0, 0, 0, 0, 0, 0};
 };
 void msg_params(const pa_exp_param *e, double scale, const double *oc, const double *op,
-                const double *C, double rot_mean, double rot_sigma, MsgParams &m);
+                const double *C, double rot_mean, double rot_sigma, int H, int W, MsgParams &m);
 
 // Kernel launchers (defined in the .cu files).  All return cudaGetLastError().
 // fast_ok[p] / n_stumps[p] are host arrays describing the classifiers.
@@ -165,6 +177,10 @@ cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, 
                                 int16_t *tables, int4 *sdesc, cudaStream_t s);
 cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
                             int *err_flag, cudaStream_t s);
+// Full-covariance messages of a batch (entries with full == 0 are skipped):
+// forward rotation, eigen-axis x and y passes, rotate-back epilogue.
+cudaError_t launch_msg_full(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int ohmax,
+                            int owmax, int kxmax, int kymax, int *err, cudaStream_t s);
 cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int pady,
                             int *err_flag, cudaStream_t s);
 cudaError_t launch_root_combine(const RootDesc *rd, int n_roots, int64_t N, cudaStream_t s);

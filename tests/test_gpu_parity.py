@@ -295,6 +295,52 @@ def test_ps_variants(ctx, orc, variant):
         assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
 
 
+# ------------------------------------------------------- full covariance
+@pytest.mark.parametrize("R", [24, 12])
+def test_rot_joint_marginal_full_covariance(ctx, orc, R):
+    """Non-diagonal C: gaussFilter2dOffset (rotation into the eigenbasis,
+    eigen-axis filter, rotation back) against the oracle."""
+    rng = np.random.default_rng(40 + R)
+    H, W = 50, 70
+    child = synth.random_log_unary(rng, 1, R, H, W, zero_frac=0.02)[0]
+    step = synth.rot_step_rad(R)
+    for k, rs, oc, op, Cm in [(1, 1.5, (4.2, -3.1), (-2.6, 5.7), [[4.0, 1.5], [1.5, 2.0]]),
+                              (0, 0.0, (-6.0, 2.5), (3.0, -1.0), [[1.0, -0.6], [-0.6, 6.25]]),
+                              (-2, 2.5, (0.5, 9.0), (1.5, -8.0), [[30.0, 12.0], [12.0, 9.0]])]:
+        e = orc.make_exp(R=R)
+        args = (np.array(oc), np.array(op), np.array(Cm), k * step, rs * step)
+        want = orc.rot_joint_marginal(e, child, *args)
+        got = ctx.rot_joint_marginal(_pa_exp(R), child, *args)
+        oob = want == LOG_ZERO
+        assert np.array_equal(got[oob], want[oob])
+        assert maxnorm_err(got, want) <= 1e-5
+        want64 = orc.rot_joint_marginal(e, child.astype(np.float64), *args, f64=True)
+        assert maxnorm_err(got, want64) <= 1e-4
+
+
+@pytest.mark.parametrize("flip", [False, True])
+def test_ps_full_covariance(ctx, orc, flip):
+    """A tree whose joints mix diagonal and full covariances (learned joints
+    carry correlations, objectdetect_learnparam.cpp:465)."""
+    rng = np.random.default_rng(31 + int(flip))
+    R, H, W = 16, 44, 60
+    tree = small_tree(rng, R)
+    for j, rho in ((1, 0.5), (4, -0.35), (6, 0.2), (8, -0.6)):
+        c = tree["C"][j]
+        off = rho * math.sqrt(c[0] * c[3])
+        tree["C"][j] = [c[0], off, off, c[3]]
+    u = synth.random_log_unary(rng, 10, R, H, W)
+    e = orc.make_exp(R=R)
+    t_or = dict(tree)
+    if flip:  # loadJoints mirroring: x of the offsets, the off-diagonal of C
+        t_or = dict(tree, offset_c=tree["offset_c"] * [-1, 1], offset_p=tree["offset_p"] * [-1, 1],
+                    C=tree["C"] * [1, -1, -1, 1], rot_mean=-tree["rot_mean"])
+    want = orc.ps_infer(e, t_or, u)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R), tree, u, flip=flip)
+    compare_ps(got, want, oracle64(orc, e, t_or, u))
+    assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
+
+
 # ---------------------------------------------------------- --find_obj path
 @pytest.mark.parametrize("interpolate", [True, False])
 def test_find_obj_pipeline(ctx, orc, interpolate):
@@ -424,11 +470,12 @@ def test_errors_are_statuses(ctx, pa):
     R = 12
     u = synth.random_log_unary(rng, 10, R, 20, 24)
     tree = small_tree(rng, R)
-    bad = dict(tree, C=tree["C"].copy())
-    bad["C"][0, 1] = bad["C"][0, 2] = 0.5
-    with pytest.raises(pa.PaError) as ei:
-        ctx.compute_root_posterior_rot(_pa_exp(R), bad, u)
-    assert ei.value.status == pa.PA_ERR_UNSUPPORTED
+    for c01, c10 in ((0.5, 0.25), (40.0, 40.0)):  # not symmetric; not positive definite
+        bad = dict(tree, C=tree["C"].copy())
+        bad["C"][0, 1], bad["C"][0, 2] = c01, c10
+        with pytest.raises(pa.PaError) as ei:
+            ctx.compute_root_posterior_rot(_pa_exp(R), bad, u)
+        assert ei.value.status == pa.PA_ERR_INVALID
     two = dict(tree, parent=tree["parent"].copy())
     two["parent"][3] = 1  # part 1 (an upper leg) now has two children
     with pytest.raises(pa.PaError) as ei:

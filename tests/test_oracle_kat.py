@@ -253,3 +253,39 @@ def test_upright_mask_and_root_rotations(orc):
     m = out["log_marg"][0]
     kept = [r for r in range(24) if m[r, 0, 0] == 0.0]
     assert kept == [11, 12]
+
+
+# -------------------------------------------------------- full covariance
+def test_eig2d_known_answers(orc):
+    V, E = orc.eig2d([[2.0, 1.0], [1.0, 2.0]])
+    assert np.allclose(E, [1.0, 3.0])
+    s = 1 / np.sqrt(2)
+    assert np.allclose(V, [[-s, -s], [s, -s]])  # columns: eigenvectors of 1 and 3
+    V, E = orc.eig2d([[4.0, 0.0], [0.0, 1.0]])
+    assert np.allclose(E, [1.0, 4.0]) and np.allclose(V, [[0, -1], [1, 0]])
+    V, E = orc.eig2d([[1.0, 0.0], [0.0, 4.0]])
+    assert np.allclose(E, [1.0, 4.0]) and np.allclose(V, [[1, 0], [0, 1]])
+
+
+def test_full_covariance_near_diagonal_matches_diagonal(orc):
+    """C with a 1e-12 off-diagonal term takes gaussFilter2dOffset: the
+    eigenbasis is the axes rotated by 90 degrees, the rotated grid is an exact
+    transpose (bilinear exact hits), so away from the border the message
+    equals the diagonal filter's; the rotated grid's adaptive size
+    (ceil(max - min)) drops the last row and column, which the reference
+    leaves at 0 (LOG_ZERO after the log)."""
+    rng = np.random.default_rng(5)
+    R, H, W = 4, 20, 24
+    child = rng.uniform(-3.0, 0.0, (R, H, W)).astype(np.float32)
+    band = 6
+    child[:, :band, :] = child[:, -band:, :] = LOG_ZERO
+    child[:, :, :band] = child[:, :, -band:] = LOG_ZERO
+    e = orc.make_exp(R=R)
+    z = np.zeros(2)
+    diag = orc.rot_joint_marginal(e, child, z, z, np.array([[2.25, 0.0], [0.0, 1.0]]), 0.0, 0.0)
+    full = orc.rot_joint_marginal(e, child, z, z, np.array([[2.25, 1e-12], [1e-12, 1.0]]), 0.0, 0.0)
+    a, b = diag[:, :H - 1, :W - 1], full[:, :H - 1, :W - 1]
+    live = a > -1e5
+    assert np.array_equal(live, b > -1e5)
+    assert np.max(np.abs(a[live] - b[live])) <= 1e-5
+    assert np.all(full[:, H - 1, :] == LOG_ZERO) and np.all(full[:, :, W - 1] == LOG_ZERO)
