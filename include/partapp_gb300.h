@@ -241,6 +241,17 @@ pa_status pa_rot_joint_marginal_noalloc(const pa_exp_param *ep, const float *chi
                                         const double *C, double rot_mean, double rot_sigma,
                                         double scale, void *stream);
 
+/* ---------------------------------------------------- building blocks */
+
+/* No counterpart in the reference.  The BF16 tensor-core GEMM the
+ * large-grid message path is built on, exposed so that it can be checked on
+ * its own: C[M][N] = A[M][K] * B[N][K]^T with bf16 operands (K contiguous,
+ * row strides lda, ldb in elements, multiples of 8, 16-byte aligned bases)
+ * and fp32 accumulation and output (row stride ldc).  Device pointers;
+ * returns after the product is complete. */
+pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, int64_t ldb,
+                       float *C, int64_t ldc, int M, int N, int K);
+
 /* ---------------------------------------------------- the --find_obj path */
 
 /* One image of `partapp --find_obj` with freshly computed scores

@@ -45,7 +45,7 @@ EXPORTS = (
     "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
     "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
     "pa_ps_infer", "pa_rot_joint_marginal", "pa_rot_joint_marginal_noalloc", "pa_find_obj",
-    "pa_find_obj_batch",
+    "pa_find_obj_batch", "pa_gemm_bf16",
 )
 
 
@@ -128,6 +128,7 @@ def load_library():
     L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, vp, ip, ip, P(PsOutputs), ip]
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
                                         dp, dp, dp, ip]
+    L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip]
     L.pa_rot_joint_marginal_noalloc.argtypes = [P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp),
                                                  P(dp), dp, dp, dp, vp]
     L.pa_find_obj.argtypes = [vp, P(ExpParam), P(Tree), ip, P(vp), ip, vp, ip, ip, ip, P(dp), ip,
@@ -368,6 +369,20 @@ class Context:
         res["part_hyps"] = ph.reshape(P, -1, 7).copy() if ph.size >= 7 * P else ph.reshape(0, 7)
         res["root_hyps"] = res["root_hyps"][: int(res["n_root_hyps"][0])]
         return res
+
+    def gemm_bf16(self, A, B, out=None):
+        """C = A @ B.T on the tensor cores: A [M][K], B [N][K] bf16 CUDA
+        tensors (K contiguous, K padded to a multiple of 8 by the caller);
+        returns C [M][N] fp32 (or fills `out`)."""
+        import torch
+
+        assert A.is_cuda and B.is_cuda and A.dtype == torch.bfloat16 and B.dtype == torch.bfloat16
+        M, K = A.shape
+        N = B.shape[0]
+        C_ = out if out is not None else torch.empty((M, N), dtype=torch.float32, device=A.device)
+        self._check(self.L.pa_gemm_bf16(self.h, A.data_ptr(), A.stride(0), B.data_ptr(),
+                                        B.stride(0), C_.data_ptr(), C_.stride(0), M, N, K))
+        return C_
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,
                                    want_marg=True):

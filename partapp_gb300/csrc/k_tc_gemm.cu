@@ -1,0 +1,269 @@
+// k_tc_gemm.cu -- BF16 GEMM on the fifth-generation tensor cores (tcgen05).
+//
+//   C[M][N] (fp32, row stride ldc) = A[M][K] (bf16, K contiguous)
+//                                   * B[N][K]^T (bf16, K contiguous)
+//
+// One CTA computes a 128 x 128 tile of C.  Operands move global -> shared
+// by TMA (cp.async.bulk.tensor, 128-byte swizzle, 64-element K blocks) in a
+// kStages-deep ring guarded by mbarriers; one thread issues tcgen05.mma
+// (kind::f16, BF16 x BF16 -> FP32) into a 128 x 128 FP32 accumulator in
+// tensor memory; the four warps read the accumulator back with tcgen05.ld
+// (warp w owns TMEM lanes = tile rows 32w .. 32w + 31) and store it.
+//
+// Every wait is bounded: after kSpinLimit polls the waiting thread sets bit 8
+// of *err and gives up; the CTA still frees its tensor memory before it
+// returns, so a failed launch leaves the device usable.
+//
+// Operand rows past M / N and K columns past K are read as zeros (TMA
+// out-of-bounds fill); rows past M / N are not stored.
+#include <cuda.h>
+
+#include "pa_internal.cuh"
+
+namespace pa {
+namespace {
+
+constexpr int kBM = 128, kBN = 128, kBK = 64, kStages = 4;
+constexpr int kTileBytesA = kBM * kBK * 2;  // 16 KB
+constexpr int kTileBytesB = kBN * kBK * 2;  // 16 KB
+constexpr int kStageBytes = kTileBytesA + kTileBytesB;
+constexpr uint32_t kSpinLimit = 1u << 24;
+constexpr int kGemmThreads = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Non-blocking probe of phase `parity`; the caller bounds the polling.
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i)
+    if (mbar_test(bar, parity)) return true;
+  atomicOr(err, 8);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile stored as TMA
+// writes it with 128-byte swizzle: rows of 128 B (64 bf16), 8-row atoms of
+// 1024 B (stride byte offset), tile base 1024-byte aligned.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused with swizzle)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: D fp32, A and B bf16, both K-major, M = 128, N = 128.
+constexpr uint32_t kIdesc = (1u << 4)                   // D format: f32
+                            | (1u << 7)                 // A format: bf16
+                            | (1u << 10)                // B format: bf16
+                            | ((uint32_t)(kBN >> 3) << 17)
+                            | ((uint32_t)(kBM >> 4) << 24);
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    k_tc_gemm_bf16(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   float *__restrict__ C, int M, int N, int K, int64_t ldc, int *err) {
+  extern __shared__ uint8_t smraw[];
+  // tiles need 1024-byte alignment (swizzle atoms)
+  uint8_t *sm = reinterpret_cast<uint8_t *>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accum;
+  __shared__ uint32_t tmem_base;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+  const int nk = (K + kBK - 1) / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&accum, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {  // 128 columns: the 128 x 128 fp32 accumulator
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(kBN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % kStages;
+      if (kb >= kStages && !mbar_wait(&empty[s], ((kb / kStages) - 1) & 1, err)) break;
+      uint8_t *a = sm + s * kStageBytes;
+      uint8_t *b = a + kTileBytesA;
+      mbar_arrive_expect_tx(&full[s], kStageBytes);
+      tma_load_2d(a, &tmA, kb * kBK, m0, &full[s]);
+      tma_load_2d(b, &tmB, kb * kBK, n0, &full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    bool ok = true;
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int s = kb % kStages;
+      if (!mbar_wait(&full[s], (kb / kStages) & 1, err)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a = smem_u32(sm + s * kStageBytes);
+      const uint32_t b = a + kTileBytesA;
+#pragma unroll
+      for (int kk = 0; kk < kBK / 16; ++kk) {  // K = 16 per instruction: +32 B
+        const uint64_t da = sw128_desc(a + kk * 32);
+        const uint64_t db = sw128_desc(b + kk * 32);
+        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+            : "memory");
+      }
+      // the stage is free once these MMAs have read it
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&empty[s]))
+          : "memory");
+    }
+    if (ok)
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&accum))
+          : "memory");
+  }
+  __syncwarp();
+
+  // epilogue: all four warps wait for the accumulator
+  bool ready = true;
+  if (lane == 0) ready = mbar_wait(&accum, 0, err);
+  ready = __shfl_sync(0xFFFFFFFFu, ready ? 1 : 0, 0) != 0;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ready) {
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kBN; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+          "%11, %12, %13, %14, %15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < M) {
+        float *crow = C + (int64_t)row * ldc + n0 + c0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (n0 + c0 + j < N) crow[j] = __uint_as_float(v[j]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBN)
+                 : "memory");
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 2-D bf16 tensor map: `rows` rows of `cols` elements, row stride in bytes;
+// box = 64 columns x 128 rows, 128-byte swizzle, zero fill outside.
+bool make_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows, uint64_t row_bytes) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {cols, rows};
+  const cuuint64_t strides[1] = {row_bytes};
+  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+cudaError_t launch_tc_gemm_bf16(const void *A, int64_t lda, const void *B, int64_t ldb, float *C,
+                                int64_t ldc, int M, int N, int K, int *err, cudaStream_t s) {
+  // TMA: 16-byte aligned bases and row strides (lda, ldb in elements)
+  if (M < 1 || N < 1 || K < 1 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15) || (lda * 2) % 16 ||
+      (ldb * 2) % 16 || lda < K || ldb < K || ldc < N)
+    return cudaErrorInvalidValue;
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, A, (uint64_t)K, (uint64_t)M, (uint64_t)lda * 2) ||
+      !make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint64_t)ldb * 2))
+    return cudaErrorInvalidValue;
+  const int smem = kStages * kStageBytes + 1024;
+  cudaError_t e = cudaFuncSetAttribute(k_tc_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((unsigned)((M + kBM - 1) / kBM), (unsigned)((N + kBN - 1) / kBN));
+  k_tc_gemm_bf16<<<grid, kGemmThreads, smem, s>>>(ma, mb, C, M, N, K, ldc, err);
+  return cudaGetLastError();
+}
+
+}  // namespace pa

@@ -1960,6 +1960,29 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
   return PA_OK;
 }
 
+pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, int64_t ldb,
+                       float *C, int64_t ldc, int M, int N, int K) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!A || !B || !C || M < 1 || N < 1 || K < 1 || lda < K || ldb < K || ldc < N || lda % 8 ||
+      ldb % 8 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
+    return fail(ctx, PA_ERR_INVALID, "invalid GEMM operands");
+  DeviceGuard dg(ctx->device);
+  Builder b1;
+  int *err1 = b1.scratch<int>(1);
+  (void)err1;
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  int *err = reinterpret_cast<int *>(ctx->arena);
+  cudaStream_t s = ctx->stream;
+  PA_CK(cudaMemsetAsync(err, 0, sizeof(int), s));
+  PA_LAUNCH("gemm_bf16", launch_tc_gemm_bf16(A, lda, B, ldb, C, ldc, M, N, K, err, s));
+  int flag = 0;
+  PA_CK(cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (pa_status ss = sync_ctx(ctx)) return ss;
+  if (flag) return fail(ctx, PA_ERR_CUDA, "GEMM pipeline wait timed out (flag %d)", flag);
+  return PA_OK;
+}
+
 pa_status pa_find_obj(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
                       const pa_classifier *const *cls, int n_cls, const float *desc, int ny,
                       int nx, int dim, const double *Tig, int tig_shared, int H, int W,

@@ -177,6 +177,11 @@ cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, 
                                 int16_t *tables, int4 *sdesc, cudaStream_t s);
 cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
                             int *err_flag, cudaStream_t s);
+// BF16 GEMM on tcgen05: C[M][N] (fp32) = A[M][K] * B[N][K]^T, bf16 operands
+// with K contiguous (lda, ldb in elements, 16-byte aligned rows).
+cudaError_t launch_tc_gemm_bf16(const void *A, int64_t lda, const void *B, int64_t ldb, float *C,
+                                int64_t ldc, int M, int N, int K, int *err, cudaStream_t s);
+
 // Full-covariance messages of a batch (entries with full == 0 are skipped):
 // forward rotation, eigen-axis x and y passes, rotate-back epilogue.
 cudaError_t launch_msg_full(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int ohmax,
