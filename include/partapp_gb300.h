@@ -52,6 +52,18 @@ pa_status pa_ctx_destroy(pa_ctx *ctx);
 /* Makes the context issue its work on `stream` (a cudaStream_t). */
 pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream);
 pa_status pa_ctx_synchronize(pa_ctx *ctx);
+/* No counterpart in the reference.  Arithmetic of the spatial Gaussian of
+ * diagonal-covariance messages in pa_ps_infer / pa_find_obj*:
+ *   PA_MSG_FP32        (default) FP32 shared-memory filters, the reference's
+ *                      arithmetic (parity as documented for each entry);
+ *   PA_MSG_BF16_TENSOR banded-Toeplitz BF16 products with FP32 accumulation
+ *                      on the tensor cores, for large grids (needs H % 8 == 0,
+ *                      else the FP32 filters run); its error against FP64 is
+ *                      larger than the FP32 path's and is reported by the tests.
+ * pa_rot_joint_marginal always uses FP32. */
+#define PA_MSG_FP32 0
+#define PA_MSG_BF16_TENSOR 1
+pa_status pa_ctx_set_message_math(pa_ctx *ctx, int mode);
 /* Message of the last failing call on this context (never NULL). */
 const char *pa_last_error(const pa_ctx *ctx);
 const char *pa_status_string(pa_status s);

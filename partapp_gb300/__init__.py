@@ -45,8 +45,9 @@ EXPORTS = (
     "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
     "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
     "pa_ps_infer", "pa_rot_joint_marginal", "pa_rot_joint_marginal_noalloc", "pa_find_obj",
-    "pa_find_obj_batch", "pa_gemm_bf16",
+    "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math",
 )
+PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
 
 class PaError(RuntimeError):
@@ -129,6 +130,7 @@ def load_library():
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
                                         dp, dp, dp, ip]
     L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip]
+    L.pa_ctx_set_message_math.argtypes = [vp, ip]
     L.pa_rot_joint_marginal_noalloc.argtypes = [P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp),
                                                  P(dp), dp, dp, dp, vp]
     L.pa_find_obj.argtypes = [vp, P(ExpParam), P(Tree), ip, P(vp), ip, vp, ip, ip, ip, P(dp), ip,
@@ -369,6 +371,11 @@ class Context:
         res["part_hyps"] = ph.reshape(P, -1, 7).copy() if ph.size >= 7 * P else ph.reshape(0, 7)
         res["root_hyps"] = res["root_hyps"][: int(res["n_root_hyps"][0])]
         return res
+
+    def set_message_math(self, mode):
+        """PA_MSG_FP32 (default) or PA_MSG_BF16_TENSOR for the spatial filter
+        of diagonal-covariance messages."""
+        self._check(self.L.pa_ctx_set_message_math(self.h, int(mode)))
 
     def gemm_bf16(self, A, B, out=None):
         """C = A @ B.T on the tensor cores: A [M][K], B [N][K] bf16 CUDA

@@ -22,6 +22,8 @@
 //               the parent frame and the epilogue (store / add / marginal).
 // The nearest-shift source indices come from per-message tables computed
 // with the reference's double-precision rounding (k_shift_tables).
+#include <cuda_bf16.h>
+
 #include "pa_internal.cuh"
 
 namespace pa {
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   float2 *tx = E + ((RP * WP + 1) & ~1);     // x taps {t, t}, zero-padded, 16B aligned
   // x taps (none for a full-covariance message: its spatial filter runs on
   // the rotated grid, and the phase's padx does not cover its kernel)
-  const int xpad = md.full ? 0 : ((md.xlen + kU - 1) / kU) * kU;
+  const int xpad = (md.full || md.tc) ? 0 : ((md.xlen + kU - 1) / kU) * kU;
   float *tr = reinterpret_cast<float *>(tx + xpmax);  // rotation taps
   const int tid = threadIdx.x;
 
@@ -260,6 +262,18 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   }
   __syncthreads();
 
+  if (md.tc) {
+    // tensor-core spatial filter: the rotation-filtered exp map goes out as
+    // bf16 rows of the GEMM operand eb [R*H][wp]
+    const float *Ef = reinterpret_cast<const float *>(E);
+    __nv_bfloat16 *eb = reinterpret_cast<__nv_bfloat16 *>(md.eb);
+    for (int idx = tid; idx < R * ncw; idx += blockDim.x) {
+      const int r = idx / ncw, j = idx - r * ncw;
+      eb[((int64_t)r * H + y) * md.wp + xc0 + j] =
+          __float2bfloat16_rn(Ef[((r >> 1) * WP + padx + j) * 2 + (r & 1)]);
+    }
+    return;
+  }
   if (md.full) {
     // full covariance: the rotation-filtered exp map of the chunk goes out
     // as is; the spatial filter runs on the rotated grid (k_full_*)
@@ -433,7 +447,7 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
                                                            int R, int H, int W, int band,
                                                            int pady, int *err) {
   const MsgDesc md = msgs[blockIdx.z];
-  if (md.full) return;  // k_full_* (uniform for the CTA)
+  if (md.full || md.tc) return;  // k_full_* / the tensor-core path (uniform for the CTA)
   const int r = blockIdx.y % R;
   const int yb = blockIdx.y / R;
   const int y0 = yb * band, y1 = min(H, y0 + band);
@@ -683,6 +697,49 @@ __global__ void __launch_bounds__(kThreadsCols) k_full_epi(const MsgDesc *__rest
 }
 
 // ---------------------------------------------------------------------------
+// Tensor-core spatial filter (large grids): the truncated separable Gaussian
+// as two banded Toeplitz products on tcgen05 (k_tc_gemm.cu).  T[i][j] =
+// t[j - i + k] for |j - i| <= k, 0 elsewhere, in bf16; the reference's
+// truncation at the border is the Toeplitz matrix restricted to the grid.
+// ---------------------------------------------------------------------------
+__global__ void k_tc_toeplitz(const MsgDesc *__restrict__ msgs, int H, int W) {
+  const MsgDesc *md = msgs + blockIdx.y;
+  if (!md->tc) return;
+  const int kx = (md->xlen - 1) / 2, ky = (md->ylen - 1) / 2;
+  __nv_bfloat16 *tx = reinterpret_cast<__nv_bfloat16 *>(md->tbx);
+  __nv_bfloat16 *ty = reinterpret_cast<__nv_bfloat16 *>(md->tby);
+  const int64_t nx = (int64_t)W * md->wp, ny = (int64_t)H * md->hp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nx + ny;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < nx) {
+      const int r = (int)(i / md->wp), c = (int)(i - (int64_t)r * md->wp), d = c - r;
+      tx[i] = __float2bfloat16_rn((d >= -kx && d <= kx && c < W) ? md->xtaps[d + kx] : 0.f);
+    } else {
+      const int64_t k = i - nx;
+      const int r = (int)(k / md->hp), c = (int)(k - (int64_t)r * md->hp), d = c - r;
+      ty[k] = __float2bfloat16_rn((d >= -ky && d <= ky && c < H) ? md->ytaps[d + ky] : 0.f);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreadsCols) k_tc_epi(const MsgDesc *__restrict__ msgs, int R,
+                                                        int H, int W) {
+  __shared__ int red[kThreadsCols / 32];
+  __shared__ unsigned long long redu[kThreadsCols / 32];
+  const MsgDesc md = msgs[blockIdx.z];
+  if (!md.tc) return;
+  const int r = blockIdx.y % R, yb = blockIdx.y / R;
+  const int y0 = yb * kFullBand, y1 = min(H, y0 + kFullBand);
+  const int x0 = blockIdx.x * kTX, x1 = min(W, x0 + kTX);
+  const int16_t *txo = md.tx_out + r * W;
+  const int16_t *tyo = md.ty_out + r * H;
+  const int4 dxo = md.sdesc[2 * R + r], dyo = md.sdesc[3 * R + r];
+  const float *yv = md.yv + (int64_t)r * H * W;
+  msg_epilogue(md, r, H, W, x0, x1, y0, y1, dxo, dyo, txo, tyo, blockIdx.x == 0 && blockIdx.y == 0,
+               [&](int sy, int sx) { return __ldg(yv + (int64_t)sy * W + sx); }, red, redu);
+}
+
+// ---------------------------------------------------------------------------
 // Shift tables: the nearest-neighbour source index of
 // transform_grid_fixed_size with a pure translation
 // (multi_array_transform.hpp:194-215): floor((x3 + a) + 0.5), -1 outside.
@@ -803,6 +860,18 @@ cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W
     case 48: return launch_rows_t<48>(msgs, n_msgs, R, H, W, padx, err, s);
     default: return launch_rows_t<0>(msgs, n_msgs, R, H, W, padx, err, s);
   }
+}
+
+cudaError_t launch_tc_toeplitz(const MsgDesc *msgs, int n_msgs, int H, int W, cudaStream_t s) {
+  k_tc_toeplitz<<<dim3(256, (unsigned)n_msgs), 256, 0, s>>>(msgs, H, W);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_epi(const MsgDesc *msgs, int n_msgs, int R, int H, int W, cudaStream_t s) {
+  k_tc_epi<<<dim3((unsigned)((W + kTX - 1) / kTX), (unsigned)(R * ((H + kFullBand - 1) / kFullBand)),
+                  (unsigned)n_msgs),
+             kThreadsCols, 0, s>>>(msgs, R, H, W);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_msg_full(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int ohmax,

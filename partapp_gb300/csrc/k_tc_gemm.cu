@@ -1,7 +1,12 @@
 // k_tc_gemm.cu -- BF16 GEMM on the fifth-generation tensor cores (tcgen05).
 //
-//   C[M][N] (fp32, row stride ldc) = A[M][K] (bf16, K contiguous)
-//                                   * B[N][K]^T (bf16, K contiguous)
+//   C[M][N] (fp32 or bf16, row stride ldc) = A[M][K] (bf16, K contiguous)
+//                                            * B[N][K]^T (bf16, K contiguous)
+//
+// batched over blockIdx.z (B read at K offset z * b_kofs, C at z * c_batch),
+// optionally banded: a CTA on rows [m0, m0 + 128) reduces only over
+// K in [m0 - band, m0 + 128 + band) (rounded out to 64-element blocks), for
+// banded (Toeplitz) A.
 //
 // One CTA computes a 128 x 128 tile of C.  Operands move global -> shared
 // by TMA (cp.async.bulk.tensor, 128-byte swizzle, 64-element K blocks) in a
@@ -17,6 +22,7 @@
 // Operand rows past M / N and K columns past K are read as zeros (TMA
 // out-of-bounds fill); rows past M / N are not stored.
 #include <cuda.h>
+#include <cuda_bf16.h>
 
 #include "pa_internal.cuh"
 
@@ -96,7 +102,8 @@ constexpr uint32_t kIdesc = (1u << 4)                   // D format: f32
 
 __global__ void __launch_bounds__(kGemmThreads, 1)
     k_tc_gemm_bf16(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   float *__restrict__ C, int M, int N, int K, int64_t ldc, int *err) {
+                   GemmArgs g, int *err) {
+  const int M = g.M, N = g.N;
   extern __shared__ uint8_t smraw[];
   // tiles need 1024-byte alignment (swizzle atoms)
   uint8_t *sm = reinterpret_cast<uint8_t *>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -104,8 +111,14 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   __shared__ uint32_t tmem_base;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
-  const int nk = (K + kBK - 1) / kBK;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN, z = blockIdx.z;
+  int k_lo = 0, k_hi = g.K;
+  if (g.band >= 0) {
+    k_lo = max(0, m0 - g.band) & ~(kBK - 1);
+    k_hi = min(g.K, m0 + kBM + g.band);
+  }
+  const int nk = k_hi > k_lo ? (k_hi - k_lo + kBK - 1) / kBK : 0;
+  const int kb_ofs = z * g.b_kofs;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -135,8 +148,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       uint8_t *a = sm + s * kStageBytes;
       uint8_t *b = a + kTileBytesA;
       mbar_arrive_expect_tx(&full[s], kStageBytes);
-      tma_load_2d(a, &tmA, kb * kBK, m0, &full[s]);
-      tma_load_2d(b, &tmB, kb * kBK, n0, &full[s]);
+      tma_load_2d(a, &tmA, k_lo + kb * kBK, m0, &full[s]);
+      tma_load_2d(b, &tmB, kb_ofs + k_lo + kb * kBK, n0, &full[s]);
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
@@ -176,16 +189,22 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   }
   __syncwarp();
 
-  // epilogue: all four warps wait for the accumulator
+  // epilogue: all four warps wait for the accumulator (an empty K range is
+  // an all-zero tile and never touches it)
   bool ready = true;
-  if (lane == 0) ready = mbar_wait(&accum, 0, err);
+  if (lane == 0 && nk > 0) ready = mbar_wait(&accum, 0, err);
   ready = __shfl_sync(0xFFFFFFFFu, ready ? 1 : 0, 0) != 0;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ready) {
     const int row = m0 + warp * 32 + lane;
+    const int64_t cbase = (int64_t)z * g.c_batch + (int64_t)row * g.ldc;
 #pragma unroll 1
     for (int c0 = 0; c0 < kBN; c0 += 16) {
       uint32_t v[16];
+      if (nk == 0) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0u;
+      } else {
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
@@ -196,11 +215,40 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           : "r"(taddr)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      }
       if (row < M) {
-        float *crow = C + (int64_t)row * ldc + n0 + c0;
+        const int n = n0 + c0;
+        if (g.out_bf16) {
+          __nv_bfloat16 *crow = reinterpret_cast<__nv_bfloat16 *>(g.C) + cbase + n;
+          if (n + 16 <= N && g.vec_ok) {
+            uint32_t h[8];
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-          if (n0 + c0 + j < N) crow[j] = __uint_as_float(v[j]);
+            for (int j = 0; j < 8; ++j) {
+              const __nv_bfloat162 q = __floats2bfloat162_rn(__uint_as_float(v[2 * j]),
+                                                             __uint_as_float(v[2 * j + 1]));
+              h[j] = *reinterpret_cast<const uint32_t *>(&q);
+            }
+            reinterpret_cast<uint4 *>(crow)[0] = make_uint4(h[0], h[1], h[2], h[3]);
+            reinterpret_cast<uint4 *>(crow)[1] = make_uint4(h[4], h[5], h[6], h[7]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              if (n + j < N) crow[j] = __float2bfloat16_rn(__uint_as_float(v[j]));
+          }
+        } else {
+          float *crow = reinterpret_cast<float *>(g.C) + cbase + n;
+          if (n + 16 <= N && g.vec_ok) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              reinterpret_cast<float4 *>(crow)[j] =
+                  make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
+                              __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              if (n + j < N) crow[j] = __uint_as_float(v[j]);
+          }
+        }
       }
     }
   }
@@ -247,23 +295,42 @@ bool make_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows, ui
 
 }  // namespace
 
-cudaError_t launch_tc_gemm_bf16(const void *A, int64_t lda, const void *B, int64_t ldb, float *C,
-                                int64_t ldc, int M, int N, int K, int *err, cudaStream_t s) {
-  // TMA: 16-byte aligned bases and row strides (lda, ldb in elements)
-  if (M < 1 || N < 1 || K < 1 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15) || (lda * 2) % 16 ||
-      (ldb * 2) % 16 || lda < K || ldb < K || ldc < N)
+cudaError_t launch_tc_gemm(const void *A, int64_t lda, int64_t a_rows, int64_t a_cols,
+                           const void *B, int64_t ldb, int64_t b_rows, int64_t b_cols,
+                           const GemmArgs &g0, int batch, int *err, cudaStream_t s) {
+  GemmArgs g = g0;
+  // TMA: 16-byte aligned bases and row strides (lda, ldb in elements); the
+  // batch offset of B is a TMA coordinate and must be a multiple of 8
+  if (g.M < 1 || g.N < 1 || g.K < 1 || batch < 1 || batch > 65535 || ((uintptr_t)A & 15) ||
+      ((uintptr_t)B & 15) || (lda * 2) % 16 || (ldb * 2) % 16 || g.b_kofs % 8 || a_rows < g.M ||
+      b_rows < g.N || g.ldc < g.N || a_cols > lda || b_cols > ldb || a_cols < 1 || b_cols < 1)
     return cudaErrorInvalidValue;
+  const int esz = g.out_bf16 ? 2 : 4;
+  g.vec_ok = ((uintptr_t)g.C % 16 == 0) && (g.ldc * esz) % 16 == 0 && (g.c_batch * esz) % 16 == 0;
   CUtensorMap ma, mb;
-  if (!make_map(&ma, A, (uint64_t)K, (uint64_t)M, (uint64_t)lda * 2) ||
-      !make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint64_t)ldb * 2))
+  if (!make_map(&ma, A, (uint64_t)a_cols, (uint64_t)a_rows, (uint64_t)lda * 2) ||
+      !make_map(&mb, B, (uint64_t)b_cols, (uint64_t)b_rows, (uint64_t)ldb * 2))
     return cudaErrorInvalidValue;
   const int smem = kStages * kStageBytes + 1024;
   cudaError_t e = cudaFuncSetAttribute(k_tc_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)((M + kBM - 1) / kBM), (unsigned)((N + kBN - 1) / kBN));
-  k_tc_gemm_bf16<<<grid, kGemmThreads, smem, s>>>(ma, mb, C, M, N, K, ldc, err);
+  dim3 grid((unsigned)((g.M + kBM - 1) / kBM), (unsigned)((g.N + kBN - 1) / kBN), (unsigned)batch);
+  k_tc_gemm_bf16<<<grid, kGemmThreads, smem, s>>>(ma, mb, g, err);
   return cudaGetLastError();
+}
+
+cudaError_t launch_tc_gemm_bf16(const void *A, int64_t lda, const void *B, int64_t ldb, float *C,
+                                int64_t ldc, int M, int N, int K, int *err, cudaStream_t s) {
+  if (lda < K || ldb < K) return cudaErrorInvalidValue;
+  GemmArgs g{};
+  g.C = C;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.ldc = ldc;
+  g.band = -1;
+  return launch_tc_gemm(A, lda, M, K, B, ldb, N, K, g, 1, err, s);
 }
 
 }  // namespace pa

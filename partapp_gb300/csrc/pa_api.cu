@@ -65,6 +65,7 @@ struct pa_ctx {
   };
   std::map<std::string, Acc> times;
   std::vector<std::string> names;  // stable storage for pa_ctx_timing_get
+  int msg_math = PA_MSG_FP32;      // spatial filter of diagonal-covariance messages
 };
 
 namespace {
@@ -588,7 +589,15 @@ struct PsPlan {
     MsgDesc *msgs = nullptr;
     int n = 0, padx = 0, pady = 0;
     int n_full = 0, ohmax = 0, owmax = 0, kxf = 0, kyf = 0;  // full-covariance messages
+    struct TcJob {
+      void *eb, *xt, *tbx, *tby;
+      float *yv;
+      int kx, ky;
+    };
+    std::vector<TcJob> tc;  // tensor-core messages
   };
+  bool tc_mode = false;  // diagonal-covariance messages on the tensor cores (H % 8 == 0)
+  int wp = 0, hp = 0;
   std::vector<Phase> up, down;
   RootDesc *roots = nullptr;
   int16_t *tables = nullptr;
@@ -713,6 +722,28 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
       g0[k] = b.scratch<float>((size_t)R * slot_cells[k]);
       g1[k] = b.scratch<float>((size_t)R * slot_cells[k]);
     }
+  // tensor-core messages: bf16 operands and the fp32 y-pass result per slot
+  const bool tc = pl.tc_mode && (H % 8) == 0;
+  pl.wp = (W + 7) / 8 * 8;
+  pl.hp = (H + 7) / 8 * 8;
+  std::vector<bool> slot_tc(maxph, false);
+  for (auto *all : {&upmp, &dnmp})
+    for (auto &v : *all)
+      for (size_t k = 0; k < v.size(); ++k)
+        if (tc && !v[k].full) slot_tc[k] = true;
+  struct TcBufs {
+    uint16_t *eb = nullptr, *xt = nullptr, *tbx = nullptr, *tby = nullptr;
+    float *yv = nullptr;
+  };
+  std::vector<TcBufs> tcb(maxph);
+  for (size_t k = 0; k < maxph; ++k)
+    if (slot_tc[k]) {
+      tcb[k].eb = b.scratch<uint16_t>((size_t)R * H * pl.wp);
+      tcb[k].xt = b.scratch<uint16_t>((size_t)W * R * H);
+      tcb[k].tbx = b.scratch<uint16_t>((size_t)W * pl.wp);
+      tcb[k].tby = b.scratch<uint16_t>((size_t)H * pl.hp);
+      tcb[k].yv = b.scratch<float>((size_t)R * H * W);
+    }
 
   pl.n_msgs_total = 0;
   for (auto &ph : upph) pl.n_msgs_total += (int)ph.size();
@@ -727,6 +758,7 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
     std::vector<MsgDesc> descs(ph.size());
     out.n = (int)ph.size();
     out.padx = out.pady = 0;
+    out.tc.clear();
     for (size_t k = 0; k < ph.size(); ++k) {
       const M &mm = ph[k];
       const int c = mm.child;
@@ -767,6 +799,17 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
         out.owmax = std::max(out.owmax, mp.ow);
         out.kxf = std::max(out.kxf, (mp.xlen - 1) / 2);
         out.kyf = std::max(out.kyf, (mp.ylen - 1) / 2);
+      } else if (slot_tc[k]) {
+        d.tc = 1;
+        d.wp = pl.wp;
+        d.hp = pl.hp;
+        d.eb = tcb[k].eb;
+        d.xt = tcb[k].xt;
+        d.tbx = tcb[k].tbx;
+        d.tby = tcb[k].tby;
+        d.yv = tcb[k].yv;
+        out.tc.push_back({tcb[k].eb, tcb[k].xt, tcb[k].tbx, tcb[k].tby, tcb[k].yv,
+                          (mp.xlen - 1) / 2, (mp.ylen - 1) / 2});
       } else {
         out.padx = std::max(out.padx, (mp.xlen - 1) / 2);
         out.pady = std::max(out.pady, (mp.ylen - 1) / 2);
@@ -888,27 +931,53 @@ void plan_localmax(Builder &b, PsPlan &pl, const pa_exp_param *e, const pa_ps_ou
 pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   cudaStream_t st = ctx->stream;
   const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
+  auto run_phase = [&](const PsPlan::Phase &ph) -> pa_status {
+    PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
+    if (ph.n_full + (int)ph.tc.size() < ph.n)
+      PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
+    if (ph.n_full)
+      PA_LAUNCH_N("msg_full", 4, launch_msg_full(ph.msgs, ph.n, R, H, W, ph.ohmax, ph.owmax,
+                                                 ph.kxf, ph.kyf, pl.err, st));
+    if (!ph.tc.empty()) {
+      PA_LAUNCH("msg_tc", launch_tc_toeplitz(ph.msgs, ph.n, H, W, st));
+      for (const auto &j : ph.tc) {
+        GemmArgs gx{};  // X^T [W][R*H] = Tx * E'^T, banded by kx, bf16 out
+        gx.C = j.xt;
+        gx.M = W;
+        gx.N = R * H;
+        gx.K = W;
+        gx.ldc = (int64_t)R * H;
+        gx.band = j.kx;
+        gx.out_bf16 = 1;
+        PA_LAUNCH("msg_tc", launch_tc_gemm(j.tbx, pl.wp, W, W, j.eb, pl.wp, (int64_t)R * H, W, gx,
+                                           1, pl.err, st));
+        GemmArgs gy{};  // Y_r [H][W] = Ty * X_r, banded by ky, fp32 out, batched over r
+        gy.C = j.yv;
+        gy.M = H;
+        gy.N = W;
+        gy.K = H;
+        gy.ldc = W;
+        gy.c_batch = (int64_t)H * W;
+        gy.b_kofs = H;
+        gy.band = j.ky;
+        PA_LAUNCH("msg_tc", launch_tc_gemm(j.tby, pl.hp, H, H, j.xt, (int64_t)R * H, W,
+                                           (int64_t)R * H, gy, R, pl.err, st));
+      }
+      PA_LAUNCH("msg_tc", launch_tc_epi(ph.msgs, ph.n, R, H, W, st));
+    }
+    return PA_OK;
+  };
   if (e->use_pairwise) {
     if (pl.n_msgs_total > 0)
       PA_LAUNCH_N("shift_tables", 2, launch_shift_tables(pl.shifts, pl.n_msgs_total, R, H, W, pl.tables, pl.sdesc, st));
     for (auto &ph : pl.up) {
       if (!ph.n) continue;
-      PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
-      if (ph.n_full < ph.n)
-        PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
-      if (ph.n_full)
-        PA_LAUNCH_N("msg_full", 4, launch_msg_full(ph.msgs, ph.n, R, H, W, ph.ohmax, ph.owmax,
-                                                   ph.kxf, ph.kyf, pl.err, st));
+      if (pa_status s2 = run_phase(ph)) return s2;
     }
     PA_LAUNCH("root_combine", launch_root_combine(pl.roots, B, pl.N, st));
     for (auto &ph : pl.down) {
       if (!ph.n) continue;
-      PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
-      if (ph.n_full < ph.n)
-        PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
-      if (ph.n_full)
-        PA_LAUNCH_N("msg_full", 4, launch_msg_full(ph.msgs, ph.n, R, H, W, ph.ohmax, ph.owmax,
-                                                   ph.kxf, ph.kyf, pl.err, st));
+      if (pa_status s2 = run_phase(ph)) return s2;
     }
     PA_LAUNCH("root_posterior", launch_root_posterior(pl.post_root_ptrs, pl.root_post_ptrs, pl.keep, pl.n_keep, B,
                                     R, H, W, st));
@@ -1036,6 +1105,8 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
   }
   if (errflag & 1)
     return fail(ctx, PA_ERR_NUMERIC, "exp() overflowed in a message (the reference asserts here)");
+  if (errflag & 8)
+    return fail(ctx, PA_ERR_CUDA, "tensor-core pipeline wait timed out (code %d)", errflag);
   if (errflag & ~1)
     return fail(ctx, PA_ERR_UNSUPPORTED, "message kernel rejected its input (code %d)", errflag);
   return PA_OK;
@@ -1203,6 +1274,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
                         int H, int W, float *scores_out, int64_t scores_field0,
                         int64_t scores_fields, const pa_ps_outputs *outs, int mem) {
   PsPlan pl;
+  pl.tc_mode = ctx->msg_math == PA_MSG_BF16_TENSOR;
   pa_status st = build_sched(ctx, &trees[0], pl.sc);
   if (st) return st;
   for (int i = 1; i < n_img; ++i)
@@ -1472,6 +1544,14 @@ pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream) {
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   ctx->stream = (cudaStream_t)stream;
   ctx->own_stream = false;
+  return PA_OK;
+}
+
+pa_status pa_ctx_set_message_math(pa_ctx *ctx, int mode) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (mode != PA_MSG_FP32 && mode != PA_MSG_BF16_TENSOR)
+    return fail(ctx, PA_ERR_INVALID, "unknown message math %d", mode);
+  ctx->msg_math = mode;
   return PA_OK;
 }
 
@@ -1811,6 +1891,7 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
     return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
   if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
   PsPlan pl;
+  pl.tc_mode = ctx->msg_math == PA_MSG_BF16_TENSOR;
   pa_status st = build_sched(ctx, tree, pl.sc);
   if (st) return st;
   std::vector<std::vector<Joint>> joints(1);

@@ -129,6 +129,16 @@ struct MsgDesc {
   float *g0, *g1;
   double tf[6];           // rotated-grid cell (x3, y3) -> e2 position (x1, y1)
   double tb[6];           // image cell (x3, y3) -> rotated-grid position
+  // tensor-core spatial filter (diagonal C, BF16 operands, FP32 accumulation):
+  // the row pass writes the rotation-filtered exp map as bf16 eb [R*H][W]
+  // (row stride wp); x pass X^T = Tx * eb^T (xt [W][R*H], bf16), y pass
+  // Y_r = Ty * X_r (yv [R][H][W], fp32), then the epilogue
+  int tc;
+  int wp;                 // row stride of eb (elements, multiple of 8)
+  void *eb, *xt;          // bf16
+  float *yv;
+  void *tbx, *tby;        // bf16 banded Toeplitz matrices [W][W], [H][H] (row strides wp, hp)
+  int hp;
 };
 
 struct RootDesc {
@@ -179,8 +189,28 @@ cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W
                             int *err_flag, cudaStream_t s);
 // BF16 GEMM on tcgen05: C[M][N] (fp32) = A[M][K] * B[N][K]^T, bf16 operands
 // with K contiguous (lda, ldb in elements, 16-byte aligned rows).
+struct GemmArgs {
+  void *C;          // fp32 or bf16 output
+  int M, N, K;      // K: the reduction length (columns of A and of B per batch)
+  int64_t ldc;      // output row stride (elements)
+  int64_t c_batch;  // output offset per batch (elements)
+  int b_kofs;       // K offset of B per batch (elements, multiple of 8)
+  int band;         // < 0: full K; else the half-width of a banded A
+  int out_bf16;
+  int vec_ok;       // set by the launcher
+};
+// A: a_rows x a_cols elements (row stride lda), B: b_rows x b_cols (stride
+// ldb); reads outside these extents are zeros; batch = grid.z.
+cudaError_t launch_tc_gemm(const void *A, int64_t lda, int64_t a_rows, int64_t a_cols,
+                           const void *B, int64_t ldb, int64_t b_rows, int64_t b_cols,
+                           const GemmArgs &g, int batch, int *err, cudaStream_t s);
 cudaError_t launch_tc_gemm_bf16(const void *A, int64_t lda, const void *B, int64_t ldb, float *C,
                                 int64_t ldc, int M, int N, int K, int *err, cudaStream_t s);
+
+// Tensor-core messages of a batch (entries with tc == 0 are skipped): the
+// Toeplitz matrices, then the epilogue after the caller's GEMMs.
+cudaError_t launch_tc_toeplitz(const MsgDesc *msgs, int n_msgs, int H, int W, cudaStream_t s);
+cudaError_t launch_tc_epi(const MsgDesc *msgs, int n_msgs, int R, int H, int W, cudaStream_t s);
 
 // Full-covariance messages of a batch (entries with full == 0 are skipped):
 // forward rotation, eigen-axis x and y passes, rotate-back epilogue.

@@ -133,3 +133,38 @@ def test_full_size_ps_properties(ctx):
         col = mr[:, y, x]
         want = col.max() + math.log(np.exp(col - col.max()).sum())
         assert abs(rp[y, x] - want) <= 1e-4 * max(1.0, abs(want))
+
+
+def test_bf16_tensor_path_error_vs_fp64(ctx, orc):
+    """The BF16 banded-Toeplitz spatial filter (tcgen05, FP32 accumulation):
+    per-part error of the marginals against the FP64 oracle, next to the
+    FP32 shared-memory path's.  Message arithmetic in BF16 carries about
+    2^-9 relative rounding per operand, so its bound is looser than the FP32
+    path's 1e-3; the argmax must still land on the FP64 maximum or on a cell
+    within the same error of it."""
+    import partapp_gb300 as pa
+
+    rng = np.random.default_rng(4096)
+    H, W = 128, 160
+    tree = large_tree(rng)
+    u = lognormal_unary(rng, 10, H, W)
+    e = orc.make_exp(R=R)
+    want64 = orc.ps_infer(e, tree, u.astype(np.float64), f64=True, want_hyps=False)
+    fp32 = ctx.compute_root_posterior_rot(_exp(), tree, u)
+    ctx.set_message_math(pa.PA_MSG_BF16_TENSOR)
+    try:
+        bf16 = ctx.compute_root_posterior_rot(_exp(), tree, u)
+    finally:
+        ctx.set_message_math(pa.PA_MSG_FP32)
+    errs = []
+    for p in range(10):
+        e32 = maxnorm_err(fp32["log_marg"][p], want64["log_marg"][p])
+        e16 = maxnorm_err(bf16["log_marg"][p], want64["log_marg"][p])
+        errs.append((p, e32, e16))
+        assert e32 <= 1e-3
+        assert e16 <= 5e-3, (p, e16)
+        m = want64["log_marg"][p].reshape(-1)
+        b = bf16["best_conf"][p]
+        flat = (int(b[2]) * H + int(b[5])) * W + int(b[4])
+        assert m.max() - m[flat] <= 5e-3, p
+    print("per-part max-normalised error vs FP64 (part, fp32, bf16):", errs)
