@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--e2e-batch", type=int, default=8,
                     help="images per end-to-end call (host descriptors through the copy ring)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--grid", type=int, default=1024, help="large-grid: H = W")
+    ap.add_argument("--workload", choices=["find_obj", "large-grid"], default="find_obj",
+                    help="large-grid: the 1024x1024, 48-rotation PS (log-normal unaries, "
+                         "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic")
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1234)
@@ -374,8 +378,70 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_large_grid(args):
+    """PS marginals of the 1024 x 1024 x 48 workload on one GPU: one image per
+    step, log-normal unaries resident in HBM, FP32 shared-memory filters and
+    the BF16 banded-Toeplitz tensor-core filters, with their difference."""
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build, synth
+
+    build.build()
+    dev = torch.device("cuda:0")
+    ctx = pa.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    RL, HL, WL = 48, args.grid, args.grid
+    rng = np.random.default_rng(args.seed)
+    tree = synth.make_tree(rng, R=RL, offset_range=(10.0, 40.0), sigma_range=(4.0, 24.0))
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed)
+    u = torch.randn((P, RL, HL, WL), generator=g, device=dev, dtype=torch.float32)
+    e = pa.exp_param(R=RL, local_max=1000)
+    out = {}
+    for name, mode in (("fp32", pa.PA_MSG_FP32), ("bf16_tensor", pa.PA_MSG_BF16_TENSOR)):
+        ctx.set_message_math(mode)
+        for _ in range(max(3, args.warmup)):
+            res = ctx.compute_root_posterior_rot(e, tree, u)
+        torch.cuda.synchronize(dev)
+        ctx.reset_timing()
+        ctx.enable_timing(True)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(1, args.steps // 4)
+        t0.record(stream)
+        for _ in range(steps):
+            res = ctx.compute_root_posterior_rot(e, tree, u)
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        ctx.enable_timing(False)
+        ms = t0.elapsed_time(t1) / steps
+        kt = {k: round(v[0] / steps, 3) for k, v in sorted(ctx.kernel_times().items(),
+                                                             key=lambda kv: -kv[1][0])}
+        out[name] = {"value": 1e3 / ms, "ms_per_image": ms, "kernels_ms": kt,
+                     "marg": res["log_marg"]}
+    ctx.set_message_math(pa.PA_MSG_FP32)
+    diff = 0.0
+    for p in range(P):
+        a, b = out["fp32"]["marg"][p].double(), out["bf16_tensor"]["marg"][p].double()
+        diff = max(diff, float((torch.exp(a - a.max()) - torch.exp(b - b.max())).abs().max()))
+    for v in out.values():
+        v.pop("marg")
+    line = {"metric": f"images/s (PS marginals, {HL}x{WL}, R=48)", "unit": "images/s",
+            "n_gpus": 1, "steps": max(1, args.steps // 4), "higher_is_better": True,
+            "data": "synthetic", "dtype": "f32 / bf16-tensor",
+            "config": {"workload": f"PS {HL}x{WL}, R=48, 10 parts, sigma 4-24 px, log-normal unaries"},
+            "fp32": out["fp32"], "bf16_tensor": out["bf16_tensor"],
+            "max_normalised_marginal_diff_bf16_vs_fp32": diff}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.workload == "large-grid":
+        run_large_grid(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -259,10 +259,11 @@ pa_status pa_rot_joint_marginal_noalloc(const pa_exp_param *ep, const float *chi
  * large-grid message path is built on, exposed so that it can be checked on
  * its own: C[M][N] = A[M][K] * B[N][K]^T with bf16 operands (K contiguous,
  * row strides lda, ldb in elements, multiples of 8, 16-byte aligned bases)
- * and fp32 accumulation and output (row stride ldc).  Device pointers;
- * returns after the product is complete. */
+ * and fp32 accumulation and output (row stride ldc).  band >= 0 declares A
+ * banded (A[m][k] = 0 for |k - m| > band: only the band is read); band < 0:
+ * dense.  Device pointers; returns after the product is complete. */
 pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, int64_t ldb,
-                       float *C, int64_t ldc, int M, int N, int K);
+                       float *C, int64_t ldc, int M, int N, int K, int band);
 
 /* ---------------------------------------------------- the --find_obj path */
 
@@ -293,6 +294,29 @@ pa_status pa_find_obj_batch(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
                             int n_cls, const float *desc, int ny, int nx, int dim,
                             const double *Tig, int tig_shared, int H, int W, float *scores_out,
                             const pa_ps_outputs *out, int mem);
+
+/* One image of pa_find_obj_multi: its own experiment parameters (rotation
+ * count), tree, sizes, transform and outputs. */
+typedef struct {
+  const pa_exp_param *ep;
+  const pa_tree *tree;
+  int flip;
+  const float *desc;      /* [R][ny][nx][dim] in the call's `mem` space */
+  int ny, nx, dim;
+  const double *Tig;      /* as pa_find_obj */
+  int tig_shared;
+  int H, W;
+  const pa_ps_outputs *out;
+} pa_image;
+
+/* The image loop of findObjectDataset (objectdetect_aux.cpp:322-406) over
+ * images of uneven sizes and rotation counts: images that share parameters,
+ * sizes and a shared Tig run together as one batch (one launch per pipeline
+ * phase for all of them, descriptors read where they lie), the groups one
+ * after another on the context's stream.  Results equal pa_find_obj per
+ * image. */
+pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
+                            const pa_classifier *const *cls, int n_cls, int mem);
 
 #ifdef __cplusplus
 }

@@ -45,9 +45,15 @@ EXPORTS = (
     "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
     "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
     "pa_ps_infer", "pa_rot_joint_marginal", "pa_rot_joint_marginal_noalloc", "pa_find_obj",
-    "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math",
+    "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math", "pa_find_obj_multi",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
+
+
+class Image(C.Structure):
+    _fields_ = [("ep", C.c_void_p), ("tree", C.c_void_p), ("flip", C.c_int), ("desc", C.c_void_p),
+                ("ny", C.c_int), ("nx", C.c_int), ("dim", C.c_int), ("Tig", C.c_void_p),
+                ("tig_shared", C.c_int), ("H", C.c_int), ("W", C.c_int), ("out", C.c_void_p)]
 
 
 class PaError(RuntimeError):
@@ -129,8 +135,9 @@ def load_library():
     L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, vp, ip, ip, P(PsOutputs), ip]
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
                                         dp, dp, dp, ip]
-    L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip]
+    L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip, ip]
     L.pa_ctx_set_message_math.argtypes = [vp, ip]
+    L.pa_find_obj_multi.argtypes = [vp, ip, P(Image), P(vp), ip, ip]
     L.pa_rot_joint_marginal_noalloc.argtypes = [P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp),
                                                  P(dp), dp, dp, dp, vp]
     L.pa_find_obj.argtypes = [vp, P(ExpParam), P(Tree), ip, P(vp), ip, vp, ip, ip, ip, P(dp), ip,
@@ -372,6 +379,34 @@ class Context:
         res["root_hyps"] = res["root_hyps"][: int(res["n_root_hyps"][0])]
         return res
 
+    def find_obj_multi(self, images, cls_list, want_marg=False):
+        """images: list of dicts {exp, tree, desc [R][ny][nx][dim], Tig, H, W,
+        flip=False} of possibly different sizes and rotation counts; all
+        descriptors numpy (host) or all CUDA tensors (device)."""
+        keep, imgs, results = [], [], []
+        mem = None
+        for im in images:
+            d = _Buf(im["desc"], np.float32)
+            mem = d.mem if mem is None else mem
+            if d.mem != mem:
+                raise ValueError("all descriptors must live in the same memory space")
+            R, ny, nx, dim = d.arr.shape
+            th = _TreeHolder(im["tree"])
+            P = th.s.n_parts
+            T = np.ascontiguousarray(im["Tig"], dtype=np.float64).reshape(-1)
+            exp = im["exp"]
+            res, o = self._outputs(P, R, im["H"], im["W"], exp.roi_save_num_samples, d.mem, d.arr,
+                                   want_marg)
+            keep += [d, th, T, exp, o]
+            imgs.append(Image(C.addressof(exp), C.addressof(th.s), int(im.get("flip", False)),
+                              d.ptr, ny, nx, dim, T.ctypes.data, 1, im["H"], im["W"],
+                              C.addressof(o)))
+            results.append((res, P))
+        arr = (Image * len(imgs))(*imgs)
+        self._check(self.L.pa_find_obj_multi(self.h, len(imgs), arr, self._cls_array(cls_list),
+                                             len(cls_list), mem))
+        return [self._finish(res, P) for res, P in results]
+
     def set_message_math(self, mode):
         """PA_MSG_FP32 (default) or PA_MSG_BF16_TENSOR for the spatial filter
         of diagonal-covariance messages."""
@@ -388,7 +423,19 @@ class Context:
         N = B.shape[0]
         C_ = out if out is not None else torch.empty((M, N), dtype=torch.float32, device=A.device)
         self._check(self.L.pa_gemm_bf16(self.h, A.data_ptr(), A.stride(0), B.data_ptr(),
-                                        B.stride(0), C_.data_ptr(), C_.stride(0), M, N, K))
+                                        B.stride(0), C_.data_ptr(), C_.stride(0), M, N, K, -1))
+        return C_
+
+    def gemm_bf16_banded(self, A, B, band):
+        """C = A @ B.T for a banded A (A[m][k] = 0 for |k - m| > band)."""
+        import torch
+
+        M, K = A.shape
+        N = B.shape[0]
+        C_ = torch.empty((M, N), dtype=torch.float32, device=A.device)
+        self._check(self.L.pa_gemm_bf16(self.h, A.data_ptr(), A.stride(0), B.data_ptr(),
+                                        B.stride(0), C_.data_ptr(), C_.stride(0), M, N, K,
+                                        int(band)))
         return C_
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,

@@ -103,7 +103,7 @@ def build_host() -> str:
     """The C++ host layer (partapp_gpu.hpp) and the partapp_find_obj CLI,
     linked against the C-ABI library (rpath $ORIGIN)."""
     srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
-    deps = srcs + [os.path.join(HOST, "partapp_gpu.hpp"), LIB,
+    deps = srcs + [os.path.join(HOST, "partapp_gpu.hpp"), os.path.join(HOST, "mat_io.hpp"), LIB,
                    os.path.join(ROOT, "include", "partapp_gb300.h")]
     if _stale(CLI, deps):
         cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"

@@ -22,6 +22,7 @@ constexpr int kLoc = 32;
 
 __global__ void __launch_bounds__(512) k_score_grids(const StumpPart *__restrict__ parts,
                                                      int n_parts, const float *__restrict__ desc,
+                                                     const float *const *__restrict__ fields,
                                                      int64_t n_loc, int dim, int dp,
                                                      int normalize, float *__restrict__ scores,
                                                      int n_fields) {
@@ -29,7 +30,7 @@ __global__ void __launch_bounds__(512) k_score_grids(const StumpPart *__restrict
   const int field = blockIdx.y;
   const int64_t loc0 = (int64_t)blockIdx.x * kLoc;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const float *src = desc + ((int64_t)field * n_loc + loc0) * dim;
+  const float *src = (fields ? fields[field] : desc + (int64_t)field * n_loc * dim) + loc0 * dim;
   const int nl = (n_loc - loc0) < kLoc ? (int)(n_loc - loc0) : kLoc;
 
   // Stage the tile: warp-contiguous global reads, swizzled conflict-free stores.
@@ -134,7 +135,8 @@ constexpr int kMaxWarps = 11;
 template <int DIM>
 __global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
     const StumpPart *__restrict__ parts, int n_parts, int n_groups, int group_size,
-    const float *__restrict__ desc, int64_t n_loc, int normalize, float *__restrict__ scores,
+    const float *__restrict__ desc, const float *const *__restrict__ fields, int64_t n_loc,
+    int normalize, float *__restrict__ scores,
     int n_fields) {
   static_assert(DIM % 32 == 0, "DIM must be a multiple of 32");
   constexpr int kCpr = DIM / 4;          // float4 chunks per row
@@ -183,7 +185,8 @@ __global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
     const int field = (int)(tt / blocks_per_field);
     const int64_t loc0 = (tt - (int64_t)field * blocks_per_field) * kLoc;
     const int nl = (n_loc - loc0) < kLoc ? (int)(n_loc - loc0) : kLoc;
-    const float4 *src = reinterpret_cast<const float4 *>(desc + ((int64_t)field * n_loc + loc0) * DIM) +
+    const float *fb = fields ? fields[field] : desc + (int64_t)field * n_loc * DIM;
+    const float4 *src = reinterpret_cast<const float4 *>(fb + loc0 * DIM) +
                         lrow * kCpr + 24 * warp + lchunk;
 #pragma unroll
     for (int k = 0; k < kChunks; ++k) {
@@ -242,12 +245,13 @@ __global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
 
 cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
                                const int *n_stumps, int n_parts, const float *desc,
+                               const float *const *fields, bool fields_aligned,
                                int64_t n_loc, int n_fields, int dim, int normalize,
                                float *scores, cudaStream_t s) {
   // pipelined kernel: groups of <= kMaxWarps classifiers with resident
   // stump tables; needs 960-dim descriptors, unit polarities and room for
   // the tables next to the 32 x 961 tile.
-  const bool aligned = ((uintptr_t)desc & 15) == 0;
+  const bool aligned = fields ? fields_aligned : ((uintptr_t)desc & 15) == 0;
   bool all_fast = true;
   for (int p = 0; p < n_parts; ++p) all_fast = all_fast && fast_ok[p];
   const int n_groups = (n_parts + kMaxWarps - 1) / kMaxWarps;
@@ -272,7 +276,7 @@ cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
     if (per_group < 1) per_group = 1;
     if (per_group > n_tiles) per_group = n_tiles;
     k_score_grids_pipe<960><<<(unsigned)(per_group * n_groups), 32 * launch_warps, smem_pipe, s>>>(
-        parts_dev, n_parts, n_groups, nw, desc, n_loc, normalize, scores, n_fields);
+        parts_dev, n_parts, n_groups, nw, desc, fields, n_loc, normalize, scores, n_fields);
     return cudaGetLastError();
   }
   const int dp = (dim + 31) & ~31;
@@ -286,7 +290,7 @@ cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
   const int gw = n_parts < 16 ? n_parts : 16;
   dim3 grid((unsigned)((n_loc + kLoc - 1) / kLoc), (unsigned)n_fields,
             (unsigned)((n_parts + gw - 1) / gw));
-  k_score_grids<<<grid, 32 * gw, smem, s>>>(parts_dev, n_parts, desc, n_loc, dim, dp, normalize,
+  k_score_grids<<<grid, 32 * gw, smem, s>>>(parts_dev, n_parts, desc, fields, n_loc, dim, dp, normalize,
                                             scores, n_fields);
   return cudaGetLastError();
 }

@@ -1270,7 +1270,8 @@ std::vector<int> stump_counts(const pa_classifier *const *cls, int n) {
 // call fills fields [scores_field0, scores_field0 + n_img*R) of it.
 pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
                         int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
-                        int in_mem, int ny, int nx, int dim, const double *Tig, int tig_shared,
+                        const float *const *img_desc, int in_mem, int ny, int nx, int dim,
+                        const double *Tig, int tig_shared,
                         int H, int W, float *scores_out, int64_t scores_field0,
                         int64_t scores_fields, const pa_ps_outputs *outs, int mem) {
   PsPlan pl;
@@ -1315,6 +1316,17 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
       (mem == PA_MEM_DEVICE && scores_out && scores_field0 == 0 && scores_fields == n_fields);
   StumpPart *sp = plan_stumps(b1, cls, n_cls);
   const float *desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b1.scratch<float>(n_fields * G * dim);
+  // per-field descriptor pointers when the images are separate device buffers
+  std::vector<const float *> fptr;
+  bool fields_al = true;
+  if (img_desc) {
+    for (int i = 0; i < n_img; ++i)
+      for (int r = 0; r < R; ++r) {
+        fptr.push_back(img_desc[i] + (size_t)r * G * dim);
+        fields_al = fields_al && ((uintptr_t)fptr.back() & 15) == 0;
+      }
+  }
+  const float *const *fields_dev = img_desc ? b1.param(fptr.data(), fptr.size()) : nullptr;
   float *scores = scores_dev_out ? scores_out : b1.scratch<float>((size_t)n_cls * n_fields * G);
   plan_ps(b1, pl, e, joints, marg_out.data(), rp_out.data());
   plan_marg_ptrs(b1, pl);
@@ -1336,6 +1348,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   PsPlan pl2 = pl;
   sp = plan_stumps(b, cls, n_cls);
   desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b.scratch<float>(n_fields * G * dim);
+  fields_dev = img_desc ? b.param(fptr.data(), fptr.size()) : nullptr;
   scores = scores_dev_out ? scores_out : b.scratch<float>((size_t)n_cls * n_fields * G);
   plan_ps(b, pl2, e, joints, marg_out.data(), rp_out.data());
   plan_marg_ptrs(b, pl2);
@@ -1360,7 +1373,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   cudaStream_t s = ctx->stream;
   const std::vector<char> ff = fast_flags(cls, n_cls);
   const std::vector<int> ns = stump_counts(cls, n_cls);
-  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_cls, desc_dev, G,
+  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_cls, desc_dev, fields_dev, fields_al, G,
                                               (int)n_fields, dim, 1, scores, s));
   if (scores_out && !scores_dev_out)
     PA_CK(cudaMemcpy2DAsync(scores_out + scores_field0 * G, (size_t)scores_fields * G * sizeof(float),
@@ -1387,8 +1400,8 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
 // max(copy, compute) per image instead of their sum.
 pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
                         int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
-                        int ny, int nx, int dim, const double *Tig, int tig_shared, int H, int W,
-                        float *scores_out, const pa_ps_outputs *outs) {
+                        const float *const *img_desc, int ny, int nx, int dim, const double *Tig,
+                        int tig_shared, int H, int W, float *scores_out, const pa_ps_outputs *outs) {
   DeviceGuard dg(ctx->device);
   const int R = e->num_rotation_steps;
   const size_t per_img = (size_t)R * ny * nx * dim;
@@ -1418,7 +1431,8 @@ pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   }
   auto issue = [&](int i) -> pa_status {
     const int k = i % nslots;
-    PA_CK(cudaMemcpyAsync(ctx->ring + k * bytes, desc + i * per_img, bytes, cudaMemcpyHostToDevice,
+    const float *src = img_desc ? img_desc[i] : desc + i * per_img;
+    PA_CK(cudaMemcpyAsync(ctx->ring + k * bytes, src, bytes, cudaMemcpyHostToDevice,
                           ctx->copy_stream));
     PA_CK(cudaEventRecord(ctx->ring_ev[k], ctx->copy_stream));
     return PA_OK;
@@ -1430,7 +1444,7 @@ pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
     const int k = i % nslots;
     PA_CK(cudaStreamWaitEvent(ctx->stream, ctx->ring_ev[k], 0));
     pa_status st = find_obj_core(ctx, e, 1, &trees[i], flip, cls, n_cls,
-                                 reinterpret_cast<const float *>(ctx->ring + k * bytes),
+                                 reinterpret_cast<const float *>(ctx->ring + k * bytes), nullptr,
                                  PA_MEM_DEVICE, ny, nx, dim, Tig, tig_shared, H, W, scores_out,
                                  (int64_t)i * R, (int64_t)n_img * R, &outs[i], PA_MEM_HOST);
     // image i is complete (the core synchronises the main stream): its slot
@@ -1457,11 +1471,11 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
     return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
   if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
   if (mem == PA_MEM_HOST && n_img > 1)
-    return find_obj_ring(ctx, e, n_img, trees, flip, cls, n_cls, desc, ny, nx, dim, Tig,
+    return find_obj_ring(ctx, e, n_img, trees, flip, cls, n_cls, desc, nullptr, ny, nx, dim, Tig,
                          tig_shared, H, W, scores_out, outs);
-  return find_obj_core(ctx, e, n_img, trees, flip, cls, n_cls, desc, mem, ny, nx, dim, Tig,
-                       tig_shared, H, W, scores_out, 0, (int64_t)n_img * e->num_rotation_steps,
-                       outs, mem);
+  return find_obj_core(ctx, e, n_img, trees, flip, cls, n_cls, desc, nullptr, mem, ny, nx, dim,
+                       Tig, tig_shared, H, W, scores_out, 0,
+                       (int64_t)n_img * e->num_rotation_steps, outs, mem);
 }
 
 }  // namespace
@@ -1766,7 +1780,7 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
   }
   const std::vector<char> ff = fast_flags(cls, n_parts);
   const std::vector<int> ns = stump_counts(cls, n_parts);
-  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, d_in, G,
+  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, d_in, nullptr, false, G,
                                               n_fields, dim, normalize, d_out, ctx->stream));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1826,7 +1840,7 @@ pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, in
                                  ok, s));
   const std::vector<char> ff = fast_flags(cls, n_parts);
   const std::vector<int> ns = stump_counts(cls, n_parts);
-  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, dense, G,
+  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, dense, nullptr, false, G,
                                               n_fields, D, normalize, d_out, s));
   PA_LAUNCH("mask_no_class", launch_mask_no_class(d_out, ok, n_parts, (int64_t)n_fields * G, s));
   if (mem == PA_MEM_HOST)
@@ -2042,7 +2056,7 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
 }
 
 pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, int64_t ldb,
-                       float *C, int64_t ldc, int M, int N, int K) {
+                       float *C, int64_t ldc, int M, int N, int K, int band) {
   if (!ctx) return PA_ERR_INVALID;
   if (!A || !B || !C || M < 1 || N < 1 || K < 1 || lda < K || ldb < K || ldc < N || lda % 8 ||
       ldb % 8 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
@@ -2056,7 +2070,14 @@ pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, i
   int *err = reinterpret_cast<int *>(ctx->arena);
   cudaStream_t s = ctx->stream;
   PA_CK(cudaMemsetAsync(err, 0, sizeof(int), s));
-  PA_LAUNCH("gemm_bf16", launch_tc_gemm_bf16(A, lda, B, ldb, C, ldc, M, N, K, err, s));
+  GemmArgs g{};
+  g.C = C;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.ldc = ldc;
+  g.band = band < 0 ? -1 : band;
+  PA_LAUNCH("gemm_bf16", launch_tc_gemm(A, lda, M, K, B, ldb, N, K, g, 1, err, s));
   int flag = 0;
   PA_CK(cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, s));
   if (pa_status ss = sync_ctx(ctx)) return ss;
@@ -2081,6 +2102,65 @@ pa_status pa_find_obj_batch(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
   if (!ctx) return PA_ERR_INVALID;
   return find_obj_impl(ctx, ep, n_images, trees, flip, cls, n_cls, desc, ny, nx, dim, Tig,
                        tig_shared, H, W, scores_out, out, mem);
+}
+
+pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
+                            const pa_classifier *const *cls, int n_cls, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (n_images < 1 || !imgs || !cls || n_cls < 1)
+    return fail(ctx, PA_ERR_INVALID, "invalid image list");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  for (int i = 0; i < n_images; ++i) {
+    const pa_image &im = imgs[i];
+    if (!im.ep || !exp_ok(im.ep) || !im.tree || !im.desc || !im.Tig || !im.out || im.ny < 1 ||
+        im.nx < 1 || im.dim < 1 || im.H < 1 || im.W < 1 || im.H > 32767 || im.W > 32767)
+      return fail(ctx, PA_ERR_INVALID, "image %d: invalid sizes, parameters or NULL input", i);
+  }
+  // images that share every size, parameter and transform run as one batch
+  auto same = [&](const pa_image &a, const pa_image &b) {
+    if (std::memcmp(a.ep, b.ep, sizeof(pa_exp_param)) != 0) return false;
+    if (a.flip != b.flip || a.ny != b.ny || a.nx != b.nx || a.dim != b.dim || a.H != b.H ||
+        a.W != b.W || !a.tig_shared || !b.tig_shared)
+      return false;
+    return std::memcmp(a.Tig, b.Tig, 9 * sizeof(double)) == 0 && same_topology(a.tree, b.tree);
+  };
+  std::vector<int> group(n_images, -1);
+  int n_groups = 0;
+  for (int i = 0; i < n_images; ++i) {
+    if (group[i] >= 0) continue;
+    group[i] = n_groups;
+    for (int j = i + 1; j < n_images; ++j)
+      if (group[j] < 0 && same(imgs[i], imgs[j])) group[j] = n_groups;
+    ++n_groups;
+  }
+  pa_status result = PA_OK;
+  for (int g = 0; g < n_groups; ++g) {
+    std::vector<int> idx;
+    for (int i = 0; i < n_images; ++i)
+      if (group[i] == g) idx.push_back(i);
+    const pa_image &f = imgs[idx[0]];
+    std::vector<pa_tree> trees;
+    std::vector<pa_ps_outputs> outs;
+    std::vector<const float *> ptrs;
+    for (int i : idx) {
+      trees.push_back(*imgs[i].tree);
+      outs.push_back(*imgs[i].out);
+      ptrs.push_back(imgs[i].desc);
+    }
+    const int n = (int)idx.size();
+    pa_status st;
+    if (mem == PA_MEM_HOST && n > 1)
+      st = find_obj_ring(ctx, f.ep, n, trees.data(), f.flip, cls, n_cls, nullptr, ptrs.data(),
+                         f.ny, f.nx, f.dim, f.Tig, f.tig_shared, f.H, f.W, nullptr, outs.data());
+    else
+      st = find_obj_core(ctx, f.ep, n, trees.data(), f.flip, cls, n_cls, ptrs[0],
+                         mem == PA_MEM_DEVICE ? ptrs.data() : nullptr, mem, f.ny, f.nx, f.dim,
+                         f.Tig, f.tig_shared, f.H, f.W, nullptr, 0,
+                         (int64_t)n * f.ep->num_rotation_steps, outs.data(), mem);
+    if (st && st != PA_ERR_NUMERIC) return st;
+    if (st) result = st;
+  }
+  return result;
 }
 
 }  // extern "C"

@@ -168,8 +168,12 @@ void msg_params(const pa_exp_param *e, double scale, const double *oc, const dou
 
 // Kernel launchers (defined in the .cu files).  All return cudaGetLastError().
 // fast_ok[p] / n_stumps[p] are host arrays describing the classifiers.
+// Score grids read field f at fields[f] (a device array) when given, else at
+// desc + f * n_loc * dim; fields_aligned: every field pointer is 16-byte
+// aligned.
 cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
                                const int *n_stumps, int n_parts, const float *desc,
+                               const float *const *fields, bool fields_aligned,
                                int64_t n_loc_per_field, int n_fields, int dim, int normalize,
                                float *scores, cudaStream_t s);
 cudaError_t launch_window_gather(const float *cells, const uint8_t *valid, int n_fields, int ny,

@@ -15,8 +15,10 @@
 //                  (libAdaBoost/AdaBoost.cc:295-338)
 //   desc_<i>.bin   float32 [R][grid_ny][grid_nx][dim] descriptors of image i
 //
-// Writes best_conf_<i>.txt (one PartHyp::toVect line per part, as the
-// reference's best_conf), log_z_<i>.txt and part_hyps_<i>.txt into --outdir.
+// Writes, into --outdir, the reference's result files pose_est_imgidx<NNNN>.mat
+// (best_conf) and, with --save_marginals, log_part_posterior_final_*.mat, plus
+// best_conf_<i>.txt (one PartHyp::toVect line per part), log_z_<i>.txt and
+// part_hyps_<i>.txt.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -77,7 +79,8 @@ void read_joints(const std::string &path, PartConfig &pc, std::vector<Joint> &js
 
 void usage() {
   std::cout << "usage: partapp_find_obj --find_obj --expdir DIR [--outdir DIR] [--first i]\n"
-               "                        [--numimgs n] [--batch b] [--flip] [--device d]\n";
+               "                        [--numimgs n] [--batch b] [--flip] [--device d]\n"
+               "                        [--save_marginals]\n";
 }
 
 }  // namespace
@@ -85,7 +88,7 @@ void usage() {
 int main(int argc, char **argv) {
   std::string expdir, outdir;
   int first = 0, numimgs = -1, batch = 1, device = 0;
-  bool find_obj = false, flip = false;
+  bool find_obj = false, flip = false, save_marg = false;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
     auto next = [&]() -> std::string {
@@ -100,6 +103,7 @@ int main(int argc, char **argv) {
     else if (a == "--batch") batch = std::atoi(next().c_str());
     else if (a == "--device") device = std::atoi(next().c_str());
     else if (a == "--flip") flip = true;
+    else if (a == "--save_marginals") save_marg = true;
     else if (a == "--help" || a == "-h") { usage(); return 0; }
     else { std::cerr << "unknown option " << a << "\n"; usage(); return 2; }
   }
@@ -165,7 +169,8 @@ int main(int argc, char **argv) {
           joints.push_back(app.m_joints);
         }
       }
-      const auto res = findObjectDataset(ctx, app, flip, joints, desc.data(), nb, ny, nx, dim, Tig, H, W);
+      const auto res =
+          findObjectDataset(ctx, app, flip, joints, desc.data(), nb, ny, nx, dim, Tig, H, W, save_marg);
       for (int b = 0; b < nb; ++b) {
         const std::string tag = std::to_string(i0 + b);
         std::ofstream bc(outdir + "/best_conf_" + tag + ".txt");
@@ -178,6 +183,8 @@ int main(int argc, char **argv) {
         std::ofstream lz(outdir + "/log_z_" + tag + ".txt");
         lz.precision(17);
         for (double z : res[b].log_z) lz << z << "\n";
+        if (!saveResults(outdir, i0 + b, flip, res[b]))
+          throw std::runtime_error("cannot write the .mat results to " + outdir);
         std::ofstream ph(outdir + "/part_hyps_" + tag + ".txt");
         ph.precision(9);
         for (size_t p = 0; p < res[b].part_hyps.size(); ++p)

@@ -2,7 +2,10 @@
 // partapp_gpu.hpp, each a thin adapter onto include/partapp_gb300.h.
 #include "partapp_gpu.hpp"
 
+#include <cstdio>
 #include <cstring>
+
+#include "mat_io.hpp"
 
 namespace partapp_gpu {
 
@@ -234,15 +237,37 @@ void computeScoreGrids(Context &ctx, const std::vector<const AdaBoostClassifier 
 
 FindObjResult findObjectImageRotJoints(Context &ctx, const PartApp &part_app, bool flip,
                                        const float *desc, int ny, int nx, int dim,
-                                       const double Tig[9], int H, int W) {
+                                       const double Tig[9], int H, int W, bool want_marginals) {
   return findObjectDataset(ctx, part_app, flip, {part_app.m_joints}, desc, 1, ny, nx, dim, Tig, H,
-                           W)[0];
+                           W, want_marginals)[0];
+}
+
+bool saveResults(const std::string &dir, int imgidx, bool flip, const FindObjResult &r) {
+  const size_t P = r.best_conf.size();
+  std::vector<float> bc;
+  for (const PartHyp &h : r.best_conf) {
+    const std::vector<float> v = h.toVect();
+    bc.insert(bc.end(), v.begin(), v.end());
+  }
+  char name[64];
+  std::snprintf(name, sizeof name, "/pose_est_imgidx%04d.mat", imgidx);
+  if (!mat_save_float(dir + name, "best_conf", {P, 7}, bc.data())) return false;
+  for (size_t p = 0; p < r.log_marginals.size(); ++p) {
+    const FloatGrid3 &g = r.log_marginals[p];
+    const std::string f = dir + "/log_part_posterior_final_imgidx" + std::to_string(imgidx) +
+                          "_scaleidx0_o" + std::to_string(flip ? 1 : 0) + "_pidx" +
+                          std::to_string(p) + ".mat";
+    if (!mat_save_float(f, "log_prob_grid", {g.shape()[0], g.shape()[1], g.shape()[2]}, g.data()))
+      return false;
+  }
+  return true;
 }
 
 std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_app, bool flip,
                                              const std::vector<std::vector<Joint>> &joints,
                                              const float *desc, int n_images, int ny, int nx,
-                                             int dim, const double Tig[9], int H, int W) {
+                                             int dim, const double Tig[9], int H, int W,
+                                             bool want_marginals) {
   require(n_images >= 1 && (int)joints.size() == n_images, "one joint set per image");
   const int P = part_app.m_part_conf.part_size();
   const pa_exp_param e = part_app.m_exp_param.c();
@@ -257,9 +282,16 @@ std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_a
   std::vector<ImageOut> outs;
   outs.reserve(n_images);
   std::vector<pa_ps_outputs> o;
+  const int R = e.num_rotation_steps;
+  const size_t N = (size_t)R * H * W;
+  std::vector<std::vector<float>> marg(want_marginals ? n_images : 0);
   for (int i = 0; i < n_images; ++i) {
     outs.emplace_back(P, K);
     o.push_back(outs.back().o);
+    if (want_marginals) {
+      marg[i].resize((size_t)P * N);
+      o.back().log_marg = marg[i].data();
+    }
   }
   std::vector<const pa_classifier *> cls;
   for (const AdaBoostClassifier *a : part_app.m_abc) cls.push_back(a->get());
@@ -267,7 +299,15 @@ std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_a
                               (int)cls.size(), desc, ny, nx, dim, Tig, 1, H, W, nullptr, o.data(),
                               PA_MEM_HOST));
   std::vector<FindObjResult> res;
-  for (int i = 0; i < n_images; ++i) res.push_back(outs[i].result(P, K));
+  for (int i = 0; i < n_images; ++i) {
+    res.push_back(outs[i].result(P, K));
+    if (want_marginals)
+      for (int p = 0; p < P; ++p) {
+        FloatGrid3 g(R, H, W);
+        std::memcpy(g.data(), marg[i].data() + (size_t)p * N, N * sizeof(float));
+        res.back().log_marginals.push_back(std::move(g));
+      }
+  }
   return res;
 }
 

@@ -164,6 +164,7 @@ struct FindObjResult {
   std::vector<std::vector<PartHyp>> part_hyps;    // local maxima per part
   std::vector<std::vector<float>> root_hyps;      // (scale, x, y, score)
   std::vector<double> log_z;                      // FP64 log-partition per part
+  std::vector<FloatGrid3> log_marginals;          // [part] final log marginals, if asked for
 };
 
 // findObjectImageRotJoints (objectdetect_findrot.cpp:729-1058) with freshly
@@ -171,14 +172,22 @@ struct FindObjResult {
 // image transform Tig (3x3, row-major), PS, marginals, local maxima.
 FindObjResult findObjectImageRotJoints(Context &ctx, const PartApp &part_app, bool flip,
                                        const float *desc, int ny, int nx, int dim,
-                                       const double Tig[9], int H, int W);
+                                       const double Tig[9], int H, int W,
+                                       bool want_marginals = false);
 
 // findObjectDataset (objectdetect_aux.cpp:322-406) over a batch of images
 // with the same sizes; joints[i] are image i's joints (per-image pairwise).
 std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_app, bool flip,
                                              const std::vector<std::vector<Joint>> &joints,
                                              const float *desc, int n_images, int ny, int nx,
-                                             int dim, const double Tig[9], int H, int W);
+                                             int dim, const double Tig[9], int H, int W,
+                                             bool want_marginals = false);
+
+// The reference's result files (objectdetect_findrot.cpp:238-251, 1005-1011):
+// pose_est_imgidx<NNNN>.mat with best_conf [P][7], and per part
+// log_part_posterior_final_imgidx<i>_scaleidx0_o<flip>_pidx<p>.mat with
+// log_prob_grid [R][H][W] when the marginals were asked for.
+bool saveResults(const std::string &dir, int imgidx, bool flip, const FindObjResult &r);
 
 }  // namespace partapp_gpu
 

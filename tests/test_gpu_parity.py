@@ -484,3 +484,36 @@ def test_errors_are_statuses(ctx, pa):
     with pytest.raises(pa.PaError) as ei:
         ctx.compute_root_posterior_rot(_pa_exp(1), tree, u[:, :1])
     assert ei.value.status == pa.PA_ERR_INVALID
+
+
+# ------------------------------------------------------- uneven batches
+@pytest.mark.parametrize("device", [False, True])
+def test_find_obj_multi_uneven_sizes(ctx, orc, device):
+    """Images of different sizes and rotation counts in one call: grouped
+    images run as a batch and must equal one-image calls bit for bit; every
+    image matches the oracle."""
+    import torch
+
+    shapes = [(12, 48, 64), (12, 48, 64), (12, 40, 56), (16, 48, 64), (8, 32, 48), (12, 48, 64)]
+    imgs = [synth.make_image(700 + i, R=R, H=H, W=W, n_stumps=60, D=96, offset_range=(3, 8),
+                             sigma_range=(1, 2.5)) for i, (R, H, W) in enumerate(shapes)]
+    models = imgs[0]["models"]
+    cls = ctx.classifiers(models)
+    todev = (lambda a: torch.from_numpy(a).cuda()) if device else (lambda a: a)
+    batch = [dict(exp=_pa_exp(im["R"]), tree=im["tree"], desc=todev(im["desc"]), Tig=im["Tig"],
+                  H=im["H"], W=im["W"]) for im in imgs]
+    got = ctx.find_obj_multi(batch, cls, want_marg=True)
+    for i, im in enumerate(imgs):
+        one = ctx.find_obj(_pa_exp(im["R"]), im["tree"], cls, todev(im["desc"]), im["Tig"],
+                           im["H"], im["W"])
+        assert np.array_equal(got[i]["best_conf"], one["best_conf"]), i
+        assert np.array_equal(np.asarray(got[i]["log_z"]), np.asarray(one["log_z"])), i
+        gm = got[i]["log_marg"]
+        om = one["log_marg"]
+        if device:
+            gm, om = gm.cpu().numpy(), om.cpu().numpy()
+        assert np.array_equal(gm, om), i
+        e = orc.make_exp(R=im["R"])
+        want = orc.find_obj(e, im["tree"], models, im["desc"], im["Tig"], im["H"], im["W"])
+        compare_ps(dict(got[i], log_marg=gm), want,
+                   oracle64(orc, e, im["tree"], want["log_unary"]))

@@ -111,3 +111,28 @@ def test_cli_find_obj_matches_c_abi(tmp_path, ctx, orc, batch):
         want = orc.find_obj(oe, im["tree"], imgs[0]["models"], im["desc"], im["Tig"], H, W)
         for p in range(got.shape[0]):
             assert tuple(got[p, [2, 4, 5]]) == tuple(want["best_conf"][p, [2, 4, 5]]), (i, p)
+
+
+@pytest.mark.gpu
+def test_cli_writes_reference_mat_files(tmp_path, ctx):
+    """pose_est_imgidx<NNNN>.mat (best_conf) and log_part_posterior_final_*.mat
+    (log_prob_grid, [R][H][W] as MATLAB sees it), read back with scipy."""
+    sio = pytest.importorskip("scipy.io")
+    import partapp_gb300 as pa
+
+    imgs = make_experiment(str(tmp_path), n_images=2)
+    r = subprocess.run([cli(), "--find_obj", "--expdir", str(tmp_path), "--batch", "2",
+                        "--save_marginals"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    cls = ctx.classifiers(imgs[0]["models"])
+    e = pa.exp_param(R=R, local_max=50, interpolate=True)
+    ref = ctx.find_obj_batch(e, [im["tree"] for im in imgs], cls,
+                             np.stack([im["desc"] for im in imgs]), imgs[0]["Tig"], H, W,
+                             want_marg=True)
+    for i in range(2):
+        bc = sio.loadmat(str(tmp_path / f"pose_est_imgidx{i:04d}.mat"))["best_conf"]
+        assert bc.shape == (10, 7) and bc.dtype == np.float32
+        assert np.array_equal(bc, ref[i]["best_conf"])
+        for p in (0, 4, 9):
+            g = sio.loadmat(str(tmp_path / f"log_part_posterior_final_imgidx{i}_scaleidx0_o0_pidx{p}.mat"))
+            assert np.array_equal(g["log_prob_grid"], ref[i]["log_marg"][p])

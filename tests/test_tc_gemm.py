@@ -49,3 +49,24 @@ def test_gemm_bf16_strided_operands(ctx):
     C = ctx.gemm_bf16(A, B)
     ref = A.float() @ B.float().T
     assert (C - ref).abs().max().item() <= 1e-4 * ref.abs().max().item()
+
+
+@pytest.mark.parametrize("M,N,K,band", [(1024, 3072, 1024, 72), (384, 520, 296, 20),
+                                        (128, 256, 128, 0)])
+def test_banded_gemm_matches_dense_product(ctx, M, N, K, band):
+    """A banded A (zero outside |k - m| <= band), the persistent band kernel:
+    equals the dense product."""
+    import torch
+
+    import partapp_gb300 as pa
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(M + N + K + band)
+    A = torch.randn((M, K), generator=g, device="cuda")
+    i = torch.arange(M, device="cuda")[:, None]
+    k = torch.arange(K, device="cuda")[None, :]
+    A = torch.where((k - i).abs() <= band, A, torch.zeros_like(A)).to(torch.bfloat16)
+    B = torch.randn((N, K), generator=g, device="cuda").to(torch.bfloat16)
+    C = ctx.gemm_bf16_banded(A, B, band)
+    ref = A.float() @ B.float().T
+    assert (C - ref).abs().max().item() <= 1e-5 * max(1.0, ref.abs().max().item()) * 4
