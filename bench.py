@@ -49,9 +49,11 @@ def parse():
                     help="images per end-to-end call (host descriptors through the copy ring)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=1024, help="large-grid: H = W")
-    ap.add_argument("--workload", choices=["find_obj", "large-grid"], default="find_obj",
+    ap.add_argument("--workload", choices=["find_obj", "large-grid", "uneven"], default="find_obj",
                     help="large-grid: the 1024x1024, 48-rotation PS (log-normal unaries, "
-                         "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic")
+                         "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic; "
+                         "uneven: images of random sizes (200-640 px) and rotation counts "
+                         "(12/24/48) through pa_find_obj_multi, throughput and latency spread")
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1234)
@@ -437,10 +439,80 @@ def run_large_grid(args):
     ctx.close()
 
 
+def run_uneven(args):
+    """find_obj over images of uneven sizes and rotation counts: heights and
+    widths ~ U{200..640} rounded to multiples of 4, R in {12, 24, 48}, 10
+    classifiers of 500 stumps over 960-d descriptors at stride 4, per-image
+    pairwise terms.  Throughput of one pa_find_obj_multi call over all images
+    (descriptors resident in HBM) and the latency spread of one-image calls."""
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build, synth
+
+    build.build()
+    dev = torch.device("cuda:0")
+    ctx = pa.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    n = max(4, 8 * args.batch)
+    rng = np.random.default_rng(args.seed)
+    models = synth.make_models(rng, n_parts=P, n_stumps=N_STUMPS, D=D)
+    cls = ctx.classifiers(models)
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed)
+    images = []
+    for i in range(n):
+        Hi = int(rng.integers(200, 641)) // 4 * 4
+        Wi = int(rng.integers(200, 641)) // 4 * 4
+        Ri = int(rng.choice([12, 24, 48]))
+        z = torch.randn((Ri, Hi // STRIDE, Wi // STRIDE, D), generator=g, device=dev)
+        z.mul_(z).mul_(0.5)
+        z.div_(torch.linalg.vector_norm(z, dim=-1, keepdim=True))
+        tree = synth.make_tree(rng, R=Ri, offset_range=(10.0, 60.0), sigma_range=(2.0, 12.0))
+        images.append(dict(exp=pa.exp_param(R=Ri, interpolate=True), tree=tree, desc=z,
+                           Tig=synth.grid_to_image(STRIDE), H=Hi, W=Wi))
+    for _ in range(max(1, min(args.warmup, 2))):
+        ctx.find_obj_multi(images, cls)
+    torch.cuda.synchronize(dev)
+    steps = max(1, args.steps // 10)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        ctx.find_obj_multi(images, cls)
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = t0.elapsed_time(t1) / steps
+    lat = []
+    for im in images:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.find_obj(im["exp"], im["tree"], cls, im["desc"], im["Tig"], im["H"], im["W"])
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        lat.append(a.elapsed_time(b))
+    lat = np.array(lat)
+    pix = [im["H"] * im["W"] * im["exp"].num_rotation_steps for im in images]
+    line = {"metric": "images/s (uneven sizes and rotation counts)", "unit": "images/s",
+            "value": n / (ms / 1e3), "ms_per_call": ms, "images_per_call": n, "n_gpus": 1,
+            "steps": steps, "higher_is_better": True, "data": "synthetic", "dtype": "f32",
+            "config": {"workload": "find_obj, H, W ~ U{200..640}/4*4, R in {12,24,48}, "
+                                   "10 classifiers x 500 stumps, 960-d, 10-part PS"},
+            "latency_ms_one_image": {"p50": float(np.percentile(lat, 50)),
+                                     "p90": float(np.percentile(lat, 90)),
+                                     "max": float(lat.max()), "min": float(lat.min())},
+            "cells_per_image": {"min": int(min(pix)), "max": int(max(pix))}}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.workload == "large-grid":
         run_large_grid(args)
+        return
+    if args.workload == "uneven":
+        run_uneven(args)
         return
     if args.impl == "reference":
         run_reference(args)
