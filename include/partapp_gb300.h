@@ -217,19 +217,23 @@ typedef struct {
  * part at most one (the reference asserts this at :210); PA_ERR_UNSUPPORTED
  * otherwise.  Covariances must be symmetric positive definite: diagonal ones
  * take gaussFilterDiag2d, others gaussFilter2dOffset (rotation into the
- * eigenbasis, libMultiArray/multi_array_filter.hpp:335-369).
+ * eigenbasis, libMultiArray/multi_array_filter.hpp:335-369).  is_sparse is
+ * computeRootPosteriorRot's bIsSparse: the upward messages rotate a full
+ * covariance's map into its eigenbasis by TM_DIRECT when set (bilinear
+ * otherwise); the downward messages are always dense (:174-179, 224-229).
+ * pa_find_obj* pass is_sparse = 1, as findObjectImageRotJoints does (:740).
  *   log_unary [P][R][H][W] */
 pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
-                      const float *log_unary, int H, int W, const pa_ps_outputs *out,
-                      int mem);
+                      int is_sparse, const float *log_unary, int H, int W,
+                      const pa_ps_outputs *out, int mem);
 
 /* computeRotJointMarginal (objectdetect_findrot.cpp:292-456): one message
- * child -> parent frame, dense path (bIsSparse = false).  child, parent
- * [R][H][W]; C as in pa_ps_infer. */
+ * child -> parent frame; is_sparse = bIsSparse (TM_DIRECT forward rotation
+ * of a full covariance).  child, parent [R][H][W]; C as in pa_ps_infer. */
 pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float *child,
                                 float *parent, int R, int H, int W, const double *offset_c,
                                 const double *offset_p, const double *C, double rot_mean,
-                                double rot_sigma, double scale, int mem);
+                                double rot_sigma, double scale, int is_sparse, int mem);
 
 /* No counterpart in the reference.  pa_rot_joint_marginal for callers that
  * cannot allocate device memory on their call path (a host application that

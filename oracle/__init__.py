@@ -37,6 +37,7 @@ class OrcExp(C.Structure):
         ("strip_border_detections", C.c_float),
         ("max_local_max", C.c_int),
         ("use_pairwise", C.c_int),
+        ("sparse_up", C.c_int),
     ]
 
 
@@ -143,9 +144,12 @@ def _declare(L):
 # ---------------------------------------------------------------------------
 
 def make_exp(R=24, min_rot=-180.0, max_rot=180.0, scale=1.0, strip=0.0, max_local_max=1000,
-             use_pairwise=True) -> OrcExp:
+             use_pairwise=True, sparse=False) -> OrcExp:
+    """sparse: bIsSparse of the upward messages (and of rot_joint_marginal);
+    the --find_obj path (find_obj) always uses True, as
+    findObjectImageRotJoints does."""
     return OrcExp(int(R), float(min_rot), float(max_rot), float(scale), float(scale), float(strip),
-                  int(max_local_max), int(bool(use_pairwise)))
+                  int(max_local_max), int(bool(use_pairwise)), int(bool(sparse)))
 
 
 class _TreeHolder:

@@ -253,10 +253,30 @@ void gauss_diag(const T *in, T *out, int H, int W, double sigma_x, double sigma_
     }
 }
 
-/* gaussFilter2dOffset with a zero offset, multi_array_filter.hpp:335-369
- * (the dense path: bilinear forward rotation). */
+/* The TM_DIRECT branch of transform_grid_helper (multi_array_transform.hpp:
+ * 173-193) with the input -> output map T31: every input cell that is not the
+ * default lands on its nearest output cell, later cells (x outer, y inner)
+ * overwriting earlier ones; unreached cells keep the default. */
 template <class T>
-void gauss_full(const T *in, T *out, int H, int W, const double *Cs) {
+void direct_map(const T *gin, int in_h, int in_w, T *gout, int out_h, int out_w,
+                const double *T31, T def) {
+  std::fill(gout, gout + (size_t)out_h * out_w, def);
+  for (int x1 = 0; x1 < in_w; ++x1)
+    for (int y1 = 0; y1 < in_h; ++y1) {
+      const T v = gin[(size_t)y1 * in_w + x1];
+      if (v != def) {
+        double x3 = T31[0] * x1 + T31[1] * y1 + T31[2];
+        double y3 = T31[3] * x1 + T31[4] * y1 + T31[5];
+        int ix3 = (int)std::floor(x3 + 0.5), iy3 = (int)std::floor(y3 + 0.5);
+        if (ix3 >= 0 && ix3 < out_w && iy3 >= 0 && iy3 < out_h) gout[(size_t)iy3 * out_w + ix3] = v;
+      }
+    }
+}
+
+/* gaussFilter2dOffset with a zero offset, multi_array_filter.hpp:335-369:
+ * bilinear forward rotation, or TM_DIRECT when bIsSparse. */
+template <class T>
+void gauss_full(const T *in, T *out, int H, int W, const double *Cs, bool sparse) {
   double V[4], E[2];
   eig2d(Cs, V, E);
   const double T21[9] = {V[0], V[2], 0, V[1], V[3], 0, 0, 0, 1};  /* [trans(V) | 0] */
@@ -268,7 +288,14 @@ void gauss_full(const T *in, T *out, int H, int W, const double *Cs) {
   hc_inverse3(T21, T12);
   prod3(T12, T23, T13);
   std::vector<T> g((size_t)oh * ow), gs((size_t)oh * ow);
-  bilinear_map(in, H, W, g.data(), oh, ow, T13, (T)0);
+  if (sparse) {
+    const double T32[9] = {1, 0, -minx, 0, 1, -miny, 0, 0, 1};
+    double T31[9];
+    prod3(T32, T21, T31);
+    direct_map(in, H, W, g.data(), oh, ow, T31, (T)0);
+  } else {
+    bilinear_map(in, H, W, g.data(), oh, ow, T13, (T)0);
+  }
   gauss_diag(g.data(), gs.data(), oh, ow, std::sqrt(E[0]), std::sqrt(E[1]));
   const double mz = -0.0;
   const double T42[9] = {V[0], V[1], mz, V[2], V[3], mz, 0, 0, 1};
@@ -285,7 +312,7 @@ template <class T>
 int rot_joint_marginal(const orc_exp *e, const T *child, T *parent, int R, int H,
                        int W, const double *oc, const double *op,
                        const double *C, double rot_mean, double rot_sigma,
-                       double scale) {
+                       double scale, bool sparse) {
   const size_t HW = (size_t)H * W, N = HW * R;
   if (R < 2 || H < 1 || W < 1) return -1;
   const bool diag = (C[1] == 0 && C[2] == 0);
@@ -359,7 +386,7 @@ int rot_joint_marginal(const orc_exp *e, const T *child, T *parent, int R, int H
     if (diag)
       gauss_diag(in, out, H, W, std::sqrt(Cs[0]), std::sqrt(Cs[3]));
     else
-      gauss_full(in, out, H, W, Cs);
+      gauss_full(in, out, H, W, Cs, sparse);
   }
 
   /* computeLogGrid + addGrid1(in_M), :432-435 */
@@ -516,7 +543,7 @@ int ps_infer(const orc_exp *e, const orc_tree *t, const T *log_unary, int H, int
         int c = ch[i], j = js[i];
         int rc = rot_joint_marginal<T>(e, post[c].data(), msg.data(), R, H, W, t->offset_c + 2 * j,
                                        t->offset_p + 2 * j, t->C + 4 * j, t->rot_mean[j],
-                                       t->rot_sigma[j], scale);
+                                       t->rot_sigma[j], scale, e->sparse_up != 0);
         if (rc) return rc;
         add_grid(post[cur], msg);
         if (cur == root)
@@ -536,7 +563,7 @@ int ps_infer(const orc_exp *e, const orc_tree *t, const T *log_unary, int H, int
       add_grid(from_root[c], unary[root]);
       int rc = rot_joint_marginal<T>(e, from_root[c].data(), msg.data(), R, H, W, t->offset_p + 2 * j,
                                      t->offset_c + 2 * j, t->C + 4 * j, -t->rot_mean[j],
-                                     t->rot_sigma[j], scale);
+                                     t->rot_sigma[j], scale, false);
       if (rc) return rc;
       from_root[c] = msg;
       stack2.push_back(c);
@@ -553,7 +580,7 @@ int ps_infer(const orc_exp *e, const orc_tree *t, const T *log_unary, int H, int
         add_grid(tmp, from_root[cur]);
         int rc = rot_joint_marginal<T>(e, tmp.data(), from_root[c].data(), R, H, W,
                                        t->offset_p + 2 * j, t->offset_c + 2 * j, t->C + 4 * j,
-                                       -t->rot_mean[j], t->rot_sigma[j], scale);
+                                       -t->rot_mean[j], t->rot_sigma[j], scale, false);
         if (rc) return rc;
         stack2.push_back(c);
       }
@@ -767,12 +794,14 @@ int orc_gaussian_filter(double sigma, double *out) {
 int orc_rot_joint_marginal_f32(const orc_exp *e, const float *child, float *parent, int R, int H,
                                int W, const double *oc, const double *op, const double *C,
                                double rot_mean, double rot_sigma, double scale) {
-  return rot_joint_marginal<float>(e, child, parent, R, H, W, oc, op, C, rot_mean, rot_sigma, scale);
+  return rot_joint_marginal<float>(e, child, parent, R, H, W, oc, op, C, rot_mean, rot_sigma, scale,
+                                   e->sparse_up != 0);
 }
 int orc_rot_joint_marginal_f64(const orc_exp *e, const double *child, double *parent, int R, int H,
                                int W, const double *oc, const double *op, const double *C,
                                double rot_mean, double rot_sigma, double scale) {
-  return rot_joint_marginal<double>(e, child, parent, R, H, W, oc, op, C, rot_mean, rot_sigma, scale);
+  return rot_joint_marginal<double>(e, child, parent, R, H, W, oc, op, C, rot_mean, rot_sigma, scale,
+                                    e->sparse_up != 0);
 }
 
 int orc_ps_infer_f32(const orc_exp *e, const orc_tree *t, const float *log_unary, int H, int W,
@@ -818,7 +847,9 @@ int orc_find_obj_f32(const orc_exp *e, const orc_tree *t, const orc_models *m, c
       orc_clip_log(u, (int64_t)HW);
     }
   if (log_unary) std::copy(unary.begin(), unary.end(), log_unary);
-  return ps_infer<float>(e, t, unary.data(), H, W, log_marg, best_conf, root_post, part_hyps,
+  orc_exp ef = *e;
+  ef.sparse_up = 1; /* findObjectImageRotJoints: bIsSparse = true (objectdetect_findrot.cpp:740) */
+  return ps_infer<float>(&ef, t, unary.data(), H, W, log_marg, best_conf, root_post, part_hyps,
                          n_part_hyps, root_hyps, n_root_hyps);
 }
 

@@ -40,6 +40,9 @@ typedef struct {
   float strip_border_detections; /* fraction of image width, default 0 */
   int max_local_max;             /* roi_save_num_samples, default 1000 */
   int use_pairwise;              /* default 1 */
+  int sparse_up;                 /* bIsSparse of the upward messages (computeRootPosteriorRot;
+                                    findObjectImageRotJoints passes true, :740) and of
+                                    orc_rot_joint_marginal_*; matters for full covariances */
 } orc_exp;
 
 /* Tree + joints (libPictStruct/objectdetect.h:54-86, already converted to

@@ -132,9 +132,9 @@ def load_library():
     L.pa_score_grids_window.argtypes = [vp, P(vp), ip, vp, vp, ip, ip, ip, ip, ip, ip, dp, ip,
                                         vp, ip]
     L.pa_unary_maps.argtypes = [vp, vp, ip, ip, ip, ip, P(dp), ip, ip, ip, ip, vp, ip]
-    L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, vp, ip, ip, P(PsOutputs), ip]
+    L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, ip, vp, ip, ip, P(PsOutputs), ip]
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
-                                        dp, dp, dp, ip]
+                                        dp, dp, dp, ip, ip]
     L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip, ip]
     L.pa_ctx_set_message_math.argtypes = [vp, ip]
     L.pa_find_obj_multi.argtypes = [vp, ip, P(Image), P(vp), ip, ip]
@@ -342,7 +342,9 @@ class Context:
 
     # ---------------------------------------------------------- messages
     def rot_joint_marginal(self, exp: ExpParam, child, offset_c, offset_p, Cmat, rot_mean,
-                           rot_sigma, scale=1.0):
+                           rot_sigma, scale=1.0, is_sparse=False):
+        """computeRotJointMarginal; is_sparse = bIsSparse (TM_DIRECT forward
+        rotation of a full covariance)."""
         c = _Buf(child, np.float32)
         R, H, W = c.arr.shape
         out = _empty_like_space((R, H, W), c.mem, c.arr)
@@ -352,7 +354,8 @@ class Context:
         pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
         self._check(self.L.pa_rot_joint_marginal(self.h, C.byref(exp), c.ptr, o.ptr, R, H, W,
                                                  pd(oc), pd(op), pd(Cm), float(rot_mean),
-                                                 float(rot_sigma), float(scale), c.mem))
+                                                 float(rot_sigma), float(scale),
+                                                 int(is_sparse), c.mem))
         return out
 
     def _outputs(self, P, R, H, W, K, mem, like, want_marg=True, want_root=True):
@@ -439,14 +442,15 @@ class Context:
         return C_
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,
-                                   want_marg=True):
-        """log_unary [P][R][H][W] (after clip_scores_fill + computeLogGrid)."""
+                                   want_marg=True, is_sparse=False):
+        """log_unary [P][R][H][W] (after clip_scores_fill + computeLogGrid);
+        is_sparse = bIsSparse of the upward messages."""
         u = _Buf(log_unary, np.float32)
         P, R, H, W = u.arr.shape
         th = _TreeHolder(tree)
         res, o = self._outputs(P, R, H, W, exp.roi_save_num_samples, u.mem, u.arr, want_marg)
-        self._check(self.L.pa_ps_infer(self.h, C.byref(exp), C.byref(th.s), int(flip), u.ptr, H,
-                                       W, C.byref(o), u.mem))
+        self._check(self.L.pa_ps_infer(self.h, C.byref(exp), C.byref(th.s), int(flip),
+                                       int(is_sparse), u.ptr, H, W, C.byref(o), u.mem))
         return self._finish(res, P)
 
     def find_obj(self, exp: ExpParam, tree, cls_list, desc, Tig, H, W, flip=False,

@@ -607,12 +607,12 @@ __device__ __forceinline__ float bilinear_at(const float *g, int in_h, int in_w,
   return __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
 }
 
-// e2 [R][H][W] -> g0 [R][oh][ow]
+// e2 [R][H][W] -> g0 [R][oh][ow] (bilinear; sparse messages take k_full_d*)
 __global__ void __launch_bounds__(256) k_full_fwd(const MsgDesc *__restrict__ msgs, int R, int H,
                                                   int W) {
   const int msg = blockIdx.z / R, r = blockIdx.z - (blockIdx.z / R) * R;
   const MsgDesc *md = msgs + msg;
-  if (!md->full) return;
+  if (!md->full || md->sparse) return;
   const int oh = md->oh, ow = md->ow;
   const int x3 = blockIdx.x * 32 + threadIdx.x, y3 = blockIdx.y * 8 + threadIdx.y;
   if (x3 >= ow || y3 >= oh) return;
@@ -620,6 +620,52 @@ __global__ void __launch_bounds__(256) k_full_fwd(const MsgDesc *__restrict__ ms
   map_pt(md->tf, x3, y3, x1, y1);
   md->g0[((int64_t)r * oh + y3) * ow + x3] =
       bilinear_at(md->e2 + (int64_t)r * H * W, H, W, x1, y1);
+}
+
+// TM_DIRECT forward rotation (bIsSparse): every e2 cell that is not 0 lands
+// on its nearest g0 cell, the last one in the reference's loop order (x
+// outer, y inner) winning; cells no input reaches stay 0.  g1 (free until the
+// x pass) holds, per g0 cell, 1 + the enumeration index of its winner.
+__global__ void __launch_bounds__(256) k_full_dclear(const MsgDesc *__restrict__ msgs, int R) {
+  const int msg = blockIdx.z / R, r = blockIdx.z - (blockIdx.z / R) * R;
+  const MsgDesc *md = msgs + msg;
+  if (!md->full || !md->sparse) return;
+  const int x3 = blockIdx.x * 32 + threadIdx.x, y3 = blockIdx.y * 8 + threadIdx.y;
+  if (x3 >= md->ow || y3 >= md->oh) return;
+  reinterpret_cast<int *>(md->g1)[((int64_t)r * md->oh + y3) * md->ow + x3] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_full_dscatter(const MsgDesc *__restrict__ msgs, int R,
+                                                       int H, int W) {
+  const int msg = blockIdx.z / R, r = blockIdx.z - (blockIdx.z / R) * R;
+  const MsgDesc *md = msgs + msg;
+  if (!md->full || !md->sparse) return;
+  const int x1 = blockIdx.x * 32 + threadIdx.x, y1 = blockIdx.y * 8 + threadIdx.y;
+  if (x1 >= W || y1 >= H) return;
+  if (md->e2[((int64_t)r * H + y1) * W + x1] == 0.f) return;  // the default is not mapped
+  double x3, y3;
+  map_pt(md->td, x1, y1, x3, y3);
+  const double fx = floor(__dadd_rn(x3, 0.5)), fy = floor(__dadd_rn(y3, 0.5));
+  if (!(fx >= 0.0 && fx < (double)md->ow && fy >= 0.0 && fy < (double)md->oh)) return;
+  const int e = x1 * H + y1 + 1;  // enumeration order of the reference's loops, 1-based
+  atomicMax(reinterpret_cast<int *>(md->g1) + ((int64_t)r * md->oh + (int)fy) * md->ow + (int)fx, e);
+}
+
+__global__ void __launch_bounds__(256) k_full_dgather(const MsgDesc *__restrict__ msgs, int R,
+                                                      int H, int W) {
+  const int msg = blockIdx.z / R, r = blockIdx.z - (blockIdx.z / R) * R;
+  const MsgDesc *md = msgs + msg;
+  if (!md->full || !md->sparse) return;
+  const int x3 = blockIdx.x * 32 + threadIdx.x, y3 = blockIdx.y * 8 + threadIdx.y;
+  if (x3 >= md->ow || y3 >= md->oh) return;
+  const int64_t o = ((int64_t)r * md->oh + y3) * md->ow + x3;
+  const int e = reinterpret_cast<const int *>(md->g1)[o];
+  float v = 0.f;
+  if (e > 0) {
+    const int x1 = (e - 1) / H, y1 = (e - 1) - x1 * H;
+    v = md->e2[((int64_t)r * H + y1) * W + x1];
+  }
+  md->g0[o] = v;
 }
 
 // x pass along the rotated rows: g0 -> g1 (truncated at the border)
@@ -881,9 +927,13 @@ cudaError_t launch_msg_full(const MsgDesc *msgs, int n_msgs, int R, int H, int W
     return cudaErrorInvalidValue;
   const size_t gx_smem = ((size_t)align4(2 * kxmax + 1) + owmax + 2 * kxmax) * sizeof(float);
   if (gx_smem > 227 * 1024) return cudaErrorInvalidValue;
-  k_full_fwd<<<dim3((unsigned)((owmax + 31) / 32), (unsigned)((ohmax + 7) / 8),
-                    (unsigned)(R * n_msgs)),
-               dim3(32, 8), 0, s>>>(msgs, R, H, W);
+  if ((int64_t)W * H >= ((int64_t)1 << 31) - 1) return cudaErrorInvalidValue;  // 1-based index
+  const dim3 gout((unsigned)((owmax + 31) / 32), (unsigned)((ohmax + 7) / 8), (unsigned)(R * n_msgs));
+  k_full_fwd<<<gout, dim3(32, 8), 0, s>>>(msgs, R, H, W);
+  k_full_dclear<<<gout, dim3(32, 8), 0, s>>>(msgs, R);
+  k_full_dscatter<<<dim3((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8), (unsigned)(R * n_msgs)),
+                    dim3(32, 8), 0, s>>>(msgs, R, H, W);
+  k_full_dgather<<<gout, dim3(32, 8), 0, s>>>(msgs, R, H, W);
   cudaFuncSetAttribute(k_full_gx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gx_smem);
   k_full_gx<<<dim3((unsigned)ohmax, (unsigned)R, (unsigned)n_msgs), 256, gx_smem, s>>>(msgs, R);
   k_full_gy<<<dim3((unsigned)((owmax + 31) / 32), (unsigned)((ohmax + kFullRows - 1) / kFullRows),

@@ -472,7 +472,7 @@ void prod3(const double *A, const double *B, double *Cm) {
 // the eigenbasis of C (transform_grid_resize, adaptive size from
 // hc::get_transformed_bbox, homogeneous_coord.cpp:140-156), filter along the
 // eigen axes, rotate back (transform_grid_fixed_size).
-void full_cov_params(const double *Cs, int H, int W, MsgParams &m, double *E) {
+void full_cov_params(const double *Cs, int H, int W, bool sparse, MsgParams &m, double *E) {
   double V[4];
   eig2d(Cs, V, E);
   const double T21[9] = {V[0], V[2], 0, V[1], V[3], 0, 0, 0, 1};  // [trans(V) | 0]
@@ -498,15 +498,22 @@ void full_cov_params(const double *Cs, int H, int W, MsgParams &m, double *E) {
   hc_inverse(T43, Tb);
   const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   prod3(Tb, I3, Tbb);
+  // TM_DIRECT (bIsSparse): input cell -> output cell, T31 = T32 * T21
+  const double T32[9] = {1, 0, -minx, 0, 1, -miny, 0, 0, 1};
+  double T31[9];
+  prod3(T32, T21, T31);
   for (int k = 0; k < 6; ++k) {
     m.tf[k] = T13[k];
     m.tb[k] = Tbb[k];
+    m.td[k] = T31[k];
   }
   m.full = true;
+  m.sparse = sparse;
 }
 
 void msg_params(const pa_exp_param *e, double scale, const double *oc, const double *op,
-                const double *C, double rot_mean, double rot_sigma, int H, int W, MsgParams &m) {
+                const double *C, double rot_mean, double rot_sigma, int H, int W, bool sparse,
+                MsgParams &m) {
   const int R = e->num_rotation_steps;
   const double step = rot_step_rad(e);
   const double rot_sigma_idx = rot_sigma / step;
@@ -531,9 +538,10 @@ void msg_params(const pa_exp_param *e, double scale, const double *oc, const dou
   const double Cs[4] = {sc2 * C[0], sc2 * C[1], sc2 * C[2], sc2 * C[3]};  // square(scale)*C
   double sx2 = Cs[0], sy2 = Cs[3];
   m.full = false;
+  m.sparse = false;
   if (Cs[1] != 0 || Cs[2] != 0) {  // gaussFilter2d -> gaussFilter2dOffset
     double E[2];
-    full_cov_params(Cs, H, W, m, E);
+    full_cov_params(Cs, H, W, sparse, m, E);
     sx2 = E[0];
     sy2 = E[1];
   }
@@ -597,6 +605,7 @@ struct PsPlan {
     std::vector<TcJob> tc;  // tensor-core messages
   };
   bool tc_mode = false;  // diagonal-covariance messages on the tensor cores (H % 8 == 0)
+  bool sparse_up = false;  // bIsSparse of the upward messages
   int wp = 0, hp = 0;
   std::vector<Phase> up, down;
   RootDesc *roots = nullptr;
@@ -700,10 +709,12 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   auto params_of = [&](const M &mm) {
     const Joint &J = joints[mm.img][mm.joint];
     MsgParams mp;
+    // upward messages take the caller's bIsSparse (objectdetect_findrot.cpp:630-635),
+    // downward ones are dense (:174-179, 224-229)
     if (mm.up)
-      msg_params(e, scale, J.oc, J.op, J.C, J.rot_mean, J.rot_sigma, H, W, mp);
+      msg_params(e, scale, J.oc, J.op, J.C, J.rot_mean, J.rot_sigma, H, W, pl.sparse_up, mp);
     else
-      msg_params(e, scale, J.op, J.oc, J.C, -J.rot_mean, J.rot_sigma, H, W, mp);
+      msg_params(e, scale, J.op, J.oc, J.C, -J.rot_mean, J.rot_sigma, H, W, false, mp);
     return mp;
   };
   std::vector<std::vector<MsgParams>> upmp(upph.size()), dnmp(dnph.size());
@@ -793,7 +804,9 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
         for (int q = 0; q < 6; ++q) {
           d.tf[q] = mp.tf[q];
           d.tb[q] = mp.tb[q];
+          d.td[q] = mp.td[q];
         }
+        d.sparse = mp.sparse ? 1 : 0;
         ++out.n_full;
         out.ohmax = std::max(out.ohmax, mp.oh);
         out.owmax = std::max(out.owmax, mp.ow);
@@ -936,7 +949,7 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
     if (ph.n_full + (int)ph.tc.size() < ph.n)
       PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st));
     if (ph.n_full)
-      PA_LAUNCH_N("msg_full", 4, launch_msg_full(ph.msgs, ph.n, R, H, W, ph.ohmax, ph.owmax,
+      PA_LAUNCH_N("msg_full", 7, launch_msg_full(ph.msgs, ph.n, R, H, W, ph.ohmax, ph.owmax,
                                                  ph.kxf, ph.kyf, pl.err, st));
     if (!ph.tc.empty()) {
       PA_LAUNCH("msg_tc", launch_tc_toeplitz(ph.msgs, ph.n, H, W, st));
@@ -1276,6 +1289,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
                         int64_t scores_fields, const pa_ps_outputs *outs, int mem) {
   PsPlan pl;
   pl.tc_mode = ctx->msg_math == PA_MSG_BF16_TENSOR;
+  pl.sparse_up = true;  // findObjectImageRotJoints passes bIsSparse = true (objectdetect_findrot.cpp:740)
   pa_status st = build_sched(ctx, &trees[0], pl.sc);
   if (st) return st;
   for (int i = 1; i < n_img; ++i)
@@ -1898,7 +1912,8 @@ pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, in
 }
 
 pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
-                      const float *log_unary, int H, int W, const pa_ps_outputs *out, int mem) {
+                      int is_sparse, const float *log_unary, int H, int W,
+                      const pa_ps_outputs *out, int mem) {
   if (!ctx) return PA_ERR_INVALID;
   if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
   if (!tree || !log_unary || !out || H < 1 || W < 1 || H > 32767 || W > 32767)
@@ -1906,6 +1921,7 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
   if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
   PsPlan pl;
   pl.tc_mode = ctx->msg_math == PA_MSG_BF16_TENSOR;
+  pl.sparse_up = is_sparse != 0;
   pa_status st = build_sched(ctx, tree, pl.sc);
   if (st) return st;
   std::vector<std::vector<Joint>> joints(1);
@@ -1961,7 +1977,7 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
 pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float *child,
                                 float *parent, int R, int H, int W, const double *offset_c,
                                 const double *offset_p, const double *C, double rot_mean,
-                                double rot_sigma, double scale, int mem) {
+                                double rot_sigma, double scale, int is_sparse, int mem) {
   if (!ctx) return PA_ERR_INVALID;
   if (!ep || !child || !parent || !offset_c || !offset_p || !C || H < 1 || W < 1 ||
       H > 32767 || W > 32767 || R != ep->num_rotation_steps || !exp_ok(ep))
@@ -1971,7 +1987,7 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
   DeviceGuard dg(ctx->device);
   const int64_t N = (int64_t)R * H * W;
   MsgParams mp;
-  msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, H, W, mp);
+  msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, H, W, is_sparse != 0, mp);
   int4 *sdesc = nullptr;
   auto plan = [&](Builder &b, MsgDesc **md, int16_t **tables, double **shifts, int **slot,
                   int **err, const float **din, float **dout, float **e2) {
@@ -1992,7 +2008,9 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
       for (int q = 0; q < 6; ++q) {
         d.tf[q] = mp.tf[q];
         d.tb[q] = mp.tb[q];
+        d.td[q] = mp.td[q];
       }
+      d.sparse = mp.sparse ? 1 : 0;
     }
     *din = (mem == PA_MEM_HOST) ? b.scratch<float>(N) : child;
     *dout = (mem == PA_MEM_HOST) ? b.scratch<float>(N) : parent;
@@ -2040,7 +2058,7 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
   PA_LAUNCH_N("shift_tables", 2, launch_shift_tables(shifts, 1, R, H, W, tables, sdesc, s));
   PA_LAUNCH("msg_rows", launch_msg_rows(md, 1, R, H, W, (mp.xlen - 1) / 2, err, s));
   if (mp.full)
-    PA_LAUNCH_N("msg_full", 4, launch_msg_full(md, 1, R, H, W, mp.oh, mp.ow, (mp.xlen - 1) / 2,
+    PA_LAUNCH_N("msg_full", 7, launch_msg_full(md, 1, R, H, W, mp.oh, mp.ow, (mp.xlen - 1) / 2,
                                                (mp.ylen - 1) / 2, err, s));
   else
     PA_LAUNCH("msg_cols", launch_msg_cols(md, 1, R, H, W, (mp.ylen - 1) / 2, err, s));

@@ -129,6 +129,8 @@ struct MsgDesc {
   float *g0, *g1;
   double tf[6];           // rotated-grid cell (x3, y3) -> e2 position (x1, y1)
   double tb[6];           // image cell (x3, y3) -> rotated-grid position
+  int sparse;             // bIsSparse: TM_DIRECT forward rotation (e2 cell -> nearest g0 cell)
+  double td[6];           // e2 cell (x1, y1) -> rotated-grid position (sparse)
   // tensor-core spatial filter (diagonal C, BF16 operands, FP32 accumulation):
   // the row pass writes the rotation-filtered exp map as bf16 eb [R*H][W]
   // (row stride wp); x pass X^T = Tx * eb^T (xt [W][R*H], bf16), y pass
@@ -160,11 +162,13 @@ struct MsgParams {
   std::vector<float> rtaps, xtaps, ytaps;
   std::vector<double> shifts;  // [4][R]: a_x_in, a_y_in, a_x_out, a_y_out
   bool full = false;           // non-diagonal covariance: taps along the eigen axes
+  bool sparse = false;         // bIsSparse: TM_DIRECT forward rotation of a full covariance
   int oh = 0, ow = 0;          // rotated-grid size (transform_grid_resize)
-  double tf[6] = {0, 0, 0, 0, 0, 0}, tb[6] = {0, 0, 0, 0, 0, 0};
+  double tf[6] = {0, 0, 0, 0, 0, 0}, tb[6] = {0, 0, 0, 0, 0, 0}, td[6] = {0, 0, 0, 0, 0, 0};
 };
 void msg_params(const pa_exp_param *e, double scale, const double *oc, const double *op,
-                const double *C, double rot_mean, double rot_sigma, int H, int W, MsgParams &m);
+                const double *C, double rot_mean, double rot_sigma, int H, int W, bool sparse,
+                MsgParams &m);
 
 // Kernel launchers (defined in the .cu files).  All return cudaGetLastError().
 // fast_ok[p] / n_stumps[p] are host arrays describing the classifiers.

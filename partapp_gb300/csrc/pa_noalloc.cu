@@ -102,7 +102,7 @@ extern "C" pa_status pa_rot_joint_marginal_noalloc(const pa_exp_param *ep, const
   if (!on_device(child) || !on_device(parent)) return PA_ERR_INVALID;
 
   MsgParams mp;
-  msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, H, W, mp);
+  msg_params(ep, scale, offset_c, offset_p, C, rot_mean, rot_sigma, H, W, false, mp);
   if (mp.xlen > kNoAllocMaxTaps || mp.ylen > kNoAllocMaxTaps) return PA_ERR_NOMEM;
 
   unsigned char *base = nullptr;

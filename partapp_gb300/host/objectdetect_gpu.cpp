@@ -160,14 +160,13 @@ void computeRotJointMarginal(Context &ctx, const ExpParam &exp_param, FloatGrid3
                              FloatGrid3 &log_prob_parent, const double offset_c_10[2],
                              const double offset_p_01[2], const double C[4], double rot_mean,
                              double rot_sigma, double scale, bool bIsSparse) {
-  require(!bIsSparse, "computeRotJointMarginal: only the dense path (bIsSparse = false) is built");
   const size_t *s = log_prob_child.shape();
   if (log_prob_parent.num_elements() != log_prob_child.num_elements())
     log_prob_parent = FloatGrid3(s[0], s[1], s[2]);
   const pa_exp_param e = exp_param.c();
   ctx.check(pa_rot_joint_marginal(ctx.get(), &e, log_prob_child.data(), log_prob_parent.data(),
                                   (int)s[0], (int)s[1], (int)s[2], offset_c_10, offset_p_01, C,
-                                  rot_mean, rot_sigma, scale, PA_MEM_HOST));
+                                  rot_mean, rot_sigma, scale, bIsSparse ? 1 : 0, PA_MEM_HOST));
 }
 
 void computeRootPosteriorRot(Context &ctx, const PartApp &part_app,
@@ -180,7 +179,6 @@ void computeRootPosteriorRot(Context &ctx, const PartApp &part_app,
   (void)flip;  // the joints are already mirrored by loadJoints; flip only names output files
   (void)imgidx;
   (void)bSaveMarginals;
-  require(!bIsSparse, "computeRootPosteriorRot: only the dense path (bIsSparse = false) is built");
   const int P = (int)log_part_detections.size();
   require(P == part_app.m_part_conf.part_size(), "one detection stack per part");
   require(P > 0 && !log_part_detections[0].empty(), "empty detections");
@@ -204,7 +202,8 @@ void computeRootPosteriorRot(Context &ctx, const PartApp &part_app,
     marg.resize((size_t)P * N);
     out.o.log_marg = marg.data();
   }
-  ctx.check(pa_ps_infer(ctx.get(), &e, &th.t, 0, unary.data(), H, W, &out.o, PA_MEM_HOST));
+  ctx.check(pa_ps_infer(ctx.get(), &e, &th.t, 0, bIsSparse ? 1 : 0, unary.data(), H, W, &out.o,
+                        PA_MEM_HOST));
   const FindObjResult r = out.result(P, K > 0 ? K : 1);
   best_part_hyp = r.part_hyps;
   if (log_marginals) {

@@ -130,7 +130,8 @@ struct PartApp {
 };
 
 // computeRotJointMarginal (objectdetect_findrot.cpp:292-456): child ->
-// parent frame message.  bIsSparse must be false (the dense path).
+// parent frame message.  bIsSparse selects TM_DIRECT for the forward
+// rotation of a full covariance's map (bilinear otherwise).
 void computeRotJointMarginal(Context &ctx, const ExpParam &exp_param, FloatGrid3 &log_prob_child,
                              FloatGrid3 &log_prob_parent, const double offset_c_10[2],
                              const double offset_p_01[2], const double C[4], double rot_mean,

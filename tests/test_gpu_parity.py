@@ -296,33 +296,38 @@ def test_ps_variants(ctx, orc, variant):
 
 
 # ------------------------------------------------------- full covariance
-@pytest.mark.parametrize("R", [24, 12])
-def test_rot_joint_marginal_full_covariance(ctx, orc, R):
+@pytest.mark.parametrize("R,sparse", [(24, False), (12, False), (24, True), (12, True)])
+def test_rot_joint_marginal_full_covariance(ctx, orc, R, sparse):
     """Non-diagonal C: gaussFilter2dOffset (rotation into the eigenbasis,
-    eigen-axis filter, rotation back) against the oracle."""
-    rng = np.random.default_rng(40 + R)
+    eigen-axis filter, rotation back) against the oracle; sparse = bIsSparse,
+    the TM_DIRECT forward rotation (multi_array_filter.hpp:351-355)."""
+    rng = np.random.default_rng(40 + R + 7 * int(sparse))
     H, W = 50, 70
     child = synth.random_log_unary(rng, 1, R, H, W, zero_frac=0.02)[0]
     step = synth.rot_step_rad(R)
     for k, rs, oc, op, Cm in [(1, 1.5, (4.2, -3.1), (-2.6, 5.7), [[4.0, 1.5], [1.5, 2.0]]),
                               (0, 0.0, (-6.0, 2.5), (3.0, -1.0), [[1.0, -0.6], [-0.6, 6.25]]),
                               (-2, 2.5, (0.5, 9.0), (1.5, -8.0), [[30.0, 12.0], [12.0, 9.0]])]:
-        e = orc.make_exp(R=R)
+        e = orc.make_exp(R=R, sparse=sparse)
         args = (np.array(oc), np.array(op), np.array(Cm), k * step, rs * step)
         want = orc.rot_joint_marginal(e, child, *args)
-        got = ctx.rot_joint_marginal(_pa_exp(R), child, *args)
+        got = ctx.rot_joint_marginal(_pa_exp(R), child, *args, is_sparse=sparse)
         oob = want == LOG_ZERO
         assert np.array_equal(got[oob], want[oob])
         assert maxnorm_err(got, want) <= 1e-5
         want64 = orc.rot_joint_marginal(e, child.astype(np.float64), *args, f64=True)
         assert maxnorm_err(got, want64) <= 1e-4
+        if sparse:  # the two forward rotations give different messages
+            dense = orc.rot_joint_marginal(orc.make_exp(R=R), child, *args)
+            assert maxnorm_err(dense, want) > 1e-3
 
 
-@pytest.mark.parametrize("flip", [False, True])
-def test_ps_full_covariance(ctx, orc, flip):
+@pytest.mark.parametrize("flip,sparse", [(False, False), (True, False), (False, True),
+                                         (True, True)])
+def test_ps_full_covariance(ctx, orc, flip, sparse):
     """A tree whose joints mix diagonal and full covariances (learned joints
     carry correlations, objectdetect_learnparam.cpp:465)."""
-    rng = np.random.default_rng(31 + int(flip))
+    rng = np.random.default_rng(31 + int(flip) + 2 * int(sparse))
     R, H, W = 16, 44, 60
     tree = small_tree(rng, R)
     for j, rho in ((1, 0.5), (4, -0.35), (6, 0.2), (8, -0.6)):
@@ -330,13 +335,13 @@ def test_ps_full_covariance(ctx, orc, flip):
         off = rho * math.sqrt(c[0] * c[3])
         tree["C"][j] = [c[0], off, off, c[3]]
     u = synth.random_log_unary(rng, 10, R, H, W)
-    e = orc.make_exp(R=R)
+    e = orc.make_exp(R=R, sparse=sparse)
     t_or = dict(tree)
     if flip:  # loadJoints mirroring: x of the offsets, the off-diagonal of C
         t_or = dict(tree, offset_c=tree["offset_c"] * [-1, 1], offset_p=tree["offset_p"] * [-1, 1],
                     C=tree["C"] * [1, -1, -1, 1], rot_mean=-tree["rot_mean"])
     want = orc.ps_infer(e, t_or, u)
-    got = ctx.compute_root_posterior_rot(_pa_exp(R), tree, u, flip=flip)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R), tree, u, flip=flip, is_sparse=sparse)
     compare_ps(got, want, oracle64(orc, e, t_or, u))
     assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
 
@@ -354,6 +359,28 @@ def test_find_obj_pipeline(ctx, orc, interpolate):
                        img["Tig"], 64, 96)
     compare_ps(got, want, oracle64(orc, e, img["tree"], want["log_unary"]))
     assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
+
+
+def test_find_obj_full_covariance(ctx, orc):
+    """--find_obj with correlated joints: findObjectImageRotJoints passes
+    bIsSparse = true (objectdetect_findrot.cpp:740), so the upward messages of
+    the full-covariance joints take the TM_DIRECT forward rotation."""
+    img = synth.make_image(17, R=12, H=64, W=96, n_stumps=120, D=96, offset_range=(3, 10),
+                           sigma_range=(1.5, 3))
+    tree = img["tree"]
+    for j, rho in ((0, 0.45), (3, -0.5), (5, 0.3)):
+        c = tree["C"][j]
+        off = rho * math.sqrt(c[0] * c[3])
+        tree["C"][j] = [c[0], off, off, c[3]]
+    e = orc.make_exp(R=12)
+    want = orc.find_obj(e, tree, img["models"], img["desc"], img["Tig"], 64, 96)
+    cls = ctx.classifiers(img["models"])
+    got = ctx.find_obj(_pa_exp(12), tree, cls, img["desc"], img["Tig"], 64, 96)
+    compare_ps(got, want, oracle64(orc, orc.make_exp(R=12, sparse=True), tree, want["log_unary"]))
+    assert maxnorm_err(got["root_post"], want["root_post"]) <= TOL_F32
+    # the same unaries through pa_ps_infer with bIsSparse = true agree
+    ps = ctx.compute_root_posterior_rot(_pa_exp(12), tree, want["log_unary"], is_sparse=True)
+    assert maxnorm_err(ps["log_marg"], got["log_marg"]) <= 1e-6
 
 
 def test_find_obj_batch_device_resident(ctx, orc):
