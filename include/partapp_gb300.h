@@ -89,12 +89,15 @@ typedef struct {
   int num_rotation_steps;        /* R [48] */
   float min_part_rotation;       /* degrees [-180] */
   float max_part_rotation;       /* degrees [180] */
-  float min_object_scale;        /* [1]; num_scale_steps is 1 */
+  float min_object_scale;        /* [1] */
   float max_object_scale;        /* [1] */
   float strip_border_detections; /* fraction of the width [0] */
   int roi_save_num_samples;      /* local maxima kept per part [1000], <= 2048 */
   int use_pairwise;              /* [1] */
   int interpolate;               /* grid->image TM_BILINEAR if 1, else TM_DIRECT [0] */
+  int num_scale_steps;           /* S [1]; 0 reads as 1.  S > 1 needs min < max object
+                                    scale and is taken by pa_ps_infer (the pa_find_obj*
+                                    entries score one scale of descriptors) */
 } pa_exp_param;
 
 void pa_exp_param_default(pa_exp_param *p);
@@ -184,15 +187,18 @@ typedef struct {
 } pa_part_hyp;
 
 /* Outputs of one image.  Every pointer may be NULL.  Map outputs live in the
- * call's `mem` space, the rest in host memory.
- *   log_marg     [P][R][H][W] final log marginals (log_part_posterior)
- *   root_post    [H][W]       log root posterior over the kept rotations
- *   best         [P]          first-maximum argmax of each marginal
- *   part_hyps    [P][roi_save_num_samples] local maxima, n_part_hyps [P]
- *   root_hyps    [1000][4]    (scale, x, y, score), n_root_hyps [1]
- *   log_z        [P]          FP64 log(sum exp(log_marg[p])) per part; the
+ * call's `mem` space, the rest in host memory.  S = num_scale_steps (1 for
+ * the pa_find_obj* entries).
+ *   log_marg     [P][S][R][H][W] final log marginals (log_part_posterior)
+ *   root_post    [S][H][W]    log root posterior over the kept rotations
+ *   best         [P]          first-maximum argmax of each marginal (of the
+ *                             last scale; scaleidx = S - 1)
+ *   part_hyps    [P][roi_save_num_samples] local maxima (of the last scale),
+ *                             n_part_hyps [P]
+ *   root_hyps    [1000][4]    (scale, x, y, score) over [S][H][W], n_root_hyps [1]
+ *   log_z        [S][P]       FP64 log(sum exp(log_marg[p])) per part; the
  *                             root's entry is the log-partition function
- *   msg_max      [2*(P-1)]    FP64 copy of the per-message normaliser in_M:
+ *   msg_max      [S][2*(P-1)] FP64 copy of the per-message normaliser in_M:
  *                             [j] upward message over joint j, [P-1+j] the
  *                             downward message over joint j */
 typedef struct {
@@ -222,7 +228,13 @@ typedef struct {
  * covariance's map into its eigenbasis by TM_DIRECT when set (bilinear
  * otherwise); the downward messages are always dense (:174-179, 224-229).
  * pa_find_obj* pass is_sparse = 1, as findObjectImageRotJoints does (:740).
- *   log_unary [P][R][H][W] */
+ * With num_scale_steps = S > 1 every scale is an independent pass with the
+ * joints at scale_from_index(s) (the scale loop :503-678); best and
+ * part_hyps come from the last scale, as computePartMarginals leaves them,
+ * and the root maxima are taken over the [S][H][W] posterior with scale
+ * neighbours (findLocalMax, objectdetect_aux.cpp:193-236).  Without pairwise
+ * terms the maxima are those of scale 0 (getMaxStates, :73-110).
+ *   log_unary [P][S][R][H][W] */
 pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
                       int is_sparse, const float *log_unary, int H, int W,
                       const pa_ps_outputs *out, int mem);

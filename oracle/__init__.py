@@ -38,6 +38,7 @@ class OrcExp(C.Structure):
         ("max_local_max", C.c_int),
         ("use_pairwise", C.c_int),
         ("sparse_up", C.c_int),
+        ("num_scale_steps", C.c_int),
     ]
 
 
@@ -144,12 +145,14 @@ def _declare(L):
 # ---------------------------------------------------------------------------
 
 def make_exp(R=24, min_rot=-180.0, max_rot=180.0, scale=1.0, strip=0.0, max_local_max=1000,
-             use_pairwise=True, sparse=False) -> OrcExp:
+             use_pairwise=True, sparse=False, n_scales=1, scale_range=None) -> OrcExp:
     """sparse: bIsSparse of the upward messages (and of rot_joint_marginal);
     the --find_obj path (find_obj) always uses True, as
-    findObjectImageRotJoints does."""
-    return OrcExp(int(R), float(min_rot), float(max_rot), float(scale), float(scale), float(strip),
-                  int(max_local_max), int(bool(use_pairwise)), int(bool(sparse)))
+    findObjectImageRotJoints does.  n_scales > 1 needs scale_range =
+    (min_object_scale, max_object_scale) with min < max."""
+    lo, hi = (scale, scale) if scale_range is None else scale_range
+    return OrcExp(int(R), float(min_rot), float(max_rot), float(lo), float(hi), float(strip),
+                  int(max_local_max), int(bool(use_pairwise)), int(bool(sparse)), int(n_scales))
 
 
 class _TreeHolder:
@@ -284,12 +287,15 @@ def ps_infer(exp: OrcExp, tree, log_unary, f64=False, want_marg=True, want_hyps=
     n_root_hyps)."""
     dt, ct = (np.float64, C.c_double) if f64 else (np.float32, C.c_float)
     u = np.ascontiguousarray(log_unary, dtype=dt)
-    P, R, H, W = u.shape
+    multi = u.ndim == 5  # [P][S][R][H][W]
+    P, S, R, H, W = u.shape if multi else (u.shape[0], 1) + u.shape[1:]
+    if S != max(1, exp.num_scale_steps):
+        raise ValueError("log_unary has a different number of scales than exp")
     th = _TreeHolder(tree)
     K = exp.max_local_max
     marg = np.empty_like(u) if want_marg else None
     best = np.zeros((P, 7), dtype=np.float32)
-    rp = np.empty((H, W), dtype=dt)
+    rp = np.empty((S, H, W) if multi else (H, W), dtype=dt)
     ph = np.zeros((P, K, 7), dtype=np.float32) if want_hyps else None
     nph = np.zeros(P, dtype=np.int32)
     rh = np.zeros((1000, 4), dtype=np.float32) if want_hyps else None

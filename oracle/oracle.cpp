@@ -61,9 +61,13 @@ int index_from_rot(const orc_exp *e, double rot) {
   return index_from_value(e->min_part_rotation, e->max_part_rotation,
                           (double)(unsigned)e->num_rotation_steps, rot);
 }
-/* scale_from_index with num_scale_steps = 1, partapp_aux.hpp:77-83 */
+/* ExpParam::num_scale_steps (ExpParam.proto:191, default 1); 0 reads as 1 */
+int n_scales(const orc_exp *e) { return e->num_scale_steps > 1 ? e->num_scale_steps : 1; }
+
+/* scale_from_index, partapp_aux.hpp:86-92 */
 double scale_from_index(const orc_exp *e, int idx) {
-  return value_from_index(e->min_object_scale, e->max_object_scale, 1.0, idx);
+  return value_from_index(e->min_object_scale, e->max_object_scale,
+                          (double)n_scales(e), idx);
 }
 
 template <class T> struct Num;
@@ -456,9 +460,10 @@ template <class T> void add_grid(std::vector<T> &a, const std::vector<T> &b) {
 
 /* PartHyp(exp_param, scaleidx, rotidx, x, y, score).toVect(),
  * objectdetect.h:95-159 */
-void part_hyp_vect(const orc_exp *e, int rotidx, int x, int y, float score, float *o) {
-  o[0] = 0.0f;
-  o[1] = (float)scale_from_index(e, 0);
+void part_hyp_vect(const orc_exp *e, int rotidx, int x, int y, float score, float *o,
+                   int scaleidx = 0) {
+  o[0] = (float)scaleidx;
+  o[1] = (float)scale_from_index(e, scaleidx);
   o[2] = (float)rotidx;
   o[3] = (float)rot_from_index(e, rotidx);
   o[4] = (float)x;
@@ -468,7 +473,8 @@ void part_hyp_vect(const orc_exp *e, int rotidx, int x, int y, float score, floa
 
 /* first strict maximum over the flat [R][H][W] index,
  * objectdetect_findrot.cpp:261-277 */
-template <class T> void best_hyp(const orc_exp *e, const T *g, int R, int H, int W, float *o) {
+template <class T>
+void best_hyp(const orc_exp *e, const T *g, int R, int H, int W, float *o, int scaleidx) {
   float bestval = (float)-std::numeric_limits<double>::max(); /* -DBL_MAX */
   T bestv = (T)bestval;
   long bestidx = -1;
@@ -482,147 +488,182 @@ template <class T> void best_hyp(const orc_exp *e, const T *g, int R, int H, int
   int r = (int)(bestidx / ((long)H * W));
   long rem = bestidx % ((long)H * W);
   int x = (int)(rem % W), y = (int)(rem / W);
-  part_hyp_vect(e, r, x, y, (float)bestv, o);
+  part_hyp_vect(e, r, x, y, (float)bestv, o, scaleidx);
 }
 
+/* One scale of computeRootPosteriorRot: the upward pass (:578-658) and
+ * computePartMarginals (:124-236) at `scale`; post[p] receives the final
+ * log marginals. */
 template <class T>
-int ps_infer(const orc_exp *e, const orc_tree *t, const T *log_unary, int H, int W,
-             T *log_marg, float *best_conf, T *root_post_out, float *part_hyps,
-             int *n_part_hyps, float *root_hyps, int *n_root_hyps) {
+int ps_one_scale(const orc_exp *e, const orc_tree *t, const std::vector<std::vector<T>> &unary,
+                 int H, int W, double scale, std::vector<std::vector<T>> &post) {
   const int P = t->n_parts, R = e->num_rotation_steps;
-  const size_t HW = (size_t)H * W, N = HW * R;
+  const size_t N = (size_t)H * W * R;
   const int root = t->root;
-  if (P < 1 || root < 0 || root >= P || t->n_joints != P - 1) return -1;
-
-  std::vector<std::vector<T>> unary(P);
-  for (int p = 0; p < P; ++p) unary[p].assign(log_unary + p * N, log_unary + (p + 1) * N);
-
-  /* enforce upright orientation, objectdetect_findrot.cpp:509-523 */
-  for (int p = 0; p < P; ++p)
-    if (t->is_upright[p])
-      for (int r = 0; r < R; ++r) {
-        double cur_rot = rot_from_index(e, r);
-        if (!(std::fabs(cur_rot) < 15.0))
-          std::fill(unary[p].begin() + r * HW, unary[p].begin() + (r + 1) * HW, (T)LOG_ZERO);
-      }
-  /* strip border detections of the root, :528-551 */
-  if (e->strip_border_detections > 0) {
-    int sw = (int)(e->strip_border_detections * W);
-    for (int r = 0; r < R; ++r)
-      for (int y = 0; y < H; ++y) {
-        T *row = unary[root].data() + r * HW + (size_t)y * W;
-        for (int x = 0; x < sw; ++x) row[x] = (T)LOG_ZERO;
-        for (int x = W - sw; x < W; ++x) row[x] = (T)LOG_ZERO;
-      }
-  }
-  const double scale = scale_from_index(e, 0);
-
-  std::vector<std::vector<T>> post(P, std::vector<T>(N, (T)0));
+  post.assign(P, std::vector<T>(N, (T)0));
   std::vector<std::vector<T>> from_root(P, std::vector<T>(N, (T)0));
   std::vector<T> msg(N);
   std::vector<int> ch, js;
 
-  if (e->use_pairwise) {
-    /* upward pass, :578-658 */
-    std::vector<bool> done(P, false);
-    std::vector<int> stack{root};
-    while (!stack.empty()) {
-      int cur = stack.back();
-      stack.pop_back();
-      bool can = true;
-      for (int j = 0; j < t->n_joints; ++j)
-        if (t->parent[j] == cur && !done[t->child[j]]) {
-          can = false;
-          stack.push_back(cur);
-          stack.push_back(t->child[j]);
-          break;
-        }
-      if (!can) continue;
-      incoming(t, cur, ch, js);
-      for (size_t i = 0; i < ch.size(); ++i) {
-        int c = ch[i], j = js[i];
-        int rc = rot_joint_marginal<T>(e, post[c].data(), msg.data(), R, H, W, t->offset_c + 2 * j,
-                                       t->offset_p + 2 * j, t->C + 4 * j, t->rot_mean[j],
-                                       t->rot_sigma[j], scale, e->sparse_up != 0);
-        if (rc) return rc;
-        add_grid(post[cur], msg);
-        if (cur == root)
-          for (size_t i2 = 0; i2 < ch.size(); ++i2)
-            if (i2 != i) add_grid(from_root[ch[i2]], msg);
+  /* upward pass, :578-658 */
+  std::vector<bool> done(P, false);
+  std::vector<int> stack{root};
+  while (!stack.empty()) {
+    int cur = stack.back();
+    stack.pop_back();
+    bool can = true;
+    for (int j = 0; j < t->n_joints; ++j)
+      if (t->parent[j] == cur && !done[t->child[j]]) {
+        can = false;
+        stack.push_back(cur);
+        stack.push_back(t->child[j]);
+        break;
       }
-      add_grid(post[cur], unary[cur]);
-      done[cur] = true;
-    }
-
-    /* computePartMarginals, :124-236 */
-    incoming(t, root, ch, js);
-    std::vector<int> stack2;
-    std::vector<int> rch = ch, rjs = js;
-    for (size_t i = 0; i < rch.size(); ++i) {
-      int c = rch[i], j = rjs[i];
-      add_grid(from_root[c], unary[root]);
-      int rc = rot_joint_marginal<T>(e, from_root[c].data(), msg.data(), R, H, W, t->offset_p + 2 * j,
-                                     t->offset_c + 2 * j, t->C + 4 * j, -t->rot_mean[j],
-                                     t->rot_sigma[j], scale, false);
+    if (!can) continue;
+    incoming(t, cur, ch, js);
+    for (size_t i = 0; i < ch.size(); ++i) {
+      int c = ch[i], j = js[i];
+      int rc = rot_joint_marginal<T>(e, post[c].data(), msg.data(), R, H, W, t->offset_c + 2 * j,
+                                     t->offset_p + 2 * j, t->C + 4 * j, t->rot_mean[j],
+                                     t->rot_sigma[j], scale, e->sparse_up != 0);
       if (rc) return rc;
-      from_root[c] = msg;
+      add_grid(post[cur], msg);
+      if (cur == root)
+        for (size_t i2 = 0; i2 < ch.size(); ++i2)
+          if (i2 != i) add_grid(from_root[ch[i2]], msg);
+    }
+    add_grid(post[cur], unary[cur]);
+    done[cur] = true;
+  }
+
+  /* computePartMarginals, :124-236 */
+  incoming(t, root, ch, js);
+  std::vector<int> stack2;
+  std::vector<int> rch = ch, rjs = js;
+  for (size_t i = 0; i < rch.size(); ++i) {
+    int c = rch[i], j = rjs[i];
+    add_grid(from_root[c], unary[root]);
+    int rc = rot_joint_marginal<T>(e, from_root[c].data(), msg.data(), R, H, W, t->offset_p + 2 * j,
+                                   t->offset_c + 2 * j, t->C + 4 * j, -t->rot_mean[j],
+                                   t->rot_sigma[j], scale, false);
+    if (rc) return rc;
+    from_root[c] = msg;
+    stack2.push_back(c);
+  }
+  while (!stack2.empty()) {
+    int cur = stack2.back();
+    stack2.pop_back();
+    add_grid(post[cur], from_root[cur]);
+    incoming(t, cur, ch, js);
+    if (ch.size() > 1) return -3; /* assert(all_children.size() <= 1), :210 */
+    if (ch.size() == 1) {
+      int c = ch[0], j = js[0];
+      std::vector<T> tmp = unary[cur];
+      add_grid(tmp, from_root[cur]);
+      int rc = rot_joint_marginal<T>(e, tmp.data(), from_root[c].data(), R, H, W,
+                                     t->offset_p + 2 * j, t->offset_c + 2 * j, t->C + 4 * j,
+                                     -t->rot_mean[j], t->rot_sigma[j], scale, false);
+      if (rc) return rc;
       stack2.push_back(c);
     }
-    while (!stack2.empty()) {
-      int cur = stack2.back();
-      stack2.pop_back();
-      add_grid(post[cur], from_root[cur]);
-      incoming(t, cur, ch, js);
-      if (ch.size() > 1) return -3; /* assert(all_children.size() <= 1), :210 */
-      if (ch.size() == 1) {
-        int c = ch[0], j = js[0];
-        std::vector<T> tmp = unary[cur];
-        add_grid(tmp, from_root[cur]);
-        int rc = rot_joint_marginal<T>(e, tmp.data(), from_root[c].data(), R, H, W,
-                                       t->offset_p + 2 * j, t->offset_c + 2 * j, t->C + 4 * j,
-                                       -t->rot_mean[j], t->rot_sigma[j], scale, false);
-        if (rc) return rc;
-        stack2.push_back(c);
+  }
+  return 0;
+}
+
+/* computeRootPosteriorRot (objectdetect_findrot.cpp:470-727) over all
+ * num_scale_steps scales, each an independent pass at its own scale (the
+ * loop :503-678).  log_unary [P][S][R][H][W]; log_marg [P][S][R][H][W];
+ * root_post [S][H][W].  best_conf and part_hyps are those of the last scale
+ * (computePartMarginals clears best_part_hyp on every scale, :254-258); the
+ * root hypotheses are the local maxima of the [S][H][W] root posterior with
+ * scale neighbours (:1037-1038).  Without pairwise terms the reference
+ * reads scale 0 only (getMaxStates, :73-110). */
+template <class T>
+int ps_infer(const orc_exp *e, const orc_tree *t, const T *log_unary, int H, int W,
+             T *log_marg, float *best_conf, T *root_post_out, float *part_hyps,
+             int *n_part_hyps, float *root_hyps, int *n_root_hyps) {
+  const int P = t->n_parts, R = e->num_rotation_steps, S = n_scales(e);
+  const size_t HW = (size_t)H * W, N = HW * R;
+  const int root = t->root;
+  if (P < 1 || root < 0 || root >= P || t->n_joints != P - 1) return -1;
+  if (S > 1 && e->min_object_scale == e->max_object_scale) return -1; /* :33-38 asserts */
+
+  /* unary[s][p] */
+  std::vector<std::vector<std::vector<T>>> unary(S, std::vector<std::vector<T>>(P));
+  for (int sc = 0; sc < S; ++sc)
+    for (int p = 0; p < P; ++p)
+      unary[sc][p].assign(log_unary + ((size_t)p * S + sc) * N,
+                          log_unary + ((size_t)p * S + sc + 1) * N);
+
+  for (int sc = 0; sc < S; ++sc) {
+    /* enforce upright orientation, objectdetect_findrot.cpp:509-523 */
+    for (int p = 0; p < P; ++p)
+      if (t->is_upright[p])
+        for (int r = 0; r < R; ++r) {
+          double cur_rot = rot_from_index(e, r);
+          if (!(std::fabs(cur_rot) < 15.0))
+            std::fill(unary[sc][p].begin() + r * HW, unary[sc][p].begin() + (r + 1) * HW,
+                      (T)LOG_ZERO);
+        }
+    /* strip border detections of the root, :528-551 */
+    if (e->strip_border_detections > 0) {
+      int sw = (int)(e->strip_border_detections * W);
+      for (int r = 0; r < R; ++r)
+        for (int y = 0; y < H; ++y) {
+          T *row = unary[sc][root].data() + r * HW + (size_t)y * W;
+          for (int x = 0; x < sw; ++x) row[x] = (T)LOG_ZERO;
+          for (int x = W - sw; x < W; ++x) row[x] = (T)LOG_ZERO;
+        }
+    }
+  }
+
+  const int hyp_scale = e->use_pairwise ? S - 1 : 0;
+  std::vector<T> root_full(e->use_pairwise ? (size_t)S * HW : 0);
+  std::vector<std::vector<T>> post;
+  for (int sc = 0; sc < S; ++sc) {
+    if (e->use_pairwise) {
+      int rc = ps_one_scale<T>(e, t, unary[sc], H, W, scale_from_index(e, sc), post);
+      if (rc) return rc;
+    } else {
+      post = unary[sc]; /* getMaxStates: the marginals are the unaries */
+    }
+    for (int p = 0; p < P; ++p) {
+      if (log_marg) std::copy(post[p].begin(), post[p].end(), log_marg + ((size_t)p * S + sc) * N);
+      if (sc != hyp_scale) continue;
+      if (best_conf) best_hyp(e, post[p].data(), R, H, W, best_conf + 7 * p, sc);
+      if (part_hyps || n_part_hyps) {
+        const int K = e->max_local_max;
+        auto lm = find_local_max(post[p].data(), R, H, W, K);
+        if (n_part_hyps) n_part_hyps[p] = (int)lm.size();
+        if (part_hyps)
+          for (size_t k = 0; k < lm.size(); ++k)
+            part_hyp_vect(e, (int)lm[k][0], (int)lm[k][1], (int)lm[k][2], (float)lm[k][3],
+                          part_hyps + ((size_t)p * K + k) * 7);
       }
     }
-  } else {
-    /* getMaxStates, :73-110: the marginals are the unaries */
-    for (int p = 0; p < P; ++p) post[p] = unary[p];
-  }
-
-  for (int p = 0; p < P; ++p) {
-    if (log_marg) std::copy(post[p].begin(), post[p].end(), log_marg + p * N);
-    if (best_conf) best_hyp(e, post[p].data(), R, H, W, best_conf + 7 * p);
-    if (part_hyps || n_part_hyps) {
-      const int K = e->max_local_max;
-      auto lm = find_local_max(post[p].data(), R, H, W, K);
-      if (n_part_hyps) n_part_hyps[p] = (int)lm.size();
-      if (part_hyps)
-        for (size_t k = 0; k < lm.size(); ++k)
-          part_hyp_vect(e, (int)lm[k][0], (int)lm[k][1], (int)lm[k][2], (float)lm[k][3],
-                        part_hyps + ((size_t)p * K + k) * 7);
+    /* root rotation marginalisation, :694-726 */
+    if (e->use_pairwise) {
+      std::vector<int> keep;
+      if (t->is_upright[root]) {
+        int k1 = index_from_rot(e, -1e-6), k2 = index_from_rot(e, 1e-6);
+        keep.push_back(k1);
+        if (k2 != k1) keep.push_back(k2);
+      } else {
+        for (int r = 0; r < R; ++r) keep.push_back(r);
+      }
+      T *rp = root_full.data() + (size_t)sc * HW;
+      const T *pr = post[root].data();
+      for (size_t i = 0; i < HW; ++i) rp[i] = Num<T>::ex(pr[keep[0] * HW + i]);
+      for (size_t k = 1; k < keep.size(); ++k)
+        for (size_t i = 0; i < HW; ++i) rp[i] = rp[i] + Num<T>::ex(pr[keep[k] * HW + i]);
+      log_grid(rp, HW);
     }
   }
 
-  /* root rotation marginalisation, :694-726 */
   if (e->use_pairwise && (root_post_out || root_hyps || n_root_hyps)) {
-    std::vector<int> keep;
-    if (t->is_upright[root]) {
-      int k1 = index_from_rot(e, -1e-6), k2 = index_from_rot(e, 1e-6);
-      keep.push_back(k1);
-      if (k2 != k1) keep.push_back(k2);
-    } else {
-      for (int r = 0; r < R; ++r) keep.push_back(r);
-    }
-    std::vector<T> rp(HW);
-    const T *pr = post[root].data();
-    for (size_t i = 0; i < HW; ++i) rp[i] = Num<T>::ex(pr[keep[0] * HW + i]);
-    for (size_t k = 1; k < keep.size(); ++k)
-      for (size_t i = 0; i < HW; ++i) rp[i] = rp[i] + Num<T>::ex(pr[keep[k] * HW + i]);
-    log_grid(rp.data(), HW);
-    if (root_post_out) std::copy(rp.begin(), rp.end(), root_post_out);
+    if (root_post_out) std::copy(root_full.begin(), root_full.end(), root_post_out);
     /* findLocalMax(..., max_hypothesis_number = 1000), :1037-1038 */
-    auto lm = find_local_max(rp.data(), 1, H, W, 1000);
+    auto lm = find_local_max(root_full.data(), S, H, W, 1000);
     if (n_root_hyps) *n_root_hyps = (int)lm.size();
     if (root_hyps)
       for (size_t k = 0; k < lm.size(); ++k) {
@@ -829,7 +870,7 @@ int orc_find_obj_f32(const orc_exp *e, const orc_tree *t, const orc_models *m, c
                      float *log_unary, float *log_marg, float *best_conf, float *root_post,
                      float *part_hyps, int *n_part_hyps, float *root_hyps, int *n_root_hyps) {
   const int P = t->n_parts, R = e->num_rotation_steps;
-  if (m->n_parts < P) return -1;
+  if (m->n_parts < P || n_scales(e) != 1) return -1; /* one scale of descriptors */
   const size_t HW = (size_t)H * W, N = HW * R, G = (size_t)ny * nx;
   std::vector<float> unary((size_t)P * N);
   std::vector<float> grid(G);

@@ -43,6 +43,7 @@ typedef struct {
   int sparse_up;                 /* bIsSparse of the upward messages (computeRootPosteriorRot;
                                     findObjectImageRotJoints passes true, :740) and of
                                     orc_rot_joint_marginal_*; matters for full covariances */
+  int num_scale_steps;           /* S, default 1 (0 reads as 1) */
 } orc_exp;
 
 /* Tree + joints (libPictStruct/objectdetect.h:54-86, already converted to
@@ -121,15 +122,16 @@ int orc_rot_joint_marginal_f64(const orc_exp *e, const double *child,
 
 /* computeRootPosteriorRot + computePartMarginals + root rotation
  * marginalisation + findLocalMax (objectdetect_findrot.cpp:73-286,470-727;
- * objectdetect_aux.cpp:193-320).  log_unary is [P][R][H][W] after
+ * objectdetect_aux.cpp:193-320).  log_unary is [P][S][R][H][W] after
  * clip_scores_fill + computeLogGrid (the function applies the upright mask
- * and the root border strip itself, as the reference does).
- *   log_marg   [P][R][H][W]  final log marginals (log_part_posterior)
- *   best_conf  [P][7]        PartHyp::toVect of the first-max argmax
- *   root_post  [H][W]        log root posterior over kept rotations
- *   part_hyps  [P][K][7]     local maxima per part (K = e->max_local_max)
+ * and the root border strip itself, as the reference does); S =
+ * num_scale_steps, each scale an independent pass at scale_from_index(s).
+ *   log_marg   [P][S][R][H][W]  final log marginals (log_part_posterior)
+ *   best_conf  [P][7]        PartHyp::toVect of the first-max argmax (last scale)
+ *   root_post  [S][H][W]     log root posterior over kept rotations
+ *   part_hyps  [P][K][7]     local maxima per part, last scale (K = e->max_local_max)
  *   n_part_hyps [P]
- *   root_hyps  [K][4]        (scale, x, y, score) of root local maxima
+ *   root_hyps  [K][4]        (scale, x, y, score) of root local maxima over [S][H][W]
  *   n_root_hyps [1]
  * Any output pointer may be NULL.  Returns 0 on success. */
 int orc_ps_infer_f32(const orc_exp *e, const orc_tree *t, const float *log_unary,

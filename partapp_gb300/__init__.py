@@ -67,7 +67,7 @@ class ExpParam(C.Structure):
                 ("max_part_rotation", C.c_float), ("min_object_scale", C.c_float),
                 ("max_object_scale", C.c_float), ("strip_border_detections", C.c_float),
                 ("roi_save_num_samples", C.c_int), ("use_pairwise", C.c_int),
-                ("interpolate", C.c_int)]
+                ("interpolate", C.c_int), ("num_scale_steps", C.c_int)]
 
 
 class Stump(C.Structure):
@@ -151,9 +151,12 @@ def load_library():
 
 
 def exp_param(R=24, min_rot=-180.0, max_rot=180.0, scale=1.0, strip=0.0, local_max=1000,
-              use_pairwise=True, interpolate=True) -> ExpParam:
-    return ExpParam(int(R), float(min_rot), float(max_rot), float(scale), float(scale),
-                    float(strip), int(local_max), int(bool(use_pairwise)), int(bool(interpolate)))
+              use_pairwise=True, interpolate=True, n_scales=1, scale_range=None) -> ExpParam:
+    """n_scales > 1 needs scale_range = (min_object_scale, max_object_scale)."""
+    lo, hi = (scale, scale) if scale_range is None else scale_range
+    return ExpParam(int(R), float(min_rot), float(max_rot), float(lo), float(hi),
+                    float(strip), int(local_max), int(bool(use_pairwise)), int(bool(interpolate)),
+                    int(n_scales))
 
 
 def _is_torch(a):
@@ -358,12 +361,17 @@ class Context:
                                                  int(is_sparse), c.mem))
         return out
 
-    def _outputs(self, P, R, H, W, K, mem, like, want_marg=True, want_root=True):
-        res = dict(best=(PartHyp * P)(), log_z=np.zeros(P), msg_max=np.zeros(max(1, 2 * (P - 1))),
+    def _outputs(self, P, R, H, W, K, mem, like, want_marg=True, want_root=True, S=0):
+        """S = 0: one-scale shapes; S >= 1: [P][S][R][H][W] / [S][H][W] maps."""
+        n = max(S, 1)
+        res = dict(best=(PartHyp * P)(), log_z=np.zeros(n * P),
+                   msg_max=np.zeros(n * max(1, 2 * (P - 1))),
                    n_part_hyps=np.zeros(P, dtype=np.int32), n_root_hyps=np.zeros(1, np.int32),
                    part_hyps=(PartHyp * max(1, P * K))(), root_hyps=np.zeros((1000, 4), np.float32))
-        res["log_marg"] = _empty_like_space((P, R, H, W), mem, like) if want_marg else None
-        res["root_post"] = _empty_like_space((H, W), mem, like) if want_root else None
+        mshape = (P, S, R, H, W) if S else (P, R, H, W)
+        rshape = (S, H, W) if S else (H, W)
+        res["log_marg"] = _empty_like_space(mshape, mem, like) if want_marg else None
+        res["root_post"] = _empty_like_space(rshape, mem, like) if want_root else None
         ptr = lambda a: None if a is None else _Buf(a, np.float32).ptr
         o = PsOutputs(ptr(res["log_marg"]), ptr(res["root_post"]), res["best"], res["part_hyps"],
                       res["n_part_hyps"].ctypes.data_as(C.POINTER(C.c_int)),
@@ -443,14 +451,23 @@ class Context:
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,
                                    want_marg=True, is_sparse=False):
-        """log_unary [P][R][H][W] (after clip_scores_fill + computeLogGrid);
-        is_sparse = bIsSparse of the upward messages."""
+        """log_unary [P][R][H][W] or, for num_scale_steps = S, [P][S][R][H][W]
+        (after clip_scores_fill + computeLogGrid); is_sparse = bIsSparse of
+        the upward messages.  With the 5-d form the maps come back as
+        [P][S][R][H][W] / [S][H][W] and log_z as [S][P]."""
         u = _Buf(log_unary, np.float32)
-        P, R, H, W = u.arr.shape
+        multi = len(u.arr.shape) == 5
+        P, S, R, H, W = u.arr.shape if multi else (u.arr.shape[0], 1) + tuple(u.arr.shape[1:])
+        if S != max(1, exp.num_scale_steps):
+            raise ValueError("log_unary has a different number of scales than exp")
         th = _TreeHolder(tree)
-        res, o = self._outputs(P, R, H, W, exp.roi_save_num_samples, u.mem, u.arr, want_marg)
+        res, o = self._outputs(P, R, H, W, exp.roi_save_num_samples, u.mem, u.arr, want_marg,
+                               S=S if multi else 0)
         self._check(self.L.pa_ps_infer(self.h, C.byref(exp), C.byref(th.s), int(flip),
                                        int(is_sparse), u.ptr, H, W, C.byref(o), u.mem))
+        if multi:
+            res["log_z"] = res["log_z"].reshape(S, P)
+            res["msg_max"] = res["msg_max"].reshape(S, -1)
         return self._finish(res, P)
 
     def find_obj(self, exp: ExpParam, tree, cls_list, desc, Tig, H, W, flip=False,

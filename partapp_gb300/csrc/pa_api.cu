@@ -258,8 +258,10 @@ int index_from_rot(const pa_exp_param *e, double rot) {
   return index_from_value(e->min_part_rotation, e->max_part_rotation,
                           (double)(unsigned)e->num_rotation_steps, rot);
 }
+// ExpParam::num_scale_steps (ExpParam.proto:191); 0 reads as 1
+int n_scales(const pa_exp_param *e) { return e->num_scale_steps > 1 ? e->num_scale_steps : 1; }
 double scale_from_index(const pa_exp_param *e, int idx) {
-  return value_from_index(e->min_object_scale, e->max_object_scale, 1.0, idx);
+  return value_from_index(e->min_object_scale, e->max_object_scale, (double)n_scales(e), idx);
 }
 
 // rotation bin width in radians, objectdetect_findrot.cpp:319-321
@@ -323,7 +325,10 @@ bool exp_ok(const pa_exp_param *e) {
   return e && e->num_rotation_steps >= 2 && e->num_rotation_steps <= kMaxRot &&
          e->max_part_rotation > e->min_part_rotation &&
          e->strip_border_detections >= 0 && e->strip_border_detections < 0.5f &&
-         e->roi_save_num_samples >= 0 && e->roi_save_num_samples <= 2048;
+         e->roi_save_num_samples >= 0 && e->roi_save_num_samples <= 2048 &&
+         e->num_scale_steps >= 0 && e->num_scale_steps <= 64 &&
+         // value_from_index asserts one step when min == max (partapp_aux.hpp:48-52)
+         (n_scales(e) == 1 || e->max_object_scale > e->min_object_scale);
 }
 
 // ------------------------------------------------------------------------
@@ -606,6 +611,12 @@ struct PsPlan {
   };
   bool tc_mode = false;  // diagonal-covariance messages on the tensor cores (H % 8 == 0)
   bool sparse_up = false;  // bIsSparse of the upward messages
+  // multi-scale computeRootPosteriorRot: batch entry i is scale img_scale[i]
+  // (empty: every entry at scale 0)
+  std::vector<int> img_scale;
+  int64_t out_pstride = 0;  // elements between the parts of a log_marg output (0: N)
+  int hyp_img = -1;         // >= 0: part local maxima of this entry only
+  bool root_joint = false;  // root local maxima over [B][H][W] with B as the scale axis
   int wp = 0, hp = 0;
   std::vector<Phase> up, down;
   RootDesc *roots = nullptr;
@@ -639,7 +650,10 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
   const int64_t N = pl.N;
   const Sched &s = pl.sc;
-  const double scale = scale_from_index(e, 0);
+  const int64_t pstride = pl.out_pstride ? pl.out_pstride : N;
+  auto scale_of = [&](int img) {
+    return scale_from_index(e, pl.img_scale.empty() ? 0 : pl.img_scale[img]);
+  };
   pl.im.assign(B, {});
   for (int i = 0; i < B; ++i) {
     ImgMaps &m = pl.im[i];
@@ -654,7 +668,7 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
       const bool inner = (p != s.root && !s.ch[p].empty());
       m.POST[p] = inner ? b.scratch<float>(N) : m.U[p];
       m.TMP[p] = inner ? b.scratch<float>(N) : nullptr;
-      m.MARG[p] = marg_out && marg_out[i] ? marg_out[i] + (int64_t)p * N : b.scratch<float>(N);
+      m.MARG[p] = marg_out && marg_out[i] ? marg_out[i] + (int64_t)p * pstride : b.scratch<float>(N);
     }
     m.POST[s.root] = m.MARG[s.root];
     for (size_t k = 0; k < m.MSGR.size(); ++k) {
@@ -711,6 +725,7 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
     MsgParams mp;
     // upward messages take the caller's bIsSparse (objectdetect_findrot.cpp:630-635),
     // downward ones are dense (:174-179, 224-229)
+    const double scale = scale_of(mm.img);
     if (mm.up)
       msg_params(e, scale, J.oc, J.op, J.C, J.rot_mean, J.rot_sigma, H, W, pl.sparse_up, mp);
     else
@@ -928,15 +943,18 @@ void plan_localmax(Builder &b, PsPlan &pl, const pa_exp_param *e, const pa_ps_ou
   if (pl.hyp_k < 1) pl.want_part_hyps = false;
   if (!e->use_pairwise) pl.want_root_hyps = false;
   size_t sb = 0;
+  const int hyp_maps = (pl.hyp_img >= 0 ? 1 : pl.B) * pl.P;
+  const int root_maps = pl.root_joint ? 1 : pl.B;
+  const int64_t root_cells = (int64_t)(pl.root_joint ? pl.B : 1) * pl.H * pl.W;
   if (pl.want_part_hyps) {
-    sb = std::max(sb, local_max_scratch_bytes(pl.B * pl.P, pl.N, pl.hyp_k));
-    pl.part_hyps = b.scratch<float>((size_t)pl.B * pl.P * pl.hyp_k * 4);
-    pl.n_part_hyps = b.scratch<int>((size_t)pl.B * pl.P);
+    sb = std::max(sb, local_max_scratch_bytes(hyp_maps, pl.N, pl.hyp_k));
+    pl.part_hyps = b.scratch<float>((size_t)hyp_maps * pl.hyp_k * 4);
+    pl.n_part_hyps = b.scratch<int>((size_t)hyp_maps);
   }
   if (pl.want_root_hyps) {
-    sb = std::max(sb, local_max_scratch_bytes(pl.B, (int64_t)pl.H * pl.W, kRootHyps));
-    pl.root_hyps = b.scratch<float>((size_t)pl.B * kRootHyps * 4);
-    pl.n_root_hyps = b.scratch<int>((size_t)pl.B);
+    sb = std::max(sb, local_max_scratch_bytes(root_maps, root_cells, kRootHyps));
+    pl.root_hyps = b.scratch<float>((size_t)root_maps * kRootHyps * 4);
+    pl.n_root_hyps = b.scratch<int>((size_t)root_maps);
   }
   pl.lm_scratch = sb ? (void *)b.scratch<char>(sb) : nullptr;
 }
@@ -1000,15 +1018,22 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
     PA_LAUNCH("argmax", launch_argmax(pl.marg_ptrs, B * P, pl.N, pl.amax, st));
   }
   PA_LAUNCH_N("log_z", 2, launch_log_z(pl.marg_ptrs, pl.amax, B * P, pl.N, pl.logz_part, pl.logz, st));
-  if (pl.want_part_hyps)
+  if (pl.want_part_hyps) {
+    const int first = pl.hyp_img >= 0 ? pl.hyp_img * P : 0;
+    const int n_maps = pl.hyp_img >= 0 ? P : B * P;
     PA_LAUNCH_N("local_max", local_max_kernels(pl.N, pl.hyp_k),
-                launch_local_max(pl.marg_ptrs, B * P, R, H, W, pl.hyp_k, pl.lm_scratch,
+                launch_local_max(pl.marg_ptrs + first, n_maps, R, H, W, pl.hyp_k, pl.lm_scratch,
                                  pl.part_hyps, pl.n_part_hyps, st, nullptr));
-  if (pl.want_root_hyps)
-    PA_LAUNCH_N("local_max", local_max_kernels((int64_t)H * W, kRootHyps),
-                launch_local_max(reinterpret_cast<const float *const *>(pl.root_post_ptrs), B, 1,
-                                 H, W, kRootHyps, pl.lm_scratch, pl.root_hyps, pl.n_root_hyps, st,
-                                 nullptr));
+  }
+  if (pl.want_root_hyps) {
+    // one [S][H][W] grid with scale neighbours (objectdetect_aux.cpp:193-236) when
+    // the entries are the scales of one image, else one [1][H][W] grid per image
+    const int n_maps = pl.root_joint ? 1 : B, S = pl.root_joint ? B : 1;
+    PA_LAUNCH_N("local_max", local_max_kernels((int64_t)S * H * W, kRootHyps),
+                launch_local_max(reinterpret_cast<const float *const *>(pl.root_post_ptrs), n_maps,
+                                 S, H, W, kRootHyps, pl.lm_scratch, pl.root_hyps, pl.n_root_hyps,
+                                 st, nullptr));
+  }
   return PA_OK;
 }
 
@@ -1024,14 +1049,15 @@ pa_status init_slots(pa_ctx *ctx, PsPlan &pl) {
   return PA_OK;
 }
 
-void decode_hyp(const pa_exp_param *e, unsigned long long key, int H, int W, pa_part_hyp *h) {
+void decode_hyp(const pa_exp_param *e, unsigned long long key, int H, int W, pa_part_hyp *h,
+                int scaleidx) {
   const float v = ukey_decode((uint32_t)(key >> 32));
   const uint32_t flat = 0xFFFFFFFFu - (uint32_t)(key & 0xFFFFFFFFu);
   const int64_t HW = (int64_t)H * W;
   const int r = (int)(flat / HW);
   const int64_t rem = flat % HW;
-  h->scaleidx = 0.f;
-  h->scale = (float)scale_from_index(e, 0);
+  h->scaleidx = (float)scaleidx;
+  h->scale = (float)scale_from_index(e, scaleidx);
   h->rotidx = (float)r;
   h->rot = (float)rot_from_index(e, r);
   h->x = (float)(rem % W);
@@ -1053,15 +1079,17 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
   PA_CK(cudaMemcpyAsync(&errflag, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   std::vector<float> ph, rh;
   std::vector<int> nph, nrh;
+  const int hyp_maps = (pl.hyp_img >= 0 ? 1 : B) * P;
+  const int root_maps = pl.root_joint ? 1 : B;
   if (pl.want_part_hyps) {
-    ph.resize((size_t)B * P * pl.hyp_k * 4);
-    nph.resize((size_t)B * P);
+    ph.resize((size_t)hyp_maps * pl.hyp_k * 4);
+    nph.resize((size_t)hyp_maps);
     PA_CK(cudaMemcpyAsync(ph.data(), pl.part_hyps, ph.size() * 4, cudaMemcpyDeviceToHost, st));
     PA_CK(cudaMemcpyAsync(nph.data(), pl.n_part_hyps, nph.size() * 4, cudaMemcpyDeviceToHost, st));
   }
   if (pl.want_root_hyps) {
-    rh.resize((size_t)B * kRootHyps * 4);
-    nrh.resize((size_t)B);
+    rh.resize((size_t)root_maps * kRootHyps * 4);
+    nrh.resize((size_t)root_maps);
     PA_CK(cudaMemcpyAsync(rh.data(), pl.root_hyps, rh.size() * 4, cudaMemcpyDeviceToHost, st));
     PA_CK(cudaMemcpyAsync(nrh.data(), pl.n_root_hyps, nrh.size() * 4, cudaMemcpyDeviceToHost, st));
   }
@@ -1070,7 +1098,8 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
     if (mem == PA_MEM_HOST) {
       if (o.log_marg)
         for (int p = 0; p < P; ++p)
-          PA_CK(cudaMemcpyAsync(o.log_marg + (int64_t)p * pl.N, pl.im[i].MARG[p],
+          PA_CK(cudaMemcpyAsync(o.log_marg + (int64_t)p * (pl.out_pstride ? pl.out_pstride : pl.N),
+                                pl.im[i].MARG[p],
                                 pl.N * sizeof(float), cudaMemcpyDeviceToHost, st));
       if (o.root_post && e->use_pairwise)
         PA_CK(cudaMemcpyAsync(o.root_post, pl.im[i].root_post, (size_t)H * W * sizeof(float),
@@ -1083,15 +1112,18 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
   }
   for (int i = 0; i < B; ++i) {
     const pa_ps_outputs &o = outs[i];
+    const int scaleidx = pl.img_scale.empty() ? 0 : pl.img_scale[i];
+    // this entry's row in the local-maximum results (-1: none computed)
+    const int hrow = pl.hyp_img < 0 ? i : (pl.hyp_img == i ? 0 : -1);
     for (int p = 0; p < P; ++p) {
-      if (o.best) decode_hyp(e, am[(size_t)i * P + p], H, W, &o.best[p]);
+      if (o.best) decode_hyp(e, am[(size_t)i * P + p], H, W, &o.best[p], scaleidx);
       if (o.log_z) o.log_z[p] = lz[(size_t)i * P + p];
-      const int n = pl.want_part_hyps ? nph[(size_t)i * P + p] : 0;
+      const int n = pl.want_part_hyps && hrow >= 0 ? nph[(size_t)hrow * P + p] : 0;
       if (o.n_part_hyps) o.n_part_hyps[p] = n;
       if (o.part_hyps)
         for (int k = 0; k < n; ++k) {
           // PartHyp(exp_param, 0, rotidx, x, y, score).toVect(), objectdetect.h:95-159
-          const float *r = &ph[(((size_t)i * P + p) * pl.hyp_k + k) * 4];
+          const float *r = &ph[(((size_t)hrow * P + p) * pl.hyp_k + k) * 4];
           pa_part_hyp &h = o.part_hyps[(size_t)p * pl.hyp_k + k];
           h.scaleidx = 0.f;
           h.scale = (float)scale_from_index(e, 0);
@@ -1104,12 +1136,13 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
     }
     if (o.msg_max)
       for (int k = 0; k < 2 * (P - 1); ++k) o.msg_max[k] = mm[(size_t)i * 2 * (P - 1) + k];
-    const int nr = pl.want_root_hyps ? nrh[i] : 0;
+    const int rrow = pl.root_joint ? (i == 0 ? 0 : -1) : i;
+    const int nr = pl.want_root_hyps && rrow >= 0 ? nrh[rrow] : 0;
     if (o.n_root_hyps) *o.n_root_hyps = nr;
     if (o.root_hyps)
       for (int k = 0; k < nr; ++k) {
         // ObjectHypothesis (scale, x, y, score), objectdetect_aux.cpp:279-290
-        const float *r = &rh[((size_t)i * kRootHyps + k) * 4];
+        const float *r = &rh[((size_t)rrow * kRootHyps + k) * 4];
         o.root_hyps[4 * k + 0] = (float)scale_from_index(e, (int)r[0]);
         o.root_hyps[4 * k + 1] = r[1];
         o.root_hyps[4 * k + 2] = r[2];
@@ -1480,6 +1513,9 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
                         int ny, int nx, int dim, const double *Tig, int tig_shared, int H, int W,
                         float *scores_out, const pa_ps_outputs *outs, int mem) {
   if (!exp_ok(e)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (n_scales(e) != 1)
+    return fail(ctx, PA_ERR_UNSUPPORTED,
+                "the descriptors are one scale; run pa_ps_infer on per-scale unaries");
   if (n_img < 1 || !trees || !desc || !Tig || !outs || ny < 1 || nx < 1 || dim < 1 || H < 1 ||
       W < 1 || H > 32767 || W > 32767)
     return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
@@ -1522,6 +1558,7 @@ void pa_exp_param_default(pa_exp_param *p) {
   p->roi_save_num_samples = 1000;
   p->use_pairwise = 1;
   p->interpolate = 0;
+  p->num_scale_steps = 1;
 }
 
 pa_status pa_ctx_create(int device, pa_ctx **out) {
@@ -1924,28 +1961,63 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
   pl.sparse_up = is_sparse != 0;
   pa_status st = build_sched(ctx, tree, pl.sc);
   if (st) return st;
-  std::vector<std::vector<Joint>> joints(1);
+  // computeRootPosteriorRot runs one independent pass per scale
+  // (objectdetect_findrot.cpp:503-678): the scales are the entries of a batch
+  const int S = n_scales(ep);
+  std::vector<std::vector<Joint>> joints(S);
   if ((st = load_joints(ctx, tree, flip, joints[0]))) return st;
+  for (int sc = 1; sc < S; ++sc) joints[sc] = joints[0];
   const int P = pl.sc.P, R = ep->num_rotation_steps;
-  pl.B = 1;
+  pl.B = S;
   pl.P = P;
   pl.R = R;
   pl.H = H;
   pl.W = W;
   pl.N = (int64_t)R * H * W;
+  const int64_t HW = (int64_t)H * W;
+  // best_part_hyp holds the last scale's maxima (computePartMarginals clears it
+  // per scale, :254-258); getMaxStates reads scale 0 (:78)
+  const int hyp_scale = ep->use_pairwise ? S - 1 : 0;
+  if (S > 1) {
+    for (int sc = 0; sc < S; ++sc) pl.img_scale.push_back(sc);
+    pl.out_pstride = (int64_t)S * pl.N;
+    pl.hyp_img = hyp_scale;
+    pl.root_joint = true;
+  }
+  std::vector<pa_ps_outputs> outs(S);
+  for (int sc = 0; sc < S; ++sc) {
+    pa_ps_outputs &o = outs[sc];
+    o = *out;
+    if (S == 1) break;
+    o.log_marg = out->log_marg ? out->log_marg + sc * pl.N : nullptr;
+    o.root_post = out->root_post ? out->root_post + sc * HW : nullptr;
+    o.log_z = out->log_z ? out->log_z + (size_t)sc * P : nullptr;
+    o.msg_max = out->msg_max ? out->msg_max + (size_t)sc * 2 * std::max(1, P - 1) : nullptr;
+    if (sc != hyp_scale) o.best = nullptr, o.part_hyps = nullptr, o.n_part_hyps = nullptr;
+    if (sc != 0) o.root_hyps = nullptr, o.n_root_hyps = nullptr;
+  }
   DeviceGuard dg(ctx->device);
-  float *marg_out = (mem == PA_MEM_DEVICE) ? out->log_marg : nullptr;
-  float *rp_out = (mem == PA_MEM_DEVICE) ? out->root_post : nullptr;
+  std::vector<float *> marg_out(S, nullptr), rp_out(S, nullptr);
+  if (mem == PA_MEM_DEVICE)
+    for (int sc = 0; sc < S; ++sc) {
+      marg_out[sc] = outs[sc].log_marg;
+      rp_out[sc] = outs[sc].root_post;
+    }
   std::vector<int> masked((size_t)P * R, 0);
   for (int p = 0; p < P; ++p)
     if (pl.sc.upright[p])
       for (int r = 0; r < R; ++r) masked[(size_t)p * R + r] = !(std::fabs(rot_from_index(ep, r)) < 15.0);
   auto plan = [&](Builder &b, PsPlan &p2, int **masked_dev, const float **unary_dev) {
     *masked_dev = b.param(masked.data(), masked.size());
-    *unary_dev = (mem == PA_MEM_HOST) ? b.scratch<float>((size_t)P * pl.N) : log_unary;
-    plan_ps(b, p2, ep, joints, &marg_out, &rp_out);
+    *unary_dev = (mem == PA_MEM_HOST) ? b.scratch<float>((size_t)P * S * pl.N) : log_unary;
+    std::vector<float *> rp = rp_out;
+    if (S > 1 && !rp[0]) {  // the scales' root posteriors form one [S][H][W] grid
+      float *g = b.scratch<float>((size_t)S * HW);
+      for (int sc = 0; sc < S; ++sc) rp[sc] = g + sc * HW;
+    }
+    plan_ps(b, p2, ep, joints, marg_out.data(), rp.data());
     plan_marg_ptrs(b, p2);
-    plan_localmax(b, p2, ep, out);
+    plan_localmax(b, p2, ep, outs.data());
   };
   Builder b1;
   PsPlan pl1 = pl;
@@ -1961,17 +2033,22 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
   plan(b, pl2, &mk, &ud);
   if ((st = upload_blob(ctx, b))) return st;
   if (mem == PA_MEM_HOST)
-    if ((st = copy_in(ctx, (void *)ud, log_unary, (size_t)P * pl.N * sizeof(float), mem))) return st;
+    if ((st = copy_in(ctx, (void *)ud, log_unary, (size_t)P * S * pl.N * sizeof(float), mem)))
+      return st;
   if ((st = init_slots(ctx, pl2))) return st;
   cudaStream_t s = ctx->stream;
   const int strip = (int)(ep->strip_border_detections * W);
-  for (int p = 0; p < P; ++p) {
-    float *dst = ep->use_pairwise ? pl2.im[0].U[p] : pl2.im[0].MARG[p];
-    PA_LAUNCH("prepare_unary", launch_prepare_unary(ud + (size_t)p * pl.N, dst, pl2.sc.upright[p] ? mk + (size_t)p * R : nullptr,
-                                   p == pl2.sc.root ? strip : 0, R, H, W, pl2.umax + p, s));
-  }
+  for (int sc = 0; sc < S; ++sc)
+    for (int p = 0; p < P; ++p) {
+      float *dst = ep->use_pairwise ? pl2.im[sc].U[p] : pl2.im[sc].MARG[p];
+      PA_LAUNCH("prepare_unary",
+                launch_prepare_unary(ud + ((size_t)p * S + sc) * pl.N, dst,
+                                     pl2.sc.upright[p] ? mk + (size_t)p * R : nullptr,
+                                     p == pl2.sc.root ? strip : 0, R, H, W,
+                                     pl2.umax + (size_t)sc * P + p, s));
+    }
   if ((st = run_ps(ctx, ep, pl2))) return st;
-  return finish_ps(ctx, ep, pl2, out, mem);
+  return finish_ps(ctx, ep, pl2, outs.data(), mem);
 }
 
 pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float *child,
@@ -2133,6 +2210,8 @@ pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
     if (!im.ep || !exp_ok(im.ep) || !im.tree || !im.desc || !im.Tig || !im.out || im.ny < 1 ||
         im.nx < 1 || im.dim < 1 || im.H < 1 || im.W < 1 || im.H > 32767 || im.W > 32767)
       return fail(ctx, PA_ERR_INVALID, "image %d: invalid sizes, parameters or NULL input", i);
+    if (n_scales(im.ep) != 1)
+      return fail(ctx, PA_ERR_UNSUPPORTED, "image %d: one scale of descriptors per image", i);
   }
   // images that share every size, parameter and transform run as one batch
   auto same = [&](const pa_image &a, const pa_image &b) {

@@ -67,8 +67,8 @@ struct ImageOut {
   std::vector<double> log_z;
   pa_ps_outputs o{};
 
-  ImageOut(int P, int K) : best(P), part_hyps((size_t)P * K), n_part_hyps(P), root_hyps(1000 * 4),
-                           log_z(P) {
+  ImageOut(int P, int K, int S = 1)
+      : best(P), part_hyps((size_t)P * K), n_part_hyps(P), root_hyps(1000 * 4), log_z((size_t)S * P) {
     o.best = best.data();
     o.part_hyps = part_hyps.data();
     o.n_part_hyps = n_part_hyps.data();
@@ -104,6 +104,7 @@ pa_exp_param ExpParam::c() const {
   e.roi_save_num_samples = roi_save_num_samples;
   e.use_pairwise = use_pairwise ? 1 : 0;
   e.interpolate = interpolate ? 1 : 0;
+  e.num_scale_steps = num_scale_steps;
   return e;
 }
 
@@ -182,35 +183,45 @@ void computeRootPosteriorRot(Context &ctx, const PartApp &part_app,
   const int P = (int)log_part_detections.size();
   require(P == part_app.m_part_conf.part_size(), "one detection stack per part");
   require(P > 0 && !log_part_detections[0].empty(), "empty detections");
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int S = (int)log_part_detections[0].size();
+  require(S == std::max(1, e.num_scale_steps), "one map per scale (num_scale_steps)");
   const size_t *s = log_part_detections[0][0].shape();
   const int R = (int)s[0], H = (int)s[1], W = (int)s[2];
   const size_t N = (size_t)R * H * W;
-  std::vector<float> unary((size_t)P * N);
-  for (int p = 0; p < P; ++p) {
-    require(!log_part_detections[p].empty() && log_part_detections[p][0].num_elements() == N,
-            "all parts need [R][H][W] maps of one size (one scale)");
-    std::memcpy(unary.data() + (size_t)p * N, log_part_detections[p][0].data(), N * sizeof(float));
-  }
+  std::vector<float> unary((size_t)P * S * N);  // [part][scale][R][H][W]
+  for (int p = 0; p < P; ++p)
+    for (int sc = 0; sc < S; ++sc) {
+      require((int)log_part_detections[p].size() == S &&
+                  log_part_detections[p][sc].num_elements() == N,
+              "all parts need [R][H][W] maps of one size at every scale");
+      std::memcpy(unary.data() + ((size_t)p * S + sc) * N, log_part_detections[p][sc].data(),
+                  N * sizeof(float));
+    }
   const TreeHolder th(part_app.m_part_conf, rootpart_idx, joints);
-  const pa_exp_param e = part_app.m_exp_param.c();
   const int K = e.roi_save_num_samples;
-  ImageOut out(P, K > 0 ? K : 1);
-  root_part_posterior = FloatGrid3(1, H, W);
+  ImageOut out(P, K > 0 ? K : 1, S);
+  root_part_posterior = FloatGrid3(S, H, W);  // [nScales][H][W], :718
   out.o.root_post = root_part_posterior.data();
   std::vector<float> marg;
   if (log_marginals) {
-    marg.resize((size_t)P * N);
+    marg.resize((size_t)P * S * N);
     out.o.log_marg = marg.data();
   }
   ctx.check(pa_ps_infer(ctx.get(), &e, &th.t, 0, bIsSparse ? 1 : 0, unary.data(), H, W, &out.o,
                         PA_MEM_HOST));
   const FindObjResult r = out.result(P, K > 0 ? K : 1);
-  best_part_hyp = r.part_hyps;
+  // best_part_hyp[p] = the argmax, then the local maxima (objectdetect_findrot.cpp:276-283)
+  best_part_hyp.assign(P, {});
+  for (int p = 0; p < P; ++p) {
+    best_part_hyp[p].push_back(r.best_conf[p]);
+    best_part_hyp[p].insert(best_part_hyp[p].end(), r.part_hyps[p].begin(), r.part_hyps[p].end());
+  }
   if (log_marginals) {
     log_marginals->clear();
-    for (int p = 0; p < P; ++p) {
+    for (size_t k = 0; k < (size_t)P * S; ++k) {
       FloatGrid3 g(R, H, W);
-      std::memcpy(g.data(), marg.data() + (size_t)p * N, N * sizeof(float));
+      std::memcpy(g.data(), marg.data() + k * N, N * sizeof(float));
       log_marginals->push_back(std::move(g));
     }
   }

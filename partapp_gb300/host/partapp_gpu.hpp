@@ -57,6 +57,7 @@ struct ExpParam {
   int roi_save_num_samples = 1000;
   bool use_pairwise = true;
   bool interpolate = false;
+  int num_scale_steps = 1;  // > 1 only for computeRootPosteriorRot (per-scale unaries)
   pa_exp_param c() const;
 };
 
@@ -138,11 +139,13 @@ void computeRotJointMarginal(Context &ctx, const ExpParam &exp_param, FloatGrid3
                              double rot_sigma, double scale, bool bIsSparse);
 
 // computeRootPosteriorRot (objectdetect_findrot.cpp:470-727) including
-// computePartMarginals and findLocalMax.  log_part_detections[part][0] are
-// the log unaries (after clip_scores_fill + computeLogGrid); they are not
-// modified.  best_part_hyp[part] receives the local maxima of the part's
-// marginal (best first when more than roi_save_num_samples); if
-// log_marginals is given it receives the final log marginals per part.
+// computePartMarginals and findLocalMax.  log_part_detections[part][scale]
+// are the log unaries (after clip_scores_fill + computeLogGrid); they are
+// not modified.  best_part_hyp[part] receives the argmax of the part's
+// marginal followed by its local maxima, of the last scale as in the
+// reference; root_part_posterior is [nScales][H][W].  If log_marginals is
+// given it receives the final log marginals in [part][scale] order
+// (index part * nScales + scale); log_z is [scale][part].
 void computeRootPosteriorRot(Context &ctx, const PartApp &part_app,
                              std::vector<std::vector<FloatGrid3>> &log_part_detections,
                              FloatGrid3 &root_part_posterior, int rootpart_idx,

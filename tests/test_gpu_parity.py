@@ -439,6 +439,73 @@ def test_config0_full_size_one_image(ctx, orc):
     compare_ps(got, want, oracle64(orc, e, img["tree"], want["log_unary"]))
 
 
+# ------------------------------------------------------------ multi-scale
+@pytest.mark.parametrize("mem", ["host", "device"])
+def test_ps_multi_scale(ctx, orc, mem):
+    """num_scale_steps = 3: one pass per scale at scale_from_index(s)
+    (objectdetect_findrot.cpp:503-678); maps [P][S][R][H][W], root posterior
+    [S][H][W], argmax and part maxima of the last scale, root maxima over the
+    scale stack."""
+    import torch
+
+    rng = np.random.default_rng(91)
+    R, H, W, S = 12, 40, 56, 3
+    tree = small_tree(rng, R)
+    u = synth.random_log_unary(rng, 10 * S, R, H, W).reshape(10, S, R, H, W)
+    kw = dict(n_scales=S, scale_range=(0.5, 2.0))
+    e = orc.make_exp(R=R, max_local_max=200, **kw)
+    want = orc.ps_infer(e, tree, u)
+    pe = _pa_exp(R, local_max=200, **kw)
+    uin = torch.from_numpy(u).cuda() if mem == "device" else u
+    got = ctx.compute_root_posterior_rot(pe, tree, uin)
+    if mem == "device":
+        got["log_marg"] = got["log_marg"].cpu().numpy()
+        got["root_post"] = got["root_post"].cpu().numpy()
+    assert got["log_marg"].shape == (10, S, R, H, W) and got["root_post"].shape == (S, H, W)
+    want64 = orc.ps_infer(e, tree, u.astype(np.float64), f64=True, want_hyps=False)
+    for s in range(S):
+        last = dict(log_marg=want["log_marg"][:, s], best_conf=want["best_conf"])
+        g = dict(log_marg=got["log_marg"][:, s], best_conf=got["best_conf"])
+        compare_ps(g, last, dict(log_marg=want64["log_marg"][:, s]), check_argmax=(s == S - 1))
+        assert maxnorm_err(got["root_post"][s], want["root_post"][s]) <= TOL_F32
+    assert (got["best_conf"][:, 0] == S - 1).all()
+    assert np.array_equal(got["best_conf"][:, 1], want["best_conf"][:, 1])
+    assert got["log_z"].shape == (S, 10)
+    for p in range(10):
+        g = {tuple(r) for r in got["part_hyps"][p, :20, 2:6:1][:, [0, 2, 3]].tolist()}
+        w = {tuple(r) for r in want["part_hyps"][p, :20, 2:6:1][:, [0, 2, 3]].tolist()}
+        assert len(g & w) >= 18, p
+    assert (got["part_hyps"][:, :, 0] == 0).all()
+    assert abs(int(got["n_root_hyps"][0]) - want["n_root_hyps"]) <= 2
+    g = {tuple(r) for r in got["root_hyps"][:20, 0:3].tolist()}
+    w = {tuple(r) for r in want["root_hyps"][:20, 0:3].tolist()}
+    assert len(g & w) >= 18
+    # maxima on every scale, in the oracle's proportions
+    ng, nw = int(got["n_root_hyps"][0]), want["n_root_hyps"]
+    hg = np.unique(got["root_hyps"][:ng, 0], return_counts=True)
+    hw = np.unique(want["root_hyps"][:nw, 0], return_counts=True)
+    assert len(hw[0]) == S and np.array_equal(hg[0], hw[0])
+    assert np.abs(hg[1] - hw[1]).max() <= 2
+
+
+def test_ps_multi_scale_without_pairwise(ctx, orc):
+    """use_pairwise off: getMaxStates reads scale 0 only (:73-110)."""
+    rng = np.random.default_rng(92)
+    R, H, W, S = 6, 30, 40, 2
+    tree = small_tree(rng, R)
+    u = np.floor(rng.uniform(0, 6, (10, S, R, H, W))).astype(np.float32) - 3.0
+    kw = dict(n_scales=S, scale_range=(0.5, 1.5))
+    want = orc.ps_infer(orc.make_exp(R=R, use_pairwise=False, max_local_max=60, **kw), tree, u)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R, use_pairwise=False, local_max=60, **kw),
+                                         tree, u)
+    assert np.array_equal(got["log_marg"], want["log_marg"])
+    assert np.array_equal(got["best_conf"], want["best_conf"])
+    assert np.array_equal(got["n_part_hyps"], want["n_part_hyps"])
+    for p in range(10):
+        n = int(want["n_part_hyps"][p])
+        assert np.array_equal(got["part_hyps"][p, :n], want["part_hyps"][p, :n]), p
+
+
 # ----------------------------------------------------------- local maxima
 @pytest.mark.parametrize("K,levels", [(50, 9), (1000, 2)])
 def test_local_max_exact_on_unaries(ctx, orc, K, levels):
@@ -511,6 +578,17 @@ def test_errors_are_statuses(ctx, pa):
     with pytest.raises(pa.PaError) as ei:
         ctx.compute_root_posterior_rot(_pa_exp(1), tree, u[:, :1])
     assert ei.value.status == pa.PA_ERR_INVALID
+    # several scales with min == max: value_from_index asserts (partapp_aux.hpp:48-52)
+    with pytest.raises(pa.PaError) as ei:
+        ctx.compute_root_posterior_rot(_pa_exp(R, n_scales=2), tree, np.stack([u, u], axis=1))
+    assert ei.value.status == pa.PA_ERR_INVALID
+    # the --find_obj entries score one scale of descriptors
+    img = synth.make_image(3, R=R, H=32, W=48, n_stumps=20, D=32)
+    cls = ctx.classifiers(img["models"])
+    with pytest.raises(pa.PaError) as ei:
+        ctx.find_obj(_pa_exp(R, n_scales=2, scale_range=(0.5, 1.5)), img["tree"], cls,
+                     img["desc"], img["Tig"], 32, 48)
+    assert ei.value.status == pa.PA_ERR_UNSUPPORTED
 
 
 # ------------------------------------------------------- uneven batches

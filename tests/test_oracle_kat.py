@@ -289,3 +289,47 @@ def test_full_covariance_near_diagonal_matches_diagonal(orc):
     assert np.array_equal(live, b > -1e5)
     assert np.max(np.abs(a[live] - b[live])) <= 1e-5
     assert np.all(full[:, H - 1, :] == LOG_ZERO) and np.all(full[:, :, W - 1] == LOG_ZERO)
+
+
+def test_multi_scale_is_independent_passes(orc):
+    """computeRootPosteriorRot over num_scale_steps = 3 (objectdetect_findrot.cpp:
+    503-678): every scale is a pass with the joints at scale_from_index(s) =
+    min + (max - min)/S * (s + 0.5) (partapp_aux.hpp:54-66); best_conf and the
+    part maxima are the last scale's, with scaleidx S - 1 on the argmax and 0
+    on the local maxima (:276-283, objectdetect_aux.cpp:300-304); the root
+    maxima come from the stacked [S][H][W] posterior with scale neighbours."""
+    from partapp_gb300 import synth
+
+    rng = np.random.default_rng(77)
+    R, H, W, S = 8, 24, 30, 3
+    tree = synth.make_tree(rng, R=R, offset_range=(2.0, 6.0), sigma_range=(1.0, 2.0))
+    u = synth.random_log_unary(rng, 10 * S, R, H, W).reshape(10, S, R, H, W)
+    lo, hi = 0.5, 2.0  # scales 0.75, 1.25, 1.75: exact in float and double
+    multi = orc.ps_infer(orc.make_exp(R=R, n_scales=S, scale_range=(lo, hi), max_local_max=50),
+                         tree, u)
+    roots = []
+    for s in range(S):
+        sc = lo + (hi - lo) / S * (s + 0.5)
+        one = orc.ps_infer(orc.make_exp(R=R, scale=sc, max_local_max=50), tree, u[:, s])
+        assert np.array_equal(multi["log_marg"][:, s], one["log_marg"]), s
+        assert np.array_equal(multi["root_post"][s], one["root_post"]), s
+        roots.append(one["root_post"])
+        if s == S - 1:
+            assert np.array_equal(multi["best_conf"][:, [2, 3, 4, 5, 6]],
+                                  one["best_conf"][:, [2, 3, 4, 5, 6]])
+            assert (multi["best_conf"][:, 0] == S - 1).all()
+            assert np.allclose(multi["best_conf"][:, 1], np.float32(sc))
+            assert np.array_equal(multi["n_part_hyps"], one["n_part_hyps"])
+            assert (multi["part_hyps"][:, :, 0] == 0).all()
+    lm = orc.find_local_max(np.stack(roots), 1000)
+    n = multi["n_root_hyps"]
+    assert n == len(lm) and n > 0
+    scales = (lo + (hi - lo) / S * (lm[:, 0] + 0.5)).astype(np.float32)
+    assert np.array_equal(multi["root_hyps"][:n, 0], scales)
+    assert np.array_equal(multi["root_hyps"][:n, 1:], lm[:, 1:].astype(np.float32))
+    # a maximum must beat both scale neighbours (objectdetect_aux.cpp:223-229)
+    stack = np.stack(roots)
+    for s, x, y in lm[:, :3].astype(int):
+        for t in (s - 1, s + 1):
+            if 0 <= t < S:
+                assert stack[t, y, x] < stack[s, y, x]
