@@ -503,8 +503,8 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
     if (tid == 0) atomicOr(err, 4);
     return;
   }
-  float *S = sm;                                          // [srows][kCW]
-  float *F = S + align4((band + 2 + 2 * pady) * kCW);     // [nrows][kCW]
+  float *S = sm;                                          // [srows + kNO + kU][kCW]
+  float *F = S + align4((band + 2 + 2 * pady + kNO + kU) * kCW);  // [nrows][kCW]
   float *ty = F + align4((band + 2) * kCW);               // y taps padded, 16B aligned
   const int ypad = ((md.ylen + kU - 1) / kU) * kU;
   for (int i = tid; i < ypad; i += blockDim.x) ty[i] = i < md.ylen ? md.ytaps[i] : 0.f;
@@ -513,13 +513,17 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
   const float *e2 = md.e2 + (int64_t)r * HW;
   if (any) {
     // stage E2 rows [rmin - ky, rmax + ky] x columns [cmin, cmin + kCW), zero
-    // outside, by asynchronous copies (all in flight at once)
-    const int n = srows * kCW;
-    for (int i = tid; i < n; i += blockDim.x) {
-      const int sr = i / kCW, c = i - sr * kCW;
-      const int yy = rmin - ky + sr, xx = cmin + c;
-      const bool ok = yy >= 0 && yy < H && xx < W && xx <= cmax;
-      cp_async4(S + i, ok ? e2 + (int64_t)yy * W + xx : e2, ok);
+    // outside, by asynchronous copies (all in flight at once); kNO + kU zero
+    // rows follow, so the y pass reads its unrolled tail without bounds tests
+    const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    for (int sr = warp; sr < srows + kNO + kU; sr += nwarps) {
+      const int yy = rmin - ky + sr;
+      const bool rowok = sr < srows && yy >= 0 && yy < H;
+      const float *g = e2 + (int64_t)(rowok ? yy : 0) * W + cmin;
+      for (int c = lane; c < kCW; c += 32) {
+        const bool ok = rowok && cmin + c < W && cmin + c <= cmax;
+        cp_async4(S + sr * kCW + c, ok ? g + c : e2, ok);
+      }
     }
     cp_async_wait_all();
   }
@@ -543,10 +547,7 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
         for (int kb = 0; kb < ypad; kb += kU) {
           float v[kNO + kU - 1];
 #pragma unroll
-          for (int i = 0; i < kNO + kU - 1; ++i) {
-            const int sr = rr0 + kb + i;
-            v[i] = sr < srows ? col[sr * kCW] : 0.f;
-          }
+          for (int i = 0; i < kNO + kU - 1; ++i) v[i] = col[(rr0 + kb + i) * kCW];
           const float4 ta = *reinterpret_cast<const float4 *>(ty + kb);
           const float4 tb = *reinterpret_cast<const float4 *>(ty + kb + 4);
           const float t[kU] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
@@ -947,13 +948,14 @@ cudaError_t launch_msg_full(const MsgDesc *msgs, int n_msgs, int R, int H, int W
 
 cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int pady,
                             int *err, cudaStream_t s) {
-  // Row band: the whole column when it fits, else bands of 256 rows.
+  // Row band: the whole column when it fits, else halved until it does.
   int band = H;
   auto smem_for = [&](int b) {
-    return ((size_t)align4((b + 2 + 2 * pady) * kCW) + (size_t)align4((b + 2) * kCW) +
+    return ((size_t)align4((b + 2 + 2 * pady + kNO + kU) * kCW) + (size_t)align4((b + 2) * kCW) +
             ((2 * pady + 1 + kU - 1) / kU) * kU) * sizeof(float);
   };
-  while (smem_for(band) > 100 * 1024 && band > 32) band = (band + 1) / 2;
+  // bands of at most ~56 KB: four CTAs per SM hide the staging and epilogue latency
+  while (smem_for(band) > 56 * 1024 && band > 32) band = (band + 1) / 2;
   const size_t smem = smem_for(band);
   if (smem > 227 * 1024) return cudaErrorInvalidValue;
   cudaFuncSetAttribute(k_msg_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -42,8 +42,25 @@ struct pa_ctx {
   uint64_t launches = 0;
   char *arena = nullptr;
   size_t arena_cap = 0;
-  char *pinned = nullptr;
-  size_t pinned_cap = 0;
+  // pinned staging of plan blobs, used round-robin: a buffer is rewritten
+  // only after the upload kernel that last read it has run, so a call can
+  // plan the next image while the GPU still works on the previous one
+  struct Staging {
+    char *p = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+  };
+  static constexpr int kStages = 4;
+  Staging stage[kStages];
+  int stage_next = 0;
+  // pinned landing blocks of the small per-image results (one per ring slot)
+  struct Landing {
+    char *p = nullptr;
+    size_t cap = 0;
+  };
+  static constexpr int kLandings = 3;
+  Landing land[kLandings];
+  std::vector<cudaEvent_t> ring_done;  // per ring slot: the slot's image is computed
   // host-input ring: descriptor slots filled on copy_stream while the main
   // stream computes on the previous slot
   cudaStream_t copy_stream = nullptr;
@@ -208,24 +225,27 @@ pa_status upload_blob(pa_ctx *ctx, const Builder &b) {
       b.blob_region() + Builder::al(b.scratch_off, 256) > ctx->arena_cap)
     return fail(ctx, PA_ERR_INVALID, "internal: plan does not fit the workspace");
   if (b.blob.empty()) return PA_OK;
-  if (ctx->pinned_cap < b.blob.size()) {
-    PA_CK(cudaStreamSynchronize(ctx->stream));
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
-    ctx->pinned = nullptr;
-    ctx->pinned_cap = 0;
+  pa_ctx::Staging &sg = ctx->stage[ctx->stage_next];
+  ctx->stage_next = (ctx->stage_next + 1) % pa_ctx::kStages;
+  if (sg.done) PA_CK(cudaEventSynchronize(sg.done));  // its previous upload has been read
+  else PA_CK(cudaEventCreateWithFlags(&sg.done, cudaEventDisableTiming));
+  if (sg.cap < b.blob.size()) {
+    if (sg.p) cudaFreeHost(sg.p);
+    sg.p = nullptr;
+    sg.cap = 0;
     const size_t cap = b.blob.size() + b.blob.size() / 4 + 4096;
-    if (cudaMallocHost(&ctx->pinned, cap) != cudaSuccess) {
+    if (cudaMallocHost(&sg.p, cap) != cudaSuccess) {
       cudaGetLastError();
       return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes of pinned staging", cap);
     }
-    ctx->pinned_cap = cap;
+    sg.cap = cap;
   }
-  PA_CK(cudaStreamSynchronize(ctx->stream));  // staging buffer is reused
-  std::memcpy(ctx->pinned, b.blob.data(), b.blob.size());
+  std::memcpy(sg.p, b.blob.data(), b.blob.size());
   // a kernel reads the pinned staging buffer directly: the parameters do not
   // queue behind large host->device copies on the copy engines
-  PA_LAUNCH("upload", launch_copy16(ctx->pinned, ctx->arena, (int64_t)((b.blob.size() + 15) / 16),
+  PA_LAUNCH("upload", launch_copy16(sg.p, ctx->arena, (int64_t)((b.blob.size() + 15) / 16),
                                     ctx->stream));
+  PA_CK(cudaEventRecord(sg.done, ctx->stream));
   return PA_OK;
 }
 
@@ -1065,65 +1085,99 @@ void decode_hyp(const pa_exp_param *e, unsigned long long key, int H, int W, pa_
   h->score = v;
 }
 
-// Reads back the small per-image results and writes host outputs.
-pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_outputs *outs,
-                    int mem) {
+// Host landing place of the small per-call results (inside a pinned block).
+struct Readback {
+  unsigned long long *am = nullptr;
+  double *lz = nullptr, *mm = nullptr;
+  int *err = nullptr, *nph = nullptr, *nrh = nullptr;
+  float *ph = nullptr, *rh = nullptr;
+};
+
+// Queues the device->host copies of a finished plan's results: the small
+// ones into landing block `slot`, the maps into the caller's host outputs.
+pa_status finish_enqueue(pa_ctx *ctx, const pa_exp_param *e, const PsPlan &pl,
+                         const pa_ps_outputs *outs, int mem, int slot, Readback &rb) {
   const int B = pl.B, P = pl.P, H = pl.H, W = pl.W;
-  std::vector<unsigned long long> am((size_t)B * P);
-  std::vector<double> lz((size_t)B * P), mm((size_t)B * 2 * std::max(1, P - 1));
-  int errflag = 0;
-  cudaStream_t st = ctx->stream;
-  PA_CK(cudaMemcpyAsync(am.data(), pl.amax, am.size() * 8, cudaMemcpyDeviceToHost, st));
-  PA_CK(cudaMemcpyAsync(lz.data(), pl.logz, lz.size() * 8, cudaMemcpyDeviceToHost, st));
-  PA_CK(cudaMemcpyAsync(mm.data(), pl.msgmax, mm.size() * 8, cudaMemcpyDeviceToHost, st));
-  PA_CK(cudaMemcpyAsync(&errflag, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-  std::vector<float> ph, rh;
-  std::vector<int> nph, nrh;
   const int hyp_maps = (pl.hyp_img >= 0 ? 1 : B) * P;
   const int root_maps = pl.root_joint ? 1 : B;
+  const size_t n_am = (size_t)B * P, n_mm = (size_t)B * 2 * std::max(1, P - 1);
+  const size_t n_ph = pl.want_part_hyps ? (size_t)hyp_maps * pl.hyp_k * 4 : 0;
+  const size_t n_rh = pl.want_root_hyps ? (size_t)root_maps * kRootHyps * 4 : 0;
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 15) / 16 * 16;
+    return o;
+  };
+  const size_t o_am = carve(n_am * 8), o_lz = carve(n_am * 8), o_mm = carve(n_mm * 8),
+               o_err = carve(4), o_nph = carve((size_t)hyp_maps * 4), o_nrh = carve((size_t)root_maps * 4),
+               o_ph = carve(n_ph * 4), o_rh = carve(n_rh * 4);
+  pa_ctx::Landing &ld = ctx->land[slot];
+  if (ld.cap < off) {  // the slot's previous results were consumed before this call
+    if (ld.p) cudaFreeHost(ld.p);
+    ld.p = nullptr;
+    ld.cap = 0;
+    if (cudaMallocHost(&ld.p, off) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes of pinned result staging", off);
+    }
+    ld.cap = off;
+  }
+  rb.am = reinterpret_cast<unsigned long long *>(ld.p + o_am);
+  rb.lz = reinterpret_cast<double *>(ld.p + o_lz);
+  rb.mm = reinterpret_cast<double *>(ld.p + o_mm);
+  rb.err = reinterpret_cast<int *>(ld.p + o_err);
+  rb.nph = reinterpret_cast<int *>(ld.p + o_nph);
+  rb.nrh = reinterpret_cast<int *>(ld.p + o_nrh);
+  rb.ph = reinterpret_cast<float *>(ld.p + o_ph);
+  rb.rh = reinterpret_cast<float *>(ld.p + o_rh);
+  cudaStream_t st = ctx->stream;
+  PA_CK(cudaMemcpyAsync(rb.am, pl.amax, n_am * 8, cudaMemcpyDeviceToHost, st));
+  PA_CK(cudaMemcpyAsync(rb.lz, pl.logz, n_am * 8, cudaMemcpyDeviceToHost, st));
+  PA_CK(cudaMemcpyAsync(rb.mm, pl.msgmax, n_mm * 8, cudaMemcpyDeviceToHost, st));
+  PA_CK(cudaMemcpyAsync(rb.err, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (pl.want_part_hyps) {
-    ph.resize((size_t)hyp_maps * pl.hyp_k * 4);
-    nph.resize((size_t)hyp_maps);
-    PA_CK(cudaMemcpyAsync(ph.data(), pl.part_hyps, ph.size() * 4, cudaMemcpyDeviceToHost, st));
-    PA_CK(cudaMemcpyAsync(nph.data(), pl.n_part_hyps, nph.size() * 4, cudaMemcpyDeviceToHost, st));
+    PA_CK(cudaMemcpyAsync(rb.ph, pl.part_hyps, n_ph * 4, cudaMemcpyDeviceToHost, st));
+    PA_CK(cudaMemcpyAsync(rb.nph, pl.n_part_hyps, (size_t)hyp_maps * 4, cudaMemcpyDeviceToHost, st));
   }
   if (pl.want_root_hyps) {
-    rh.resize((size_t)root_maps * kRootHyps * 4);
-    nrh.resize((size_t)root_maps);
-    PA_CK(cudaMemcpyAsync(rh.data(), pl.root_hyps, rh.size() * 4, cudaMemcpyDeviceToHost, st));
-    PA_CK(cudaMemcpyAsync(nrh.data(), pl.n_root_hyps, nrh.size() * 4, cudaMemcpyDeviceToHost, st));
+    PA_CK(cudaMemcpyAsync(rb.rh, pl.root_hyps, n_rh * 4, cudaMemcpyDeviceToHost, st));
+    PA_CK(cudaMemcpyAsync(rb.nrh, pl.n_root_hyps, (size_t)root_maps * 4, cudaMemcpyDeviceToHost, st));
   }
-  for (int i = 0; i < B; ++i) {
-    const pa_ps_outputs &o = outs[i];
-    if (mem == PA_MEM_HOST) {
+  if (mem == PA_MEM_HOST)
+    for (int i = 0; i < B; ++i) {
+      const pa_ps_outputs &o = outs[i];
       if (o.log_marg)
         for (int p = 0; p < P; ++p)
           PA_CK(cudaMemcpyAsync(o.log_marg + (int64_t)p * (pl.out_pstride ? pl.out_pstride : pl.N),
-                                pl.im[i].MARG[p],
-                                pl.N * sizeof(float), cudaMemcpyDeviceToHost, st));
+                                pl.im[i].MARG[p], pl.N * sizeof(float), cudaMemcpyDeviceToHost, st));
       if (o.root_post && e->use_pairwise)
         PA_CK(cudaMemcpyAsync(o.root_post, pl.im[i].root_post, (size_t)H * W * sizeof(float),
                               cudaMemcpyDeviceToHost, st));
     }
-  }
-  {
-    pa_status ss = sync_ctx(ctx);
-    if (ss) return ss;
-  }
+  return PA_OK;
+}
+
+// Decodes the landed results into the host outputs (after the stream has
+// passed the copies that finish_enqueue queued).
+pa_status finish_complete(pa_ctx *ctx, const pa_exp_param *e, const PsPlan &pl,
+                          const pa_ps_outputs *outs, const Readback &rb) {
+  const int B = pl.B, P = pl.P, H = pl.H, W = pl.W;
+  const int errflag = *rb.err;
   for (int i = 0; i < B; ++i) {
     const pa_ps_outputs &o = outs[i];
     const int scaleidx = pl.img_scale.empty() ? 0 : pl.img_scale[i];
     // this entry's row in the local-maximum results (-1: none computed)
     const int hrow = pl.hyp_img < 0 ? i : (pl.hyp_img == i ? 0 : -1);
     for (int p = 0; p < P; ++p) {
-      if (o.best) decode_hyp(e, am[(size_t)i * P + p], H, W, &o.best[p], scaleidx);
-      if (o.log_z) o.log_z[p] = lz[(size_t)i * P + p];
-      const int n = pl.want_part_hyps && hrow >= 0 ? nph[(size_t)hrow * P + p] : 0;
+      if (o.best) decode_hyp(e, rb.am[(size_t)i * P + p], H, W, &o.best[p], scaleidx);
+      if (o.log_z) o.log_z[p] = rb.lz[(size_t)i * P + p];
+      const int n = pl.want_part_hyps && hrow >= 0 ? rb.nph[(size_t)hrow * P + p] : 0;
       if (o.n_part_hyps) o.n_part_hyps[p] = n;
       if (o.part_hyps)
         for (int k = 0; k < n; ++k) {
           // PartHyp(exp_param, 0, rotidx, x, y, score).toVect(), objectdetect.h:95-159
-          const float *r = &ph[(((size_t)hrow * P + p) * pl.hyp_k + k) * 4];
+          const float *r = &rb.ph[(((size_t)hrow * P + p) * pl.hyp_k + k) * 4];
           pa_part_hyp &h = o.part_hyps[(size_t)p * pl.hyp_k + k];
           h.scaleidx = 0.f;
           h.scale = (float)scale_from_index(e, 0);
@@ -1135,14 +1189,14 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
         }
     }
     if (o.msg_max)
-      for (int k = 0; k < 2 * (P - 1); ++k) o.msg_max[k] = mm[(size_t)i * 2 * (P - 1) + k];
+      for (int k = 0; k < 2 * (P - 1); ++k) o.msg_max[k] = rb.mm[(size_t)i * 2 * (P - 1) + k];
     const int rrow = pl.root_joint ? (i == 0 ? 0 : -1) : i;
-    const int nr = pl.want_root_hyps && rrow >= 0 ? nrh[rrow] : 0;
+    const int nr = pl.want_root_hyps && rrow >= 0 ? rb.nrh[rrow] : 0;
     if (o.n_root_hyps) *o.n_root_hyps = nr;
     if (o.root_hyps)
       for (int k = 0; k < nr; ++k) {
         // ObjectHypothesis (scale, x, y, score), objectdetect_aux.cpp:279-290
-        const float *r = &rh[((size_t)rrow * kRootHyps + k) * 4];
+        const float *r = &rb.rh[((size_t)rrow * kRootHyps + k) * 4];
         o.root_hyps[4 * k + 0] = (float)scale_from_index(e, (int)r[0]);
         o.root_hyps[4 * k + 1] = r[1];
         o.root_hyps[4 * k + 2] = r[2];
@@ -1156,6 +1210,15 @@ pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_
   if (errflag & ~1)
     return fail(ctx, PA_ERR_UNSUPPORTED, "message kernel rejected its input (code %d)", errflag);
   return PA_OK;
+}
+
+// Reads back the small per-image results and writes host outputs.
+pa_status finish_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl, const pa_ps_outputs *outs,
+                    int mem) {
+  Readback rb;
+  if (pa_status st = finish_enqueue(ctx, e, pl, outs, mem, 0, rb)) return st;
+  if (pa_status st = sync_ctx(ctx)) return st;
+  return finish_complete(ctx, e, pl, outs, rb);
 }
 
 // Unary-map descriptors for B images x P parts x R rotations.
@@ -1314,12 +1377,27 @@ std::vector<int> stump_counts(const pa_classifier *const *cls, int n) {
 // The whole --find_obj pipeline for n_img images.
 // scores_out (if any) is laid out [n_cls][scores_fields][ny][nx] and this
 // call fills fields [scores_field0, scores_field0 + n_img*R) of it.
+// An image whose results are still on their way to the host: its plan, the
+// landing slot of its small results and its outputs.
+struct PendingImage {
+  PsPlan pl;
+  Readback rb;
+  const pa_ps_outputs *outs = nullptr;
+  int slot = 0;
+  bool busy = false;
+};
+
+// `defer` null: runs the batch and returns with its results written.
+// `defer` set: only queues the work and the result copies (landing slot
+// defer->slot); the caller completes it with finish_complete once the
+// stream has passed them.
 pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
                         int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
                         const float *const *img_desc, int in_mem, int ny, int nx, int dim,
                         const double *Tig, int tig_shared,
                         int H, int W, float *scores_out, int64_t scores_field0,
-                        int64_t scores_fields, const pa_ps_outputs *outs, int mem) {
+                        int64_t scores_fields, const pa_ps_outputs *outs, int mem,
+                        PendingImage *defer = nullptr) {
   PsPlan pl;
   pl.tc_mode = ctx->msg_math == PA_MSG_BF16_TENSOR;
   pl.sparse_up = true;  // findObjectImageRotJoints passes bIsSparse = true (objectdetect_findrot.cpp:740)
@@ -1438,13 +1516,22 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   }
   st = run_ps(ctx, e, pl2);
   if (st) return st;
+  if (defer) {
+    defer->pl = std::move(pl2);
+    defer->outs = outs;
+    return finish_enqueue(ctx, e, defer->pl, outs, mem, defer->slot, defer->rb);
+  }
   return finish_ps(ctx, e, pl2, outs, mem);
 }
 
 // Host descriptors, several images: images go through a ring of device
-// slots.  The copy of image i+k (k < slots) runs on the context's copy
-// stream while image i is being computed, so a batch costs about
-// max(copy, compute) per image instead of their sum.
+// slots.  The copy of image i + k (k < slots) runs on the context's copy
+// stream while image i is computed; the host plans and queues image i + 1
+// without waiting for image i (the copy into a slot waits on the device for
+// the slot's previous image, and an image's small results land in the
+// slot's pinned block, read once the stream has passed them), so a batch
+// costs about max(copy, compute) per image and host jitter does not stall
+// the copy engine.
 pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_tree *trees,
                         int flip, const pa_classifier *const *cls, int n_cls, const float *desc,
                         const float *const *img_desc, int ny, int nx, int dim, const double *Tig,
@@ -1453,20 +1540,26 @@ pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   const int R = e->num_rotation_steps;
   const size_t per_img = (size_t)R * ny * nx * dim;
   const size_t bytes = per_img * sizeof(float);
-  const int nslots = n_img < 3 ? n_img : 3;
+  const int nslots = n_img < pa_ctx::kLandings ? n_img : pa_ctx::kLandings;
   if (!ctx->copy_stream) {
     if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
       return fail(ctx, PA_ERR_CUDA, "cannot create the copy stream");
     }
   }
-  while ((int)ctx->ring_ev.size() < 3) {
+  while ((int)ctx->ring_ev.size() < pa_ctx::kLandings) {
     cudaEvent_t ev;
     PA_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     ctx->ring_ev.push_back(ev);
   }
+  while ((int)ctx->ring_done.size() < pa_ctx::kLandings) {
+    cudaEvent_t ev;
+    PA_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ctx->ring_done.push_back(ev);
+  }
   if (ctx->ring_cap < nslots * bytes) {
     PA_CK(cudaStreamSynchronize(ctx->copy_stream));
+    PA_CK(cudaStreamSynchronize(ctx->stream));
     if (ctx->ring) cudaFree(ctx->ring);
     ctx->ring = nullptr;
     ctx->ring_cap = 0;
@@ -1476,6 +1569,9 @@ pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
     }
     ctx->ring_cap = nslots * bytes;
   }
+  // the copy stream starts behind everything queued so far on the main stream
+  PA_CK(cudaEventRecord(ctx->ring_done[0], ctx->stream));
+  PA_CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ring_done[0], 0));
   auto issue = [&](int i) -> pa_status {
     const int k = i % nslots;
     const float *src = img_desc ? img_desc[i] : desc + i * per_img;
@@ -1484,27 +1580,64 @@ pa_status find_obj_ring(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
     PA_CK(cudaEventRecord(ctx->ring_ev[k], ctx->copy_stream));
     return PA_OK;
   };
-  for (int i = 0; i < nslots; ++i)
-    if (pa_status st = issue(i)) return st;
+  std::vector<PendingImage> pend(nslots);
+  auto drain = [&]() {  // leaves both streams idle after an error
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamSynchronize(ctx->stream);
+  };
   pa_status result = PA_OK;
+  // completes the image in slot k; NUMERIC is reported at the end, as the
+  // images after it still run
+  auto complete = [&](int k) -> pa_status {
+    PendingImage &pi = pend[k];
+    pi.busy = false;
+    PA_CK(cudaEventSynchronize(ctx->ring_done[k]));
+    const pa_status st = finish_complete(ctx, e, pi.pl, pi.outs, pi.rb);
+    if (st == PA_ERR_NUMERIC) {
+      result = st;
+      return PA_OK;
+    }
+    return st;
+  };
+  for (int i = 0; i < nslots; ++i)
+    if (pa_status st = issue(i)) {
+      drain();
+      return st;
+    }
   for (int i = 0; i < n_img; ++i) {
     const int k = i % nslots;
+    if (pend[k].busy)
+      if (pa_status st = complete(k)) {
+        drain();
+        return st;
+      }
     PA_CK(cudaStreamWaitEvent(ctx->stream, ctx->ring_ev[k], 0));
+    pend[k].slot = k;
     pa_status st = find_obj_core(ctx, e, 1, &trees[i], flip, cls, n_cls,
                                  reinterpret_cast<const float *>(ctx->ring + k * bytes), nullptr,
                                  PA_MEM_DEVICE, ny, nx, dim, Tig, tig_shared, H, W, scores_out,
-                                 (int64_t)i * R, (int64_t)n_img * R, &outs[i], PA_MEM_HOST);
-    // image i is complete (the core synchronises the main stream): its slot
-    // can take image i + nslots
-    if (st && st != PA_ERR_NUMERIC) {
-      cudaStreamSynchronize(ctx->copy_stream);
+                                 (int64_t)i * R, (int64_t)n_img * R, &outs[i], PA_MEM_HOST,
+                                 &pend[k]);
+    if (st) {
+      drain();
       return st;
     }
-    if (st) result = st;
-    if (i + nslots < n_img)
-      if (pa_status s2 = issue(i + nslots)) return s2;
+    pend[k].busy = true;
+    PA_CK(cudaEventRecord(ctx->ring_done[k], ctx->stream));
+    // slot k takes image i + nslots once image i has been computed
+    if (i + nslots < n_img) {
+      PA_CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ring_done[k], 0));
+      if (pa_status s2 = issue(i + nslots)) {
+        drain();
+        return s2;
+      }
+    }
   }
   PA_CK(cudaStreamSynchronize(ctx->copy_stream));
+  if (pa_status st = sync_ctx(ctx)) return st;
+  for (int i = std::max(0, n_img - nslots); i < n_img; ++i)
+    if (pend[i % nslots].busy)
+      if (pa_status st = complete(i % nslots)) return st;
   return result;
 }
 
@@ -1589,7 +1722,13 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) {
     resolve_timing(ctx);
     for (cudaEvent_t e : ctx->pool) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    for (auto &sg : ctx->stage) {
+      if (sg.p) cudaFreeHost(sg.p);
+      if (sg.done) cudaEventDestroy(sg.done);
+    }
+    for (auto &ld : ctx->land)
+      if (ld.p) cudaFreeHost(ld.p);
+    for (cudaEvent_t e : ctx->ring_done) cudaEventDestroy(e);
     if (ctx->copy_stream) {
       cudaStreamSynchronize(ctx->copy_stream);
       cudaStreamDestroy(ctx->copy_stream);
