@@ -347,6 +347,17 @@ def run_ours(args):
     e2e_val = replicas.throughput(replicas.sum_over_ranks(Be * e2e_steps, dist, dev), e2e_ms)
     h2d = Be * R * NY * NX * D * 4
     d2h = Be * P * (7 * 4 + 8) + Be * 2 * (P - 1) * 8
+    # the host->device copy ceiling of this machine: one image of descriptors
+    # from the same pinned buffer, timed alone
+    scratch = torch.empty_like(desc[0])
+    for _ in range(2):
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        scratch.copy_(host[0], non_blocking=True)
+        c1.record(stream)
+        torch.cuda.synchronize(dev)
+    h2d_gbs = host[0].numel() * 4 / (c0.elapsed_time(c1) / 1e3) / 1e9
+    del scratch
 
     cpu = None
     if rank == 0 and args.cpu_baseline:
@@ -368,7 +379,9 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (%.1f GB of descriptors per step)"
                              % (B * R * NY * NX * D * 4 / 1e9)},
             "e2e": {"value": e2e_val, "unit": "images/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "images_per_step": Be},
+                    "d2h_bytes_per_step": d2h, "images_per_step": Be,
+                    "h2d_gbs_measured": h2d_gbs,
+                    "copy_bound_images_per_s": h2d_gbs * 1e9 / (h2d / Be)},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches, "kernels": kernels,
             "sample_best_conf_part0": [float(x) for x in best[0]],

@@ -137,6 +137,32 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
                          const float *desc, int n_fields, int ny, int nx, int dim,
                          int normalize, float *scores, int mem);
 
+/* ------------------------------------------------ shape-context descriptors */
+
+/* FeatureGrid(img_width, img_height, x_axis, y_axis, desc_step, desc_size)
+ * (libPartDetect/FeatureGrid.cpp:22-97): size of the grid whose axes are
+ * x_axis / y_axis (partdetect_test.cpp:171-185 uses (cos r, sin r) and
+ * (-sin r, cos r), x_axis negated for a flipped image) and that covers the
+ * rotated image at desc_step pixels.  Host only. */
+pa_status pa_feature_grid_size(int img_w, int img_h, const double *x_axis, const double *y_axis,
+                               double desc_step, int *nx, int *ny);
+
+/* computeDescriptorGrid(image, grid, "SHAPEv5", no detection mask, whole
+ * image) (libPartDetect/partdetect_aux.cpp:77-190) with libKMA2's SHAPEv5
+ * descriptor (ShapeDescriptor.cpp:168-261): for every grid position inside
+ * the image by desc_size + 1 pixels, a 21 x 21 patch resampled along the
+ * axes, normalised, Canny edges (5, 15), a 3 x 4 log-polar x 8 orientation
+ * histogram, normalised, clipped at 0.2, renormalised, quantised to
+ * integers (int)(512 v) <= 255.  A patch without edges gives INT_MIN in all
+ * 96 entries, as the reference's float -> int conversion does on x86-64.
+ *   image [img_h][img_w] grey levels; cells [ny][nx][96]; valid [ny][nx]
+ *   (0: position outside, its cell zero).  desc_size <= 10 (patch_scale <=
+ *   1); larger sizes need the pre-smoothed source and give
+ *   PA_ERR_UNSUPPORTED.  The cells feed pa_score_grids_window. */
+pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img_w,
+                             const double *x_axis, const double *y_axis, double desc_step,
+                             int desc_size, float *cells, uint8_t *valid, int mem);
+
 /* computeScoreGrid over a grid of per-cell descriptors: each window vector is
  * the reverse-order concatenation of gx*gy cell descriptors taken every
  * round(k*grid_step) cells (FeatureGrid::concatenate,

@@ -358,3 +358,77 @@ def find_obj_batch(exp: OrcExp, tree, models, descs, Tig, H, W, interpolate=True
     if rc:
         raise ValueError(f"orc_find_obj_batch failed: {rc}")
     return best
+
+
+# ---------------------------------------------------------------- SHAPEv5
+PATCH = 21
+SHAPE_DIM = 96
+
+
+def _desc_decl(L):
+    if getattr(L, "_desc_declared", False):
+        return L
+    fp, dp, ip = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int)
+    L.orc_patch_tables.argtypes = [fp, dp, dp]
+    L.orc_patch_tables.restype = None
+    L.orc_shape_descriptor.argtypes = [fp, fp]
+    L.orc_shape_descriptor.restype = None
+    L.orc_feature_grid.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp, ip, ip]
+    L.orc_feature_grid.restype = None
+    L.orc_descriptor_grid.argtypes = [fp, C.c_int, C.c_int, dp, dp, C.c_double, C.c_int, fp,
+                                      C.POINTER(C.c_uint8)]
+    L.orc_descriptor_grid.restype = C.c_int
+    L._desc_declared = True
+    return L
+
+
+def patch_tables():
+    """(mask [21][21] f32, lcpos [21][21] f64, lrpos [21][21] f64)."""
+    L = _desc_decl(lib())
+    m = np.zeros((PATCH, PATCH), np.float32)
+    lc = np.zeros((PATCH, PATCH), np.float64)
+    lr = np.zeros((PATCH, PATCH), np.float64)
+    L.orc_patch_tables(_p(m, C.c_float), _p(lc, C.c_double), _p(lr, C.c_double))
+    return m, lc, lr
+
+
+def shape_descriptor(patch):
+    """KMAcomputeShape of one normalised [21][21] patch -> 96 floats."""
+    L = _desc_decl(lib())
+    p = np.ascontiguousarray(patch, dtype=np.float32).reshape(PATCH, PATCH)
+    v = np.zeros(SHAPE_DIM, np.float32)
+    L.orc_shape_descriptor(_p(p, C.c_float), _p(v, C.c_float))
+    return v
+
+
+def _axes(x_axis, y_axis):
+    return (np.ascontiguousarray(x_axis, dtype=np.float64).reshape(2),
+            np.ascontiguousarray(y_axis, dtype=np.float64).reshape(2))
+
+
+def feature_grid(img_w, img_h, x_axis, y_axis, desc_step):
+    """(rect [4], nx, ny) of FeatureGrid's rotated grid."""
+    L = _desc_decl(lib())
+    ax, ay = _axes(x_axis, y_axis)
+    rect = np.zeros(4, np.float64)
+    nx, ny = C.c_int(), C.c_int()
+    L.orc_feature_grid(int(img_w), int(img_h), _p(ax, C.c_double), _p(ay, C.c_double),
+                       float(desc_step), _p(rect, C.c_double), C.byref(nx), C.byref(ny))
+    return rect, nx.value, ny.value
+
+
+def descriptor_grid(image, x_axis, y_axis, desc_step, desc_size):
+    """computeDescriptorGrid (SHAPEv5): (cells [ny][nx][96] f32, valid [ny][nx] u8)."""
+    L = _desc_decl(lib())
+    img = np.ascontiguousarray(image, dtype=np.float32)
+    h, w = img.shape
+    _, nx, ny = feature_grid(w, h, x_axis, y_axis, desc_step)
+    ax, ay = _axes(x_axis, y_axis)
+    cells = np.zeros((ny, nx, SHAPE_DIM), np.float32)
+    valid = np.zeros((ny, nx), np.uint8)
+    rc = L.orc_descriptor_grid(_p(img, C.c_float), h, w, _p(ax, C.c_double), _p(ay, C.c_double),
+                               float(desc_step), int(desc_size), _p(cells, C.c_float),
+                               _p(valid, C.c_uint8))
+    if rc:
+        raise ValueError(f"orc_descriptor_grid failed: {rc}")
+    return cells, valid

@@ -1,0 +1,358 @@
+/* desc.cpp -- CPU restatement of the SHAPEv5 shape-context descriptor grid
+ * (libPartDetect/partdetect_aux.cpp:77-190, computeDescriptorGrid, and the
+ * libKMA2 code it calls).  TEST INFRASTRUCTURE ONLY, like oracle.cpp: the
+ * checker for the GPU descriptor kernels, never part of the product path.
+ *
+ * Every floating-point expression keeps the reference's types (float where
+ * the reference stores float, double where a double literal or a double
+ * variable promotes it) and its evaluation order; the file is compiled with
+ * -ffp-contract=off so no multiply-add is fused.  The one place where the
+ * reference depends on its platform is the conversion of a NaN to int
+ * ((int)(512.0 * NaN) in KMAcomputeShape, reached by patches without edges):
+ * x86-64, where the reference runs, yields INT_MIN; this file writes INT_MIN
+ * explicitly so that x86 and Arm hosts agree. */
+#include "oracle.h"
+
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+/* libKMA2/descriptor/feature.h:25, ShapeDescriptor.h:35-38 */
+constexpr int kPatch = 21;
+constexpr int kSr = 3, kSc = 4, kSOri = 8;
+constexpr int kShape = kSr * kSc * kSOri;
+constexpr float kMaxIndexVal = 0.2f;
+/* libKMA2/gauss_iir/gauss_iir.h:21 */
+constexpr double kM2Pi = 6.2831853072;
+
+struct Img {  /* DARY: fel[row][col], x() = columns, y() = rows */
+  int w, h;
+  const float *p;
+  float at(int r, int c) const { return p[(size_t)r * w + c]; }
+};
+
+/* ImageContent::interpolate, ImageContent/ImageContent.cpp:658-727: a
+ * kPatch x kPatch patch sampled around (m_x, m_y) along the two axes, with
+ * the reference's clamping of samples that fall off the image. */
+void interpolate(const Img &in, float m_x, float m_y, float vec0x, float vec0y, float vec1x,
+                 float vec1y, float *patch) {
+  const int half = kPatch >> 1;
+  const int xim = in.w - 1, yim = in.h - 1;
+  for (int j = -half; j <= half; ++j)
+    for (int i = -half; i <= half; ++i) {
+      const float px = m_x + i * vec0x + j * vec0y;
+      const float py = m_y + i * vec1x + j * vec1y;
+      const int ax = (int)std::floor(px), ay = (int)std::floor(py);
+      const float dx = px - ax, dy = py - ay;
+      float &o = patch[(j + half) * kPatch + (i + half)];
+      if (ax >= 0 && ay >= 0 && ax < xim && ay < yim) {
+        o = (float)((1.0 - dy) * ((1.0 - dx) * in.at(ay, ax) + dx * in.at(ay, ax + 1)) +
+                    dy * ((1.0 - dx) * in.at(ay + 1, ax) + dx * in.at(ay + 1, ax + 1)));
+      } else if (ax < 0 && ay < 0) {
+        o = in.at(0, 0);
+      } else if (ax >= xim && ay >= yim) {
+        o = in.at(yim, xim);
+      } else if (ax < 0 && ay > yim) {
+        o = in.at(yim, 0);
+      } else if (ax >= xim && ay < 0) {
+        o = in.at(0, xim);
+      } else if (ax > xim && ay >= 0) {
+        o = in.at(ay, xim);
+      } else if (ax >= 0 && ay < 0) {
+        o = in.at(0, ax);
+      } else if (ax >= 0 && ay >= yim) {
+        o = in.at(yim, ax);
+      } else if (ax < 0 && ay >= 0) {
+        o = in.at(ay, 0);
+      } else if (ax >= xim && ay >= 0) {
+        o = in.at(ay, xim);
+      }
+    }
+}
+
+/* ImageContent::getValue, ImageContent/ImageContent.cpp:29-50 */
+float get_value(const float *g, int w, int h, float x, float y) {
+  const unsigned ix = (unsigned)(long long)std::floor(x);
+  const unsigned iy = (unsigned)(long long)std::floor(y);
+  const float dx = x - ix, dy = y - iy;
+  const unsigned xs = (unsigned)w, ys = (unsigned)h;
+  auto at = [&](unsigned r, unsigned c) { return g[(size_t)r * w + c]; };
+  float val = 0;
+  if (ix < xs - 1 && iy < ys - 1) {
+    val = (float)((1.0 - dy) * ((1.0 - dx) * at(iy, ix) + dx * at(iy, ix + 1)) +
+                  dy * ((1.0 - dx) * at(iy + 1, ix) + dx * at(iy + 1, ix + 1)));
+  } else if (ix == xs - 1 && iy < ys - 1) {
+    val = (float)((1.0 - dy) * at(iy, ix) + dy * (at(iy + 1, ix)));
+  } else if (iy == ys - 1 && ix < xs - 1) {
+    val = (float)((1.0 - dx) * at(iy, ix) + dx * (at(iy, ix + 1)));
+  } else if (iy == ys - 1 && ix == xs - 1) {
+    val = at(iy, ix);
+  }
+  return val;
+}
+
+/* normalize, descriptor/FeatureDescriptor.cpp:80-113 */
+void normalize_patch(float *img, const float *mask) {
+  float sum = 0, gsum = 0;
+  for (int j = 0; j < kPatch; ++j)
+    for (int i = 0; i < kPatch; ++i)
+      if (mask[j * kPatch + i] > 0) {
+        sum += img[j * kPatch + i];
+        gsum++;
+      }
+  sum = sum / gsum;
+  float var = 0;
+  for (int j = 0; j < kPatch; ++j)
+    for (int i = 0; i < kPatch; ++i)
+      if (mask[j * kPatch + i] > 0)
+        var += (sum - img[j * kPatch + i]) * (sum - img[j * kPatch + i]);
+  var = std::sqrt(var / gsum);
+  const float fac = 50.0 / var;
+  for (int k = 0; k < kPatch * kPatch; ++k) {
+    img[k] = 128 + fac * (img[k] - sum);
+    if (img[k] > 255) img[k] = 255;
+    if (img[k] < 0) img[k] = 0;
+  }
+}
+
+/* cannyEdges(dx, dy, grad, edge, lower, higher), descriptor/EdgeDetector.cpp:74-147:
+ * non-maximum suppression along the gradient, strong edges above `higher`,
+ * weak ones kept when connected to a strong one (raster-order labels). */
+void canny(const float *dx, const float *dy, const float *grad, float *edge, float lower,
+           float higher) {
+  const int W = kPatch, H = kPatch;
+  std::vector<float> tmp(W * H, 0.f);
+  std::vector<int> cor{0};
+  const float color = 255;
+  float nb = 1;
+  auto E = [&](int j, int i) -> float & { return edge[j * W + i]; };
+  auto T = [&](int j, int i) -> float & { return tmp[j * W + i]; };
+  for (int j = 1; j < H - 2; ++j)
+    for (int i = 1; i < W - 2; ++i) {
+      const float g = grad[j * W + i];
+      if (g < lower) continue;
+      const float ux = dx[j * W + i], uy = dy[j * W + i];
+      const float x1 = i + ux / g, y1 = j + uy / g;
+      const float x2 = i - ux / g, y2 = j - uy / g;
+      const float g1 = get_value(grad, W, H, x1, y1);
+      const float g2 = get_value(grad, W, H, x2, y2);
+      if (g <= g1 || g <= g2) continue;
+      if (g > higher) {
+        E(j, i) = color;
+      } else if (g > lower && (E(j - 1, i - 1) == color || E(j - 1, i) == color ||
+                               E(j - 1, i + 1) == color || E(j, i - 1) == color)) {
+        E(j, i) = color;
+      } else if (g > lower) {
+        if (T(j - 1, i - 1) > 0) T(j, i) = T(j - 1, i - 1);
+        else if (T(j - 1, i) > 0) T(j, i) = T(j - 1, i);
+        else if (T(j - 1, i + 1) > 0) T(j, i) = T(j - 1, i + 1);
+        else if (T(j, i - 1) > 0) T(j, i) = T(j, i - 1);
+        else if (T(j, i + 1) > 0) T(j, i) = T(j, i + 1);
+        else {
+          T(j, i) = nb;
+          cor.push_back(0);
+          nb++;
+        }
+      }
+    }
+  for (int j = H - 2; j > 0; --j)
+    for (int i = W - 2; i > 0; --i)
+      if (E(j - 1, i - 1) == color || E(j - 1, i) == color || E(j - 1, i + 1) == color ||
+          E(j, i - 1) == color || E(j, i + 1) == color || E(j + 1, i - 1) == color ||
+          E(j + 1, i) == color || E(j + 1, i + 1) == color)
+        cor[(int)T(j, i)] = 1;
+  for (int j = H - 2; j > 0; --j)
+    for (int i = W - 2; i > 0; --i)
+      if (T(j, i) > 0 && cor[(int)T(j, i)] == 1) E(j, i) = color;
+  for (int k = 0; k < W * H; ++k) edge[k] = edge[k] > 0 ? grad[k] : 0;
+}
+
+/* KMANormalizeVect, ShapeDescriptor.cpp:26-39 */
+void normalize_vect(float *v) {
+  float sqlen = 0.0;
+  for (int i = 0; i < kShape; ++i) sqlen += v[i] * v[i];
+  const float fac = 1.0 / std::sqrt(sqlen);
+  for (int i = 0; i < kShape; ++i) v[i] *= fac;
+}
+
+/* KMAPlaceInLogPolIndex, ShapeDescriptor.cpp:71-121 (orientation modulo pi) */
+void place(float *index, float mag, float ori, float rx, float cx) {
+  const float oval = kSOri * ori / (M_PI);
+  const int ri = (int)((rx >= 0.0) ? rx : rx - 1.0);
+  const int ci = (int)((cx >= 0.0) ? cx : cx - 1.0);
+  const int oi = (int)((oval >= 0.0) ? oval : oval - 1.0);
+  const float rfrac = rx - ri, cfrac = cx - ci, ofrac = oval - oi;
+  for (int r = 0; r < 2; ++r) {
+    const int rindex = ri + r;
+    if (rindex >= 0 && rindex < kSr) {
+      const float rweight = mag * ((r == 0) ? 1.0 - rfrac : rfrac);
+      for (int c = 0; c < 2; ++c) {
+        int cindex = ci + c;
+        if (cindex >= kSc) cindex = 0;
+        if (cindex >= 0 && cindex < kSc) {
+          const float cweight = rweight * ((c == 0) ? 1.0 - cfrac : cfrac);
+          const int rcindex = (rindex * kSc + cindex) << 3;
+          for (int ort = 0; ort < 2; ++ort) {
+            int oindex = oi + ort;
+            if (oindex >= kSOri) oindex = 0;
+            const float oweight = cweight * ((ort == 0) ? 1.0 - ofrac : ofrac);
+            index[rcindex + oindex] += oweight;
+          }
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_patch_tables(float *mask, double *lcpos, double *lrpos) {
+  /* initPatchMask(PATCH_SIZE), FeatureDescriptor.cpp:118-137 */
+  const int center = kPatch >> 1;
+  const float radius = center * center;
+  const float sigma = 0.9 * radius;
+  for (int i = 0; i < kPatch; ++i)
+    for (int j = 0; j < kPatch; ++j) {
+      const float disq = (i - center) * (i - center) + (j - center) * (j - center);
+      mask[j * kPatch + i] = disq < radius ? std::exp(-disq / sigma) : 0.f;
+    }
+  /* precompute_patch_idx(.., iradius = PATCH_SIZE / 2, SrSize, ScSize), ShapeDescriptor.cpp:42-64 */
+  const int ir = center;
+  const float cspacing = kSc / (kM2Pi);
+  for (int i = -ir; i <= ir; ++i)
+    for (int j = -ir; j <= ir; ++j) {
+      const int rpos = i, cpos = j;
+      lcpos[(ir + j) * kPatch + (ir + i)] = (M_PI + std::atan2((double)rpos, (double)cpos)) * cspacing;
+      lrpos[(ir + j) * kPatch + (ir + i)] =
+          std::log(1 + std::sqrt((float)i * i + j * j) / ir) * kSr;
+    }
+}
+
+/* KMAcomputeShape, ShapeDescriptor.cpp:168-261, on a normalised patch
+ * [kPatch][kPatch]: gradients (dX2/dY2, gauss_iir.cpp:1182-1225), magnitude
+ * and orientation, Canny edges (thresholds 5 and 15), log-polar histogram
+ * of edge orientations weighted by the patch mask, L2 normalisation with a
+ * 0.2 clip and integer quantisation (int)(512 v) capped at 255. */
+void orc_shape_descriptor(const float *patch, float *vec) {
+  float mask[kPatch * kPatch];
+  double lc[kPatch * kPatch], lr[kPatch * kPatch];
+  orc_patch_tables(mask, lc, lr);
+  const int W = kPatch, H = kPatch;
+  float dx[W * H], dy[W * H], grad[W * H], ori[W * H], edge[W * H];
+  /* dX2 / dY2: central differences, zero on the border */
+  for (int k = 0; k < W * H; ++k) dx[k] = dy[k] = 0;
+  for (int y = 1; y < H - 1; ++y)
+    for (int x = 1; x < W - 1; ++x) dx[y * W + x] = patch[y * W + x + 1] - patch[y * W + x - 1];
+  for (int x = 1; x < W - 1; ++x)
+    for (int y = 1; y < H - 1; ++y) dy[y * W + x] = patch[(y + 1) * W + x] - patch[(y - 1) * W + x];
+  for (int k = 0; k < W * H; ++k) {
+    grad[k] = std::sqrt(dx[k] * dx[k] + dy[k] * dy[k]);
+    ori[k] = std::atan2(dy[k], dx[k]);
+    edge[k] = 0;
+  }
+  canny(dx, dy, grad, edge, 5, 15);
+  for (int k = 0; k < kShape; ++k) vec[k] = 0;
+  const int ir = kPatch / 2;
+  for (int i = -ir; i <= ir; ++i)
+    for (int j = -ir; j <= ir; ++j) {
+      const double lcpos = lc[(ir + j) * kPatch + (ir + i)];
+      const double lrpos = lr[(ir + j) * kPatch + (ir + i)];
+      const double rx = lrpos, cx = lcpos;
+      if (!(rx > -1.0 && rx < (float)kSr && cx > -1.0 && cx < (float)kSc)) continue;
+      /* KMAAddLogPolSample(vec, edge, ori, 0.0, ir + i, ir + j, ...), :126-164 */
+      const int r = ir + i, c = ir + j;
+      if (edge[r * W + c] < 1e-10) continue;
+      const float mag = mask[r * W + c] * edge[r * W + c];
+      float o = ori[r * W + c] - (float)0.0;
+      while (o > M_PI) o -= M_PI;
+      while (o < 0.0) o += M_PI;
+      place(vec, mag, o, (float)lrpos, (float)lcpos);
+    }
+  normalize_vect(vec);
+  bool changed = false;
+  for (int i = 0; i < kShape; ++i)
+    if (vec[i] > kMaxIndexVal) {
+      vec[i] = kMaxIndexVal;
+      changed = true;
+    }
+  if (changed) normalize_vect(vec);
+  for (int i = 0; i < kShape; ++i) {
+    const double s = 512.0 * vec[i];
+    const int intval = std::isnan(s) ? INT_MIN : (int)s; /* x86-64 cvttsd2si */
+    vec[i] = (255 < intval) ? 255 : intval;
+  }
+}
+
+/* FeatureGrid(img_width, img_height, x_axis, y_axis, desc_step, desc_size)
+ * (libPartDetect/FeatureGrid.cpp:22-97): the bounding box of the image in
+ * the rotated frame and the grid size. */
+void orc_feature_grid(int img_w, int img_h, const double *ax, const double *ay, double desc_step,
+                      double *rect, int *nx, int *ny) {
+  /* boost_math::inv for 2x2, boost_math.hpp:103-110, of T12 = [x_axis y_axis] */
+  const double m00 = ax[0], m01 = ay[0], m10 = ax[1], m11 = ay[1];
+  const double D = m00 * m11 - m10 * m01;
+  const double t00 = m11 / D, t01 = -m01 / D, t10 = -m10 / D, t11 = m00 / D;
+  const double cx[4] = {0, (double)img_w, (double)img_w, 0};
+  const double cy[4] = {0, 0, (double)img_h, (double)img_h};
+  double mnx = 0, mxx = 0, mny = 0, mxy = 0;
+  for (int i = 0; i < 4; ++i) {
+    const double px = t00 * cx[i] + t01 * cy[i], py = t10 * cx[i] + t11 * cy[i];
+    if (i == 0) {
+      mnx = mxx = px;
+      mny = mxy = py;
+      continue;
+    }
+    if (mnx > px) mnx = px;
+    if (mxx < px) mxx = px;
+    if (mny > py) mny = py;
+    if (mxy < py) mxy = py;
+  }
+  rect[0] = mnx;
+  rect[1] = mxx;
+  rect[2] = mny;
+  rect[3] = mxy;
+  *nx = (int)std::floor(((mxx - mnx + 1) / desc_step)) + 1;
+  *ny = (int)std::floor(((mxy - mny + 1) / desc_step)) + 1;
+}
+
+int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *ax,
+                        const double *ay, double desc_step, int desc_size, float *cells,
+                        uint8_t *valid) {
+  double rect[4];
+  int nx = 0, ny = 0;
+  orc_feature_grid(img_w, img_h, ax, ay, desc_step, rect, &nx, &ny);
+  const double patch_scale = (2 * desc_size + 1) / (float)kPatch;
+  if (patch_scale > 1.0) return -2; /* the smoothed-source branch is not restated */
+  float mask[kPatch * kPatch];
+  double lc[kPatch * kPatch], lr[kPatch * kPatch];
+  orc_patch_tables(mask, lc, lr);
+  const Img src{img_w, img_h, image};
+  float patch[kPatch * kPatch];
+  for (int iy = 0; iy < ny; ++iy)
+    for (int ix = 0; ix < nx; ++ix) {
+      const size_t cell = (size_t)iy * nx + ix;
+      valid[cell] = 0;
+      std::memset(cells + cell * kShape, 0, kShape * sizeof(float));
+      const double x2 = rect[0] + ix * desc_step, y2 = rect[2] + iy * desc_step;
+      const double px = (0.0 + x2 * ax[0]) + y2 * ay[0];
+      const double py = (0.0 + x2 * ax[1]) + y2 * ay[1];
+      if (!(px >= desc_size + 1 && px <= img_w - (desc_size + 1) && py >= desc_size + 1 &&
+            py <= img_h - (desc_size + 1)))
+        continue;
+      interpolate(src, (float)px, (float)py, (float)(patch_scale * ax[0]),
+                  (float)(patch_scale * ay[0]), (float)(patch_scale * ax[1]),
+                  (float)(patch_scale * ay[1]), patch);
+      normalize_patch(patch, mask);
+      orc_shape_descriptor(patch, cells + cell * kShape);
+      valid[cell] = 1;
+    }
+  return 0;
+}
+
+}  // extern "C"

@@ -189,6 +189,32 @@ int orc_find_obj_batch_f32(const orc_exp *e, const orc_tree *t,
                            const double *Tig, int interpolate, int H, int W,
                            float *best_conf, int n_threads);
 
+/* ---- SHAPEv5 shape-context descriptors (desc.cpp) ---------------------- */
+
+/* initPatchMask(21) (libKMA2/descriptor/FeatureDescriptor.cpp:118-137) and
+ * precompute_patch_idx (libKMA2/ShapeDescriptor.cpp:42-64): mask [21][21]
+ * float, lcpos / lrpos [21][21] log-polar angle / radius bin coordinates. */
+void orc_patch_tables(float *mask, double *lcpos, double *lrpos);
+
+/* KMAcomputeShape (ShapeDescriptor.cpp:168-261) of one normalised 21 x 21
+ * patch: 96 values (3 radii x 4 angles x 8 orientations), integers in
+ * [0, 255], or INT_MIN everywhere for a patch without edges. */
+void orc_shape_descriptor(const float *patch, float *vec);
+
+/* FeatureGrid(img_width, img_height, x_axis, y_axis, desc_step, _)
+ * (libPartDetect/FeatureGrid.cpp:22-97): rect = {min_proj_x, max_proj_x,
+ * min_proj_y, max_proj_y}, nx, ny. */
+void orc_feature_grid(int img_w, int img_h, const double *x_axis, const double *y_axis,
+                      double desc_step, double *rect, int *nx, int *ny);
+
+/* computeDescriptorGrid with SHAPEv5 (libPartDetect/partdetect_aux.cpp:77-190)
+ * on a grayscale image [img_h][img_w]: cells [ny][nx][96] (zero where the
+ * descriptor window leaves the image), valid [ny][nx].  Returns 0, or -2 for
+ * desc_size > 10 (the pre-smoothed source branch is not restated). */
+int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *x_axis,
+                        const double *y_axis, double desc_step, int desc_size, float *cells,
+                        uint8_t *valid);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,7 @@ EXPORTS = (
     "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
     "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
     "pa_ps_infer", "pa_rot_joint_marginal", "pa_rot_joint_marginal_noalloc", "pa_find_obj",
+    "pa_feature_grid_size", "pa_descriptor_grid",
     "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math", "pa_find_obj_multi",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
@@ -133,6 +134,8 @@ def load_library():
                                         vp, ip]
     L.pa_unary_maps.argtypes = [vp, vp, ip, ip, ip, ip, P(dp), ip, ip, ip, ip, vp, ip]
     L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, ip, vp, ip, ip, P(PsOutputs), ip]
+    L.pa_feature_grid_size.argtypes = [ip, ip, P(dp), P(dp), dp, P(ip), P(ip)]
+    L.pa_descriptor_grid.argtypes = [vp, vp, ip, ip, P(dp), P(dp), dp, ip, vp, vp, ip]
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
                                         dp, dp, dp, ip, ip]
     L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip, ip]
@@ -342,6 +345,32 @@ class Context:
                                          T.ctypes.data_as(C.POINTER(C.c_double)), shared,
                                          int(interpolate), H, W, o.ptr, s.mem))
         return out
+
+    # ------------------------------------------------------ descriptors
+    def descriptor_grid(self, image, x_axis, y_axis, desc_step, desc_size):
+        """computeDescriptorGrid with SHAPEv5 on a grey image [h][w] (numpy or
+        CUDA tensor): returns (cells [ny][nx][96] f32, valid [ny][nx] u8) in
+        the image's memory space."""
+        im = _Buf(image, np.float32)
+        h, w = im.arr.shape
+        ax = np.ascontiguousarray(x_axis, dtype=np.float64).reshape(2)
+        ay = np.ascontiguousarray(y_axis, dtype=np.float64).reshape(2)
+        pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        nx, ny = C.c_int(), C.c_int()
+        self._check(self.L.pa_feature_grid_size(w, h, pd(ax), pd(ay), float(desc_step),
+                                                C.byref(nx), C.byref(ny)))
+        cells = _empty_like_space((ny.value, nx.value, 96), im.mem, im.arr)
+        if im.mem == PA_MEM_DEVICE:
+            import torch
+            valid = torch.empty((ny.value, nx.value), dtype=torch.uint8, device=im.arr.device)
+            vptr = valid.data_ptr()
+        else:
+            valid = np.empty((ny.value, nx.value), np.uint8)
+            vptr = valid.ctypes.data
+        self._check(self.L.pa_descriptor_grid(self.h, im.ptr, h, w, pd(ax), pd(ay),
+                                              float(desc_step), int(desc_size),
+                                              _Buf(cells, np.float32).ptr, vptr, im.mem))
+        return cells, valid
 
     # ---------------------------------------------------------- messages
     def rot_joint_marginal(self, exp: ExpParam, child, offset_c, offset_p, Cmat, rot_mean,

@@ -25,7 +25,7 @@ HOST = os.path.join(HERE, "host")
 CLI = os.path.join(OUT, "partapp_find_obj")
 HOST_SOURCES = ["objectdetect_gpu.cpp", "find_obj_main.cpp"]
 SOURCES = ["k_stump.cu", "k_unary.cu", "k_msg.cu", "k_reduce.cu", "k_localmax.cu", "k_tc_gemm.cu",
-           "pa_api.cu", "pa_noalloc.cu"]
+           "k_desc.cu", "pa_api.cu", "pa_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

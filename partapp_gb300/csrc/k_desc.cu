@@ -1,0 +1,361 @@
+// k_desc.cu -- SHAPEv5 shape-context descriptor grid on GB300.
+//
+// Replaces computeDescriptorGrid (libPartDetect/partdetect_aux.cpp:77-190)
+// with the SHAPEv5 descriptor of libKMA2 (ShapeDescriptor.cpp:168-261): for
+// every position of a rotated grid, a 21 x 21 patch is resampled from the
+// image (ImageContent::interpolate), normalised to mean 128 / deviation 50
+// (normalize, FeatureDescriptor.cpp:80-113), its central-difference
+// gradients (dX2 / dY2) go through Canny (EdgeDetector.cpp:74-147) and the
+// edge magnitudes are binned by log-polar position and orientation into 96
+// values, normalised, clipped at 0.2, renormalised and quantised.
+//
+// One warp owns one grid position; its patch and the intermediate maps live
+// in the warp's slice of shared memory.  Elementwise steps run on all 32
+// lanes; the steps whose float sums or scan order define the result (the
+// patch mean and variance, the Canny raster scan with its label
+// propagation, the histogram accumulation, the vector norms) run on lane 0
+// in the reference's order, so the arithmetic matches the reference's
+// operation for operation.  No multiply-add is fused: every product that
+// feeds a sum goes through an explicitly rounded intrinsic, in float or in
+// double as the reference's expression types dictate.  The one library
+// function whose result can differ in the last bit from the host's is
+// atan2f (gradient orientation).
+#include <climits>
+
+#include "pa_internal.cuh"
+
+namespace pa {
+namespace {
+
+constexpr int kP = 21;          // PATCH_SIZE, libKMA2/descriptor/feature.h:25
+constexpr int kPP = kP * kP;
+constexpr int kHalf = kP / 2;
+constexpr int kShape = 96;      // SrSize * ScSize * SOriSize (3 * 4 * 8), ShapeDescriptor.h:35-37
+constexpr int kSr = 3, kSc = 4, kSOri = 8;
+constexpr float kMaxIndexVal = 0.2f;  // ShapeDescriptor.h:38
+constexpr float kColor = 255.f;       // EdgeDetector.cpp:79
+constexpr float kLower = 5.f, kHigher = 15.f;  // cannyEdges(dx, dy, grad, edge, 5, 15)
+constexpr double kPi = 3.14159265358979323846;
+constexpr int kDescWarps = 4;   // grid positions (one per warp) per CTA
+
+struct WarpScratch {
+  float patch[kPP];
+  float dx[kPP], dy[kPP], grad[kPP], ori[kPP], edge[kPP], tmp[kPP];
+  float vec[kShape];
+  int cor[kPP + 1];        // connected-to-strong flag per weak-edge label
+  unsigned char state[kPP];  // 0 none, 1 strong edge, 2 weak edge candidate
+  float sum, fac;
+};
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// (1 - dy) * ((1 - dx) * a + dx * b) + dy * ((1 - dx) * c + dx * d) with the
+// reference's types: 1.0 - d in double, dx * b a float product.
+__device__ __forceinline__ float bilinear4(float dx, float dy, float a, float b, float c, float d) {
+  const double omdx = dsub(1.0, (double)dx), omdy = dsub(1.0, (double)dy);
+  const double t1 = dadd(dmul(omdx, (double)a), (double)fmul(dx, b));
+  const double t2 = dadd(dmul(omdx, (double)c), (double)fmul(dx, d));
+  return __double2float_rn(dadd(dmul(omdy, t1), dmul((double)dy, t2)));
+}
+
+// ImageContent::getValue (ImageContent.cpp:29-50) on a 21 x 21 map.
+__device__ float get_value(const float *g, float x, float y) {
+  const unsigned ix = (unsigned)(long long)floorf(x);
+  const unsigned iy = (unsigned)(long long)floorf(y);
+  const float dx = fsub(x, (float)ix), dy = fsub(y, (float)iy);
+  const unsigned n = kP - 1;
+  if (ix < n && iy < n)
+    return bilinear4(dx, dy, g[iy * kP + ix], g[iy * kP + ix + 1], g[(iy + 1) * kP + ix],
+                     g[(iy + 1) * kP + ix + 1]);
+  // (1.0 - dy) * a + dy * b: the second product is a float one
+  if (ix == n && iy < n)
+    return __double2float_rn(dadd(dmul(dsub(1.0, (double)dy), (double)g[iy * kP + ix]),
+                                  (double)fmul(dy, g[(iy + 1) * kP + ix])));
+  if (iy == n && ix < n)
+    return __double2float_rn(dadd(dmul(dsub(1.0, (double)dx), (double)g[iy * kP + ix]),
+                                  (double)fmul(dx, g[iy * kP + ix + 1])));
+  if (iy == n && ix == n) return g[iy * kP + ix];
+  return 0.f;
+}
+
+// KMAPlaceInLogPolIndex (ShapeDescriptor.cpp:71-121), orientation modulo pi.
+__device__ void place(float *index, float mag, float ori, float rx, float cx) {
+  const float oval = __double2float_rn(__ddiv_rn((double)fmul((float)kSOri, ori), kPi));
+  const int ri = (int)((rx >= 0.0f) ? (double)rx : dsub((double)rx, 1.0));
+  const int ci = (int)((cx >= 0.0f) ? (double)cx : dsub((double)cx, 1.0));
+  const int oi = (int)((oval >= 0.0f) ? (double)oval : dsub((double)oval, 1.0));
+  const float rfrac = fsub(rx, (float)ri), cfrac = fsub(cx, (float)ci), ofrac = fsub(oval, (float)oi);
+  for (int r = 0; r < 2; ++r) {
+    const int rindex = ri + r;
+    if (rindex < 0 || rindex >= kSr) continue;
+    const float rweight =
+        __double2float_rn(dmul((double)mag, r == 0 ? dsub(1.0, (double)rfrac) : (double)rfrac));
+    for (int c = 0; c < 2; ++c) {
+      int cindex = ci + c;
+      if (cindex >= kSc) cindex = 0;
+      if (cindex < 0 || cindex >= kSc) continue;
+      const float cweight = __double2float_rn(
+          dmul((double)rweight, c == 0 ? dsub(1.0, (double)cfrac) : (double)cfrac));
+      const int rcindex = (rindex * kSc + cindex) << 3;
+      for (int ort = 0; ort < 2; ++ort) {
+        int oindex = oi + ort;
+        if (oindex >= kSOri) oindex = 0;
+        const float oweight = __double2float_rn(
+            dmul((double)cweight, ort == 0 ? dsub(1.0, (double)ofrac) : (double)ofrac));
+        index[rcindex + oindex] = fadd(index[rcindex + oindex], oweight);
+      }
+    }
+  }
+}
+
+// KMANormalizeVect (ShapeDescriptor.cpp:26-39), lane 0.
+__device__ void normalize_vect(float *v) {
+  float sqlen = 0.f;
+  for (int i = 0; i < kShape; ++i) sqlen = fadd(sqlen, fmul(v[i], v[i]));
+  const float fac = __double2float_rn(__ddiv_rn(1.0, (double)__fsqrt_rn(sqlen)));
+  for (int i = 0; i < kShape; ++i) v[i] = fmul(v[i], fac);
+}
+
+__global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
+    const float *__restrict__ img, int h, int w, DescGrid g, const DescTables *__restrict__ tabs,
+    float *__restrict__ cells, uint8_t *__restrict__ valid) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  DescTables &T = *reinterpret_cast<DescTables *>(dsm);
+  WarpScratch *scratch = reinterpret_cast<WarpScratch *>(dsm + sizeof(DescTables));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  {
+    const int *src = reinterpret_cast<const int *>(tabs);
+    int *dst = reinterpret_cast<int *>(&T);
+    for (int i = threadIdx.x; i < (int)(sizeof(DescTables) / 4); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const int64_t cell = (int64_t)blockIdx.x * kDescWarps + warp;
+  if (cell >= (int64_t)g.nx * g.ny) return;  // uniform for the warp; no block barrier follows
+  WarpScratch &S = scratch[warp];
+  const int iy = (int)(cell / g.nx), ix = (int)(cell - (int64_t)iy * g.nx);
+  float *out = cells + cell * kShape;
+
+  // grid -> image position (partdetect_aux.cpp:133-142) and the inside test
+  const double x2 = dadd(g.min_x, dmul((double)ix, g.step));
+  const double y2 = dadd(g.min_y, dmul((double)iy, g.step));
+  const double px = dadd(dadd(0.0, dmul(x2, g.ax0)), dmul(y2, g.ay0));
+  const double py = dadd(dadd(0.0, dmul(x2, g.ax1)), dmul(y2, g.ay1));
+  if (!(px >= g.lo && px <= g.hi_x && py >= g.lo && py <= g.hi_y)) {
+    for (int k = lane; k < kShape; k += 32) out[k] = 0.f;
+    if (lane == 0) valid[cell] = 0;
+    return;
+  }
+  const float mx = __double2float_rn(px), my = __double2float_rn(py);
+
+  // (1) ImageContent::interpolate (ImageContent.cpp:658-727)
+  const int xim = w - 1, yim = h - 1;
+  for (int k = lane; k < kPP; k += 32) {
+    const int j = k / kP - kHalf, i = k - (k / kP) * kP - kHalf;
+    const float pxf = fadd(fadd(mx, fmul((float)i, g.v0x)), fmul((float)j, g.v0y));
+    const float pyf = fadd(fadd(my, fmul((float)i, g.v1x)), fmul((float)j, g.v1y));
+    const int ax = (int)floorf(pxf), ay = (int)floorf(pyf);
+    const float dx = fsub(pxf, (float)ax), dy = fsub(pyf, (float)ay);
+    float v = 0.f;
+    if (ax >= 0 && ay >= 0 && ax < xim && ay < yim) {
+      const float *r0 = img + (int64_t)ay * w + ax;
+      v = bilinear4(dx, dy, r0[0], r0[1], r0[w], r0[w + 1]);
+    } else if (ax < 0 && ay < 0) {
+      v = img[0];
+    } else if (ax >= xim && ay >= yim) {
+      v = img[(int64_t)yim * w + xim];
+    } else if (ax < 0 && ay > yim) {
+      v = img[(int64_t)yim * w];
+    } else if (ax >= xim && ay < 0) {
+      v = img[xim];
+    } else if (ax > xim && ay >= 0) {
+      v = img[(int64_t)ay * w + xim];
+    } else if (ax >= 0 && ay < 0) {
+      v = img[ax];
+    } else if (ax >= 0 && ay >= yim) {
+      v = img[(int64_t)yim * w + ax];
+    } else if (ax < 0 && ay >= 0) {
+      v = img[(int64_t)ay * w];
+    } else if (ax >= xim && ay >= 0) {
+      v = img[(int64_t)ay * w + xim];
+    }
+    S.patch[k] = v;
+  }
+  __syncwarp();
+
+  // (2) normalize: mean and deviation over the mask, in the reference's order
+  if (lane == 0) {
+    float sum = 0.f, gsum = 0.f;
+    for (int k = 0; k < kPP; ++k)
+      if (T.mask[k] > 0) {
+        sum = fadd(sum, S.patch[k]);
+        gsum = fadd(gsum, 1.f);
+      }
+    sum = __fdiv_rn(sum, gsum);
+    float var = 0.f;
+    for (int k = 0; k < kPP; ++k)
+      if (T.mask[k] > 0) {
+        const float d = fsub(sum, S.patch[k]);
+        var = fadd(var, fmul(d, d));
+      }
+    var = __fsqrt_rn(__fdiv_rn(var, gsum));
+    S.sum = sum;
+    S.fac = __double2float_rn(__ddiv_rn(50.0, (double)var));
+  }
+  __syncwarp();
+  {
+    const float sum = S.sum, fac = S.fac;
+    for (int k = lane; k < kPP; k += 32) {
+      float v = fadd(128.f, fmul(fac, fsub(S.patch[k], sum)));
+      if (v > 255) v = 255;
+      if (v < 0) v = 0;
+      S.patch[k] = v;
+    }
+  }
+  __syncwarp();
+
+  // (3) dX2 / dY2 (gauss_iir.cpp:1182-1225), magnitude and orientation
+  for (int k = lane; k < kPP; k += 32) {
+    const int y = k / kP, x = k - y * kP;
+    const bool in = y >= 1 && y < kP - 1 && x >= 1 && x < kP - 1;
+    const float ddx = in ? fsub(S.patch[k + 1], S.patch[k - 1]) : 0.f;
+    const float ddy = in ? fsub(S.patch[k + kP], S.patch[k - kP]) : 0.f;
+    S.dx[k] = ddx;
+    S.dy[k] = ddy;
+    S.grad[k] = __fsqrt_rn(fadd(fmul(ddx, ddx), fmul(ddy, ddy)));
+    S.ori[k] = atan2f(ddy, ddx);
+    S.edge[k] = 0.f;
+    S.tmp[k] = 0.f;
+  }
+  __syncwarp();
+
+  // (4) Canny: non-maximum suppression on all lanes ...
+  for (int k = lane; k < kPP; k += 32) {
+    const int j = k / kP, i = k - j * kP;
+    unsigned char st = 0;
+    if (j >= 1 && j < kP - 2 && i >= 1 && i < kP - 2) {
+      const float gv = S.grad[k];
+      if (!(gv < kLower)) {
+        const float ux = S.dx[k], uy = S.dy[k];
+        const float qx = __fdiv_rn(ux, gv), qy = __fdiv_rn(uy, gv);
+        const float g1 = get_value(S.grad, fadd((float)i, qx), fadd((float)j, qy));
+        const float g2 = get_value(S.grad, fsub((float)i, qx), fsub((float)j, qy));
+        if (gv <= g1 || gv <= g2) st = 0;
+        else if (gv > kHigher) st = 1;
+        else if (gv > kLower) st = 2;
+      }
+    }
+    S.state[k] = st;
+  }
+  __syncwarp();
+  // ... the raster scan with its order-dependent promotion and labels on lane 0
+  if (lane == 0) {
+    float nb = 1.f;
+    S.cor[0] = 0;
+    for (int j = 1; j < kP - 2; ++j)
+      for (int i = 1; i < kP - 2; ++i) {
+        const int k = j * kP + i;
+        const unsigned char st = S.state[k];
+        if (!st) continue;
+        if (st == 1) {
+          S.edge[k] = kColor;
+        } else if (S.edge[k - kP - 1] == kColor || S.edge[k - kP] == kColor ||
+                   S.edge[k - kP + 1] == kColor || S.edge[k - 1] == kColor) {
+          S.edge[k] = kColor;
+        } else if (S.tmp[k - kP - 1] > 0) {
+          S.tmp[k] = S.tmp[k - kP - 1];
+        } else if (S.tmp[k - kP] > 0) {
+          S.tmp[k] = S.tmp[k - kP];
+        } else if (S.tmp[k - kP + 1] > 0) {
+          S.tmp[k] = S.tmp[k - kP + 1];
+        } else if (S.tmp[k - 1] > 0) {
+          S.tmp[k] = S.tmp[k - 1];
+        } else if (S.tmp[k + 1] > 0) {
+          S.tmp[k] = S.tmp[k + 1];
+        } else {
+          S.tmp[k] = nb;
+          S.cor[(int)nb] = 0;
+          nb = fadd(nb, 1.f);
+        }
+      }
+  }
+  __syncwarp();
+  // labels touching an edge pixel (8-neighbourhood) join it
+  for (int k = lane; k < kPP; k += 32) {
+    const int j = k / kP, i = k - j * kP;
+    if (j < 1 || j > kP - 2 || i < 1 || i > kP - 2) continue;
+    const float *e = S.edge;
+    if (e[k - kP - 1] == kColor || e[k - kP] == kColor || e[k - kP + 1] == kColor ||
+        e[k - 1] == kColor || e[k + 1] == kColor || e[k + kP - 1] == kColor ||
+        e[k + kP] == kColor || e[k + kP + 1] == kColor)
+      S.cor[(int)S.tmp[k]] = 1;
+  }
+  __syncwarp();
+  for (int k = lane; k < kPP; k += 32) {
+    const int j = k / kP, i = k - j * kP;
+    if (j < 1 || j > kP - 2 || i < 1 || i > kP - 2) continue;
+    if (S.tmp[k] > 0 && S.cor[(int)S.tmp[k]] == 1) S.edge[k] = kColor;
+  }
+  __syncwarp();
+  for (int k = lane; k < kPP; k += 32) S.edge[k] = S.edge[k] > 0 ? S.grad[k] : 0.f;
+  for (int k = lane; k < kShape; k += 32) S.vec[k] = 0.f;
+  __syncwarp();
+
+  // (5) log-polar histogram (KMAcomputeShape's sampling loop, :209-237, and
+  // KMAAddLogPolSample, :126-164), the norms and the quantisation, lane 0
+  if (lane == 0) {
+    for (int i = -kHalf; i <= kHalf; ++i)
+      for (int j = -kHalf; j <= kHalf; ++j) {
+        const int t = (kHalf + j) * kP + (kHalf + i);  // patch_lcpos(iradius + j, iradius + i)
+        if (!T.inrange[t]) continue;
+        const int k = (kHalf + i) * kP + (kHalf + j);  // fel[r][c], r = iradius + i
+        const float e = S.edge[k];
+        if ((double)e < 1e-10) continue;
+        const float mag = fmul(T.mask[k], e);
+        float o = fsub(S.ori[k], 0.f);
+        while ((double)o > kPi) o = __double2float_rn(dsub((double)o, kPi));
+        while ((double)o < 0.0) o = __double2float_rn(dadd((double)o, kPi));
+        place(S.vec, mag, o, T.lr[t], T.lc[t]);
+      }
+    normalize_vect(S.vec);
+    bool changed = false;
+    for (int i = 0; i < kShape; ++i)
+      if (S.vec[i] > kMaxIndexVal) {
+        S.vec[i] = kMaxIndexVal;
+        changed = true;
+      }
+    if (changed) normalize_vect(S.vec);
+    for (int i = 0; i < kShape; ++i) {
+      const double s = dmul(512.0, (double)S.vec[i]);
+      // (int)(512.0 * v): a NaN (a patch without edges) truncates to INT_MIN on
+      // x86-64, where the reference runs
+      const int iv = (s != s) ? INT_MIN : (int)s;
+      S.vec[i] = (float)((255 < iv) ? 255 : iv);
+    }
+  }
+  __syncwarp();
+  for (int k = lane; k < kShape; k += 32) out[k] = S.vec[k];
+  if (lane == 0) valid[cell] = 1;
+}
+
+}  // namespace
+
+size_t desc_smem_bytes() { return sizeof(DescTables) + kDescWarps * sizeof(WarpScratch); }
+
+cudaError_t launch_shape_grid(const float *img, int h, int w, const DescGrid &g,
+                              const DescTables *tabs, float *cells, uint8_t *valid,
+                              cudaStream_t s) {
+  const int64_t n = (int64_t)g.nx * g.ny;
+  if (n <= 0) return cudaSuccess;
+  const size_t smem = desc_smem_bytes();
+  cudaFuncSetAttribute(k_shape_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_shape_grid<<<(unsigned)((n + kDescWarps - 1) / kDescWarps), 32 * kDescWarps, smem, s>>>(
+      img, h, w, g, tabs, cells, valid);
+  return cudaGetLastError();
+}
+
+}  // namespace pa

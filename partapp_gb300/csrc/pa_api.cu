@@ -1977,6 +1977,150 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
   return sync_ctx(ctx);
 }
 
+// ------------------------------------------------------------------------
+// SHAPEv5 descriptor grid (computeDescriptorGrid, partdetect_aux.cpp:77-190)
+// ------------------------------------------------------------------------
+namespace {
+
+// FeatureGrid(img_width, img_height, x_axis, y_axis, desc_step, _)
+// (libPartDetect/FeatureGrid.cpp:22-97): the image's bounding box in the
+// grid frame, from the 2 x 2 inverse of boost_math::inv (boost_math.hpp:103-110).
+bool feature_grid(int w, int h, const double *ax, const double *ay, double step, double *rect,
+                  int *nx, int *ny) {
+  const double m00 = ax[0], m01 = ay[0], m10 = ax[1], m11 = ay[1];
+  const double D = m00 * m11 - m10 * m01;
+  if (!(D != 0.0) || !std::isfinite(D)) return false;
+  const double t00 = m11 / D, t01 = -m01 / D, t10 = -m10 / D, t11 = m00 / D;
+  const double cx[4] = {0, (double)w, (double)w, 0}, cy[4] = {0, 0, (double)h, (double)h};
+  double mnx = 0, mxx = 0, mny = 0, mxy = 0;
+  for (int i = 0; i < 4; ++i) {
+    const double px = t00 * cx[i] + t01 * cy[i], py = t10 * cx[i] + t11 * cy[i];
+    if (i == 0) {
+      mnx = mxx = px;
+      mny = mxy = py;
+      continue;
+    }
+    if (mnx > px) mnx = px;
+    if (mxx < px) mxx = px;
+    if (mny > py) mny = py;
+    if (mxy < py) mxy = py;
+  }
+  rect[0] = mnx;
+  rect[1] = mxx;
+  rect[2] = mny;
+  rect[3] = mxy;
+  const double fx = std::floor(((mxx - mnx + 1) / step)) + 1;
+  const double fy = std::floor(((mxy - mny + 1) / step)) + 1;
+  if (!(fx >= 1 && fy >= 1 && fx * fy <= (double)(1 << 28))) return false;
+  *nx = (int)fx;
+  *ny = (int)fy;
+  return true;
+}
+
+// initPatchMask(21) (FeatureDescriptor.cpp:118-137) and precompute_patch_idx
+// (ShapeDescriptor.cpp:42-64) with the reference's float / double types.
+void patch_tables(DescTables &t) {
+  constexpr int P = 21, center = P >> 1;
+  constexpr double m2pi = 6.2831853072;  // M_2PI, libKMA2/gauss_iir/gauss_iir.h:21
+  std::memset(&t, 0, sizeof t);
+  const float radius = center * center;
+  const float sigma = 0.9 * radius;
+  for (int i = 0; i < P; ++i)
+    for (int j = 0; j < P; ++j) {
+      const float disq = (i - center) * (i - center) + (j - center) * (j - center);
+      t.mask[j * P + i] = disq < radius ? std::exp(-disq / sigma) : 0.f;
+    }
+  const float cspacing = 4 / (m2pi);  // ScSize / M_2PI
+  for (int i = -center; i <= center; ++i)
+    for (int j = -center; j <= center; ++j) {
+      const double lcpos = (M_PI + std::atan2((double)i, (double)j)) * cspacing;
+      const double lrpos = std::log(1 + std::sqrt((float)i * i + j * j) / center) * 3;  // SrSize
+      const int k = (center + j) * P + (center + i);
+      t.lc[k] = (float)lcpos;
+      t.lr[k] = (float)lrpos;
+      t.inrange[k] = (lrpos > -1.0 && lrpos < (float)3 && lcpos > -1.0 && lcpos < (float)4) ? 1 : 0;
+    }
+}
+
+}  // namespace
+
+pa_status pa_feature_grid_size(int img_w, int img_h, const double *x_axis, const double *y_axis,
+                               double desc_step, int *nx, int *ny) {
+  if (img_w < 1 || img_h < 1 || !x_axis || !y_axis || !nx || !ny || !(desc_step > 0))
+    return PA_ERR_INVALID;
+  double rect[4];
+  return feature_grid(img_w, img_h, x_axis, y_axis, desc_step, rect, nx, ny) ? PA_OK
+                                                                              : PA_ERR_INVALID;
+}
+
+pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img_w,
+                             const double *x_axis, const double *y_axis, double desc_step,
+                             int desc_size, float *cells, uint8_t *valid, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!image || !cells || !valid || !x_axis || !y_axis || img_h < 2 || img_w < 2 ||
+      !(desc_step > 0) || desc_size < 0 || img_h > 65535 || img_w > 65535)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  DescGrid g;
+  double rect[4];
+  if (!feature_grid(img_w, img_h, x_axis, y_axis, desc_step, rect, &g.nx, &g.ny))
+    return fail(ctx, PA_ERR_INVALID, "degenerate grid axes or step");
+  // patch_scale = (2 * desc_size + 1) / (float)PATCH_SIZE (partdetect_aux.cpp:88)
+  const double patch_scale = (2 * desc_size + 1) / (float)21;
+  if (patch_scale > 1.0)
+    return fail(ctx, PA_ERR_UNSUPPORTED,
+                "desc_size > 10 needs the pre-smoothed source image (gauss_iir smooth)");
+  g.min_x = rect[0];
+  g.min_y = rect[2];
+  g.step = desc_step;
+  g.ax0 = x_axis[0];
+  g.ax1 = x_axis[1];
+  g.ay0 = y_axis[0];
+  g.ay1 = y_axis[1];
+  // imgpos >= desc_size + 1 and imgpos <= x() - (desc_size + 1) in unsigned arithmetic
+  g.lo = (double)(desc_size + 1);
+  g.hi_x = (double)((unsigned)img_w - (unsigned)(desc_size + 1));
+  g.hi_y = (double)((unsigned)img_h - (unsigned)(desc_size + 1));
+  g.v0x = (float)(patch_scale * x_axis[0]);
+  g.v0y = (float)(patch_scale * y_axis[0]);
+  g.v1x = (float)(patch_scale * x_axis[1]);
+  g.v1y = (float)(patch_scale * y_axis[1]);
+  DescTables tabs;
+  patch_tables(tabs);
+  DeviceGuard dg(ctx->device);
+  const size_t npx = (size_t)img_h * img_w, ncell = (size_t)g.nx * g.ny;
+  auto plan = [&](Builder &b, const DescTables **t, const float **din, float **dout,
+                  uint8_t **vout) {
+    *t = b.param(&tabs, 1);
+    *din = mem == PA_MEM_HOST ? b.scratch<float>(npx) : image;
+    *dout = mem == PA_MEM_HOST ? b.scratch<float>(ncell * 96) : cells;
+    *vout = mem == PA_MEM_HOST ? b.scratch<uint8_t>(ncell) : valid;
+  };
+  Builder b1;
+  const DescTables *t = nullptr;
+  const float *din = nullptr;
+  float *dout = nullptr;
+  uint8_t *vout = nullptr;
+  plan(b1, &t, &din, &dout, &vout);
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  b.base = ctx->arena;
+  plan(b, &t, &din, &dout, &vout);
+  if ((st = upload_blob(ctx, b))) return st;
+  if (mem == PA_MEM_HOST)
+    if ((st = copy_in(ctx, (void *)din, image, npx * sizeof(float), mem))) return st;
+  PA_LAUNCH("shape_grid", launch_shape_grid(din, img_h, img_w, g, t, dout, vout, ctx->stream));
+  if (mem == PA_MEM_HOST) {
+    PA_CK(cudaMemcpyAsync(cells, dout, ncell * 96 * sizeof(float), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+    PA_CK(cudaMemcpyAsync(valid, vout, ncell, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  return sync_ctx(ctx);
+}
+
 pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
                                 const float *cells, const uint8_t *valid, int n_fields, int ny,
                                 int nx, int dc, int gx, int gy, double grid_step, int normalize,

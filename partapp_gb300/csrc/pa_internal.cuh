@@ -68,6 +68,27 @@ struct StumpPart {
 };
 
 // ---------------------------------------------------------------------------
+// SHAPEv5 descriptor grid (k_desc.cu): the per-patch tables and the rotated
+// grid of one computeDescriptorGrid call.
+// ---------------------------------------------------------------------------
+struct DescTables {
+  float mask[441];            // initPatchMask(21)
+  float lc[441], lr[441];     // (float) precompute_patch_idx, [iradius + j][iradius + i]
+  unsigned char inrange[444]; // rx > -1 && rx < 3 && cx > -1 && cx < 4 on the double values
+};
+struct DescGrid {
+  double min_x, min_y, step;            // rect.min_proj_x / min_proj_y, desc_step
+  double ax0, ax1, ay0, ay1;            // x_axis, y_axis
+  double lo, hi_x, hi_y;                // inside test bounds
+  float v0x, v0y, v1x, v1y;             // patch_scale * axes, as float
+  int nx, ny;
+};
+size_t desc_smem_bytes();
+cudaError_t launch_shape_grid(const float *img, int h, int w, const DescGrid &g,
+                              const DescTables *tabs, float *cells, uint8_t *valid,
+                              cudaStream_t s);
+
+// ---------------------------------------------------------------------------
 // Unary-map descriptor: one (part, rotation) score grid -> log map.
 // ---------------------------------------------------------------------------
 struct UnaryMap {
