@@ -156,9 +156,11 @@ pa_status pa_feature_grid_size(int img_w, int img_h, const double *x_axis, const
  * integers (int)(512 v) <= 255.  A patch without edges gives INT_MIN in all
  * 96 entries, as the reference's float -> int conversion does on x86-64.
  *   image [img_h][img_w] grey levels; cells [ny][nx][96]; valid [ny][nx]
- *   (0: position outside, its cell zero).  desc_size <= 10 (patch_scale <=
- *   1); larger sizes need the pre-smoothed source and give
- *   PA_ERR_UNSUPPORTED.  The cells feed pa_score_grids_window. */
+ *   (0: position outside, its cell zero).  For desc_size > 10 (patch scale
+ *   (2 desc_size + 1) / 21 > 1) the patches are sampled from the image
+ *   smoothed once by libKMA2's recursive Gaussian (gauss_iir.cpp:1391-1400)
+ *   with sigma = patch scale, as the reference does.  The cells feed
+ *   pa_score_grids_window. */
 pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img_w,
                              const double *x_axis, const double *y_axis, double desc_step,
                              int desc_size, float *cells, uint8_t *valid, int mem);

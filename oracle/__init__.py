@@ -378,6 +378,8 @@ def _desc_decl(L):
     L.orc_descriptor_grid.argtypes = [fp, C.c_int, C.c_int, dp, dp, C.c_double, C.c_int, fp,
                                       C.POINTER(C.c_uint8)]
     L.orc_descriptor_grid.restype = C.c_int
+    L.orc_smooth.argtypes = [fp, C.c_int, C.c_int, C.c_float, fp]
+    L.orc_smooth.restype = C.c_int
     L._desc_declared = True
     return L
 
@@ -432,3 +434,14 @@ def descriptor_grid(image, x_axis, y_axis, desc_step, desc_size):
     if rc:
         raise ValueError(f"orc_descriptor_grid failed: {rc}")
     return cells, valid
+
+
+def smooth(image, sigma):
+    """libKMA2's recursive Gaussian smooth(image, out, sigma): along y, then x."""
+    L = _desc_decl(lib())
+    img = np.ascontiguousarray(image, dtype=np.float32)
+    out = np.empty_like(img)
+    if L.orc_smooth(_p(img, C.c_float), img.shape[0], img.shape[1], float(sigma),
+                    _p(out, C.c_float)):
+        raise ValueError("orc_smooth needs an image of at least 5 x 5")
+    return out

@@ -208,9 +208,91 @@ void place(float *index, float mag, float ori, float rx, float cx) {
   }
 }
 
+/* set_nii_and_dii + set_smooth_coefficients, gauss_iir.cpp:47-120: the
+ * fourth-order recursive Gaussian (Deriche) of width sigma, in float. */
+void smooth_coefficients(float sigma, float *coefs) {
+  const float a0 = 1.68f, a1 = 3.735f, b0 = 1.783f, b1 = 1.723f, c0 = -0.6803f, c1 = -0.2598f,
+              omega0 = 0.6318f, omega1 = 1.997f;
+  coefs[0] = a0 + c0;
+  coefs[1] = std::exp(-b1 / sigma) * (c1 * std::sin(omega1 / sigma) - (c0 + 2 * a0) * std::cos(omega1 / sigma)) +
+             std::exp(-b0 / sigma) * (a1 * std::sin(omega0 / sigma) - (2 * c0 + a0) * std::cos(omega0 / sigma));
+  coefs[2] = 2 * std::exp(-b0 / sigma - b1 / sigma) *
+                 ((a0 + c0) * std::cos(omega1 / sigma) * std::cos(omega0 / sigma) -
+                  std::cos(omega1 / sigma) * a1 * std::sin(omega0 / sigma) -
+                  std::cos(omega0 / sigma) * c1 * std::sin(omega1 / sigma)) +
+             c0 * std::exp(-2 * b0 / sigma) + a0 * std::exp(-2 * b1 / sigma);
+  coefs[3] = std::exp(-b1 / sigma - 2 * b0 / sigma) * (c1 * std::sin(omega1 / sigma) - c0 * std::cos(omega1 / sigma)) +
+             std::exp(-b0 / sigma - 2 * b1 / sigma) * (a1 * std::sin(omega0 / sigma) - a0 * std::cos(omega0 / sigma));
+  coefs[8] = -2 * std::exp(-b1 / sigma) * std::cos(omega1 / sigma) - 2 * std::exp(-b0 / sigma) * std::cos(omega0 / sigma);
+  coefs[9] = 4 * std::cos(omega1 / sigma) * std::cos(omega0 / sigma) * std::exp(-b0 / sigma - b1 / sigma) +
+             std::exp(-2 * b1 / sigma) + std::exp(-2 * b0 / sigma);
+  coefs[10] = -2 * std::cos(omega0 / sigma) * std::exp(-b0 / sigma - 2 * b1 / sigma) -
+              2 * std::cos(omega1 / sigma) * std::exp(-b1 / sigma - 2 * b0 / sigma);
+  coefs[11] = std::exp(-2 * b0 / sigma - 2 * b1 / sigma);
+  coefs[12] = coefs[8];
+  coefs[13] = coefs[9];
+  coefs[14] = coefs[10];
+  coefs[15] = coefs[11];
+  coefs[4] = coefs[1] - coefs[8] * coefs[0];
+  coefs[5] = coefs[2] - coefs[9] * coefs[0];
+  coefs[6] = coefs[3] - coefs[10] * coefs[0];
+  coefs[7] = -coefs[11] * coefs[0];
+  coefs[16] = 1 / (std::sqrt(2 * 3.141) * sigma);
+}
+
+/* One recursive pass along a line of n samples at stride st (the body of
+ * horizontal() / vertical(), gauss_iir.cpp:197-420): causal y+, anticausal
+ * y-, out = (y+ + y-) * scale.  out may not alias in. */
+void iir_line(const float *in, float *out, int n, int st, const float *c) {
+  const float n00p = c[0], n11p = c[1], n22p = c[2], n33p = c[3], n11m = c[4], n22m = c[5],
+              n33m = c[6], n44m = c[7], d11p = c[8], d22p = c[9], d33p = c[10], d44p = c[11],
+              d11m = c[12], d22m = c[13], d33m = c[14], d44m = c[15], scale = c[16];
+  auto I = [&](int k) { return in[(size_t)k * st]; };
+  std::vector<float> p(n), m(n);
+  const float np = n00p + n11p + n22p + n33p;
+  const float dp = d11p + d22p + d33p + d44p;
+  float z = np / (1 + dp);
+  p[0] = z * I(0);
+  p[1] = n00p * I(1) + n11p * I(0) + n22p * I(0) + n33p * I(0) - dp * p[0];
+  p[2] = n00p * I(2) + n11p * I(1) + n22p * I(0) + n33p * I(0) - d11p * p[1] - d22p * p[0] -
+         d33p * p[0] - d44p * p[0];
+  p[3] = n00p * I(3) + n11p * I(2) + n22p * I(1) + n33p * I(0) - d11p * p[2] - d22p * p[1] -
+         d33p * p[0] - d44p * p[0];
+  for (int k = 4; k < n; ++k)
+    p[k] = n00p * I(k) + n11p * I(k - 1) + n22p * I(k - 2) + n33p * I(k - 3) - d11p * p[k - 1] -
+           d22p * p[k - 2] - d33p * p[k - 3] - d44p * p[k - 4];
+  const float nm = n11m + n22m + n33m + n44m;
+  const float dm = d11m + d22m + d33m + d44m;
+  z = nm / (1 + dm);
+  const int e = n - 1;
+  m[e] = z * I(e);
+  m[e - 1] = nm * I(e) - dm * m[e];
+  m[e - 2] = n11m * I(e - 1) + n22m * I(e) + n33m * I(e) + n44m * I(e) - d11m * m[e - 1] -
+             d22m * m[e] - d33m * m[e] - d44m * m[e];
+  m[e - 3] = n11m * I(e - 2) + n22m * I(e - 1) + n33m * I(e) + n44m * I(e) - d11m * m[e - 2] -
+             d22m * m[e - 1] - d33m * m[e] - d44m * m[e];
+  for (int k = n - 5; k >= 0; --k)
+    m[k] = n11m * I(k + 1) + n22m * I(k + 2) + n33m * I(k + 3) + n44m * I(k + 4) -
+           d11m * m[k + 1] - d22m * m[k + 2] - d33m * m[k + 3] - d44m * m[k + 4];
+  for (int k = 0; k < n; ++k) out[(size_t)k * st] = (p[k] + m[k]) * scale;
+}
+
 }  // namespace
 
 extern "C" {
+
+/* smooth(image_in, smooth_image, scale), gauss_iir.cpp:1391-1400: the
+ * recursive Gaussian along y (horizontal()) then along x (vertical()). */
+int orc_smooth(const float *in, int h, int w, float sigma, float *out) {
+  if (h < 5 || w < 5) return -1;
+  float c[17];
+  smooth_coefficients(sigma, c);
+  std::vector<float> tmp((size_t)h * w);
+  for (int x = 0; x < w; ++x) iir_line(in + x, tmp.data() + x, h, w, c);
+  for (int y = 0; y < h; ++y) iir_line(tmp.data() + (size_t)y * w, out + (size_t)y * w, w, 1, c);
+  return 0;
+}
+
 
 void orc_patch_tables(float *mask, double *lcpos, double *lrpos) {
   /* initPatchMask(PATCH_SIZE), FeatureDescriptor.cpp:118-137 */
@@ -328,11 +410,16 @@ int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *
   int nx = 0, ny = 0;
   orc_feature_grid(img_w, img_h, ax, ay, desc_step, rect, &nx, &ny);
   const double patch_scale = (2 * desc_size + 1) / (float)kPatch;
-  if (patch_scale > 1.0) return -2; /* the smoothed-source branch is not restated */
   float mask[kPatch * kPatch];
   double lc[kPatch * kPatch], lr[kPatch * kPatch];
   orc_patch_tables(mask, lc, lr);
-  const Img src{img_w, img_h, image};
+  /* smooth once for all descriptors if the patch is smaller than the window */
+  std::vector<float> smoothed;
+  if (patch_scale > 1.0) {
+    smoothed.resize((size_t)img_h * img_w);
+    if (orc_smooth(image, img_h, img_w, (float)patch_scale, smoothed.data())) return -2;
+  }
+  const Img src{img_w, img_h, patch_scale > 1.0 ? smoothed.data() : image};
   float patch[kPatch * kPatch];
   for (int iy = 0; iy < ny; ++iy)
     for (int ix = 0; ix < nx; ++ix) {

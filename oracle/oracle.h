@@ -207,10 +207,15 @@ void orc_shape_descriptor(const float *patch, float *vec);
 void orc_feature_grid(int img_w, int img_h, const double *x_axis, const double *y_axis,
                       double desc_step, double *rect, int *nx, int *ny);
 
+/* smooth(image_in, smooth_image, sigma) (libKMA2/gauss_iir/gauss_iir.cpp:
+ * 1391-1400): recursive Gaussian along y then x.  h, w >= 5. */
+int orc_smooth(const float *in, int h, int w, float sigma, float *out);
+
 /* computeDescriptorGrid with SHAPEv5 (libPartDetect/partdetect_aux.cpp:77-190)
  * on a grayscale image [img_h][img_w]: cells [ny][nx][96] (zero where the
- * descriptor window leaves the image), valid [ny][nx].  Returns 0, or -2 for
- * desc_size > 10 (the pre-smoothed source branch is not restated). */
+ * descriptor window leaves the image), valid [ny][nx].  For desc_size > 10
+ * the patches are sampled from the image smoothed once with sigma =
+ * patch_scale.  Returns 0. */
 int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *x_axis,
                         const double *y_axis, double desc_step, int desc_size, float *cells,
                         uint8_t *valid);

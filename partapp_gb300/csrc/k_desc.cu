@@ -342,7 +342,114 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
   if (lane == 0) valid[cell] = 1;
 }
 
+// One line of the recursive Gaussian (horizontal() / vertical(),
+// libKMA2/gauss_iir/gauss_iir.cpp:197-420): causal pass y+ stored in out,
+// anticausal pass y- folded in as out = (y+ + y-) * scale.  Every sum runs
+// left to right over rounded float products, as the reference's
+// expressions do.
+__device__ void iir_line(const float *__restrict__ in, float *__restrict__ out, int n, int st,
+                         const IirCoefs &cf) {
+  const float *c = cf.c;
+  const float n00p = c[0], n11p = c[1], n22p = c[2], n33p = c[3], n11m = c[4], n22m = c[5],
+              n33m = c[6], n44m = c[7], d11p = c[8], d22p = c[9], d33p = c[10], d44p = c[11],
+              d11m = c[12], d22m = c[13], d33m = c[14], d44m = c[15], scale = c[16];
+  auto I = [&](int k) { return in[(int64_t)k * st]; };
+  // a0*b0 + a1*b1 + a2*b2 + a3*b3 - e0*f0 - e1*f1 - e2*f2 - e3*f3
+  auto rec = [&](float a0, float b0, float a1, float b1, float a2, float b2, float a3, float b3,
+                 float e0, float f0, float e1, float f1, float e2, float f2, float e3, float f3) {
+    float t = fmul(a0, b0);
+    t = fadd(t, fmul(a1, b1));
+    t = fadd(t, fmul(a2, b2));
+    t = fadd(t, fmul(a3, b3));
+    t = fsub(t, fmul(e0, f0));
+    t = fsub(t, fmul(e1, f1));
+    t = fsub(t, fmul(e2, f2));
+    return fsub(t, fmul(e3, f3));
+  };
+  const float np = fadd(fadd(fadd(n00p, n11p), n22p), n33p);
+  const float dp = fadd(fadd(fadd(d11p, d22p), d33p), d44p);
+  float z = __fdiv_rn(np, fadd(1.f, dp));
+  const float i0 = I(0), i1 = I(1), i2 = I(2), i3 = I(3);
+  float p0 = fmul(z, i0);
+  float p1 = fsub(fadd(fadd(fadd(fmul(n00p, i1), fmul(n11p, i0)), fmul(n22p, i0)), fmul(n33p, i0)),
+                  fmul(dp, p0));
+  float p2 = rec(n00p, i2, n11p, i1, n22p, i0, n33p, i0, d11p, p1, d22p, p0, d33p, p0, d44p, p0);
+  float p3 = rec(n00p, i3, n11p, i2, n22p, i1, n33p, i0, d11p, p2, d22p, p1, d33p, p0, d44p, p0);
+  out[0] = p0;
+  out[(int64_t)st] = p1;
+  out[(int64_t)2 * st] = p2;
+  out[(int64_t)3 * st] = p3;
+  float a1 = i3, a2 = i2, a3 = i1;          // I(k-1), I(k-2), I(k-3)
+  float q1 = p3, q2 = p2, q3 = p1, q4 = p0;  // p(k-1) .. p(k-4)
+  for (int k = 4; k < n; ++k) {
+    const float ik = I(k);
+    const float pk = rec(n00p, ik, n11p, a1, n22p, a2, n33p, a3, d11p, q1, d22p, q2, d33p, q3,
+                         d44p, q4);
+    out[(int64_t)k * st] = pk;
+    a3 = a2;
+    a2 = a1;
+    a1 = ik;
+    q4 = q3;
+    q3 = q2;
+    q2 = q1;
+    q1 = pk;
+  }
+  const float nm = fadd(fadd(fadd(n11m, n22m), n33m), n44m);
+  const float dm = fadd(fadd(fadd(d11m, d22m), d33m), d44m);
+  z = __fdiv_rn(nm, fadd(1.f, dm));
+  const int e = n - 1;
+  const float ie = I(e), ie1 = I(e - 1), ie2 = I(e - 2), ie3 = I(e - 3);
+  const float m0 = fmul(z, ie);
+  const float m1 = fsub(fmul(nm, ie), fmul(dm, m0));
+  const float m2 = rec(n11m, ie1, n22m, ie, n33m, ie, n44m, ie, d11m, m1, d22m, m0, d33m, m0, d44m, m0);
+  const float m3 = rec(n11m, ie2, n22m, ie1, n33m, ie, n44m, ie, d11m, m2, d22m, m1, d33m, m0, d44m, m0);
+  auto fold = [&](int k, float m) {
+    float *o = out + (int64_t)k * st;
+    *o = fmul(fadd(*o, m), scale);
+  };
+  fold(e, m0);
+  fold(e - 1, m1);
+  fold(e - 2, m2);
+  fold(e - 3, m3);
+  float b1 = ie3, b2 = ie2, b3 = ie1, b4 = ie;  // I(k+1) .. I(k+4)
+  float r1 = m3, r2 = m2, r3 = m1, r4 = m0;     // m(k+1) .. m(k+4)
+  for (int k = n - 5; k >= 0; --k) {
+    const float mk = rec(n11m, b1, n22m, b2, n33m, b3, n44m, b4, d11m, r1, d22m, r2, d33m, r3,
+                         d44m, r4);
+    fold(k, mk);
+    b4 = b3;
+    b3 = b2;
+    b2 = b1;
+    b1 = I(k);
+    r4 = r3;
+    r3 = r2;
+    r2 = r1;
+    r1 = mk;
+  }
+}
+
+// smooth(): the recursive Gaussian along y (one thread per column) ...
+__global__ void k_iir_y(const float *__restrict__ in, float *__restrict__ out, int h, int w,
+                        IirCoefs cf) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < w) iir_line(in + x, out + x, h, w, cf);
+}
+// ... then along x (one thread per row)
+__global__ void k_iir_x(const float *__restrict__ in, float *__restrict__ out, int h, int w,
+                        IirCoefs cf) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  if (y < h) iir_line(in + (int64_t)y * w, out + (int64_t)y * w, w, 1, cf);
+}
+
 }  // namespace
+
+cudaError_t launch_smooth(const float *in, float *tmp, float *out, int h, int w,
+                          const IirCoefs &cf, cudaStream_t s) {
+  if (h < 5 || w < 5) return cudaErrorInvalidValue;
+  k_iir_y<<<(unsigned)((w + 127) / 128), 128, 0, s>>>(in, tmp, h, w, cf);
+  k_iir_x<<<(unsigned)((h + 127) / 128), 128, 0, s>>>(tmp, out, h, w, cf);
+  return cudaGetLastError();
+}
 
 size_t desc_smem_bytes() { return sizeof(DescTables) + kDescWarps * sizeof(WarpScratch); }
 

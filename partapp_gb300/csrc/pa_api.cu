@@ -2042,6 +2042,41 @@ void patch_tables(DescTables &t) {
     }
 }
 
+// set_nii_and_dii + set_smooth_coefficients (libKMA2/gauss_iir/gauss_iir.cpp:
+// 47-120): Deriche's fourth-order recursive Gaussian of width sigma, float.
+void smooth_coefficients(float sigma, float *coefs) {
+  const float a0 = 1.68f, a1 = 3.735f, b0 = 1.783f, b1 = 1.723f, c0 = -0.6803f, c1 = -0.2598f,
+              omega0 = 0.6318f, omega1 = 1.997f;
+  using std::cos;
+  using std::exp;
+  using std::sin;
+  coefs[0] = a0 + c0;
+  coefs[1] = exp(-b1 / sigma) * (c1 * sin(omega1 / sigma) - (c0 + 2 * a0) * cos(omega1 / sigma)) +
+             exp(-b0 / sigma) * (a1 * sin(omega0 / sigma) - (2 * c0 + a0) * cos(omega0 / sigma));
+  coefs[2] = 2 * exp(-b0 / sigma - b1 / sigma) *
+                 ((a0 + c0) * cos(omega1 / sigma) * cos(omega0 / sigma) -
+                  cos(omega1 / sigma) * a1 * sin(omega0 / sigma) -
+                  cos(omega0 / sigma) * c1 * sin(omega1 / sigma)) +
+             c0 * exp(-2 * b0 / sigma) + a0 * exp(-2 * b1 / sigma);
+  coefs[3] = exp(-b1 / sigma - 2 * b0 / sigma) * (c1 * sin(omega1 / sigma) - c0 * cos(omega1 / sigma)) +
+             exp(-b0 / sigma - 2 * b1 / sigma) * (a1 * sin(omega0 / sigma) - a0 * cos(omega0 / sigma));
+  coefs[8] = -2 * exp(-b1 / sigma) * cos(omega1 / sigma) - 2 * exp(-b0 / sigma) * cos(omega0 / sigma);
+  coefs[9] = 4 * cos(omega1 / sigma) * cos(omega0 / sigma) * exp(-b0 / sigma - b1 / sigma) +
+             exp(-2 * b1 / sigma) + exp(-2 * b0 / sigma);
+  coefs[10] = -2 * cos(omega0 / sigma) * exp(-b0 / sigma - 2 * b1 / sigma) -
+              2 * cos(omega1 / sigma) * exp(-b1 / sigma - 2 * b0 / sigma);
+  coefs[11] = exp(-2 * b0 / sigma - 2 * b1 / sigma);
+  coefs[12] = coefs[8];
+  coefs[13] = coefs[9];
+  coefs[14] = coefs[10];
+  coefs[15] = coefs[11];
+  coefs[4] = coefs[1] - coefs[8] * coefs[0];
+  coefs[5] = coefs[2] - coefs[9] * coefs[0];
+  coefs[6] = coefs[3] - coefs[10] * coefs[0];
+  coefs[7] = -coefs[11] * coefs[0];
+  coefs[16] = 1 / (std::sqrt(2 * 3.141) * sigma);
+}
+
 }  // namespace
 
 pa_status pa_feature_grid_size(int img_w, int img_h, const double *x_axis, const double *y_axis,
@@ -2065,11 +2100,15 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
   double rect[4];
   if (!feature_grid(img_w, img_h, x_axis, y_axis, desc_step, rect, &g.nx, &g.ny))
     return fail(ctx, PA_ERR_INVALID, "degenerate grid axes or step");
-  // patch_scale = (2 * desc_size + 1) / (float)PATCH_SIZE (partdetect_aux.cpp:88)
+  // patch_scale = (2 * desc_size + 1) / (float)PATCH_SIZE (partdetect_aux.cpp:88); a
+  // window wider than the patch samples the image smoothed once with sigma =
+  // patch_scale (:92-98)
   const double patch_scale = (2 * desc_size + 1) / (float)21;
-  if (patch_scale > 1.0)
-    return fail(ctx, PA_ERR_UNSUPPORTED,
-                "desc_size > 10 needs the pre-smoothed source image (gauss_iir smooth)");
+  const bool smooth = patch_scale > 1.0;
+  if (smooth && (img_h < 5 || img_w < 5))
+    return fail(ctx, PA_ERR_INVALID, "the smoothing filter needs images of at least 5 x 5");
+  IirCoefs cf;
+  if (smooth) smooth_coefficients((float)patch_scale, cf.c);
   g.min_x = rect[0];
   g.min_y = rect[2];
   g.step = desc_step;
@@ -2089,12 +2128,15 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
   patch_tables(tabs);
   DeviceGuard dg(ctx->device);
   const size_t npx = (size_t)img_h * img_w, ncell = (size_t)g.nx * g.ny;
+  float *sm_tmp = nullptr, *sm_out = nullptr;
   auto plan = [&](Builder &b, const DescTables **t, const float **din, float **dout,
                   uint8_t **vout) {
     *t = b.param(&tabs, 1);
     *din = mem == PA_MEM_HOST ? b.scratch<float>(npx) : image;
     *dout = mem == PA_MEM_HOST ? b.scratch<float>(ncell * 96) : cells;
     *vout = mem == PA_MEM_HOST ? b.scratch<uint8_t>(ncell) : valid;
+    sm_tmp = smooth ? b.scratch<float>(npx) : nullptr;
+    sm_out = smooth ? b.scratch<float>(npx) : nullptr;
   };
   Builder b1;
   const DescTables *t = nullptr;
@@ -2112,6 +2154,10 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
   if ((st = upload_blob(ctx, b))) return st;
   if (mem == PA_MEM_HOST)
     if ((st = copy_in(ctx, (void *)din, image, npx * sizeof(float), mem))) return st;
+  if (smooth) {
+    PA_LAUNCH_N("smooth", 2, launch_smooth(din, sm_tmp, sm_out, img_h, img_w, cf, ctx->stream));
+    din = sm_out;
+  }
   PA_LAUNCH("shape_grid", launch_shape_grid(din, img_h, img_w, g, t, dout, vout, ctx->stream));
   if (mem == PA_MEM_HOST) {
     PA_CK(cudaMemcpyAsync(cells, dout, ncell * 96 * sizeof(float), cudaMemcpyDeviceToHost,

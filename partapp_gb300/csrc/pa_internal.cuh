@@ -83,7 +83,12 @@ struct DescGrid {
   float v0x, v0y, v1x, v1y;             // patch_scale * axes, as float
   int nx, ny;
 };
+struct IirCoefs {
+  float c[17];  // set_smooth_coefficients order (gauss_iir.cpp:77-120)
+};
 size_t desc_smem_bytes();
+cudaError_t launch_smooth(const float *in, float *tmp, float *out, int h, int w,
+                          const IirCoefs &cf, cudaStream_t s);
 cudaError_t launch_shape_grid(const float *img, int h, int w, const DescGrid &g,
                               const DescTables *tabs, float *cells, uint8_t *valid,
                               cudaStream_t s);

@@ -96,10 +96,33 @@ def test_descriptor_grid_valid_positions(orc):
         assert ((v == INT_MIN) | ((v >= 0) & (v <= 255) & (v == np.round(v)))).all()
 
 
-def test_descriptor_grid_rejects_large_windows(orc):
+def test_recursive_gaussian_impulse_response(orc):
+    """smooth() (gauss_iir.cpp:1391-1400) is Deriche's recursive Gaussian:
+    away from the borders an impulse comes out as a separable bump close to
+    exp(-d^2 / (2 sigma^2)), with unit-order gain."""
+    sigma = 1.6
+    img = np.zeros((64, 64), np.float32)
+    img[32, 32] = 1.0
+    out = orc.smooth(img, sigma).astype(np.float64)
+    c = out[32, 32]
+    d = np.arange(-4, 5)
+    row = out[32, 32 + d] / c
+    assert np.abs(row - np.exp(-d**2 / (2 * sigma**2))).max() < 0.03
+    assert np.allclose(row, out[32 + d, 32] / c, atol=1e-5)  # same filter along y and x
+    sep = np.outer(out[:, 32], out[32, :]) / c
+    assert np.abs(out - sep).max() < 1e-6 * abs(c) + 1e-9
+    assert 0.9 < out.sum() < 1.1
+
+
+def test_large_windows_sample_the_smoothed_image(orc):
+    """desc_size > 10: patch_scale = (2 d + 1) / 21 > 1, the patches come from
+    the image smoothed with sigma = patch_scale (partdetect_aux.cpp:88-98)."""
+    img = grey_image(1, 48, 56)
     ax, ay = axes(0.0)
-    with pytest.raises(ValueError):
-        orc.descriptor_grid(grey_image(1, 40, 40), ax, ay, 4.0, 11)
+    cells, valid = orc.descriptor_grid(img, ax, ay, 4.0, 12)
+    assert valid.sum() > 0
+    v = cells[valid.astype(bool)]
+    assert ((v == INT_MIN) | ((v >= 0) & (v <= 255))).all()
 
 
 # --------------------------------------------------------------- GPU parity
@@ -159,13 +182,27 @@ def test_descriptor_grid_device_memory_and_smaller_window(ctx, orc):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("desc_size,deg", [(12, 20.0), (16, -60.0)])
+def test_descriptor_grid_smoothed_source(ctx, orc, desc_size, deg):
+    """Windows wider than the 21-pixel patch: the recursive Gaussian runs on
+    the GPU first; still bit-exact."""
+    img = grey_image(30 + desc_size, 96, 112)
+    ax, ay = axes(deg)
+    want, vw = orc.descriptor_grid(img, ax, ay, 4.0, desc_size)
+    got, vg = ctx.descriptor_grid(img, ax, ay, 4.0, desc_size)
+    frac, worst = _compare(got, want, vg, vw)
+    print(f"desc_size {desc_size}: {vw.sum()} cells, mismatching entries {frac:.2e}, max |d| {worst}")
+    assert frac == 0.0 and vw.sum() > 20
+
+
+@pytest.mark.gpu
 def test_descriptor_grid_errors(ctx, pa):
-    ax, ay = axes(0.0)
     with pytest.raises(pa.PaError) as ei:
-        ctx.descriptor_grid(grey_image(1, 40, 40), ax, ay, 4.0, 11)
-    assert ei.value.status == pa.PA_ERR_UNSUPPORTED
-    with pytest.raises(pa.PaError):
         ctx.descriptor_grid(grey_image(1, 40, 40), [0.0, 0.0], [0.0, 1.0], 4.0, 5)
+    assert ei.value.status == pa.PA_ERR_INVALID
+    with pytest.raises(pa.PaError) as ei:
+        ctx.descriptor_grid(grey_image(1, 40, 40), *axes(0.0), -1.0, 5)
+    assert ei.value.status == pa.PA_ERR_INVALID
 
 
 @pytest.mark.gpu
