@@ -49,7 +49,8 @@ def parse():
                     help="images per end-to-end call (host descriptors through the copy ring)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=1024, help="large-grid: H = W")
-    ap.add_argument("--workload", choices=["find_obj", "large-grid", "uneven"], default="find_obj",
+    ap.add_argument("--workload", choices=["find_obj", "large-grid", "uneven", "descriptors"],
+                    default="find_obj",
                     help="large-grid: the 1024x1024, 48-rotation PS (log-normal unaries, "
                          "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic; "
                          "uneven: images of random sizes (200-640 px) and rotation counts "
@@ -519,8 +520,105 @@ def run_uneven(args):
     ctx.close()
 
 
+def grey_image(seed, h, w):
+    """Seeded synthetic grey image: box-blurred noise plus straight step edges
+    (no image data set is available here)."""
+    rng = np.random.default_rng(seed)
+    img = rng.uniform(0, 255, (h + 4, w + 4))
+    c = np.cumsum(np.cumsum(img, 0), 1)
+    img = (c[4:, 4:] - c[:-4, 4:] - c[4:, :-4] + c[:-4, :-4]) / 16.0
+    yy, xx = np.mgrid[0:h, 0:w]
+    for _ in range(8):
+        a = rng.uniform(0, np.pi)
+        t = rng.uniform(0.2, 0.8) * (h * abs(np.sin(a)) + w * abs(np.cos(a)))
+        img = img + 60.0 * ((xx * np.cos(a) + yy * np.sin(a)) > t)
+    img = (img - img.min()) / (img.max() - img.min()) * 255.0
+    return img.astype(np.float32)
+
+
+def run_descriptors(args):
+    """SHAPEv5 descriptor grids of one 640 x 480 grey image at R = 24 rotations
+    (partdetect_dense's rotation loop, partdetect_test.cpp:171-192: desc_step 4,
+    desc_size 10 -> 21-pixel patches), image resident in HBM.  One step = the 24
+    grids of one image.  The oracle port times one rotation on one host core."""
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build
+
+    build.build()
+    dev = torch.device("cuda:0")
+    ctx = pa.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    Hh, Ww, Rr, step, dsz = 480, 640, 24, 4.0, 10
+    img = grey_image(args.seed, Hh, Ww)
+    img_d = torch.from_numpy(img).to(dev)
+    axes = []
+    for r in range(Rr):
+        a = np.deg2rad(-180.0 + 360.0 / Rr * (r + 0.5))
+        axes.append((np.array([np.cos(a), np.sin(a)]), np.array([-np.sin(a), np.cos(a)])))
+
+    def one_image():
+        n = 0
+        for ax, ay in axes:
+            cells, valid = ctx.descriptor_grid(img_d, ax, ay, step, dsz)
+            n += cells.shape[0] * cells.shape[1]
+        return n
+
+    for _ in range(max(3, args.warmup)):
+        n_pos = one_image()
+    torch.cuda.synchronize(dev)
+    steps = max(2, args.steps // 4)
+    ctx.reset_timing()
+    ctx.enable_timing(True)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for _ in range(steps):
+            one_image()
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    ctx.enable_timing(False)
+    ms = t0.elapsed_time(t1) / steps
+    kt = ctx.kernel_times()
+    cells, valid = ctx.descriptor_grid(img_d, axes[3][0], axes[3][1], step, dsz)
+    n_valid = int(valid.sum().item())
+    cpu = None
+    if args.cpu_baseline:
+        import time
+
+        import oracle
+
+        oracle.build()
+        t = time.perf_counter()
+        _, vw = oracle.descriptor_grid(img, axes[3][0], axes[3][1], step, dsz)
+        dt = time.perf_counter() - t
+        cpu = {"value": 1.0 / (dt * Rr), "unit": "images/s", "cores": 1, "kind": "port",
+               "sample": f"one of the 24 rotation grids ({int(vw.sum())} descriptors) on one "
+                         f"host core, {dt:.2f} s, scaled to 24 rotations"}
+    line = {"metric": "images/s (SHAPEv5 descriptor grids, 24 rotations)", "unit": "images/s",
+            "value": 1e3 / ms, "ms_per_step": ms, "n_gpus": 1, "steps": steps,
+            "warmup": max(3, args.warmup), "higher_is_better": True, "data": "synthetic",
+            "dtype": "f32/f64", "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": "computeDescriptorGrid SHAPEv5, 640x480 grey image, "
+                                   "R=24, desc_step 4, desc_size 10",
+                       "grid_positions_per_image": n_pos,
+                       "descriptors_per_rotation": n_valid},
+            "descriptors_per_s": n_valid * Rr * 1e3 / ms,
+            "kernels": {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[1] / steps}
+                        for k, v in kt.items()},
+            "cpu_baseline": cpu, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.workload == "descriptors":
+        run_descriptors(args)
+        return
     if args.workload == "large-grid":
         run_large_grid(args)
         return

@@ -37,6 +37,7 @@ constexpr float kColor = 255.f;       // EdgeDetector.cpp:79
 constexpr float kLower = 5.f, kHigher = 15.f;  // cannyEdges(dx, dy, grad, edge, 5, 15)
 constexpr double kPi = 3.14159265358979323846;
 constexpr int kDescWarps = 4;   // grid positions (one per warp) per CTA
+constexpr int kChunk = 160;     // histogram samples per increment batch (fits patch..grad)
 
 struct WarpScratch {
   float patch[kPP];
@@ -83,8 +84,10 @@ __device__ float get_value(const float *g, float x, float y) {
   return 0.f;
 }
 
-// KMAPlaceInLogPolIndex (ShapeDescriptor.cpp:71-121), orientation modulo pi.
-__device__ void place(float *index, float mag, float ori, float rx, float cx) {
+// KMAPlaceInLogPolIndex (ShapeDescriptor.cpp:71-121), orientation modulo pi:
+// the up to 8 (bin, weight) increments of one sample, in the reference's
+// r -> c -> orientation order (bin 255: no increment).
+__device__ void place_entries(float mag, float ori, float rx, float cx, uint8_t *bins, float *ws) {
   const float oval = __double2float_rn(__ddiv_rn((double)fmul((float)kSOri, ori), kPi));
   const int ri = (int)((rx >= 0.0f) ? (double)rx : dsub((double)rx, 1.0));
   const int ci = (int)((cx >= 0.0f) ? (double)cx : dsub((double)cx, 1.0));
@@ -92,22 +95,24 @@ __device__ void place(float *index, float mag, float ori, float rx, float cx) {
   const float rfrac = fsub(rx, (float)ri), cfrac = fsub(cx, (float)ci), ofrac = fsub(oval, (float)oi);
   for (int r = 0; r < 2; ++r) {
     const int rindex = ri + r;
-    if (rindex < 0 || rindex >= kSr) continue;
+    const bool rok = rindex >= 0 && rindex < kSr;
     const float rweight =
         __double2float_rn(dmul((double)mag, r == 0 ? dsub(1.0, (double)rfrac) : (double)rfrac));
     for (int c = 0; c < 2; ++c) {
       int cindex = ci + c;
       if (cindex >= kSc) cindex = 0;
-      if (cindex < 0 || cindex >= kSc) continue;
+      const bool cok = rok && cindex >= 0 && cindex < kSc;
       const float cweight = __double2float_rn(
           dmul((double)rweight, c == 0 ? dsub(1.0, (double)cfrac) : (double)cfrac));
       const int rcindex = (rindex * kSc + cindex) << 3;
       for (int ort = 0; ort < 2; ++ort) {
         int oindex = oi + ort;
         if (oindex >= kSOri) oindex = 0;
-        const float oweight = __double2float_rn(
-            dmul((double)cweight, ort == 0 ? dsub(1.0, (double)ofrac) : (double)ofrac));
-        index[rcindex + oindex] = fadd(index[rcindex + oindex], oweight);
+        const int e = (r * 2 + c) * 2 + ort;
+        bins[e] = cok ? (uint8_t)(rcindex + oindex) : (uint8_t)255;
+        ws[e] = cok ? __double2float_rn(dmul((double)cweight,
+                                             ort == 0 ? dsub(1.0, (double)ofrac) : (double)ofrac))
+                    : 0.f;
       }
     }
   }
@@ -252,15 +257,25 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
     S.state[k] = st;
   }
   __syncwarp();
-  // ... the raster scan with its order-dependent promotion and labels on lane 0
+  // ... the candidates in raster order (the patch buffer is free by now) ...
+  short *cand = reinterpret_cast<short *>(S.patch);
+  int ncand = 0;
+  for (int base = 0; base < kPP; base += 32) {
+    const int k = base + lane;
+    const bool c = k < kPP && S.state[k] != 0;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, c);
+    if (c) cand[ncand + __popc(m & ((1u << lane) - 1u))] = (short)k;
+    ncand += __popc(m);
+  }
+  __syncwarp();
+  // ... and the raster scan with its order-dependent promotion and labels on lane 0
   if (lane == 0) {
     float nb = 1.f;
     S.cor[0] = 0;
-    for (int j = 1; j < kP - 2; ++j)
-      for (int i = 1; i < kP - 2; ++i) {
-        const int k = j * kP + i;
+    for (int n = 0; n < ncand; ++n) {
+      const int k = cand[n];
+      {
         const unsigned char st = S.state[k];
-        if (!st) continue;
         if (st == 1) {
           S.edge[k] = kColor;
         } else if (S.edge[k - kP - 1] == kColor || S.edge[k - kP] == kColor ||
@@ -282,6 +297,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
           nb = fadd(nb, 1.f);
         }
       }
+    }
   }
   __syncwarp();
   // labels touching an edge pixel (8-neighbourhood) join it
@@ -302,25 +318,60 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
   }
   __syncwarp();
   for (int k = lane; k < kPP; k += 32) S.edge[k] = S.edge[k] > 0 ? S.grad[k] : 0.f;
-  for (int k = lane; k < kShape; k += 32) S.vec[k] = 0.f;
   __syncwarp();
 
   // (5) log-polar histogram (KMAcomputeShape's sampling loop, :209-237, and
-  // KMAAddLogPolSample, :126-164), the norms and the quantisation, lane 0
+  // KMAAddLogPolSample, :126-164).  The loop visits (i, j) with i outer, so
+  // its pixel k = (10 + i) * 21 + (10 + j) runs through 0..440 in order.
+  // (a) the samples that add to the histogram, in that order
+  short *list = reinterpret_cast<short *>(S.tmp);  // the labels are no longer needed
+  int nlist = 0;
+  for (int base = 0; base < kPP; base += 32) {
+    const int k = base + lane;
+    bool c = false;
+    if (k < kPP) {
+      const int i = k / kP - kHalf, j = k - (k / kP) * kP - kHalf;
+      c = T.inrange[(kHalf + j) * kP + (kHalf + i)] && !((double)S.edge[k] < 1e-10);
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, c);
+    if (c) list[nlist + __popc(m & ((1u << lane) - 1u))] = (short)k;
+    nlist += __popc(m);
+  }
+  __syncwarp();
+  // (b) chunks of samples: all lanes compute the increments (double
+  // arithmetic), then lane b accumulates bins b, b + 32, b + 64 in the
+  // reference's order
+  float *ws = S.patch;  // patch, dx, dy, grad: free, 4 * 441 floats
+  uint8_t *bins = reinterpret_cast<uint8_t *>(S.patch + kChunk * 8);
+  float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f;
+  for (int c0 = 0; c0 < nlist; c0 += kChunk) {
+    const int nc = min(kChunk, nlist - c0);
+    for (int n = lane; n < nc; n += 32) {
+      const int k = list[c0 + n];
+      const int i = k / kP - kHalf, j = k - (k / kP) * kP - kHalf;
+      const int t = (kHalf + j) * kP + (kHalf + i);  // patch_lcpos(iradius + j, iradius + i)
+      const float mag = fmul(T.mask[k], S.edge[k]);
+      float o = fsub(S.ori[k], 0.f);
+      while ((double)o > kPi) o = __double2float_rn(dsub((double)o, kPi));
+      while ((double)o < 0.0) o = __double2float_rn(dadd((double)o, kPi));
+      place_entries(mag, o, T.lr[t], T.lc[t], bins + n * 8, ws + n * 8);
+    }
+    __syncwarp();
+    for (int e = 0; e < nc * 8; ++e) {
+      const int b = bins[e];
+      const float wv = ws[e];
+      if (b == lane) acc0 = fadd(acc0, wv);
+      else if (b == lane + 32) acc1 = fadd(acc1, wv);
+      else if (b == lane + 64) acc2 = fadd(acc2, wv);
+    }
+    __syncwarp();
+  }
+  S.vec[lane] = acc0;
+  S.vec[lane + 32] = acc1;
+  S.vec[lane + 64] = acc2;
+  __syncwarp();
+  // (c) norms and quantisation, lane 0
   if (lane == 0) {
-    for (int i = -kHalf; i <= kHalf; ++i)
-      for (int j = -kHalf; j <= kHalf; ++j) {
-        const int t = (kHalf + j) * kP + (kHalf + i);  // patch_lcpos(iradius + j, iradius + i)
-        if (!T.inrange[t]) continue;
-        const int k = (kHalf + i) * kP + (kHalf + j);  // fel[r][c], r = iradius + i
-        const float e = S.edge[k];
-        if ((double)e < 1e-10) continue;
-        const float mag = fmul(T.mask[k], e);
-        float o = fsub(S.ori[k], 0.f);
-        while ((double)o > kPi) o = __double2float_rn(dsub((double)o, kPi));
-        while ((double)o < 0.0) o = __double2float_rn(dadd((double)o, kPi));
-        place(S.vec, mag, o, T.lr[t], T.lc[t]);
-      }
     normalize_vect(S.vec);
     bool changed = false;
     for (int i = 0; i < kShape; ++i)
