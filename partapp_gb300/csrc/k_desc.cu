@@ -36,6 +36,7 @@ constexpr float kMaxIndexVal = 0.2f;  // ShapeDescriptor.h:38
 constexpr float kColor = 255.f;       // EdgeDetector.cpp:79
 constexpr float kLower = 5.f, kHigher = 15.f;  // cannyEdges(dx, dy, grad, edge, 5, 15)
 constexpr double kPi = 3.14159265358979323846;
+constexpr float kPiAbove = 3.14159274101257324f;  // the float nearest pi, above it
 constexpr int kDescWarps = 4;   // grid positions (one per warp) per CTA
 constexpr int kChunk = 160;     // histogram samples per increment batch (fits patch..grad)
 
@@ -118,11 +119,15 @@ __device__ void place_entries(float mag, float ori, float rx, float cx, uint8_t 
   }
 }
 
-// KMANormalizeVect (ShapeDescriptor.cpp:26-39), lane 0.
+// KMANormalizeVect (ShapeDescriptor.cpp:26-39), lane 0.  fac = 1.0 / sqrt(sqlen)
+// divides in double and rounds to float; a quotient of two floats rounded
+// first to 53 and then to 24 bits equals the correctly rounded float quotient
+// (53 >= 2 * 24 + 2, Figueroa's double-rounding bound), so the float division
+// gives the same bits without the FP64 pipe.
 __device__ void normalize_vect(float *v) {
   float sqlen = 0.f;
   for (int i = 0; i < kShape; ++i) sqlen = fadd(sqlen, fmul(v[i], v[i]));
-  const float fac = __double2float_rn(__ddiv_rn(1.0, (double)__fsqrt_rn(sqlen)));
+  const float fac = __fdiv_rn(1.f, __fsqrt_rn(sqlen));
   for (int i = 0; i < kShape; ++i) v[i] = fmul(v[i], fac);
 }
 
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
       }
     var = __fsqrt_rn(__fdiv_rn(var, gsum));
     S.sum = sum;
-    S.fac = __double2float_rn(__ddiv_rn(50.0, (double)var));
+    S.fac = __fdiv_rn(50.f, var);  // 50.0 / var in double, rounded: the same bits (see normalize_vect)
   }
   __syncwarp();
   {
@@ -352,8 +357,9 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
       const int t = (kHalf + j) * kP + (kHalf + i);  // patch_lcpos(iradius + j, iradius + i)
       const float mag = fmul(T.mask[k], S.edge[k]);
       float o = fsub(S.ori[k], 0.f);
-      while ((double)o > kPi) o = __double2float_rn(dsub((double)o, kPi));
-      while ((double)o < 0.0) o = __double2float_rn(dadd((double)o, kPi));
+      // (double)o > pi  <=>  o >= the float just above pi
+      while (o >= kPiAbove) o = __double2float_rn(dsub((double)o, kPi));
+      while (o < 0.f) o = __double2float_rn(dadd((double)o, kPi));
       place_entries(mag, o, T.lr[t], T.lc[t], bins + n * 8, ws + n * 8);
     }
     __syncwarp();
@@ -381,9 +387,10 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
       }
     if (changed) normalize_vect(S.vec);
     for (int i = 0; i < kShape; ++i) {
-      const double s = dmul(512.0, (double)S.vec[i]);
-      // (int)(512.0 * v): a NaN (a patch without edges) truncates to INT_MIN on
-      // x86-64, where the reference runs
+      // (int)(512.0 * v): scaling by a power of two is exact in float too.  A
+      // NaN (a patch without edges) truncates to INT_MIN on x86-64, where the
+      // reference runs
+      const float s = fmul(512.f, S.vec[i]);
       const int iv = (s != s) ? INT_MIN : (int)s;
       S.vec[i] = (float)((255 < iv) ? 255 : iv);
     }
