@@ -165,6 +165,43 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
                              const double *x_axis, const double *y_axis, double desc_step,
                              int desc_size, float *cells, uint8_t *valid, int mem);
 
+/* AbcDetectorParam fields of the dense part detector
+ * (libPartDetect/AbcDetectorParam.proto:2-12). */
+typedef struct {
+  int desc_step;                 /* pixels between descriptors */
+  int desc_size;                 /* descriptor radius in pixels */
+  double window_desc_step_ratio; /* (0, 1]: window_step = ratio * desc_step (>= 1) */
+} pa_abc_param;
+
+/* PartWindowParam.part(p) fields a part detector's window uses
+ * (libPartDetect/PartWindowParam.proto:8-12): window size in pixels and the
+ * offset of the part position from the window's grid origin. */
+typedef struct {
+  int window_size_x, window_size_y;
+  double pos_offset_x, pos_offset_y;
+} pa_part_window;
+
+/* partdetect_dense (libPartDetect/partdetect_test.cpp:53-294) for one image
+ * and the in-memory path of findObjectDataset (force_recompute_scores,
+ * objectdetect_aux.cpp:376-384) up to the log unaries findObjectImageRotJoints
+ * builds (objectdetect_findrot.cpp:834-845): the image gets the mirrored
+ * border of add_image_border2 (ceil(desc_size + max_part_diag / 2) pixels);
+ * per rotation of `ep` the rotated FeatureGrid (step window_step), its SHAPEv5
+ * descriptor grid, every classifier's window scores (computeScoreGrid with
+ * bSqueeze and normalised votes: grid_x_count = window_size_x / desc_step +
+ * 1, likewise in y; grid_step = desc_step / window_step), the squeeze to the
+ * non-empty box, the TM_DIRECT map into the image by Tig = (Ti_ei Ti2)(T2g
+ * Tg4), then clip_scores_fill + computeLogGrid.  One scale (num_scale_steps
+ * 1); `flip` negates the grid's x axis (partdetect_test.cpp:181-184; the
+ * --find_obj path itself passes 0).  Classifier c needs dim = grid_x_count *
+ * grid_y_count * 96.
+ *   image      [img_h][img_w] grey levels
+ *   log_unary  [n_cls][R][img_h][img_w] */
+pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image, int img_h,
+                        int img_w, int flip, const pa_classifier *const *cls, int n_cls,
+                        const pa_part_window *windows, const pa_abc_param *abc,
+                        float *log_unary, int mem);
+
 /* computeScoreGrid over a grid of per-cell descriptors: each window vector is
  * the reverse-order concatenation of gx*gy cell descriptors taken every
  * round(k*grid_step) cells (FeatureGrid::concatenate,

@@ -380,6 +380,11 @@ def _desc_decl(L):
     L.orc_descriptor_grid.restype = C.c_int
     L.orc_smooth.argtypes = [fp, C.c_int, C.c_int, C.c_float, fp]
     L.orc_smooth.restype = C.c_int
+    L.orc_add_border.argtypes = [fp, C.c_int, C.c_int, C.c_int, fp]
+    L.orc_add_border.restype = C.c_int
+    L.orc_partdetect.argtypes = [C.c_void_p, C.c_void_p, ip, dp, C.c_int, C.c_int, C.c_double,
+                                 fp, C.c_int, C.c_int, C.c_int, fp]
+    L.orc_partdetect.restype = C.c_int
     L._desc_declared = True
     return L
 
@@ -444,4 +449,35 @@ def smooth(image, sigma):
     if L.orc_smooth(_p(img, C.c_float), img.shape[0], img.shape[1], float(sigma),
                     _p(out, C.c_float)):
         raise ValueError("orc_smooth needs an image of at least 5 x 5")
+    return out
+
+
+def add_border(image, b):
+    """add_image_border2: mirrored border; returns (bordered image, border used)."""
+    L = _desc_decl(lib())
+    img = np.ascontiguousarray(image, dtype=np.float32)
+    h, w = img.shape
+    bb = b if (b < w and b < h) else min(w, h) - 1
+    out = np.zeros((h + 2 * bb, w + 2 * bb), np.float32)
+    used = L.orc_add_border(_p(img, C.c_float), h, w, int(b), _p(out, C.c_float))
+    return out, used
+
+
+def partdetect(exp: OrcExp, models, windows, desc_step, desc_size, ratio, image, flip=False):
+    """partdetect_dense (one image, one scale, in-memory path) + clip/log:
+    windows = [(window_size_x, window_size_y, pos_offset_x, pos_offset_y)] per
+    classifier; returns log unaries [n][R][h][w]."""
+    L = _desc_decl(lib())
+    mh = _ModelsHolder(models)
+    n = mh.s.n_parts
+    img = np.ascontiguousarray(image, dtype=np.float32)
+    h, w = img.shape
+    ws = np.ascontiguousarray([[int(a[0]), int(a[1])] for a in windows], dtype=np.int32)
+    po = np.ascontiguousarray([[float(a[2]), float(a[3])] for a in windows], dtype=np.float64)
+    out = np.zeros((n, exp.num_rotation_steps, h, w), np.float32)
+    rc = L.orc_partdetect(C.addressof(exp), C.addressof(mh.s), _p(ws, C.c_int),
+                          _p(po, C.c_double), int(desc_step), int(desc_size), float(ratio),
+                          _p(img, C.c_float), h, w, int(bool(flip)), _p(out, C.c_float))
+    if rc:
+        raise ValueError(f"orc_partdetect failed: {rc}")
     return out

@@ -13,6 +13,7 @@
  * explicitly so that x86 and Arm hosts agree. */
 #include "oracle.h"
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdint>
@@ -28,6 +29,21 @@ constexpr int kShape = kSr * kSc * kSOri;
 constexpr float kMaxIndexVal = 0.2f;
 /* libKMA2/gauss_iir/gauss_iir.h:21 */
 constexpr double kM2Pi = 6.2831853072;
+
+/* num_scale_steps, scale_from_index(0) and rot_from_index
+ * (libPartApp/partapp_aux.hpp:45-58, 86-129), as oracle.cpp states them */
+int n_scales_desc(const orc_exp *e) { return e->num_scale_steps > 1 ? e->num_scale_steps : 1; }
+double scale_value(const orc_exp *e) {
+  if (e->min_object_scale == e->max_object_scale) return e->min_object_scale;
+  const double step = ((double)e->max_object_scale - e->min_object_scale) / 1.0;
+  return e->min_object_scale + step * 0.5;
+}
+double rot_value(const orc_exp *e, int idx) {
+  if (e->min_part_rotation == e->max_part_rotation) return e->min_part_rotation;
+  const double step = ((double)e->max_part_rotation - e->min_part_rotation) /
+                      (double)(unsigned)e->num_rotation_steps;
+  return e->min_part_rotation + step * (0.5 + idx);
+}
 
 struct Img {  /* DARY: fel[row][col], x() = columns, y() = rows */
   int w, h;
@@ -442,4 +458,146 @@ int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *
   return 0;
 }
 
+/* add_image_border2 (libKMA2/ImageContent/ImageContent.cpp:937-999): a
+ * mirrored border of b pixels (b reduced to min(w, h) - 1 when too wide). */
+int orc_add_border(const float *in, int h, int w, int b, float *out) {
+  if (!(b < w && b < h)) b = std::min(w, h) - 1;
+  const int W2 = w + 2 * b;
+  for (int ix = 0; ix < w; ++ix)
+    for (int iy = 0; iy < h; ++iy) out[(size_t)(b + iy) * W2 + b + ix] = in[(size_t)iy * w + ix];
+  const int bx2 = b + w, by1 = b + 1, by2 = b + h;
+  for (int bidx = 1; bidx <= b; ++bidx)
+    for (int yidx = by1; yidx <= by2; ++yidx) {
+      out[(size_t)(yidx - 1) * W2 + bidx - 1] = in[(size_t)(yidx - by1) * w + b - bidx];
+      out[(size_t)(yidx - 1) * W2 + bx2 + bidx - 1] = in[(size_t)(yidx - by1) * w + w - bidx];
+    }
+  for (int bidx = 1; bidx <= b; ++bidx)
+    for (int xidx = 0; xidx < W2; ++xidx) {
+      out[(size_t)(bidx - 1) * W2 + xidx] = out[(size_t)(by1 + b - bidx - 1) * W2 + xidx];
+      out[(size_t)(by2 + bidx - 1) * W2 + xidx] = out[(size_t)(by2 - bidx) * W2 + xidx];
+    }
+  return b;
+}
+
+}  // extern "C"
+
+namespace {
+
+/* hc::inverse (libBoostMath/homogeneous_coord.cpp:49-69) and the ublas 3 x 3
+ * product, as in oracle.cpp. */
+void hc_inv(const double *T, double *I) {
+  double D = T[0] * T[4] - T[3] * T[1];
+  I[0] = T[4] / D;
+  I[1] = -T[1] / D;
+  I[3] = -T[3] / D;
+  I[4] = T[0] / D;
+  double t0 = I[0] * T[2] + I[1] * T[5];
+  double t1 = I[3] * T[2] + I[4] * T[5];
+  I[2] = -t0;
+  I[5] = -t1;
+  I[6] = 0;
+  I[7] = 0;
+  I[8] = 1;
+}
+void mul3(const double *A, const double *B, double *Cm) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double t = 0;
+      for (int k = 0; k < 3; ++k) t += A[3 * i + k] * B[3 * k + j];
+      Cm[3 * i + j] = t;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+/* partdetect_dense for one image, one scale, in-memory path
+ * (libPartDetect/partdetect_test.cpp:53-294) followed by clip_scores_fill +
+ * computeLogGrid (objectdetect_findrot.cpp:834-845): see oracle.h. */
+int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size,
+                   const double *pos_offset, int desc_step0, int desc_size0, double ratio,
+                   const float *image, int h, int w, int flip, float *log_unary) {
+  if (n_scales_desc(e) != 1) return -1;
+  const double scale = scale_value(e);
+  const int R = e->num_rotation_steps, n = m->n_parts;
+  const double desc_step = scale * desc_step0;
+  const int desc_size = (int)std::floor(scale * desc_size0 + 0.5); /* boost_math::round */
+  double max_part_diag = 0;
+  for (int c = 0; c < n; ++c) {
+    const int wx = window_size[2 * c], wy = window_size[2 * c + 1];
+    const double d = std::sqrt((double)(wx * wx + wy * wy));
+    if (d > max_part_diag) max_part_diag = d;
+  }
+  int border = (int)std::ceil(desc_size + 0.5 * scale * max_part_diag);
+  const int b = (border < w && border < h) ? border : std::min(w, h) - 1;
+  const int eh = h + 2 * b, ew = w + 2 * b;
+  std::vector<float> ext((size_t)eh * ew);
+  orc_add_border(image, h, w, b, ext.data());
+  double window_step = ratio * desc_step;
+  if (window_step < 1) window_step = 1;
+  const double grid_step = desc_step / window_step;
+  const size_t HW = (size_t)h * w;
+  for (int r = 0; r < R; ++r) {
+    double rotation = rot_value(e, r);
+    rotation *= M_PI / 180.0;
+    double ax[2] = {std::cos(rotation), std::sin(rotation)};
+    const double ay[2] = {-std::sin(rotation), std::cos(rotation)};
+    if (flip) {
+      ax[0] = -ax[0];
+      ax[1] = -ax[1];
+    }
+    double rect[4];
+    int nx = 0, ny = 0;
+    orc_feature_grid(ew, eh, ax, ay, window_step, rect, &nx, &ny);
+    std::vector<float> cells((size_t)nx * ny * kShape);
+    std::vector<uint8_t> valid((size_t)nx * ny);
+    if (orc_descriptor_grid(ext.data(), eh, ew, ax, ay, window_step, desc_size, cells.data(),
+                            valid.data()))
+      return -2;
+    const double T32[9] = {1, 0, -rect[0], 0, 1, -rect[2], 0, 0, 1};
+    double T23[9];
+    hc_inv(T32, T23);
+    const double Ti2[9] = {ax[0], ay[0], 0, ax[1], ay[1], 0, 0, 0, 1};
+    const double Tie[9] = {1, 0, (double)-b, 0, 1, (double)-b, 0, 0, 1};
+    double Ti2e[9];
+    mul3(Tie, Ti2, Ti2e);
+    for (int c = 0; c < n; ++c) {
+      const int gx = window_size[2 * c] / desc_step0 + 1, gy = window_size[2 * c + 1] / desc_step0 + 1;
+      const size_t so = (size_t)c * m->n_stumps;
+      std::vector<float> grid((size_t)nx * ny);
+      orc_score_grid_window(m->f + so, m->p + so, m->theta + so, m->alpha + so, m->n_stumps,
+                            m->sum_alpha[c], cells.data(), valid.data(), ny, nx, kShape, gx, gy,
+                            grid_step, 1, grid.data());
+      /* computeScoreGrid's transforms, :379-403 */
+      double T3g[9] = {window_step, 0, 0, 0, window_step, 0, 0, 0, 1};
+      T3g[2] = scale * pos_offset[2 * c];
+      T3g[5] = scale * pos_offset[2 * c + 1];
+      double T2g[9];
+      mul3(T23, T3g, T2g);
+      /* squeezeScoreGrid, :407-449 */
+      int bb[4];
+      std::vector<float> sq = grid;
+      int sny = ny, snx = nx;
+      if (orc_squeeze_bbox(grid.data(), ny, nx, bb)) {
+        snx = bb[2] - bb[0] + 1;
+        sny = bb[3] - bb[1] + 1;
+        sq.assign((size_t)snx * sny, 0.f);
+        for (int y = 0; y < sny; ++y)
+          for (int x = 0; x < snx; ++x)
+            sq[(size_t)y * snx + x] = grid[(size_t)(y + bb[1]) * nx + x + bb[0]];
+        const double Tg4[9] = {1, 0, (double)bb[0], 0, 1, (double)bb[1], 0, 0, 1};
+        double M[9];
+        mul3(T2g, Tg4, M);
+        std::memcpy(T2g, M, sizeof M);
+      }
+      double Tig[9];
+      mul3(Ti2e, T2g, Tig);
+      float *out = log_unary + ((size_t)c * R + r) * HW;
+      orc_transform_grid(sq.data(), sny, snx, out, h, w, Tig, 0.f, 2);
+      orc_clip_log(out, (int64_t)HW);
+    }
+  }
+  return 0;
+}
 }  // extern "C"

@@ -220,6 +220,21 @@ int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *
                         const double *y_axis, double desc_step, int desc_size, float *cells,
                         uint8_t *valid);
 
+/* add_image_border2 (libKMA2/ImageContent/ImageContent.cpp:937-999): out is
+ * [h + 2b][w + 2b]; returns the border used (b, or min(w, h) - 1). */
+int orc_add_border(const float *in, int h, int w, int b, float *out);
+
+/* partdetect_dense for one image at one scale, in-memory path
+ * (libPartDetect/partdetect_test.cpp:53-294, as findObjectDataset's
+ * force_recompute_scores branch runs it), then clip_scores_fill +
+ * computeLogGrid: mirrored border, per rotation the rotated FeatureGrid, its
+ * SHAPEv5 descriptors, every classifier's window scores (window_size [n][2],
+ * grid_x_count = window_size_x / desc_step + 1), squeezeScoreGrid, TM_DIRECT
+ * into the image.  m->n_parts classifiers; log_unary [n][R][h][w]. */
+int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size,
+                   const double *pos_offset, int desc_step, int desc_size, double ratio,
+                   const float *image, int h, int w, int flip, float *log_unary);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,7 +45,7 @@ EXPORTS = (
     "pa_classifier_create", "pa_classifier_parse", "pa_classifier_destroy",
     "pa_classifier_info", "pa_score_grids", "pa_score_grids_window", "pa_unary_maps",
     "pa_ps_infer", "pa_rot_joint_marginal", "pa_rot_joint_marginal_noalloc", "pa_find_obj",
-    "pa_feature_grid_size", "pa_descriptor_grid",
+    "pa_feature_grid_size", "pa_descriptor_grid", "pa_partdetect",
     "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math", "pa_find_obj_multi",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
@@ -69,6 +69,16 @@ class ExpParam(C.Structure):
                 ("max_object_scale", C.c_float), ("strip_border_detections", C.c_float),
                 ("roi_save_num_samples", C.c_int), ("use_pairwise", C.c_int),
                 ("interpolate", C.c_int), ("num_scale_steps", C.c_int)]
+
+
+class AbcParam(C.Structure):
+    _fields_ = [("desc_step", C.c_int), ("desc_size", C.c_int),
+                ("window_desc_step_ratio", C.c_double)]
+
+
+class PartWindow(C.Structure):
+    _fields_ = [("window_size_x", C.c_int), ("window_size_y", C.c_int),
+                ("pos_offset_x", C.c_double), ("pos_offset_y", C.c_double)]
 
 
 class Stump(C.Structure):
@@ -136,6 +146,8 @@ def load_library():
     L.pa_ps_infer.argtypes = [vp, P(ExpParam), P(Tree), ip, ip, vp, ip, ip, P(PsOutputs), ip]
     L.pa_feature_grid_size.argtypes = [ip, ip, P(dp), P(dp), dp, P(ip), P(ip)]
     L.pa_descriptor_grid.argtypes = [vp, vp, ip, ip, P(dp), P(dp), dp, ip, vp, vp, ip]
+    L.pa_partdetect.argtypes = [vp, P(ExpParam), vp, ip, ip, ip, vp, ip, P(PartWindow),
+                                P(AbcParam), vp, ip]
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
                                         dp, dp, dp, ip, ip]
     L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip, ip]
@@ -371,6 +383,24 @@ class Context:
                                               float(desc_step), int(desc_size),
                                               _Buf(cells, np.float32).ptr, vptr, im.mem))
         return cells, valid
+
+    def partdetect(self, exp: ExpParam, image, cls_list, windows, desc_step, desc_size,
+                   ratio=1.0, flip=False):
+        """partdetect_dense + clip/log on one grey image [h][w] (numpy or CUDA
+        tensor): windows = [(window_size_x, window_size_y, pos_offset_x,
+        pos_offset_y)] per classifier; returns log unaries [n][R][h][w]."""
+        im = _Buf(image, np.float32)
+        h, w = im.arr.shape
+        n = len(cls_list)
+        R = exp.num_rotation_steps
+        wins = (PartWindow * n)(*[PartWindow(int(a[0]), int(a[1]), float(a[2]), float(a[3]))
+                                  for a in windows])
+        abc = AbcParam(int(desc_step), int(desc_size), float(ratio))
+        out = _empty_like_space((n, R, h, w), im.mem, im.arr)
+        self._check(self.L.pa_partdetect(self.h, C.byref(exp), im.ptr, h, w, int(bool(flip)),
+                                         self._cls_array(cls_list), n, wins, C.byref(abc),
+                                         _Buf(out, np.float32).ptr, im.mem))
+        return out
 
     # ---------------------------------------------------------- messages
     def rot_joint_marginal(self, exp: ExpParam, child, offset_c, offset_p, Cmat, rot_mean,

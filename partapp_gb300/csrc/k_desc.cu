@@ -499,7 +499,81 @@ __global__ void k_iir_x(const float *__restrict__ in, float *__restrict__ out, i
   if (y < h) iir_line(in + (int64_t)y * w, out + (int64_t)y * w, w, 1, cf);
 }
 
+// add_image_border2: copy, then mirrored columns left/right (rows b..b+h-1),
+// then mirrored rows top/bottom over the full width (from the padded image).
+__global__ void k_border_cols(const float *__restrict__ in, int h, int w, int b,
+                              float *__restrict__ out) {
+  const int W2 = w + 2 * b;
+  const int64_t n = (int64_t)h * W2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int yy = (int)(i / W2), xx = (int)(i - (int64_t)yy * W2);
+    int sx;
+    if (xx < b) sx = b - 1 - xx;                // out[.][bidx-1] = in[.][b-bidx]
+    else if (xx < b + w) sx = xx - b;
+    else sx = w - 1 - (xx - b - w);             // out[.][b+w+bidx-1] = in[.][w-bidx]
+    out[(int64_t)(b + yy) * W2 + xx] = in[(int64_t)yy * w + sx];
+  }
+}
+__global__ void k_border_rows(int h, int w, int b, float *__restrict__ out) {
+  const int W2 = w + 2 * b;
+  const int64_t n = (int64_t)2 * b * W2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i / W2), xx = (int)(i - (int64_t)k * W2);
+    if (k < b) {  // top row bidx - 1 = k from row 2b - 1 - k (inside the copied band)
+      out[(int64_t)k * W2 + xx] = out[(int64_t)(2 * b - 1 - k) * W2 + xx];
+    } else {      // bottom row b + h + j from row b + h - 1 - j
+      const int j = k - b;
+      out[(int64_t)(b + h + j) * W2 + xx] = out[(int64_t)(b + h - 1 - j) * W2 + xx];
+    }
+  }
+}
+
+__global__ void k_grid_bbox(const float *const *__restrict__ grids, int ny, int nx,
+                            int4 *__restrict__ bbox) {
+  __shared__ int mnx, mny, mxx, mxy;
+  if (threadIdx.x == 0) {
+    mnx = nx;
+    mny = ny;
+    mxx = -1;
+    mxy = -1;
+  }
+  __syncthreads();
+  const float *g = grids[blockIdx.x];
+  int a = nx, c = ny, d = -1, e = -1;
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x)
+    if (g[i] != kNoClassValue) {
+      const int y = i / nx, x = i - y * nx;
+      a = min(a, x);
+      c = min(c, y);
+      d = max(d, x);
+      e = max(e, y);
+    }
+  atomicMin(&mnx, a);
+  atomicMin(&mny, c);
+  atomicMax(&mxx, d);
+  atomicMax(&mxy, e);
+  __syncthreads();
+  if (threadIdx.x == 0) bbox[blockIdx.x] = make_int4(mnx, mny, mxx, mxy);
+}
+
 }  // namespace
+
+cudaError_t launch_mirror_border(const float *in, int h, int w, int b, float *out,
+                                 cudaStream_t s) {
+  if (b < 0 || b >= w || b >= h) return cudaErrorInvalidValue;
+  k_border_cols<<<608, 256, 0, s>>>(in, h, w, b, out);
+  if (b > 0) k_border_rows<<<152, 256, 0, s>>>(h, w, b, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grid_bbox(const float *const *grids, int n, int ny, int nx, int4 *bbox,
+                             cudaStream_t s) {
+  if (n < 1) return cudaSuccess;
+  k_grid_bbox<<<(unsigned)n, 256, 0, s>>>(grids, ny, nx, bbox);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_smooth(const float *in, float *tmp, float *out, int h, int w,
                           const IirCoefs &cf, cudaStream_t s) {

@@ -182,8 +182,9 @@ __global__ void __launch_bounds__(kThreads) k_unary_direct_scatter(const UnaryMa
       ix3 = m.colx[x1];
       iy3 = m.rowy[y1];
     } else {
-      const double x3 = __dadd_rn(__dadd_rn(__dmul_rn(m.T31[0], (double)x1), __dmul_rn(m.T31[1], (double)y1)), m.T31[2]);
-      const double y3 = __dadd_rn(__dadd_rn(__dmul_rn(m.T31[3], (double)x1), __dmul_rn(m.T31[4], (double)y1)), m.T31[5]);
+      const double xs = (double)(x1 - m.ox), ys = (double)(y1 - m.oy);
+      const double x3 = __dadd_rn(__dadd_rn(__dmul_rn(m.T31[0], xs), __dmul_rn(m.T31[1], ys)), m.T31[2]);
+      const double y3 = __dadd_rn(__dadd_rn(__dmul_rn(m.T31[3], xs), __dmul_rn(m.T31[4], ys)), m.T31[5]);
       ix3 = (int)floor(__dadd_rn(x3, 0.5));
       iy3 = (int)floor(__dadd_rn(y3, 0.5));
     }

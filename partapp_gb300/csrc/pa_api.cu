@@ -249,6 +249,30 @@ pa_status upload_blob(pa_ctx *ctx, const Builder &b) {
   return PA_OK;
 }
 
+// Host bytes -> a device location through the pinned staging ring and a copy
+// kernel (stream-ordered, no host synchronisation); bytes a multiple of 16.
+pa_status upload_to(pa_ctx *ctx, void *dst, const void *src, size_t bytes) {
+  if (!bytes) return PA_OK;
+  pa_ctx::Staging &sg = ctx->stage[ctx->stage_next];
+  ctx->stage_next = (ctx->stage_next + 1) % pa_ctx::kStages;
+  if (sg.done) PA_CK(cudaEventSynchronize(sg.done));
+  else PA_CK(cudaEventCreateWithFlags(&sg.done, cudaEventDisableTiming));
+  if (sg.cap < bytes) {
+    if (sg.p) cudaFreeHost(sg.p);
+    sg.p = nullptr;
+    sg.cap = 0;
+    if (cudaMallocHost(&sg.p, bytes + 4096) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes of pinned staging", bytes);
+    }
+    sg.cap = bytes + 4096;
+  }
+  std::memcpy(sg.p, src, bytes);
+  PA_LAUNCH("upload", launch_copy16(sg.p, dst, (int64_t)((bytes + 15) / 16), ctx->stream));
+  PA_CK(cudaEventRecord(sg.done, ctx->stream));
+  return PA_OK;
+}
+
 pa_status copy_in(pa_ctx *ctx, void *dst, const void *src, size_t bytes, int mem) {
   if (!bytes) return PA_OK;
   PA_CK(cudaMemcpyAsync(dst, src, bytes,
@@ -2164,6 +2188,247 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
                           ctx->stream));
     PA_CK(cudaMemcpyAsync(valid, vout, ncell, cudaMemcpyDeviceToHost, ctx->stream));
   }
+  return sync_ctx(ctx);
+}
+
+pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image, int img_h,
+                        int img_w, int flip, const pa_classifier *const *cls, int n_cls,
+                        const pa_part_window *windows, const pa_abc_param *abc,
+                        float *log_unary, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (n_scales(ep) != 1) return fail(ctx, PA_ERR_UNSUPPORTED, "one scale per call");
+  if (!image || !log_unary || !windows || !abc || img_h < 5 || img_w < 5 || img_h > 16384 ||
+      img_w > 16384 || abc->desc_step < 1 || abc->desc_size < 0 ||
+      !(abc->window_desc_step_ratio > 0 && abc->window_desc_step_ratio <= 1))
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes, parameters or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  if (!cls || n_cls < 1) return fail(ctx, PA_ERR_INVALID, "no classifiers");
+  const int R = ep->num_rotation_steps;
+  const double scale = scale_from_index(ep, 0);
+  // partdetect_dense, partdetect_test.cpp:116-165 (one scale)
+  const double desc_step = scale * abc->desc_step;
+  const int desc_size = (int)std::floor(scale * abc->desc_size + 0.5);  // boost_math::round
+  double max_part_diag = 0;
+  std::vector<int> gx(n_cls), gy(n_cls);
+  for (int c = 0; c < n_cls; ++c) {
+    if (!cls[c]) return fail(ctx, PA_ERR_INVALID, "classifier %d is NULL", c);
+    const pa_part_window &pw = windows[c];
+    if (pw.window_size_x < 0 || pw.window_size_y < 0)
+      return fail(ctx, PA_ERR_INVALID, "classifier %d: negative window size", c);
+    const double d = std::sqrt((double)pw.window_size_x * pw.window_size_x +
+                               (double)pw.window_size_y * pw.window_size_y);
+    if (d > max_part_diag) max_part_diag = d;
+    // get_window_feature_counts, partdetect_aux.cpp:245-250
+    gx[c] = pw.window_size_x / abc->desc_step + 1;
+    gy[c] = pw.window_size_y / abc->desc_step + 1;
+    if ((int64_t)gx[c] * gy[c] * 96 != cls[c]->dim)
+      return fail(ctx, PA_ERR_INVALID, "classifier %d has dim %d, its window needs %d x %d x 96",
+                  c, cls[c]->dim, gx[c], gy[c]);
+  }
+  int border = (int)std::ceil(desc_size + 0.5 * scale * max_part_diag);
+  if (!(border < img_w && border < img_h)) border = std::min(img_w, img_h) - 1;  // add_image_border2
+  const int eh = img_h + 2 * border, ew = img_w + 2 * border;
+  double window_step = abc->window_desc_step_ratio * desc_step;
+  if (window_step < 1) window_step = 1;
+  const double grid_step = desc_step / window_step;
+  // TM_DIRECT of a rotated grid into the image keeps the reference's result only
+  // when no two cells round to one pixel ("last write wins" has no parallel
+  // order); cells window_step apart never share a pixel when window_step > sqrt 2
+  if (!(window_step * window_step > 2.0))
+    return fail(ctx, PA_ERR_UNSUPPORTED,
+                "window step %.3f px: the rotated grid -> image map may collide", window_step);
+  // the rotated grids (partdetect_test.cpp:171-185)
+  struct Rot {
+    double ax[2], ay[2], rect[4];
+    int nx, ny;
+  };
+  std::vector<Rot> rots(R);
+  for (int r = 0; r < R; ++r) {
+    const double rotation = rot_from_index(ep, r) * (M_PI / 180.0);
+    Rot &q = rots[r];
+    q.ax[0] = std::cos(rotation);
+    q.ax[1] = std::sin(rotation);
+    q.ay[0] = -std::sin(rotation);
+    q.ay[1] = std::cos(rotation);
+    if (flip) {
+      q.ax[0] = -q.ax[0];
+      q.ax[1] = -q.ax[1];
+    }
+    if (!feature_grid(ew, eh, q.ax, q.ay, window_step, q.rect, &q.nx, &q.ny))
+      return fail(ctx, PA_ERR_INVALID, "rotation %d: degenerate grid", r);
+  }
+  const double patch_scale = (2 * desc_size + 1) / (float)21;
+  const bool smooth = patch_scale > 1.0;
+  IirCoefs cf;
+  if (smooth) smooth_coefficients((float)patch_scale, cf.c);
+  DescTables tabs;
+  patch_tables(tabs);
+  // classifier groups by window shape (one window gather + one score launch each)
+  std::vector<int> order(n_cls);
+  for (int c = 0; c < n_cls; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return gx[a] != gx[b] ? gx[a] < gx[b] : gy[a] < gy[b];
+  });
+  std::vector<std::pair<int, int>> groups;  // [first, end) in `order`
+  for (int k = 0; k < n_cls; ++k)
+    if (k == 0 || gx[order[k]] != gx[order[k - 1]] || gy[order[k]] != gy[order[k - 1]])
+      groups.push_back({k, k + 1});
+    else
+      groups.back().second = k + 1;
+  std::vector<const pa_classifier *> cls_sorted(n_cls);
+  for (int k = 0; k < n_cls; ++k) cls_sorted[k] = cls[order[k]];
+  size_t max_cells = 0, max_dense = 0, total_scores = 0;
+  std::vector<size_t> score_off(R);
+  for (int r = 0; r < R; ++r) {
+    const size_t G = (size_t)rots[r].nx * rots[r].ny;
+    max_cells = std::max(max_cells, G);
+    for (auto &g : groups)
+      max_dense = std::max(max_dense, G * (size_t)gx[order[g.first]] * gy[order[g.first]] * 96);
+    score_off[r] = total_scores;
+    total_scores += G * n_cls;
+  }
+  const size_t npx = (size_t)img_h * img_w, nepx = (size_t)eh * ew;
+  DeviceGuard dg(ctx->device);
+  struct Dev {
+    const DescTables *tabs;
+    StumpPart *sp;
+    const float *img;
+    float *ext, *sm_tmp, *sm_out, *cells, *dense, *scores, *out;
+    uint8_t *valid, *ok;
+    int4 *bbox;
+    const float **grid_ptrs;
+    UnaryMap *maps;
+  } d{};
+  std::vector<const float *> grid_ptrs((size_t)R * n_cls);
+  auto plan = [&](Builder &b) {
+    d.tabs = b.param(&tabs, 1);
+    d.sp = plan_stumps(b, cls_sorted.data(), n_cls);
+    d.img = mem == PA_MEM_HOST ? b.scratch<float>(npx) : image;
+    d.ext = b.scratch<float>(nepx);
+    d.sm_tmp = smooth ? b.scratch<float>(nepx) : nullptr;
+    d.sm_out = smooth ? b.scratch<float>(nepx) : nullptr;
+    d.cells = b.scratch<float>(max_cells * 96);
+    d.valid = b.scratch<uint8_t>(max_cells);
+    d.dense = b.scratch<float>(max_dense);
+    d.ok = b.scratch<uint8_t>(max_cells);
+    d.scores = b.scratch<float>(total_scores);
+    d.bbox = b.scratch<int4>((size_t)R * n_cls);
+    for (int r = 0; r < R; ++r)
+      for (int k = 0; k < n_cls; ++k)
+        grid_ptrs[(size_t)r * n_cls + k] =
+            b.dry ? nullptr : d.scores + score_off[r] + (size_t)k * rots[r].nx * rots[r].ny;
+    d.grid_ptrs = b.param(grid_ptrs.data(), grid_ptrs.size());
+    d.maps = b.scratch<UnaryMap>((size_t)R * n_cls + 1);  // + 1: the 16-byte copy tail
+    d.out = mem == PA_MEM_HOST ? b.scratch<float>((size_t)n_cls * R * npx) : log_unary;
+  };
+  Builder b1;
+  plan(b1);
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  b.base = ctx->arena;
+  plan(b);
+  if ((st = upload_blob(ctx, b))) return st;
+  cudaStream_t s = ctx->stream;
+  if (mem == PA_MEM_HOST)
+    if ((st = copy_in(ctx, (void *)d.img, image, npx * sizeof(float), mem))) return st;
+  PA_LAUNCH_N("border", border > 0 ? 2 : 1, launch_mirror_border(d.img, img_h, img_w, border, d.ext, s));
+  const float *src = d.ext;
+  if (smooth) {
+    PA_LAUNCH_N("smooth", 2, launch_smooth(d.ext, d.sm_tmp, d.sm_out, eh, ew, cf, s));
+    src = d.sm_out;
+  }
+  const std::vector<char> ff = fast_flags(cls_sorted.data(), n_cls);
+  const std::vector<int> ns = stump_counts(cls_sorted.data(), n_cls);
+  for (int r = 0; r < R; ++r) {
+    const Rot &q = rots[r];
+    DescGrid g;
+    g.min_x = q.rect[0];
+    g.min_y = q.rect[2];
+    g.step = window_step;
+    g.ax0 = q.ax[0];
+    g.ax1 = q.ax[1];
+    g.ay0 = q.ay[0];
+    g.ay1 = q.ay[1];
+    g.lo = (double)(desc_size + 1);
+    g.hi_x = (double)((unsigned)ew - (unsigned)(desc_size + 1));
+    g.hi_y = (double)((unsigned)eh - (unsigned)(desc_size + 1));
+    g.v0x = (float)(patch_scale * q.ax[0]);
+    g.v0y = (float)(patch_scale * q.ay[0]);
+    g.v1x = (float)(patch_scale * q.ax[1]);
+    g.v1y = (float)(patch_scale * q.ay[1]);
+    g.nx = q.nx;
+    g.ny = q.ny;
+    PA_LAUNCH("shape_grid", launch_shape_grid(src, eh, ew, g, d.tabs, d.cells, d.valid, s));
+    const int64_t G = (int64_t)q.nx * q.ny;
+    for (auto &grp : groups) {
+      const int c0 = order[grp.first], n = grp.second - grp.first;
+      const int D = gx[c0] * gy[c0] * 96;
+      PA_LAUNCH("window_gather", launch_window_gather(d.cells, d.valid, 1, q.ny, q.nx, 96, gx[c0],
+                                                      gy[c0], grid_step, d.dense, d.ok, s));
+      float *sc = d.scores + score_off[r] + (size_t)grp.first * G;
+      PA_LAUNCH("score_grids",
+                launch_score_grids(d.sp + grp.first, (const bool *)ff.data() + grp.first,
+                                   ns.data() + grp.first, n, d.dense, nullptr, false, G, 1, D, 1,
+                                   sc, s));
+      PA_LAUNCH("mask_no_class", launch_mask_no_class(sc, d.ok, n, G, s));
+    }
+    PA_LAUNCH("grid_bbox", launch_grid_bbox(d.grid_ptrs + (size_t)r * n_cls, n_cls, q.ny, q.nx,
+                                            d.bbox + (size_t)r * n_cls, s));
+  }
+  std::vector<int4> bbox((size_t)R * n_cls);
+  PA_CK(cudaMemcpyAsync(bbox.data(), d.bbox, bbox.size() * sizeof(int4), cudaMemcpyDeviceToHost, s));
+  if ((st = sync_ctx(ctx))) return st;
+  // computeScoreGrid's transforms (partdetect_test.cpp:379-403), squeezeScoreGrid
+  // (:407-449) and Tig = (Ti_ei Ti2)(T2g Tg4) (:205-213, 272-283), host double
+  std::vector<UnaryMap> maps((size_t)R * n_cls);
+  for (int r = 0; r < R; ++r) {
+    const Rot &q = rots[r];
+    const double T32[9] = {1, 0, -q.rect[0], 0, 1, -q.rect[2], 0, 0, 1};
+    double T23[9];
+    hc_inverse(T32, T23);
+    const double Ti2[9] = {q.ax[0], q.ay[0], 0, q.ax[1], q.ay[1], 0, 0, 0, 1};
+    const double Tie[9] = {1, 0, (double)-border, 0, 1, (double)-border, 0, 0, 1};
+    double Ti2e[9];
+    prod3(Tie, Ti2, Ti2e);
+    for (int k = 0; k < n_cls; ++k) {
+      const int c = order[k];
+      const pa_part_window &pw = windows[c];
+      double T3g[9] = {window_step, 0, 0, 0, window_step, 0, 0, 0, 1};
+      T3g[2] = scale * pw.pos_offset_x;
+      T3g[5] = scale * pw.pos_offset_y;
+      double T2g[9], Tig[9];
+      prod3(T23, T3g, T2g);
+      const int4 bb = bbox[(size_t)r * n_cls + k];
+      int ox = 0, oy = 0;
+      if (bb.z > bb.x && bb.w > bb.y) {  // maxx > minx && maxy > miny
+        const double Tg4[9] = {1, 0, (double)bb.x, 0, 1, (double)bb.y, 0, 0, 1};
+        double M[9];
+        prod3(T2g, Tg4, M);
+        std::memcpy(T2g, M, sizeof M);
+        ox = bb.x;
+        oy = bb.y;
+      }
+      prod3(Ti2e, T2g, Tig);
+      UnaryMap &m = maps[(size_t)r * n_cls + k];
+      std::memset(&m, 0, sizeof m);
+      m.grid = grid_ptrs[(size_t)r * n_cls + k];
+      m.out = d.out + ((size_t)c * R + r) * npx;
+      for (int t = 0; t < 6; ++t) m.T31[t] = Tig[t];
+      m.ox = ox;
+      m.oy = oy;
+    }
+  }
+  if ((st = upload_to(ctx, d.maps, maps.data(), maps.size() * sizeof(UnaryMap)))) return st;
+  for (int r = 0; r < R; ++r)
+    PA_LAUNCH_N("unary_maps", 2, launch_unary_maps(d.maps + (size_t)r * n_cls, n_cls, rots[r].ny,
+                                                   rots[r].nx, img_h, img_w, 1, 0, s));
+  if (mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(log_unary, d.out, (size_t)n_cls * R * npx * sizeof(float),
+                          cudaMemcpyDeviceToHost, s));
   return sync_ctx(ctx);
 }
 

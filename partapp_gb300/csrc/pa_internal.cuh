@@ -87,6 +87,12 @@ struct IirCoefs {
   float c[17];  // set_smooth_coefficients order (gauss_iir.cpp:77-120)
 };
 size_t desc_smem_bytes();
+// add_image_border2 (libKMA2/ImageContent/ImageContent.cpp:937-999): mirrored border of b pixels
+cudaError_t launch_mirror_border(const float *in, int h, int w, int b, float *out, cudaStream_t s);
+// squeezeScoreGrid's box (partdetect_test.cpp:407-431): per grid {minx, miny, maxx, maxy} of
+// the cells != NO_CLASS_VALUE; grids[g] is [ny][nx]
+cudaError_t launch_grid_bbox(const float *const *grids, int n, int ny, int nx, int4 *bbox,
+                             cudaStream_t s);
 cudaError_t launch_smooth(const float *in, float *tmp, float *out, int h, int w,
                           const IirCoefs &cf, cudaStream_t s);
 cudaError_t launch_shape_grid(const float *img, int h, int w, const DescGrid &g,
@@ -109,6 +115,7 @@ struct UnaryMap {
   int masked_all;        // upright part and this rotation is not kept
   int strip;             // root border strip width in pixels (0 if none)
   int *max_slot;         // fkey of max over the part's masked map
+  int ox, oy;            // general DIRECT path: T31 applies to (x1 - ox, y1 - oy)
 };
 
 // ---------------------------------------------------------------------------
