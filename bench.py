@@ -49,7 +49,8 @@ def parse():
                     help="images per end-to-end call (host descriptors through the copy ring)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=1024, help="large-grid: H = W")
-    ap.add_argument("--workload", choices=["find_obj", "large-grid", "uneven", "descriptors"],
+    ap.add_argument("--workload", choices=["find_obj", "large-grid", "uneven", "descriptors",
+                                           "from-images"],
                     default="find_obj",
                     help="large-grid: the 1024x1024, 48-rotation PS (log-normal unaries, "
                          "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic; "
@@ -626,8 +627,91 @@ def run_descriptors(args):
     ctx.close()
 
 
+def run_from_images(args):
+    """--find_obj from a grey image: pa_partdetect (mirrored border, 24 rotated
+    SHAPEv5 grids, 22 classifiers over 2 x 5-cell windows = 960-d, squeeze,
+    TM_DIRECT into the image, clip/log) then pa_ps_infer over the first 10
+    classifiers' unaries (10-part PS, bIsSparse = 1).  640 x 480 image resident
+    in HBM.  The oracle port times the partdetect of one rotation on one host
+    core."""
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build, synth
+
+    build.build()
+    dev = torch.device("cuda:0")
+    ctx = pa.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    Hh, Ww, Rr = 480, 640, 24
+    img = grey_image(args.seed, Hh, Ww)
+    img_d = torch.from_numpy(img).to(dev)
+    rng = np.random.default_rng(args.seed)
+    n_cls = 22
+    models = dict(f=rng.integers(0, 960, (n_cls, N_STUMPS)).astype(np.int32),
+                  p=np.where(rng.random((n_cls, N_STUMPS)) < 0.5, -1.0, 1.0).astype(np.float32),
+                  theta=rng.uniform(0, 60, (n_cls, N_STUMPS)).astype(np.float32),
+                  alpha=rng.uniform(0, 1, (n_cls, N_STUMPS)).astype(np.float32), D=960)
+    cls = ctx.classifiers(models)
+    windows = [(4, 16, 2.0, 8.0)] * n_cls
+    tree = synth.make_tree(rng, R=Rr, offset_range=(10.0, 60.0), sigma_range=(2.0, 12.0))
+    e = pa.exp_param(R=Rr, interpolate=False)
+
+    def one_image():
+        lu = ctx.partdetect(e, img_d, cls, windows, 4, 10, 1.0)
+        return ctx.compute_root_posterior_rot(e, tree, lu[:P], want_marg=True, is_sparse=True)
+
+    for _ in range(max(2, min(args.warmup, 3))):
+        one_image()
+    torch.cuda.synchronize(dev)
+    steps = max(2, args.steps // 8)
+    ctx.reset_timing()
+    ctx.enable_timing(True)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for _ in range(steps):
+            one_image()
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    ctx.enable_timing(False)
+    ms = t0.elapsed_time(t1) / steps
+    kt = ctx.kernel_times()
+    cpu = None
+    if args.cpu_baseline:
+        import time
+
+        import oracle
+
+        oracle.build()
+        e1 = oracle.make_exp(R=1, min_rot=-15.0, max_rot=15.0)  # one rotation (0 deg)
+        t = time.perf_counter()
+        oracle.partdetect(e1, models, windows, 4, 10, 1.0, img)
+        dt = time.perf_counter() - t
+        cpu = {"value": 1.0 / (dt * Rr), "unit": "images/s", "cores": 1, "kind": "port",
+               "sample": f"partdetect_dense of one rotation (22 classifiers) on one host core, "
+                         f"{dt:.2f} s, scaled to 24 rotations; the PS is not included"}
+    line = {"metric": "images/s (grey image -> unaries -> PS marginals)", "unit": "images/s",
+            "value": 1e3 / ms, "ms_per_step": ms, "n_gpus": 1, "steps": steps,
+            "warmup": max(2, min(args.warmup, 3)), "higher_is_better": True,
+            "data": "synthetic", "dtype": "f32/f64", "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": "partdetect_dense + computeRootPosteriorRot, 640x480 grey "
+                                   "image, R=24, desc_step 4, desc_size 10, 22 classifiers x "
+                                   "500 stumps over 2x5-cell windows, 10-part PS"},
+            "kernels": {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[1] / steps}
+                        for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
+            "cpu_baseline": cpu, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.workload == "from-images":
+        run_from_images(args)
+        return
     if args.workload == "descriptors":
         run_descriptors(args)
         return

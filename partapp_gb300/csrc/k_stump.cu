@@ -100,6 +100,49 @@ __global__ void k_window_gather(const float *__restrict__ cells, const uint8_t *
   }
 }
 
+// The same gather with 16-byte copies, one warp per window (dc % 4 == 0 and
+// 16-byte aligned cells and windows): the window's cells are copied by all
+// lanes at once; the cell offsets round(k * grid_step) come from a table.
+struct CellOffsets {
+  int2 o[64];  // (round(kx * grid_step), round(ky * grid_step)) for k = ky * gx + kx
+};
+
+__global__ void __launch_bounds__(256) k_window_gather4(
+    const float4 *__restrict__ cells, const uint8_t *__restrict__ valid, int n_fields, int ny,
+    int nx, int dc4, int gx, int gy, const CellOffsets offs_t, int last_ix, int last_iy,
+    float4 *__restrict__ dense, uint8_t *__restrict__ ok) {
+  const int2 *offs = offs_t.o;
+  const int lane = threadIdx.x & 31;
+  const int K = gx * gy, D4 = K * dc4;
+  const int64_t n_win = (int64_t)n_fields * ny * nx;
+  const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t win = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); win < n_win;
+       win += wstride) {
+    const int field = (int)(win / ((int64_t)ny * nx));
+    const int rem = (int)(win - (int64_t)field * ny * nx);
+    const int iy = rem / nx, ix = rem - (rem / nx) * nx;
+    bool good = ix <= last_ix && iy <= last_iy;
+    if (good) {
+      bool mine = true;
+      for (int k = lane; k < K; k += 32)
+        mine = mine && valid[((int64_t)field * ny + iy + offs[k].y) * nx + ix + offs[k].x] != 0;
+      good = __all_sync(0xFFFFFFFFu, mine);
+    }
+    float4 *out = dense + win * D4;
+    if (lane == 0) ok[win] = good ? 1 : 0;
+    if (!good) {
+      for (int j = lane; j < D4; j += 32) out[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    for (int j = lane; j < D4; j += 32) {
+      const int k = j / dc4, o = j - (j / dc4) * dc4;
+      const float4 *cell =
+          cells + (((int64_t)field * ny + iy + offs[k].y) * nx + ix + offs[k].x) * dc4;
+      out[(int64_t)(K - 1 - k) * dc4 + o] = __ldg(cell + o);
+    }
+  }
+}
+
 __global__ void k_mask_no_class(float *__restrict__ scores, const uint8_t *__restrict__ ok,
                                 int64_t n_per_part, int n_parts) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -300,6 +343,21 @@ cudaError_t launch_window_gather(const float *cells, const uint8_t *valid, int n
                                  uint8_t *ok, cudaStream_t s) {
   const int last_ix = nx - (int)floor(grid_step * (gx - 1) + 0.5) - 1;
   const int last_iy = ny - (int)floor(grid_step * (gy - 1) + 0.5) - 1;
+  const int K = gx * gy;
+  if (dc % 4 == 0 && K <= 64 && ((uintptr_t)cells & 15) == 0 && ((uintptr_t)dense & 15) == 0) {
+    CellOffsets t;
+    for (int k = 0; k < K; ++k) {
+      const int ky = k / gx, kx = k - ky * gx;
+      t.o[k] = make_int2((int)floor(kx * grid_step + 0.5), (int)floor(ky * grid_step + 0.5));
+    }
+    const int64_t n_win = (int64_t)n_fields * ny * nx;
+    int64_t blocks = (n_win + 7) / 8;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_window_gather4<<<(unsigned)blocks, 256, 0, s>>>(
+        reinterpret_cast<const float4 *>(cells), valid, n_fields, ny, nx, dc / 4, gx, gy, t,
+        last_ix, last_iy, reinterpret_cast<float4 *>(dense), ok);
+    return cudaGetLastError();
+  }
   dim3 grid((unsigned)(nx < 64 ? nx : 64), (unsigned)ny, (unsigned)n_fields);
   k_window_gather<<<grid, 128, 0, s>>>(cells, valid, ny, nx, dc, gx, gy, grid_step, last_ix,
                                        last_iy, dense, ok);
