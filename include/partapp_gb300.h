@@ -191,12 +191,14 @@ typedef struct {
  * bSqueeze and normalised votes: grid_x_count = window_size_x / desc_step +
  * 1, likewise in y; grid_step = desc_step / window_step), the squeeze to the
  * non-empty box, the TM_DIRECT map into the image by Tig = (Ti_ei Ti2)(T2g
- * Tg4), then clip_scores_fill + computeLogGrid.  One scale (num_scale_steps
- * 1); `flip` negates the grid's x axis (partdetect_test.cpp:181-184; the
- * --find_obj path itself passes 0).  Classifier c needs dim = grid_x_count *
- * grid_y_count * 96.
+ * Tg4), then clip_scores_fill + computeLogGrid.  Every one of the
+ * num_scale_steps = S scales has its own descriptor step and size
+ * (scale * desc_step, round(scale * desc_size)), border and grids (the scale
+ * loop, :116); the result feeds pa_ps_infer unchanged.  `flip` negates the
+ * grid's x axis (partdetect_test.cpp:181-184; the --find_obj path itself
+ * passes 0).  Classifier c needs dim = grid_x_count * grid_y_count * 96.
  *   image      [img_h][img_w] grey levels
- *   log_unary  [n_cls][R][img_h][img_w] */
+ *   log_unary  [n_cls][S][R][img_h][img_w] */
 pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image, int img_h,
                         int img_w, int flip, const pa_classifier *const *cls, int n_cls,
                         const pa_part_window *windows, const pa_abc_param *abc,

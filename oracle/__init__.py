@@ -464,9 +464,10 @@ def add_border(image, b):
 
 
 def partdetect(exp: OrcExp, models, windows, desc_step, desc_size, ratio, image, flip=False):
-    """partdetect_dense (one image, one scale, in-memory path) + clip/log:
-    windows = [(window_size_x, window_size_y, pos_offset_x, pos_offset_y)] per
-    classifier; returns log unaries [n][R][h][w]."""
+    """partdetect_dense (one image, in-memory path) + clip/log: windows =
+    [(window_size_x, window_size_y, pos_offset_x, pos_offset_y)] per
+    classifier; returns log unaries [n][R][h][w], or [n][S][R][h][w] for
+    num_scale_steps = S > 1."""
     L = _desc_decl(lib())
     mh = _ModelsHolder(models)
     n = mh.s.n_parts
@@ -474,10 +475,11 @@ def partdetect(exp: OrcExp, models, windows, desc_step, desc_size, ratio, image,
     h, w = img.shape
     ws = np.ascontiguousarray([[int(a[0]), int(a[1])] for a in windows], dtype=np.int32)
     po = np.ascontiguousarray([[float(a[2]), float(a[3])] for a in windows], dtype=np.float64)
-    out = np.zeros((n, exp.num_rotation_steps, h, w), np.float32)
+    S = max(1, exp.num_scale_steps)
+    out = np.zeros((n, S, exp.num_rotation_steps, h, w), np.float32)
     rc = L.orc_partdetect(C.addressof(exp), C.addressof(mh.s), _p(ws, C.c_int),
                           _p(po, C.c_double), int(desc_step), int(desc_size), float(ratio),
                           _p(img, C.c_float), h, w, int(bool(flip)), _p(out, C.c_float))
     if rc:
         raise ValueError(f"orc_partdetect failed: {rc}")
-    return out
+    return out if S > 1 else out[:, 0]

@@ -33,10 +33,10 @@ constexpr double kM2Pi = 6.2831853072;
 /* num_scale_steps, scale_from_index(0) and rot_from_index
  * (libPartApp/partapp_aux.hpp:45-58, 86-129), as oracle.cpp states them */
 int n_scales_desc(const orc_exp *e) { return e->num_scale_steps > 1 ? e->num_scale_steps : 1; }
-double scale_value(const orc_exp *e) {
+double scale_value(const orc_exp *e, int idx) {
   if (e->min_object_scale == e->max_object_scale) return e->min_object_scale;
-  const double step = ((double)e->max_object_scale - e->min_object_scale) / 1.0;
-  return e->min_object_scale + step * 0.5;
+  const double step = ((double)e->max_object_scale - e->min_object_scale) / n_scales_desc(e);
+  return e->min_object_scale + step * (0.5 + idx);
 }
 double rot_value(const orc_exp *e, int idx) {
   if (e->min_part_rotation == e->max_part_rotation) return e->min_part_rotation;
@@ -499,6 +499,10 @@ void hc_inv(const double *T, double *I) {
   I[7] = 0;
   I[8] = 1;
 }
+int partdetect_scale(const orc_exp *e, int si, const orc_models *m, const int *window_size,
+                     const double *pos_offset, int desc_step0, int desc_size0, double ratio,
+                     const float *image, int h, int w, int flip, float *log_unary);
+
 void mul3(const double *A, const double *B, double *Cm) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
@@ -518,8 +522,27 @@ extern "C" {
 int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size,
                    const double *pos_offset, int desc_step0, int desc_size0, double ratio,
                    const float *image, int h, int w, int flip, float *log_unary) {
-  if (n_scales_desc(e) != 1) return -1;
-  const double scale = scale_value(e);
+  const int S = n_scales_desc(e);
+  if (S > 1 && e->min_object_scale == e->max_object_scale) return -1;
+  for (int si = 0; si < S; ++si) {
+    const int rc = partdetect_scale(e, si, m, window_size, pos_offset, desc_step0, desc_size0,
+                                    ratio, image, h, w, flip, log_unary);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+/* one scale of partdetect_dense: log unaries of scale si into
+ * log_unary [n][S][R][h][w] */
+int partdetect_scale(const orc_exp *e, int si, const orc_models *m, const int *window_size,
+                     const double *pos_offset, int desc_step0, int desc_size0, double ratio,
+                     const float *image, int h, int w, int flip, float *log_unary) {
+  const int S = n_scales_desc(e);
+  const double scale = scale_value(e, si);
   const int R = e->num_rotation_steps, n = m->n_parts;
   const double desc_step = scale * desc_step0;
   const int desc_size = (int)std::floor(scale * desc_size0 + 0.5); /* boost_math::round */
@@ -593,11 +616,12 @@ int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size
       }
       double Tig[9];
       mul3(Ti2e, T2g, Tig);
-      float *out = log_unary + ((size_t)c * R + r) * HW;
+      float *out = log_unary + (((size_t)c * S + si) * R + r) * HW;
       orc_transform_grid(sq.data(), sny, snx, out, h, w, Tig, 0.f, 2);
       orc_clip_log(out, (int64_t)HW);
     }
   }
   return 0;
 }
-}  // extern "C"
+
+}  // namespace

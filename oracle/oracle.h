@@ -230,7 +230,8 @@ int orc_add_border(const float *in, int h, int w, int b, float *out);
  * computeLogGrid: mirrored border, per rotation the rotated FeatureGrid, its
  * SHAPEv5 descriptors, every classifier's window scores (window_size [n][2],
  * grid_x_count = window_size_x / desc_step + 1), squeezeScoreGrid, TM_DIRECT
- * into the image.  m->n_parts classifiers; log_unary [n][R][h][w]. */
+ * into the image, for each of the num_scale_steps = S scales (the scale loop,
+ * :116).  m->n_parts classifiers; log_unary [n][S][R][h][w]. */
 int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size,
                    const double *pos_offset, int desc_step, int desc_size, double ratio,
                    const float *image, int h, int w, int flip, float *log_unary);

@@ -388,15 +388,17 @@ class Context:
                    ratio=1.0, flip=False):
         """partdetect_dense + clip/log on one grey image [h][w] (numpy or CUDA
         tensor): windows = [(window_size_x, window_size_y, pos_offset_x,
-        pos_offset_y)] per classifier; returns log unaries [n][R][h][w]."""
+        pos_offset_y)] per classifier; returns log unaries [n][R][h][w], or
+        [n][S][R][h][w] for num_scale_steps = S > 1."""
         im = _Buf(image, np.float32)
         h, w = im.arr.shape
         n = len(cls_list)
         R = exp.num_rotation_steps
+        S = max(1, exp.num_scale_steps)
         wins = (PartWindow * n)(*[PartWindow(int(a[0]), int(a[1]), float(a[2]), float(a[3]))
                                   for a in windows])
         abc = AbcParam(int(desc_step), int(desc_size), float(ratio))
-        out = _empty_like_space((n, R, h, w), im.mem, im.arr)
+        out = _empty_like_space((n, S, R, h, w) if S > 1 else (n, R, h, w), im.mem, im.arr)
         self._check(self.L.pa_partdetect(self.h, C.byref(exp), im.ptr, h, w, int(bool(flip)),
                                          self._cls_array(cls_list), n, wins, C.byref(abc),
                                          _Buf(out, np.float32).ptr, im.mem))

@@ -2191,22 +2191,16 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
   return sync_ctx(ctx);
 }
 
-pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image, int img_h,
-                        int img_w, int flip, const pa_classifier *const *cls, int n_cls,
-                        const pa_part_window *windows, const pa_abc_param *abc,
-                        float *log_unary, int mem) {
-  if (!ctx) return PA_ERR_INVALID;
-  if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
-  if (n_scales(ep) != 1) return fail(ctx, PA_ERR_UNSUPPORTED, "one scale per call");
-  if (!image || !log_unary || !windows || !abc || img_h < 5 || img_w < 5 || img_h > 16384 ||
-      img_w > 16384 || abc->desc_step < 1 || abc->desc_size < 0 ||
-      !(abc->window_desc_step_ratio > 0 && abc->window_desc_step_ratio <= 1))
-    return fail(ctx, PA_ERR_INVALID, "invalid sizes, parameters or NULL input");
-  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
-  if (!cls || n_cls < 1) return fail(ctx, PA_ERR_INVALID, "no classifiers");
-  const int R = ep->num_rotation_steps;
-  const double scale = scale_from_index(ep, 0);
-  // partdetect_dense, partdetect_test.cpp:116-165 (one scale)
+namespace {
+
+// partdetect_dense at scale index si (partdetect_test.cpp:116-237); writes the
+// log unaries of scale si into log_unary [n_cls][S][R][img_h][img_w].
+pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const float *image,
+                           int img_h, int img_w, int flip, const pa_classifier *const *cls,
+                           int n_cls, const pa_part_window *windows, const pa_abc_param *abc,
+                           float *log_unary, int mem) {
+  const int R = ep->num_rotation_steps, S = n_scales(ep);
+  const double scale = scale_from_index(ep, si);
   const double desc_step = scale * abc->desc_step;
   const int desc_size = (int)std::floor(scale * abc->desc_size + 0.5);  // boost_math::round
   double max_part_diag = 0;
@@ -2320,8 +2314,11 @@ pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
             b.dry ? nullptr : d.scores + score_off[r] + (size_t)k * rots[r].nx * rots[r].ny;
     d.grid_ptrs = b.param(grid_ptrs.data(), grid_ptrs.size());
     d.maps = b.scratch<UnaryMap>((size_t)R * n_cls + 1);  // + 1: the 16-byte copy tail
+    // host memory: this scale's [n_cls][R][img_h][img_w] block, copied out below
     d.out = mem == PA_MEM_HOST ? b.scratch<float>((size_t)n_cls * R * npx) : log_unary;
   };
+  const size_t cstride = (mem == PA_MEM_HOST ? (size_t)R : (size_t)S * R) * npx;  // per classifier
+  const size_t sofs = mem == PA_MEM_HOST ? 0 : (size_t)si * R * npx;
   Builder b1;
   plan(b1);
   Builder b;
@@ -2416,7 +2413,7 @@ pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
       UnaryMap &m = maps[(size_t)r * n_cls + k];
       std::memset(&m, 0, sizeof m);
       m.grid = grid_ptrs[(size_t)r * n_cls + k];
-      m.out = d.out + ((size_t)c * R + r) * npx;
+      m.out = d.out + c * cstride + sofs + (size_t)r * npx;
       for (int t = 0; t < 6; ++t) m.T31[t] = Tig[t];
       m.ox = ox;
       m.oy = oy;
@@ -2427,9 +2424,33 @@ pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
     PA_LAUNCH_N("unary_maps", 2, launch_unary_maps(d.maps + (size_t)r * n_cls, n_cls, rots[r].ny,
                                                    rots[r].nx, img_h, img_w, 1, 0, s));
   if (mem == PA_MEM_HOST)
-    PA_CK(cudaMemcpyAsync(log_unary, d.out, (size_t)n_cls * R * npx * sizeof(float),
-                          cudaMemcpyDeviceToHost, s));
+    PA_CK(cudaMemcpy2DAsync(log_unary + (size_t)si * R * npx, (size_t)S * R * npx * sizeof(float),
+                            d.out, (size_t)R * npx * sizeof(float), (size_t)R * npx * sizeof(float),
+                            (size_t)n_cls, cudaMemcpyDeviceToHost, s));
   return sync_ctx(ctx);
+}
+
+}  // namespace
+
+pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image, int img_h,
+                        int img_w, int flip, const pa_classifier *const *cls, int n_cls,
+                        const pa_part_window *windows, const pa_abc_param *abc,
+                        float *log_unary, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (!image || !log_unary || !windows || !abc || img_h < 5 || img_w < 5 || img_h > 16384 ||
+      img_w > 16384 || abc->desc_step < 1 || abc->desc_size < 0 ||
+      !(abc->window_desc_step_ratio > 0 && abc->window_desc_step_ratio <= 1))
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes, parameters or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  if (!cls || n_cls < 1) return fail(ctx, PA_ERR_INVALID, "no classifiers");
+  // the scale loop of partdetect_dense (partdetect_test.cpp:116): every scale
+  // its own descriptor step and size, border, grids and windows
+  for (int si = 0; si < n_scales(ep); ++si)
+    if (pa_status st = partdetect_scale(ctx, ep, si, image, img_h, img_w, flip, cls, n_cls,
+                                        windows, abc, log_unary, mem))
+      return st;
+  return PA_OK;
 }
 
 pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,

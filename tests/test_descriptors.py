@@ -306,3 +306,41 @@ def test_partdetect_rejects_colliding_maps(ctx, pa):
     with pytest.raises(pa.PaError) as ei:  # window step 1 px < sqrt 2
         ctx.partdetect(pa.exp_param(R=2), grey_image(1, 40, 48), cls, WINDOWS[:1], 4, 10, 0.25)
     assert ei.value.status == pa.PA_ERR_UNSUPPORTED
+
+
+def _maxnorm(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(np.exp(a - a.max()) - np.exp(b - b.max())).max())
+
+
+@pytest.mark.gpu
+def test_find_obj_from_image_two_scales(ctx, orc, pa):
+    """--find_obj from a grey image at two scales: pa_partdetect (scale 0.875:
+    3.5 px descriptor step, 9 px descriptors; scale 1.125: 4.5 px, 11 px ->
+    pre-smoothed patches) then pa_ps_infer with bIsSparse, against the
+    oracle's partdetect_dense + computeRootPosteriorRot."""
+    from partapp_gb300 import synth
+
+    img = grey_image(77, 64, 80)
+    wins = [(4, 16, 2.0, 8.0)] * 10
+    m, dims = _pd_models(9, wins)
+    cls = [pa.Classifier.from_stumps(ctx, m["f"][i], m["p"][i], m["theta"][i], m["alpha"][i],
+                                     dims[i]) for i in range(10)]
+    kw = dict(n_scales=2, scale_range=(0.75, 1.25))
+    want_lu = orc.partdetect(orc.make_exp(R=4, **kw), m, wins, 4, 10, 1.0, img)
+    got_lu = ctx.partdetect(pa.exp_param(R=4, **kw), img, cls, wins, 4, 10, 1.0)
+    assert got_lu.shape == want_lu.shape == (10, 2, 4, 64, 80)
+    z = want_lu == np.float32(-1e6)
+    assert np.array_equal(got_lu == np.float32(-1e6), z)
+    off = np.abs(got_lu[~z] - want_lu[~z]) > 4e-7 * np.maximum(1.0, np.abs(want_lu[~z]))
+    assert off.mean() <= 1e-3
+    rng = np.random.default_rng(3)
+    tree = synth.make_tree(rng, R=4, offset_range=(3.0, 10.0), sigma_range=(1.0, 3.0))
+    want = orc.ps_infer(orc.make_exp(R=4, sparse=True, max_local_max=50, **kw), tree, want_lu)
+    got = ctx.compute_root_posterior_rot(pa.exp_param(R=4, local_max=50, **kw), tree, got_lu,
+                                         is_sparse=True)
+    for p in range(10):
+        for s in range(2):
+            assert _maxnorm(got["log_marg"][p, s], want["log_marg"][p, s]) <= 1e-4, (p, s)
+    assert np.array_equal(got["best_conf"][:, [0, 2, 4, 5]], want["best_conf"][:, [0, 2, 4, 5]])
