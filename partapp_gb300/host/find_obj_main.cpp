@@ -15,10 +15,20 @@
 //                  (libAdaBoost/AdaBoost.cc:295-338)
 //   desc_<i>.bin   float32 [R][grid_ny][grid_nx][dim] descriptors of image i
 //
+// With --from_images the descriptors are computed on the GPU from grey
+// images (partdetect, the force_recompute_scores branch of findObjectDataset):
+//   img_<i>.pgm    8-bit binary PGM (P5) grey image i
+//   windows.txt    one line per classifier: window_size_x window_size_y
+//                  pos_offset_x pos_offset_y (PartWindowParam)
+//   exp.txt        additionally desc_step, desc_size, window_desc_step_ratio
+//                  (AbcDetectorParam); height, width, grid_*, dim and tig.txt
+//                  are not used
+//
 // Writes, into --outdir, the reference's result files pose_est_imgidx<NNNN>.mat
 // (best_conf) and, with --save_marginals, log_part_posterior_final_*.mat, plus
 // best_conf_<i>.txt (one PartHyp::toVect line per part), log_z_<i>.txt and
 // part_hyps_<i>.txt.
+#include <cctype>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -77,10 +87,61 @@ void read_joints(const std::string &path, PartConfig &pc, std::vector<Joint> &js
   }
 }
 
+// Binary 8-bit PGM (P5) -> grey levels 0..255 as float (the reference loads
+// images as float grey levels, kma::load_convert_gray_image).
+std::vector<float> read_pgm(const std::string &path, int &h, int &w) {
+  const std::string d = read_file(path);
+  size_t pos = 0;
+  auto token = [&]() -> std::string {
+    for (;;) {
+      while (pos < d.size() && std::isspace((unsigned char)d[pos])) ++pos;
+      if (pos < d.size() && d[pos] == '#') {
+        while (pos < d.size() && d[pos] != '\n') ++pos;
+        continue;
+      }
+      break;
+    }
+    const size_t b = pos;
+    while (pos < d.size() && !std::isspace((unsigned char)d[pos])) ++pos;
+    return d.substr(b, pos - b);
+  };
+  if (token() != "P5") throw std::runtime_error(path + ": not a binary PGM (P5)");
+  w = std::atoi(token().c_str());
+  h = std::atoi(token().c_str());
+  const int maxval = std::atoi(token().c_str());
+  ++pos;  // the single whitespace after maxval
+  if (w < 1 || h < 1 || maxval < 1 || maxval > 255 || d.size() < pos + (size_t)w * h)
+    throw std::runtime_error(path + ": unsupported or truncated PGM");
+  std::vector<float> img((size_t)w * h);
+  for (size_t k = 0; k < img.size(); ++k) img[k] = (float)(unsigned char)d[pos + k];
+  return img;
+}
+
+void write_outputs(const std::string &outdir, int img, bool flip, const FindObjResult &r) {
+  const std::string tag = std::to_string(img);
+  std::ofstream bc(outdir + "/best_conf_" + tag + ".txt");
+  bc.precision(9);
+  for (const PartHyp &h : r.best_conf) {
+    const auto v = h.toVect();
+    for (size_t k = 0; k < v.size(); ++k) bc << (k ? " " : "") << v[k];
+    bc << "\n";
+  }
+  std::ofstream lz(outdir + "/log_z_" + tag + ".txt");
+  lz.precision(17);
+  for (double z : r.log_z) lz << z << "\n";
+  if (!saveResults(outdir, img, flip, r))
+    throw std::runtime_error("cannot write the .mat results to " + outdir);
+  std::ofstream ph(outdir + "/part_hyps_" + tag + ".txt");
+  ph.precision(9);
+  for (size_t p = 0; p < r.part_hyps.size(); ++p)
+    for (const PartHyp &h : r.part_hyps[p])
+      ph << p << " " << h.m_rotidx << " " << h.m_x << " " << h.m_y << " " << h.m_score << "\n";
+}
+
 void usage() {
   std::cout << "usage: partapp_find_obj --find_obj --expdir DIR [--outdir DIR] [--first i]\n"
                "                        [--numimgs n] [--batch b] [--flip] [--device d]\n"
-               "                        [--save_marginals]\n";
+               "                        [--save_marginals] [--from_images]\n";
 }
 
 }  // namespace
@@ -88,7 +149,7 @@ void usage() {
 int main(int argc, char **argv) {
   std::string expdir, outdir;
   int first = 0, numimgs = -1, batch = 1, device = 0;
-  bool find_obj = false, flip = false, save_marg = false;
+  bool find_obj = false, flip = false, save_marg = false, from_images = false;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
     auto next = [&]() -> std::string {
@@ -104,6 +165,7 @@ int main(int argc, char **argv) {
     else if (a == "--device") device = std::atoi(next().c_str());
     else if (a == "--flip") flip = true;
     else if (a == "--save_marginals") save_marg = true;
+    else if (a == "--from_images") from_images = true;
     else if (a == "--help" || a == "-h") { usage(); return 0; }
     else { std::cerr << "unknown option " << a << "\n"; usage(); return 2; }
   }
@@ -124,14 +186,49 @@ int main(int argc, char **argv) {
     e.roi_save_num_samples = (int)need(kv, "roi_save_num_samples");
     e.use_pairwise = need(kv, "use_pairwise") != 0;
     e.interpolate = need(kv, "interpolate") != 0;
-    const int H = (int)need(kv, "height"), W = (int)need(kv, "width");
-    const int ny = (int)need(kv, "grid_ny"), nx = (int)need(kv, "grid_nx");
-    const int dim = (int)need(kv, "dim"), n_cls = (int)need(kv, "n_classifiers");
+    const int n_cls = (int)need(kv, "n_classifiers");
     const int n_images = (int)need(kv, "n_images");
-    const int R = e.num_rotation_steps;
     if (numimgs < 0) numimgs = n_images - first;
     if (first < 0 || first + numimgs > n_images || batch < 1)
       throw std::runtime_error("image range outside the experiment");
+    if (from_images) {
+      app.m_abc_param.desc_step = (int)need(kv, "desc_step");
+      app.m_abc_param.desc_size = (int)need(kv, "desc_size");
+      app.m_abc_param.window_desc_step_ratio = need(kv, "window_desc_step_ratio");
+      std::istringstream win(read_file(expdir + "/windows.txt"));
+      for (int c = 0; c < n_cls; ++c) {
+        PartWindow pw;
+        win >> pw.window_size_x >> pw.window_size_y >> pw.pos_offset_x >> pw.pos_offset_y;
+        if (!win) throw std::runtime_error("windows.txt: need one line per classifier");
+        app.m_window_param.push_back(pw);
+      }
+      read_joints(expdir + "/joints.txt", app.m_part_conf, app.m_joints);
+      Context ctx(device);
+      std::vector<std::unique_ptr<AdaBoostClassifier>> abc;
+      for (int c = 0; c < n_cls; ++c) {
+        abc.emplace_back(new AdaBoostClassifier(ctx, read_file(expdir + "/class_" + std::to_string(c) + ".txt")));
+        app.m_abc.push_back(abc.back().get());
+      }
+      for (int i = first; i < first + numimgs; ++i) {
+        int h = 0, w = 0;
+        const std::vector<float> img = read_pgm(expdir + "/img_" + std::to_string(i) + ".pgm", h, w);
+        std::vector<Joint> joints = app.m_joints;
+        const std::string jp = expdir + "/joints_" + std::to_string(i) + ".txt";
+        if (exists(jp)) {
+          PartConfig pc;
+          read_joints(jp, pc, joints);
+        }
+        const FindObjResult r = findObjectImageFromImage(ctx, app, flip, joints, img.data(), h, w,
+                                                         save_marg);
+        write_outputs(outdir, i, flip, r);
+        std::cout << "find_obj: image " << i << " (" << w << "x" << h << ") done\n";
+      }
+      return 0;
+    }
+    const int H = (int)need(kv, "height"), W = (int)need(kv, "width");
+    const int ny = (int)need(kv, "grid_ny"), nx = (int)need(kv, "grid_nx");
+    const int dim = (int)need(kv, "dim");
+    const int R = e.num_rotation_steps;
 
     double Tig[9];
     {
@@ -171,26 +268,7 @@ int main(int argc, char **argv) {
       }
       const auto res =
           findObjectDataset(ctx, app, flip, joints, desc.data(), nb, ny, nx, dim, Tig, H, W, save_marg);
-      for (int b = 0; b < nb; ++b) {
-        const std::string tag = std::to_string(i0 + b);
-        std::ofstream bc(outdir + "/best_conf_" + tag + ".txt");
-        bc.precision(9);
-        for (const PartHyp &h : res[b].best_conf) {
-          const auto v = h.toVect();
-          for (size_t k = 0; k < v.size(); ++k) bc << (k ? " " : "") << v[k];
-          bc << "\n";
-        }
-        std::ofstream lz(outdir + "/log_z_" + tag + ".txt");
-        lz.precision(17);
-        for (double z : res[b].log_z) lz << z << "\n";
-        if (!saveResults(outdir, i0 + b, flip, res[b]))
-          throw std::runtime_error("cannot write the .mat results to " + outdir);
-        std::ofstream ph(outdir + "/part_hyps_" + tag + ".txt");
-        ph.precision(9);
-        for (size_t p = 0; p < res[b].part_hyps.size(); ++p)
-          for (const PartHyp &h : res[b].part_hyps[p])
-            ph << p << " " << h.m_rotidx << " " << h.m_x << " " << h.m_y << " " << h.m_score << "\n";
-      }
+      for (int b = 0; b < nb; ++b) write_outputs(outdir, i0 + b, flip, res[b]);
       std::cout << "find_obj: images " << i0 << ".." << i0 + nb - 1 << " done\n";
     }
   } catch (const std::exception &ex) {

@@ -2,6 +2,7 @@
 // partapp_gpu.hpp, each a thin adapter onto include/partapp_gb300.h.
 #include "partapp_gpu.hpp"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -250,6 +251,78 @@ FindObjResult findObjectImageRotJoints(Context &ctx, const PartApp &part_app, bo
                                        const double Tig[9], int H, int W, bool want_marginals) {
   return findObjectDataset(ctx, part_app, flip, {part_app.m_joints}, desc, 1, ny, nx, dim, Tig, H,
                            W, want_marginals)[0];
+}
+
+namespace {
+
+std::vector<float> partdetect_raw(Context &ctx, const PartApp &part_app, const float *image,
+                                  int img_h, int img_w, bool flip) {
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int n = (int)part_app.m_abc.size();
+  require(n > 0 && (int)part_app.m_window_param.size() == n, "one window per classifier");
+  std::vector<const pa_classifier *> cls;
+  for (const AdaBoostClassifier *a : part_app.m_abc) cls.push_back(a->get());
+  std::vector<pa_part_window> wins(n);
+  for (int c = 0; c < n; ++c) {
+    const PartWindow &w = part_app.m_window_param[c];
+    wins[c] = {w.window_size_x, w.window_size_y, w.pos_offset_x, w.pos_offset_y};
+  }
+  const pa_abc_param abc = {part_app.m_abc_param.desc_step, part_app.m_abc_param.desc_size,
+                            part_app.m_abc_param.window_desc_step_ratio};
+  const int S = std::max(1, e.num_scale_steps), R = e.num_rotation_steps;
+  std::vector<float> lu((size_t)n * S * R * img_h * img_w);
+  ctx.check(pa_partdetect(ctx.get(), &e, image, img_h, img_w, flip ? 1 : 0, cls.data(), n,
+                          wins.data(), &abc, lu.data(), PA_MEM_HOST));
+  return lu;
+}
+
+}  // namespace
+
+void partdetect(Context &ctx, const PartApp &part_app, const float *image, int img_h,
+                int img_w, bool flip, std::vector<std::vector<FloatGrid3>> &log_part_detections) {
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int n = (int)part_app.m_abc.size();
+  const int S = std::max(1, e.num_scale_steps), R = e.num_rotation_steps;
+  const std::vector<float> lu = partdetect_raw(ctx, part_app, image, img_h, img_w, flip);
+  const size_t N = (size_t)R * img_h * img_w;
+  log_part_detections.assign(n, std::vector<FloatGrid3>());
+  for (int c = 0; c < n; ++c)
+    for (int sc = 0; sc < S; ++sc) {
+      FloatGrid3 g(R, img_h, img_w);
+      std::memcpy(g.data(), lu.data() + ((size_t)c * S + sc) * N, N * sizeof(float));
+      log_part_detections[c].push_back(std::move(g));
+    }
+}
+
+FindObjResult findObjectImageFromImage(Context &ctx, const PartApp &part_app, bool flip,
+                                       const std::vector<Joint> &joints, const float *image,
+                                       int img_h, int img_w, bool want_marginals) {
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int P = part_app.m_part_conf.part_size();
+  require((int)part_app.m_abc.size() >= P, "a detector for every part");
+  const int S = std::max(1, e.num_scale_steps), R = e.num_rotation_steps;
+  // partdetect(part_app, imgidx, imgidx, false /* flip */, ...), objectdetect_aux.cpp:383
+  const std::vector<float> lu = partdetect_raw(ctx, part_app, image, img_h, img_w, false);
+  const TreeHolder th(part_app.m_part_conf, part_app.m_part_conf.rootpart_idx, joints);
+  const int K = e.roi_save_num_samples > 0 ? e.roi_save_num_samples : 1;
+  ImageOut out(P, K, S);
+  const size_t N = (size_t)R * img_h * img_w;
+  std::vector<float> marg;
+  if (want_marginals) {
+    marg.resize((size_t)P * S * N);
+    out.o.log_marg = marg.data();
+  }
+  // the first P classifiers' unaries are the leading [P][S][R][H][W] block
+  ctx.check(pa_ps_infer(ctx.get(), &e, &th.t, flip ? 1 : 0, 1, lu.data(), img_h, img_w, &out.o,
+                        PA_MEM_HOST));
+  FindObjResult r = out.result(P, K);
+  if (want_marginals)
+    for (size_t k = 0; k < (size_t)P * S; ++k) {
+      FloatGrid3 g(R, img_h, img_w);
+      std::memcpy(g.data(), marg.data() + k * N, N * sizeof(float));
+      r.log_marginals.push_back(std::move(g));
+    }
+  return r;
 }
 
 bool saveResults(const std::string &dir, int imgidx, bool flip, const FindObjResult &r) {

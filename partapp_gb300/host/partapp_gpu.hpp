@@ -122,12 +122,28 @@ class AdaBoostClassifier {
   pa_classifier *cls_ = nullptr;
 };
 
+// AbcDetectorParam (libPartDetect/AbcDetectorParam.proto:2-12) fields of the
+// dense detector.
+struct AbcDetectorParam {
+  int desc_step = 4;
+  int desc_size = 10;
+  double window_desc_step_ratio = 1.0;
+};
+
+// PartWindowParam.part(p) (libPartDetect/PartWindowParam.proto:8-12).
+struct PartWindow {
+  int window_size_x = 0, window_size_y = 0;
+  double pos_offset_x = 0, pos_offset_y = 0;
+};
+
 // What the reference's PartApp carries for this path.
 struct PartApp {
   ExpParam m_exp_param;
   PartConfig m_part_conf;
   std::vector<Joint> m_joints;                    // loadJoints output
   std::vector<const AdaBoostClassifier *> m_abc;  // part detectors first
+  AbcDetectorParam m_abc_param;                   // for detection from images
+  std::vector<PartWindow> m_window_param;         // one per classifier in m_abc
 };
 
 // computeRotJointMarginal (objectdetect_findrot.cpp:292-456): child ->
@@ -186,6 +202,21 @@ std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_a
                                              const float *desc, int n_images, int ny, int nx,
                                              int dim, const double Tig[9], int H, int W,
                                              bool want_marginals = false);
+
+// partdetect (libPartDetect/partdetect_test.cpp:296-341 -> partdetect_dense)
+// on a grey image [img_h][img_w] followed by clip_scores_fill + computeLogGrid:
+// log_part_detections[classifier][scale] = FloatGrid3(R, img_h, img_w).
+void partdetect(Context &ctx, const PartApp &part_app, const float *image, int img_h,
+                int img_w, bool flip, std::vector<std::vector<FloatGrid3>> &log_part_detections);
+
+// findObjectImageRotJoints with freshly computed detections, the
+// force_recompute_scores branch of findObjectDataset (objectdetect_aux.cpp:
+// 376-384): partdetect on the image (unflipped, as the reference calls it),
+// then computeRootPosteriorRot with bIsSparse = true and the joints
+// (as stored; mirrored inside when flip).
+FindObjResult findObjectImageFromImage(Context &ctx, const PartApp &part_app, bool flip,
+                                       const std::vector<Joint> &joints, const float *image,
+                                       int img_h, int img_w, bool want_marginals = false);
 
 // The reference's result files (objectdetect_findrot.cpp:238-251, 1005-1011):
 // pose_est_imgidx<NNNN>.mat with best_conf [P][7], and per part

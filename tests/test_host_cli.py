@@ -136,3 +136,57 @@ def test_cli_writes_reference_mat_files(tmp_path, ctx):
         for p in (0, 4, 9):
             g = sio.loadmat(str(tmp_path / f"log_part_posterior_final_imgidx{i}_scaleidx0_o0_pidx{p}.mat"))
             assert np.array_equal(g["log_prob_grid"], ref[i]["log_marg"][p])
+
+
+@pytest.mark.gpu
+def test_cli_find_obj_from_images(tmp_path, ctx):
+    """`--find_obj --from_images`: grey PGM images -> partdetect on the GPU ->
+    PS with bIsSparse; best_conf equals the C-ABI path (pa_partdetect +
+    pa_ps_infer) through the Python mirror bit for bit."""
+    import partapp_gb300 as pa
+
+    rng = np.random.default_rng(8)
+    Rr, h, w, n_cls = 6, 56, 72, 10
+    windows = [(4, 16, 2.0, 8.0)] * n_cls
+    models = dict(f=rng.integers(0, 960, (n_cls, 80)).astype(np.int32),
+                  p=np.where(rng.random((n_cls, 80)) < 0.5, -1.0, 1.0).astype(np.float32),
+                  theta=rng.uniform(0, 60, (n_cls, 80)).astype(np.float32),
+                  alpha=rng.uniform(0, 1, (n_cls, 80)).astype(np.float32), D=960)
+    tree = synth.make_tree(rng, R=Rr, offset_range=(3.0, 8.0), sigma_range=(1.0, 2.5))
+    d = str(tmp_path)
+    imgs = []
+    for i in range(2):
+        g = np.clip(rng.uniform(0, 255, (h, w)), 0, 255)
+        k = np.ones(5) / 5.0
+        g = np.apply_along_axis(lambda v: np.convolve(v, k, mode="same"), 0, g)
+        g = np.apply_along_axis(lambda v: np.convolve(v, k, mode="same"), 1, g)
+        g[:, w // 2:] += 70.0
+        g8 = np.clip(g, 0, 255).astype(np.uint8)
+        with open(os.path.join(d, f"img_{i}.pgm"), "wb") as fh:
+            fh.write(f"P5\n# synthetic\n{w} {h}\n255\n".encode())
+            fh.write(g8.tobytes())
+        imgs.append(g8.astype(np.float32))
+    with open(os.path.join(d, "exp.txt"), "w") as fh:
+        for k_, v in (("num_rotation_steps", Rr), ("min_part_rotation", -180),
+                      ("max_part_rotation", 180), ("object_scale", 1),
+                      ("strip_border_detections", 0), ("roi_save_num_samples", 50),
+                      ("use_pairwise", 1), ("interpolate", 0), ("n_classifiers", n_cls),
+                      ("n_images", 2), ("desc_step", 4), ("desc_size", 10),
+                      ("window_desc_step_ratio", 1)):
+            fh.write(f"{k_} {v}\n")
+    with open(os.path.join(d, "windows.txt"), "w") as fh:
+        for wx, wy, ox, oy in windows:
+            fh.write(f"{wx} {wy} {ox} {oy}\n")
+    write_joints(os.path.join(d, "joints.txt"), tree)
+    for c in range(n_cls):
+        write_classifier(os.path.join(d, f"class_{c}.txt"), models, c)
+    r = subprocess.run([cli(), "--find_obj", "--from_images", "--expdir", d], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    cls = ctx.classifiers(models)
+    e = pa.exp_param(R=Rr, local_max=50, interpolate=False)
+    for i in range(2):
+        lu = ctx.partdetect(e, imgs[i], cls, windows, 4, 10, 1.0)
+        ref = ctx.compute_root_posterior_rot(e, tree, lu[:10], is_sparse=True)
+        got = np.loadtxt(os.path.join(d, f"best_conf_{i}.txt"), dtype=np.float64).astype(np.float32)
+        assert np.array_equal(got, ref["best_conf"]), i
