@@ -571,7 +571,7 @@ cudaError_t launch_mirror_border(const float *in, int h, int w, int b, float *ou
 cudaError_t launch_grid_bbox(const float *const *grids, int n, int ny, int nx, int4 *bbox,
                              cudaStream_t s) {
   if (n < 1) return cudaSuccess;
-  k_grid_bbox<<<(unsigned)n, 256, 0, s>>>(grids, ny, nx, bbox);
+  k_grid_bbox<<<(unsigned)n, 1024, 0, s>>>(grids, ny, nx, bbox);
   return cudaGetLastError();
 }
 

@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kThreads) k_unary_direct_scatter(const UnaryMa
                                                                    int ny, int nx, int H, int W) {
   const UnaryMap m = maps[blockIdx.x];
   int kmax = kFkeyNegInf;
-  for (int i = threadIdx.x; i < ny * nx; i += blockDim.x) {
+  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < ny * nx; i += gridDim.y * blockDim.x) {
     const int y1 = i / nx, x1 = i - y1 * nx;
     const float v = __ldg(m.grid + i);
     if (v == kNoClassValue) continue;
@@ -260,7 +260,11 @@ cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, 
     }
   } else {
     k_unary_direct_fill<<<grid, kThreads, 0, s>>>(maps, H, W, rows);
-    k_unary_direct_scatter<<<(unsigned)n_maps, kThreads, 0, s>>>(maps, ny, nx, H, W);
+    // cells of a map spread over several CTAs (injective map: no write order)
+    int chunks = (ny * nx + 8 * kThreads - 1) / (8 * kThreads);
+    if (chunks > 64) chunks = 64;
+    k_unary_direct_scatter<<<dim3((unsigned)n_maps, (unsigned)chunks), kThreads, 0, s>>>(
+        maps, ny, nx, H, W);
   }
   return cudaGetLastError();
 }
