@@ -38,15 +38,17 @@ constexpr float kLower = 5.f, kHigher = 15.f;  // cannyEdges(dx, dy, grad, edge,
 constexpr double kPi = 3.14159265358979323846;
 constexpr float kPiAbove = 3.14159274101257324f;  // the float nearest pi, above it
 constexpr int kDescWarps = 4;   // grid positions (one per warp) per CTA
-constexpr int kChunk = 160;     // histogram samples per increment batch (fits patch..grad)
+constexpr int kChunk = 88;      // histogram samples per increment batch (fits patch + grad)
 
 struct WarpScratch {
-  float patch[kPP];
-  float dx[kPP], dy[kPP], grad[kPP], ori[kPP], edge[kPP], tmp[kPP];
+  float patch[kPP];          // patch, then Canny candidates, then histogram increments
+  float grad[kPP];           // (adjacent to patch: the increments use both)
+  float ori[kPP], edge[kPP];
   float vec[kShape];
-  int cor[kPP + 1];        // connected-to-strong flag per weak-edge label
-  unsigned char state[kPP];  // 0 none, 1 strong edge, 2 weak edge candidate
   float sum, fac;
+  unsigned short tmp[kPP + 1];  // weak-edge labels, then the histogram sample list
+  unsigned char cor[kPP + 1];   // connected-to-strong flag per label
+  unsigned char state[kPP];     // 0 none, 1 strong edge, 2 weak edge candidate
 };
 
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
@@ -131,7 +133,7 @@ __device__ void normalize_vect(float *v) {
   for (int i = 0; i < kShape; ++i) v[i] = fmul(v[i], fac);
 }
 
-__global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
+__global__ void __launch_bounds__(32 * kDescWarps, 5) k_shape_grid(
     const float *__restrict__ img, int h, int w, DescGrid g, const DescTables *__restrict__ tabs,
     float *__restrict__ cells, uint8_t *__restrict__ valid) {
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -234,12 +236,10 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
     const bool in = y >= 1 && y < kP - 1 && x >= 1 && x < kP - 1;
     const float ddx = in ? fsub(S.patch[k + 1], S.patch[k - 1]) : 0.f;
     const float ddy = in ? fsub(S.patch[k + kP], S.patch[k - kP]) : 0.f;
-    S.dx[k] = ddx;
-    S.dy[k] = ddy;
     S.grad[k] = __fsqrt_rn(fadd(fmul(ddx, ddx), fmul(ddy, ddy)));
     S.ori[k] = atan2f(ddy, ddx);
     S.edge[k] = 0.f;
-    S.tmp[k] = 0.f;
+    S.tmp[k] = 0;
   }
   __syncwarp();
 
@@ -250,7 +250,9 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
     if (j >= 1 && j < kP - 2 && i >= 1 && i < kP - 2) {
       const float gv = S.grad[k];
       if (!(gv < kLower)) {
-        const float ux = S.dx[k], uy = S.dy[k];
+        // dX2 / dY2 at an interior pixel, recomputed (the patch is still intact)
+        const float ux = fsub(S.patch[k + 1], S.patch[k - 1]);
+        const float uy = fsub(S.patch[k + kP], S.patch[k - kP]);
         const float qx = __fdiv_rn(ux, gv), qy = __fdiv_rn(uy, gv);
         const float g1 = get_value(S.grad, fadd((float)i, qx), fadd((float)j, qy));
         const float g2 = get_value(S.grad, fsub((float)i, qx), fsub((float)j, qy));
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
   __syncwarp();
   // ... and the raster scan with its order-dependent promotion and labels on lane 0
   if (lane == 0) {
-    float nb = 1.f;
+    int nb = 1;  // the reference counts labels in a float; they stay below 2^24
     S.cor[0] = 0;
     for (int n = 0; n < ncand; ++n) {
       const int k = cand[n];
@@ -297,9 +299,9 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
         } else if (S.tmp[k + 1] > 0) {
           S.tmp[k] = S.tmp[k + 1];
         } else {
-          S.tmp[k] = nb;
-          S.cor[(int)nb] = 0;
-          nb = fadd(nb, 1.f);
+          S.tmp[k] = (unsigned short)nb;
+          S.cor[nb] = 0;
+          ++nb;
         }
       }
     }
@@ -313,13 +315,13 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
     if (e[k - kP - 1] == kColor || e[k - kP] == kColor || e[k - kP + 1] == kColor ||
         e[k - 1] == kColor || e[k + 1] == kColor || e[k + kP - 1] == kColor ||
         e[k + kP] == kColor || e[k + kP + 1] == kColor)
-      S.cor[(int)S.tmp[k]] = 1;
+      S.cor[S.tmp[k]] = 1;
   }
   __syncwarp();
   for (int k = lane; k < kPP; k += 32) {
     const int j = k / kP, i = k - j * kP;
     if (j < 1 || j > kP - 2 || i < 1 || i > kP - 2) continue;
-    if (S.tmp[k] > 0 && S.cor[(int)S.tmp[k]] == 1) S.edge[k] = kColor;
+    if (S.tmp[k] > 0 && S.cor[S.tmp[k]] == 1) S.edge[k] = kColor;
   }
   __syncwarp();
   for (int k = lane; k < kPP; k += 32) S.edge[k] = S.edge[k] > 0 ? S.grad[k] : 0.f;
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_shape_grid(
   // (b) chunks of samples: all lanes compute the increments (double
   // arithmetic), then lane b accumulates bins b, b + 32, b + 64 in the
   // reference's order
-  float *ws = S.patch;  // patch, dx, dy, grad: free, 4 * 441 floats
+  float *ws = S.patch;  // patch and grad: free, 2 * 441 floats
   uint8_t *bins = reinterpret_cast<uint8_t *>(S.patch + kChunk * 8);
   float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f;
   for (int c0 = 0; c0 < nlist; c0 += kChunk) {
