@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=1024, help="large-grid: H = W")
     ap.add_argument("--workload", choices=["find_obj", "large-grid", "uneven", "descriptors",
-                                           "from-images"],
+                                           "from-images", "link-probe"],
                     default="find_obj",
                     help="large-grid: the 1024x1024, 48-rotation PS (log-normal unaries, "
                          "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic; "
@@ -707,8 +707,79 @@ def run_from_images(args):
     ctx.close()
 
 
+def run_link_probe(args):
+    """How the host link behaves while the bench runs: three repetitions of
+    (a) the 8 images' descriptor copies alone, (b) the 8 images computed one
+    per call from HBM, (c) (a) and (b) together on two streams, (d) the 8-image
+    host-buffer call (copies overlapped through the ring).  Wall-clock around
+    synchronised calls; the link is shared with other tenants, so the spread
+    across repetitions is the point."""
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build, synth
+
+    build.build()
+    dev = torch.device("cuda:0")
+    ctx = pa.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    Be = args.e2e_batch
+    models = make_models(args.seed)
+    trees = make_trees(args.seed + 97, Be)
+    cls = ctx.classifiers(models)
+    desc = device_descriptors(4, args.seed + 7919, dev)
+    Tig = synth.grid_to_image(STRIDE)
+    e = pa.exp_param(R=R, interpolate=True)
+    host = torch.empty((Be,) + tuple(desc.shape[1:]), dtype=torch.float32, pin_memory=True)
+    for i in range(Be):
+        host[i].copy_(desc[i % 4])
+    host_np = host.numpy()
+    side = torch.cuda.Stream(dev)
+    scratch = torch.empty_like(desc[0])
+
+    def copies():
+        with torch.cuda.stream(side):
+            for i in range(Be):
+                scratch.copy_(host[i], non_blocking=True)
+
+    def compute():
+        for i in range(Be):
+            ctx.find_obj_batch(e, trees[i:i + 1], cls, desc[i % 4:i % 4 + 1], Tig, H, W)
+
+    def both():
+        copies()
+        compute()
+
+    def ring():
+        ctx.find_obj_batch(e, trees[:Be], cls, host_np, Tig, H, W)
+
+    def wall(f):
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        f()
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t) * 1e3
+
+    ring()
+    compute()
+    copies()
+    reps = []
+    for _ in range(3):
+        reps.append({"copies_ms": wall(copies), "compute_ms": wall(compute),
+                     "copies_and_compute_ms": wall(both), "host_buffer_call_ms": wall(ring)})
+    gb = Be * R * NY * NX * D * 4 / 1e9
+    line = {"metric": "host link probe", "images": Be, "descriptor_gb": gb, "repetitions": reps,
+            "copy_gbs": [gb / (r["copies_ms"] / 1e3) for r in reps]}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.workload == "link-probe":
+        run_link_probe(args)
+        return
     if args.workload == "from-images":
         run_from_images(args)
         return
