@@ -100,7 +100,7 @@ class ClockSampler:
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index, self.rows, self.proc = index, [], None
+        self.index, self.rows, self.proc, self.after = index, [], None, False
 
     def __enter__(self):
         try:
@@ -123,7 +123,13 @@ class ClockSampler:
             self.rows.append([c.strip() for c in line.split(",")])
 
     def __exit__(self, *a):
+        self.after = False
         if self.proc:
+            if not self.rows:  # region shorter than one sampling period: take the next sample
+                t0 = time.time()
+                while not self.rows and time.time() - t0 < 1.0:
+                    time.sleep(0.02)
+                self.after = bool(self.rows)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -140,7 +146,8 @@ class ClockSampler:
                           if len(r) > 5 + k and r[5 + k].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+                "samples": len(self.rows),
+                **({"sampled": "just after the timed region"} if self.after else {})}
 
 
 def measured_peaks():
