@@ -50,12 +50,16 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=1024, help="large-grid: H = W")
     ap.add_argument("--workload", choices=["find_obj", "large-grid", "uneven", "descriptors",
-                                           "from-images", "link-probe"],
+                                           "from-images", "link-probe", "learned"],
                     default="find_obj",
                     help="large-grid: the 1024x1024, 48-rotation PS (log-normal unaries, "
                          "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic; "
                          "uneven: images of random sizes (200-640 px) and rotation counts "
                          "(12/24/48) through pa_find_obj_multi, throughput and latency spread")
+    ap.add_argument("--learned", type=int, default=1,
+                    help="find_obj: add the learned-vs-plain comparison (320x240, R=24)")
+    ap.add_argument("--train-fields", type=int, default=20000)
+    ap.add_argument("--eval-fields", type=int, default=2000)
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1234)
@@ -378,6 +382,10 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     compute_ms = c0.elapsed_time(c1)
 
+    lvp = None
+    if rank == 0 and args.learned and world == 1:
+        lvp = learned_vs_plain(ctx, dev, stream, args)
+
     cpu = None
     if rank == 0 and args.cpu_baseline:
         n_thr = args.cpu_threads or os.cpu_count() or 1
@@ -404,7 +412,7 @@ def run_ours(args):
                     "breakdown_ms": {"call": e2e_ms / e2e_steps, "host_to_device_copies": copy_ms,
                                      "compute_one_image_per_call": compute_ms}},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "gpu_launches": launches, "kernels": kernels,
+            "gpu_launches": launches, "kernels": kernels, "learned_vs_plain": lvp,
             "sample_best_conf_part0": [float(x) for x in best[0]],
         }
         print(json.dumps(line), flush=True)
@@ -782,6 +790,135 @@ def run_link_probe(args):
     ctx.close()
 
 
+def learned_vs_plain(ctx, dev, stream, args, steps=10, B=8):
+    """The learned unary against the plain AdaBoost unary at 320 x 240,
+    R = 24, 10 parts x 500 stumps over 960-d descriptors: the net is trained
+    on the GPU on args.train_fields seeded 80 x 60 fields (batch 32, Adam,
+    cosine decay), evaluated on args.eval_fields fresh ones, calibrated
+    (fall-back above 1e-2 max log-score error), then both pipelines are timed
+    on B-image steps with inputs resident in HBM (FP32 descriptors for the
+    plain path, BF16 fields for the net)."""
+    import time
+
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import learned, synth
+
+    Hs, Ws, ny, nx, P0 = 240, 320, 60, 80, 10
+    rng = np.random.default_rng(args.seed + 3)
+    models = synth.make_models(rng, n_parts=P0, n_stumps=N_STUMPS, D=D)
+    cls = ctx.classifiers(models)
+    net = pa.UnaryNet(ctx, dim=D, n_parts=P0, seed=args.seed)
+    t0 = time.time()
+    losses = learned.train(ctx, net, cls, n_fields=args.train_fields, batch=32, ny=ny, nx=nx,
+                           lr=2e-3, lr_final=2e-4, epochs=1, seed=args.seed + 11)
+    torch.cuda.synchronize(dev)
+    train_s = time.time() - t0
+    ev = learned.evaluate(ctx, net, cls, n_fields=args.eval_fields, batch=32, ny=ny, nx=nx,
+                          seed=args.seed + 13)
+    flags = learned.calibrate(ev["max_abs_err"])
+    ctx.set_stream(stream.cuda_stream)
+
+    trees = [synth.make_tree(rng, R=R, offset_range=(10.0, 40.0), sigma_range=(2.0, 8.0))
+             for _ in range(B)]
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 17)
+    desc = torch.empty((B, R, ny, nx, D), dtype=torch.float32, device=dev)
+    for i in range(B):
+        z = torch.randn((R, ny, nx, D), generator=g, device=dev)
+        z.mul_(z).mul_(0.5)
+        desc[i] = z / torch.linalg.vector_norm(z, dim=-1, keepdim=True)
+    fields = desc.to(torch.bfloat16)
+    Tig = synth.grid_to_image(STRIDE)
+    e = pa.exp_param(R=R, interpolate=True)
+    ones = np.ones(P0, np.int32)
+
+    def plain():
+        return ctx.find_obj_batch(e, trees, cls, desc, Tig, Hs, Ws)
+
+    def net_all():
+        return pa.find_obj_batch_learned(ctx, e, trees, net, fields, Tig, Hs, Ws,
+                                         part_on_net=ones)
+
+    def net_fallback():
+        return pa.find_obj_batch_learned(ctx, e, trees, net, fields, Tig, Hs, Ws,
+                                         part_on_net=flags, cls_list=cls, desc=desc)
+
+    out = {}
+    for name, fn in (("plain", plain), ("learned", net_all), ("learned_with_fallback", net_fallback)):
+        for _ in range(3):
+            res = fn()
+        ctx.reset_timing()
+        ctx.enable_timing(True)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        for _ in range(steps):
+            res = fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        ctx.enable_timing(False)
+        ms = a.elapsed_time(b) / steps
+        kt = ctx.kernel_times()
+        out[name] = {"images_per_s": B * 1e3 / ms, "ms_per_step": ms,
+                     "unary_ms_per_image": sum(v[0] for k, v in kt.items()
+                                               if k.startswith("net_") or k == "score_grids")
+                     / (steps * B)}
+        out[name + "_best"] = [r["best_conf"] for r in res]
+    # (rotation, x, y) of each part's best hypothesis, per image
+    agree = np.mean([np.array_equal(pb[p, 2:6], lb[p, 2:6])
+                     for pb, lb in zip(out.pop("plain_best"), out.pop("learned_best"))
+                     for p in range(P0)])
+    out.pop("learned_with_fallback_best")
+    # the net's roofline: layer 0 reads the BF16 field once (the dominant
+    # traffic); algorithmic bytes of the five layers per image
+    G = ny * nx * R
+    net_bytes = G * (D * 2 + 64 * 2) + 3 * G * 64 * 2 * 2 + G * 64 * 2 + P0 * G * 4
+    out["learned"]["net_alg_gb_per_image"] = net_bytes / 1e9
+    out["learned"]["net_gbs"] = net_bytes / (out["learned"]["unary_ms_per_image"] / 1e3) / 1e9
+    net.close()
+    return {
+        "config": "320x240, R=24, 10 parts x 500 stumps, 960-d descriptors (BF16 fields for the "
+                  "net), net 1x1 960->64 + 3x3 64->64 x3 + 3x3 64->10",
+        "train": {"fields": args.train_fields, "batch": 32, "seconds": train_s,
+                  "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-10:].mean())},
+        "eval": {"fields": ev["n_fields"], "mse": ev["mse"].round(4).tolist(),
+                 "const_mse": ev["const_mse"].round(4).tolist(),
+                 "gain": ev["gain"].round(4).tolist(),
+                 "max_abs_log_err": ev["max_abs_err"].round(4).tolist()},
+        "part_on_net": flags.tolist(),
+        "plain": out["plain"], "learned": out["learned"],
+        "learned_with_fallback": out["learned_with_fallback"],
+        "ratio_learned_vs_plain": out["learned"]["images_per_s"] / out["plain"]["images_per_s"],
+        "ratio_with_fallback_vs_plain": (out["learned_with_fallback"]["images_per_s"]
+                                         / out["plain"]["images_per_s"]),
+        "argmax_agreement_learned_vs_plain": float(agree),
+        "images_per_step": B,
+    }
+
+
+def run_learned(args):
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build
+
+    build.build()
+    dev = torch.device("cuda:0")
+    ctx = pa.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    with ClockSampler(0) as clk:
+        r = learned_vs_plain(ctx, dev, stream, args, steps=max(3, args.steps // 4))
+    line = {"metric": "images/s (unary+PS marginals) learned vs plain", "unit": "images/s",
+            "value": r["learned"]["images_per_s"], "n_gpus": 1, "higher_is_better": True,
+            "data": "synthetic", "dtype": "bf16/f32", "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": r["config"]}, "learned_vs_plain": r, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.workload == "link-probe":
@@ -798,6 +935,9 @@ def main():
         return
     if args.workload == "uneven":
         run_uneven(args)
+        return
+    if args.workload == "learned":
+        run_learned(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -401,6 +401,73 @@ typedef struct {
 pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
                             const pa_classifier *const *cls, int n_cls, int mem);
 
+/* ---------------------------------------------------- learned unary */
+
+/* No counterpart in the reference: a convolutional network that maps a
+ * descriptor field to the log scores of the part detectors and can stand in
+ * for the AdaBoost unaries (computeScoreGrid + clip_scores_fill + log) of
+ * chosen parts.  Layers, all with zero padding and bias:
+ *   1x1 conv  dim -> 64, ReLU
+ *   3x3 conv  64 -> 64, ReLU   (three layers)
+ *   3x3 conv  64 -> n_parts     (log scores)
+ * BF16 weights and activations, FP32 accumulation on the tensor cores,
+ * FP32 master weights trained with Adam.  Parameters, flat FP32, in order:
+ *   W0 [64][dim], b0 [64], then for l = 1..3: Wl [64][9][64], bl [64],
+ *   then W4 [n_parts][9][64], b4 [n_parts]
+ * (weights [out channel][tap (dy, dx row-major)][in channel]).
+ * Fields are NHWC: [n_fields][ny][nx][dim], dim a multiple of 64, FP32 or
+ * BF16, 16-byte aligned.  All data pointers of these calls are device
+ * pointers. */
+typedef struct pa_unary_net pa_unary_net;
+
+typedef struct {
+  float lr, beta1, beta2, eps;
+} pa_adam_param;
+
+/* Weights drawn from `seed` (He-normal; the output layer's scaled by 0.1),
+ * zero biases; Adam state zero. */
+pa_status pa_unary_net_create(pa_ctx *ctx, int dim, int n_parts, uint64_t seed,
+                              pa_unary_net **out);
+pa_status pa_unary_net_destroy(pa_ctx *ctx, pa_unary_net *net);
+/* Number of parameters; copies them to host `params` when not NULL. */
+pa_status pa_unary_net_get_params(pa_ctx *ctx, const pa_unary_net *net, float *params,
+                                  int64_t *n_params);
+/* Replaces the parameters (host array) and resets the Adam state. */
+pa_status pa_unary_net_set_params(pa_ctx *ctx, pa_unary_net *net, const float *params);
+/* Log scores (exp_out = 0) or scores (exp_out = 1) of the n_parts outputs:
+ * element (field f, part p, row y, column x) at
+ * out[f * out_field_stride + p * out_part_stride + y * nx + x]. */
+pa_status pa_unary_net_forward(pa_ctx *ctx, pa_unary_net *net, const void *fields, int fields_bf16,
+                               int n_fields, int ny, int nx, float *out, int64_t out_field_stride,
+                               int64_t out_part_stride, int exp_out);
+/* Mean squared error against the log of AdaBoost score grids, and its
+ * gradient with respect to every parameter (kept in the net; copied to host
+ * `grads` when not NULL).  scores: [n_parts][n_fields][ny][nx] as
+ * pa_score_grids writes them (normalised); the target of a cell is
+ * log(s) for s > 0, log(1e-4) for s < 0 (clip_scores_fill), and cells with
+ * s == 0 (LOG_ZERO) are left out.  loss = sum of squared errors over
+ * (n_fields * n_parts * ny * nx). */
+pa_status pa_unary_net_backward(pa_ctx *ctx, pa_unary_net *net, const void *fields,
+                                int fields_bf16, const float *scores, int n_fields, int ny,
+                                int nx, double *loss, float *grads);
+/* One Adam step with the gradient of the last pa_unary_net_backward. */
+pa_status pa_unary_net_adam(pa_ctx *ctx, pa_unary_net *net, const pa_adam_param *opt);
+
+/* pa_find_obj_batch with the net as the unary of the parts whose
+ * part_on_net[p] is non-zero (all parts when part_on_net is NULL) and the
+ * AdaBoost classifiers cls[p] for the others.
+ *   fields  [n_images][R][ny][nx][dim] BF16, read by the net (may be NULL
+ *           when no part is on the net)
+ *   desc    the same descriptors in FP32 for the AdaBoost parts (may be
+ *           NULL when every part is on the net)
+ * Device pointers (mem = PA_MEM_DEVICE) only. */
+pa_status pa_find_obj_batch_learned(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
+                                    const pa_tree *trees, int flip, pa_unary_net *net,
+                                    const int *part_on_net, const pa_classifier *const *cls,
+                                    int n_cls, const void *fields, const float *desc, int ny,
+                                    int nx, int dim, const double *Tig, int tig_shared, int H,
+                                    int W, const pa_ps_outputs *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,9 @@ points:
                                (objectdetect_findrot.cpp:124-286, 470-727)
   Context.find_obj             findObjectImageRotJoints with fresh scores
   Context.find_obj_batch       many images per call
+  UnaryNet                     the learned unary (no reference counterpart):
+                               forward, backward, Adam, and
+                               Context.find_obj_batch_learned
 
 Arrays: numpy arrays are host memory (copied through the device workspace);
 torch CUDA tensors are used in place as device memory.  There is no CPU
@@ -47,6 +50,9 @@ EXPORTS = (
     "pa_ps_infer", "pa_rot_joint_marginal", "pa_rot_joint_marginal_noalloc", "pa_find_obj",
     "pa_feature_grid_size", "pa_descriptor_grid", "pa_partdetect",
     "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math", "pa_find_obj_multi",
+    "pa_unary_net_create", "pa_unary_net_destroy", "pa_unary_net_get_params",
+    "pa_unary_net_set_params", "pa_unary_net_forward", "pa_unary_net_backward",
+    "pa_unary_net_adam", "pa_find_obj_batch_learned",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
@@ -95,6 +101,10 @@ class Tree(C.Structure):
 
 class PartHyp(C.Structure):
     _fields_ = [(n, C.c_float) for n in ("scaleidx", "scale", "rotidx", "rot", "x", "y", "score")]
+
+
+class AdamParam(C.Structure):
+    _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float)]
 
 
 class PsOutputs(C.Structure):
@@ -159,6 +169,15 @@ def load_library():
                               ip, ip, vp, P(PsOutputs), ip]
     L.pa_find_obj_batch.argtypes = [vp, P(ExpParam), ip, P(Tree), ip, P(vp), ip, vp, ip, ip, ip,
                                     P(dp), ip, ip, ip, vp, P(PsOutputs), ip]
+    L.pa_unary_net_create.argtypes = [vp, ip, ip, C.c_uint64, P(vp)]
+    L.pa_unary_net_destroy.argtypes = [vp, vp]
+    L.pa_unary_net_get_params.argtypes = [vp, vp, vp, P(C.c_int64)]
+    L.pa_unary_net_set_params.argtypes = [vp, vp, vp]
+    L.pa_unary_net_forward.argtypes = [vp, vp, vp, ip, ip, ip, ip, vp, C.c_int64, C.c_int64, ip]
+    L.pa_unary_net_backward.argtypes = [vp, vp, vp, ip, vp, ip, ip, ip, P(dp), vp]
+    L.pa_unary_net_adam.argtypes = [vp, vp, P(AdamParam)]
+    L.pa_find_obj_batch_learned.argtypes = [vp, P(ExpParam), ip, P(Tree), ip, vp, vp, P(vp), ip,
+                                            vp, vp, ip, ip, ip, P(dp), ip, ip, ip, P(PsOutputs)]
     for name in EXPORTS:
         getattr(L, name)  # every declared entry point must resolve
     _lib = L
@@ -570,3 +589,127 @@ class Context:
                                              nx, dim, T.ctypes.data_as(C.POINTER(C.c_double)),
                                              int(T.size == 9), H, W, so, outs, d.mem))
         return [self._finish(r, P) for r in results]
+
+
+def _dev_field_ptr(t):
+    """(pointer, is_bf16) of a contiguous CUDA float32 / bfloat16 tensor."""
+    import torch
+
+    if not _is_torch(t) or not t.is_cuda or not t.is_contiguous():
+        raise ValueError("fields must be a contiguous CUDA tensor")
+    if t.dtype == torch.bfloat16:
+        return t.data_ptr(), 1
+    if t.dtype == torch.float32:
+        return t.data_ptr(), 0
+    raise ValueError("fields must be float32 or bfloat16")
+
+
+class UnaryNet:
+    """The learned unary (pa_unary_net): 1x1 conv dim -> 64, three 3x3 64 -> 64
+    and a 3x3 64 -> n_parts, ReLU between, BF16 operands with FP32
+    accumulation on the tensor cores, FP32 master weights and Adam.  Fields
+    are CUDA tensors [n][ny][nx][dim] (float32 or bfloat16)."""
+
+    def __init__(self, ctx: Context, dim: int = 960, n_parts: int = 10, seed: int = 0):
+        self.ctx, self.dim, self.P = ctx, int(dim), int(n_parts)
+        h = C.c_void_p()
+        ctx._check(ctx.L.pa_unary_net_create(ctx.h, self.dim, self.P, int(seed) & (2**64 - 1),
+                                             C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.pa_unary_net_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_params(self) -> int:
+        n = C.c_int64()
+        self.ctx._check(self.ctx.L.pa_unary_net_get_params(self.ctx.h, self.h, None, C.byref(n)))
+        return n.value
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.n_params, dtype=np.float32)
+        n = C.c_int64()
+        self.ctx._check(self.ctx.L.pa_unary_net_get_params(self.ctx.h, self.h,
+                                                           out.ctypes.data, C.byref(n)))
+        return out
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters, got {p.size}")
+        self.ctx._check(self.ctx.L.pa_unary_net_set_params(self.ctx.h, self.h, p.ctypes.data))
+
+    def forward(self, fields, exp_out=False, out=None):
+        """Log scores (or scores with exp_out) as a CUDA tensor [P][n][ny][nx]."""
+        import torch
+
+        ptr, bf = _dev_field_ptr(fields)
+        n, ny, nx, dim = fields.shape
+        if dim != self.dim:
+            raise ValueError("field depth differs from the net's")
+        if out is None:
+            out = torch.empty((self.P, n, ny, nx), dtype=torch.float32, device=fields.device)
+        self.ctx._check(self.ctx.L.pa_unary_net_forward(
+            self.ctx.h, self.h, ptr, bf, n, ny, nx, out.data_ptr(), ny * nx, n * ny * nx,
+            int(bool(exp_out))))
+        return out
+
+    def backward(self, fields, scores, want_grads=False):
+        """Loss (float) and, with want_grads, the host copy of the gradient.
+        scores: CUDA float32 [P][n][ny][nx] AdaBoost score grids."""
+        ptr, bf = _dev_field_ptr(fields)
+        n, ny, nx, dim = fields.shape
+        if tuple(scores.shape) != (self.P, n, ny, nx) or not scores.is_contiguous():
+            raise ValueError("scores must be a contiguous [P][n][ny][nx] tensor")
+        loss = C.c_double()
+        g = np.empty(self.n_params, dtype=np.float32) if want_grads else None
+        self.ctx._check(self.ctx.L.pa_unary_net_backward(
+            self.ctx.h, self.h, ptr, bf, scores.data_ptr(), n, ny, nx, C.byref(loss),
+            None if g is None else g.ctypes.data))
+        return (loss.value, g) if want_grads else loss.value
+
+    def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        a = AdamParam(float(lr), float(beta1), float(beta2), float(eps))
+        self.ctx._check(self.ctx.L.pa_unary_net_adam(self.ctx.h, self.h, C.byref(a)))
+
+    def train_step(self, fields, scores, lr=1e-3, **kw):
+        loss = self.backward(fields, scores)
+        self.adam(lr=lr, **kw)
+        return loss
+
+
+def find_obj_batch_learned(ctx: Context, exp: ExpParam, trees, net: UnaryNet, fields, Tig, H, W,
+                           part_on_net=None, cls_list=None, desc=None, flip=False,
+                           want_marg=False, want_root=False):
+    """pa_find_obj_batch_learned: fields [B][R][ny][nx][dim] bfloat16 CUDA tensor
+    (read by the net), desc the float32 descriptors for the parts off the net."""
+    B, R, ny, nx, dim = fields.shape
+    ths = [_TreeHolder(t) for t in trees]
+    arr = (Tree * B)(*[t.s for t in ths])
+    P = ths[0].s.n_parts
+    T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(-1)
+    results, outs = [], (PsOutputs * B)()
+    for i in range(B):
+        res, o = ctx._outputs(P, R, H, W, exp.roi_save_num_samples, PA_MEM_DEVICE, fields,
+                              want_marg, want_root)
+        results.append(res)
+        outs[i] = o
+    on = None
+    if part_on_net is not None:
+        on_arr = np.ascontiguousarray(part_on_net, dtype=np.int32)
+        on = on_arr.ctypes.data
+    fptr = _dev_field_ptr(fields)[0] if fields is not None else None
+    dptr = _Buf(desc, np.float32).ptr if desc is not None else None
+    cl = ctx._cls_array(cls_list) if cls_list else None
+    ctx._check(ctx.L.pa_find_obj_batch_learned(
+        ctx.h, C.byref(exp), B, arr, int(flip), net.h, on, cl, len(cls_list or []), fptr, dptr,
+        ny, nx, dim, T.ctypes.data_as(C.POINTER(C.c_double)), int(T.size == 9), H, W, outs))
+    return [ctx._finish(r, P) for r in results]

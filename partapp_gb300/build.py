@@ -25,7 +25,7 @@ HOST = os.path.join(HERE, "host")
 CLI = os.path.join(OUT, "partapp_find_obj")
 HOST_SOURCES = ["objectdetect_gpu.cpp", "find_obj_main.cpp"]
 SOURCES = ["k_stump.cu", "k_unary.cu", "k_msg.cu", "k_reduce.cu", "k_localmax.cu", "k_tc_gemm.cu",
-           "k_desc.cu", "pa_api.cu", "pa_noalloc.cu"]
+           "k_desc.cu", "k_conv.cu", "pa_api.cu", "pa_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -54,8 +54,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
-    deps = [os.path.join(CSRC, src), os.path.join(CSRC, "pa_internal.cuh"),
-            os.path.join(ROOT, "include", "partapp_gb300.h")]
+    deps = [os.path.join(CSRC, src), os.path.join(ROOT, "include", "partapp_gb300.h")]
+    deps += [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
     if _stale(obj, deps):
         cmd = [nvcc()] + flags() + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -27,6 +27,7 @@
 #include <algorithm>
 
 #include "pa_internal.cuh"
+#include "tc_common.cuh"
 
 namespace pa {
 namespace {
@@ -35,72 +36,17 @@ constexpr int kBM = 128, kBN = 128, kBK = 64, kStages = 3;
 constexpr int kTileBytesA = kBM * kBK * 2;  // 16 KB
 constexpr int kTileBytesB = kBN * kBK * 2;  // 16 KB
 constexpr int kStageBytes = kTileBytesA + kTileBytesB;
-constexpr uint32_t kSpinLimit = 1u << 24;
 constexpr int kGemmThreads = 128;
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-// Non-blocking probe of phase `parity`; the caller bounds the polling.
-__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
-    if (mbar_test(bar, parity)) return true;
-  atomicOr(err, 8);
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
-                                            uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Shared-memory matrix descriptor of a K-major operand tile stored as TMA
-// writes it with 128-byte swizzle: rows of 128 B (64 bf16), 8-row atoms of
-// 1024 B (stride byte offset), tile base 1024-byte aligned.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
-  d |= (uint64_t)1 << 16;                    // leading byte offset (unused with swizzle)
-  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: 8 rows x 128 B
-  d |= (uint64_t)1 << 46;                    // descriptor version
-  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
-  return d;
-}
+using tc::mbar_arrive_expect_tx;
+using tc::mbar_init;
+using tc::mbar_wait;
+using tc::smem_u32;
+using tc::sw128_desc;
+using tc::tma_load_2d;
 
 // Instruction descriptor: D fp32, A and B bf16, both K-major, M = 128, N = 128.
-constexpr uint32_t kIdesc = (1u << 4)                   // D format: f32
-                            | (1u << 7)                 // A format: bf16
-                            | (1u << 10)                // B format: bf16
-                            | ((uint32_t)(kBN >> 3) << 17)
-                            | ((uint32_t)(kBM >> 4) << 24);
+constexpr uint32_t kIdesc = tc::idesc_bf16(kBM, kBN);
 
 // Store 16 consecutive accumulator columns of one output row (fp32 or
 // bf16; vector stores when the row segment is aligned and complete).
@@ -439,36 +385,8 @@ __global__ void __launch_bounds__(kBandThreads, 1)
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
-}
-
-// 2-D bf16 tensor map: `rows` rows of `cols` elements, row stride in bytes;
-// box = 64 columns x 128 rows, 128-byte swizzle, zero fill outside.
 bool make_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows, uint64_t row_bytes) {
-  EncodeTiledFn enc = encode_fn();
-  if (!enc) return false;
-  const cuuint64_t dims[2] = {cols, rows};
-  const cuuint64_t strides[1] = {row_bytes};
-  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
-  const cuuint32_t estr[2] = {1, 1};
-  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box,
-             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return tc::make_map_2d(m, base, cols, rows, row_bytes, kBK, kBM);
 }
 
 }  // namespace
@@ -535,4 +453,51 @@ cudaError_t launch_tc_gemm_bf16(const void *A, int64_t lda, const void *B, int64
   return launch_tc_gemm(A, lda, M, K, B, ldb, N, K, g, 1, err, s);
 }
 
+namespace tc {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+bool make_map_2d(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows,
+                 uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {cols, rows};
+  const cuuint64_t strides[1] = {row_bytes};
+  const cuuint32_t box[2] = {box_cols, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool make_map_nhwc(CUtensorMap *m, const void *base, uint64_t C, uint64_t W, uint64_t H,
+                   uint64_t N, uint32_t box_w) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[4] = {C, W, H, N};
+  const cuuint64_t strides[3] = {C * 2, C * 2 * W, C * 2 * W * H};
+  const cuuint32_t box[4] = {64, box_w, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace tc
 }  // namespace pa

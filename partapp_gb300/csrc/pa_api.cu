@@ -1403,6 +1403,219 @@ std::vector<int> stump_counts(const pa_classifier *const *cls, int n) {
 // call fills fields [scores_field0, scores_field0 + n_img*R) of it.
 // An image whose results are still on their way to the host: its plan, the
 // landing slot of its small results and its outputs.
+}  // namespace
+
+// ------------------------------------------------------------------------
+// Learned unary (no reference counterpart): network state and the layer
+// sequence of its forward and backward passes.
+// ------------------------------------------------------------------------
+struct pa_unary_net {
+  int device = 0;
+  int dim = 0, P = 0;
+  int64_t off_w[5] = {}, off_b[5] = {}, n_params = 0;
+  float *params = nullptr, *grads = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+  __nv_bfloat16 *wf0 = nullptr, *wf[4] = {}, *wd[4] = {};
+  int64_t step = 0;  // Adam steps taken
+  char *scratch = nullptr;
+  size_t scratch_cap = 0;
+  int *err = nullptr;
+};
+
+namespace {
+
+void net_layout(pa_unary_net *n) {
+  int64_t o = 0;
+  for (int l = 0; l < 5; ++l) {
+    const int64_t cout = l == 4 ? n->P : 64, k = l == 0 ? n->dim : 576;
+    n->off_w[l] = o;
+    o += cout * k;
+    n->off_b[l] = o;
+    o += cout;
+  }
+  n->n_params = o;
+}
+
+struct NetScratch {
+  __nv_bfloat16 *x = nullptr;       // BF16 copy of FP32 fields
+  __nv_bfloat16 *act[4] = {};       // post-ReLU activations of layers 0..3
+  float *y = nullptr;               // training: output log scores [P][n][ny][nx]
+  __nv_bfloat16 *dz4 = nullptr, *dza = nullptr, *dzb = nullptr;
+  float *wpart = nullptr;
+  size_t wpart_floats = 0;
+  float *bpart = nullptr;
+  float *lpart = nullptr;
+  double *loss = nullptr;
+};
+constexpr int kBiasBlocks = 256;
+
+pa_status net_scratch(pa_ctx *ctx, pa_unary_net *net, int n, int ny, int nx, bool cast,
+                      bool train, NetScratch &sc) {
+  const size_t L = (size_t)n * ny * nx;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = (off + 255) / 256 * 256;
+    off = o + bytes;
+    return o;
+  };
+  const size_t ox = cast ? take(L * net->dim * 2) : 0;
+  size_t oa[4];
+  for (int l = 0; l < 4; ++l) oa[l] = take(L * 64 * 2);
+  size_t oy = 0, od4 = 0, oda = 0, odb = 0, ow = 0, ob = 0, ol = 0, olo = 0, wf = 0;
+  if (train) {
+    oy = take(L * net->P * 4);
+    od4 = take(L * 64 * 2);
+    oda = take(L * 64 * 2);
+    odb = take(L * 64 * 2);
+    wf = std::max(conv_wgrad_part_floats(net->dim, 1, n, ny, nx),
+                  conv_wgrad_part_floats(64, 9, n, ny, nx));
+    ow = take(wf * 4);
+    ob = take((size_t)kBiasBlocks * 64 * 4);
+    ol = take((size_t)loss_blocks((int64_t)L) * 4);
+    olo = take(8);
+  }
+  if (off > net->scratch_cap) {
+    PA_CK(cudaStreamSynchronize(ctx->stream));
+    if (net->scratch) cudaFree(net->scratch);
+    net->scratch = nullptr;
+    net->scratch_cap = 0;
+    const size_t cap = off + off / 8 + 4096;
+    if (cudaMalloc(&net->scratch, cap) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes for the unary net", cap);
+    }
+    net->scratch_cap = cap;
+  }
+  char *b = net->scratch;
+  sc = NetScratch{};
+  if (cast) sc.x = reinterpret_cast<__nv_bfloat16 *>(b + ox);
+  for (int l = 0; l < 4; ++l) sc.act[l] = reinterpret_cast<__nv_bfloat16 *>(b + oa[l]);
+  if (train) {
+    sc.y = reinterpret_cast<float *>(b + oy);
+    sc.dz4 = reinterpret_cast<__nv_bfloat16 *>(b + od4);
+    sc.dza = reinterpret_cast<__nv_bfloat16 *>(b + oda);
+    sc.dzb = reinterpret_cast<__nv_bfloat16 *>(b + odb);
+    sc.wpart = reinterpret_cast<float *>(b + ow);
+    sc.wpart_floats = wf;
+    sc.bpart = reinterpret_cast<float *>(b + ob);
+    sc.lpart = reinterpret_cast<float *>(b + ol);
+    sc.loss = reinterpret_cast<double *>(b + olo);
+  }
+  return PA_OK;
+}
+
+pa_status net_check_fields(pa_ctx *ctx, const pa_unary_net *net, const void *fields, int n, int ny,
+                           int nx) {
+  if (!net || !fields || n < 1 || ny < 1 || nx < 1 || n > 65535 || ny > 65535 ||
+      ((uintptr_t)fields & 15))
+    return fail(ctx, PA_ERR_INVALID, "invalid net input (NULL, sizes or alignment)");
+  return PA_OK;
+}
+
+pa_status net_pack(pa_ctx *ctx, pa_unary_net *net) {
+  PackArgs a{};
+  a.dim = net->dim;
+  a.P = net->P;
+  for (int l = 0; l < 5; ++l) a.off_w[l] = net->off_w[l];
+  a.wf0 = net->wf0;
+  for (int l = 0; l < 4; ++l) {
+    a.wf[l] = net->wf[l];
+    a.wd[l] = net->wd[l];
+  }
+  PA_LAUNCH("net_pack", launch_pack_weights(net->params, a, ctx->stream));
+  return PA_OK;
+}
+
+// Forward pass, queued on the context's stream.  `out` spec as
+// pa_unary_net_forward.
+pa_status net_forward(pa_ctx *ctx, pa_unary_net *net, const void *fields, int bf16, int n, int ny,
+                      int nx, float *out, int64_t sf, int64_t sc_, int exp_out, NetScratch &sc) {
+  cudaStream_t s = ctx->stream;
+  const void *x = fields;
+  if (!bf16) {
+    PA_LAUNCH("net_cast", launch_cast_bf16(reinterpret_cast<const float *>(fields), sc.x,
+                                           (int64_t)n * ny * nx * net->dim, s));
+    x = sc.x;
+  }
+  ConvArgs a{};
+  a.mode = kConvReluBf16;
+  a.bias = net->params + net->off_b[0];
+  a.out = sc.act[0];
+  PA_LAUNCH("net_conv", launch_conv(x, net->dim, 1, n, ny, nx, net->wf0, a, net->err, s));
+  for (int l = 1; l < 4; ++l) {
+    a.bias = net->params + net->off_b[l];
+    a.out = sc.act[l];
+    PA_LAUNCH("net_conv", launch_conv(sc.act[l - 1], 64, 9, n, ny, nx, net->wf[l - 1], a, net->err, s));
+  }
+  a.mode = kConvOutF32;
+  a.bias = net->params + net->off_b[4];
+  a.out = out;
+  a.n_out = net->P;
+  a.out_sf = sf;
+  a.out_sc = sc_;
+  a.exp_out = exp_out;
+  PA_LAUNCH("net_conv", launch_conv(sc.act[3], 64, 9, n, ny, nx, net->wf[3], a, net->err, s));
+  return PA_OK;
+}
+
+// Forward, loss and the gradient of every parameter (into net->grads),
+// queued on the context's stream; the loss lands in *sc.loss.
+pa_status net_backward(pa_ctx *ctx, pa_unary_net *net, const void *fields, int bf16,
+                       const float *scores, int n, int ny, int nx, NetScratch &sc) {
+  cudaStream_t s = ctx->stream;
+  const int64_t G = (int64_t)ny * nx, L = (int64_t)n * G;
+  if (pa_status st = net_forward(ctx, net, fields, bf16, n, ny, nx, sc.y, G, n * G, 0, sc)) return st;
+  const void *x = bf16 ? fields : sc.x;
+  LossArgs la{};
+  la.pred = sc.y;
+  la.scores = scores;
+  la.pred_sf = la.score_sf = G;
+  la.pred_sc = la.score_sc = n * G;
+  la.n = n;
+  la.P = net->P;
+  la.H = ny;
+  la.W = nx;
+  la.inv_count = (float)(1.0 / ((double)L * net->P));
+  PA_LAUNCH_N("net_loss", 2, launch_loss_grad(la, sc.dz4, sc.lpart, sc.loss, s));
+  // layer l: input in[l], output gradient dz[l]; the input gradient of
+  // layer l (l >= 1), masked by ReLU, is the output gradient of layer l - 1
+  const void *in[5] = {x, sc.act[0], sc.act[1], sc.act[2], sc.act[3]};
+  __nv_bfloat16 *dz = sc.dz4;
+  for (int l = 4; l >= 0; --l) {
+    const int cin = l == 0 ? net->dim : 64, taps = l == 0 ? 1 : 9, cout = l == 4 ? net->P : 64;
+    PA_LAUNCH_N("net_wgrad", 2, launch_conv_wgrad(in[l], cin, taps, dz, n, ny, nx, cout, sc.wpart,
+                                                  sc.wpart_floats, net->grads + net->off_w[l],
+                                                  net->err, s));
+    PA_LAUNCH_N("net_bgrad", 2, launch_bias_grad(dz, L, cout, sc.bpart, kBiasBlocks,
+                                                 net->grads + net->off_b[l], s));
+    if (l == 0) break;
+    __nv_bfloat16 *next = (dz == sc.dza) ? sc.dzb : sc.dza;
+    ConvArgs a{};
+    a.mode = kConvMaskBf16;
+    a.act = sc.act[l - 1];
+    a.out = next;
+    PA_LAUNCH("net_dgrad", launch_conv(dz, 64, 9, n, ny, nx, net->wd[l - 1], a, net->err, s));
+    dz = next;
+  }
+  return PA_OK;
+}
+
+pa_status net_err_check(pa_ctx *ctx, pa_unary_net *net) {
+  int flag = 0;
+  PA_CK(cudaMemcpyAsync(&flag, net->err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (pa_status st = sync_ctx(ctx)) return st;
+  if (flag) return fail(ctx, PA_ERR_CUDA, "unary net pipeline wait timed out (flag %d)", flag);
+  return PA_OK;
+}
+
+// Learned unary of find_obj_core: the net's scores for the parts on the
+// net, AdaBoost for the others.
+struct LearnedUnary {
+  pa_unary_net *net = nullptr;
+  const void *fields = nullptr;  // BF16 [n_fields][ny][nx][dim]
+  std::vector<char> on_net;      // per part
+  bool any_net = false, any_ada = false;
+};
+
 struct PendingImage {
   PsPlan pl;
   Readback rb;
@@ -1421,7 +1634,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
                         const double *Tig, int tig_shared,
                         int H, int W, float *scores_out, int64_t scores_field0,
                         int64_t scores_fields, const pa_ps_outputs *outs, int mem,
-                        PendingImage *defer = nullptr) {
+                        PendingImage *defer = nullptr, const LearnedUnary *lu = nullptr) {
   PsPlan pl;
   pl.tc_mode = ctx->msg_math == PA_MSG_BF16_TENSOR;
   pl.sparse_up = true;  // findObjectImageRotJoints passes bIsSparse = true (objectdetect_findrot.cpp:740)
@@ -1431,9 +1644,24 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
     if (!same_topology(&trees[0], &trees[i]))
       return fail(ctx, PA_ERR_INVALID, "image %d: tree topology differs from image 0", i);
   const int P = pl.sc.P, R = e->num_rotation_steps;
+  // the AdaBoost classifiers are evaluated unless every part is on the net;
+  // with a learned unary only those of the parts off the net, in one launch
+  const bool ada = !lu || lu->any_ada;
+  std::vector<const pa_classifier *> ada_cls;
+  std::vector<int> ada_part;
+  if (lu) {
+    for (int p = 0; p < (int)lu->on_net.size() && p < n_cls; ++p)
+      if (!lu->on_net[p]) {
+        ada_cls.push_back(cls[p]);
+        ada_part.push_back(p);
+      }
+  }
+  const pa_classifier *const *run_cls = lu ? ada_cls.data() : cls;
+  const int n_run = lu ? (int)ada_cls.size() : n_cls;
+  if (lu && (int)lu->on_net.size() != P)
+    return fail(ctx, PA_ERR_INVALID, "the net's part count differs from the tree's");
   if (n_cls < P) return fail(ctx, PA_ERR_INVALID, "need at least n_parts classifiers");
-  st = check_classifiers(ctx, cls, n_cls, dim);
-  if (st) return st;
+  if (ada && (st = check_classifiers(ctx, cls, n_cls, dim))) return st;
   std::vector<std::vector<Joint>> joints(n_img);
   for (int i = 0; i < n_img; ++i) {
     st = load_joints(ctx, &trees[i], flip, joints[i]);
@@ -1463,8 +1691,11 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   // is exactly this call's [n_cls][n_fields] block
   const bool scores_dev_out =
       (mem == PA_MEM_DEVICE && scores_out && scores_field0 == 0 && scores_fields == n_fields);
-  StumpPart *sp = plan_stumps(b1, cls, n_cls);
+  StumpPart *sp = ada ? plan_stumps(b1, run_cls, n_run) : nullptr;
   const float *desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b1.scratch<float>(n_fields * G * dim);
+  // scores of the AdaBoost parts when the net writes the others
+  const bool split_scores = lu && lu->any_ada && lu->any_net;
+  float *ada_scores = split_scores ? b1.scratch<float>((size_t)n_run * n_fields * G) : nullptr;
   // per-field descriptor pointers when the images are separate device buffers
   std::vector<const float *> fptr;
   bool fields_al = true;
@@ -1495,8 +1726,9 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   if (st) return st;
   b.base = ctx->arena;
   PsPlan pl2 = pl;
-  sp = plan_stumps(b, cls, n_cls);
+  sp = ada ? plan_stumps(b, run_cls, n_run) : nullptr;
   desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b.scratch<float>(n_fields * G * dim);
+  ada_scores = split_scores ? b.scratch<float>((size_t)n_run * n_fields * G) : nullptr;
   fields_dev = img_desc ? b.param(fptr.data(), fptr.size()) : nullptr;
   scores = scores_dev_out ? scores_out : b.scratch<float>((size_t)n_cls * n_fields * G);
   plan_ps(b, pl2, e, joints, marg_out.data(), rp_out.data());
@@ -1520,10 +1752,35 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   st = init_slots(ctx, pl2);
   if (st) return st;
   cudaStream_t s = ctx->stream;
-  const std::vector<char> ff = fast_flags(cls, n_cls);
-  const std::vector<int> ns = stump_counts(cls, n_cls);
-  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_cls, desc_dev, fields_dev, fields_al, G,
-                                              (int)n_fields, dim, 1, scores, s));
+  if (!lu) {
+    const std::vector<char> ff = fast_flags(cls, n_cls);
+    const std::vector<int> ns = stump_counts(cls, n_cls);
+    PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_cls, desc_dev, fields_dev, fields_al, G,
+                                                (int)n_fields, dim, 1, scores, s));
+  } else {
+    // the net writes the scores of all P parts ([part][field][ny][nx]); the
+    // AdaBoost parts are then overwritten with their classifiers' grids
+    if (lu->any_net) {
+      NetScratch nsc;
+      if ((st = net_scratch(ctx, lu->net, (int)n_fields, ny, nx, false, false, nsc))) return st;
+      PA_CK(cudaMemsetAsync(lu->net->err, 0, sizeof(int), s));
+      if ((st = net_forward(ctx, lu->net, lu->fields, 1, (int)n_fields, ny, nx, scores, G,
+                            n_fields * G, 1, nsc)))
+        return st;
+    }
+    if (lu->any_ada) {
+      const std::vector<char> ff = fast_flags(run_cls, n_run);
+      const std::vector<int> ns = stump_counts(run_cls, n_run);
+      PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_run, desc_dev, nullptr,
+                                                  false, G, (int)n_fields, dim, 1,
+                                                  split_scores ? ada_scores : scores, s));
+      if (split_scores)
+        for (int k = 0; k < n_run; ++k)
+          PA_CK(cudaMemcpyAsync(scores + (size_t)ada_part[k] * n_fields * G,
+                                ada_scores + (size_t)k * n_fields * G,
+                                (size_t)n_fields * G * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+  }
   if (scores_out && !scores_dev_out)
     PA_CK(cudaMemcpy2DAsync(scores_out + scores_field0 * G, (size_t)scores_fields * G * sizeof(float),
                             scores, (size_t)n_fields * G * sizeof(float),
@@ -2873,6 +3130,197 @@ pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
     if (st) result = st;
   }
   return result;
+}
+
+// ------------------------------------------------------------------------
+// Learned unary
+// ------------------------------------------------------------------------
+pa_status pa_unary_net_create(pa_ctx *ctx, int dim, int n_parts, uint64_t seed,
+                              pa_unary_net **out) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!out || dim < 64 || dim % 64 || dim > 4096 || n_parts < 1 || n_parts > 64)
+    return fail(ctx, PA_ERR_INVALID, "net: dim must be a multiple of 64 (<= 4096), 1 <= n_parts <= 64");
+  *out = nullptr;
+  DeviceGuard dg(ctx->device);
+  pa_unary_net *net = new pa_unary_net;
+  net->device = ctx->device;
+  net->dim = dim;
+  net->P = n_parts;
+  net_layout(net);
+  const size_t np = (size_t)net->n_params;
+  const size_t bytes = np * 16 + ((size_t)64 * dim + 8 * 64 * 576) * 2 + 256;
+  char *base = nullptr;
+  if (cudaMalloc(&base, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete net;
+    return fail(ctx, PA_ERR_NOMEM, "cannot allocate %zu bytes for the unary net", bytes);
+  }
+  net->params = reinterpret_cast<float *>(base);
+  net->grads = net->params + np;
+  net->adam_m = net->grads + np;
+  net->adam_v = net->adam_m + np;
+  __nv_bfloat16 *w = reinterpret_cast<__nv_bfloat16 *>(net->adam_v + np);
+  net->wf0 = w;
+  w += (size_t)64 * dim;
+  for (int l = 0; l < 4; ++l, w += 64 * 576) net->wf[l] = w;
+  for (int l = 0; l < 4; ++l, w += 64 * 576) net->wd[l] = w;
+  net->err = reinterpret_cast<int *>(w);
+  // He-normal weights from splitmix64 + Box-Muller (the output layer at a
+  // tenth of that, so that its first predictions are close to its bias),
+  // zero biases
+  std::vector<float> h(np, 0.f);
+  uint64_t st = seed ^ 0x6a09e667f3bcc909ull;
+  auto next = [&]() {
+    uint64_t z = (st += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+  };
+  auto unit = [&]() { return ((double)(next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
+  for (int l = 0; l < 5; ++l) {
+    const double sd = std::sqrt(2.0 / (l == 0 ? dim : 576)) * (l == 4 ? 0.1 : 1.0);
+    for (int64_t i = net->off_w[l]; i < net->off_b[l]; i += 2) {
+      const double r = std::sqrt(-2.0 * std::log(unit())), t = 2.0 * M_PI * unit();
+      h[i] = (float)(sd * r * std::cos(t));
+      if (i + 1 < net->off_b[l]) h[i + 1] = (float)(sd * r * std::sin(t));
+    }
+  }
+  *out = net;
+  pa_status s = pa_unary_net_set_params(ctx, net, h.data());
+  if (s) {
+    pa_unary_net_destroy(ctx, net);
+    *out = nullptr;
+  }
+  return s;
+}
+
+pa_status pa_unary_net_destroy(pa_ctx *ctx, pa_unary_net *net) {
+  if (!net) return PA_OK;
+  DeviceGuard dg(net->device);
+  if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (net->scratch) cudaFree(net->scratch);
+  if (net->params) cudaFree(net->params);
+  delete net;
+  return PA_OK;
+}
+
+pa_status pa_unary_net_get_params(pa_ctx *ctx, const pa_unary_net *net, float *params,
+                                  int64_t *n_params) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!net) return fail(ctx, PA_ERR_INVALID, "NULL net");
+  if (n_params) *n_params = net->n_params;
+  if (!params) return PA_OK;
+  DeviceGuard dg(ctx->device);
+  PA_CK(cudaMemcpyAsync(params, net->params, (size_t)net->n_params * 4, cudaMemcpyDeviceToHost,
+                        ctx->stream));
+  return sync_ctx(ctx);
+}
+
+pa_status pa_unary_net_set_params(pa_ctx *ctx, pa_unary_net *net, const float *params) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!net || !params) return fail(ctx, PA_ERR_INVALID, "NULL net or parameters");
+  DeviceGuard dg(ctx->device);
+  const size_t np = (size_t)net->n_params;
+  PA_CK(cudaMemcpyAsync(net->params, params, np * 4, cudaMemcpyHostToDevice, ctx->stream));
+  PA_CK(cudaMemsetAsync(net->grads, 0, np * 12, ctx->stream));  // grads, Adam m and v
+  PA_CK(cudaMemsetAsync(net->err, 0, sizeof(int), ctx->stream));
+  net->step = 0;
+  if (pa_status st = net_pack(ctx, net)) return st;
+  return sync_ctx(ctx);
+}
+
+pa_status pa_unary_net_forward(pa_ctx *ctx, pa_unary_net *net, const void *fields, int fields_bf16,
+                               int n_fields, int ny, int nx, float *out, int64_t out_field_stride,
+                               int64_t out_part_stride, int exp_out) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (pa_status st = net_check_fields(ctx, net, fields, n_fields, ny, nx)) return st;
+  if (!out) return fail(ctx, PA_ERR_INVALID, "NULL output");
+  DeviceGuard dg(ctx->device);
+  NetScratch sc;
+  if (pa_status st = net_scratch(ctx, net, n_fields, ny, nx, !fields_bf16, false, sc)) return st;
+  PA_CK(cudaMemsetAsync(net->err, 0, sizeof(int), ctx->stream));
+  if (pa_status st = net_forward(ctx, net, fields, fields_bf16 ? 1 : 0, n_fields, ny, nx, out,
+                                 out_field_stride, out_part_stride, exp_out ? 1 : 0, sc))
+    return st;
+  return net_err_check(ctx, net);
+}
+
+pa_status pa_unary_net_backward(pa_ctx *ctx, pa_unary_net *net, const void *fields,
+                                int fields_bf16, const float *scores, int n_fields, int ny,
+                                int nx, double *loss, float *grads) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (pa_status st = net_check_fields(ctx, net, fields, n_fields, ny, nx)) return st;
+  if (!scores) return fail(ctx, PA_ERR_INVALID, "NULL scores");
+  DeviceGuard dg(ctx->device);
+  NetScratch sc;
+  if (pa_status st = net_scratch(ctx, net, n_fields, ny, nx, !fields_bf16, true, sc)) return st;
+  PA_CK(cudaMemsetAsync(net->err, 0, sizeof(int), ctx->stream));
+  if (pa_status st = net_backward(ctx, net, fields, fields_bf16 ? 1 : 0, scores, n_fields, ny, nx, sc))
+    return st;
+  double l = 0.0;
+  PA_CK(cudaMemcpyAsync(&l, sc.loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (grads)
+    PA_CK(cudaMemcpyAsync(grads, net->grads, (size_t)net->n_params * 4, cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  if (pa_status st = net_err_check(ctx, net)) return st;
+  if (loss) *loss = l * (1.0 / ((double)n_fields * ny * nx * net->P));
+  return PA_OK;
+}
+
+pa_status pa_unary_net_adam(pa_ctx *ctx, pa_unary_net *net, const pa_adam_param *opt) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!net || !opt || !(opt->lr >= 0.f) || !(opt->beta1 >= 0.f && opt->beta1 < 1.f) ||
+      !(opt->beta2 >= 0.f && opt->beta2 < 1.f) || !(opt->eps > 0.f))
+    return fail(ctx, PA_ERR_INVALID, "invalid Adam parameters");
+  DeviceGuard dg(ctx->device);
+  net->step += 1;
+  AdamArgs a{};
+  a.lr = opt->lr;
+  a.b1 = opt->beta1;
+  a.b2 = opt->beta2;
+  a.eps = opt->eps;
+  a.bc1 = (float)(1.0 - std::pow((double)opt->beta1, (double)net->step));
+  a.bc2 = (float)(1.0 - std::pow((double)opt->beta2, (double)net->step));
+  PA_LAUNCH("net_adam", launch_adam(net->params, net->grads, net->adam_m, net->adam_v,
+                                    net->n_params, a, ctx->stream));
+  if (pa_status st = net_pack(ctx, net)) return st;
+  return sync_ctx(ctx);
+}
+
+pa_status pa_find_obj_batch_learned(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
+                                    const pa_tree *trees, int flip, pa_unary_net *net,
+                                    const int *part_on_net, const pa_classifier *const *cls,
+                                    int n_cls, const void *fields, const float *desc, int ny,
+                                    int nx, int dim, const double *Tig, int tig_shared, int H,
+                                    int W, const pa_ps_outputs *out) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!ep || !exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (n_scales(ep) != 1)
+    return fail(ctx, PA_ERR_UNSUPPORTED,
+                "the descriptors are one scale; run pa_ps_infer on per-scale unaries");
+  if (!net || n_images < 1 || !trees || !Tig || !out || ny < 1 || nx < 1 || dim != net->dim ||
+      H < 1 || W < 1 || H > 32767 || W > 32767 || trees[0].n_parts != net->P)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes, NULL input, or a net of another shape");
+  LearnedUnary lu;
+  lu.net = net;
+  lu.fields = fields;
+  lu.on_net.assign(net->P, 1);
+  if (part_on_net)
+    for (int p = 0; p < net->P; ++p) lu.on_net[p] = part_on_net[p] ? 1 : 0;
+  for (int p = 0; p < net->P; ++p) (lu.on_net[p] ? lu.any_net : lu.any_ada) = true;
+  if (lu.any_net && (!fields || ((uintptr_t)fields & 15)))
+    return fail(ctx, PA_ERR_INVALID, "the net's parts need BF16 fields (16-byte aligned)");
+  if (lu.any_ada && (!desc || !cls || n_cls < net->P))
+    return fail(ctx, PA_ERR_INVALID, "the AdaBoost parts need FP32 descriptors and classifiers");
+  DeviceGuard dg(ctx->device);
+  pa_status st = find_obj_core(ctx, ep, n_images, trees, flip, cls, net->P,
+                               desc, nullptr, PA_MEM_DEVICE, ny, nx, dim, Tig, tig_shared, H, W,
+                               nullptr, 0, (int64_t)n_images * ep->num_rotation_steps, out,
+                               PA_MEM_DEVICE, nullptr, &lu);
+  if (st && st != PA_ERR_NUMERIC) return st;
+  if (lu.any_net)
+    if (pa_status s2 = net_err_check(ctx, net)) return s2;
+  return st;
 }
 
 }  // extern "C"

@@ -2,6 +2,7 @@
 // orchestration of libpartapp_gb300.  Not part of the public C-ABI.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -278,5 +279,59 @@ cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
                           unsigned long long *amax, cudaStream_t s);
 cudaError_t launch_log_z(const float *const *maps, const unsigned long long *amax, int n_maps,
                          int64_t N, double *partials, double *log_z, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Learned unary: convolutions on the tensor cores (k_conv.cu).
+// Activations NHWC bf16 [field][row][column][channel]; weights bf16
+// [64 out channels][taps * cin] (rows past the layer's outputs zero).
+// ---------------------------------------------------------------------------
+enum { kConvReluBf16 = 0, kConvOutF32 = 1, kConvMaskBf16 = 2 };
+struct ConvArgs {
+  int n, H, W, cin_blocks, taps;  // set by launch_conv
+  int mode;                       // kConv*
+  const float *bias;              // kConvReluBf16 / kConvOutF32: [64] / [n_out]
+  void *out;                      // bf16 [pos][64] or fp32 (strided, below)
+  const __nv_bfloat16 *act;       // kConvMaskBf16: gradient kept where act > 0
+  int n_out;                      // kConvOutF32: channels written (1..64)
+  int64_t out_sf, out_sc;         // kConvOutF32: element strides of a field / channel
+  int exp_out;                    // kConvOutF32: write exp of the value
+};
+struct WgradArgs {
+  int H, cin_blocks, taps, n_atoms, m_tiles, xb, kblocks, kb_per_split;
+  float *part;  // [splits][m_tiles * 128][64]
+};
+struct LossArgs {
+  const float *pred, *scores;  // fp32, spatial row-major inside a (field, channel) map
+  int64_t pred_sf, pred_sc, score_sf, score_sc;
+  int n, P, H, W;
+  float inv_count;
+};
+struct AdamArgs {
+  float lr, b1, b2, eps, bc1, bc2;
+};
+struct PackArgs {
+  int dim, P;
+  int64_t off_w[5];
+  __nv_bfloat16 *wf0;    // [64][dim]
+  __nv_bfloat16 *wf[4];  // 3x3 layers 1..4, forward [64][9*64]
+  __nv_bfloat16 *wd[4];  // 3x3 layers 1..4, input gradient [64][9*64]
+};
+// conv over `in` (NHWC, cin channels) with `wts`; see ConvArgs for the output.
+cudaError_t launch_conv(const void *in, int cin, int taps, int n, int H, int W, const void *wts,
+                        const ConvArgs &a, int *err, cudaStream_t s);
+size_t conv_wgrad_part_floats(int cin, int taps, int n, int H, int W);
+// grad[co][tap][ci] (co < cout) from the layer input `in` and dZ [pos][64].
+cudaError_t launch_conv_wgrad(const void *in, int cin, int taps, const void *dz, int n, int H,
+                              int W, int cout, float *part, size_t part_floats, float *grad,
+                              int *err, cudaStream_t s);
+cudaError_t launch_bias_grad(const void *dz, int64_t n_pos, int cout, float *part, int part_blocks,
+                             float *grad, cudaStream_t s);
+int loss_blocks(int64_t n_pos);
+cudaError_t launch_loss_grad(const LossArgs &l, void *dz, float *loss_part, double *loss,
+                             cudaStream_t s);
+cudaError_t launch_adam(float *p, const float *g, float *m, float *v, int64_t n, const AdamArgs &a,
+                        cudaStream_t s);
+cudaError_t launch_pack_weights(const float *params, const PackArgs &a, cudaStream_t s);
+cudaError_t launch_cast_bf16(const float *src, void *dst, int64_t n, cudaStream_t s);
 
 }  // namespace pa
