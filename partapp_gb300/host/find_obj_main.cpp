@@ -24,6 +24,18 @@
 //                  (AbcDetectorParam); height, width, grid_*, dim and tig.txt
 //                  are not used
 //
+// With --scoregrid_dir DIR the unaries come from the score grids the
+// reference's part detector saved (the default branch of findObjectDataset,
+// force_recompute_scores off: findObjectImageRotJoints with bLoadScoreGrid):
+//   DIR/imgidx<i>-pidx<p>-o<flip>-scoregrid.mat   cell_scoregrid, transform_Ti2,
+//                                                 transform_T2g (compressed or not)
+//   exp.txt, joints.txt as above; the image size is exp.txt's height and width,
+//   or the header of img_<i>.pgm when that file exists; classifiers, tig.txt and
+//   descriptors are not used.
+//
+// --mat_dump FILE prints every variable of a MAT-file (name, class, dims and
+// values in MATLAB's column-major order, cells one by one).
+//
 // Writes, into --outdir, the reference's result files pose_est_imgidx<NNNN>.mat
 // (best_conf) and, with --save_marginals, log_part_posterior_final_*.mat, plus
 // best_conf_<i>.txt (one PartHyp::toVect line per part), log_z_<i>.txt and
@@ -39,6 +51,7 @@
 #include <string>
 #include <vector>
 
+#include "mat_io.hpp"
 #include "partapp_gpu.hpp"
 
 using namespace partapp_gpu;
@@ -138,16 +151,56 @@ void write_outputs(const std::string &outdir, int img, bool flip, const FindObjR
       ph << p << " " << h.m_rotidx << " " << h.m_x << " " << h.m_y << " " << h.m_score << "\n";
 }
 
+bool pgm_size(const std::string &path, int &h, int &w) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return false;
+  std::string magic;
+  in >> magic;
+  auto next_int = [&](int &v) {
+    in >> std::ws;
+    while (in.peek() == '#') {
+      std::string line;
+      std::getline(in, line);
+      in >> std::ws;
+    }
+    in >> v;
+  };
+  int maxv = 0;
+  next_int(w);
+  next_int(h);
+  next_int(maxv);
+  return magic == "P5" && (bool)in && w > 0 && h > 0;
+}
+
+void dump_array(const MatArray &a, const std::string &indent) {
+  std::cout << indent << "var " << (a.name.empty() ? "-" : a.name) << " class " << a.mx_class
+            << " dims";
+  for (size_t d : a.dims) std::cout << ' ' << d;
+  std::cout << '\n';
+  if (a.is_cell()) {
+    for (const MatArray &c : a.cells) dump_array(c, indent + "  ");
+    return;
+  }
+  std::cout << indent;
+  char buf[32];
+  for (double v : a.re) {
+    std::snprintf(buf, sizeof buf, "%.17g ", v);
+    std::cout << buf;
+  }
+  std::cout << '\n';
+}
+
 void usage() {
   std::cout << "usage: partapp_find_obj --find_obj --expdir DIR [--outdir DIR] [--first i]\n"
                "                        [--numimgs n] [--batch b] [--flip] [--device d]\n"
-               "                        [--save_marginals] [--from_images]\n";
+               "                        [--save_marginals] [--from_images | --scoregrid_dir DIR]\n"
+               "       partapp_find_obj --mat_dump FILE\n";
 }
 
 }  // namespace
 
 int main(int argc, char **argv) {
-  std::string expdir, outdir;
+  std::string expdir, outdir, scoregrid_dir;
   int first = 0, numimgs = -1, batch = 1, device = 0;
   bool find_obj = false, flip = false, save_marg = false, from_images = false;
   for (int i = 1; i < argc; ++i) {
@@ -166,6 +219,16 @@ int main(int argc, char **argv) {
     else if (a == "--flip") flip = true;
     else if (a == "--save_marginals") save_marg = true;
     else if (a == "--from_images") from_images = true;
+    else if (a == "--scoregrid_dir") scoregrid_dir = next();
+    else if (a == "--mat_dump") {
+      try {
+        for (const MatArray &v : mat_read(next())) dump_array(v, "");
+      } catch (const std::exception &ex) {
+        std::cerr << "partapp_find_obj: " << ex.what() << "\n";
+        return 1;
+      }
+      return 0;
+    }
     else if (a == "--help" || a == "-h") { usage(); return 0; }
     else { std::cerr << "unknown option " << a << "\n"; usage(); return 2; }
   }
@@ -186,7 +249,8 @@ int main(int argc, char **argv) {
     e.roi_save_num_samples = (int)need(kv, "roi_save_num_samples");
     e.use_pairwise = need(kv, "use_pairwise") != 0;
     e.interpolate = need(kv, "interpolate") != 0;
-    const int n_cls = (int)need(kv, "n_classifiers");
+    // the saved-score-grid branch needs no classifiers
+    const int n_cls = scoregrid_dir.empty() ? (int)need(kv, "n_classifiers") : 0;
     const int n_images = (int)need(kv, "n_images");
     if (numimgs < 0) numimgs = n_images - first;
     if (first < 0 || first + numimgs > n_images || batch < 1)
@@ -222,6 +286,32 @@ int main(int argc, char **argv) {
                                                          save_marg);
         write_outputs(outdir, i, flip, r);
         std::cout << "find_obj: image " << i << " (" << w << "x" << h << ") done\n";
+      }
+      return 0;
+    }
+    if (!scoregrid_dir.empty()) {
+      read_joints(expdir + "/joints.txt", app.m_part_conf, app.m_joints);
+      const int P = app.m_part_conf.part_size();
+      Context ctx(device);
+      for (int i = first; i < first + numimgs; ++i) {
+        int h = 0, w = 0;
+        if (!pgm_size(expdir + "/img_" + std::to_string(i) + ".pgm", h, w)) {
+          h = (int)need(kv, "height");
+          w = (int)need(kv, "width");
+        }
+        std::vector<Joint> joints = app.m_joints;
+        const std::string jp = expdir + "/joints_" + std::to_string(i) + ".txt";
+        if (exists(jp)) {
+          PartConfig pc;
+          read_joints(jp, pc, joints);
+        }
+        std::vector<ScoreGridSet> parts;
+        for (int p = 0; p < P; ++p)
+          parts.push_back(loadScoreGrid(scoreGridFileName(scoregrid_dir, i, p, flip)));
+        const FindObjResult r =
+            findObjectImageFromScoreGrids(ctx, app, flip, joints, parts, h, w, save_marg);
+        write_outputs(outdir, i, flip, r);
+        std::cout << "find_obj: image " << i << " (" << w << "x" << h << ", saved score grids) done\n";
       }
       return 0;
     }

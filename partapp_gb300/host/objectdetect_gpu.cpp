@@ -55,7 +55,7 @@ PartHyp to_hyp(const pa_part_hyp &h) {
   return p;
 }
 
-void require(bool ok, const char *what) {
+void require(bool ok, const std::string &what) {
   if (!ok) throw Error(PA_ERR_INVALID, what);
 }
 
@@ -313,6 +313,100 @@ FindObjResult findObjectImageFromImage(Context &ctx, const PartApp &part_app, bo
     out.o.log_marg = marg.data();
   }
   // the first P classifiers' unaries are the leading [P][S][R][H][W] block
+  ctx.check(pa_ps_infer(ctx.get(), &e, &th.t, flip ? 1 : 0, 1, lu.data(), img_h, img_w, &out.o,
+                        PA_MEM_HOST));
+  FindObjResult r = out.result(P, K);
+  if (want_marginals)
+    for (size_t k = 0; k < (size_t)P * S; ++k) {
+      FloatGrid3 g(R, img_h, img_w);
+      std::memcpy(g.data(), marg.data() + k * N, N * sizeof(float));
+      r.log_marginals.push_back(std::move(g));
+    }
+  return r;
+}
+
+std::string scoreGridFileName(const std::string &dir, int imgidx, int pidx, bool flip) {
+  return dir + "/imgidx" + std::to_string(imgidx) + "-pidx" + std::to_string(pidx) + "-o" +
+         std::to_string(flip ? 1 : 0) + "-scoregrid.mat";
+}
+
+ScoreGridSet loadScoreGrid(const std::string &path) {
+  const std::vector<MatArray> vars = mat_read(path);
+  const MatArray &cell = mat_find(vars, "cell_scoregrid");
+  const MatArray &ti2 = mat_find(vars, "transform_Ti2");
+  const MatArray &t2g = mat_find(vars, "transform_T2g");
+  require(cell.is_cell() && cell.dims.size() == 2, path + ": cell_scoregrid is not a 2-d cell");
+  ScoreGridSet g;
+  g.S = (int)cell.dims[0];
+  g.R = (int)cell.dims[1];
+  for (const MatArray *t : {&ti2, &t2g})
+    require(!t->is_cell() && t->dims.size() == 4 && (int)t->dims[0] == g.S &&
+                (int)t->dims[1] == g.R && t->dims[2] == 3 && t->dims[3] == 3,
+            path + ": transforms are not [scales][rotations][3][3]");
+  for (int s = 0; s < g.S; ++s)
+    for (int r = 0; r < g.R; ++r) {
+      const MatArray &e = cell.cells[(size_t)s + (size_t)g.S * r];  // Fortran order
+      require(!e.is_cell() && e.dims.size() == 2, path + ": a score grid is not 2-d");
+      const int ny = (int)e.dims[0], nx = (int)e.dims[1];
+      std::vector<float> v((size_t)ny * nx);
+      for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) v[(size_t)y * nx + x] = (float)e.re[(size_t)y + (size_t)ny * x];
+      g.ny.push_back(ny);
+      g.nx.push_back(nx);
+      g.grid.push_back(std::move(v));
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          // the float arrays become the double matrices of the product
+          g.Ti2.push_back((double)(float)mat_at(ti2, {(size_t)s, (size_t)r, (size_t)i, (size_t)j}));
+          g.T2g.push_back((double)(float)mat_at(t2g, {(size_t)s, (size_t)r, (size_t)i, (size_t)j}));
+        }
+    }
+  return g;
+}
+
+FindObjResult findObjectImageFromScoreGrids(Context &ctx, const PartApp &part_app, bool flip,
+                                            const std::vector<Joint> &joints,
+                                            const std::vector<ScoreGridSet> &parts, int img_h,
+                                            int img_w, bool want_marginals) {
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int P = part_app.m_part_conf.part_size();
+  const int S = std::max(1, e.num_scale_steps), R = e.num_rotation_steps;
+  require((int)parts.size() >= P, "saved score grids for every part");
+  const size_t N = (size_t)R * img_h * img_w;
+  std::vector<float> lu((size_t)P * S * N);
+  for (int p = 0; p < P; ++p) {
+    const ScoreGridSet &g = parts[p];
+    require(g.S == S && g.R == R, "saved score grids: scale or rotation count differs");
+    for (int s = 0; s < S; ++s) {
+      // one pa_unary_maps call per (part, scale): the grids of a scale share
+      // their size; Tig = prod(Ti2, T2g) per rotation (partapp.cpp:877-880)
+      const int ny = g.ny[(size_t)s * R], nx = g.nx[(size_t)s * R];
+      std::vector<float> sc((size_t)R * ny * nx);
+      std::vector<double> tig((size_t)R * 9);
+      for (int r = 0; r < R; ++r) {
+        const size_t k = (size_t)s * R + r;
+        require(g.ny[k] == ny && g.nx[k] == nx, "saved score grids of one scale differ in size");
+        std::memcpy(sc.data() + (size_t)r * ny * nx, g.grid[k].data(), sizeof(float) * ny * nx);
+        const double *a = &g.Ti2[k * 9], *b = &g.T2g[k * 9];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int q = 0; q < 3; ++q) acc += a[i * 3 + q] * b[q * 3 + j];
+            tig[(size_t)r * 9 + i * 3 + j] = acc;
+          }
+      }
+      ctx.check(pa_unary_maps(ctx.get(), sc.data(), 1, R, ny, nx, tig.data(), 0, e.interpolate,
+                              img_h, img_w, lu.data() + ((size_t)p * S + s) * N, PA_MEM_HOST));
+    }
+  }
+  const TreeHolder th(part_app.m_part_conf, part_app.m_part_conf.rootpart_idx, joints);
+  const int K = e.roi_save_num_samples > 0 ? e.roi_save_num_samples : 1;
+  ImageOut out(P, K, S);
+  std::vector<float> marg;
+  if (want_marginals) {
+    marg.resize((size_t)P * S * N);
+    out.o.log_marg = marg.data();
+  }
   ctx.check(pa_ps_infer(ctx.get(), &e, &th.t, flip ? 1 : 0, 1, lu.data(), img_h, img_w, &out.o,
                         PA_MEM_HOST));
   FindObjResult r = out.result(P, K);

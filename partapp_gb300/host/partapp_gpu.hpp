@@ -218,6 +218,30 @@ FindObjResult findObjectImageFromImage(Context &ctx, const PartApp &part_app, bo
                                        const std::vector<Joint> &joints, const float *image,
                                        int img_h, int img_w, bool want_marginals = false);
 
+// One part's saved score grids as PartApp::loadScoreGrid reads them
+// (libPartApp/partapp.cpp:830-903) from
+// <dir>/imgidx<i>-pidx<p>-o<flip>-scoregrid.mat (getScoreGridFileName,
+// partapp.cpp:792-799): cell_scoregrid[scale][rot] grids [ny][nx] (C order
+// here) and transform_Ti2 / transform_T2g [scale][rot][3][3].
+struct ScoreGridSet {
+  int S = 0, R = 0;
+  std::vector<int> ny, nx;                 // per (scale, rot)
+  std::vector<std::vector<float>> grid;    // per (scale, rot): [ny][nx]
+  std::vector<double> Ti2, T2g;            // [S][R][9], row-major 3x3
+};
+std::string scoreGridFileName(const std::string &dir, int imgidx, int pidx, bool flip);
+ScoreGridSet loadScoreGrid(const std::string &path);
+
+// findObjectImageRotJoints with bLoadScoreGrid = true, the default branch of
+// findObjectDataset (objectdetect_aux.cpp:382-390): every part's saved grids
+// mapped into the image with Tig = Ti2 * T2g per (scale, rot)
+// (loadScoreGrid, TM_BILINEAR if interpolate else TM_DIRECT), clip_scores_fill
+// + computeLogGrid, then computeRootPosteriorRot with bIsSparse = true.
+FindObjResult findObjectImageFromScoreGrids(Context &ctx, const PartApp &part_app, bool flip,
+                                            const std::vector<Joint> &joints,
+                                            const std::vector<ScoreGridSet> &parts, int img_h,
+                                            int img_w, bool want_marginals = false);
+
 // The reference's result files (objectdetect_findrot.cpp:238-251, 1005-1011):
 // pose_est_imgidx<NNNN>.mat with best_conf [P][7], and per part
 // log_part_posterior_final_imgidx<i>_scaleidx0_o<flip>_pidx<p>.mat with
