@@ -23,6 +23,9 @@
 // split over CTAs; each CTA writes its partial sums and k_wgrad_reduce adds
 // them in a fixed order (deterministic results).
 //
+// k_conv3_persist: the 3x3 layers as persistent CTAs (resident weights, each
+// input row loaded once per output row segment; see below).
+//
 // Every mbarrier wait is bounded (bit 8 of *err on time-out) and tensor
 // memory is freed on every path.
 #include <cuda.h>
@@ -72,6 +75,48 @@ __device__ __forceinline__ void tap_shift(int taps, int t, int &dy, int &dx) {
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const __nv_bfloat162 q = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t *>(&q);
+}
+
+// Epilogue of one thread's output position: 16 accumulator columns from
+// c0, stored as the layer's mode asks (ConvArgs).
+__device__ __forceinline__ void conv_store16(const ConvArgs &a, int64_t pos, int f, int y, int x,
+                                             int c0, const uint32_t (&v)[16]) {
+  if (a.mode == kConvReluBf16) {
+    uint32_t h[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      h[j] = pack_bf16(fmaxf(__uint_as_float(v[2 * j]) + a.bias[c0 + 2 * j], 0.f),
+                       fmaxf(__uint_as_float(v[2 * j + 1]) + a.bias[c0 + 2 * j + 1], 0.f));
+    uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(a.out) + pos * kCN + c0);
+    o[0] = make_uint4(h[0], h[1], h[2], h[3]);
+    o[1] = make_uint4(h[4], h[5], h[6], h[7]);
+  } else if (a.mode == kConvMaskBf16) {
+    const uint4 *m = reinterpret_cast<const uint4 *>(a.act + pos * kCN + c0);
+    const uint4 m0 = m[0], m1 = m[1];
+    const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+    uint32_t h[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const __nv_bfloat162 q = *reinterpret_cast<const __nv_bfloat162 *>(&mw[j]);
+      const float lo = __low2float(q) > 0.f ? __uint_as_float(v[2 * j]) : 0.f;
+      const float hi = __high2float(q) > 0.f ? __uint_as_float(v[2 * j + 1]) : 0.f;
+      h[j] = pack_bf16(lo, hi);
+    }
+    uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(a.out) + pos * kCN + c0);
+    o[0] = make_uint4(h[0], h[1], h[2], h[3]);
+    o[1] = make_uint4(h[4], h[5], h[6], h[7]);
+  } else {
+    float *o = reinterpret_cast<float *>(a.out) + (int64_t)f * a.out_sf + (int64_t)y * a.W + x;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int c = c0 + j;
+      if (c < a.n_out) {
+        float val = __uint_as_float(v[j]) + a.bias[c];
+        if (a.exp_out) val = expf(val);
+        o[(int64_t)c * a.out_sc] = val;
+      }
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kConvThreads, 2)
@@ -148,43 +193,7 @@ __global__ void __launch_bounds__(kConvThreads, 2)
     for (int c0 = 0; c0 < c_end; c0 += 16) {
       uint32_t v[16];
       tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (!live) continue;
-      if (a.mode == kConvReluBf16) {
-        uint32_t h[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          h[j] = pack_bf16(fmaxf(__uint_as_float(v[2 * j]) + a.bias[c0 + 2 * j], 0.f),
-                           fmaxf(__uint_as_float(v[2 * j + 1]) + a.bias[c0 + 2 * j + 1], 0.f));
-        uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(a.out) + pos * kCN + c0);
-        o[0] = make_uint4(h[0], h[1], h[2], h[3]);
-        o[1] = make_uint4(h[4], h[5], h[6], h[7]);
-      } else if (a.mode == kConvMaskBf16) {
-        const uint4 *m = reinterpret_cast<const uint4 *>(a.act + pos * kCN + c0);
-        const uint4 m0 = m[0], m1 = m[1];
-        const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
-        uint32_t h[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const __nv_bfloat162 q = *reinterpret_cast<const __nv_bfloat162 *>(&mw[j]);
-          const float lo = __low2float(q) > 0.f ? __uint_as_float(v[2 * j]) : 0.f;
-          const float hi = __high2float(q) > 0.f ? __uint_as_float(v[2 * j + 1]) : 0.f;
-          h[j] = pack_bf16(lo, hi);
-        }
-        uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(a.out) + pos * kCN + c0);
-        o[0] = make_uint4(h[0], h[1], h[2], h[3]);
-        o[1] = make_uint4(h[4], h[5], h[6], h[7]);
-      } else {
-        float *o = reinterpret_cast<float *>(a.out) + (int64_t)f * a.out_sf + (int64_t)y * a.W + x;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int c = c0 + j;
-          if (c < a.n_out) {
-            float val = __uint_as_float(v[j]) + a.bias[c];
-            if (a.exp_out) val = expf(val);
-            o[(int64_t)c * a.out_sc] = val;
-          }
-        }
-      }
+      if (live) conv_store16(a, pos, f, y, x, c0, v);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -293,6 +302,121 @@ __global__ void __launch_bounds__(kConvThreads, 2)
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     tc::tmem_dealloc(tmem, kCN);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_conv3_persist: the 3x3, 64-channel layers (forward and input gradient).
+// Persistent: one CTA per SM walks row segments t = blockIdx.x, +gridDim.x.
+// The layer's nine 64 x 64 weight blocks stay resident in shared memory; per
+// row segment the three input rows y-1, y, y+1 are loaded once (130
+// positions x0-1 .. x0+128 each, zero-filled outside the field) and tap
+// (dy, dx) reads rows dx+1 .. dx+128 of row tile dy+1: its A descriptor
+// starts (dx+1) * 128 bytes into the tile.  Row tiles and accumulators are
+// double-buffered: warp 0 loads tile j+1 and warp 1 issues its MMAs while
+// warps 2..5 drain tile j from tensor memory.
+// ---------------------------------------------------------------------------
+constexpr int kRowPos = kCM + 2;                          // 130 positions per input row
+constexpr int kRowTile = ((kRowPos * 128 + 1023) / 1024) * 1024;  // 17 KB
+constexpr int kP3Threads = 192;
+constexpr int kP3W = 9 * kBBytes;                         // resident weights, 72 KB
+constexpr int kP3Smem = kP3W + 2 * 3 * kRowTile + 1024;
+
+__global__ void __launch_bounds__(kP3Threads, 1)
+    k_conv3_persist(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    ConvArgs a, int n_tiles, int *err) {
+  extern __shared__ uint8_t smraw[];
+  uint8_t *sm = reinterpret_cast<uint8_t *>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  uint8_t *sw = sm;                // [9] weight blocks (8 KB each)
+  uint8_t *srow = sm + kP3W;       // [2][3] row tiles
+  __shared__ __align__(8) uint64_t wfull, full[2], empty[2], acc_full[2], acc_empty[2];
+  __shared__ uint32_t tmem_base;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int xt = (a.W + kCM - 1) / kCM;
+  if (threadIdx.x == 0) {
+    mbar_init(&wfull, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], 1);
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 4);  // one arrive per epilogue warp
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 2 * kCN);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 0 && lane == 0) {
+    mbar_arrive_expect_tx(&wfull, kP3W);
+    for (int t = 0; t < 9; ++t) tc::tma_load_2d(sw + t * kBBytes, &tmB, t * kCK, 0, &wfull);
+    int j = 0;
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++j) {
+      const int b = j & 1;
+      if (j >= 2 && !mbar_wait(&empty[b], ((j >> 1) - 1) & 1, err)) break;
+      const int xi = tile % xt, r = tile / xt, y = r % a.H, f = r / a.H;
+      mbar_arrive_expect_tx(&full[b], 3 * kRowPos * 128);
+      for (int dy = 0; dy < 3; ++dy)
+        tc::tma_load_4d(srow + (b * 3 + dy) * kRowTile, &tmA, 0, xi * kCM - 1, y + dy - 1, f,
+                        &full[b]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    bool ok = mbar_wait(&wfull, 0, err);
+    int j = 0;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++j) {
+      const int b = j & 1;
+      if (j >= 2 && !mbar_wait(&acc_empty[b], ((j >> 1) - 1) & 1, err)) break;
+      if (!mbar_wait(&full[b], (j >> 1) & 1, err)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t acc = tmem + (uint32_t)(b * kCN);
+      for (int t = 0; t < 9; ++t) {
+        const uint32_t sa = smem_u32(srow + (b * 3 + t / 3) * kRowTile) + (uint32_t)((t % 3) * 128);
+        const uint32_t sb = smem_u32(sw + t * kBBytes);
+#pragma unroll
+        for (int kk = 0; kk < kCK / 16; ++kk)
+          tc::mma_bf16(acc, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), kIdescConv,
+                       (t > 0 || kk > 0) ? 1u : 0u);
+      }
+      tc::mma_commit(&empty[b]);     // the row tiles are free once read
+      tc::mma_commit(&acc_full[b]);  // the accumulator is complete
+    }
+  } else if (warp >= 2) {
+    const int lg = warp & 3;  // TMEM lane group of this warp
+    int j = 0;
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++j) {
+      const int b = j & 1;
+      bool ready = true;
+      if (lane == 0) ready = mbar_wait(&acc_full[b], (j >> 1) & 1, err);
+      ready = __shfl_sync(0xFFFFFFFFu, ready ? 1 : 0, 0) != 0;
+      if (!ready) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int xi = tile % xt, r = tile / xt, y = r % a.H, f = r / a.H;
+      const int x = xi * kCM + lg * 32 + lane;
+      const bool live = x < a.W;
+      const int64_t pos = ((int64_t)f * a.H + y) * a.W + x;
+      const int c_end = a.mode == kConvOutF32 ? a.n_out : kCN;
+#pragma unroll 1
+      for (int c0 = 0; c0 < c_end; c0 += 16) {
+        uint32_t v[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * kCN + c0), v);
+        if (live) conv_store16(a, pos, f, y, x, c0, v);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b]))
+                     : "memory");
+    }
+  }
+  __syncwarp();
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tc::tmem_dealloc(tmem, 2 * kCN);
   }
 }
 
@@ -471,11 +595,25 @@ cudaError_t launch_conv(const void *in, int cin, int taps, int n, int H, int W, 
   a.cin_blocks = cin / 64;
   a.taps = taps;
   CUtensorMap ma, mb;
-  if (!tc::make_map_nhwc(&ma, in, cin, W, H, n, kCM) ||
-      !tc::make_map_2d(&mb, wts, (uint64_t)taps * cin, 64, (uint64_t)taps * cin * 2, kCK, kCN))
+  if (!tc::make_map_2d(&mb, wts, (uint64_t)taps * cin, 64, (uint64_t)taps * cin * 2, kCK, kCN))
     return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_igemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kConvSmem);
+  cudaError_t e;
+  if (taps == 9 && cin == 64) {
+    // 3x3 layers: persistent CTAs with resident weights and reused input rows
+    if (!tc::make_map_nhwc(&ma, in, cin, W, H, n, kRowPos)) return cudaErrorInvalidValue;
+    e = cudaFuncSetAttribute(k_conv3_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, kP3Smem);
+    if (e != cudaSuccess) return e;
+    const int64_t n_tiles = (int64_t)n * H * ((W + kCM - 1) / kCM);
+    if (n_tiles > 0x7FFFFFFF) return cudaErrorInvalidValue;
+    int sms = 152, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = (int)std::min<int64_t>(n_tiles, sms);
+    k_conv3_persist<<<grid, kP3Threads, kP3Smem, s>>>(ma, mb, a, (int)n_tiles, err);
+    return cudaGetLastError();
+  }
+  if (!tc::make_map_nhwc(&ma, in, cin, W, H, n, kCM)) return cudaErrorInvalidValue;
+  e = cudaFuncSetAttribute(k_conv_igemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
   if (e != cudaSuccess) return e;
   dim3 grid((unsigned)((W + kCM - 1) / kCM), (unsigned)H, (unsigned)n);
   k_conv_igemm<<<grid, kConvThreads, kConvSmem, s>>>(ma, mb, a, err);
