@@ -23,8 +23,11 @@
 // split over CTAs; each CTA writes its partial sums and k_wgrad_reduce adds
 // them in a fixed order (deterministic results).
 //
-// k_conv3_persist: the 3x3 layers as persistent CTAs (resident weights, each
-// input row loaded once per output row segment; see below).
+// k_conv3_persist: the 3x3, 64-channel layers as persistent CTAs (resident
+// weights, each input row loaded once per output row segment, double-buffered
+// accumulators; see below).  k_conv_igemm serves the 1x1 layer: one row
+// segment per CTA, two CTAs per SM, measured faster there than a persistent
+// form whose resident weights leave room for fewer loads in flight.
 //
 // Every mbarrier wait is bounded (bit 8 of *err on time-out) and tensor
 // memory is freed on every path.

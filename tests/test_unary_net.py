@@ -104,8 +104,10 @@ def _layer_errs(g, want, dim, P):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dim,n,H,W", [(192, 3, 7, 150), (960, 2, 6, 80), (64, 1, 1, 1)])
+@pytest.mark.parametrize("dim,n,H,W", [(192, 3, 7, 150), (960, 2, 6, 80), (64, 1, 1, 1),
+                                       (1344, 1, 3, 20)])
 def test_forward_matches_oracle(ctx, pa, dim, n, H, W):
+    """Shapes: two row tiles (W = 150), 960-d fields, a 1 x 1 field, 21 channel blocks."""
     import torch
 
     rng = np.random.default_rng(dim + W)
