@@ -131,7 +131,10 @@ __global__ void __launch_bounds__(kConvThreads, 2)
   __shared__ uint32_t tmem_base;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // a.flat (1x1 layers): the tile is 128 consecutive positions of the
+  // flattened [field][row][column] index, read through a 2-D map
   const int x0 = blockIdx.x * kCM, y = blockIdx.y, f = blockIdx.z;
+  const int64_t p0 = (int64_t)blockIdx.x * kCM;
   const int nk = a.taps * a.cin_blocks;
 
   if (threadIdx.x == 0) {
@@ -158,7 +161,8 @@ __global__ void __launch_bounds__(kConvThreads, 2)
       tap_shift(a.taps, t, dy, dx);
       uint8_t *sa = sm + s * kStageC;
       mbar_arrive_expect_tx(&full[s], kStageC);
-      tc::tma_load_4d(sa, &tmA, cb * kCK, x0 + dx, y + dy, f, &full[s]);
+      if (a.flat) tc::tma_load_2d(sa, &tmA, cb * kCK, (int)p0, &full[s]);
+      else tc::tma_load_4d(sa, &tmA, cb * kCK, x0 + dx, y + dy, f, &full[s]);
       tc::tma_load_2d(sa + kABytes, &tmB, kb * kCK, 0, &full[s]);
     }
   } else if (warp == 1 && lane == 0) {
@@ -188,15 +192,27 @@ __global__ void __launch_bounds__(kConvThreads, 2)
   ready = __shfl_sync(0xFFFFFFFFu, ready ? 1 : 0, 0) != 0;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ready) {
-    const int x = x0 + warp * 32 + lane;
-    const bool live = x < a.W;
-    const int64_t pos = ((int64_t)f * a.H + y) * a.W + x;
+    int64_t pos;
+    int pf = f, py = y, px = x0 + warp * 32 + lane;
+    bool live;
+    if (a.flat) {
+      pos = p0 + warp * 32 + lane;
+      const int64_t hw = (int64_t)a.H * a.W;
+      live = pos < (int64_t)a.n * hw;
+      pf = (int)(pos / hw);
+      const int yx = (int)(pos - pf * hw);
+      py = yx / a.W;
+      px = yx - py * a.W;
+    } else {
+      live = px < a.W;
+      pos = ((int64_t)f * a.H + y) * a.W + px;
+    }
     const int c_end = a.mode == kConvOutF32 ? a.n_out : kCN;
 #pragma unroll 1
     for (int c0 = 0; c0 < c_end; c0 += 16) {
       uint32_t v[16];
       tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (live) conv_store16(a, pos, f, y, x, c0, v);
+      if (live) conv_store16(a, pos, pf, py, px, c0, v);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -615,10 +631,16 @@ cudaError_t launch_conv(const void *in, int cin, int taps, int n, int H, int W, 
     k_conv3_persist<<<grid, kP3Threads, kP3Smem, s>>>(ma, mb, a, (int)n_tiles, err);
     return cudaGetLastError();
   }
-  if (!tc::make_map_nhwc(&ma, in, cin, W, H, n, kCM)) return cudaErrorInvalidValue;
+  // 1x1: one GEMM over the flattened positions (full 128-position tiles)
+  const int64_t n_pos = (int64_t)n * H * W;
+  a.flat = taps == 1 && (n_pos + kCM - 1) / kCM <= 0x7FFFFFFF && n_pos <= 0x7FFFFFFF;
+  if (a.flat ? !tc::make_map_2d(&ma, in, (uint64_t)cin, (uint64_t)n_pos, (uint64_t)cin * 2, kCK, kCM)
+             : !tc::make_map_nhwc(&ma, in, cin, W, H, n, kCM))
+    return cudaErrorInvalidValue;
   e = cudaFuncSetAttribute(k_conv_igemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)((W + kCM - 1) / kCM), (unsigned)H, (unsigned)n);
+  dim3 grid = a.flat ? dim3((unsigned)((n_pos + kCM - 1) / kCM), 1, 1)
+                     : dim3((unsigned)((W + kCM - 1) / kCM), (unsigned)H, (unsigned)n);
   k_conv_igemm<<<grid, kConvThreads, kConvSmem, s>>>(ma, mb, a, err);
   return cudaGetLastError();
 }

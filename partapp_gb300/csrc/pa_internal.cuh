@@ -295,6 +295,7 @@ struct ConvArgs {
   int n_out;                      // kConvOutF32: channels written (1..64)
   int64_t out_sf, out_sc;         // kConvOutF32: element strides of a field / channel
   int exp_out;                    // kConvOutF32: write exp of the value
+  int flat;                       // set by launch_conv: 1x1 over flattened positions
 };
 struct WgradArgs {
   int H, cin_blocks, taps, n_atoms, m_tiles, xb, kblocks, kb_per_split;
