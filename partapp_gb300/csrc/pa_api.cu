@@ -83,6 +83,10 @@ struct pa_ctx {
   std::map<std::string, Acc> times;
   std::vector<std::string> names;  // stable storage for pa_ctx_timing_get
   int msg_math = PA_MSG_FP32;      // spatial filter of diagonal-covariance messages
+  // worker contexts (own stream, workspace, staging and landing slots) that
+  // run independent image groups of one pa_find_obj_multi call side by side
+  static constexpr int kWorkers = 4;
+  std::vector<pa_ctx *> workers;
 };
 
 namespace {
@@ -1997,6 +2001,8 @@ pa_status pa_ctx_create(int device, pa_ctx **out) {
 
 pa_status pa_ctx_destroy(pa_ctx *ctx) {
   if (!ctx) return PA_OK;
+  for (pa_ctx *w : ctx->workers) pa_ctx_destroy(w);
+  ctx->workers.clear();
   {
     DeviceGuard dg(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -3103,6 +3109,130 @@ pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
     ++n_groups;
   }
   pa_status result = PA_OK;
+  if (mem == PA_MEM_DEVICE && n_groups > 1) {
+    // Device inputs: the groups run on up to kWorkers worker contexts, each
+    // with its own stream and workspace, so that the small grids of several
+    // images fill the GPU together.  On each worker the groups are queued
+    // back to back: the host plans group g + NW while the GPU computes the
+    // worker's previous groups; each group's small results land in one of
+    // the worker's pinned slots and are decoded once its stream has passed
+    // them, before the slot is reused.
+    DeviceGuard dg(ctx->device);
+    const int NW = std::min(n_groups, pa_ctx::kWorkers);
+    while ((int)ctx->workers.size() < NW) {
+      pa_ctx *w = nullptr;
+      if (pa_ctx_create(ctx->device, &w) != PA_OK)
+        return fail(ctx, PA_ERR_CUDA, "cannot create a worker context");
+      ctx->workers.push_back(w);
+    }
+    while (ctx->ring_done.empty()) {
+      cudaEvent_t ev;
+      PA_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      ctx->ring_done.push_back(ev);
+    }
+    // the workers start behind everything queued on the caller's stream
+    PA_CK(cudaEventRecord(ctx->ring_done[0], ctx->stream));
+    const int nslots = pa_ctx::kLandings;
+    struct WorkerState {
+      std::vector<PendingImage> pend;
+      std::vector<const pa_exp_param *> pend_e;
+      int count = 0;
+    };
+    std::vector<WorkerState> ws(NW);
+    for (int w = 0; w < NW; ++w) {
+      pa_ctx *wc = ctx->workers[w];
+      wc->msg_math = ctx->msg_math;
+      wc->timing = ctx->timing;
+      while ((int)wc->ring_done.size() < nslots) {
+        cudaEvent_t ev;
+        PA_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        wc->ring_done.push_back(ev);
+      }
+      PA_CK(cudaStreamWaitEvent(wc->stream, ctx->ring_done[0], 0));
+      ws[w].pend.resize(nslots);
+      ws[w].pend_e.assign(nslots, nullptr);
+    }
+    std::vector<std::vector<pa_ps_outputs>> gouts(n_groups);
+    auto drain = [&]() {
+      for (int w = 0; w < NW; ++w) cudaStreamSynchronize(ctx->workers[w]->stream);
+    };
+    auto complete = [&](int w, int k) -> pa_status {
+      pa_ctx *wc = ctx->workers[w];
+      PendingImage &pi = ws[w].pend[k];
+      pi.busy = false;
+      if (cudaEventSynchronize(wc->ring_done[k]) != cudaSuccess)
+        return fail(ctx, PA_ERR_CUDA, "worker stream: %s", cudaGetErrorString(cudaGetLastError()));
+      const pa_status st = finish_complete(wc, ws[w].pend_e[k], pi.pl, pi.outs, pi.rb);
+      if (st == PA_ERR_NUMERIC) {
+        result = st;
+        return PA_OK;
+      }
+      if (st) ctx->err = wc->err;
+      return st;
+    };
+    for (int g = 0; g < n_groups; ++g) {
+      const int w = g % NW, k = ws[w].count % nslots;
+      pa_ctx *wc = ctx->workers[w];
+      if (ws[w].pend[k].busy)
+        if (pa_status st = complete(w, k)) {
+          drain();
+          return st;
+        }
+      std::vector<pa_tree> trees;
+      std::vector<const float *> ptrs;
+      int first = -1;
+      for (int i = 0; i < n_images; ++i)
+        if (group[i] == g) {
+          if (first < 0) first = i;
+          trees.push_back(*imgs[i].tree);
+          gouts[g].push_back(*imgs[i].out);
+          ptrs.push_back(imgs[i].desc);
+        }
+      const pa_image &f = imgs[first];
+      const int n = (int)trees.size();
+      ws[w].pend[k].slot = k;
+      ws[w].pend_e[k] = f.ep;
+      pa_status st = find_obj_core(wc, f.ep, n, trees.data(), f.flip, cls, n_cls, ptrs[0],
+                                   ptrs.data(), PA_MEM_DEVICE, f.ny, f.nx, f.dim, f.Tig,
+                                   f.tig_shared, f.H, f.W, nullptr, 0,
+                                   (int64_t)n * f.ep->num_rotation_steps, gouts[g].data(),
+                                   PA_MEM_DEVICE, &ws[w].pend[k]);
+      if (st) {
+        ctx->err = wc->err;
+        drain();
+        return st;
+      }
+      ws[w].pend[k].busy = true;
+      ++ws[w].count;
+      if (cudaEventRecord(wc->ring_done[k], wc->stream) != cudaSuccess) {
+        drain();
+        return fail(ctx, PA_ERR_CUDA, "cannot record a worker event");
+      }
+    }
+    pa_status first_err = PA_OK;
+    for (int w = 0; w < NW; ++w) {
+      pa_ctx *wc = ctx->workers[w];
+      if (pa_status st = sync_ctx(wc)) {
+        ctx->err = wc->err;
+        if (!first_err) first_err = st;
+        continue;
+      }
+      for (int k = 0; k < nslots; ++k)
+        if (ws[w].pend[k].busy)
+          if (pa_status st = complete(w, k))
+            if (!first_err) first_err = st;
+      // the worker's launches and kernel times count for the caller's context
+      ctx->launches += wc->launches;
+      wc->launches = 0;
+      for (auto &kv : wc->times) {
+        auto &acc = ctx->times[kv.first];
+        acc.ms += kv.second.ms;
+        acc.n += kv.second.n;
+      }
+      wc->times.clear();
+    }
+    return first_err ? first_err : result;
+  }
   for (int g = 0; g < n_groups; ++g) {
     std::vector<int> idx;
     for (int i = 0; i < n_images; ++i)
