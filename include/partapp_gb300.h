@@ -401,6 +401,40 @@ typedef struct {
 pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
                             const pa_classifier *const *cls, int n_cls, int mem);
 
+/* ------------------------------------------------- extra unary terms */
+
+/* The poselet-conditioned terms findObjectImageRotJoints adds to the log
+ * detections before computeRootPosteriorRot
+ * (libPictStruct/objectdetect_findrot.cpp:915-948), in that order:
+ *   rotation score  getRotScoreGrid + addExtraUnary (objectdetect_icps.cpp:
+ *                   228-281, 524-547): every detected part p and rotation r
+ *                   gets + rot_weight * log(max(exp(-(rot_r - mu)^2 / (2 var)), 1e-4))
+ *   position score  getPosScoreGrid + addExtraUnary (:366-448): every detected
+ *                   part but the root gets, per pixel (x, y),
+ *                   + pos_weight * log(max(gx * gy, 1e-4)) with
+ *                   gx = exp(-(x - root_det_x - mu_x)^2 / (2 var_x)), gy alike
+ *   torso prior     setTorsoPosPrior (:137-191): the root part gets
+ *                   + log(max(torso_weight * gx * gy, 1e-4)) with
+ *                   gx = exp(-(W/2 - x - mu_x)^2 / (2 var_x)), gy alike
+ * with the reference's float/double typing.  Parameters as the reference's
+ * loaders leave them (getRotParams: variance = squared deviation;
+ * getPosParams; getRootPosDet; getTorsoPosPriorParams).  A NULL parameter
+ * array switches its term off.
+ *   log_unary [n_parts][S][R][H][W] (S = num_scale_steps), updated in place */
+typedef struct {
+  float rot_weight;            /* pred_unary_rot_weight */
+  const double *rot_params;    /* [n_parts][2]: mean rotation (radians), variance */
+  float pos_weight;            /* pred_unary_pos_weight */
+  const double *pos_params;    /* [n_parts][4]: mu_x, mu_y, var_x, var_y (pixels) */
+  double root_det_x, root_det_y;  /* rootpos_det: the root detection (pixels) */
+  float torso_weight;          /* torso_pos_prior_weight */
+  const double *torso_prior;   /* [4]: mu_x, mu_y, var_x, var_y */
+  const int *is_detect;        /* [n_parts] PartDef::is_detect flags, or NULL: all */
+} pa_extra_unary;
+
+pa_status pa_add_extra_unaries(pa_ctx *ctx, const pa_exp_param *ep, const pa_extra_unary *ex,
+                               int n_parts, int root, float *log_unary, int H, int W, int mem);
+
 /* ---------------------------------------------------- learned unary */
 
 /* No counterpart in the reference: a convolutional network that maps a

@@ -129,6 +129,10 @@ def _declare(L):
         fn.restype = C.c_int
     L.orc_find_local_max.argtypes = [fp, C.c_int, C.c_int, C.c_int, C.c_int, dp]
     L.orc_find_local_max.restype = C.c_int
+    L.orc_extra_unary.argtypes = [C.POINTER(OrcExp), C.c_int, C.c_int, C.c_float, dp, C.c_float,
+                                  dp, C.c_double, C.c_double, C.c_float, dp, C.POINTER(C.c_int),
+                                  fp, C.c_int, C.c_int, C.c_int]
+    L.orc_extra_unary.restype = C.c_int
     L.orc_find_obj_f32.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree), C.POINTER(OrcModels), fp,
                                    C.c_int, C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, fp, fp,
                                    fp, fp, fp, ip, fp, ip]
@@ -315,6 +319,39 @@ def find_local_max(grid, max_n):
     out = np.zeros((max(max_n, 1), 4), dtype=np.float64)
     n = lib().orc_find_local_max(_p(g, C.c_float), S, H, W, int(max_n), _p(out, C.c_double))
     return out[:n].copy()
+
+
+def extra_unary(exp: OrcExp, log_unary, root, rot=None, pos=None, torso=None, is_detect=None):
+    """findObjectImageRotJoints' extra unary terms on a copy of log_unary
+    [P][S][R][H][W] (or [P][R][H][W]).  rot = (weight, params [P][2]);
+    pos = (weight, params [P][4], (det_x, det_y)); torso = (weight, params[4])."""
+    u = np.array(log_unary, dtype=np.float32, copy=True)
+    shape = u.shape
+    if u.ndim == 4:
+        u = u[:, None]
+    P, S, R, H, W = u.shape
+    u = np.ascontiguousarray(u)
+    keep = []
+    def arr(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        keep.append(a)
+        return _p(a, C.c_double)
+    rw, rp = (0.0, None) if rot is None else (rot[0], arr(rot[1]))
+    pw, pp, det = (0.0, None, (0.0, 0.0)) if pos is None else (pos[0], arr(pos[1]), pos[2])
+    tw, tp = (0.0, None) if torso is None else (torso[0], arr(torso[1]))
+    isd = None
+    if is_detect is not None:
+        isd_a = np.ascontiguousarray(is_detect, dtype=np.int32)
+        keep.append(isd_a)
+        isd = _p(isd_a, C.c_int)
+    rc = lib().orc_extra_unary(C.byref(exp), P, int(root), float(rw), rp, float(pw), pp,
+                               float(det[0]), float(det[1]), float(tw), tp, isd,
+                               _p(u, C.c_float), S, H, W)
+    if rc:
+        raise ValueError(f"orc_extra_unary failed: {rc}")
+    return u.reshape(shape)
 
 
 def find_obj(exp: OrcExp, tree, models, desc, Tig, H, W, interpolate=True):

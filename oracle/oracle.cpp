@@ -751,6 +751,100 @@ void orc_score_grid_window(const int32_t *f, const float *p, const float *theta,
     }
 }
 
+/* The poselet-conditioned extra unaries findObjectImageRotJoints adds before
+ * computeRootPosteriorRot (libPictStruct/objectdetect_findrot.cpp:915-948),
+ * restated from objectdetect_icps.cpp with the reference's typing:
+ * getRotScoreGrid (:228-281) and addExtraUnary (:524-547), getPosScoreGrid
+ * (:366-448) and addExtraUnary, setTorsoPosPrior (:137-191).  The grids the
+ * reference materialises (log_rot_scores, log_pos_scores: float, zero for
+ * the parts they skip; pred_pos: double) are materialised here too.
+ * lu: [P][S][R][H][W]. */
+int orc_extra_unary(const orc_exp *e, int P, int root, float rot_weight, const double *rot_params,
+                    float pos_weight, const double *pos_params, double root_det_x,
+                    double root_det_y, float torso_weight, const double *torso_prior,
+                    const int *is_detect, float *lu, int S, int H, int W) {
+  if (!e || P < 1 || root < 0 || root >= P || !lu || S < 1 || H < 1 || W < 1) return 1;
+  const int R = e->num_rotation_steps;
+  const size_t HW = (size_t)H * W, N3 = (size_t)R * HW;
+  auto detect = [&](int p) { return is_detect ? is_detect[p] != 0 : true; };
+  std::vector<float> grid((size_t)P * S * N3);
+  if (rot_params) {
+    std::fill(grid.begin(), grid.end(), 0.f);
+    for (int p = 0; p < P; ++p) {
+      if (!detect(p)) continue;
+      std::vector<double> pred_rot(R);
+      const float mu = (float)rot_params[2 * p];
+      const float var = (float)rot_params[2 * p + 1];
+      for (int r = 0; r < R; ++r) {
+        const float rot = (float)(rot_from_index(e, r) / 180 * M_PI);
+        const float d = rot - mu;
+        const float sq = d * d;  /* square(), libMisc/misc.hpp:29 */
+        float score = (float)std::exp(-0.5 * sq / var);
+        if (score < 1e-4) score = (float)1e-4;
+        score = std::log(score);
+        pred_rot[r] = score;
+      }
+      for (int s = 0; s < S; ++s)
+        for (int r = 0; r < R; ++r)
+          for (size_t i = 0; i < HW; ++i)
+            grid[((size_t)p * S + s) * N3 + (size_t)r * HW + i] = (float)pred_rot[r];
+    }
+    for (size_t i = 0; i < grid.size(); ++i) lu[i] += rot_weight * grid[i];
+  }
+  if (pos_params) {
+    std::fill(grid.begin(), grid.end(), 0.f);
+    for (int p = 0; p < P; ++p) {
+      if (p == root || !detect(p)) continue;
+      std::vector<double> pred_pos(HW);
+      const float mu_x = (float)pos_params[4 * p], mu_y = (float)pos_params[4 * p + 1];
+      const float var_x = (float)(pos_params[4 * p + 2] * 1.0f);
+      const float var_y = (float)(pos_params[4 * p + 3] * 1.0f);
+      for (int iy = 0; iy < H; ++iy)
+        for (int ix = 0; ix < W; ++ix) {
+          const float ix_rel = (float)(ix - root_det_x);
+          const float iy_rel = (float)(iy - root_det_y);
+          const float score_x = (float)std::exp(-0.5 * std::pow((double)(ix_rel - mu_x), 2) / var_x);
+          const float score_y = (float)std::exp(-0.5 * std::pow((double)(iy_rel - mu_y), 2) / var_y);
+          float score = score_x * score_y;
+          if (score < 1e-4) score = (float)1e-4;
+          score = std::log(score);
+          pred_pos[(size_t)iy * W + ix] = score;
+        }
+      for (int s = 0; s < S; ++s)
+        for (int r = 0; r < R; ++r)
+          for (size_t i = 0; i < HW; ++i)
+            grid[((size_t)p * S + s) * N3 + (size_t)r * HW + i] = (float)pred_pos[i];
+    }
+    for (size_t i = 0; i < grid.size(); ++i) lu[i] += pos_weight * grid[i];
+  }
+  if (torso_prior) {
+    const float mu_x = (float)torso_prior[0], mu_y = (float)torso_prior[1];
+    float var_x = (float)torso_prior[2], var_y = (float)torso_prior[3];
+    const float img_c_x = (float)(0.5 * W), img_c_y = (float)(0.5 * H);
+    const float sigma_weight = 1.0f, var_weight = sigma_weight * sigma_weight;
+    var_x *= var_weight;
+    var_y *= var_weight;
+    std::vector<double> pred_pos(HW);
+    for (int iy = 0; iy < H; ++iy)
+      for (int ix = 0; ix < W; ++ix) {
+        const float ix_rel = img_c_x - ix, iy_rel = img_c_y - iy;
+        const float score_x = (float)std::exp(-0.5 * std::pow((double)(ix_rel - mu_x), 2) / var_x);
+        const float score_y = (float)std::exp(-0.5 * std::pow((double)(iy_rel - mu_y), 2) / var_y);
+        float score = torso_weight * score_x * score_y;
+        if (score < 1e-4) score = (float)1e-4;
+        score = std::log(score);
+        pred_pos[(size_t)iy * W + ix] = score;
+      }
+    for (int s = 0; s < S; ++s)
+      for (int r = 0; r < R; ++r)
+        for (size_t i = 0; i < HW; ++i) {
+          float &c = lu[((size_t)root * S + s) * N3 + (size_t)r * HW + i];
+          c = (float)(c + pred_pos[i]);
+        }
+  }
+  return 0;
+}
+
 int orc_squeeze_bbox(const float *grid, int ny, int nx, int *bbox) {
   int minx = nx, maxx = -1, miny = ny, maxy = -1;
   for (int ix = 0; ix < nx; ++ix)

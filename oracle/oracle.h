@@ -236,6 +236,12 @@ int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size
                    const double *pos_offset, int desc_step, int desc_size, double ratio,
                    const float *image, int h, int w, int flip, float *log_unary);
 
+/* extra unary terms of findObjectImageRotJoints (objectdetect_findrot.cpp:915-948) */
+int orc_extra_unary(const orc_exp *e, int P, int root, float rot_weight, const double *rot_params,
+                    float pos_weight, const double *pos_params, double root_det_x,
+                    double root_det_y, float torso_weight, const double *torso_prior,
+                    const int *is_detect, float *lu, int S, int H, int W);
+
 #ifdef __cplusplus
 }
 #endif

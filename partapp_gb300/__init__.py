@@ -52,7 +52,7 @@ EXPORTS = (
     "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math", "pa_find_obj_multi",
     "pa_unary_net_create", "pa_unary_net_destroy", "pa_unary_net_get_params",
     "pa_unary_net_set_params", "pa_unary_net_forward", "pa_unary_net_backward",
-    "pa_unary_net_adam", "pa_find_obj_batch_learned",
+    "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
@@ -105,6 +105,13 @@ class PartHyp(C.Structure):
 
 class AdamParam(C.Structure):
     _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float)]
+
+
+class ExtraUnary(C.Structure):
+    _fields_ = [("rot_weight", C.c_float), ("rot_params", C.c_void_p), ("pos_weight", C.c_float),
+                ("pos_params", C.c_void_p), ("root_det_x", C.c_double), ("root_det_y", C.c_double),
+                ("torso_weight", C.c_float), ("torso_prior", C.c_void_p),
+                ("is_detect", C.c_void_p)]
 
 
 class PsOutputs(C.Structure):
@@ -169,6 +176,7 @@ def load_library():
                               ip, ip, vp, P(PsOutputs), ip]
     L.pa_find_obj_batch.argtypes = [vp, P(ExpParam), ip, P(Tree), ip, P(vp), ip, vp, ip, ip, ip,
                                     P(dp), ip, ip, ip, vp, P(PsOutputs), ip]
+    L.pa_add_extra_unaries.argtypes = [vp, P(ExpParam), P(ExtraUnary), ip, ip, vp, ip, ip, ip]
     L.pa_unary_net_create.argtypes = [vp, ip, ip, C.c_uint64, P(vp)]
     L.pa_unary_net_destroy.argtypes = [vp, vp]
     L.pa_unary_net_get_params.argtypes = [vp, vp, vp, P(C.c_int64)]
@@ -528,6 +536,41 @@ class Context:
                                         B.stride(0), C_.data_ptr(), C_.stride(0), M, N, K,
                                         int(band)))
         return C_
+
+    def add_extra_unaries(self, exp: ExpParam, log_unary, root, rot=None, pos=None, torso=None,
+                          is_detect=None):
+        """findObjectImageRotJoints' poselet-conditioned terms, in place on
+        log_unary [P][S][R][H][W] or [P][R][H][W] (numpy or CUDA tensor).
+        rot = (weight, params [P][2]: mean (rad), variance); pos = (weight,
+        params [P][4]: mu_x, mu_y, var_x, var_y, (det_x, det_y)); torso =
+        (weight, params [4])."""
+        u = _Buf(log_unary, np.float32)
+        shp = u.arr.shape
+        P, H, W = shp[0], shp[-2], shp[-1]
+        keep = []
+
+        def arr(a, dt=np.float64):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data
+
+        ex = ExtraUnary()
+        if rot is not None:
+            ex.rot_weight, ex.rot_params = float(rot[0]), arr(rot[1])
+        if pos is not None:
+            ex.pos_weight, ex.pos_params = float(pos[0]), arr(pos[1])
+            ex.root_det_x, ex.root_det_y = float(pos[2][0]), float(pos[2][1])
+        if torso is not None:
+            ex.torso_weight, ex.torso_prior = float(torso[0]), arr(torso[1])
+        if is_detect is not None:
+            ex.is_detect = arr(is_detect, np.int32)
+        self._check(self.L.pa_add_extra_unaries(self.h, C.byref(exp), C.byref(ex), P, int(root),
+                                                u.ptr, H, W, u.mem))
+        if u.mem == PA_MEM_HOST and u.arr is not log_unary:
+            np.copyto(log_unary, u.arr)
+        return log_unary
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,
                                    want_marg=True, is_sparse=False):

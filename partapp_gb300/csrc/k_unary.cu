@@ -302,4 +302,72 @@ cudaError_t launch_fill_int(int *p, int v, int64_t n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Poselet-conditioned extra unaries of findObjectImageRotJoints
+// (libPictStruct/objectdetect_findrot.cpp:915-948, the functions of
+// objectdetect_icps.cpp), added to the log detections in the reference's
+// order and typing:
+//   rotation:  u = u + w_rot * rot_tab[p][r]           (getRotScoreGrid :228-281
+//              + addExtraUnary :524-547, float products and sums)
+//   position:  u = u + w_pos * log(max(gx * gy, 1e-4))  for parts != root
+//              (getPosScoreGrid :366-448), gx = exp(-0.5 (x - det_x - mu_x)^2
+//              / var_x) in double, rounded to float
+//   torso:     u = u + log(max(w * gx * gy, 1e-4))     for the root part, the sum in
+//              double (setTorsoPosPrior :137-191, relative to the image centre)
+// One thread per (part, pixel), walking the part's scales and rotations.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gauss_term(float rel, float mu, float var) {
+  const double d = (double)__fsub_rn(rel, mu);
+  return (float)exp(-0.5 * (d * d) / (double)var);
+}
+
+__global__ void k_extra_unary(ExtraUnary ex, float *__restrict__ lu, int S, int R, int H, int W) {
+  const int p = blockIdx.y;
+  const int64_t HW = (int64_t)H * W;
+  const int64_t pix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (pix >= HW) return;
+  const int iy = (int)(pix / W), ix = (int)(pix - (int64_t)iy * W);
+  const bool detect = ex.is_detect ? ex.is_detect[p] != 0 : true;
+  const bool rot = ex.rot_on;
+  // parts without a position score still get weight * 0 added (the zero
+  // grids of addExtraUnary)
+  float pos_w = __fmul_rn(ex.pos_weight, 0.f);
+  const bool pos = ex.pos_on;
+  if (ex.pos_on && detect && p != ex.root) {
+    const float ixr = (float)((double)ix - ex.root_det_x), iyr = (float)((double)iy - ex.root_det_y);
+    float sc = __fmul_rn(gauss_term(ixr, ex.pos[p].x, ex.pos[p].z), gauss_term(iyr, ex.pos[p].y, ex.pos[p].w));
+    if ((double)sc < 1e-4) sc = 1e-4f;
+    pos_w = __fmul_rn(ex.pos_weight, logf(sc));
+  }
+  bool torso = false;
+  double torso_v = 0.0;
+  if (ex.torso_on && p == ex.root) {
+    const float ixr = __fsub_rn(ex.img_cx, (float)ix), iyr = __fsub_rn(ex.img_cy, (float)iy);
+    float sc = __fmul_rn(__fmul_rn(ex.torso_weight, gauss_term(ixr, ex.torso.x, ex.torso.z)),
+                         gauss_term(iyr, ex.torso.y, ex.torso.w));
+    if ((double)sc < 1e-4) sc = 1e-4f;
+    torso_v = (double)logf(sc);
+    torso = true;
+  }
+  for (int s = 0; s < S; ++s)
+    for (int r = 0; r < R; ++r) {
+      float *c = lu + (((int64_t)p * S + s) * R + r) * HW + pix;
+      float u = *c;
+      if (rot) u = __fadd_rn(u, __fmul_rn(ex.rot_weight, ex.rot_tab[p * R + r]));
+      if (pos) u = __fadd_rn(u, pos_w);
+      if (torso) u = (float)((double)u + torso_v);
+      *c = u;
+    }
+}
+
+cudaError_t launch_extra_unary(const ExtraUnary &ex, float *lu, int P, int S, int R, int H, int W,
+                               cudaStream_t s) {
+  const int64_t HW = (int64_t)H * W;
+  if (P < 1 || P > 65535 || HW < 1 || (HW + kThreads - 1) / kThreads > 0x7FFFFFFF)
+    return cudaErrorInvalidValue;
+  k_extra_unary<<<dim3((unsigned)((HW + kThreads - 1) / kThreads), (unsigned)P), kThreads, 0, s>>>(
+      ex, lu, S, R, H, W);
+  return cudaGetLastError();
+}
+
 }  // namespace pa

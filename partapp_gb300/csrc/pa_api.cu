@@ -3263,6 +3263,81 @@ pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
 }
 
 // ------------------------------------------------------------------------
+// Poselet-conditioned extra unaries (objectdetect_findrot.cpp:915-948)
+// ------------------------------------------------------------------------
+pa_status pa_add_extra_unaries(pa_ctx *ctx, const pa_exp_param *ep, const pa_extra_unary *ex,
+                               int n_parts, int root, float *log_unary, int H, int W, int mem) {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!ep || !exp_ok(ep) || !ex || !log_unary || n_parts < 1 || root < 0 || root >= n_parts ||
+      H < 1 || W < 1 || H > 32767 || W > 32767)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes, parameters or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  DeviceGuard dg(ctx->device);
+  const int S = n_scales(ep), R = ep->num_rotation_steps;
+  const size_t n = (size_t)n_parts * S * R * H * W;
+  // getRotScoreGrid's per-rotation table, typed as the reference types it:
+  // float rot = rot_from_index / 180 * M_PI, square() in float, exp in
+  // double, clipped and logged in float
+  std::vector<float> rot_tab((size_t)n_parts * R, 0.f);
+  if (ex->rot_params)
+    for (int p = 0; p < n_parts; ++p) {
+      if (ex->is_detect && !ex->is_detect[p]) continue;
+      const float mu = (float)ex->rot_params[2 * p], var = (float)ex->rot_params[2 * p + 1];
+      for (int r = 0; r < R; ++r) {
+        const float rot = (float)(rot_from_index(ep, r) / 180 * M_PI);
+        const float d = rot - mu;
+        const float sq = d * d;
+        float sc = (float)std::exp(-0.5 * (double)sq / (double)var);
+        if ((double)sc < 1e-4) sc = 1e-4f;
+        rot_tab[(size_t)p * R + r] = std::log(sc);
+      }
+    }
+  std::vector<float4> pos(n_parts, make_float4(0.f, 0.f, 1.f, 1.f));
+  if (ex->pos_params)
+    for (int p = 0; p < n_parts; ++p)
+      pos[p] = make_float4((float)ex->pos_params[4 * p], (float)ex->pos_params[4 * p + 1],
+                           (float)ex->pos_params[4 * p + 2], (float)ex->pos_params[4 * p + 3]);
+  std::vector<int> det(n_parts, 1);
+  if (ex->is_detect)
+    for (int p = 0; p < n_parts; ++p) det[p] = ex->is_detect[p] ? 1 : 0;
+  Builder b1;
+  b1.param(rot_tab.data(), rot_tab.size());
+  b1.param(pos.data(), pos.size());
+  b1.param(det.data(), det.size());
+  if (mem == PA_MEM_HOST) b1.scratch<float>(n);
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  b.base = ctx->arena;
+  ExtraUnary eu{};
+  eu.root = root;
+  eu.rot_on = ex->rot_params != nullptr;
+  eu.pos_on = ex->pos_params != nullptr;
+  eu.torso_on = ex->torso_prior != nullptr;
+  eu.rot_weight = ex->rot_weight;
+  eu.pos_weight = ex->pos_weight;
+  eu.torso_weight = ex->torso_weight;
+  eu.rot_tab = b.param(rot_tab.data(), rot_tab.size());
+  eu.pos = b.param(pos.data(), pos.size());
+  eu.is_detect = b.param(det.data(), det.size());
+  eu.root_det_x = ex->root_det_x;
+  eu.root_det_y = ex->root_det_y;
+  if (ex->torso_prior)
+    eu.torso = make_float4((float)ex->torso_prior[0], (float)ex->torso_prior[1],
+                           (float)ex->torso_prior[2], (float)ex->torso_prior[3]);
+  eu.img_cx = (float)(0.5 * W);
+  eu.img_cy = (float)(0.5 * H);
+  float *d = mem == PA_MEM_HOST ? b.scratch<float>(n) : log_unary;
+  if ((st = upload_blob(ctx, b))) return st;
+  if (mem == PA_MEM_HOST) PA_CK(cudaMemcpyAsync(d, log_unary, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  PA_LAUNCH("extra_unary", launch_extra_unary(eu, d, n_parts, S, R, H, W, ctx->stream));
+  if (mem == PA_MEM_HOST) PA_CK(cudaMemcpyAsync(log_unary, d, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_ctx(ctx);
+}
+
+// ------------------------------------------------------------------------
 // Learned unary
 // ------------------------------------------------------------------------
 pa_status pa_unary_net_create(pa_ctx *ctx, int dim, int n_parts, uint64_t seed,

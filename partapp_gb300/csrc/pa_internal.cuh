@@ -280,6 +280,22 @@ cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
 cudaError_t launch_log_z(const float *const *maps, const unsigned long long *amax, int n_maps,
                          int64_t N, double *partials, double *log_z, cudaStream_t s);
 
+// Poselet-conditioned extra unaries (k_unary.cu): the rotation score table is
+// built on the host, the position and torso terms per pixel on the device.
+struct ExtraUnary {
+  int root;
+  int rot_on, pos_on, torso_on;
+  float rot_weight, pos_weight, torso_weight;
+  const float *rot_tab;    // [P][R] log rotation scores (float, as the reference stores them)
+  const float4 *pos;       // [P] {mu_x, mu_y, var_x, var_y}
+  double root_det_x, root_det_y;
+  float4 torso;            // {mu_x, mu_y, var_x, var_y}
+  float img_cx, img_cy;    // 0.5 * width, 0.5 * height
+  const int *is_detect;    // [P] or null (every part detected)
+};
+cudaError_t launch_extra_unary(const ExtraUnary &ex, float *lu, int P, int S, int R, int H, int W,
+                               cudaStream_t s);
+
 // ---------------------------------------------------------------------------
 // Learned unary: convolutions on the tensor cores (k_conv.cu).
 // Activations NHWC bf16 [field][row][column][channel]; weights bf16

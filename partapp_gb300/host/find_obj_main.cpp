@@ -33,6 +33,14 @@
 //   or the header of img_<i>.pgm when that file exists; classifiers, tig.txt and
 //   descriptors are not used.
 //
+// The poselet-conditioned extra unary terms (findObjectImageRotJoints,
+// objectdetect_findrot.cpp:855-948) are added, in the --scoregrid_dir and
+// --from_images modes, when asked for:
+//   --pred_dir DIR --pred_rot_weight w   rotation score (testlist_params_rot_imgidx_<i>.mat)
+//   --pred_dir DIR --pred_pos_weight w --torso_det_dir DIR [--rootidx_det k]
+//                                        position score around the torso detection
+//   --torso_prior FILE --torso_prior_weight w   torso position prior
+//
 // --mat_dump FILE prints every variable of a MAT-file (name, class, dims and
 // values in MATLAB's column-major order, cells one by one).
 //
@@ -194,13 +202,18 @@ void usage() {
   std::cout << "usage: partapp_find_obj --find_obj --expdir DIR [--outdir DIR] [--first i]\n"
                "                        [--numimgs n] [--batch b] [--flip] [--device d]\n"
                "                        [--save_marginals] [--from_images | --scoregrid_dir DIR]\n"
+               "                        [--pred_dir DIR --pred_rot_weight w --pred_pos_weight w\n"
+               "                         --torso_det_dir DIR --rootidx_det k]\n"
+               "                        [--torso_prior FILE --torso_prior_weight w]\n"
                "       partapp_find_obj --mat_dump FILE\n";
 }
 
 }  // namespace
 
 int main(int argc, char **argv) {
-  std::string expdir, outdir, scoregrid_dir;
+  std::string expdir, outdir, scoregrid_dir, pred_dir, torso_det_dir, torso_prior;
+  float rot_w = 0.f, pos_w = 0.f, torso_w = 0.f;
+  int rootidx_det = -1;
   int first = 0, numimgs = -1, batch = 1, device = 0;
   bool find_obj = false, flip = false, save_marg = false, from_images = false;
   for (int i = 1; i < argc; ++i) {
@@ -220,6 +233,13 @@ int main(int argc, char **argv) {
     else if (a == "--save_marginals") save_marg = true;
     else if (a == "--from_images") from_images = true;
     else if (a == "--scoregrid_dir") scoregrid_dir = next();
+    else if (a == "--pred_dir") pred_dir = next();
+    else if (a == "--pred_rot_weight") rot_w = (float)std::atof(next().c_str());
+    else if (a == "--pred_pos_weight") pos_w = (float)std::atof(next().c_str());
+    else if (a == "--torso_det_dir") torso_det_dir = next();
+    else if (a == "--rootidx_det") rootidx_det = std::atoi(next().c_str());
+    else if (a == "--torso_prior") torso_prior = next();
+    else if (a == "--torso_prior_weight") torso_w = (float)std::atof(next().c_str());
     else if (a == "--mat_dump") {
       try {
         for (const MatArray &v : mat_read(next())) dump_array(v, "");
@@ -282,6 +302,10 @@ int main(int argc, char **argv) {
           PartConfig pc;
           read_joints(jp, pc, joints);
         }
+        const ExtraUnaryParams extra = loadExtraUnaryParams(
+            i, app.m_part_conf.part_size(), app.m_part_conf.rootpart_idx, pred_dir, rot_w, pos_w,
+            torso_det_dir, rootidx_det, torso_prior, torso_w);
+        app.m_extra = &extra;
         const FindObjResult r = findObjectImageFromImage(ctx, app, flip, joints, img.data(), h, w,
                                                          save_marg);
         write_outputs(outdir, i, flip, r);
@@ -308,6 +332,10 @@ int main(int argc, char **argv) {
         std::vector<ScoreGridSet> parts;
         for (int p = 0; p < P; ++p)
           parts.push_back(loadScoreGrid(scoreGridFileName(scoregrid_dir, i, p, flip)));
+        const ExtraUnaryParams extra =
+            loadExtraUnaryParams(i, P, app.m_part_conf.rootpart_idx, pred_dir, rot_w, pos_w,
+                                 torso_det_dir, rootidx_det, torso_prior, torso_w);
+        app.m_extra = &extra;
         const FindObjResult r =
             findObjectImageFromScoreGrids(ctx, app, flip, joints, parts, h, w, save_marg);
         write_outputs(outdir, i, flip, r);

@@ -276,6 +276,31 @@ std::vector<float> partdetect_raw(Context &ctx, const PartApp &part_app, const f
   return lu;
 }
 
+// Adds part_app.m_extra's terms to the host log unaries [P][S][R][H][W].
+void applyExtraUnaries(Context &ctx, const PartApp &part_app, std::vector<float> &lu, int H,
+                       int W) {
+  const ExtraUnaryParams *x = part_app.m_extra;
+  if (!x || (x->rot.empty() && x->pos.empty() && x->torso.empty())) return;
+  const pa_exp_param e = part_app.m_exp_param.c();
+  const int P = part_app.m_part_conf.part_size();
+  require(x->rot.empty() || (int)x->rot.size() == 2 * P, "rotation parameters: 2 per part");
+  require(x->pos.empty() || (int)x->pos.size() == 4 * P, "position parameters: 4 per part");
+  require(x->torso.empty() || x->torso.size() == 4, "torso prior: 4 parameters");
+  require(x->is_detect.empty() || (int)x->is_detect.size() == P, "is_detect: one flag per part");
+  pa_extra_unary ex{};
+  ex.rot_weight = x->rot_weight;
+  ex.rot_params = x->rot.empty() ? nullptr : x->rot.data();
+  ex.pos_weight = x->pos_weight;
+  ex.pos_params = x->pos.empty() ? nullptr : x->pos.data();
+  ex.root_det_x = x->root_det_x;
+  ex.root_det_y = x->root_det_y;
+  ex.torso_weight = x->torso_weight;
+  ex.torso_prior = x->torso.empty() ? nullptr : x->torso.data();
+  ex.is_detect = x->is_detect.empty() ? nullptr : x->is_detect.data();
+  ctx.check(pa_add_extra_unaries(ctx.get(), &e, &ex, P, part_app.m_part_conf.rootpart_idx,
+                                 lu.data(), H, W, PA_MEM_HOST));
+}
+
 }  // namespace
 
 void partdetect(Context &ctx, const PartApp &part_app, const float *image, int img_h,
@@ -302,7 +327,9 @@ FindObjResult findObjectImageFromImage(Context &ctx, const PartApp &part_app, bo
   require((int)part_app.m_abc.size() >= P, "a detector for every part");
   const int S = std::max(1, e.num_scale_steps), R = e.num_rotation_steps;
   // partdetect(part_app, imgidx, imgidx, false /* flip */, ...), objectdetect_aux.cpp:383
-  const std::vector<float> lu = partdetect_raw(ctx, part_app, image, img_h, img_w, false);
+  std::vector<float> lu = partdetect_raw(ctx, part_app, image, img_h, img_w, false);
+  // the first P classifiers' unaries are the parts' [P][S][R][H][W] block
+  applyExtraUnaries(ctx, part_app, lu, img_h, img_w);
   const TreeHolder th(part_app.m_part_conf, part_app.m_part_conf.rootpart_idx, joints);
   const int K = e.roi_save_num_samples > 0 ? e.roi_save_num_samples : 1;
   ImageOut out(P, K, S);
@@ -323,6 +350,54 @@ FindObjResult findObjectImageFromImage(Context &ctx, const PartApp &part_app, bo
       r.log_marginals.push_back(std::move(g));
     }
   return r;
+}
+
+ExtraUnaryParams loadExtraUnaryParams(int imgidx, int n_parts, int root, const std::string &pred_dir,
+                                      float rot_weight, float pos_weight,
+                                      const std::string &torso_det_dir, int rootidx_det,
+                                      const std::string &torso_prior_file, float torso_weight) {
+  ExtraUnaryParams x;
+  if (!pred_dir.empty() && rot_weight != 0.f) {
+    const auto v = mat_read(pred_dir + "/testlist_params_rot_imgidx_" + std::to_string(imgidx) + ".mat");
+    const MatArray &a = mat_find(v, "rot_test");
+    require(a.dims.size() == 2 && (int)a.dims[0] >= n_parts && a.dims[1] >= 2, "rot_test: [P][2+]");
+    x.rot_weight = rot_weight;
+    for (int p = 0; p < n_parts; ++p) {
+      const double sd = mat_at(a, {(size_t)p, 1});
+      x.rot.push_back(mat_at(a, {(size_t)p, 0}));
+      x.rot.push_back(sd * sd);  // square()
+    }
+  }
+  if (!pred_dir.empty() && pos_weight != 0.f) {
+    const auto v = mat_read(pred_dir + "/testlist_params_pos_imgidx_" + std::to_string(imgidx) + ".mat");
+    const MatArray &a = mat_find(v, "pos_test");
+    require(a.dims.size() == 2 && (int)a.dims[0] >= n_parts && a.dims[1] >= 4, "pos_test: [P][4+]");
+    x.pos_weight = pos_weight;
+    for (int p = 0; p < n_parts; ++p) {
+      const double sx = mat_at(a, {(size_t)p, 2}), sy = mat_at(a, {(size_t)p, 3});
+      x.pos.push_back(mat_at(a, {(size_t)p, 0}));
+      x.pos.push_back(mat_at(a, {(size_t)p, 1}));
+      x.pos.push_back(sx * sx);
+      x.pos.push_back(sy * sy);
+    }
+    require(!torso_det_dir.empty(), "the position score needs the torso detections");
+    char name[64];
+    std::snprintf(name, sizeof name, "/pose_est_imgidx%04d.mat", imgidx);
+    const auto d = mat_read(torso_det_dir + name);
+    const MatArray &bc = mat_find(d, "best_conf");
+    const int k = rootidx_det >= 0 ? rootidx_det : root;
+    require(bc.dims.size() == 2 && (int)bc.dims[0] > k && bc.dims[1] >= 6, "best_conf: [P][7]");
+    x.root_det_x = (double)(int)mat_at(bc, {(size_t)k, 4});  // int root_pos_x
+    x.root_det_y = (double)(int)mat_at(bc, {(size_t)k, 5});
+  }
+  if (!torso_prior_file.empty()) {
+    const auto v = mat_read(torso_prior_file);
+    const MatArray &a = mat_find(v, "params");
+    require(a.dims.size() == 2 && a.dims[1] >= 4, "torso prior params: [1][4]");
+    for (size_t j = 0; j < 4; ++j) x.torso.push_back(mat_at(a, {0, j}));
+    x.torso_weight = torso_weight;
+  }
+  return x;
 }
 
 std::string scoreGridFileName(const std::string &dir, int imgidx, int pidx, bool flip) {
@@ -399,6 +474,7 @@ FindObjResult findObjectImageFromScoreGrids(Context &ctx, const PartApp &part_ap
                               img_h, img_w, lu.data() + ((size_t)p * S + s) * N, PA_MEM_HOST));
     }
   }
+  applyExtraUnaries(ctx, part_app, lu, img_h, img_w);
   const TreeHolder th(part_app.m_part_conf, part_app.m_part_conf.rootpart_idx, joints);
   const int K = e.roi_save_num_samples > 0 ? e.roi_save_num_samples : 1;
   ImageOut out(P, K, S);

@@ -137,6 +137,36 @@ struct PartWindow {
 };
 
 // What the reference's PartApp carries for this path.
+// The poselet-conditioned extra unary terms of findObjectImageRotJoints
+// (objectdetect_findrot.cpp:855-948), with their parameters as the reference's
+// loaders leave them (getRotParams, getPosParams, getRootPosDet,
+// getTorsoPosPriorParams in objectdetect_icps.cpp).  Empty vectors switch a
+// term off.
+struct ExtraUnaryParams {
+  float rot_weight = 0.f;           // pred_unary_rot_weight
+  std::vector<double> rot;          // [P][2]: mean rotation (rad), variance
+  float pos_weight = 0.f;           // pred_unary_pos_weight
+  std::vector<double> pos;          // [P][4]: mu_x, mu_y, var_x, var_y
+  double root_det_x = 0, root_det_y = 0;
+  float torso_weight = 0.f;         // torso_pos_prior_weight
+  std::vector<double> torso;        // [4]: mu_x, mu_y, var_x, var_y
+  std::vector<int> is_detect;       // [P] (empty: every part)
+};
+
+// Reads the reference's prediction files for image imgidx:
+//   rot:   <pred_dir>/testlist_params_rot_imgidx<i>.mat, "rot_test" [P][2+]
+//          (mean, deviation -> variance = deviation^2), getRotParams :193-226
+//   pos:   <pred_dir>/testlist_params_pos_imgidx<i>.mat, "pos_test" [P][4+]
+//          (mu_x, mu_y, deviations -> variances), getPosParams :326-364
+//   root:  <torso_det_dir>/pose_est_imgidx<NNNN>.mat, "best_conf" row
+//          rootidx_det, columns 4, 5 truncated to int, getRootPosDet :283-324
+//   torso: <torso_prior_file>, "params" [1][4], getTorsoPosPriorParams :32-45
+// An empty directory or file name leaves that term off.
+ExtraUnaryParams loadExtraUnaryParams(int imgidx, int n_parts, int root, const std::string &pred_dir,
+                                      float rot_weight, float pos_weight,
+                                      const std::string &torso_det_dir, int rootidx_det,
+                                      const std::string &torso_prior_file, float torso_weight);
+
 struct PartApp {
   ExpParam m_exp_param;
   PartConfig m_part_conf;
@@ -144,6 +174,7 @@ struct PartApp {
   std::vector<const AdaBoostClassifier *> m_abc;  // part detectors first
   AbcDetectorParam m_abc_param;                   // for detection from images
   std::vector<PartWindow> m_window_param;         // one per classifier in m_abc
+  const ExtraUnaryParams *m_extra = nullptr;       // extra unary terms, if any
 };
 
 // computeRotJointMarginal (objectdetect_findrot.cpp:292-456): child ->

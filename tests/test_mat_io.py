@@ -140,24 +140,13 @@ def test_corrupt_stream_is_an_error(tmp_path):
     assert r.returncode == 1 and "inflate" in r.stderr
 
 
-# ------------------------------------------------------------------ GPU
-@pytest.mark.gpu
-def test_find_obj_from_saved_score_grids(tmp_path):
-    """`--find_obj --scoregrid_dir`: per part the saved cell_scoregrid with
-    per-rotation Ti2, T2g (compressed, as partdetect saves them) -> Tig = Ti2
-    T2g -> pa_unary_maps -> pa_ps_infer (bIsSparse); best_conf and log Z equal
-    the same composition through the Python mirror bit for bit."""
-    import torch
-
-    import partapp_gb300 as pa
-
-    assert torch.cuda.is_available()
+def make_scoregrid_experiment(d, rng, Rr=8, H=40, W=56, P=10):
+    """exp.txt, joints.txt and per-part compressed score-grid files under d/sg
+    as partdetect saves them; returns (tree, scores[p] [R][ny][nx], Tig[p]
+    [R][3][3] computed as the host does, Rr, H, W, P)."""
     from test_host_cli import write_joints
 
-    rng = np.random.default_rng(5)
-    Rr, H, W, P = 8, 40, 56, 10
     tree = synth.make_tree(rng, R=Rr, offset_range=(3.0, 8.0), sigma_range=(1.0, 2.5))
-    d = str(tmp_path)
     with open(os.path.join(d, "exp.txt"), "w") as fh:
         for k, val in (("num_rotation_steps", Rr), ("min_part_rotation", -180),
                        ("max_part_rotation", 180), ("object_scale", 1),
@@ -191,6 +180,23 @@ def test_find_obj_from_saved_score_grids(tmp_path):
                     do_compression=True)
         scores.append(np.stack([cells[0, r] for r in range(Rr)]))
         tigs.append(tig)
+    return tree, scores, tigs, Rr, H, W, P
+
+
+# ------------------------------------------------------------------ GPU
+@pytest.mark.gpu
+def test_find_obj_from_saved_score_grids(tmp_path):
+    """`--find_obj --scoregrid_dir`: per part the saved cell_scoregrid with
+    per-rotation Ti2, T2g (compressed, as partdetect saves them) -> Tig = Ti2
+    T2g -> pa_unary_maps -> pa_ps_infer (bIsSparse); best_conf and log Z equal
+    the same composition through the Python mirror bit for bit."""
+    import torch
+
+    import partapp_gb300 as pa
+
+    assert torch.cuda.is_available()
+    d = str(tmp_path)
+    tree, scores, tigs, Rr, H, W, P = make_scoregrid_experiment(d, np.random.default_rng(5))
     r = subprocess.run([cli(), "--find_obj", "--expdir", d, "--scoregrid_dir",
                         os.path.join(d, "sg")], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
