@@ -122,6 +122,44 @@ class AdaBoostClassifier {
   pa_classifier *cls_ = nullptr;
 };
 
+// The learned unary (no reference counterpart; pa_unary_net): a convolution
+// network over descriptor fields that stands in for the AdaBoost unaries of
+// chosen parts.  Device pointers throughout.
+class UnaryNet {
+ public:
+  UnaryNet(Context &ctx, int dim, int n_parts, uint64_t seed = 0) : ctx_(ctx) {
+    ctx_.check(pa_unary_net_create(ctx_.get(), dim, n_parts, seed, &net_));
+  }
+  ~UnaryNet() { pa_unary_net_destroy(ctx_.get(), net_); }
+  UnaryNet(const UnaryNet &) = delete;
+  UnaryNet &operator=(const UnaryNet &) = delete;
+  pa_unary_net *get() const { return net_; }
+  std::vector<float> params() const {
+    int64_t n = 0;
+    ctx_.check(pa_unary_net_get_params(ctx_.get(), net_, nullptr, &n));
+    std::vector<float> p((size_t)n);
+    ctx_.check(pa_unary_net_get_params(ctx_.get(), net_, p.data(), &n));
+    return p;
+  }
+  void set_params(const std::vector<float> &p) {
+    ctx_.check(pa_unary_net_set_params(ctx_.get(), net_, p.data()));
+  }
+  // One Adam step on the squared error against the log of AdaBoost scores
+  // [P][n][ny][nx] of the same fields; returns the loss.
+  double train_step(const void *fields, bool fields_bf16, const float *scores, int n, int ny,
+                    int nx, const pa_adam_param &opt) {
+    double loss = 0.0;
+    ctx_.check(pa_unary_net_backward(ctx_.get(), net_, fields, fields_bf16 ? 1 : 0, scores, n, ny,
+                                     nx, &loss, nullptr));
+    ctx_.check(pa_unary_net_adam(ctx_.get(), net_, &opt));
+    return loss;
+  }
+
+ private:
+  Context &ctx_;
+  pa_unary_net *net_ = nullptr;
+};
+
 // AbcDetectorParam (libPartDetect/AbcDetectorParam.proto:2-12) fields of the
 // dense detector.
 struct AbcDetectorParam {
