@@ -428,8 +428,8 @@ def test_find_obj_batch_host_ring_matches_device(ctx):
         assert np.array_equal(h["log_z"], d["log_z"])
 
 
-def test_config0_full_size_one_image(ctx, orc):
-    """The BASELINE config-0 workload: 320x240, 24 rotations, 10 parts x 500
+def test_full_size_320x240_one_image(ctx, orc):
+    """The plain single-image workload: 320x240, 24 rotations, 10 parts x 500
     stumps over 960-dim descriptors at stride 4, bilinear upsampling."""
     img = synth.make_image(2024)
     e = orc.make_exp(R=24)
