@@ -22,6 +22,8 @@
 // atan2f (gradient orientation).
 #include <climits>
 
+#include <cstddef>
+
 #include "pa_internal.cuh"
 
 namespace pa {
@@ -58,13 +60,96 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 
+// ---------------------------------------------------------------------------
+// FP32 fast path of the double-typed interpolation expressions.  The
+// reference evaluates them in double and rounds once to float.  Here they are
+// evaluated in float-float arithmetic (Knuth's TwoSum and the FMA form of
+// Dekker's TwoProduct are exact), and the float result is used only when it
+// is certain to be the double result's rounding: with all terms
+// non-negative, the double evaluation is within 6 * 2^-53 and the float-float
+// one within about 2^-43 of the exact value, so every value within 2^-40 of
+// the float-float sum rounds to the same float unless that sum lies within
+// 2^-40 (relative) of a rounding midpoint.  Those rare cases, and operands
+// outside the analysed ranges, take the double path, so the bits never change.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bv = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
+}
+
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+
+// r = the float nearest to hi + lo, when every value within 2^-40 (relative)
+// of hi + lo rounds to it.
+__device__ __forceinline__ bool certified_round(float hi, float lo, float &r) {
+  float sr, e;
+  two_sum(hi, lo, sr, e);  // sr = fl(hi + lo), sr + e = hi + lo
+  if (!(sr >= 0x1p-100f && sr < 0x1p100f)) {
+    if (hi == 0.f && lo == 0.f) {
+      r = 0.f;
+      return true;
+    }
+    return false;
+  }
+  const unsigned b = __float_as_uint(sr);
+  const float up = __fsub_rn(__uint_as_float(b + 1u), sr);  // spacing above sr (exact)
+  const float dn = __fsub_rn(sr, __uint_as_float(b - 1u));  // spacing below sr (exact)
+  const float half = 0.5f * (e >= 0.f ? up : dn);
+  if (__fadd_ru(fabsf(e), sr * 0x1p-40f) < half) {
+    r = sr;
+    return true;
+  }
+  return false;
+}
+
+// (1 - t) * a + fl(t * b) for t in [0, 1), a, b >= 0: hi + lo within about
+// 2^-46 of the exact value (1 - t is exact as oh + ol).
+__device__ __forceinline__ void ff_lerp(float t, float a, float b, float &hi, float &lo) {
+  float oh, ol, ph, pl, sh, sl;
+  two_sum(1.f, -t, oh, ol);
+  two_prod(oh, a, ph, pl);
+  two_sum(ph, __fmul_rn(t, b), sh, sl);
+  hi = sh;
+  lo = __fadd_rn(__fadd_rn(sl, pl), __fmul_rn(ol, a));
+}
+
+__device__ __forceinline__ bool lerp_ok(float t, float a, float b) {
+  return t >= 0.f && t < 1.f && a >= 0.f && b >= 0.f;
+}
+
 // (1 - dy) * ((1 - dx) * a + dx * b) + dy * ((1 - dx) * c + dx * d) with the
 // reference's types: 1.0 - d in double, dx * b a float product.
 __device__ __forceinline__ float bilinear4(float dx, float dy, float a, float b, float c, float d) {
+  if (lerp_ok(dx, a, b) && lerp_ok(dy, c, d) && dy >= 0.f && c >= 0.f) {
+    float t1h, t1l, t2h, t2l, oh, ol, uh, ul, vh, vl, wh, wl, r;
+    ff_lerp(dx, a, b, t1h, t1l);
+    ff_lerp(dx, c, d, t2h, t2l);
+    two_sum(1.f, -dy, oh, ol);
+    two_prod(oh, t1h, uh, ul);
+    two_prod(dy, t2h, vh, vl);
+    const float cross = __fadd_rn(__fadd_rn(__fmul_rn(oh, t1l), __fmul_rn(ol, t1h)),
+                                  __fmul_rn(dy, t2l));
+    two_sum(uh, vh, wh, wl);
+    if (certified_round(wh, __fadd_rn(__fadd_rn(__fadd_rn(wl, ul), vl), cross), r)) return r;
+  }
   const double omdx = dsub(1.0, (double)dx), omdy = dsub(1.0, (double)dy);
   const double t1 = dadd(dmul(omdx, (double)a), (double)fmul(dx, b));
   const double t2 = dadd(dmul(omdx, (double)c), (double)fmul(dx, d));
   return __double2float_rn(dadd(dmul(omdy, t1), dmul((double)dy, t2)));
+}
+
+// (1.0 - t) * a + t * b, 1.0 - t in double, t * b a float product.
+__device__ __forceinline__ float lerp1(float t, float a, float b) {
+  if (lerp_ok(t, a, b)) {
+    float hi, lo, r;
+    ff_lerp(t, a, b, hi, lo);
+    if (certified_round(hi, lo, r)) return r;
+  }
+  return __double2float_rn(dadd(dmul(dsub(1.0, (double)t), (double)a), (double)fmul(t, b)));
 }
 
 // ImageContent::getValue (ImageContent.cpp:29-50) on a 21 x 21 map.
@@ -77,12 +162,8 @@ __device__ float get_value(const float *g, float x, float y) {
     return bilinear4(dx, dy, g[iy * kP + ix], g[iy * kP + ix + 1], g[(iy + 1) * kP + ix],
                      g[(iy + 1) * kP + ix + 1]);
   // (1.0 - dy) * a + dy * b: the second product is a float one
-  if (ix == n && iy < n)
-    return __double2float_rn(dadd(dmul(dsub(1.0, (double)dy), (double)g[iy * kP + ix]),
-                                  (double)fmul(dy, g[(iy + 1) * kP + ix])));
-  if (iy == n && ix < n)
-    return __double2float_rn(dadd(dmul(dsub(1.0, (double)dx), (double)g[iy * kP + ix]),
-                                  (double)fmul(dx, g[iy * kP + ix + 1])));
+  if (ix == n && iy < n) return lerp1(dy, g[iy * kP + ix], g[(iy + 1) * kP + ix]);
+  if (iy == n && ix < n) return lerp1(dx, g[iy * kP + ix], g[iy * kP + ix + 1]);
   if (iy == n && ix == n) return g[iy * kP + ix];
   return 0.f;
 }
@@ -348,8 +429,13 @@ __global__ void __launch_bounds__(32 * kDescWarps, 5) k_shape_grid(
   // (b) chunks of samples: all lanes compute the increments (double
   // arithmetic), then lane b accumulates bins b, b + 32, b + 64 in the
   // reference's order
-  float *ws = S.patch;  // patch and grad: free, 2 * 441 floats
-  uint8_t *bins = reinterpret_cast<uint8_t *>(S.patch + kChunk * 8);
+  // patch and grad (adjacent, free now): kChunk * 8 weights, then the bins
+  static_assert(offsetof(WarpScratch, grad) == offsetof(WarpScratch, patch) + kPP * sizeof(float),
+                "grad must follow patch");
+  static_assert(kChunk * 8 * (sizeof(float) + 1) <= 2 * kPP * sizeof(float),
+                "histogram increments must fit in patch + grad");
+  float *ws = reinterpret_cast<float *>(reinterpret_cast<char *>(&S) + offsetof(WarpScratch, patch));
+  uint8_t *bins = reinterpret_cast<uint8_t *>(ws + kChunk * 8);
   float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f;
   for (int c0 = 0; c0 < nlist; c0 += kChunk) {
     const int nc = min(kChunk, nlist - c0);
