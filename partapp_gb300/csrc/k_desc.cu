@@ -168,35 +168,91 @@ __device__ float get_value(const float *g, float x, float y) {
   return 0.f;
 }
 
+// r = the float nearest to hi + lo when every value within m_abs of hi + lo
+// rounds to it (for sums that may cancel, with an absolute error bound).
+__device__ __forceinline__ bool certified_round_abs(float hi, float lo, float m_abs, float &r) {
+  float sr, e;
+  two_sum(hi, lo, sr, e);
+  if (!(sr >= 0x1p-100f && sr < 0x1p100f)) return false;
+  const unsigned b = __float_as_uint(sr);
+  const float up = __fsub_rn(__uint_as_float(b + 1u), sr);
+  const float dn = __fsub_rn(sr, __uint_as_float(b - 1u));
+  const float half = 0.5f * (e >= 0.f ? up : dn);
+  if (__fadd_ru(fabsf(e), m_abs) < half) {
+    r = sr;
+    return true;
+  }
+  return false;
+}
+
+// fl_f(fl_d(m * (1.0 - f))) for m >= 0, f in [0, 1): m * (1 - f) = m * oh + m * ol
+// with the first product exact, within about 2^-46; the double path otherwise.
+__device__ __forceinline__ float weight_om(float m, float f) {
+  if (m >= 0.f && f >= 0.f && f < 1.f) {
+    float oh, ol, ph, pl, r;
+    two_sum(1.f, -f, oh, ol);
+    two_prod(m, oh, ph, pl);
+    if (certified_round(ph, __fadd_rn(pl, __fmul_rn(m, ol)), r)) return r;
+  }
+  return __double2float_rn(dmul((double)m, dsub(1.0, (double)f)));
+}
+
+// pi (the double constant) as a float pair: kPiAbove + kPiLo = pi within 2^-49.
+constexpr float kPiLo = (float)(kPi - (double)kPiAbove);
+
+// fl_f(fl_d((double)x / pi)) for x >= 0: q0 = fl(x / kPiAbove), the remainder
+// x - q0 * kPiAbove exact by FMA, the correction q1 within about 2^-46.
+__device__ __forceinline__ float div_pi(float x) {
+  if (x >= 0.f && x < 0x1p100f) {
+    const float q0 = __fdiv_rn(x, kPiAbove);
+    const float rem = __fmaf_rn(-q0, kPiAbove, x);
+    const float q1 = __fdiv_rn(__fmaf_rn(-q0, kPiLo, rem), kPiAbove);
+    float r;
+    if (certified_round(q0, q1, r)) return r;
+  }
+  return __double2float_rn(__ddiv_rn((double)x, kPi));
+}
+
+// fl_f(fl_d((double)o + pi)) for o in [-pi, 0): o + kPiAbove exact as a pair, plus
+// kPiLo, within 2^-44 absolute (the sum can cancel).
+__device__ __forceinline__ float add_pi(float o) {
+  float sh, sl, r;
+  two_sum(o, kPiAbove, sh, sl);
+  if (certified_round_abs(sh, __fadd_rn(sl, kPiLo), 0x1p-44f, r)) return r;
+  return __double2float_rn(dadd((double)o, kPi));
+}
+
+// (int)(v >= 0 ? (double)v : (double)v - 1.0): truncating v - 1 for v < 0
+// is ceil(v) - 1, exact in float.
+__device__ __forceinline__ int index_below(float v) {
+  return v >= 0.0f ? (int)v : (int)ceilf(v) - 1;
+}
+
 // KMAPlaceInLogPolIndex (ShapeDescriptor.cpp:71-121), orientation modulo pi:
 // the up to 8 (bin, weight) increments of one sample, in the reference's
 // r -> c -> orientation order (bin 255: no increment).
 __device__ void place_entries(float mag, float ori, float rx, float cx, uint8_t *bins, float *ws) {
-  const float oval = __double2float_rn(__ddiv_rn((double)fmul((float)kSOri, ori), kPi));
-  const int ri = (int)((rx >= 0.0f) ? (double)rx : dsub((double)rx, 1.0));
-  const int ci = (int)((cx >= 0.0f) ? (double)cx : dsub((double)cx, 1.0));
-  const int oi = (int)((oval >= 0.0f) ? (double)oval : dsub((double)oval, 1.0));
+  const float oval = div_pi(fmul((float)kSOri, ori));
+  const int ri = index_below(rx), ci = index_below(cx), oi = index_below(oval);
   const float rfrac = fsub(rx, (float)ri), cfrac = fsub(cx, (float)ci), ofrac = fsub(oval, (float)oi);
   for (int r = 0; r < 2; ++r) {
     const int rindex = ri + r;
     const bool rok = rindex >= 0 && rindex < kSr;
-    const float rweight =
-        __double2float_rn(dmul((double)mag, r == 0 ? dsub(1.0, (double)rfrac) : (double)rfrac));
+    // m * frac: the double product of two floats is exact, so its rounding
+    // is the float product
+    const float rweight = r == 0 ? weight_om(mag, rfrac) : fmul(mag, rfrac);
     for (int c = 0; c < 2; ++c) {
       int cindex = ci + c;
       if (cindex >= kSc) cindex = 0;
       const bool cok = rok && cindex >= 0 && cindex < kSc;
-      const float cweight = __double2float_rn(
-          dmul((double)rweight, c == 0 ? dsub(1.0, (double)cfrac) : (double)cfrac));
+      const float cweight = c == 0 ? weight_om(rweight, cfrac) : fmul(rweight, cfrac);
       const int rcindex = (rindex * kSc + cindex) << 3;
       for (int ort = 0; ort < 2; ++ort) {
         int oindex = oi + ort;
         if (oindex >= kSOri) oindex = 0;
         const int e = (r * 2 + c) * 2 + ort;
         bins[e] = cok ? (uint8_t)(rcindex + oindex) : (uint8_t)255;
-        ws[e] = cok ? __double2float_rn(dmul((double)cweight,
-                                             ort == 0 ? dsub(1.0, (double)ofrac) : (double)ofrac))
-                    : 0.f;
+        ws[e] = cok ? (ort == 0 ? weight_om(cweight, ofrac) : fmul(cweight, ofrac)) : 0.f;
       }
     }
   }
@@ -419,7 +475,8 @@ __global__ void __launch_bounds__(32 * kDescWarps, 5) k_shape_grid(
     bool c = false;
     if (k < kPP) {
       const int i = k / kP - kHalf, j = k - (k / kP) * kP - kHalf;
-      c = T.inrange[(kHalf + j) * kP + (kHalf + i)] && !((double)S.edge[k] < 1e-10);
+      // (double)edge < 1e-10  <=>  edge < the smallest float >= 1e-10
+      c = T.inrange[(kHalf + j) * kP + (kHalf + i)] && !(S.edge[k] < __uint_as_float(0x2EDBE6FFu));
     }
     const unsigned m = __ballot_sync(0xFFFFFFFFu, c);
     if (c) list[nlist + __popc(m & ((1u << lane) - 1u))] = (short)k;
@@ -447,7 +504,7 @@ __global__ void __launch_bounds__(32 * kDescWarps, 5) k_shape_grid(
       float o = fsub(S.ori[k], 0.f);
       // (double)o > pi  <=>  o >= the float just above pi
       while (o >= kPiAbove) o = __double2float_rn(dsub((double)o, kPi));
-      while (o < 0.f) o = __double2float_rn(dadd((double)o, kPi));
+      while (o < 0.f) o = add_pi(o);
       place_entries(mag, o, T.lr[t], T.lc[t], bins + n * 8, ws + n * 8);
     }
     __syncwarp();
