@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
       const int nl = (n_loc - loc0) < kLoc ? (int)(n_loc - loc0) : kLoc;
       const float *v = sm + lane * kStride;
       float s = 0.f;
-#pragma unroll 2
+#pragma unroll 4
       for (int j = 0; j < my_npad / 8; ++j) {
         const uint4 fq = my_f8[j];
         const float4 q0 = my_ta[4 * j], q1 = my_ta[4 * j + 1];
