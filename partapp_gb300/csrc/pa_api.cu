@@ -2178,14 +2178,21 @@ pa_status pa_classifier_parse(pa_ctx *ctx, const char *text, size_t len, pa_clas
     return true;
   };
   double dv, nv;
-  if (!next_num(dv) || !next_num(nv) || dv < 1 || nv < 1)
-    return fail(ctx, PA_ERR_INVALID, "classifier text: missing D / number of stumps");
+  if (!next_num(dv) || !next_num(nv) || !(dv >= 1 && dv <= (1 << 24)) ||
+      !(nv >= 1 && nv <= (1 << 24)))
+    return fail(ctx, PA_ERR_INVALID, "classifier text: missing or out-of-range D / number of stumps");
   const int D = (int)dv, ns = (int)nv;
+  // every stump takes at least 10 characters ("f p a j t" with separators):
+  // a count the text cannot hold is rejected before anything is allocated
+  if ((size_t)ns > len / 10 + 1)
+    return fail(ctx, PA_ERR_INVALID, "classifier text: %d stumps announced, the text is shorter", ns);
   std::vector<pa_stump> st(ns);
   for (int i = 0; i < ns; ++i) {
     double f, pp, a, j, th;
     if (!next_num(f) || !next_num(pp) || !next_num(a) || !next_num(j) || !next_num(th))
       return fail(ctx, PA_ERR_INVALID, "classifier text: stump %d truncated", i);
+    if (!(f >= 0 && f < D))
+      return fail(ctx, PA_ERR_INVALID, "classifier text: stump %d: feature index out of range", i);
     st[i].f = (int32_t)f;
     st[i].p = (float)pp;
     st[i].alpha = (float)a;

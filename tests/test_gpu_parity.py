@@ -119,6 +119,17 @@ def test_classifier_text_format(ctx, orc):
     assert got[0, 0, 0, 0] == want[0, 0, 0]
 
 
+def test_malformed_classifier_text_is_an_error(ctx, pa):
+    """Bad model files give PA_ERR_INVALID: out-of-range or non-numeric
+    counts, a stump count the text cannot hold, truncated stumps, feature
+    indices outside [0, D)."""
+    for text in ("", "abc", "1e30 5\n", "nan 3\n", "960 nan\n", "960 1000000000\n",
+                 "960 2\n1 1 0.5 0 0.1\n", "960 1\n1e12 1 1 0 0.1\n",
+                 "960 1\n-1 1 1 0 0.1\n", "960 1\n960 1 1 0 0.1\n", "0 1\n0 1 1 0 0\n"):
+        with pytest.raises(pa.PaError):
+            pa.Classifier.parse(ctx, text)
+
+
 @pytest.mark.parametrize("grid_step", [1.0, 2.0])
 def test_score_grids_window_bit_exact(ctx, orc, grid_step):
     rng = np.random.default_rng(2)
