@@ -8,7 +8,8 @@
  * the reference function(s) it replaces (paths relative to the reference
  * tree).  Conventions:
  *   - every call returns a pa_status and never aborts (the reference reports
- *     errors only through assert());
+ *     errors only through assert()); no C++ exception crosses the boundary
+ *     (a failed host allocation is PA_ERR_NOMEM);
  *   - maps use the reference's FloatGrid3 layout, C order [rot][y][x], float;
  *     per-part stacks are [part][rot][y][x];
  *   - buffers are caller-owned; `mem` says whether the data pointers of a call

@@ -17,6 +17,8 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -1979,7 +1981,7 @@ void pa_exp_param_default(pa_exp_param *p) {
   p->num_scale_steps = 1;
 }
 
-pa_status pa_ctx_create(int device, pa_ctx **out) {
+pa_status pa_ctx_create(int device, pa_ctx **out) try {
   if (!out) return PA_ERR_INVALID;
   *out = nullptr;
   int n = 0;
@@ -1997,9 +1999,13 @@ pa_status pa_ctx_create(int device, pa_ctx **out) {
   c->own_stream = true;
   *out = c.release();
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return PA_ERR_NOMEM;
+} catch (...) {
+  return PA_ERR_INVALID;
 }
 
-pa_status pa_ctx_destroy(pa_ctx *ctx) {
+pa_status pa_ctx_destroy(pa_ctx *ctx) try {
   if (!ctx) return PA_OK;
   for (pa_ctx *w : ctx->workers) pa_ctx_destroy(w);
   ctx->workers.clear();
@@ -2026,9 +2032,13 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) {
   }
   delete ctx;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream) {
+pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream) try {
   if (!ctx) return PA_ERR_INVALID;
   DeviceGuard dg(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -2036,43 +2046,63 @@ pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream) {
   ctx->stream = (cudaStream_t)stream;
   ctx->own_stream = false;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_ctx_set_message_math(pa_ctx *ctx, int mode) {
+pa_status pa_ctx_set_message_math(pa_ctx *ctx, int mode) try {
   if (!ctx) return PA_ERR_INVALID;
   if (mode != PA_MSG_FP32 && mode != PA_MSG_BF16_TENSOR)
     return fail(ctx, PA_ERR_INVALID, "unknown message math %d", mode);
   ctx->msg_math = mode;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_ctx_synchronize(pa_ctx *ctx) {
+pa_status pa_ctx_synchronize(pa_ctx *ctx) try {
   if (!ctx) return PA_ERR_INVALID;
   DeviceGuard dg(ctx->device);
   PA_CK(cudaStreamSynchronize(ctx->stream));
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 const char *pa_last_error(const pa_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
 uint64_t pa_ctx_kernel_launches(const pa_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
-pa_status pa_ctx_enable_timing(pa_ctx *ctx, int on) {
+pa_status pa_ctx_enable_timing(pa_ctx *ctx, int on) try {
   if (!ctx) return PA_ERR_INVALID;
   DeviceGuard dg(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   resolve_timing(ctx);
   ctx->timing = on != 0;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_ctx_timing_reset(pa_ctx *ctx) {
+pa_status pa_ctx_timing_reset(pa_ctx *ctx) try {
   if (!ctx) return PA_ERR_INVALID;
   DeviceGuard dg(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   resolve_timing(ctx);
   ctx->times.clear();
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 int pa_ctx_timing_count(pa_ctx *ctx) {
@@ -2083,17 +2113,21 @@ int pa_ctx_timing_count(pa_ctx *ctx) {
 }
 
 pa_status pa_ctx_timing_get(pa_ctx *ctx, int i, const char **name, double *total_ms,
-                            uint64_t *launches) {
+                            uint64_t *launches) try {
   if (!ctx || i < 0 || i >= (int)ctx->names.size()) return PA_ERR_INVALID;
   const auto &acc = ctx->times[ctx->names[i]];
   if (name) *name = ctx->names[i].c_str();
   if (total_ms) *total_ms = acc.ms;
   if (launches) *launches = acc.n;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int n_stumps,
-                               pa_classifier **out) {
+                               pa_classifier **out) try {
   if (!ctx || !out) return PA_ERR_INVALID;
   *out = nullptr;
   if (dim < 1 || n_stumps < 1 || !stumps)
@@ -2164,9 +2198,13 @@ pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int
   }
   *out = c.release();
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_classifier_parse(pa_ctx *ctx, const char *text, size_t len, pa_classifier **out) {
+pa_status pa_classifier_parse(pa_ctx *ctx, const char *text, size_t len, pa_classifier **out) try {
   if (!ctx || !text || !out) return PA_ERR_INVALID;
   std::string s(text, len);
   const char *p = s.c_str();
@@ -2199,9 +2237,13 @@ pa_status pa_classifier_parse(pa_ctx *ctx, const char *text, size_t len, pa_clas
     st[i].theta = (float)th;
   }
   return pa_classifier_create(ctx, D, st.data(), ns, out);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_classifier_destroy(pa_ctx *ctx, pa_classifier *cls) {
+pa_status pa_classifier_destroy(pa_ctx *ctx, pa_classifier *cls) try {
   if (!cls) return PA_OK;
   if (ctx) {
     DeviceGuard dg(ctx->device);
@@ -2215,19 +2257,27 @@ pa_status pa_classifier_destroy(pa_ctx *ctx, pa_classifier *cls) {
   }
   delete cls;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_classifier_info(const pa_classifier *cls, int *dim, int *n_stumps, float *sum_alpha) {
+pa_status pa_classifier_info(const pa_classifier *cls, int *dim, int *n_stumps, float *sum_alpha) try {
   if (!cls) return PA_ERR_INVALID;
   if (dim) *dim = cls->dim;
   if (n_stumps) *n_stumps = cls->n;
   if (sum_alpha) *sum_alpha = cls->sum_alpha;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return PA_ERR_NOMEM;
+} catch (...) {
+  return PA_ERR_INVALID;
 }
 
 pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
                          const float *desc, int n_fields, int ny, int nx, int dim, int normalize,
-                         float *scores, int mem) {
+                         float *scores, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!desc || !scores || n_fields < 1 || ny < 1 || nx < 1 || dim < 1)
     return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
@@ -2269,6 +2319,10 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 // ------------------------------------------------------------------------
@@ -2374,17 +2428,21 @@ void smooth_coefficients(float sigma, float *coefs) {
 }  // namespace
 
 pa_status pa_feature_grid_size(int img_w, int img_h, const double *x_axis, const double *y_axis,
-                               double desc_step, int *nx, int *ny) {
+                               double desc_step, int *nx, int *ny) try {
   if (img_w < 1 || img_h < 1 || !x_axis || !y_axis || !nx || !ny || !(desc_step > 0))
     return PA_ERR_INVALID;
   double rect[4];
   return feature_grid(img_w, img_h, x_axis, y_axis, desc_step, rect, nx, ny) ? PA_OK
                                                                               : PA_ERR_INVALID;
+} catch (const std::bad_alloc &) {
+  return PA_ERR_NOMEM;
+} catch (...) {
+  return PA_ERR_INVALID;
 }
 
 pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img_w,
                              const double *x_axis, const double *y_axis, double desc_step,
-                             int desc_size, float *cells, uint8_t *valid, int mem) {
+                             int desc_size, float *cells, uint8_t *valid, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!image || !cells || !valid || !x_axis || !y_axis || img_h < 2 || img_w < 2 ||
       !(desc_step > 0) || desc_size < 0 || img_h > 65535 || img_w > 65535)
@@ -2459,6 +2517,10 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
     PA_CK(cudaMemcpyAsync(valid, vout, ncell, cudaMemcpyDeviceToHost, ctx->stream));
   }
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 namespace {
@@ -2705,7 +2767,7 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
 pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image, int img_h,
                         int img_w, int flip, const pa_classifier *const *cls, int n_cls,
                         const pa_part_window *windows, const pa_abc_param *abc,
-                        float *log_unary, int mem) {
+                        float *log_unary, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
   if (!image || !log_unary || !windows || !abc || img_h < 5 || img_w < 5 || img_h > 16384 ||
@@ -2721,12 +2783,16 @@ pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
                                         windows, abc, log_unary, mem))
       return st;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
                                 const float *cells, const uint8_t *valid, int n_fields, int ny,
                                 int nx, int dc, int gx, int gy, double grid_step, int normalize,
-                                float *scores, int mem) {
+                                float *scores, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!cells || !valid || !scores || n_fields < 1 || ny < 1 || nx < 1 || dc < 1 || gx < 1 ||
       gy < 1 || !(grid_step > 0))
@@ -2782,11 +2848,15 @@ pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls, in
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, s));
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, int ny, int nx,
                         const double *Tig, int tig_shared, int interpolate, int H, int W,
-                        float *log_unary, int mem) {
+                        float *log_unary, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!scores || !Tig || !log_unary || n_parts < 1 || R < 1 || ny < 1 || nx < 1 || H < 1 || W < 1)
     return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
@@ -2831,11 +2901,15 @@ pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, in
     PA_CK(cudaMemcpyAsync(log_unary, d_out, nout * sizeof(float), cudaMemcpyDeviceToHost,
                           ctx->stream));
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
                       int is_sparse, const float *log_unary, int H, int W,
-                      const pa_ps_outputs *out, int mem) {
+                      const pa_ps_outputs *out, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
   if (!tree || !log_unary || !out || H < 1 || W < 1 || H > 32767 || W > 32767)
@@ -2934,12 +3008,16 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
     }
   if ((st = run_ps(ctx, ep, pl2))) return st;
   return finish_ps(ctx, ep, pl2, outs.data(), mem);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float *child,
                                 float *parent, int R, int H, int W, const double *offset_c,
                                 const double *offset_p, const double *C, double rot_mean,
-                                double rot_sigma, double scale, int is_sparse, int mem) {
+                                double rot_sigma, double scale, int is_sparse, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!ep || !child || !parent || !offset_c || !offset_p || !C || H < 1 || W < 1 ||
       H > 32767 || W > 32767 || R != ep->num_rotation_steps || !exp_ok(ep))
@@ -3033,10 +3111,14 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
     return fail(ctx, PA_ERR_NUMERIC, "exp() overflowed in the message (the reference asserts here)");
   if (errflag) return fail(ctx, PA_ERR_UNSUPPORTED, "message kernel rejected its input (code %d)", errflag);
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, int64_t ldb,
-                       float *C, int64_t ldc, int M, int N, int K, int band) {
+                       float *C, int64_t ldc, int M, int N, int K, int band) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!A || !B || !C || M < 1 || N < 1 || K < 1 || lda < K || ldb < K || ldc < N || lda % 8 ||
       ldb % 8 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
@@ -3063,29 +3145,41 @@ pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, i
   if (pa_status ss = sync_ctx(ctx)) return ss;
   if (flag) return fail(ctx, PA_ERR_CUDA, "GEMM pipeline wait timed out (flag %d)", flag);
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_find_obj(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
                       const pa_classifier *const *cls, int n_cls, const float *desc, int ny,
                       int nx, int dim, const double *Tig, int tig_shared, int H, int W,
-                      float *scores_out, const pa_ps_outputs *out, int mem) {
+                      float *scores_out, const pa_ps_outputs *out, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   return find_obj_impl(ctx, ep, 1, tree, flip, cls, n_cls, desc, ny, nx, dim, Tig, tig_shared, H,
                        W, scores_out, out, mem);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_find_obj_batch(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
                             const pa_tree *trees, int flip, const pa_classifier *const *cls,
                             int n_cls, const float *desc, int ny, int nx, int dim,
                             const double *Tig, int tig_shared, int H, int W, float *scores_out,
-                            const pa_ps_outputs *out, int mem) {
+                            const pa_ps_outputs *out, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   return find_obj_impl(ctx, ep, n_images, trees, flip, cls, n_cls, desc, ny, nx, dim, Tig,
                        tig_shared, H, W, scores_out, out, mem);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
-                            const pa_classifier *const *cls, int n_cls, int mem) {
+                            const pa_classifier *const *cls, int n_cls, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (n_images < 1 || !imgs || !cls || n_cls < 1)
     return fail(ctx, PA_ERR_INVALID, "invalid image list");
@@ -3267,13 +3361,17 @@ pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
     if (st) result = st;
   }
   return result;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 // ------------------------------------------------------------------------
 // Poselet-conditioned extra unaries (objectdetect_findrot.cpp:915-948)
 // ------------------------------------------------------------------------
 pa_status pa_add_extra_unaries(pa_ctx *ctx, const pa_exp_param *ep, const pa_extra_unary *ex,
-                               int n_parts, int root, float *log_unary, int H, int W, int mem) {
+                               int n_parts, int root, float *log_unary, int H, int W, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!ep || !exp_ok(ep) || !ex || !log_unary || n_parts < 1 || root < 0 || root >= n_parts ||
       H < 1 || W < 1 || H > 32767 || W > 32767)
@@ -3342,13 +3440,17 @@ pa_status pa_add_extra_unaries(pa_ctx *ctx, const pa_exp_param *ep, const pa_ext
   PA_LAUNCH("extra_unary", launch_extra_unary(eu, d, n_parts, S, R, H, W, ctx->stream));
   if (mem == PA_MEM_HOST) PA_CK(cudaMemcpyAsync(log_unary, d, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 // ------------------------------------------------------------------------
 // Learned unary
 // ------------------------------------------------------------------------
 pa_status pa_unary_net_create(pa_ctx *ctx, int dim, int n_parts, uint64_t seed,
-                              pa_unary_net **out) {
+                              pa_unary_net **out) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!out || dim < 64 || dim % 64 || dim > 4096 || n_parts < 1 || n_parts > 64)
     return fail(ctx, PA_ERR_INVALID, "net: dim must be a multiple of 64 (<= 4096), 1 <= n_parts <= 64");
@@ -3404,9 +3506,13 @@ pa_status pa_unary_net_create(pa_ctx *ctx, int dim, int n_parts, uint64_t seed,
     *out = nullptr;
   }
   return s;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_unary_net_destroy(pa_ctx *ctx, pa_unary_net *net) {
+pa_status pa_unary_net_destroy(pa_ctx *ctx, pa_unary_net *net) try {
   if (!net) return PA_OK;
   DeviceGuard dg(net->device);
   if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -3414,10 +3520,14 @@ pa_status pa_unary_net_destroy(pa_ctx *ctx, pa_unary_net *net) {
   if (net->params) cudaFree(net->params);
   delete net;
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_unary_net_get_params(pa_ctx *ctx, const pa_unary_net *net, float *params,
-                                  int64_t *n_params) {
+                                  int64_t *n_params) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!net) return fail(ctx, PA_ERR_INVALID, "NULL net");
   if (n_params) *n_params = net->n_params;
@@ -3426,9 +3536,13 @@ pa_status pa_unary_net_get_params(pa_ctx *ctx, const pa_unary_net *net, float *p
   PA_CK(cudaMemcpyAsync(params, net->params, (size_t)net->n_params * 4, cudaMemcpyDeviceToHost,
                         ctx->stream));
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_unary_net_set_params(pa_ctx *ctx, pa_unary_net *net, const float *params) {
+pa_status pa_unary_net_set_params(pa_ctx *ctx, pa_unary_net *net, const float *params) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!net || !params) return fail(ctx, PA_ERR_INVALID, "NULL net or parameters");
   DeviceGuard dg(ctx->device);
@@ -3439,11 +3553,15 @@ pa_status pa_unary_net_set_params(pa_ctx *ctx, pa_unary_net *net, const float *p
   net->step = 0;
   if (pa_status st = net_pack(ctx, net)) return st;
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_unary_net_forward(pa_ctx *ctx, pa_unary_net *net, const void *fields, int fields_bf16,
                                int n_fields, int ny, int nx, float *out, int64_t out_field_stride,
-                               int64_t out_part_stride, int exp_out) {
+                               int64_t out_part_stride, int exp_out) try {
   if (!ctx) return PA_ERR_INVALID;
   if (pa_status st = net_check_fields(ctx, net, fields, n_fields, ny, nx)) return st;
   if (!out) return fail(ctx, PA_ERR_INVALID, "NULL output");
@@ -3455,11 +3573,15 @@ pa_status pa_unary_net_forward(pa_ctx *ctx, pa_unary_net *net, const void *field
                                  out_field_stride, out_part_stride, exp_out ? 1 : 0, sc))
     return st;
   return net_err_check(ctx, net);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_unary_net_backward(pa_ctx *ctx, pa_unary_net *net, const void *fields,
                                 int fields_bf16, const float *scores, int n_fields, int ny,
-                                int nx, double *loss, float *grads) {
+                                int nx, double *loss, float *grads) try {
   if (!ctx) return PA_ERR_INVALID;
   if (pa_status st = net_check_fields(ctx, net, fields, n_fields, ny, nx)) return st;
   if (!scores) return fail(ctx, PA_ERR_INVALID, "NULL scores");
@@ -3477,9 +3599,13 @@ pa_status pa_unary_net_backward(pa_ctx *ctx, pa_unary_net *net, const void *fiel
   if (pa_status st = net_err_check(ctx, net)) return st;
   if (loss) *loss = l * (1.0 / ((double)n_fields * ny * nx * net->P));
   return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_unary_net_adam(pa_ctx *ctx, pa_unary_net *net, const pa_adam_param *opt) {
+pa_status pa_unary_net_adam(pa_ctx *ctx, pa_unary_net *net, const pa_adam_param *opt) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!net || !opt || !(opt->lr >= 0.f) || !(opt->beta1 >= 0.f && opt->beta1 < 1.f) ||
       !(opt->beta2 >= 0.f && opt->beta2 < 1.f) || !(opt->eps > 0.f))
@@ -3497,6 +3623,10 @@ pa_status pa_unary_net_adam(pa_ctx *ctx, pa_unary_net *net, const pa_adam_param 
                                     net->n_params, a, ctx->stream));
   if (pa_status st = net_pack(ctx, net)) return st;
   return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 pa_status pa_find_obj_batch_learned(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
@@ -3504,7 +3634,7 @@ pa_status pa_find_obj_batch_learned(pa_ctx *ctx, const pa_exp_param *ep, int n_i
                                     const int *part_on_net, const pa_classifier *const *cls,
                                     int n_cls, const void *fields, const float *desc, int ny,
                                     int nx, int dim, const double *Tig, int tig_shared, int H,
-                                    int W, const pa_ps_outputs *out) {
+                                    int W, const pa_ps_outputs *out) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!ep || !exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
   if (n_scales(ep) != 1)
@@ -3533,6 +3663,10 @@ pa_status pa_find_obj_batch_learned(pa_ctx *ctx, const pa_exp_param *ep, int n_i
   if (lu.any_net)
     if (pa_status s2 = net_err_check(ctx, net)) return s2;
   return st;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
 }  // extern "C"
