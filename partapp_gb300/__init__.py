@@ -733,15 +733,19 @@ def find_obj_batch_learned(ctx: Context, exp: ExpParam, trees, net: UnaryNet, fi
                            part_on_net=None, cls_list=None, desc=None, flip=False,
                            want_marg=False, want_root=False):
     """pa_find_obj_batch_learned: fields [B][R][ny][nx][dim] bfloat16 CUDA tensor
-    (read by the net), desc the float32 descriptors for the parts off the net."""
-    B, R, ny, nx, dim = fields.shape
+    (read by the net; may be None when no part is on the net), desc the float32
+    descriptors for the parts off the net (may be None when every part is)."""
+    ref = fields if fields is not None else desc
+    if ref is None:
+        raise ValueError("need the BF16 fields, the FP32 descriptors, or both")
+    B, R, ny, nx, dim = ref.shape
     ths = [_TreeHolder(t) for t in trees]
     arr = (Tree * B)(*[t.s for t in ths])
     P = ths[0].s.n_parts
     T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(-1)
     results, outs = [], (PsOutputs * B)()
     for i in range(B):
-        res, o = ctx._outputs(P, R, H, W, exp.roi_save_num_samples, PA_MEM_DEVICE, fields,
+        res, o = ctx._outputs(P, R, H, W, exp.roi_save_num_samples, PA_MEM_DEVICE, ref,
                               want_marg, want_root)
         results.append(res)
         outs[i] = o
