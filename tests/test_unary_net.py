@@ -223,9 +223,13 @@ def test_find_obj_learned_equals_its_parts(ctx, pa, on_net):
     if on_net == "none":
         plain = ctx.find_obj_batch(e, [im["tree"] for im in imgs], cls, desc, imgs[0]["Tig"], H,
                                    W, want_marg=True)
-        for a, b in zip(got, plain):
+        no_fields = pa.find_obj_batch_learned(ctx, e, [im["tree"] for im in imgs], net, None,
+                                              imgs[0]["Tig"], H, W, part_on_net=flags,
+                                              cls_list=cls, desc=desc, want_marg=True)
+        for a, b, c in zip(got, plain, no_fields):
             assert np.array_equal(a["best_conf"], b["best_conf"])
             assert np.array_equal(a["log_marg"].cpu().numpy(), b["log_marg"].cpu().numpy())
+            assert np.array_equal(c["log_marg"].cpu().numpy(), b["log_marg"].cpu().numpy())
     net.close()
 
 
