@@ -436,6 +436,36 @@ typedef struct {
 pa_status pa_add_extra_unaries(pa_ctx *ctx, const pa_exp_param *ep, const pa_extra_unary *ex,
                                int n_parts, int root, float *log_unary, int H, int W, int mem);
 
+/* The DPM score terms findObjectImageRotJoints adds to the log detections
+ * before the extra unary terms above (libPictStruct/objectdetect_findrot.cpp:
+ * 883-914), in that order:
+ *   torso  addDPMScore (objectdetect_icps.cpp:488-522) on the root part, every
+ *          scale and rotation: + torso_weight * L(x, y) with L the torso grid
+ *          after computeLogGrid (0 -> LOG_ZERO = -1e6, else log), in float
+ *   head   addLoadDPMScore (:445-486) on part head_part (skipped unless
+ *          detected): + (v > 1e-4 ? head_weight * log(v) : log(1e-4)), v the
+ *          grid value, the conditional in double
+ *   unary  addLoadDPMScore on every detected part with its own grid, per
+ *          rotation (unary_rot = 1, do_dpm_rot) or one for all rotations
+ * Grids hold the raw (not logged) scores loadDPMScoreGrid (:550-576) reads:
+ * torso and head [H][W], unary [n_parts][unary_rot ? R : 1][H][W].  A NULL
+ * grid switches its term off.  `mem` tells where log_unary and the grids lie.
+ *   log_unary [n_parts][S][R][H][W] (S = num_scale_steps), updated in place */
+typedef struct {
+  float torso_weight;          /* dpm_torso_weight */
+  const float *torso;          /* [H][W] torso DPM scores, or NULL */
+  float head_weight;           /* dpm_head_weight */
+  int head_part;               /* 5 (1 for 12 parts, 11 for 22 parts) in the reference */
+  const float *head;           /* [H][W] head DPM scores, or NULL */
+  float unary_weight;          /* dpm_unary_weight */
+  int unary_rot;               /* do_dpm_rot */
+  const float *unary;          /* [n_parts][unary_rot ? R : 1][H][W], or NULL */
+  const int *is_detect;        /* [n_parts] PartDef::is_detect flags (host), or NULL: all */
+} pa_dpm_terms;
+
+pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_terms *dt,
+                            int n_parts, int root, float *log_unary, int H, int W, int mem);
+
 /* ---------------------------------------------------- learned unary */
 
 /* No counterpart in the reference: a convolutional network that maps a

@@ -133,6 +133,10 @@ def _declare(L):
                                   dp, C.c_double, C.c_double, C.c_float, dp, C.POINTER(C.c_int),
                                   fp, C.c_int, C.c_int, C.c_int]
     L.orc_extra_unary.restype = C.c_int
+    L.orc_dpm_score.argtypes = [C.POINTER(OrcExp), C.c_int, C.c_int, C.c_float, fp, C.c_float,
+                                C.c_int, fp, C.c_float, C.c_int, fp, C.POINTER(C.c_int), fp,
+                                C.c_int, C.c_int, C.c_int]
+    L.orc_dpm_score.restype = C.c_int
     L.orc_find_obj_f32.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree), C.POINTER(OrcModels), fp,
                                    C.c_int, C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, fp, fp,
                                    fp, fp, fp, ip, fp, ip]
@@ -351,6 +355,40 @@ def extra_unary(exp: OrcExp, log_unary, root, rot=None, pos=None, torso=None, is
                                _p(u, C.c_float), S, H, W)
     if rc:
         raise ValueError(f"orc_extra_unary failed: {rc}")
+    return u.reshape(shape)
+
+
+def dpm_score(exp: OrcExp, log_unary, root, torso=None, head=None, unary=None, is_detect=None):
+    """findObjectImageRotJoints' DPM terms on a copy of log_unary [P][S][R][H][W]
+    (or [P][R][H][W]).  torso = (weight, grid [H][W]); head = (weight, part,
+    grid [H][W]); unary = (weight, grids [P][R or 1][H][W]); raw scores."""
+    u = np.array(log_unary, dtype=np.float32, copy=True)
+    shape = u.shape
+    if u.ndim == 4:
+        u = u[:, None]
+    P, S, R, H, W = u.shape
+    u = np.ascontiguousarray(u)
+    keep = []
+
+    def arr(a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        keep.append(a)
+        return _p(a, C.c_float)
+    tw, tg = (0.0, None) if torso is None else (torso[0], arr(torso[1]))
+    hw, hp, hg = (0.0, 0, None) if head is None else (head[0], head[1], arr(head[2]))
+    uw, ur, ug = 0.0, 0, None
+    if unary is not None:
+        g = np.asarray(unary[1])
+        uw, ur, ug = unary[0], int(g.shape[1] == R and R > 1), arr(g)
+    isd = None
+    if is_detect is not None:
+        isd_a = np.ascontiguousarray(is_detect, dtype=np.int32)
+        keep.append(isd_a)
+        isd = _p(isd_a, C.c_int)
+    rc = lib().orc_dpm_score(C.byref(exp), P, int(root), float(tw), tg, float(hw), int(hp), hg,
+                             float(uw), ur, ug, isd, _p(u, C.c_float), S, H, W)
+    if rc:
+        raise ValueError(f"orc_dpm_score failed: {rc}")
     return u.reshape(shape)
 
 

@@ -845,6 +845,54 @@ int orc_extra_unary(const orc_exp *e, int P, int root, float rot_weight, const d
   return 0;
 }
 
+/* The DPM terms of findObjectImageRotJoints, objectdetect_findrot.cpp:883-914,
+ * in that order, each a full pass over lu [P][S][R][H][W] as the reference
+ * makes it:
+ *   torso: computeLogGrid of the torso grid (float), then addDPMScore
+ *          (objectdetect_icps.cpp:488-522) on the root part
+ *   head:  addLoadDPMScore (:445-486) with pidx_only = head_part, one grid
+ *   unary: addLoadDPMScore on every detected part, grids [P][Ru][H][W] with
+ *          Ru = R (rotidx_dpm = rotidx) or 1 (rotidx_dpm = 0) */
+static void load_dpm_add(float *lu, const float *grid, int Ru, float dpm_weight, int S, int R,
+                         size_t HW) {
+  for (int s = 0; s < S; ++s)
+    for (int r = 0; r < R; ++r) {
+      const int rd = (Ru == R ? r : 0);
+      for (size_t i = 0; i < HW; ++i) {
+        const float val = grid[(size_t)rd * HW + i];
+        float &c = lu[((size_t)s * R + r) * HW + i];
+        c += (val > 1e-4 ? dpm_weight * std::log(val) : std::log(1e-4));
+      }
+    }
+}
+
+int orc_dpm_score(const orc_exp *e, int P, int root, float torso_weight, const float *torso,
+                  float head_weight, int head_part, const float *head, float unary_weight,
+                  int unary_rot, const float *unary, const int *is_detect, float *lu, int S,
+                  int H, int W) {
+  if (!e || P < 1 || root < 0 || root >= P || !lu || S < 1 || H < 1 || W < 1) return 1;
+  if (head && (head_part < 0 || head_part >= P)) return 1;
+  const int R = e->num_rotation_steps;
+  const size_t HW = (size_t)H * W, NP = (size_t)S * R * HW;
+  auto detect = [&](int p) { return is_detect ? is_detect[p] != 0 : true; };
+  if (torso) {
+    std::vector<float> lg(torso, torso + HW);
+    log_grid(lg.data(), HW);
+    for (int s = 0; s < S; ++s)
+      for (int r = 0; r < R; ++r)
+        for (size_t i = 0; i < HW; ++i)
+          lu[(size_t)root * NP + ((size_t)s * R + r) * HW + i] += torso_weight * lg[i];
+  }
+  if (head && detect(head_part))
+    load_dpm_add(lu + (size_t)head_part * NP, head, 1, head_weight, S, R, HW);
+  if (unary) {
+    const int Ru = unary_rot ? R : 1;
+    for (int p = 0; p < P; ++p)
+      if (detect(p)) load_dpm_add(lu + (size_t)p * NP, unary + (size_t)p * Ru * HW, Ru, unary_weight, S, R, HW);
+  }
+  return 0;
+}
+
 int orc_squeeze_bbox(const float *grid, int ny, int nx, int *bbox) {
   int minx = nx, maxx = -1, miny = ny, maxy = -1;
   for (int ix = 0; ix < nx; ++ix)

@@ -242,6 +242,14 @@ int orc_extra_unary(const orc_exp *e, int P, int root, float rot_weight, const d
                     double root_det_y, float torso_weight, const double *torso_prior,
                     const int *is_detect, float *lu, int S, int H, int W);
 
+/* addDPMScore + addLoadDPMScore (torso, head, unary DPM grids) on lu
+ * [P][S][R][H][W]; raw grids torso/head [H][W], unary [P][unary_rot ? R : 1]
+ * [H][W]; a NULL grid switches its term off. */
+int orc_dpm_score(const orc_exp *e, int P, int root, float torso_weight, const float *torso,
+                  float head_weight, int head_part, const float *head, float unary_weight,
+                  int unary_rot, const float *unary, const int *is_detect, float *lu, int S,
+                  int H, int W);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,7 +52,7 @@ EXPORTS = (
     "pa_find_obj_batch", "pa_gemm_bf16", "pa_ctx_set_message_math", "pa_find_obj_multi",
     "pa_unary_net_create", "pa_unary_net_destroy", "pa_unary_net_get_params",
     "pa_unary_net_set_params", "pa_unary_net_forward", "pa_unary_net_backward",
-    "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries",
+    "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries", "pa_add_dpm_scores",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
@@ -112,6 +112,12 @@ class ExtraUnary(C.Structure):
                 ("pos_params", C.c_void_p), ("root_det_x", C.c_double), ("root_det_y", C.c_double),
                 ("torso_weight", C.c_float), ("torso_prior", C.c_void_p),
                 ("is_detect", C.c_void_p)]
+
+
+class DpmTerms(C.Structure):
+    _fields_ = [("torso_weight", C.c_float), ("torso", C.c_void_p), ("head_weight", C.c_float),
+                ("head_part", C.c_int), ("head", C.c_void_p), ("unary_weight", C.c_float),
+                ("unary_rot", C.c_int), ("unary", C.c_void_p), ("is_detect", C.c_void_p)]
 
 
 class PsOutputs(C.Structure):
@@ -177,6 +183,7 @@ def load_library():
     L.pa_find_obj_batch.argtypes = [vp, P(ExpParam), ip, P(Tree), ip, P(vp), ip, vp, ip, ip, ip,
                                     P(dp), ip, ip, ip, vp, P(PsOutputs), ip]
     L.pa_add_extra_unaries.argtypes = [vp, P(ExpParam), P(ExtraUnary), ip, ip, vp, ip, ip, ip]
+    L.pa_add_dpm_scores.argtypes = [vp, P(ExpParam), P(DpmTerms), ip, ip, vp, ip, ip, ip]
     L.pa_unary_net_create.argtypes = [vp, ip, ip, C.c_uint64, P(vp)]
     L.pa_unary_net_destroy.argtypes = [vp, vp]
     L.pa_unary_net_get_params.argtypes = [vp, vp, vp, P(C.c_int64)]
@@ -568,6 +575,49 @@ class Context:
             ex.is_detect = arr(is_detect, np.int32)
         self._check(self.L.pa_add_extra_unaries(self.h, C.byref(exp), C.byref(ex), P, int(root),
                                                 u.ptr, H, W, u.mem))
+        if u.mem == PA_MEM_HOST and u.arr is not log_unary:
+            np.copyto(log_unary, u.arr)
+        return log_unary
+
+    def add_dpm_scores(self, exp: ExpParam, log_unary, root, torso=None, head=None, unary=None,
+                       is_detect=None):
+        """findObjectImageRotJoints' DPM terms, in place on log_unary
+        [P][S][R][H][W] or [P][R][H][W] (numpy or CUDA tensor; the grids are
+        taken to the same place).  torso = (weight, grid [H][W]); head =
+        (weight, part, grid [H][W]); unary = (weight, grids [P][R or 1][H][W]);
+        grids hold raw DPM scores."""
+        u = _Buf(log_unary, np.float32)
+        shp = u.arr.shape
+        P, R, H, W = shp[0], shp[-3], shp[-2], shp[-1]
+        keep = []
+
+        def grid(a):
+            if u.mem == PA_MEM_DEVICE:
+                import torch
+
+                t = torch.as_tensor(a, dtype=torch.float32, device=log_unary.device).contiguous()
+                keep.append(t)
+                return t.data_ptr()
+            a = np.ascontiguousarray(a, dtype=np.float32)
+            keep.append(a)
+            return a.ctypes.data
+
+        dt = DpmTerms()
+        if torso is not None:
+            dt.torso_weight, dt.torso = float(torso[0]), grid(torso[1])
+        if head is not None:
+            dt.head_weight, dt.head_part, dt.head = float(head[0]), int(head[1]), grid(head[2])
+        if unary is not None:
+            g = unary[1]
+            if tuple(g.shape) not in ((P, R, H, W), (P, 1, H, W)):
+                raise ValueError("unary DPM grids must be [P][R or 1][H][W]")
+            dt.unary_weight, dt.unary_rot, dt.unary = float(unary[0]), int(g.shape[1] == R and R > 1), grid(g)
+        if is_detect is not None:
+            isd = np.ascontiguousarray(is_detect, dtype=np.int32)
+            keep.append(isd)
+            dt.is_detect = isd.ctypes.data
+        self._check(self.L.pa_add_dpm_scores(self.h, C.byref(exp), C.byref(dt), P, int(root),
+                                             u.ptr, H, W, u.mem))
         if u.mem == PA_MEM_HOST and u.arr is not log_unary:
             np.copyto(log_unary, u.arr)
         return log_unary

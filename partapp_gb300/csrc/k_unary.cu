@@ -370,4 +370,57 @@ cudaError_t launch_extra_unary(const ExtraUnary &ex, float *lu, int P, int S, in
   return cudaGetLastError();
 }
 
+// addLoadDPMScore's term (objectdetect_icps.cpp:476-482): val > 1e-4 compares
+// in double, dpm_weight * log(val) is float (std::log(float)), log(1e-4) is
+// double, so the conditional is double and the += rounds once to float.
+__device__ __forceinline__ float add_loaded_dpm(float u, float val, float w, double log_floor) {
+  const double t = (double)val > 1e-4 ? (double)__fmul_rn(w, logf(val)) : log_floor;
+  return (float)((double)u + t);
+}
+
+// The DPM terms of findObjectImageRotJoints (objectdetect_findrot.cpp:883-914)
+// in the reference's order: the torso grid, computeLogGrid'ed in float and
+// added to the root part by addDPMScore (objectdetect_icps.cpp:488-522, float
+// products and sums); the head grid (addLoadDPMScore for one part); the
+// per-part unary grids (addLoadDPMScore for every detected part).  Thread per
+// (part, pixel); every scale and rotation of that pixel in turn.
+__global__ void k_dpm_score(DpmTerms dt, float *__restrict__ lu, int S, int R, int H, int W) {
+  const int p = blockIdx.y;
+  const int64_t HW = (int64_t)H * W;
+  const int64_t pix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (pix >= HW) return;
+  const bool detect = dt.is_detect ? dt.is_detect[p] != 0 : true;
+  const bool torso = dt.torso && p == dt.root;
+  float torso_w = 0.f;
+  if (torso) {
+    const float g = dt.torso[pix];
+    torso_w = __fmul_rn(dt.torso_weight, g == 0.f ? (float)-1e6 : logf(g));
+  }
+  const bool head = dt.head && detect && p == dt.head_part;
+  const float head_v = head ? dt.head[pix] : 0.f;
+  const bool unary = dt.unary && detect;
+  const int Ru = dt.unary_rot ? R : 1;
+  for (int s = 0; s < S; ++s)
+    for (int r = 0; r < R; ++r) {
+      float *c = lu + (((int64_t)p * S + s) * R + r) * HW + pix;
+      float u = *c;
+      if (torso) u = __fadd_rn(u, torso_w);
+      if (head) u = add_loaded_dpm(u, head_v, dt.head_weight, dt.log_floor);
+      if (unary)
+        u = add_loaded_dpm(u, dt.unary[((int64_t)p * Ru + (dt.unary_rot ? r : 0)) * HW + pix],
+                           dt.unary_weight, dt.log_floor);
+      *c = u;
+    }
+}
+
+cudaError_t launch_dpm_score(const DpmTerms &dt, float *lu, int P, int S, int R, int H, int W,
+                             cudaStream_t s) {
+  const int64_t HW = (int64_t)H * W;
+  if (P < 1 || P > 65535 || HW < 1 || (HW + kThreads - 1) / kThreads > 0x7FFFFFFF)
+    return cudaErrorInvalidValue;
+  k_dpm_score<<<dim3((unsigned)((HW + kThreads - 1) / kThreads), (unsigned)P), kThreads, 0, s>>>(
+      dt, lu, S, R, H, W);
+  return cudaGetLastError();
+}
+
 }  // namespace pa

@@ -19,6 +19,7 @@
 #include <memory>
 #include <new>
 #include <stdexcept>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -3439,6 +3440,75 @@ pa_status pa_add_extra_unaries(pa_ctx *ctx, const pa_exp_param *ep, const pa_ext
   if (mem == PA_MEM_HOST) PA_CK(cudaMemcpyAsync(d, log_unary, n * 4, cudaMemcpyHostToDevice, ctx->stream));
   PA_LAUNCH("extra_unary", launch_extra_unary(eu, d, n_parts, S, R, H, W, ctx->stream));
   if (mem == PA_MEM_HOST) PA_CK(cudaMemcpyAsync(log_unary, d, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_ctx(ctx);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
+}
+
+pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_terms *dt,
+                            int n_parts, int root, float *log_unary, int H, int W, int mem) try {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!ep || !exp_ok(ep) || !dt || !log_unary || n_parts < 1 || root < 0 || root >= n_parts ||
+      H < 1 || W < 1 || H > 32767 || W > 32767)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes, parameters or NULL input");
+  if (dt->head && (dt->head_part < 0 || dt->head_part >= n_parts))
+    return fail(ctx, PA_ERR_INVALID, "head_part out of range");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  DeviceGuard dg(ctx->device);
+  const int S = n_scales(ep), R = ep->num_rotation_steps;
+  const size_t HW = (size_t)H * W;
+  const size_t n = (size_t)n_parts * S * R * HW;
+  const size_t n_unary = dt->unary ? (size_t)n_parts * (dt->unary_rot ? R : 1) * HW : 0;
+  const size_t n_torso = dt->torso ? HW : 0, n_head = dt->head ? HW : 0;
+  std::vector<int> det(n_parts, 1);
+  if (dt->is_detect)
+    for (int p = 0; p < n_parts; ++p) det[p] = dt->is_detect[p] ? 1 : 0;
+  Builder b1;
+  b1.param(det.data(), det.size());
+  if (mem == PA_MEM_HOST) {
+    b1.scratch<float>(n);
+    b1.scratch<float>(n_torso + n_head + n_unary);
+  }
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  b.base = ctx->arena;
+  DpmTerms d{};
+  d.root = root;
+  d.head_part = dt->head_part;
+  d.unary_rot = dt->unary_rot ? 1 : 0;
+  d.torso_weight = dt->torso_weight;
+  d.head_weight = dt->head_weight;
+  d.unary_weight = dt->unary_weight;
+  d.log_floor = std::log(1e-4);
+  d.is_detect = b.param(det.data(), det.size());
+  float *lu = log_unary, *grids = nullptr;
+  if (mem == PA_MEM_HOST) {
+    lu = b.scratch<float>(n);
+    grids = b.scratch<float>(n_torso + n_head + n_unary);
+  }
+  if ((st = upload_blob(ctx, b))) return st;
+  if (mem == PA_MEM_HOST) {
+    PA_CK(cudaMemcpyAsync(lu, log_unary, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    float *g = grids;
+    for (auto [src, cnt, dst] : {std::tuple<const float *, size_t, const float **>{dt->torso, n_torso, &d.torso},
+                                 {dt->head, n_head, &d.head}, {dt->unary, n_unary, &d.unary}}) {
+      if (!src) continue;
+      PA_CK(cudaMemcpyAsync(g, src, cnt * 4, cudaMemcpyHostToDevice, ctx->stream));
+      *dst = g;
+      g += cnt;
+    }
+  } else {
+    d.torso = dt->torso;
+    d.head = dt->head;
+    d.unary = dt->unary;
+  }
+  PA_LAUNCH("dpm_score", launch_dpm_score(d, lu, n_parts, S, R, H, W, ctx->stream));
+  if (mem == PA_MEM_HOST) PA_CK(cudaMemcpyAsync(log_unary, lu, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   return sync_ctx(ctx);
 } catch (const std::bad_alloc &) {
   return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");

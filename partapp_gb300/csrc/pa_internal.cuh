@@ -296,6 +296,18 @@ struct ExtraUnary {
 cudaError_t launch_extra_unary(const ExtraUnary &ex, float *lu, int P, int S, int R, int H, int W,
                                cudaStream_t s);
 
+// DPM score terms (pa_add_dpm_scores): raw grids [H][W] (torso, head) and
+// [P][Rd][H][W] (unary, Rd = R or 1), all >= 0 as the reference loads them.
+struct DpmTerms {
+  int root, head_part, unary_rot;
+  float torso_weight, head_weight, unary_weight;
+  const float *torso, *head, *unary;  // null: term off
+  double log_floor;                   // log(1e-4) in double
+  const int *is_detect;               // [P] or null (every part detected)
+};
+cudaError_t launch_dpm_score(const DpmTerms &dt, float *lu, int P, int S, int R, int H, int W,
+                             cudaStream_t s);
+
 // ---------------------------------------------------------------------------
 // Learned unary: convolutions on the tensor cores (k_conv.cu).
 // Activations NHWC bf16 [field][row][column][channel]; weights bf16

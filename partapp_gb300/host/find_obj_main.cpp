@@ -40,6 +40,11 @@
 //   --pred_dir DIR --pred_pos_weight w --torso_det_dir DIR [--rootidx_det k]
 //                                        position score around the torso detection
 //   --torso_prior FILE --torso_prior_weight w   torso position prior
+// and, before them, the DPM score terms (objectdetect_findrot.cpp:883-914):
+//   --dpm_torso_dir DIR [--dpm_torso_weight w]  torso grid on the root part
+//   --dpm_unary_dir DIR --use_dpm_head [--dpm_head_weight w]   head grid
+//   --dpm_unary_dir DIR --use_dpm_unary [--dpm_unary_weight w] [--dpm_rot]
+//                                        per-part grids (per rotation)
 //
 // --mat_dump FILE prints every variable of a MAT-file (name, class, dims and
 // values in MATLAB's column-major order, cells one by one).
@@ -205,6 +210,9 @@ void usage() {
                "                        [--pred_dir DIR --pred_rot_weight w --pred_pos_weight w\n"
                "                         --torso_det_dir DIR --rootidx_det k]\n"
                "                        [--torso_prior FILE --torso_prior_weight w]\n"
+               "                        [--dpm_torso_dir DIR --dpm_torso_weight w]\n"
+               "                        [--dpm_unary_dir DIR --use_dpm_head --dpm_head_weight w\n"
+               "                         --use_dpm_unary --dpm_unary_weight w --dpm_rot]\n"
                "       partapp_find_obj --mat_dump FILE\n";
 }
 
@@ -214,6 +222,7 @@ int main(int argc, char **argv) {
   std::string expdir, outdir, scoregrid_dir, pred_dir, torso_det_dir, torso_prior;
   float rot_w = 0.f, pos_w = 0.f, torso_w = 0.f;
   int rootidx_det = -1;
+  DpmOptions dpm;
   int first = 0, numimgs = -1, batch = 1, device = 0;
   bool find_obj = false, flip = false, save_marg = false, from_images = false;
   for (int i = 1; i < argc; ++i) {
@@ -240,6 +249,14 @@ int main(int argc, char **argv) {
     else if (a == "--rootidx_det") rootidx_det = std::atoi(next().c_str());
     else if (a == "--torso_prior") torso_prior = next();
     else if (a == "--torso_prior_weight") torso_w = (float)std::atof(next().c_str());
+    else if (a == "--dpm_torso_dir") dpm.torso_dir = next();
+    else if (a == "--dpm_torso_weight") dpm.torso_weight = (float)std::atof(next().c_str());
+    else if (a == "--dpm_unary_dir") dpm.unary_dir = next();
+    else if (a == "--use_dpm_head") dpm.head = true;
+    else if (a == "--dpm_head_weight") dpm.head_weight = (float)std::atof(next().c_str());
+    else if (a == "--use_dpm_unary") dpm.unary = true;
+    else if (a == "--dpm_unary_weight") dpm.unary_weight = (float)std::atof(next().c_str());
+    else if (a == "--dpm_rot") dpm.rot = true;
     else if (a == "--mat_dump") {
       try {
         for (const MatArray &v : mat_read(next())) dump_array(v, "");
@@ -302,9 +319,11 @@ int main(int argc, char **argv) {
           PartConfig pc;
           read_joints(jp, pc, joints);
         }
-        const ExtraUnaryParams extra = loadExtraUnaryParams(
+        ExtraUnaryParams extra = loadExtraUnaryParams(
             i, app.m_part_conf.part_size(), app.m_part_conf.rootpart_idx, pred_dir, rot_w, pos_w,
             torso_det_dir, rootidx_det, torso_prior, torso_w);
+        loadDpmScores(extra, i, app.m_part_conf.part_size(), app.m_exp_param.c().num_rotation_steps,
+                      h, w, dpm);
         app.m_extra = &extra;
         const FindObjResult r = findObjectImageFromImage(ctx, app, flip, joints, img.data(), h, w,
                                                          save_marg);
@@ -332,9 +351,10 @@ int main(int argc, char **argv) {
         std::vector<ScoreGridSet> parts;
         for (int p = 0; p < P; ++p)
           parts.push_back(loadScoreGrid(scoreGridFileName(scoregrid_dir, i, p, flip)));
-        const ExtraUnaryParams extra =
+        ExtraUnaryParams extra =
             loadExtraUnaryParams(i, P, app.m_part_conf.rootpart_idx, pred_dir, rot_w, pos_w,
                                  torso_det_dir, rootidx_det, torso_prior, torso_w);
+        loadDpmScores(extra, i, P, app.m_exp_param.c().num_rotation_steps, h, w, dpm);
         app.m_extra = &extra;
         const FindObjResult r =
             findObjectImageFromScoreGrids(ctx, app, flip, joints, parts, h, w, save_marg);

@@ -280,9 +280,31 @@ std::vector<float> partdetect_raw(Context &ctx, const PartApp &part_app, const f
 void applyExtraUnaries(Context &ctx, const PartApp &part_app, std::vector<float> &lu, int H,
                        int W) {
   const ExtraUnaryParams *x = part_app.m_extra;
-  if (!x || (x->rot.empty() && x->pos.empty() && x->torso.empty())) return;
+  if (!x) return;
   const pa_exp_param e = part_app.m_exp_param.c();
   const int P = part_app.m_part_conf.part_size();
+  const int R = e.num_rotation_steps;
+  const size_t HW = (size_t)H * W;
+  if (!x->dpm_torso.empty() || !x->dpm_head.empty() || !x->dpm_unary.empty()) {
+    require(x->dpm_torso.empty() || x->dpm_torso.size() == HW, "DPM torso grid: [H][W]");
+    require(x->dpm_head.empty() || x->dpm_head.size() == HW, "DPM head grid: [H][W]");
+    require(x->dpm_unary.empty() ||
+                x->dpm_unary.size() == (size_t)P * (x->dpm_unary_rot ? R : 1) * HW,
+            "DPM unary grids: [P][R or 1][H][W]");
+    pa_dpm_terms dt{};
+    dt.torso_weight = x->dpm_torso_weight;
+    dt.torso = x->dpm_torso.empty() ? nullptr : x->dpm_torso.data();
+    dt.head_weight = x->dpm_head_weight;
+    dt.head_part = x->dpm_head_part;
+    dt.head = x->dpm_head.empty() ? nullptr : x->dpm_head.data();
+    dt.unary_weight = x->dpm_unary_weight;
+    dt.unary_rot = x->dpm_unary_rot;
+    dt.unary = x->dpm_unary.empty() ? nullptr : x->dpm_unary.data();
+    dt.is_detect = x->is_detect.empty() ? nullptr : x->is_detect.data();
+    ctx.check(pa_add_dpm_scores(ctx.get(), &e, &dt, P, part_app.m_part_conf.rootpart_idx,
+                                lu.data(), H, W, PA_MEM_HOST));
+  }
+  if (x->rot.empty() && x->pos.empty() && x->torso.empty()) return;
   require(x->rot.empty() || (int)x->rot.size() == 2 * P, "rotation parameters: 2 per part");
   require(x->pos.empty() || (int)x->pos.size() == 4 * P, "position parameters: 4 per part");
   require(x->torso.empty() || x->torso.size() == 4, "torso prior: 4 parameters");
@@ -398,6 +420,67 @@ ExtraUnaryParams loadExtraUnaryParams(int imgidx, int n_parts, int root, const s
     x.torso_weight = torso_weight;
   }
   return x;
+}
+
+namespace {
+
+// One [H][W] MATLAB array (column-major) as a row-major float grid.
+void dpm_grid(const MatArray &a, int H, int W, const std::string &what, float *dst) {
+  require(!a.is_cell() && a.dims.size() == 2 && (int)a.dims[0] == H && (int)a.dims[1] == W,
+          what + ": scoregrid is not [" + std::to_string(H) + "][" + std::to_string(W) + "]");
+  for (int y = 0; y < H; ++y)
+    for (int xx = 0; xx < W; ++xx) dst[(size_t)y * W + xx] = (float)a.re[y + (size_t)H * xx];
+}
+
+std::string dpm_file(const std::string &dir, int imgidx) {
+  char name[64];
+  std::snprintf(name, sizeof name, "/imgidx_%04d.mat", imgidx + 1);
+  return dir + name;
+}
+
+// The cell form of loadDPMScoreGrid: a [Rd][1] cell of [H][W] grids.
+void dpm_cell(const std::string &path, int Rd, int H, int W, float *dst) {
+  const auto v = mat_read(path);
+  const MatArray &c = mat_find(v, "scoregrid");
+  require(c.is_cell() && c.dims.size() == 2 && (int)c.dims[0] == Rd && c.dims[1] == 1,
+          path + ": scoregrid is not a [" + std::to_string(Rd) + "][1] cell");
+  for (int r = 0; r < Rd; ++r) dpm_grid(c.cells[r], H, W, path, dst + (size_t)r * H * W);
+}
+
+}  // namespace
+
+void loadDpmScores(ExtraUnaryParams &x, int imgidx, int n_parts, int R, int H, int W,
+                   const DpmOptions &o) {
+  const size_t HW = (size_t)H * W;
+  if (!o.torso_dir.empty()) {
+    const std::string path = dpm_file(o.torso_dir, imgidx);
+    const auto v = mat_read(path);
+    x.dpm_torso.resize(HW);
+    dpm_grid(mat_find(v, "scoregrid"), H, W, path, x.dpm_torso.data());
+    x.dpm_torso_weight = o.torso_weight;
+  }
+  auto detect = [&](int p) { return x.is_detect.empty() || x.is_detect[p] != 0; };
+  if (o.head && !o.unary_dir.empty()) {
+    x.dpm_head_part = n_parts == 22 ? 11 : n_parts == 12 ? 1 : 5;
+    require(x.dpm_head_part < n_parts, "DPM head: no head part");
+    if (detect(x.dpm_head_part)) {
+      x.dpm_head.resize(HW);
+      dpm_cell(dpm_file(o.unary_dir + "/head", imgidx), 1, H, W, x.dpm_head.data());
+      x.dpm_head_weight = o.head_weight;
+    }
+  }
+  if (o.unary && !o.unary_dir.empty()) {
+    const int Rd = o.rot ? R : 1;
+    x.dpm_unary.assign((size_t)n_parts * Rd * HW, 0.f);
+    for (int p = 0; p < n_parts; ++p) {
+      if (!detect(p)) continue;
+      char sub[32];
+      std::snprintf(sub, sizeof sub, "/pidx_%04d", p);
+      dpm_cell(dpm_file(o.unary_dir + sub, imgidx), Rd, H, W, x.dpm_unary.data() + (size_t)p * Rd * HW);
+    }
+    x.dpm_unary_rot = o.rot ? 1 : 0;
+    x.dpm_unary_weight = o.unary_weight;
+  }
 }
 
 std::string scoreGridFileName(const std::string &dir, int imgidx, int pidx, bool flip) {

@@ -189,7 +189,41 @@ struct ExtraUnaryParams {
   float torso_weight = 0.f;         // torso_pos_prior_weight
   std::vector<double> torso;        // [4]: mu_x, mu_y, var_x, var_y
   std::vector<int> is_detect;       // [P] (empty: every part)
+  // DPM score terms, added before the terms above (raw grids; empty: off)
+  float dpm_torso_weight = 0.f;     // dpm_torso_weight
+  std::vector<float> dpm_torso;     // [H][W]
+  float dpm_head_weight = 0.f;      // dpm_head_weight
+  int dpm_head_part = 5;
+  std::vector<float> dpm_head;      // [H][W]
+  float dpm_unary_weight = 0.f;     // dpm_unary_weight
+  int dpm_unary_rot = 0;            // do_dpm_rot
+  std::vector<float> dpm_unary;     // [P][dpm_unary_rot ? R : 1][H][W]
 };
+
+// Where the DPM grids lie and how they are weighted (use_dpm_torso with
+// test_dpm_torso_dir, use_dpm_head and use_dpm_unary with test_dpm_unary_dir,
+// do_dpm_rot).  An empty directory leaves that term off.
+struct DpmOptions {
+  std::string torso_dir;
+  float torso_weight = 1.f;
+  bool head = false;
+  float head_weight = 1.f;
+  bool unary = false;
+  std::string unary_dir;
+  float unary_weight = 1.f;
+  bool rot = false;
+};
+
+// Reads the DPM grids of image imgidx as loadDPMScoreGrid
+// (objectdetect_icps.cpp:550-576) finds them: <dir>/imgidx_<NNNN>.mat with
+// NNNN = imgidx + 1, variable "scoregrid" -- a plain [H][W] array for the
+// torso, a cell of [H][W] arrays, one per DPM rotation, for the head
+// (<test_dpm_unary_dir>/head) and the unary grids
+// (<test_dpm_unary_dir>/pidx_<NNNN>, NNNN = part index, detected parts only).
+// The head part is part 5, 1 with 12 parts, 11 with 22 parts
+// (objectdetect_findrot.cpp:893-898).
+void loadDpmScores(ExtraUnaryParams &x, int imgidx, int n_parts, int R, int H, int W,
+                   const DpmOptions &o);
 
 // Reads the reference's prediction files for image imgidx:
 //   rot:   <pred_dir>/testlist_params_rot_imgidx<i>.mat, "rot_test" [P][2+]
