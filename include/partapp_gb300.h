@@ -466,6 +466,20 @@ typedef struct {
 pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_terms *dt,
                             int n_parts, int root, float *log_unary, int H, int W, int mem);
 
+/* ------------------------------------------- hypothesis suppression */
+
+/* nms_recursive (libPictStruct/objectdetect_aux.cpp:407-451), as
+ * saveRecoResults (:453-600) runs it on the merged root hypotheses of an
+ * image: hypotheses sorted by descending score; suppressed[j] = 1 when an
+ * earlier hypothesis i has (x_i - x_j)^2 / e1 + (y_i - y_j)^2 / e2 < 1 with
+ * e1 = (0.5 * scale_i * train_object_width)^2, e2 likewise with the height
+ * (the differences in float, the rest in double, as the reference types it).
+ * Scores out of descending order are PA_ERR_INVALID (the reference asserts).
+ * `mem` tells where the five arrays lie; n = 0 is a no-op. */
+pa_status pa_nms_recursive(pa_ctx *ctx, int n, const float *x, const float *y, const float *scale,
+                           const float *score, double train_object_width,
+                           double train_object_height, int *suppressed, int mem);
+
 /* ---------------------------------------------------- learned unary */
 
 /* No counterpart in the reference: a convolutional network that maps a

@@ -137,6 +137,9 @@ def _declare(L):
                                 C.c_int, fp, C.c_float, C.c_int, fp, C.POINTER(C.c_int), fp,
                                 C.c_int, C.c_int, C.c_int]
     L.orc_dpm_score.restype = C.c_int
+    L.orc_nms_recursive.argtypes = [C.c_int, fp, fp, fp, fp, C.c_double, C.c_double,
+                                    C.POINTER(C.c_int)]
+    L.orc_nms_recursive.restype = C.c_int
     L.orc_find_obj_f32.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree), C.POINTER(OrcModels), fp,
                                    C.c_int, C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, fp, fp,
                                    fp, fp, fp, ip, fp, ip]
@@ -390,6 +393,18 @@ def dpm_score(exp: OrcExp, log_unary, root, torso=None, head=None, unary=None, i
     if rc:
         raise ValueError(f"orc_dpm_score failed: {rc}")
     return u.reshape(shape)
+
+
+def nms_recursive(x, y, scale, score, train_w, train_h):
+    """Suppressed flags (bool [n]) of hypotheses sorted by descending score."""
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, scale, score)]
+    n = len(a[0])
+    out = np.zeros(max(n, 1), np.int32)
+    rc = lib().orc_nms_recursive(n, *[_p(v, C.c_float) for v in a], float(train_w),
+                                 float(train_h), _p(out, C.c_int))
+    if rc:
+        raise ValueError(f"orc_nms_recursive failed: {rc}")
+    return out[:n].astype(bool)
 
 
 def find_obj(exp: OrcExp, tree, models, desc, Tig, H, W, interpolate=True):

@@ -893,6 +893,31 @@ int orc_dpm_score(const orc_exp *e, int P, int root, float torso_weight, const f
   return 0;
 }
 
+/* nms_recursive, libPictStruct/objectdetect_aux.cpp:407-451: hypotheses
+ * sorted by descending score (returns 2 when not, where the reference
+ * asserts); ellipse_size 0.5, dist_threshold 1.0; the coordinates and scale
+ * are the float fields of HypothesisList.proto. */
+int orc_nms_recursive(int n, const float *x, const float *y, const float *scale,
+                      const float *score, double train_object_width,
+                      double train_object_height, int *nms) {
+  const double dist_threshold = 1.0, ellipse_size = 0.5;
+  if (n < 0) return 1;
+  for (int i = 0; i < n; ++i) nms[i] = 0;
+  for (int i = 0; i < n; ++i) {
+    if (i != n - 1 && score[i] < score[i + 1]) return 2;
+    const double sc = scale[i];
+    for (int j = i + 1; j < n; ++j) {
+      const double a = ellipse_size * sc * train_object_width;
+      const double b = ellipse_size * sc * train_object_height;
+      const double e1 = a * a, e2 = b * b;
+      const double dx = x[i] - x[j];
+      const double dy = y[i] - y[j];
+      if (dx * dx / e1 + dy * dy / e2 < dist_threshold) nms[j] = 1;
+    }
+  }
+  return 0;
+}
+
 int orc_squeeze_bbox(const float *grid, int ny, int nx, int *bbox) {
   int minx = nx, maxx = -1, miny = ny, maxy = -1;
   for (int ix = 0; ix < nx; ++ix)

@@ -245,6 +245,12 @@ int orc_extra_unary(const orc_exp *e, int P, int root, float rot_weight, const d
 /* addDPMScore + addLoadDPMScore (torso, head, unary DPM grids) on lu
  * [P][S][R][H][W]; raw grids torso/head [H][W], unary [P][unary_rot ? R : 1]
  * [H][W]; a NULL grid switches its term off. */
+/* nms_recursive: suppressed flags of hypotheses sorted by descending score;
+ * 2 when they are not sorted. */
+int orc_nms_recursive(int n, const float *x, const float *y, const float *scale,
+                      const float *score, double train_object_width,
+                      double train_object_height, int *nms);
+
 int orc_dpm_score(const orc_exp *e, int P, int root, float torso_weight, const float *torso,
                   float head_weight, int head_part, const float *head, float unary_weight,
                   int unary_rot, const float *unary, const int *is_detect, float *lu, int S,

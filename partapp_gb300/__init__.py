@@ -53,6 +53,7 @@ EXPORTS = (
     "pa_unary_net_create", "pa_unary_net_destroy", "pa_unary_net_get_params",
     "pa_unary_net_set_params", "pa_unary_net_forward", "pa_unary_net_backward",
     "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries", "pa_add_dpm_scores",
+    "pa_nms_recursive",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
@@ -184,6 +185,7 @@ def load_library():
                                     P(dp), ip, ip, ip, vp, P(PsOutputs), ip]
     L.pa_add_extra_unaries.argtypes = [vp, P(ExpParam), P(ExtraUnary), ip, ip, vp, ip, ip, ip]
     L.pa_add_dpm_scores.argtypes = [vp, P(ExpParam), P(DpmTerms), ip, ip, vp, ip, ip, ip]
+    L.pa_nms_recursive.argtypes = [vp, ip, vp, vp, vp, vp, dp, dp, vp, ip]
     L.pa_unary_net_create.argtypes = [vp, ip, ip, C.c_uint64, P(vp)]
     L.pa_unary_net_destroy.argtypes = [vp, vp]
     L.pa_unary_net_get_params.argtypes = [vp, vp, vp, P(C.c_int64)]
@@ -621,6 +623,27 @@ class Context:
         if u.mem == PA_MEM_HOST and u.arr is not log_unary:
             np.copyto(log_unary, u.arr)
         return log_unary
+
+    def nms_recursive(self, x, y, scale, score, train_object_width, train_object_height):
+        """nms_recursive over hypotheses sorted by descending score (numpy
+        arrays or CUDA tensors, all alike): suppressed flags, bool [n] (int32
+        CUDA tensor for tensor input)."""
+        bufs = [_Buf(v, np.float32) for v in (x, y, scale, score)]
+        n = int(bufs[0].arr.shape[0])
+        if any(int(b.arr.shape[0]) != n or b.mem != bufs[0].mem for b in bufs):
+            raise ValueError("x, y, scale and score must have one length and one place")
+        if bufs[0].mem == PA_MEM_DEVICE:
+            import torch
+
+            out = torch.zeros(n, dtype=torch.int32, device=x.device)
+            ptr = out.data_ptr()
+        else:
+            out = np.zeros(n, np.int32)
+            ptr = out.ctypes.data
+        self._check(self.L.pa_nms_recursive(self.h, n, *[b.ptr for b in bufs],
+                                            float(train_object_width), float(train_object_height),
+                                            ptr, bufs[0].mem))
+        return out if bufs[0].mem == PA_MEM_DEVICE else out.astype(bool)
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,
                                    want_marg=True, is_sparse=False):

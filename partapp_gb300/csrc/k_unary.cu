@@ -423,4 +423,55 @@ cudaError_t launch_dpm_score(const DpmTerms &dt, float *lu, int P, int S, int R,
   return cudaGetLastError();
 }
 
+// nms_recursive (libPictStruct/objectdetect_aux.cpp:407-451): hypothesis j is
+// suppressed when some earlier (higher-scored) hypothesis i lies inside i's
+// ellipse, dx^2 / e1_i + dy^2 / e2_i < 1 with e1_i = (ellipse * scale_i *
+// width)^2; whether i is itself suppressed does not matter, so every j is
+// independent.  dx is the float difference of the float coordinates, widened;
+// the rest is double, each operation rounded on its own (no fused multiply-add).
+// A thread per j, the earlier hypotheses staged through shared memory in
+// tiles.  err bit 1: scores not in descending order (the reference asserts).
+constexpr int kNmsTile = 256;
+__global__ void __launch_bounds__(kNmsTile) k_nms(const float *__restrict__ x, const float *__restrict__ y,
+                                                 const float *__restrict__ scale, const float *__restrict__ score,
+                                                 int n, double ew, double eh, int *__restrict__ out,
+                                                 int *__restrict__ err) {
+  __shared__ float sx[kNmsTile], sy[kNmsTile];
+  __shared__ double se1[kNmsTile], se2[kNmsTile];
+  const int j = blockIdx.x * kNmsTile + threadIdx.x;
+  const bool live = j < n;
+  const float xj = live ? x[j] : 0.f, yj = live ? y[j] : 0.f;
+  if (live && j + 1 < n && score[j] < score[j + 1]) atomicOr(err, 1);
+  bool sup = false;
+  const int i_end = min(n, (int)(blockIdx.x + 1) * kNmsTile);  // the block's last j + 1
+  for (int t0 = 0; t0 < i_end; t0 += kNmsTile) {
+    __syncthreads();
+    const int i = t0 + threadIdx.x;
+    if (i < n) {
+      sx[threadIdx.x] = x[i];
+      sy[threadIdx.x] = y[i];
+      const double sc = (double)scale[i];
+      const double a = __dmul_rn(__dmul_rn(0.5, sc), ew), b = __dmul_rn(__dmul_rn(0.5, sc), eh);
+      se1[threadIdx.x] = __dmul_rn(a, a);
+      se2[threadIdx.x] = __dmul_rn(b, b);
+    }
+    __syncthreads();
+    const int m = min(kNmsTile, j - t0);  // earlier hypotheses of this tile
+    for (int k = 0; k < m && !sup; ++k) {
+      const double dx = (double)__fsub_rn(sx[k], xj), dy = (double)__fsub_rn(sy[k], yj);
+      const double q = __dadd_rn(__ddiv_rn(__dmul_rn(dx, dx), se1[k]), __ddiv_rn(__dmul_rn(dy, dy), se2[k]));
+      sup = q < 1.0;
+    }
+  }
+  if (live) out[j] = sup ? 1 : 0;
+}
+
+cudaError_t launch_nms(const float *x, const float *y, const float *scale, const float *score, int n,
+                       double train_w, double train_h, int *out, int *err, cudaStream_t s) {
+  if (n < 1) return cudaSuccess;
+  k_nms<<<(n + kNmsTile - 1) / kNmsTile, kNmsTile, 0, s>>>(x, y, scale, score, n, train_w, train_h,
+                                                          out, err);
+  return cudaGetLastError();
+}
+
 }  // namespace pa

@@ -3516,6 +3516,58 @@ pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_te
   return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
+pa_status pa_nms_recursive(pa_ctx *ctx, int n, const float *x, const float *y, const float *scale,
+                           const float *score, double train_object_width,
+                           double train_object_height, int *suppressed, int mem) try {
+  if (!ctx) return PA_ERR_INVALID;
+  if (n < 0 || n > (1 << 26) || (n > 0 && (!x || !y || !scale || !score || !suppressed)) ||
+      !(train_object_width > 0) || !(train_object_height > 0))
+    return fail(ctx, PA_ERR_INVALID, "invalid hypothesis count, sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  if (n == 0) return PA_OK;
+  DeviceGuard dg(ctx->device);
+  Builder b1;
+  b1.scratch<int>(1);
+  if (mem == PA_MEM_HOST) {
+    b1.scratch<float>((size_t)4 * n);
+    b1.scratch<int>(n);
+  }
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  b.base = ctx->arena;
+  int *err = b.scratch<int>(1);
+  cudaStream_t s = ctx->stream;
+  const float *dx = x, *dy = y, *ds = scale, *dsc = score;
+  int *dout = suppressed;
+  if (mem == PA_MEM_HOST) {
+    float *h = b.scratch<float>((size_t)4 * n);
+    dout = b.scratch<int>(n);
+    const float *src[4] = {x, y, scale, score};
+    for (int k = 0; k < 4; ++k)
+      PA_CK(cudaMemcpyAsync(h + (size_t)k * n, src[k], (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    dx = h;
+    dy = h + n;
+    ds = h + 2 * (size_t)n;
+    dsc = h + 3 * (size_t)n;
+  }
+  PA_CK(cudaMemsetAsync(err, 0, sizeof(int), s));
+  PA_LAUNCH("nms", launch_nms(dx, dy, ds, dsc, n, train_object_width, train_object_height, dout, err, s));
+  int flag = 0;
+  PA_CK(cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(suppressed, dout, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  if (pa_status ss = sync_ctx(ctx)) return ss;
+  if (flag) return fail(ctx, PA_ERR_INVALID, "unsorted hypothesis vector");
+  return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
+}
+
 // ------------------------------------------------------------------------
 // Learned unary
 // ------------------------------------------------------------------------

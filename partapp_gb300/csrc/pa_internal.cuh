@@ -307,6 +307,8 @@ struct DpmTerms {
 };
 cudaError_t launch_dpm_score(const DpmTerms &dt, float *lu, int P, int S, int R, int H, int W,
                              cudaStream_t s);
+cudaError_t launch_nms(const float *x, const float *y, const float *scale, const float *score, int n,
+                       double train_w, double train_h, int *out, int *err, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Learned unary: convolutions on the tensor cores (k_conv.cu).

@@ -1,0 +1,79 @@
+"""Hypothesis suppression, nms_recursive (libPictStruct/objectdetect_aux.cpp:
+407-451), as saveRecoResults runs it on an image's merged root hypotheses.
+
+The oracle (oracle/oracle.cpp, orc_nms_recursive) restates the double loop
+with the reference's typing; it is pinned by hand-made cases (a hypothesis on
+top of a better one is suppressed, one just outside the ellipse is not, the
+ellipse's axes scale with the earlier hypothesis' scale, a suppressed
+hypothesis still suppresses later ones).  The GPU flags must equal the
+oracle's exactly, for ragged counts and coordinates placed on the ellipse's
+edge.
+"""
+import numpy as np
+import pytest
+
+import oracle as orc_mod
+
+
+@pytest.fixture(scope="module")
+def orc():
+    orc_mod.build()
+    return orc_mod
+
+
+def test_pins(orc):
+    # train box 20 x 50: the ellipse of a scale-1 hypothesis has half axes 10, 25
+    x = [100.0, 105.0, 109.9, 100.0, 300.0, 300.0, 318.0]
+    y = [100.0, 100.0, 100.0, 124.9, 100.0, 100.0, 100.0]
+    s = [1.0, 1.0, 1.0, 1.0, 2.0, 1.0, 1.0]
+    sc = [9.0, 8.0, 7.0, 6.0, 5.0, 4.0, 3.0]
+    got = orc.nms_recursive(x, y, s, sc, 20.0, 50.0)
+    # 1: inside 0's ellipse; 2: x 9.9 < 10; 3: y 24.9 < 25; 5: on 4; 6: 18 < 20 (4 has scale 2)
+    assert got.tolist() == [False, True, True, True, False, True, True]
+    got = orc.nms_recursive([0.0, 10.0, 20.0], [0.0] * 3, [1.0] * 3, [3.0, 2.0, 1.0], 20.0, 50.0)
+    assert got.tolist() == [False, False, False]  # exactly on the edge: 1.0 is not < 1
+    got = orc.nms_recursive([0.0, 6.0, 12.0], [0.0] * 3, [1.0] * 3, [3.0, 2.0, 1.0], 20.0, 50.0)
+    assert got.tolist() == [False, True, True]  # 2 is suppressed by 1, itself suppressed
+    with pytest.raises(ValueError):
+        orc.nms_recursive([0.0, 1.0], [0.0, 0.0], [1.0, 1.0], [1.0, 2.0], 20.0, 50.0)
+    assert orc.nms_recursive([], [], [], [], 20.0, 50.0).shape == (0,)
+
+
+def _case(rng, n):
+    x = rng.uniform(0, 640, n).astype(np.float32)
+    y = rng.uniform(0, 480, n).astype(np.float32)
+    s = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    sc = np.sort(rng.normal(0, 5, n).astype(np.float32))[::-1].copy()
+    sc[n // 3: n // 3 + 5] = sc[n // 3]  # ties are sorted too
+    # some pairs on the edge of the earlier one's ellipse
+    for k in range(1, n, 7):
+        x[k] = np.float32(x[k - 1] + np.float32(0.5 * s[k - 1] * 25.0))
+        y[k] = y[k - 1]
+    return x, y, s, sc
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 2, 255, 256, 257, 3001])
+def test_gpu_matches_oracle(orc, n):
+    import torch
+
+    import partapp_gb300 as pa
+    from partapp_gb300 import build
+
+    build.build()
+    x, y, s, sc = _case(np.random.default_rng(n), n)
+    want = orc.nms_recursive(x, y, s, sc, 25.0, 62.5)
+    ctx = pa.Context(0)
+    try:
+        got = ctx.nms_recursive(x, y, s, sc, 25.0, 62.5)
+        dev = ctx.nms_recursive(*[torch.from_numpy(v).cuda() for v in (x, y, s, sc)], 25.0, 62.5)
+        assert np.array_equal(got, want)
+        assert np.array_equal(dev.cpu().numpy().astype(bool), want)
+        if n > 1:
+            bad = sc.copy()
+            bad[n - 1] = bad[0] + 1.0
+            with pytest.raises(pa.PaError):
+                ctx.nms_recursive(x, y, s, bad, 25.0, 62.5)
+        assert ctx.nms_recursive(x[:0], y[:0], s[:0], sc[:0], 25.0, 62.5).shape == (0,)
+    finally:
+        ctx.close()
