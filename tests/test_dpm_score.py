@@ -167,3 +167,28 @@ def test_cli_adds_the_dpm_grids(tmp_path):
     assert np.array_equal(got, want["best_conf"])
     lz = np.loadtxt(tmp_path / "log_z_0.txt", dtype=np.float64)
     assert np.array_equal(lz, np.asarray(want["log_z"], dtype=np.float64))
+
+
+@pytest.mark.gpu
+def test_invalid_arguments_are_errors():
+    import partapp_gb300 as pa
+    from partapp_gb300 import build
+
+    build.build()
+    u = np.zeros((3, 4, 5, 6), np.float32)
+    g = np.ones((5, 6), np.float32)
+    ctx = pa.Context(0)
+    try:
+        pe = pa.exp_param(R=4)
+        for kw in (dict(head=(1.0, 3, g)), dict(head=(1.0, -1, g))):
+            with pytest.raises(pa.PaError):
+                ctx.add_dpm_scores(pe, u, 0, **kw)
+        with pytest.raises(pa.PaError):
+            ctx.add_dpm_scores(pe, u, 3, torso=(1.0, g))
+        with pytest.raises(ValueError):
+            ctx.add_dpm_scores(pe, u, 0, unary=(1.0, np.ones((3, 2, 5, 6), np.float32)))
+        assert np.all(u == 0.0)  # nothing written by a refused call
+        ctx.add_dpm_scores(pe, u, 0, torso=(1.0, g))  # the context still works
+        assert np.all(u == 0.0)
+    finally:
+        ctx.close()

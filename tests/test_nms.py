@@ -77,3 +77,22 @@ def test_gpu_matches_oracle(orc, n):
         assert ctx.nms_recursive(x[:0], y[:0], s[:0], sc[:0], 25.0, 62.5).shape == (0,)
     finally:
         ctx.close()
+
+
+@pytest.mark.gpu
+def test_invalid_arguments_are_errors():
+    import partapp_gb300 as pa
+    from partapp_gb300 import build
+
+    build.build()
+    v = np.zeros(4, np.float32)
+    ctx = pa.Context(0)
+    try:
+        for w, h in ((0.0, 50.0), (20.0, -1.0), (float("nan"), 50.0)):
+            with pytest.raises(pa.PaError):
+                ctx.nms_recursive(v, v, v + 1, v, w, h)
+        with pytest.raises(ValueError):
+            ctx.nms_recursive(v, v[:3], v, v, 20.0, 50.0)
+        assert ctx.nms_recursive(v, v, v + 1, v, 20.0, 50.0).tolist() == [False, True, True, True]
+    finally:
+        ctx.close()
