@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--train-fields", type=int, default=20000)
     ap.add_argument("--eval-fields", type=int, default=2000)
     ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--agreement", type=int, default=112,
+                    help="find_obj: full-size images whose argmax is compared with the oracle "
+                         "(0: skip)")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1234)
     return ap.parse_args()
@@ -224,6 +227,67 @@ def cpu_baseline_run(models, trees, desc0, n_threads):
     return n_threads / dt, dt
 
 
+def argmax_agreement(ctx, e, cls, models, args, dev):
+    """Argmax (rotation, x, y) of every part, GPU against the FP32 oracle,
+    over `args.agreement` full-size images of the workload, each with its own
+    tree.  The GPU runs pa_find_obj_batch and keeps the score grids; the
+    oracle maps the tree's grids to log unaries and runs its PS on every host
+    thread.  The score grids themselves are checked bit for bit against the
+    oracle's AdaBoost on one rotation field of every chunk."""
+    import concurrent.futures as cf
+
+    import torch
+
+    import oracle
+    from partapp_gb300 import synth
+
+    oracle.build()
+    n_img = args.agreement
+    n_thr = args.cpu_threads or os.cpu_count() or 1
+    chunk = max(4, n_thr)
+    oe = oracle.make_exp(R=R, sparse=True)
+    Tig = synth.grid_to_image(STRIDE)
+    trees = make_trees(args.seed + 31337, n_img)
+    same_img = same_part = 0
+    scores_exact, gaps = True, []
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=n_thr) as pool:
+        for c0 in range(0, n_img, chunk):
+            idx = list(range(c0, min(n_img, c0 + chunk)))
+            got, grids = [], []
+            for b0 in range(0, len(idx), args.batch):
+                ib = idx[b0:b0 + args.batch]
+                desc = device_descriptors(len(ib), args.seed + 104729 + 13 * ib[0], dev)
+                sc = torch.empty((N_CLS, len(ib) * R, NY, NX), dtype=torch.float32, device=dev)
+                got += ctx.find_obj_batch(e, [trees[i] for i in ib], cls, desc, Tig, H, W,
+                                          scores_out=sc)
+                sch = sc[:P].cpu().numpy().reshape(P, len(ib), R, NY, NX)
+                grids += [np.ascontiguousarray(sch[:, j]) for j in range(len(ib))]
+                if b0 == 0:  # one rotation field of the chunk, all 22 classifiers
+                    f0 = desc[0, 0:1].cpu().numpy()
+                    chk = sc[:, 0].cpu().numpy()
+                    futs = [pool.submit(oracle.adaboost_eval, models["f"][c], models["p"][c],
+                                        models["theta"][c], models["alpha"][c], f0)
+                            for c in range(N_CLS)]
+                    for c, f in enumerate(futs):
+                        scores_exact = scores_exact and np.array_equal(chk[c], f.result()[0])
+                del desc, sc
+            want = oracle.ps_from_scores_batch(oe, [trees[i] for i in idx], grids, Tig, H, W,
+                                               True, n_thr)
+            for j, i in enumerate(idx):
+                g, w = got[j]["best_conf"], want[j]
+                ok = [tuple(g[p, [2, 4, 5]]) == tuple(w[p, [2, 4, 5]]) for p in range(P)]
+                same_part += sum(ok)
+                same_img += all(ok)
+                gaps += [abs(float(g[p, 6]) - float(w[p, 6])) for p in range(P) if not ok[p]]
+    return {"images": n_img, "reference": "FP32 oracle (PS from the GPU's score grids)",
+            "identical_argmax_images": same_img / n_img,
+            "identical_argmax_parts": same_part / (n_img * P),
+            "score_gap_of_differing_parts_max": max(gaps) if gaps else 0.0,
+            "score_grids_bit_exact_sampled": bool(scores_exact),
+            "host_threads": n_thr, "seconds": time.perf_counter() - t0}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -350,37 +414,46 @@ def run_ours(args):
         step_e2e()
     torch.cuda.synchronize(dev)
     e2e_steps = max(2, args.steps // 2)
-    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for _ in range(e2e_steps):
-        r = step_e2e()
-    t1.record(stream)
-    torch.cuda.synchronize(dev)
-    e2e_ms = replicas.max_over_ranks(t0.elapsed_time(t1), dist, dev)
-    e2e_val = replicas.throughput(replicas.sum_over_ranks(Be * e2e_steps, dist, dev), e2e_ms)
     h2d = Be * R * NY * NX * D * 4
     d2h = Be * P * (7 * 4 + 8) + Be * 2 * (P - 1) * 8
-    # the host->device copy ceiling of this machine right after the timed e2e
-    # region: the same step's descriptor bytes from the same pinned buffer,
-    # copied alone (the host link is shared with other tenants, so the rate
-    # is measured here rather than assumed)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     scratch = torch.empty_like(desc[0])
-    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    c0.record(stream)
-    for i in range(Be):
-        scratch.copy_(host[i], non_blocking=True)
-    c1.record(stream)
-    torch.cuda.synchronize(dev)
-    copy_ms = c0.elapsed_time(c1)
-    h2d_gbs = h2d / (copy_ms / 1e3) / 1e9
+    # Three repetitions of: the timed host-buffer calls; right after them the
+    # same step's descriptor bytes copied alone from the same pinned buffer
+    # (the host link is shared with other tenants, so its rate is measured
+    # here rather than assumed); the compute side of a call (the same images,
+    # one per call, from HBM).  The e2e value is the median repetition.
+    reps = []
+    for _ in range(3):
+        t0.record(stream)
+        for _ in range(e2e_steps):
+            r = step_e2e()
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        call_ms = replicas.max_over_ranks(t0.elapsed_time(t1), dist, dev)
+        t0.record(stream)
+        for i in range(Be):
+            scratch.copy_(host[i], non_blocking=True)
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        copy_ms = t0.elapsed_time(t1)
+        t0.record(stream)
+        for i in range(Be):
+            ctx.find_obj_batch(e, trees[i:i + 1], cls, desc[i % B:i % B + 1], Tig, H, W)
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        reps.append((call_ms, copy_ms, t0.elapsed_time(t1)))
     del scratch
-    # and the compute side of a call: the same images, one per call, from HBM
-    c0.record(stream)
-    for i in range(Be):
-        ctx.find_obj_batch(e, trees[i:i + 1], cls, desc[i % B:i % B + 1], Tig, H, W)
-    c1.record(stream)
-    torch.cuda.synchronize(dev)
-    compute_ms = c0.elapsed_time(c1)
+    call_ms, copy_ms, compute_ms = sorted(reps)[1]
+    e2e_ms = call_ms
+    e2e_val = replicas.throughput(replicas.sum_over_ranks(Be * e2e_steps, dist, dev), e2e_ms)
+    h2d_gbs = h2d / (copy_ms / 1e3) / 1e9
+    e2e_reps = {}
+    for k, (a, b_, c_) in enumerate(reps):
+        e2e_reps[f"rep{k}_call_ms"] = a / e2e_steps
+        e2e_reps[f"rep{k}_copies_alone_ms"] = b_
+        e2e_reps[f"rep{k}_compute_alone_ms"] = c_
+        e2e_reps[f"rep{k}_call_over_copies"] = (a / e2e_steps) / b_
 
     lvp = None
     if rank == 0 and args.learned and world == 1:
@@ -394,6 +467,10 @@ def run_ours(args):
         cpu = {"value": v, "unit": "images/s", "cores": n_thr, "kind": "port",
                "sample": f"{n_thr} images, one per host thread ({dt:.1f} s), oracle port of the "
                          f"reference CPU path on this workload"}
+
+    agree = None
+    if rank == 0 and args.agreement > 0 and world == 1:
+        agree = argmax_agreement(ctx, e, cls, models, args, dev)
 
     if rank == 0:
         best = res[0]["best_conf"]
@@ -409,10 +486,11 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h, "images_per_step": Be,
                     "h2d_gbs_measured": h2d_gbs,
                     "copy_bound_images_per_s": h2d_gbs * 1e9 / (h2d / Be),
-                    "breakdown_ms": {"call": e2e_ms / e2e_steps, "host_to_device_copies": copy_ms,
-                                     "compute_one_image_per_call": compute_ms}},
+                    "call_ms": e2e_ms / e2e_steps, "copies_alone_ms": copy_ms,
+                    "compute_alone_ms": compute_ms, **e2e_reps},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches, "kernels": kernels, "learned_vs_plain": lvp,
+            "argmax_agreement": agree,
             "sample_best_conf_part0": [float(x) for x in best[0]],
         }
         print(json.dumps(line), flush=True)

@@ -327,9 +327,11 @@ pa_status pa_rot_joint_marginal(pa_ctx *ctx, const pa_exp_param *ep, const float
  * 1024 spatial taps per axis; larger sizes return PA_ERR_NOMEM.  C must be
  * diagonal (PA_ERR_UNSUPPORTED otherwise: the rotated-grid path of a full
  * covariance needs scratch sized by the rotation).
- * Calls share the array: calls whose GPU work overlaps race.  The first call
- * on a device looks up the array's address; make it before any stream
- * capture. */
+ * Calls share the array: calls whose GPU work overlaps race.  Every call
+ * looks up the array's address on the current device (so it stays right
+ * after a cudaDeviceReset); child and parent must be memory of that device
+ * (PA_ERR_INVALID otherwise).  The first call on a device may load the
+ * library's module there: make it before any stream capture. */
 #define PA_NOALLOC_MAX_CELLS 2097152
 pa_status pa_rot_joint_marginal_noalloc(const pa_exp_param *ep, const float *child,
                                         float *parent, int R, int H, int W,
@@ -450,6 +452,8 @@ pa_status pa_add_extra_unaries(pa_ctx *ctx, const pa_exp_param *ep, const pa_ext
  * Grids hold the raw (not logged) scores loadDPMScoreGrid (:550-576) reads:
  * torso and head [H][W], unary [n_parts][unary_rot ? R : 1][H][W].  A NULL
  * grid switches its term off.  `mem` tells where log_unary and the grids lie.
+ * A torso score below 0 (or NaN) is PA_ERR_INVALID, as computeLogGrid asserts
+ * data >= 0; log_unary is then undefined.
  *   log_unary [n_parts][S][R][H][W] (S = num_scale_steps), updated in place */
 typedef struct {
   float torso_weight;          /* dpm_torso_weight */
@@ -475,7 +479,11 @@ pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_te
  * e1 = (0.5 * scale_i * train_object_width)^2, e2 likewise with the height
  * (the differences in float, the rest in double, as the reference types it).
  * Scores out of descending order are PA_ERR_INVALID (the reference asserts).
- * `mem` tells where the five arrays lie; n = 0 is a no-op. */
+ * `mem` tells where the five arrays lie; n = 0 is a no-op.  The pair test is
+ * O(n^2) double divisions, so n is capped at PA_NMS_MAX_HYPS (the reference
+ * runs it on one image's root hypotheses, a few hundred); larger n is
+ * PA_ERR_INVALID. */
+#define PA_NMS_MAX_HYPS 65536
 pa_status pa_nms_recursive(pa_ctx *ctx, int n, const float *x, const float *y, const float *scale,
                            const float *score, double train_object_width,
                            double train_object_height, int *suppressed, int mem);

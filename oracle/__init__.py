@@ -149,6 +149,10 @@ def _declare(L):
                                          C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, fp,
                                          C.c_int]
     L.orc_find_obj_batch_f32.restype = C.c_int
+    L.orc_ps_from_scores_batch_f32.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree), C.c_int,
+                                               C.POINTER(fp), C.c_int, C.c_int, dp, C.c_int,
+                                               C.c_int, C.c_int, fp, C.c_int]
+    L.orc_ps_from_scores_batch_f32.restype = C.c_int
 
 
 # ---------------------------------------------------------------------------
@@ -447,6 +451,28 @@ def find_obj_batch(exp: OrcExp, tree, models, descs, Tig, H, W, interpolate=True
                                       _p(best, C.c_float), int(n_threads))
     if rc:
         raise ValueError(f"orc_find_obj_batch failed: {rc}")
+    return best
+
+
+def ps_from_scores_batch(exp: OrcExp, trees, scores, Tig, H, W, interpolate=True, n_threads=1):
+    """The PS half of --find_obj for many images from their score grids:
+    scores is a list of [P][R][ny][nx] float32 arrays (the tree's parts),
+    trees one tree dict per image (one topology); returns best_conf
+    [n][P][7].  Images run on n_threads host threads."""
+    ths = [_TreeHolder(t) for t in trees]
+    arr_t = (OrcTree * len(ths))(*[t.s for t in ths])
+    sc = [np.ascontiguousarray(a, dtype=np.float32) for a in scores]
+    P, R, ny, nx = sc[0].shape
+    if any(a.shape != sc[0].shape for a in sc) or len(sc) != len(ths):
+        raise ValueError("one [P][R][ny][nx] score array per tree, all of one shape")
+    ptrs = (C.POINTER(C.c_float) * len(sc))(*[_p(a, C.c_float) for a in sc])
+    best = np.zeros((len(sc), P, 7), dtype=np.float32)
+    T = np.ascontiguousarray(Tig, dtype=np.float64).reshape(9)
+    rc = lib().orc_ps_from_scores_batch_f32(C.byref(exp), arr_t, len(sc), ptrs, ny, nx,
+                                            _p(T, C.c_double), int(interpolate), H, W,
+                                            _p(best, C.c_float), int(n_threads))
+    if rc:
+        raise ValueError(f"orc_ps_from_scores_batch failed: {rc}")
     return best
 
 

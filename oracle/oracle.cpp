@@ -1080,4 +1080,39 @@ int orc_find_obj_batch_f32(const orc_exp *e, const orc_tree *t, const orc_models
   return 0;
 }
 
+int orc_ps_from_scores_batch_f32(const orc_exp *e, const orc_tree *trees, int n_img,
+                                 const float *const *scores, int ny, int nx,
+                                 const double *Tig, int interpolate, int H, int W,
+                                 float *best_conf, int n_threads) {
+  if (n_threads < 1) n_threads = 1;
+  if (n_scales(e) != 1) return -1;
+  std::vector<int> rcs(n_img, 0);
+  std::vector<std::thread> pool;
+  for (int w = 0; w < n_threads; ++w)
+    pool.emplace_back([&, w]() {
+      for (int i = w; i < n_img; i += n_threads) {
+        const orc_tree *t = trees + i;
+        const int P = t->n_parts, R = e->num_rotation_steps;
+        const size_t HW = (size_t)H * W, N = HW * R, G = (size_t)ny * nx;
+        std::vector<float> unary((size_t)P * N);
+        for (int p = 0; p < P; ++p)
+          for (int r = 0; r < R; ++r) {
+            float *u = unary.data() + (size_t)p * N + (size_t)r * HW;
+            orc_transform_grid(scores[i] + ((size_t)p * R + r) * G, ny, nx, u, H, W, Tig,
+                               NO_CLASS_VALUE, interpolate ? 1 : 2);
+            orc_clip_log(u, (int64_t)HW);
+          }
+        orc_exp ef = *e;
+        ef.sparse_up = 1; /* findObjectImageRotJoints: bIsSparse = true */
+        rcs[i] = ps_infer<float>(&ef, t, unary.data(), H, W, nullptr,
+                                 best_conf + (size_t)i * P * 7, nullptr, nullptr, nullptr,
+                                 nullptr, nullptr);
+      }
+    });
+  for (auto &th : pool) th.join();
+  for (int rc : rcs)
+    if (rc) return rc;
+  return 0;
+}
+
 }  // extern "C"

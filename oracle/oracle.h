@@ -189,6 +189,19 @@ int orc_find_obj_batch_f32(const orc_exp *e, const orc_tree *t,
                            const double *Tig, int interpolate, int H, int W,
                            float *best_conf, int n_threads);
 
+/* The PS half of the --find_obj path from given score grids, for many
+ * images with their own trees (findObjectImageRotJoints after
+ * partdetect_dense, objectdetect_findrot.cpp:729-1058): scores[i] is image
+ * i's [P][R][ny][nx] normalised AdaBoost grids (the tree's P parts), mapped
+ * by Tig, clipped and logged as orc_find_obj_f32 does, then
+ * computeRootPosteriorRot with bIsSparse = true.  trees[i] is image i's
+ * tree (one topology); best_conf is [n_img][P][7].  Images are spread over
+ * n_threads threads, one image per thread at a time.  Returns 0. */
+int orc_ps_from_scores_batch_f32(const orc_exp *e, const orc_tree *trees, int n_img,
+                                 const float *const *scores, int ny, int nx,
+                                 const double *Tig, int interpolate, int H, int W,
+                                 float *best_conf, int n_threads);
+
 /* ---- SHAPEv5 shape-context descriptors (desc.cpp) ---------------------- */
 
 /* initPatchMask(21) (libKMA2/descriptor/FeatureDescriptor.cpp:118-137) and

@@ -605,6 +605,9 @@ class Context:
             return a.ctypes.data
 
         dt = DpmTerms()
+        for name, term, idx in (("torso", torso, 1), ("head", head, 2)):
+            if term is not None and tuple(term[idx].shape) != (H, W):
+                raise ValueError(f"the {name} DPM grid must be [H][W] = [{H}][{W}]")
         if torso is not None:
             dt.torso_weight, dt.torso = float(torso[0]), grid(torso[1])
         if head is not None:

@@ -93,26 +93,112 @@ __global__ void __launch_bounds__(kThreads) k_root_posterior(const float *const 
   }
 }
 
-// log(sum_i exp(x_i)) of each map, in double.  With M the map's maximum
-// (from its argmax key) every term exp(x_i - M) lies in [0, 1]; each thread
-// keeps a compensated (Kahan) float sum of its terms, blocks and maps are
-// combined in double in a fixed order, so the result is deterministic.
+// ---------------------------------------------------------------------------
+// Log-partition log(sum_i exp(x_i)) of each map, accurate to double.
+//
+// GB300 runs FP64 at 1/64 of the FP32 rate, so one double operation per cell
+// would cost more than the rest of the reduction; the sum is carried in
+// float-float arithmetic instead (value = hi + lo, about 48 significant
+// bits; Knuth's TwoSum and the FMA TwoProduct as error-free transforms,
+// Dekker's double-length addition and multiplication), and the per-block
+// partials are combined in double.
+//
+// Each term t = exp(x - M) with M the map's maximum (from its argmax key):
+//   y = x - M exactly as the float-float (s, e) (TwoSum),
+//   n = round(64 s), r = (s - n/64) + e with |r| <= 1/128 (s - n/64 is exact
+//       by Sterbenz's lemma), renormalised,
+//   t = T[n] * (1 + p),  p = r + r^2/2 + r^3/6 + r^4/24 + r^5/120,
+// where T[n] = exp(n/64) for n in [-kExpTabN, 0] comes from the table kernel
+// (FP64 exp rounded to float-float).  The dropped Taylor terms are below
+// 3e-16 of t and the float-rounded r^3.. terms contribute ~1e-14 of t.
+// Cells with y <= -kExpTabN/64 take expf (their whole sum is below
+// N * exp(-36), so its 1e-7 relative error is negligible).  Thread, warp and
+// block orders are fixed, so the result is deterministic.
+// ---------------------------------------------------------------------------
+constexpr int kExpTabN = 36 * 64;  // T[n], n in [-kExpTabN, 0]
+
+struct ff {
+  float hi, lo;
+};
+
+// Knuth's TwoSum: a + b = s + e exactly.
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+// |a| >= |b|: a + b = s + e exactly.
+__device__ __forceinline__ ff quick_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+// a * b = p + e exactly (FMA TwoProduct).
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = two_sum(a.hi, b.hi);
+  const ff t = two_sum(a.lo, b.lo);
+  s.lo = __fadd_rn(s.lo, t.hi);
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo = __fadd_rn(s.lo, t.lo);
+  return quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  ff p = two_prod(a.hi, b.hi);
+  p.lo = __fadd_rn(p.lo, __fadd_rn(__fmul_rn(a.hi, b.lo), __fmul_rn(a.lo, b.hi)));
+  return quick_two_sum(p.hi, p.lo);
+}
+
+// tab[k] = exp(-k / 64) as float-float, k = 0..kExpTabN.
+__global__ void k_exp_table(float2 *__restrict__ tab) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > kExpTabN) return;
+  const double v = exp(-(double)k / 64.0);
+  const float hi = __double2float_rn(v);
+  tab[k] = make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
 __global__ void __launch_bounds__(kThreads) k_log_z_partial(const float *const *__restrict__ maps,
                                                             const unsigned long long *__restrict__ amax,
-                                                            int64_t N, double *__restrict__ partials) {
+                                                            int64_t N, const float2 *__restrict__ tab,
+                                                            double *__restrict__ partials) {
+  __shared__ float2 st[kExpTabN + 1];
+  for (int k = threadIdx.x; k <= kExpTabN; k += blockDim.x) st[k] = tab[k];
+  __syncthreads();
   const int map = blockIdx.y;
   const float *x = maps[map];
   const float M = ukey_decode((uint32_t)(amax[map] >> 32));
-  float s = 0.f, c = 0.f;
+  ff acc{0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const float t = expf(__fsub_rn(__ldg(x + i), M));
-    const float yk = __fsub_rn(t, c);
-    const float tt = __fadd_rn(s, yk);
-    c = __fsub_rn(__fsub_rn(tt, s), yk);
-    s = tt;
+    const float xv = __ldg(x + i);
+    const ff y = two_sum(xv, -M);  // x - M exactly
+    ff t;
+    if (y.hi > -(float)(kExpTabN / 64)) {
+      // y <= 0 since M is the maximum; the clamp only guards the table index
+      const int n = min(0, max(-kExpTabN, __float2int_rn(__fmul_rn(y.hi, 64.f))));
+      const ff r = two_sum(__fsub_rn(y.hi, __fmul_rn((float)n, 1.f / 64.f)), y.lo);
+      ff r2 = two_prod(r.hi, r.hi);
+      r2.lo = __fadd_rn(r2.lo, __fmul_rn(2.f, __fmul_rn(r.hi, r.lo)));
+      r2 = {__fmul_rn(r2.hi, 0.5f), __fmul_rn(r2.lo, 0.5f)};  // r^2 / 2
+      // r^3/6 + r^4/24 + r^5/120 in float
+      const float c = __fmul_rn(__fmul_rn(__fmul_rn(r.hi, r.hi), r.hi),
+                                __fadd_rn(1.f / 6.f, __fmul_rn(r.hi, __fadd_rn(1.f / 24.f,
+                                                                               __fmul_rn(r.hi, 1.f / 120.f)))));
+      ff pp = ff_add(r, r2);
+      pp = ff_add(pp, ff{c, 0.f});
+      const float2 tv = st[-n];
+      const ff T{tv.x, tv.y};
+      t = ff_add(T, ff_mul(T, pp));
+    } else {
+      t = ff{expf(y.hi), 0.f};
+    }
+    acc = ff_add(acc, t);
   }
-  double d = (double)s - (double)c;
+  double d = (double)acc.hi + (double)acc.lo;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, o);
   __shared__ double sd[kThreads / 32];
@@ -188,10 +274,17 @@ cudaError_t launch_root_posterior(const float *const *post_root, float *const *r
   return cudaGetLastError();
 }
 
+size_t log_z_scratch_bytes(int n_maps) {
+  return (size_t)n_maps * kLogZBlocks * sizeof(double) + (size_t)(kExpTabN + 1) * sizeof(float2);
+}
+
 cudaError_t launch_log_z(const float *const *maps, const unsigned long long *amax, int n_maps,
-                         int64_t N, double *partials, double *log_z, cudaStream_t s) {
+                         int64_t N, void *scratch, double *log_z, cudaStream_t s) {
+  double *partials = static_cast<double *>(scratch);
+  float2 *tab = reinterpret_cast<float2 *>(partials + (size_t)n_maps * kLogZBlocks);
+  k_exp_table<<<(kExpTabN + 256) / 256, 256, 0, s>>>(tab);
   dim3 grid((unsigned)kLogZBlocks, (unsigned)n_maps);
-  k_log_z_partial<<<grid, kThreads, 0, s>>>(maps, amax, N, partials);
+  k_log_z_partial<<<grid, kThreads, 0, s>>>(maps, amax, N, tab, partials);
   k_log_z_final<<<(n_maps + 127) / 128, 128, 0, s>>>(partials, kLogZBlocks, amax, n_maps, log_z);
   return cudaGetLastError();
 }

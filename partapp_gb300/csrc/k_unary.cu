@@ -394,6 +394,10 @@ __global__ void k_dpm_score(DpmTerms dt, float *__restrict__ lu, int S, int R, i
   float torso_w = 0.f;
   if (torso) {
     const float g = dt.torso[pix];
+    if (!(g >= 0.f)) {  // computeLogGrid's domain: the call fails, the maps are undefined
+      atomicOr(dt.err, 1);
+      return;
+    }
     torso_w = __fmul_rn(dt.torso_weight, g == 0.f ? (float)-1e6 : logf(g));
   }
   const bool head = dt.head && detect && p == dt.head_part;

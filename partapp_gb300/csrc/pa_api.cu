@@ -647,7 +647,8 @@ struct PsPlan {
   int *umax = nullptr, *pmax = nullptr, *frmax = nullptr, *tmax = nullptr;  // [B][P]
   unsigned long long *amax = nullptr;                                         // [B][P]
   double *msgmax = nullptr;                                                   // [B][2(P-1)]
-  double *logz = nullptr, *logz_part = nullptr;                               // [B][P]
+  double *logz = nullptr;                                                     // [B][P]
+  void *logz_part = nullptr;  // log_z_scratch_bytes(B * P)
   int *err = nullptr;
   struct Phase {
     MsgDesc *msgs = nullptr;
@@ -736,7 +737,7 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   pl.amax = b.scratch<unsigned long long>((size_t)B * P);
   pl.msgmax = b.scratch<double>((size_t)B * 2 * std::max(1, P - 1));
   pl.logz = b.scratch<double>((size_t)B * P);
-  pl.logz_part = b.scratch<double>((size_t)B * P * kLogZBlocks);
+  pl.logz_part = b.scratch<double>((log_z_scratch_bytes(B * P) + 7) / 8);
   pl.err = b.scratch<int>(1);
 
   if (!e->use_pairwise) return;
@@ -1068,7 +1069,7 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   } else {
     PA_LAUNCH("argmax", launch_argmax(pl.marg_ptrs, B * P, pl.N, pl.amax, st));
   }
-  PA_LAUNCH_N("log_z", 2, launch_log_z(pl.marg_ptrs, pl.amax, B * P, pl.N, pl.logz_part, pl.logz, st));
+  PA_LAUNCH_N("log_z", 3, launch_log_z(pl.marg_ptrs, pl.amax, B * P, pl.N, pl.logz_part, pl.logz, st));
   if (pl.want_part_hyps) {
     const int first = pl.hyp_img >= 0 ? pl.hyp_img * P : 0;
     const int n_maps = pl.hyp_img >= 0 ? P : B * P;
@@ -3467,6 +3468,7 @@ pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_te
     for (int p = 0; p < n_parts; ++p) det[p] = dt->is_detect[p] ? 1 : 0;
   Builder b1;
   b1.param(det.data(), det.size());
+  b1.scratch<int>(1);
   if (mem == PA_MEM_HOST) {
     b1.scratch<float>(n);
     b1.scratch<float>(n_torso + n_head + n_unary);
@@ -3486,6 +3488,7 @@ pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_te
   d.unary_weight = dt->unary_weight;
   d.log_floor = std::log(1e-4);
   d.is_detect = b.param(det.data(), det.size());
+  d.err = b.scratch<int>(1);
   float *lu = log_unary, *grids = nullptr;
   if (mem == PA_MEM_HOST) {
     lu = b.scratch<float>(n);
@@ -3507,9 +3510,15 @@ pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_te
     d.head = dt->head;
     d.unary = dt->unary;
   }
+  PA_CK(cudaMemsetAsync(d.err, 0, sizeof(int), ctx->stream));
   PA_LAUNCH("dpm_score", launch_dpm_score(d, lu, n_parts, S, R, H, W, ctx->stream));
+  int flag = 0;
+  PA_CK(cudaMemcpyAsync(&flag, d.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (mem == PA_MEM_HOST) PA_CK(cudaMemcpyAsync(log_unary, lu, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  return sync_ctx(ctx);
+  if (pa_status ss = sync_ctx(ctx)) return ss;
+  // computeLogGrid asserts data >= 0 (multi_array_op.hpp:154-167)
+  if (flag) return fail(ctx, PA_ERR_INVALID, "negative or NaN torso DPM score");
+  return PA_OK;
 } catch (const std::bad_alloc &) {
   return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
 } catch (const std::exception &exc) {
@@ -3520,7 +3529,7 @@ pa_status pa_nms_recursive(pa_ctx *ctx, int n, const float *x, const float *y, c
                            const float *score, double train_object_width,
                            double train_object_height, int *suppressed, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
-  if (n < 0 || n > (1 << 26) || (n > 0 && (!x || !y || !scale || !score || !suppressed)) ||
+  if (n < 0 || n > PA_NMS_MAX_HYPS || (n > 0 && (!x || !y || !scale || !score || !suppressed)) ||
       !(train_object_width > 0) || !(train_object_height > 0))
     return fail(ctx, PA_ERR_INVALID, "invalid hypothesis count, sizes or NULL input");
   if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");

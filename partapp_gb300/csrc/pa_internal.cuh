@@ -277,8 +277,11 @@ cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H,
                              int *n_kernels);
 cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
                           unsigned long long *amax, cudaStream_t s);
+// log Z of each map in double (float-float partial sums, FP64 total);
+// scratch holds log_z_scratch_bytes(n_maps) bytes, 16-byte aligned.
+size_t log_z_scratch_bytes(int n_maps);
 cudaError_t launch_log_z(const float *const *maps, const unsigned long long *amax, int n_maps,
-                         int64_t N, double *partials, double *log_z, cudaStream_t s);
+                         int64_t N, void *scratch, double *log_z, cudaStream_t s);
 
 // Poselet-conditioned extra unaries (k_unary.cu): the rotation score table is
 // built on the host, the position and torso terms per pixel on the device.
@@ -304,6 +307,7 @@ struct DpmTerms {
   const float *torso, *head, *unary;  // null: term off
   double log_floor;                   // log(1e-4) in double
   const int *is_detect;               // [P] or null (every part detected)
+  int *err;                           // bit 1: a torso score < 0 or NaN (log undefined)
 };
 cudaError_t launch_dpm_score(const DpmTerms &dt, float *lu, int P, int S, int R, int H, int W,
                              cudaStream_t s);

@@ -20,12 +20,14 @@
 // call, every other region is fully rewritten.  Calls whose GPU work
 // overlaps (two streams, or two host threads) race on the array.
 //
-// Set-up: the first call on a device, with that device current, takes the
-// array's device address with cudaGetSymbolAddress (the symbol's name is a
-// host-side stand-in, not a device address).  Make that first call before
-// any stream capture.
+// Set-up: every call, with the target device current, looks up the array's
+// device address with cudaGetSymbolAddress (the symbol's name is a host-side
+// stand-in, not a device address).  The lookup allocates nothing; doing it on
+// every call keeps the address right after a cudaDeviceReset, which gives the
+// device a new primary context and the array a new address.  The first call
+// on a device may load the library's module onto it, so make that first call
+// before any stream capture.
 #include <cstring>
-#include <mutex>
 
 #include "pa_internal.cuh"
 
@@ -50,33 +52,30 @@ constexpr size_t kScratchBytes = al256(kOffE2 + (size_t)PA_NOALLOC_MAX_CELLS * s
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-std::mutex g_setup_mutex;
-unsigned char *g_scratch_addr[256] = {};
-
-// Device address of g_noalloc_scratch on the current device (set up once).
+// Device address of g_noalloc_scratch on the current device.
 cudaError_t scratch_address(unsigned char **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = static_cast<unsigned char *>(p);
-  }
-  *out = g_scratch_addr[dev];
+  *out = static_cast<unsigned char *>(p);
   return cudaSuccess;
 }
 
+// True for device (or managed) memory of the current device: a buffer on
+// another GPU would be reached through peer addressing, or fault.
 bool on_device(const void *p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace

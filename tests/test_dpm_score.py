@@ -187,7 +187,15 @@ def test_invalid_arguments_are_errors():
             ctx.add_dpm_scores(pe, u, 3, torso=(1.0, g))
         with pytest.raises(ValueError):
             ctx.add_dpm_scores(pe, u, 0, unary=(1.0, np.ones((3, 2, 5, 6), np.float32)))
+        for kw in (dict(torso=(1.0, np.ones((4, 6), np.float32))),
+                   dict(head=(1.0, 1, np.ones((5, 7), np.float32)))):
+            with pytest.raises(ValueError):  # torso and head grids are [H][W]
+                ctx.add_dpm_scores(pe, u, 0, **kw)
         assert np.all(u == 0.0)  # nothing written by a refused call
+        bad = g.copy()
+        bad[2, 3] = -0.5  # computeLogGrid's domain is data >= 0
+        with pytest.raises(pa.PaError):
+            ctx.add_dpm_scores(pe, u.copy(), 0, torso=(1.0, bad))
         ctx.add_dpm_scores(pe, u, 0, torso=(1.0, g))  # the context still works
         assert np.all(u == 0.0)
     finally:

@@ -279,6 +279,27 @@ def test_ps_infer_matches_oracle(ctx, orc, R):
         assert abs(got["log_z"][p] - lz) <= 1e-3 * max(1.0, abs(lz))
 
 
+@pytest.mark.parametrize("R,H,W,case", [(24, 60, 80, "spread"), (12, 96, 128, "zeros"),
+                                        (16, 64, 96, "flat")])
+def test_log_z_is_fp64_logsumexp_of_the_device_map(ctx, R, H, W, case):
+    """The log-partition reduction on its own: log Z of every part against an
+    FP64 log-sum-exp (numpy, pairwise summation) of the same device marginal,
+    |d| <= 1e-12 * max(1, |log Z|).  "flat" keeps nearly every cell within a
+    few nats of the maximum, "zeros" plants LOG_ZERO cells."""
+    rng = np.random.default_rng(600 + R)
+    tree = small_tree(rng, R)
+    if case == "flat":
+        u = np.log(rng.uniform(0.95, 1.0, (10, R, H, W))).astype(np.float32)
+    else:
+        u = synth.random_log_unary(rng, 10, R, H, W, 0.2 if case == "zeros" else 0.0)
+    got = ctx.compute_root_posterior_rot(_pa_exp(R), tree, u)
+    for p in range(10):
+        m = np.asarray(got["log_marg"][p], dtype=np.float64)
+        M = m.max()
+        lz = M + math.log(np.exp(m - M).sum())
+        assert abs(got["log_z"][p] - lz) <= 1e-12 * max(1.0, abs(lz)), (p, got["log_z"][p], lz)
+
+
 @pytest.mark.parametrize("variant", ["flip", "upright", "strip", "no_pairwise", "interp_direct"])
 def test_ps_variants(ctx, orc, variant):
     rng = np.random.default_rng(sum(map(ord, variant)))

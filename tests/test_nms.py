@@ -93,6 +93,9 @@ def test_invalid_arguments_are_errors():
                 ctx.nms_recursive(v, v, v + 1, v, w, h)
         with pytest.raises(ValueError):
             ctx.nms_recursive(v, v[:3], v, v, 20.0, 50.0)
+        big = np.zeros(65537, np.float32)  # past the O(n^2) cap, refused before any work
+        with pytest.raises(pa.PaError):
+            ctx.nms_recursive(big, big, big + 1, big, 20.0, 50.0)
         assert ctx.nms_recursive(v, v, v + 1, v, 20.0, 50.0).tolist() == [False, True, True, True]
     finally:
         ctx.close()

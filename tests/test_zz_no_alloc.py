@@ -66,4 +66,11 @@ def test_noalloc_matches_allocating_entry_point_twice():
                                            pd(dp((1, 1))), pd(dp((1, 1))),
                                            pd(dp(np.eye(2).reshape(-1))), 0.0, 0.1, 1.0, None)
     assert st == pa.PA_ERR_NOMEM
+    # host memory is not a device buffer of the current device
+    hb = np.zeros((12, 40, 56), np.float32)
+    st = lib.pa_rot_joint_marginal_noalloc(C.byref(pa.exp_param(R=12)), hb.ctypes.data_as(C.c_void_p),
+                                           hb.ctypes.data_as(C.c_void_p), 12, 40, 56,
+                                           pd(dp((1, 1))), pd(dp((1, 1))),
+                                           pd(dp(np.eye(2).reshape(-1))), 0.0, 0.1, 1.0, None)
+    assert st == pa.PA_ERR_INVALID
     ctx.close()
