@@ -46,6 +46,13 @@
 //   --dpm_unary_dir DIR --use_dpm_unary [--dpm_unary_weight w] [--dpm_rot]
 //                                        per-part grids (per rotation)
 //
+// The joints come from joints.txt (above), or from the reference's own
+// experiment files: --part_conf FILE (PartConfig, protobuf text format) with
+// --spatial_dir DIR (joint_<child>_<parent>.mat, load_joint) and, for
+// mixtures of pairwise terms (num_joint_types > 1), --pred_dir DIR
+// (testlist_pred_pwise_imgidx_<i>.mat, clusidx_test -> joint_<c>_<p>_tidx_<t>.mat).
+// --joints_dump prints the joints as loaded (no GPU needed).
+//
 // --mat_dump FILE prints every variable of a MAT-file (name, class, dims and
 // values in MATLAB's column-major order, cells one by one).
 //
@@ -53,6 +60,7 @@
 // (best_conf) and, with --save_marginals, log_part_posterior_final_*.mat, plus
 // best_conf_<i>.txt (one PartHyp::toVect line per part), log_z_<i>.txt and
 // part_hyps_<i>.txt.
+#include <algorithm>
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -111,6 +119,50 @@ void read_joints(const std::string &path, PartConfig &pc, std::vector<Joint> &js
     if (!in) throw std::runtime_error(path + ": bad joint line");
     js.push_back(J);
   }
+}
+
+// Where the joints come from: the reference's experiment files (the part
+// configuration in protobuf text format and joint_<c>_<p>[_tidx_<t>].mat
+// under the spatial directory, mixture components from predictFactors'
+// output under --pred_dir) when --part_conf is given, else joints.txt and
+// the per-image joints_<i>.txt.
+struct JointSource {
+  std::string part_conf, spatial_dir, pred_dir;
+  PartConfigFile pcf;
+
+  void load_base(const std::string &expdir, PartConfig &pc, std::vector<Joint> &js) {
+    if (part_conf.empty()) {
+      read_joints(expdir + "/joints.txt", pc, js);
+      return;
+    }
+    if (spatial_dir.empty()) throw std::runtime_error("--part_conf needs --spatial_dir");
+    pcf = parsePartConfig(read_file(part_conf));
+    pc = partConfigOf(pcf);
+    js = loadJoints(pcf, spatial_dir);
+  }
+  std::vector<Joint> for_image(const std::string &expdir, int img,
+                               const std::vector<Joint> &base) const {
+    if (!part_conf.empty()) {
+      if (pred_dir.empty() || pcf.joints.empty() || pcf.joints[0].num_joint_types <= 1) return base;
+      return loadJoints(pcf, spatial_dir, loadJointTypes(pcf, pred_dir, img));
+    }
+    const std::string jp = expdir + "/joints_" + std::to_string(img) + ".txt";
+    if (!exists(jp)) return base;
+    PartConfig pc;
+    std::vector<Joint> js;
+    read_joints(jp, pc, js);
+    return js;
+  }
+};
+
+void dump_joints(const PartConfig &pc, const std::vector<Joint> &js) {
+  std::printf("parts %d root %d upright", pc.part_size(), pc.rootpart_idx);
+  for (int u : pc.is_upright) std::printf(" %d", u);
+  std::printf("\n");
+  for (const Joint &J : js)
+    std::printf("joint %d %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n",
+                J.child_idx, J.parent_idx, J.offset_c[0], J.offset_c[1], J.offset_p[0],
+                J.offset_p[1], J.C[0], J.C[1], J.C[2], J.C[3], J.rot_mean, J.rot_sigma);
 }
 
 // Binary 8-bit PGM (P5) -> grey levels 0..255 as float (the reference loads
@@ -213,6 +265,9 @@ void usage() {
                "                        [--dpm_torso_dir DIR --dpm_torso_weight w]\n"
                "                        [--dpm_unary_dir DIR --use_dpm_head --dpm_head_weight w\n"
                "                         --use_dpm_unary --dpm_unary_weight w --dpm_rot]\n"
+               "                        [--part_conf FILE --spatial_dir DIR [--pred_dir DIR]]\n"
+               "       partapp_find_obj --joints_dump [--expdir DIR | --part_conf FILE\n"
+               "                        --spatial_dir DIR [--pred_dir DIR]] [--first i --numimgs n]\n"
                "       partapp_find_obj --mat_dump FILE\n";
 }
 
@@ -224,7 +279,8 @@ int main(int argc, char **argv) {
   int rootidx_det = -1;
   DpmOptions dpm;
   int first = 0, numimgs = -1, batch = 1, device = 0;
-  bool find_obj = false, flip = false, save_marg = false, from_images = false;
+  bool find_obj = false, flip = false, save_marg = false, from_images = false, joints_dump = false;
+  JointSource jsrc;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
     auto next = [&]() -> std::string {
@@ -242,7 +298,10 @@ int main(int argc, char **argv) {
     else if (a == "--save_marginals") save_marg = true;
     else if (a == "--from_images") from_images = true;
     else if (a == "--scoregrid_dir") scoregrid_dir = next();
-    else if (a == "--pred_dir") pred_dir = next();
+    else if (a == "--part_conf") jsrc.part_conf = next();
+    else if (a == "--spatial_dir") jsrc.spatial_dir = next();
+    else if (a == "--joints_dump") joints_dump = true;
+    else if (a == "--pred_dir") jsrc.pred_dir = pred_dir = next();
     else if (a == "--pred_rot_weight") rot_w = (float)std::atof(next().c_str());
     else if (a == "--pred_pos_weight") pos_w = (float)std::atof(next().c_str());
     else if (a == "--torso_det_dir") torso_det_dir = next();
@@ -268,6 +327,21 @@ int main(int argc, char **argv) {
     }
     else if (a == "--help" || a == "-h") { usage(); return 0; }
     else { std::cerr << "unknown option " << a << "\n"; usage(); return 2; }
+  }
+  if (joints_dump) {
+    try {
+      PartApp app;
+      jsrc.load_base(expdir, app.m_part_conf, app.m_joints);
+      dump_joints(app.m_part_conf, app.m_joints);
+      for (int i = first; i < first + std::max(0, numimgs); ++i) {
+        std::printf("image %d\n", i);
+        dump_joints(app.m_part_conf, jsrc.for_image(expdir, i, app.m_joints));
+      }
+    } catch (const std::exception &ex) {
+      std::cerr << "partapp_find_obj: " << ex.what() << "\n";
+      return 1;
+    }
+    return 0;
   }
   if (!find_obj || expdir.empty()) {
     usage();
@@ -303,7 +377,7 @@ int main(int argc, char **argv) {
         if (!win) throw std::runtime_error("windows.txt: need one line per classifier");
         app.m_window_param.push_back(pw);
       }
-      read_joints(expdir + "/joints.txt", app.m_part_conf, app.m_joints);
+      jsrc.load_base(expdir, app.m_part_conf, app.m_joints);
       Context ctx(device);
       std::vector<std::unique_ptr<AdaBoostClassifier>> abc;
       for (int c = 0; c < n_cls; ++c) {
@@ -313,12 +387,7 @@ int main(int argc, char **argv) {
       for (int i = first; i < first + numimgs; ++i) {
         int h = 0, w = 0;
         const std::vector<float> img = read_pgm(expdir + "/img_" + std::to_string(i) + ".pgm", h, w);
-        std::vector<Joint> joints = app.m_joints;
-        const std::string jp = expdir + "/joints_" + std::to_string(i) + ".txt";
-        if (exists(jp)) {
-          PartConfig pc;
-          read_joints(jp, pc, joints);
-        }
+        const std::vector<Joint> joints = jsrc.for_image(expdir, i, app.m_joints);
         ExtraUnaryParams extra = loadExtraUnaryParams(
             i, app.m_part_conf.part_size(), app.m_part_conf.rootpart_idx, pred_dir, rot_w, pos_w,
             torso_det_dir, rootidx_det, torso_prior, torso_w);
@@ -333,7 +402,7 @@ int main(int argc, char **argv) {
       return 0;
     }
     if (!scoregrid_dir.empty()) {
-      read_joints(expdir + "/joints.txt", app.m_part_conf, app.m_joints);
+      jsrc.load_base(expdir, app.m_part_conf, app.m_joints);
       const int P = app.m_part_conf.part_size();
       Context ctx(device);
       for (int i = first; i < first + numimgs; ++i) {
@@ -342,12 +411,7 @@ int main(int argc, char **argv) {
           h = (int)need(kv, "height");
           w = (int)need(kv, "width");
         }
-        std::vector<Joint> joints = app.m_joints;
-        const std::string jp = expdir + "/joints_" + std::to_string(i) + ".txt";
-        if (exists(jp)) {
-          PartConfig pc;
-          read_joints(jp, pc, joints);
-        }
+        const std::vector<Joint> joints = jsrc.for_image(expdir, i, app.m_joints);
         std::vector<ScoreGridSet> parts;
         for (int p = 0; p < P; ++p)
           parts.push_back(loadScoreGrid(scoreGridFileName(scoregrid_dir, i, p, flip)));
@@ -374,7 +438,7 @@ int main(int argc, char **argv) {
       for (double &t : Tig) in >> t;
       if (!in) throw std::runtime_error("tig.txt: need 9 numbers");
     }
-    read_joints(expdir + "/joints.txt", app.m_part_conf, app.m_joints);
+    jsrc.load_base(expdir, app.m_part_conf, app.m_joints);
 
     Context ctx(device);
     std::vector<std::unique_ptr<AdaBoostClassifier>> abc;
@@ -394,15 +458,7 @@ int main(int argc, char **argv) {
         if (d.size() != per_img * sizeof(float))
           throw std::runtime_error("desc_" + std::to_string(img) + ".bin: wrong size");
         std::memcpy(desc.data() + per_img * b, d.data(), d.size());
-        const std::string jp = expdir + "/joints_" + std::to_string(img) + ".txt";
-        if (exists(jp)) {
-          PartConfig pc;
-          std::vector<Joint> js;
-          read_joints(jp, pc, js);
-          joints.push_back(js);
-        } else {
-          joints.push_back(app.m_joints);
-        }
+        joints.push_back(jsrc.for_image(expdir, img, app.m_joints));
       }
       const auto res =
           findObjectDataset(ctx, app, flip, joints, desc.data(), nb, ny, nx, dim, Tig, H, W, save_marg);

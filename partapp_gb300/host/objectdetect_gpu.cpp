@@ -3,6 +3,8 @@
 #include "partapp_gpu.hpp"
 
 #include <algorithm>
+#include <cctype>
+#include <fstream>
 #include <cstdio>
 #include <cstring>
 
@@ -645,6 +647,247 @@ std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_a
       }
   }
   return res;
+}
+
+// ------------------------------------------------------------------------
+// Part configuration and joints of a reference experiment
+// ------------------------------------------------------------------------
+namespace {
+
+// Tokens of the protobuf text format: names, numbers, quoted strings and the
+// punctuation : { } < > ; , (comments run from # to the end of the line).
+struct PbTokens {
+  std::vector<std::string> t;
+  size_t i = 0;
+  explicit PbTokens(const std::string &s) {
+    size_t k = 0;
+    while (k < s.size()) {
+      const char c = s[k];
+      if (std::isspace((unsigned char)c)) { ++k; continue; }
+      if (c == '#') {
+        while (k < s.size() && s[k] != '\n') ++k;
+        continue;
+      }
+      if (c == '"' || c == '\'') {
+        std::string v(1, '"');
+        ++k;
+        while (k < s.size() && s[k] != c) {
+          if (s[k] == '\\' && k + 1 < s.size()) ++k;
+          v += s[k++];
+        }
+        if (k >= s.size()) throw std::runtime_error("part configuration: unterminated string");
+        ++k;
+        t.push_back(v);
+        continue;
+      }
+      if (std::strchr(":{}<>;,[]", c)) {
+        t.emplace_back(1, c);
+        ++k;
+        continue;
+      }
+      const size_t b = k;
+      while (k < s.size() && !std::isspace((unsigned char)s[k]) && !std::strchr(":{}<>;,[]#\"'", s[k]))
+        ++k;
+      t.push_back(s.substr(b, k - b));
+    }
+  }
+  bool done() const { return i >= t.size(); }
+  const std::string &peek() const {
+    if (done()) throw std::runtime_error("part configuration: unexpected end");
+    return t[i];
+  }
+  std::string next() {
+    const std::string &v = peek();
+    ++i;
+    return v;
+  }
+  void skip_sep() {
+    while (!done() && (t[i] == ";" || t[i] == ",")) ++i;
+  }
+};
+
+bool pb_is_open(const std::string &s) { return s == "{" || s == "<"; }
+bool pb_is_close(const std::string &s) { return s == "}" || s == ">"; }
+
+// A scalar value after "name:"; a list [a, b] is read as its last element.
+std::string pb_scalar(PbTokens &tk) {
+  if (tk.peek() == "[") {
+    tk.next();
+    std::string last;
+    while (tk.peek() != "]") {
+      const std::string v = tk.next();
+      if (v != ",") last = v;
+    }
+    tk.next();
+    return last;
+  }
+  return tk.next();
+}
+
+void pb_skip_message(PbTokens &tk) {
+  int depth = 1;
+  while (depth > 0) {
+    const std::string v = tk.next();
+    if (pb_is_open(v)) ++depth;
+    else if (pb_is_close(v)) --depth;
+  }
+}
+
+int pb_int(const std::string &v) {
+  char *end = nullptr;
+  const long x = std::strtol(v.c_str(), &end, 0);
+  if (v.empty() || *end) throw std::runtime_error("part configuration: not an integer: " + v);
+  return (int)x;
+}
+
+bool pb_bool(const std::string &v) {
+  if (v == "true" || v == "True" || v == "t" || v == "1") return true;
+  if (v == "false" || v == "False" || v == "f" || v == "0") return false;
+  throw std::runtime_error("part configuration: not a boolean: " + v);
+}
+
+// Fields of one message body up to its closing brace; `on_field` gets
+// (name, scalar value) and returns false for a field it does not know.
+template <class F>
+void pb_fields(PbTokens &tk, F on_field) {
+  for (;;) {
+    tk.skip_sep();
+    if (pb_is_close(tk.peek())) {
+      tk.next();
+      return;
+    }
+    const std::string name = tk.next();
+    if (tk.peek() == ":") tk.next();
+    if (pb_is_open(tk.peek())) {  // nested message of a field we do not read
+      tk.next();
+      pb_skip_message(tk);
+      continue;
+    }
+    on_field(name, pb_scalar(tk));
+  }
+}
+
+std::string pb_string(const std::string &v) { return !v.empty() && v[0] == '"' ? v.substr(1) : v; }
+
+}  // namespace
+
+PartConfigFile parsePartConfig(const std::string &text) {
+  PbTokens tk(text);
+  PartConfigFile pc;
+  while (!tk.done()) {
+    tk.skip_sep();
+    if (tk.done()) break;
+    const std::string name = tk.next();
+    if (tk.peek() == ":") tk.next();
+    if (!pb_is_open(tk.next()))
+      throw std::runtime_error("part configuration: expected a message after " + name);
+    if (name == "part") {
+      PartConfigFile::Part p;
+      pb_fields(tk, [&](const std::string &f, const std::string &v) {
+        if (f == "part_id") p.part_id = pb_int(v);
+        else if (f == "is_root") p.is_root = pb_bool(v);
+        else if (f == "is_upright") p.is_upright = pb_bool(v);
+        else if (f == "is_detect") p.is_detect = pb_bool(v);
+      });
+      pc.parts.push_back(p);
+    } else if (name == "joint") {
+      PartConfigFile::JointDef j;
+      pb_fields(tk, [&](const std::string &f, const std::string &v) {
+        if (f == "child_idx") j.child_id = pb_int(v);
+        else if (f == "parent_idx") j.parent_id = pb_int(v);
+        else if (f == "type") j.type = pb_string(v);
+        else if (f == "num_joint_types") j.num_joint_types = pb_int(v);
+      });
+      pc.joints.push_back(j);
+    } else {
+      pb_skip_message(tk);  // app_group and anything else off this path
+    }
+  }
+  return pc;
+}
+
+PartConfig partConfigOf(const PartConfigFile &pc) {
+  PartConfig out;
+  const int P = (int)pc.parts.size();
+  if (P < 1) throw std::runtime_error("part configuration: no parts");
+  out.is_upright.assign(P, 0);
+  out.rootpart_idx = -1;
+  for (int p = 0; p < P; ++p) {
+    if (pc.parts[p].part_id != p + 1)
+      throw std::runtime_error("part configuration: part ids must be 1..n in order");
+    out.is_upright[p] = pc.parts[p].is_upright ? 1 : 0;
+    if (pc.parts[p].is_detect && pc.parts[p].is_root) {
+      if (out.rootpart_idx != -1) throw std::runtime_error("part configuration: two root parts");
+      out.rootpart_idx = p;
+    }
+  }
+  if (out.rootpart_idx < 0) throw std::runtime_error("part configuration: no detected root part");
+  return out;
+}
+
+std::vector<int> loadJointTypes(const PartConfigFile &pc, const std::string &pred_dir, int imgidx,
+                                bool is_test) {
+  const size_t J = pc.joints.size();
+  std::vector<int> tidx(J, -1);
+  if (J == 0 || pc.joints[0].num_joint_types <= 1 || imgidx < 0) return tidx;
+  const std::string list = is_test ? "test" : "train";
+  const std::string path =
+      pred_dir + "/" + list + "list_pred_pwise_imgidx_" + std::to_string(imgidx) + ".mat";
+  const std::vector<MatArray> vars = mat_read(path);
+  const MatArray &c = mat_find(vars, "clusidx_" + list);
+  if (c.numel() < J) throw std::runtime_error(path + ": clusidx_" + list + " is shorter than the joints");
+  for (size_t j = 0; j < J; ++j) tidx[j] = (int)c.re[j];
+  return tidx;
+}
+
+std::vector<Joint> loadJoints(const PartConfigFile &pc, const std::string &spatial_dir,
+                              const std::vector<int> &tidx) {
+  const int P = (int)pc.parts.size();
+  std::vector<Joint> js;
+  for (size_t j = 0; j < pc.joints.size(); ++j) {
+    const PartConfigFile::JointDef &d = pc.joints[j];
+    const int t = j < tidx.size() ? tidx[j] : -1;
+    const std::string stem =
+        spatial_dir + "/joint_" + std::to_string(d.child_id) + "_" + std::to_string(d.parent_id);
+    const std::string gen = stem + ".mat";
+    const std::string mix = t > -1 ? stem + "_tidx_" + std::to_string(t) + ".mat" : gen;
+    const bool have_mix = std::ifstream(mix).good();
+    const std::vector<MatArray> vars = mat_read(have_mix ? mix : gen);
+    auto scalar = [&](const char *name) {
+      const MatArray &a = mat_find(vars, name);
+      if (a.numel() < 1) throw std::runtime_error(gen + ": " + name + " is empty");
+      return a.re[0];
+    };
+    const int type = (int)scalar("type");
+    if ((int)scalar("child_idx") != d.child_id || (int)scalar("parent_idx") != d.parent_id)
+      throw std::runtime_error(stem + ": child_idx / parent_idx differ from the part configuration");
+    Joint J;
+    const MatArray &oc = mat_find(vars, "offset_c"), &op = mat_find(vars, "offset_p");
+    const MatArray &C = mat_find(vars, "C");
+    if (oc.numel() != 2 || op.numel() != 2) throw std::runtime_error(stem + ": offsets must have 2 entries");
+    if (C.numel() != 4 || C.dims.size() != 2 || C.dims[0] != 2)
+      throw std::runtime_error(stem + ": C must be 2 x 2");
+    for (int k = 0; k < 2; ++k) {
+      J.offset_c[k] = oc.re[k];
+      J.offset_p[k] = op.re[k];
+    }
+    for (int r = 0; r < 2; ++r)
+      for (int c = 0; c < 2; ++c) J.C[r * 2 + c] = mat_at(C, {(size_t)r, (size_t)c});
+    if (type == 2) {  // Joint::ROT_GAUSSIAN
+      if (!have_mix) throw std::runtime_error(mix + ": missing mixture component of a rotation joint");
+      J.rot_mean = scalar("rot_mean");
+      J.rot_sigma = scalar("rot_sigma");
+    } else if (type != 1) {  // Joint::POS_GAUSSIAN
+      throw std::runtime_error(stem + ": unknown joint type " + std::to_string(type));
+    }
+    J.child_idx = d.child_id - 1;
+    J.parent_idx = d.parent_id - 1;
+    if (J.child_idx < 0 || J.child_idx >= P || J.parent_idx < 0 || J.parent_idx >= P)
+      throw std::runtime_error(stem + ": part id outside the configuration");
+    js.push_back(J);
+  }
+  if ((int)js.size() != P - 1) throw std::runtime_error("part configuration: need n_parts - 1 joints");
+  return js;
 }
 
 }  // namespace partapp_gpu

@@ -239,6 +239,52 @@ ExtraUnaryParams loadExtraUnaryParams(int imgidx, int n_parts, int root, const s
                                       const std::string &torso_det_dir, int rootidx_det,
                                       const std::string &torso_prior_file, float torso_weight);
 
+// PartConfig (libPartDetect/PartConfig.proto) as the protobuf text format of
+// an experiment holds it, reduced to the fields this path reads: part ids
+// and the is_root / is_upright / is_detect flags, and the joints between
+// part ids (child_idx, parent_idx, type, num_joint_types).  Other fields are
+// skipped.
+struct PartConfigFile {
+  struct Part {
+    int part_id = 0;
+    bool is_root = false, is_upright = false, is_detect = true;
+  };
+  struct JointDef {
+    int child_id = 0, parent_id = 0;  // part ids (1-based)
+    std::string type = "Gaussian";
+    int num_joint_types = 1;
+  };
+  std::vector<Part> parts;
+  std::vector<JointDef> joints;
+};
+PartConfigFile parsePartConfig(const std::string &text);
+
+// The root index and upright flags of a part configuration; part ids must be
+// 1..P in order (loadJoints asserts part_id == pidx + 1) and exactly one
+// detected part the root (findObjectImageRotJoints, objectdetect_findrot.cpp:783-788).
+PartConfig partConfigOf(const PartConfigFile &pc);
+
+// Per-joint mixture component of image imgidx, as loadJoints takes it from
+// predictFactors' output (objectdetect_aux.cpp:73-92):
+// <pred_dir>/<list>list_pred_pwise_imgidx_<imgidx>.mat, vector "clusidx_<list>"
+// with list "test" or "train".  Used only when the configuration's first
+// joint has num_joint_types > 1; otherwise every entry is -1.
+std::vector<int> loadJointTypes(const PartConfigFile &pc, const std::string &pred_dir, int imgidx,
+                                bool is_test = true);
+
+// load_joint for every joint of the configuration (libPictStruct/
+// objectdetect_learnparam.cpp:92-180) followed by loadJoints' conversion of
+// part ids to indices (objectdetect_aux.cpp:54-141): reads
+// <spatial_dir>/joint_<child>_<parent>[_tidx_<t>].mat (the general file when
+// the mixture file is missing; a missing mixture file of a rotation joint is
+// an error, as the reference asserts), variables type, child_idx,
+// parent_idx, offset_c, offset_p, C (2 x 2) and, for ROT_GAUSSIAN (type 2),
+// rot_mean and rot_sigma.  The flip of loadJoints is not applied here: the
+// pa_* entries apply it from their flip argument.  tidx[j] < 0 (or an empty
+// vector) selects the general file.
+std::vector<Joint> loadJoints(const PartConfigFile &pc, const std::string &spatial_dir,
+                              const std::vector<int> &tidx = {});
+
 struct PartApp {
   ExpParam m_exp_param;
   PartConfig m_part_conf;

@@ -190,3 +190,156 @@ def test_cli_find_obj_from_images(tmp_path, ctx):
         ref = ctx.compute_root_posterior_rot(e, tree, lu[:10], is_sparse=True)
         got = np.loadtxt(os.path.join(d, f"best_conf_{i}.txt"), dtype=np.float64).astype(np.float32)
         assert np.array_equal(got, ref["best_conf"]), i
+
+
+# ------------------------------------------- the reference's joint files
+def write_part_conf(path, tree, n_joint_types=1):
+    """PartConfig (libPartDetect/PartConfig.proto) in protobuf text format,
+    with fields this path does not read mixed in."""
+    P = int(tree["n_parts"])
+    root = int(tree["root"])
+    with open(path, "w") as fh:
+        fh.write("# part configuration\n")
+        for p in range(P):
+            fh.write("part {\n  part_id: %d\n  part_pos: %d\n  part_pos: %d\n" % (p + 1, 2 * p, 2 * p + 1))
+            if p == root:
+                fh.write("  is_root: true\n")
+            fh.write("  is_upright: %s\n  ext_x_pos: 2.5\n}\n" %
+                     ("true" if tree["is_upright"][p] else "false"))
+        for j in range(P - 1):
+            fh.write('joint { child_idx: %d parent_idx: %d type: "RotGaussian" joint_pos: 3 '
+                     'num_joint_types: %d }\n' % (int(tree["child"][j]) + 1,
+                                                  int(tree["parent"][j]) + 1, n_joint_types))
+        fh.write("app_group { part_id: 1 part_id: 2 }\n")
+
+
+def write_joint_files(spatial, tree, suffix="", scale=1.0):
+    """joint_<child>_<parent><suffix>.mat as the reference's save_joint writes
+    them (objectdetect_learnparam.cpp:66-90): doubles, vectors as columns."""
+    sio = pytest.importorskip("scipy.io")
+    os.makedirs(spatial, exist_ok=True)
+    for j in range(int(tree["n_parts"]) - 1):
+        c, p = int(tree["child"][j]) + 1, int(tree["parent"][j]) + 1
+        sio.savemat(os.path.join(spatial, f"joint_{c}_{p}{suffix}.mat"), {
+            "type": 2.0, "child_idx": float(c), "parent_idx": float(p),
+            "offset_c": (scale * np.asarray(tree["offset_c"][j], np.float64)).reshape(2, 1),
+            "offset_p": (scale * np.asarray(tree["offset_p"][j], np.float64)).reshape(2, 1),
+            "C": np.asarray(tree["C"][j], np.float64).reshape(2, 2),
+            "rot_mean": float(tree["rot_mean"][j]), "rot_sigma": float(tree["rot_sigma"][j])})
+
+
+def parse_dump(text):
+    blocks, cur = [], None
+    for line in text.splitlines():
+        f = line.split()
+        if f[0] == "parts":
+            cur = dict(P=int(f[1]), root=int(f[3]), upright=[int(v) for v in f[5:]], joints=[])
+            blocks.append(cur)
+        elif f[0] == "joint":
+            cur["joints"].append([int(f[1]), int(f[2])] + [float(v) for v in f[3:]])
+    return blocks
+
+
+def tree_rows(tree, scale=1.0):
+    return [[int(tree["child"][j]), int(tree["parent"][j]),
+             *(scale * np.asarray(tree["offset_c"][j])), *(scale * np.asarray(tree["offset_p"][j])),
+             *tree["C"][j], tree["rot_mean"][j], tree["rot_sigma"][j]]
+            for j in range(int(tree["n_parts"]) - 1)]
+
+
+def test_joints_from_reference_files(tmp_path):
+    """load_joint (objectdetect_learnparam.cpp:92-180) + loadJoints' id ->
+    index conversion (objectdetect_aux.cpp:54-141) over scipy-written joint
+    files and a text-format part configuration."""
+    tree = synth.make_tree(np.random.default_rng(3), R=R, upright=[2, 7])
+    write_part_conf(tmp_path / "parts.txt", tree)
+    write_joint_files(str(tmp_path / "spatial"), tree)
+    r = subprocess.run([cli(), "--joints_dump", "--part_conf", str(tmp_path / "parts.txt"),
+                        "--spatial_dir", str(tmp_path / "spatial")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    (b,) = parse_dump(r.stdout)
+    assert b["P"] == 10 and b["root"] == int(tree["root"])
+    assert b["upright"] == [int(u) for u in tree["is_upright"]]
+    assert b["joints"] == tree_rows(tree)
+
+
+def test_joint_mixtures_from_prediction_files(tmp_path):
+    """num_joint_types > 1: the mixture component of each joint comes from
+    clusidx_test of testlist_pred_pwise_imgidx_<i>.mat and selects
+    joint_<c>_<p>_tidx_<t>.mat (objectdetect_aux.cpp:73-92)."""
+    sio = pytest.importorskip("scipy.io")
+    tree = synth.make_tree(np.random.default_rng(4), R=R)
+    write_part_conf(tmp_path / "parts.txt", tree, n_joint_types=3)
+    sp = str(tmp_path / "spatial")
+    write_joint_files(sp, tree)
+    for t in range(3):
+        write_joint_files(sp, tree, suffix=f"_tidx_{t}", scale=1.0 + t)
+    pred = tmp_path / "pred"
+    pred.mkdir()
+    clus = np.array([[t % 3 for t in range(9)], [2] * 9], np.float64)
+    for i in range(2):
+        sio.savemat(str(pred / f"testlist_pred_pwise_imgidx_{i}.mat"),
+                    {"clusidx_test": clus[i].reshape(9, 1)})
+    r = subprocess.run([cli(), "--joints_dump", "--part_conf", str(tmp_path / "parts.txt"),
+                        "--spatial_dir", sp, "--pred_dir", str(pred), "--first", "0",
+                        "--numimgs", "2"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    base, img0, img1 = parse_dump(r.stdout)
+    assert base["joints"] == tree_rows(tree)
+    assert img1["joints"] == tree_rows(tree, 3.0)
+    for j in range(9):
+        assert img0["joints"][j] == tree_rows(tree, 1.0 + j % 3)[j]
+
+
+def test_joint_file_errors(tmp_path):
+    """What load_joint asserts on is an error: ids that differ from the part
+    configuration, a missing joint file, a missing mixture file of a rotation
+    joint."""
+    sio = pytest.importorskip("scipy.io")
+    tree = synth.make_tree(np.random.default_rng(5), R=R)
+    write_part_conf(tmp_path / "parts.txt", tree)
+    sp = str(tmp_path / "spatial")
+    write_joint_files(sp, tree)
+    args = [cli(), "--joints_dump", "--part_conf", str(tmp_path / "parts.txt"), "--spatial_dir", sp]
+    c, p = int(tree["child"][4]) + 1, int(tree["parent"][4]) + 1
+    f = os.path.join(sp, f"joint_{c}_{p}.mat")
+    good = sio.loadmat(f)
+    good = {k: v for k, v in good.items() if not k.startswith("__")}
+    sio.savemat(f, dict(good, child_idx=float(c + 1)))
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 1 and "differ" in r.stderr
+    os.remove(f)
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr
+    sio.savemat(f, good)
+    write_part_conf(tmp_path / "parts.txt", tree, n_joint_types=2)
+    pred = tmp_path / "pred"
+    pred.mkdir()
+    sio.savemat(str(pred / "testlist_pred_pwise_imgidx_0.mat"), {"clusidx_test": np.ones((9, 1))})
+    r = subprocess.run(args + ["--pred_dir", str(pred), "--numimgs", "1"], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "mixture" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_find_obj_from_reference_joint_files(tmp_path):
+    """--part_conf / --spatial_dir give the same results as the same joints
+    in joints.txt."""
+    imgs = make_experiment(str(tmp_path), n_images=2)
+    for i in range(2):
+        os.remove(tmp_path / f"joints_{i}.txt")
+    write_part_conf(tmp_path / "parts.txt", imgs[0]["tree"])
+    write_joint_files(str(tmp_path / "spatial"), imgs[0]["tree"])
+    out_a, out_b = tmp_path / "a", tmp_path / "b"
+    out_a.mkdir()
+    out_b.mkdir()
+    base = [cli(), "--find_obj", "--expdir", str(tmp_path), "--batch", "2"]
+    r = subprocess.run(base + ["--outdir", str(out_a)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(base + ["--outdir", str(out_b), "--part_conf", str(tmp_path / "parts.txt"),
+                               "--spatial_dir", str(tmp_path / "spatial")],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    for i in range(2):
+        for name in (f"best_conf_{i}.txt", f"log_z_{i}.txt"):
+            assert (out_a / name).read_text() == (out_b / name).read_text()
