@@ -50,7 +50,11 @@ typedef struct pa_classifier pa_classifier;
 /* Creates a context on `device` with its own non-blocking stream. */
 pa_status pa_ctx_create(int device, pa_ctx **out);
 pa_status pa_ctx_destroy(pa_ctx *ctx);
-/* Makes the context issue its work on `stream` (a cudaStream_t). */
+/* Makes the context issue its work on `stream` (a cudaStream_t).  Device
+ * inputs are read, and device outputs written, in the order of this stream:
+ * inputs produced on another stream must be complete there first (set the
+ * producing stream here, or make this stream wait on an event).  Calls that
+ * return host results return after their work on the stream has finished. */
 pa_status pa_ctx_set_stream(pa_ctx *ctx, void *stream);
 pa_status pa_ctx_synchronize(pa_ctx *ctx);
 /* No counterpart in the reference.  Arithmetic of the spatial Gaussian of

@@ -298,7 +298,13 @@ class Classifier:
 
 
 class Context:
-    """A pa_ctx: one device, one stream, its own workspace."""
+    """A pa_ctx: one device, one stream, its own workspace.
+
+    The context issues its work on torch's current stream of `device` (when
+    torch with CUDA is present), so CUDA tensors produced by torch just before
+    a call are complete when the call reads them, and torch sees the outputs
+    in order; set_stream() moves it to another stream.  Without torch the
+    context keeps its own stream."""
 
     def __init__(self, device: int = 0):
         self.L = load_library()
@@ -307,6 +313,13 @@ class Context:
         if st != PA_OK:
             raise PaError(st, "pa_ctx_create failed (no CUDA device?)")
         self.h = h
+        try:
+            import torch
+
+            if torch.cuda.is_available():
+                self.set_stream(torch.cuda.current_stream(int(device)).cuda_stream)
+        except ImportError:
+            pass
 
     def close(self):
         if getattr(self, "h", None):

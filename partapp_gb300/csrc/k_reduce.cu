@@ -99,14 +99,13 @@ __global__ void __launch_bounds__(kThreads) k_root_posterior(const float *const 
 // GB300 runs FP64 at 1/64 of the FP32 rate, so one double operation per cell
 // would cost more than the rest of the reduction; the sum is carried in
 // float-float arithmetic instead (value = hi + lo, about 48 significant
-// bits; Knuth's TwoSum and the FMA TwoProduct as error-free transforms,
-// Dekker's double-length addition and multiplication), and the per-block
-// partials are combined in double.
+// bits; Knuth's TwoSum, Dekker's Fast2Sum and the FMA TwoProduct as
+// error-free transforms), and the per-block partials are combined in double.
 //
 // Each term t = exp(x - M) with M the map's maximum (from its argmax key):
 //   y = x - M exactly as the float-float (s, e) (TwoSum),
-//   n = round(64 s), r = (s - n/64) + e with |r| <= 1/128 (s - n/64 is exact
-//       by Sterbenz's lemma), renormalised,
+//   n = round(64 s) (by the 1.5 * 2^23 rounding constant), r = (s - n/64) + e
+//       with |r| <= 1/128 (s - n/64 is exact by Sterbenz's lemma), renormalised,
 //   t = T[n] * (1 + p),  p = r + r^2/2 + r^3/6 + r^4/24 + r^5/120,
 // where T[n] = exp(n/64) for n in [-kExpTabN, 0] comes from the table kernel
 // (FP64 exp rounded to float-float).  The dropped Taylor terms are below
@@ -133,25 +132,6 @@ __device__ __forceinline__ ff quick_two_sum(float a, float b) {
   const float s = __fadd_rn(a, b);
   return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
-// a * b = p + e exactly (FMA TwoProduct).
-__device__ __forceinline__ ff two_prod(float a, float b) {
-  const float p = __fmul_rn(a, b);
-  return {p, __fmaf_rn(a, b, -p)};
-}
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
-  ff s = two_sum(a.hi, b.hi);
-  const ff t = two_sum(a.lo, b.lo);
-  s.lo = __fadd_rn(s.lo, t.hi);
-  s = quick_two_sum(s.hi, s.lo);
-  s.lo = __fadd_rn(s.lo, t.lo);
-  return quick_two_sum(s.hi, s.lo);
-}
-__device__ __forceinline__ ff ff_mul(ff a, ff b) {
-  ff p = two_prod(a.hi, b.hi);
-  p.lo = __fadd_rn(p.lo, __fadd_rn(__fmul_rn(a.hi, b.lo), __fmul_rn(a.lo, b.hi)));
-  return quick_two_sum(p.hi, p.lo);
-}
-
 // tab[k] = exp(-k / 64) as float-float, k = 0..kExpTabN.
 __global__ void k_exp_table(float2 *__restrict__ tab) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,32 +151,46 @@ __global__ void __launch_bounds__(kThreads) k_log_z_partial(const float *const *
   const int map = blockIdx.y;
   const float *x = maps[map];
   const float M = ukey_decode((uint32_t)(amax[map] >> 32));
+  constexpr float kMagic = 12582912.f;  // 1.5 * 2^23: x + kMagic rounds x to an integer
   ff acc{0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const float xv = __ldg(x + i);
-    const ff y = two_sum(xv, -M);  // x - M exactly
-    ff t;
+    const ff y = two_sum(__ldg(x + i), -M);  // x - M exactly
+    float th, tl;                            // the term as th + tl
     if (y.hi > -(float)(kExpTabN / 64)) {
-      // y <= 0 since M is the maximum; the clamp only guards the table index
-      const int n = min(0, max(-kExpTabN, __float2int_rn(__fmul_rn(y.hi, 64.f))));
-      const ff r = two_sum(__fsub_rn(y.hi, __fmul_rn((float)n, 1.f / 64.f)), y.lo);
-      ff r2 = two_prod(r.hi, r.hi);
-      r2.lo = __fadd_rn(r2.lo, __fmul_rn(2.f, __fmul_rn(r.hi, r.lo)));
-      r2 = {__fmul_rn(r2.hi, 0.5f), __fmul_rn(r2.lo, 0.5f)};  // r^2 / 2
-      // r^3/6 + r^4/24 + r^5/120 in float
-      const float c = __fmul_rn(__fmul_rn(__fmul_rn(r.hi, r.hi), r.hi),
-                                __fadd_rn(1.f / 6.f, __fmul_rn(r.hi, __fadd_rn(1.f / 24.f,
-                                                                               __fmul_rn(r.hi, 1.f / 120.f)))));
-      ff pp = ff_add(r, r2);
-      pp = ff_add(pp, ff{c, 0.f});
-      const float2 tv = st[-n];
-      const ff T{tv.x, tv.y};
-      t = ff_add(T, ff_mul(T, pp));
+      // n = round(64 y.hi) in [-kExpTabN, 0] (y <= 0: M is the maximum;
+      // the clamp only guards the table index)
+      const float t = __fmaf_rn(y.hi, 64.f, kMagic);
+      const int n = min(0, max(-kExpTabN, __float_as_int(t) - __float_as_int(kMagic)));
+      const float nf = __fsub_rn(t, kMagic);
+      // r = (y.hi - n/64) + y.lo, the first difference exact (Sterbenz)
+      const ff r = two_sum(__fmaf_rn(nf, -1.f / 64.f, y.hi), y.lo);
+      // exp(r) - 1 = r + r^2/2 + c as ph + pl: r^2 = r2h + r2l exactly (FMA),
+      // c = r^3/6 + r^4/24 + r^5/120 and the cross term r.hi * r.lo in float
+      const float r2h = __fmul_rn(r.hi, r.hi);
+      const float r2l = __fmaf_rn(r.hi, r.hi, -r2h);
+      const float c = __fmul_rn(__fmul_rn(r.hi, r2h),
+                                __fmaf_rn(r.hi, __fmaf_rn(r.hi, 1.f / 120.f, 1.f / 24.f), 1.f / 6.f));
+      const float u = __fmaf_rn(r.hi, r.lo, __fmaf_rn(r2l, 0.5f, c));
+      const ff v = two_sum(__fmul_rn(r2h, 0.5f), u);  // r^2/2 + c
+      ff pp = quick_two_sum(r.hi, v.hi);               // |r| >= r^2/2 + c
+      pp.lo = __fadd_rn(pp.lo, __fadd_rn(v.lo, r.lo));
+      // term = T (1 + p) = T.hi + T.hi p + T.lo (1 + p); |T.hi p| <= T.hi / 128
+      const float2 T = st[-n];
+      const float q = __fmul_rn(T.x, pp.hi);
+      const float qe = __fmaf_rn(T.x, pp.hi, -q);
+      const float small = __fadd_rn(__fmaf_rn(T.x, pp.lo, __fmaf_rn(T.y, pp.hi, qe)), T.y);
+      const ff tt = quick_two_sum(T.x, q);
+      th = tt.hi;
+      tl = __fadd_rn(tt.lo, small);
     } else {
-      t = ff{expf(y.hi), 0.f};
+      th = expf(y.hi);  // below exp(-36): the tail's 1e-7 relative error is negligible
+      tl = 0.f;
     }
-    acc = ff_add(acc, t);
+    // acc += (th, tl)
+    ff s1 = two_sum(acc.hi, th);
+    s1.lo = __fadd_rn(s1.lo, __fadd_rn(acc.lo, tl));
+    acc = quick_two_sum(s1.hi, s1.lo);
   }
   double d = (double)acc.hi + (double)acc.lo;
 #pragma unroll

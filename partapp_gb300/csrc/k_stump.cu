@@ -169,7 +169,7 @@ __global__ void k_mask_no_class(float *__restrict__ scores, const uint8_t *__res
 // v*p < theta*p is v < theta; for p = -1 it is v > theta, i.e.
 // !(v < nextafter(theta, +inf)).  With t = theta or nextafter(theta, +inf)
 // and a = p*alpha the reference's vote (v*p < theta*p) ? alpha : -alpha is
-// (v < t) ? a : -a for every finite v -- one compare, one select, one add.
+// (v < t) ? a : -a for every non-NaN v -- one compare, one select, one add.
 // Classifiers with other polarities use the literal form (k_score_grids).
 // ---------------------------------------------------------------------------
 constexpr int kChunks = 24;

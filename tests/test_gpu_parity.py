@@ -84,11 +84,14 @@ def test_score_grids_bit_exact(ctx, orc):
 
 
 @pytest.mark.parametrize("polarity,n_parts", [("unit", 22), ("unit", 13), ("unit", 10),
-                                              ("general", 22)])
+                                              ("general", 22), ("special", 22)])
 def test_score_grids_960_pipelined_bit_exact(ctx, orc, polarity, n_parts):
     """The 960-dim path (staged tiles, sign-folded stump test) on a ragged
     tile count, 22 classifiers and planted v == theta ties; a classifier with
-    a non-unit polarity exercises the literal v*p < theta*p form."""
+    a non-unit polarity exercises the literal v*p < theta*p form; "special"
+    plants +-inf and -0 descriptor values and +-0 and negative thresholds.
+    (NaN descriptor values are outside the folded test's domain: it is exact
+    for every non-NaN v.)"""
     rng = np.random.default_rng(9)
     R, ny, nx, D = 2, 7, 33, 960
     desc = synth.make_descriptors(rng, R, ny, nx, D)
@@ -96,6 +99,13 @@ def test_score_grids_960_pipelined_bit_exact(ctx, orc, polarity, n_parts):
     for p in range(n_parts):
         for i in range(0, 120, 5):
             m["theta"][p, i] = desc[i % R, (i // 3) % ny, i % nx, m["f"][p, i]]
+    if polarity == "special":
+        flat = desc.reshape(-1)
+        for k, v in enumerate((np.inf, -np.inf, -0.0, 0.0)):
+            flat[k::37] = v
+        m["theta"][:, ::11] = 0.0
+        m["theta"][:, 3::11] = -0.0
+        m["theta"][:, 5::11] = -m["theta"][:, 5::11]
     if polarity == "general":
         m["p"][3, ::7] = 0.5
         m["p"][4, ::9] = -2.0
