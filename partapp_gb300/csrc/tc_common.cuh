@@ -57,6 +57,15 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c, int x, int y,
                                             int z, uint64_t *bar) {
   asm volatile(
@@ -149,6 +158,14 @@ bool make_map_2d(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows,
                  uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows);
 bool make_map_nhwc(CUtensorMap *m, const void *base, uint64_t C, uint64_t W, uint64_t H,
                    uint64_t N, uint32_t box_w);
+// fp32 2-D map without swizzle, zero fill outside: `rows` rows of `cols`
+// floats (row stride in bytes, a multiple of 16), box box_cols x box_rows.
+bool make_map_f32_2d(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows,
+                     uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows);
+// fp32 3-D map of a dense [planes][rows][cols] array, box box_cols x box_rows
+// x 1, zero fill outside every dimension.
+bool make_map_f32_3d(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows,
+                     uint64_t planes, uint32_t box_cols, uint32_t box_rows);
 
 }  // namespace tc
 }  // namespace pa
