@@ -17,9 +17,13 @@
 //               the row as exp(J10 - M) in shared memory, applies the rotation
 //               filter per column in registers and the x pass along the row,
 //               and writes the exp-domain intermediate E2.
-//   k_msg_cols  one CTA per (32-column strip, row band, rotation, message):
-//               y pass over the staged strip, log, + M, the shift back into
-//               the parent frame and the epilogue (store / add / marginal).
+//   k_msg_cols_tma  one CTA per (32-column strip, 176-row band, rotation,
+//               message): TMA stages the E2 strip with its y halo and the
+//               epilogue's inputs, then the y pass (packed FMAs), log, + M,
+//               the shift back into the parent frame and the epilogue
+//               (store / add / marginal).  k_msg_cols is the same pass with
+//               gathered rows, for messages without TMA maps (shift tables
+//               that are not plain shifts, widths not a multiple of 4).
 // The nearest-shift source indices come from per-message tables computed
 // with the reference's double-precision rounding (k_shift_tables).
 #include <cuda_bf16.h>
@@ -333,254 +337,12 @@ __global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(con
   }
 }
 
-// ---------------------------------------------------------------------------
-// k_msg_rows_tma: the row kernel with the shifted child rows staged by TMA.
-//
-// For rotation r the log_joint_10 row y is the child's row sy_r of rotation
-// r - kidx, shifted by the integer c_r (the uniform case of the shift
-// tables, valid on the output columns [lo_r, hi_r)).  That row segment is one
-// run of a 2-D tensor map over the child viewed as [R*H][W]: boxes of
-// kRowBox x 1 floats at x = floor4(first column + c_r) (TMA wants the inner
-// coordinate on a 16-byte boundary), so the shift lives in the box
-// coordinate and output column lx reads staged element lx + o_r with
-// o_r = (first column + c_r) mod 4.  Columns outside [lo_r, hi_r) and rows
-// without a source are LOG_ZERO (computeRotJointMarginal's fill), exactly as
-// the gather kernel stages them; rows whose table is not a plain shift are
-// gathered element by element.
-//
-// Rotation pairs stream through a two-slot ring (each slot the two rows of a
-// pair), one mbarrier per slot with bounded waits: while pair p is turned
-// into exp(J10 - M) in the pair-interleaved E layout, pair p + 1 is in
-// flight.  The rotation filter and the x pass then run as in k_msg_rows, so
-// E2 is bit-identical to that kernel's.
-// ---------------------------------------------------------------------------
-constexpr int kRowBox = 256;  // TMA box width of a staged row (floats)
-
 // The dynamic shared memory from its first 128-byte boundary (TMA
 // destinations start on one); launchers add kSmemAlign bytes.
 constexpr int kSmemAlign = 128;
 __device__ __forceinline__ float *smem_align128(float *p) {
   const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
   return p + (((kSmemAlign - (a & (kSmemAlign - 1))) & (kSmemAlign - 1)) >> 2);
-}
-
-struct __align__(16) RowInfo {
-  int mode;    // 0: no source row (all LOG_ZERO), 1: TMA-staged shift, 2: gathered
-  int o;       // staged element of local column 0 (mode 1)
-  int lo, hi;  // valid local columns [lo, hi) (mode 1)
-  int x0, yrow;  // TMA coordinates of the first box (mode 1); yrow also the source row (mode 2)
-  int pad0, pad1;
-};
-
-static_assert(sizeof(RowInfo) == 32, "RowInfo is eight ints");
-
-__host__ __device__ __forceinline__ size_t rows_tma_ring_floats(int nbox) {
-  return (size_t)2 * 2 * nbox * kRowBox;  // 2 slots x 2 rows
-}
-
-template <int RT>
-__global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2)
-    k_msg_rows_tma(const MsgDesc *__restrict__ msgs, int H, int W, int padx, int cw, int nbox,
-                   int *err) {
-  constexpr int R = RT;
-  constexpr int RP = RT / 2;
-  static_assert(RT % 2 == 0, "rotation pairs");
-  const MsgDesc md = msgs[blockIdx.y];
-  const int y = blockIdx.x;
-  const int xc0 = blockIdx.z * cw;
-  const int ncw = min(cw, W - xc0);
-  const int WP = rows_stride(cw, padx);
-  const int gx0 = max(0, xc0 - padx), gx1 = min(W, xc0 + ncw + padx);
-  const int lg0 = gx0 - xc0 + padx, lg1 = gx1 - xc0 + padx;
-  const int gw = gx1 - gx0;
-  const int xl0 = xc0 - padx;  // image column of local column 0
-  extern __shared__ __align__(16) float sm_raw[];
-  float *sm = smem_align128(sm_raw);
-  // layout (floats from a 128-byte boundary): ring [2][2][nbox * kRowBox]
-  // (TMA destinations, 1 KB boxes), info [R], E [RP][WP] pairs, x taps,
-  // rotation taps, output staging [warps][32 * kNO]
-  float *ring = sm;
-  RowInfo *info = reinterpret_cast<RowInfo *>(sm + rows_tma_ring_floats(nbox));
-  float2 *E = reinterpret_cast<float2 *>(info + R);
-  const int xpmax = ((2 * padx + 1 + kU - 1) / kU) * kU;
-  float2 *tx = E + ((RP * WP + 1) & ~1);
-  const int xpad = ((md.xlen + kU - 1) / kU) * kU;
-  float *tr = reinterpret_cast<float *>(tx + xpmax);
-  float *ostage = tr + kMaxRot;
-  __shared__ __align__(8) uint64_t bar[2];
-  const int tid = threadIdx.x;
-  const CUtensorMap *map = md.tm_in;
-
-  for (int i = tid; i < xpad; i += blockDim.x) {
-    const float t = i < md.xlen ? md.xtaps[i] : 0.f;
-    tx[i] = make_float2(t, t);
-  }
-  for (int i = tid; i < md.rlen; i += blockDim.x) tr[i] = md.rtaps[i];
-  const float negM = -fkey_decode(*md.in_max);
-  const int HW = H * W;
-  for (int r = tid; r < R; r += blockDim.x) {
-    RowInfo f{};
-    const int4 dy = md.sdesc[R + r], dx = md.sdesc[r];
-    const int sy = shift_src(dy, md.ty_in + r * H, y);
-    if (sy >= 0) {
-      const int srow = (r - md.kidx) * H + sy;
-      if (dx.w) {
-        const int a = xl0 + dx.x;      // source column of local column 0
-        const int x0 = a & ~3;         // floor to a multiple of 4 (two's complement)
-        f.mode = 1;
-        f.o = a - x0;
-        f.lo = max(lg0, dx.y - xl0);
-        f.hi = min(lg1, dx.z - xl0);
-        f.x0 = x0;
-        f.yrow = srow;
-      } else {
-        f.mode = 2;
-        f.yrow = srow;
-      }
-    }
-    info[r] = f;
-  }
-  if (tid == 0) {
-    tc::mbar_init(&bar[0], 1);
-    tc::mbar_init(&bar[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  // columns outside the image are zeros of E (the reference's filter truncates)
-  const int npad = WP - gw;
-  for (int idx = tid; idx < RP * npad; idx += blockDim.x) {
-    const int p = idx / npad, k = idx - p * npad;
-    E[p * WP + (k < lg0 ? k : lg1 + (k - lg0))] = make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-
-  // thread 0 queues the TMA boxes of pair p into slot p & 1
-  // TMA wants 128-byte aligned destinations and a 64-byte aligned map: a
-  // violation is reported (error bit 16) and no box is issued
-  const bool tma_ok = (tc::smem_u32(ring) & 127u) == 0 && ((uintptr_t)map & 63u) == 0;
-  if (!tma_ok && tid == 0) atomicOr(err, 16);
-  auto issue = [&](int p) {
-    const int s = p & 1;
-    uint32_t bytes = 0;
-    for (int h = 0; h < 2; ++h)
-      if (tma_ok && info[2 * p + h].mode == 1) bytes += (uint32_t)nbox * kRowBox * 4;
-    tc::mbar_arrive_expect_tx(&bar[s], bytes);
-    for (int h = 0; h < 2 && tma_ok; ++h) {
-      const RowInfo f = info[2 * p + h];
-      if (f.mode != 1) continue;
-      float *dst = ring + (size_t)(s * 2 + h) * nbox * kRowBox;
-      for (int b = 0; b < nbox; ++b) tc::tma_load_2d(dst + b * kRowBox, map, f.x0 + b * kRowBox, f.yrow, &bar[s]);
-    }
-  };
-  __shared__ int s_issued[RP], s_fail;  // s_fail: first pair whose wait ran out, RP if none
-  if (tid == 0) {
-    s_fail = RP;
-    for (int p = 0; p < RP; ++p) s_issued[p] = p < 2;
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
-    issue(0);
-    if (RP > 1) issue(1);
-  }
-  __syncthreads();
-  for (int p = 0; p < RP; ++p) {
-    const int s = p & 1;
-    if (s_issued[p] && !tc::mbar_wait(&bar[s], (uint32_t)((p >> 1) & 1), err)) atomicMin(&s_fail, p);
-    const float *P0 = ring + (size_t)(s * 2) * nbox * kRowBox;
-    const RowInfo f0 = info[2 * p], f1 = info[2 * p + 1];
-    bool inf = false;
-    for (int lx = lg0 + tid; lx < lg1; lx += blockDim.x) {
-      float v[2];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const RowInfo &f = h ? f1 : f0;
-        float x = kLogZero;
-        if (f.mode == 1) {
-          if (lx >= f.lo && lx < f.hi) x = P0[h * nbox * kRowBox + lx + f.o];
-        } else if (f.mode == 2) {
-          const int sx = shift_src(md.sdesc[2 * p + h], md.tx_in + (2 * p + h) * W, xl0 + lx);
-          if (sx >= 0) x = __ldg(md.in + (int64_t)f.yrow * W + sx);
-        }
-        v[h] = expf(__fadd_rn(x, negM));
-        inf = inf || v[h] == INFINITY;
-      }
-      E[p * WP + lx] = make_float2(v[0], v[1]);
-    }
-    if (inf) atomicOr(err, 1);
-    __syncthreads();  // slot s is free again
-    if (tid == 0 && p + 2 < RP && s_fail == RP) {
-      issue(p + 2);
-      s_issued[p + 2] = 1;
-    }
-  }
-  if (s_fail < RP) {
-    // a wait ran out (error bit set) and no box was issued after it: wait
-    // once more, bounded, for the copies of that pair and the next, then leave
-    if (tid == 0)
-      for (int p = s_fail; p < RP && p < s_fail + 2; ++p)
-        if (s_issued[p]) tc::mbar_wait(&bar[p & 1], (uint32_t)((p >> 1) & 1), err);
-    return;
-  }
-
-  // rotation filter, column by column, in place
-  if (md.rlen <= 0) {
-    if (md.rlen == 0)
-      for (int idx = tid; idx < RP * gw; idx += blockDim.x) {
-        const int p = idx / gw, x = lg0 + idx - p * gw;
-        E[p * WP + x] = make_float2(0.f, 0.f);
-      }
-  } else {
-    const int nr = (md.rlen - 1) / 2;
-    for (int x = lg0 + tid; x < lg1; x += blockDim.x) {
-      float e[RT];
-#pragma unroll
-      for (int p = 0; p < RP; ++p) {
-        const float2 v = E[p * WP + x];
-        e[2 * p] = v.x;
-        e[2 * p + 1] = v.y;
-      }
-      if (!rot_filter_dispatch<RT, (RT - 1) / 2>(nr, e, E + x, WP, tr)) atomicOr(err, 2);
-    }
-  }
-  __syncthreads();
-
-  // x pass (as k_msg_rows)
-  const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  const int kx = (md.xlen - 1) / 2;
-  float *e2 = md.e2;
-  float *ws = ostage + warp * (32 * kNO);
-  const int nstrips = (ncw + 32 * kNO - 1) / (32 * kNO);
-  for (int task = warp; task < RP * nstrips; task += nwarps) {
-    const int p = task / nstrips;
-    const int xs = (task - p * nstrips) * 32 * kNO;
-    const int x0 = xs + lane * kNO;
-    float2 acc[kNO];
-#pragma unroll
-    for (int i = 0; i < kNO; ++i) acc[i] = make_float2(0.f, 0.f);
-    if (x0 < ncw) {
-      const float2 *row = E + p * WP + padx - kx + x0;
-      for (int kb = 0; kb < xpad; kb += kU) {
-        float2 v[kNO + kU - 1];
-#pragma unroll
-        for (int i = 0; i < kNO + kU - 1; ++i) v[i] = row[kb + i];
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          const float2 t = tx[kb + u];
-#pragma unroll
-          for (int i = 0; i < kNO; ++i) acc[i] = ffma2(t, v[i + u], acc[i]);
-        }
-      }
-    }
-    const int nx = min(32 * kNO, ncw - xs);
-    float *o = e2 + (int64_t)(2 * p) * HW + (int64_t)y * W + xc0 + xs;
-#pragma unroll
-    for (int i = 0; i < kNO; ++i) ws[lane * kNO + i] = acc[i].x;
-    __syncwarp();
-    for (int j = lane; j < nx; j += 32) o[j] = ws[j];
-    __syncwarp();
-#pragma unroll
-    for (int i = 0; i < kNO; ++i) ws[lane * kNO + i] = acc[i].y;
-    __syncwarp();
-    for (int j = lane; j < nx; j += 32) o[HW + j] = ws[j];
-    __syncwarp();
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -840,7 +602,7 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
 // ---------------------------------------------------------------------------
 // k_msg_cols_tma: the column pass with the E2 strip staged by TMA.
 //
-// CTA = 32 parent columns x kCBand rows x one rotation, four warps.  When
+// CTA = 32 parent columns x kCBand rows x one rotation, eight warps.  When
 // both shift-back tables of the rotation are plain shifts (the usual case)
 // the strip needs source columns [cmin, cmin + 32) and source rows
 // [rmin - ky, rmin + nrows + ky) of E2 rotation r: boxes of kCWT x kCBoxRows
@@ -852,9 +614,9 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
 // back and combines with the caller's accumulation as msg_epilogue does,
 // with 32-bit cell indices.  Other tables take cols_gather_tile.
 // ---------------------------------------------------------------------------
-constexpr int kColWarps = 4;
+constexpr int kColWarps = 8;
 constexpr int kColThreads = 32 * kColWarps;
-constexpr int kCBand = 2 * kColWarps * kNO;  // 88 rows: one task of 2 x kNO rows per warp
+constexpr int kCBand = 2 * kColWarps * kNO;  // 176 rows: one task of 2 x kNO rows per warp
 constexpr int kCWT = 36;                     // staged columns: 32 + the 16-byte slack
 constexpr int kCBoxRows = 64;                // TMA box height
 constexpr int kFP = 33;                      // pitch of the filtered tile F
@@ -862,14 +624,20 @@ constexpr int kFP = 33;                      // pitch of the filtered tile F
 __host__ __device__ __forceinline__ int cols_tma_boxes(int pady) {
   return (kCBand + 2 * pady + kU + kCBoxRows - 1) / kCBoxRows;
 }
+// offset (floats) of the epilogue input tiles src0 / src1 [kCBand][kTX]
+// each, 128-byte aligned after the E2 tile, F and the y taps
+__host__ __device__ __forceinline__ size_t cols_src_off(int pady) {
+  const size_t o = (size_t)cols_tma_boxes(pady) * kCBoxRows * kCWT + (size_t)kCBand * kFP +
+                   ((2 * pady + 1 + kU - 1) / kU) * kU;
+  return (o + 31) / 32 * 32;
+}
 __host__ __device__ __forceinline__ size_t cols_tma_smem(int pady) {
-  const size_t tile = (size_t)cols_tma_boxes(pady) * kCBoxRows * kCWT + (size_t)kCBand * kFP +
-                      ((2 * pady + 1 + kU - 1) / kU) * kU;
+  const size_t tile = cols_src_off(pady) + (size_t)2 * kCBand * kTX;
   const size_t g = cols_gather_smem(kCBand, pady) / sizeof(float);
   return (tile > g ? tile : g) * sizeof(float) + kSmemAlign;
 }
 
-__global__ void __launch_bounds__(kColThreads) k_msg_cols_tma(const MsgDesc *__restrict__ msgs,
+__global__ void __launch_bounds__(kColThreads, 2) k_msg_cols_tma(const MsgDesc *__restrict__ msgs,
                                                               int R, int H, int W, int pady,
                                                               int *err) {
   const MsgDesc md = msgs[blockIdx.z];
@@ -883,7 +651,7 @@ __global__ void __launch_bounds__(kColThreads) k_msg_cols_tma(const MsgDesc *__r
   __shared__ int lim[4];
   __shared__ int red[kColWarps];
   __shared__ unsigned long long redu[kColWarps];
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bar, bar_src;
   const int4 dxo = md.sdesc[2 * R + r], dyo = md.sdesc[3 * R + r];
   if (!dxo.w || !dyo.w) {  // uniform for the CTA
     cols_gather_tile(md, R, H, W, r, y0, y1, x0, x1, kCBand, pady, first_block, err, sm, lim, red,
@@ -902,28 +670,46 @@ __global__ void __launch_bounds__(kColThreads) k_msg_cols_tma(const MsgDesc *__r
   float *S = sm;                                               // [nb * kCBoxRows][kCWT]
   float *F = S + (size_t)cols_tma_boxes(pady) * kCBoxRows * kCWT;  // [kCBand][kFP]
   float *ty = F + kCBand * kFP;
+  float *S0 = sm + cols_src_off(pady), *S1 = S0 + kCBand * kTX;  // [kCBand][kTX] each
   const int ypad = ((md.ylen + kU - 1) / kU) * kU;
+  const int nsrc = md.mode == EPI_STORE ? 0 : (md.mode == EPI_DOWN && md.dst1 ? 2 : 1);
   for (int i = tid; i < ypad; i += blockDim.x) ty[i] = i < md.ylen ? md.ytaps[i] : 0.f;
   const int xs0 = cmin & ~3, o = cmin - xs0;
   // TMA wants 128-byte aligned destinations and a 64-byte aligned map: a
   // violation is reported (error bit 16) and the tile is not staged
-  const bool tma_ok = (tc::smem_u32(S) & 127u) == 0 && ((uintptr_t)md.tm_e2 & 63u) == 0;
+  const bool tma_ok = (tc::smem_u32(S) & 127u) == 0 && (tc::smem_u32(S0) & 127u) == 0 &&
+                      ((uintptr_t)md.tm_e2 & 63u) == 0 && ((uintptr_t)md.tm_src0 & 63u) == 0 &&
+                      ((uintptr_t)md.tm_src1 & 63u) == 0 && (nsrc < 1 || md.tm_src0) &&
+                      (nsrc < 2 || md.tm_src1);
   if (!tma_ok && tid == 0) atomicOr(err, 16);
-  if (any && tma_ok && tid == 0) {
+  if (tma_ok && tid == 0) {
     tc::mbar_init(&bar, 1);
+    tc::mbar_init(&bar_src, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(md.tm_e2) : "memory");
-    tc::mbar_arrive_expect_tx(&bar, (uint32_t)(nb * kCBoxRows * kCWT * 4));
-    for (int b = 0; b < nb; ++b)
-      tc::tma_load_3d(S + (size_t)b * kCBoxRows * kCWT, md.tm_e2, xs0, rmin - ky + b * kCBoxRows, r,
-                      &bar);
+    if (any) {
+      asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(md.tm_e2) : "memory");
+      tc::mbar_arrive_expect_tx(&bar, (uint32_t)(nb * kCBoxRows * kCWT * 4));
+      for (int b = 0; b < nb; ++b)
+        tc::tma_load_3d(S + (size_t)b * kCBoxRows * kCWT, md.tm_e2, xs0, rmin - ky + b * kCBoxRows,
+                        r, &bar);
+    }
+    // the epilogue's inputs arrive while the y pass runs
+    tc::mbar_arrive_expect_tx(&bar_src, (uint32_t)(nsrc * kCBand * kTX * 4));
+    for (int k = 0; k < nsrc; ++k) {
+      const CUtensorMap *m = k ? md.tm_src1 : md.tm_src0;
+      asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
+      tc::tma_load_3d(k ? S1 : S0, m, x0, y0, r, &bar_src);
+    }
   }
   // thread 0 watches the copies (bounded); the barrier then hands the tile
   // to the CTA, and a run-out wait sends the whole CTA home (error bit set)
   __shared__ int s_ok;
   if (tid == 0) {
-    s_ok = !tma_ok ? 0 : any ? (int)tc::mbar_wait(&bar, 0, err) : 1;
-    if (!s_ok && tma_ok) tc::mbar_wait(&bar, 0, err);  // once more for the copies in flight
+    s_ok = !tma_ok ? 0 : any ? (int)tc::mbar_wait_try(&bar, 0, err) : 1;
+    if (!s_ok && tma_ok) {  // once more for the copies in flight
+      tc::mbar_wait_try(&bar, 0, err);
+      tc::mbar_wait_try(&bar_src, 0, err);
+    }
   }
   __syncthreads();
   if (!s_ok) return;
@@ -957,9 +743,14 @@ __global__ void __launch_bounds__(kColThreads) k_msg_cols_tma(const MsgDesc *__r
       }
     }
   }
+  if (tid == 0 && !tc::mbar_wait_try(&bar_src, 0, err)) {
+    tc::mbar_wait_try(&bar_src, 0, err);  // once more for the copies in flight
+    s_ok = 0;
+  }
   __syncthreads();
+  if (!s_ok) return;
 
-  // epilogue (msg_epilogue's arithmetic for plain shifts)
+  // epilogue (msg_epilogue's arithmetic for plain shifts), inputs from S0 / S1
   const float M = fkey_decode(*md.in_max);
   if (md.in_max_f64 && first_block && tid == 0) *md.in_max_f64 = (double)M;
   const int HW = H * W;
@@ -968,7 +759,6 @@ __global__ void __launch_bounds__(kColThreads) k_msg_cols_tma(const MsgDesc *__r
   const bool colok = colin && xx >= xa && xx < xb;
   const int fc = xx - xa;  // F column of xx (source column xx + dxo.x - cmin)
   const int mode = md.mode;
-  const float *src0 = md.src0, *src1 = md.src1;
   float *dst0 = md.dst0, *dst1 = md.dst1;
   int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
   unsigned long long am = 0ull;
@@ -978,19 +768,20 @@ __global__ void __launch_bounds__(kColThreads) k_msg_cols_tma(const MsgDesc *__r
     float m = kLogZero;
     if (colok && yy >= ya && yy < yb) m = __fadd_rn(log_or_zero(F[(yy - ya) * kFP + fc]), M);
     const int idx = r * HW + yy * W + xx;
+    const int si = (yy - y0) * kTX + lane;
     if (mode == EPI_STORE) {
       dst0[idx] = m;
     } else if (mode == EPI_ADD) {
-      const float ov = __fadd_rn(m, __ldg(src0 + idx));
+      const float ov = __fadd_rn(m, S0[si]);
       dst0[idx] = ov;
       k0 = max(k0, (ov == ov) ? fkey(ov) : kFkeyNegInf);
     } else {
-      const float ov = __fadd_rn(__ldg(src0 + idx), m);
+      const float ov = __fadd_rn(S0[si], m);
       dst0[idx] = ov;
       const unsigned long long k = akey(ov, (uint32_t)idx);
       am = k > am ? k : am;
       if (dst1) {
-        const float o1 = __fadd_rn(__ldg(src1 + idx), m);
+        const float o1 = __fadd_rn(S1[si], m);
         dst1[idx] = o1;
         k1 = max(k1, (o1 == o1) ? fkey(o1) : kFkeyNegInf);
       }
@@ -1331,47 +1122,6 @@ cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, 
   return cudaGetLastError();
 }
 
-// Shared memory of k_msg_rows_tma: the staging ring, then the layout of
-// k_msg_rows<RT> with per-rotation RowInfo records in place of the shift
-// summaries.
-template <int RT>
-size_t rows_tma_smem(int cw, int padx, int nbox) {
-  const int WP = rows_stride(cw, padx);
-  const int RP = RT / 2;
-  size_t f = rows_tma_ring_floats(nbox);
-  f += (size_t)RT * sizeof(RowInfo) / sizeof(float);
-  f += (size_t)2 * ((RP * WP + 1) & ~1);
-  f += (size_t)2 * ((2 * padx + 1 + kU - 1) / kU) * kU;
-  f += kMaxRot;
-  f += (size_t)(kThreadsRows / 32) * 32 * kNO;
-  return f * sizeof(float) + kSmemAlign;
-}
-
-template <int RT>
-cudaError_t launch_rows_tma(const MsgDesc *msgs, int n_msgs, int H, int W, int padx, int *err,
-                            cudaStream_t s) {
-  // column chunk: the whole row when two CTAs fit on an SM (one for R = 48),
-  // else the widest multiple of 32 * kNO outputs that does
-  const size_t target = (RT == 48 ? 227 : 113) * 1024;
-  auto nbox_of = [&](int cw) { return (cw + 2 * padx + 3 + kRowBox - 1) / kRowBox; };
-  int cw = W;
-  if (rows_tma_smem<RT>(cw, padx, nbox_of(cw)) > target) {
-    cw = 0;
-    for (size_t lim : {target, (size_t)227 * 1024}) {
-      for (int c = 32 * kNO; c < W; c += 32 * kNO)
-        if (rows_tma_smem<RT>(c, padx, nbox_of(c)) <= lim) cw = c;
-      if (cw) break;
-    }
-  }
-  if (cw <= 0 || (int64_t)RT * H * W >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
-  const int nbox = nbox_of(cw);
-  const size_t smem = rows_tma_smem<RT>(cw, padx, nbox);
-  cudaFuncSetAttribute(k_msg_rows_tma<RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 grid((unsigned)H, (unsigned)n_msgs, (unsigned)((W + cw - 1) / cw));
-  k_msg_rows_tma<RT><<<grid, kThreadsRows, smem, s>>>(msgs, H, W, padx, cw, nbox, err);
-  return cudaGetLastError();
-}
-
 }  // namespace
 
 cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,
@@ -1382,20 +1132,8 @@ cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, 
   return cudaGetLastError();
 }
 
-bool make_row_map(CUtensorMap *m, const float *in, int R, int H, int W) {
-  if (W % 4 != 0 || ((uintptr_t)in & 15) != 0 || R < 1 || H < 1) return false;
-  return tc::make_map_f32_2d(m, in, (uint64_t)W, (uint64_t)R * H, (uint64_t)W * 4, kRowBox, 1);
-}
-
 cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
-                            int *err, cudaStream_t s, bool tma) {
-  if (tma && (R == 12 || R == 24 || R == 48)) {
-    switch (R) {
-      case 12: return launch_rows_tma<12>(msgs, n_msgs, H, W, padx, err, s);
-      case 24: return launch_rows_tma<24>(msgs, n_msgs, H, W, padx, err, s);
-      default: return launch_rows_tma<48>(msgs, n_msgs, H, W, padx, err, s);
-    }
-  }
+                            int *err, cudaStream_t s) {
   switch (R) {
     case 12: return launch_rows_t<12>(msgs, n_msgs, R, H, W, padx, err, s);
     case 24: return launch_rows_t<24>(msgs, n_msgs, R, H, W, padx, err, s);
@@ -1439,6 +1177,11 @@ cudaError_t launch_msg_full(const MsgDesc *msgs, int n_msgs, int R, int H, int W
                     (unsigned)n_msgs),
                kThreadsCols, 0, s>>>(msgs, R, H, W);
   return cudaGetLastError();
+}
+
+bool make_src_map(CUtensorMap *m, const float *src, int R, int H, int W) {
+  if (W % 4 != 0 || ((uintptr_t)src & 15) != 0 || R < 1 || H < 1) return false;
+  return tc::make_map_f32_3d(m, src, (uint64_t)W, (uint64_t)H, (uint64_t)R, kTX, kCBand);
 }
 
 bool make_e2_map(CUtensorMap *m, const float *e2, int R, int H, int W) {

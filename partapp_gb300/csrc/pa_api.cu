@@ -653,7 +653,7 @@ struct PsPlan {
   struct Phase {
     MsgDesc *msgs = nullptr;
     int n = 0, padx = 0, pady = 0;
-    bool tma = false;  // every message of the phase has TMA row maps
+    bool tma = false;  // every message of the phase has TMA maps for the column pass
     int n_full = 0, ohmax = 0, owmax = 0, kxf = 0, kyf = 0;  // full-covariance messages
     struct TcJob {
       void *eb, *xt, *tbx, *tby;
@@ -930,23 +930,26 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
       d.in_max_f64 = b.dry ? nullptr
                            : pl.msgmax + (size_t)mm.img * 2 * (P - 1) + (mm.up ? 0 : P - 1) + mm.joint;
     }
-    // TMA maps of the child maps the row kernel stages (plain messages only)
-    // (the blob space is reserved alike in both passes; a map that cannot be
-    // made, e.g. for a caller's unaligned buffer, sends the phase to the
-    // gathering row kernel)
-    // and of the e2 buffers the column pass stages: [2][n] maps
-    std::vector<CUtensorMap> maps(2 * ph.size());
+    // TMA maps of what the column pass stages (plain messages only): the e2
+    // buffer and the epilogue's inputs src0 / src1, [3][n] maps.  The blob
+    // space is reserved alike in both passes; a map that cannot be made (a
+    // caller's unaligned buffer) sends the phase to the gathering kernel.
+    std::vector<CUtensorMap> maps(3 * ph.size());
     const size_t n = ph.size();
     const bool reserve = out.n_full == 0 && out.tc.empty() && !ph.empty() && W % 4 == 0;
     bool tma = reserve && !b.dry;
-    for (size_t k = 0; k < n && tma; ++k)
-      tma = make_row_map(&maps[k], descs[k].in, R, H, W) &&
-            make_e2_map(&maps[n + k], descs[k].e2, R, H, W);
+    for (size_t k = 0; k < n && tma; ++k) {
+      const MsgDesc &d = descs[k];
+      tma = make_e2_map(&maps[k], d.e2, R, H, W) &&
+            (!d.src0 || make_src_map(&maps[n + k], d.src0, R, H, W)) &&
+            (!d.src1 || make_src_map(&maps[2 * n + k], d.src1, R, H, W));
+    }
     const CUtensorMap *tm = reserve ? b.param(maps.data(), maps.size()) : nullptr;
     out.tma = tma;
     for (size_t k = 0; k < n; ++k) {
-      descs[k].tm_in = tma ? tm + k : nullptr;
-      descs[k].tm_e2 = tma ? tm + n + k : nullptr;
+      descs[k].tm_e2 = tma ? tm + k : nullptr;
+      descs[k].tm_src0 = tma && descs[k].src0 ? tm + n + k : nullptr;
+      descs[k].tm_src1 = tma && descs[k].src1 ? tm + 2 * n + k : nullptr;
     }
     out.msgs = b.param(descs.data(), descs.size());
   };
@@ -1034,7 +1037,7 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   cudaStream_t st = ctx->stream;
   const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
   auto run_phase = [&](const PsPlan::Phase &ph) -> pa_status {
-    PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st, ph.tma));
+    PA_LAUNCH("msg_rows", launch_msg_rows(ph.msgs, ph.n, R, H, W, ph.padx, pl.err, st));
     if (ph.n_full + (int)ph.tc.size() < ph.n)
       PA_LAUNCH("msg_cols", launch_msg_cols(ph.msgs, ph.n, R, H, W, ph.pady, pl.err, st, ph.tma));
     if (ph.n_full)

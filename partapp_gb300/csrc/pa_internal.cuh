@@ -133,8 +133,8 @@ enum EpiMode : int {
 
 struct MsgDesc {
   const float *in;        // [R][H][W]
-  const CUtensorMap *tm_in;  // TMA map of `in` as [R*H][W], box kRowBox x 1 (null: gathered rows)
   const CUtensorMap *tm_e2;  // TMA map of e2 as {W, H, R} for the column pass (null: gathered)
+  const CUtensorMap *tm_src0, *tm_src1;  // TMA maps of src0 / src1 as {W, H, R} (null: absent)
   const int *in_max;      // fkey of max(in)
   float *e2;              // [R][H][W] row-filtered exp-domain intermediate
   const int16_t *tx_in;   // [R][W] source column in `in` for log_joint_10 column (or -1)
@@ -231,10 +231,7 @@ cudaError_t launch_prepare_unary(const float *in, float *out, const int *masked_
 cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,
                                 int16_t *tables, int4 *sdesc, cudaStream_t s);
 cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
-                            int *err_flag, cudaStream_t s, bool tma = false);
-// Row-kernel TMA maps: true when rows of `in` ([R*H][W] floats) can be
-// staged by TMA (W a multiple of 4, 16-byte aligned base); fills *m.
-bool make_row_map(CUtensorMap *m, const float *in, int R, int H, int W);
+                            int *err_flag, cudaStream_t s);
 // BF16 GEMM on tcgen05: C[M][N] (fp32) = A[M][K] * B[N][K]^T, bf16 operands
 // with K contiguous (lda, ldb in elements, 16-byte aligned rows).
 struct GemmArgs {
@@ -269,6 +266,8 @@ cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W
 // Column-pass TMA map of an e2 buffer [R][H][W] (W a multiple of 4, 16-byte
 // aligned); false if it cannot be made.
 bool make_e2_map(CUtensorMap *m, const float *e2, int R, int H, int W);
+// Column-pass TMA map of an epilogue input (src0 / src1) [R][H][W].
+bool make_src_map(CUtensorMap *m, const float *src, int R, int H, int W);
 cudaError_t launch_root_combine(const RootDesc *rd, int n_roots, int64_t N, cudaStream_t s);
 cudaError_t launch_root_posterior(const float *const *post_root, float *const *root_post,
                                   const int *keep, int n_keep, int n_images, int R, int H, int W,

@@ -40,6 +40,30 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Blocking probe: the thread may be suspended until the phase completes or
+// a hardware time limit passes; the caller bounds the retries.
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits with mbar_try, at most kTryLimit retries; on time-out sets bit 8 of
+// *err.
+constexpr uint32_t kTryLimit = 1u << 20;
+__device__ __forceinline__ bool mbar_wait_try(uint64_t *bar, uint32_t parity, int *err) {
+  for (uint32_t i = 0; i < kTryLimit; ++i)
+    if (mbar_try(bar, parity)) return true;
+  atomicOr(err, 8);
+  return false;
+}
+
 // Polls at most kSpinLimit times; on time-out sets bit 8 of *err.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
   for (uint32_t i = 0; i < kSpinLimit; ++i)
