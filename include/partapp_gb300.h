@@ -35,6 +35,7 @@ typedef int pa_status;
 #define PA_ERR_CUDA 3         /* CUDA runtime error (message in pa_last_error) */
 #define PA_ERR_NOMEM 4        /* device or host allocation failed */
 #define PA_ERR_NUMERIC 5      /* exp() overflow: the reference asserts here */
+#define PA_ERR_TIMEOUT 6      /* a bounded device-side wait ran out (pa_find_obj_queue) */
 
 #define PA_MEM_DEVICE 0
 #define PA_MEM_HOST 1
@@ -543,6 +544,35 @@ pa_status pa_unary_net_backward(pa_ctx *ctx, pa_unary_net *net, const void *fiel
                                 int nx, double *loss, float *grads);
 /* One Adam step with the gradient of the last pa_unary_net_backward. */
 pa_status pa_unary_net_adam(pa_ctx *ctx, pa_unary_net *net, const pa_adam_param *opt);
+
+/* The image loop of findObjectDataset (objectdetect_aux.cpp:322-406) over
+ * images of uneven sizes and rotation counts, as pa_find_obj_multi, with the
+ * message passing of all images of a wave in ONE persistent launch:
+ * no counterpart in the reference, which loops over images serially.
+ * Per wave (up to images_per_wave images, bounded by device memory) the
+ * unaries run as one launch per group of images that share sizes; then a
+ * persistent kernel drains a device work queue of tiles -- the rows and
+ * column bands of every message of every image and the root combinations --
+ * in the order of computeRootPosteriorRot (objectdetect_findrot.cpp:582-658
+ * upward, then computePartMarginals :192-236 downward), each image's tree
+ * order enforced by per-job completion counters in device memory; then the
+ * root posterior, log-partition and local maxima per group.  Every device
+ * wait is bounded by wait_timeout_ms: a wait that runs out abandons the
+ * wave and the call returns PA_ERR_TIMEOUT.  Row-tile widths are chosen per
+ * shape class by measuring candidates once (autotune) and cached in the
+ * context.  Results equal pa_find_obj_multi's bit for bit.  Device inputs
+ * only; images whose messages need the full-covariance or tensor-core
+ * paths are processed as pa_find_obj_multi does. */
+typedef struct {
+  int images_per_wave;    /* images per persistent launch (0: 32) */
+  double wait_timeout_ms; /* bound of each dependency wait (<= 0: 20000 ms) */
+  int autotune;           /* measure row-tile widths per shape class (1) or take the default (0) */
+  int hold_start;         /* diagnostic: the host never opens the queue's start gate, so every
+                           * wait runs out (tests of the time-out path); 0 normally */
+} pa_queue_opts;
+void pa_queue_opts_default(pa_queue_opts *o);
+pa_status pa_find_obj_queue(pa_ctx *ctx, int n_images, const pa_image *imgs,
+                            const pa_classifier *const *cls, int n_cls, const pa_queue_opts *opts);
 
 /* pa_find_obj_batch with the net as the unary of the parts whose
  * part_on_net[p] is non-zero (all parts when part_on_net is NULL) and the

@@ -34,7 +34,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libpartapp_gb300.so")
 
-PA_OK, PA_ERR_INVALID, PA_ERR_UNSUPPORTED, PA_ERR_CUDA, PA_ERR_NOMEM, PA_ERR_NUMERIC = range(6)
+PA_OK, PA_ERR_INVALID, PA_ERR_UNSUPPORTED, PA_ERR_CUDA, PA_ERR_NOMEM, PA_ERR_NUMERIC, \
+    PA_ERR_TIMEOUT = range(7)
 PA_MEM_DEVICE, PA_MEM_HOST = 0, 1
 LOG_ZERO = -1e6
 NO_CLASS_VALUE = 0.0
@@ -53,9 +54,15 @@ EXPORTS = (
     "pa_unary_net_create", "pa_unary_net_destroy", "pa_unary_net_get_params",
     "pa_unary_net_set_params", "pa_unary_net_forward", "pa_unary_net_backward",
     "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries", "pa_add_dpm_scores",
-    "pa_nms_recursive",
+    "pa_nms_recursive", "pa_queue_opts_default", "pa_find_obj_queue",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
+
+
+class QueueOpts(C.Structure):
+    """pa_queue_opts."""
+    _fields_ = [("images_per_wave", C.c_int), ("wait_timeout_ms", C.c_double),
+                ("autotune", C.c_int), ("hold_start", C.c_int)]
 
 
 class Image(C.Structure):
@@ -177,6 +184,9 @@ def load_library():
     L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip, ip]
     L.pa_ctx_set_message_math.argtypes = [vp, ip]
     L.pa_find_obj_multi.argtypes = [vp, ip, P(Image), P(vp), ip, ip]
+    L.pa_find_obj_queue.argtypes = [vp, ip, P(Image), P(vp), ip, P(QueueOpts)]
+    L.pa_queue_opts_default.argtypes = [P(QueueOpts)]
+    L.pa_queue_opts_default.restype = None
     L.pa_rot_joint_marginal_noalloc.argtypes = [P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp),
                                                  P(dp), dp, dp, dp, vp]
     L.pa_find_obj.argtypes = [vp, P(ExpParam), P(Tree), ip, P(vp), ip, vp, ip, ip, ip, P(dp), ip,
@@ -500,10 +510,7 @@ class Context:
         res["root_hyps"] = res["root_hyps"][: int(res["n_root_hyps"][0])]
         return res
 
-    def find_obj_multi(self, images, cls_list, want_marg=False):
-        """images: list of dicts {exp, tree, desc [R][ny][nx][dim], Tig, H, W,
-        flip=False} of possibly different sizes and rotation counts; all
-        descriptors numpy (host) or all CUDA tensors (device)."""
+    def _image_list(self, images, want_marg):
         keep, imgs, results = [], [], []
         mem = None
         for im in images:
@@ -523,9 +530,28 @@ class Context:
                               d.ptr, ny, nx, dim, T.ctypes.data, 1, im["H"], im["W"],
                               C.addressof(o)))
             results.append((res, P))
-        arr = (Image * len(imgs))(*imgs)
-        self._check(self.L.pa_find_obj_multi(self.h, len(imgs), arr, self._cls_array(cls_list),
+        return (Image * len(imgs))(*imgs), results, mem, keep
+
+    def find_obj_multi(self, images, cls_list, want_marg=False):
+        """images: list of dicts {exp, tree, desc [R][ny][nx][dim], Tig, H, W,
+        flip=False} of possibly different sizes and rotation counts; all
+        descriptors numpy (host) or all CUDA tensors (device)."""
+        arr, results, mem, keep = self._image_list(images, want_marg)
+        self._check(self.L.pa_find_obj_multi(self.h, len(arr), arr, self._cls_array(cls_list),
                                              len(cls_list), mem))
+        return [self._finish(res, P) for res, P in results]
+
+    def find_obj_queue(self, images, cls_list, want_marg=False, images_per_wave=32,
+                       wait_timeout_ms=20000.0, autotune=True, hold_start=False):
+        """pa_find_obj_queue: as find_obj_multi (CUDA tensors only), the
+        message passing of each wave of images in one persistent launch."""
+        arr, results, mem, keep = self._image_list(images, want_marg)
+        if mem != PA_MEM_DEVICE:
+            raise ValueError("find_obj_queue takes CUDA tensors")
+        o = QueueOpts(int(images_per_wave), float(wait_timeout_ms), int(bool(autotune)),
+                      int(bool(hold_start)))
+        self._check(self.L.pa_find_obj_queue(self.h, len(arr), arr, self._cls_array(cls_list),
+                                             len(cls_list), C.byref(o)))
         return [self._finish(res, P) for res, P in results]
 
     def set_message_math(self, mode):

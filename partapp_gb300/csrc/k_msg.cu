@@ -138,23 +138,23 @@ __host__ __device__ __forceinline__ int align4(int n) { return (n + 3) & ~3; }
 // E[2p+1][col]} (float2), so one 64-bit load feeds both halves of a packed
 // FMA in the x pass.  An odd R gets a zero dummy rotation.
 // ---------------------------------------------------------------------------
+// One tile of the row pass: image row y, column chunk `chunk` of width cw,
+// of message *mdp; kThreadsRows threads; sm: dynamic shared memory of
+// rows_smem<RT>(R, cw, padx).
 template <int RT>
-__global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(const MsgDesc *__restrict__ msgs,
-                                                           int Rrt, int H, int W, int padx,
-                                                           int cw, int *err) {
+__device__ __forceinline__ void rows_tile(const MsgDesc *__restrict__ mdp, int Rrt, int H, int W,
+                                          int padx, int cw, int y, int chunk, int *err, float *sm) {
   const int R = RT > 0 ? RT : Rrt;
   const int RP = (R + 1) / 2;  // rotation pairs
-  const MsgDesc md = msgs[blockIdx.y];
-  const int y = blockIdx.x;
+  const MsgDesc md = *mdp;
   // column chunk [xc0, xc0 + ncw) of the outputs; E holds its columns plus a
   // padx halo on each side (local column lx <-> image column xc0 - padx + lx)
-  const int xc0 = blockIdx.z * cw;
+  const int xc0 = chunk * cw;
   const int ncw = min(cw, W - xc0);
   const int WP = rows_stride(cw, padx);
   const int gx0 = max(0, xc0 - padx), gx1 = min(W, xc0 + ncw + padx);  // gathered columns
   const int lg0 = gx0 - xc0 + padx, lg1 = gx1 - xc0 + padx;            // their local range
   const int gw = gx1 - gx0;
-  extern __shared__ __align__(16) float sm[];
   float2 *E = reinterpret_cast<float2 *>(sm);  // [RP][WP] rotation pairs
   const int xpmax = ((2 * padx + 1 + kU - 1) / kU) * kU;
   float2 *tx = E + ((RP * WP + 1) & ~1);     // x taps {t, t}, zero-padded, 16B aligned
@@ -343,6 +343,14 @@ constexpr int kSmemAlign = 128;
 __device__ __forceinline__ float *smem_align128(float *p) {
   const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
   return p + (((kSmemAlign - (a & (kSmemAlign - 1))) & (kSmemAlign - 1)) >> 2);
+}
+
+template <int RT>
+__global__ void __launch_bounds__(kThreadsRows, RT == 48 ? 1 : 2) k_msg_rows(const MsgDesc *__restrict__ msgs,
+                                                           int Rrt, int H, int W, int padx,
+                                                           int cw, int *err) {
+  extern __shared__ __align__(16) float sm[];
+  rows_tile<RT>(msgs + blockIdx.y, Rrt, H, W, padx, cw, (int)blockIdx.x, (int)blockIdx.z, err, sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -617,6 +625,7 @@ __global__ void __launch_bounds__(kThreadsCols) k_msg_cols(const MsgDesc *__rest
 constexpr int kColWarps = 8;
 constexpr int kColThreads = 32 * kColWarps;
 constexpr int kCBand = 2 * kColWarps * kNO;  // 176 rows: one task of 2 x kNO rows per warp
+static_assert(kCBand == kColBandRows, "column band of the host's tile count");
 constexpr int kCWT = 36;                     // staged columns: 32 + the 16-byte slack
 constexpr int kCBoxRows = 64;                // TMA box height
 constexpr int kFP = 33;                      // pitch of the filtered tile F
@@ -637,20 +646,23 @@ __host__ __device__ __forceinline__ size_t cols_tma_smem(int pady) {
   return (tile > g ? tile : g) * sizeof(float) + kSmemAlign;
 }
 
-__global__ void __launch_bounds__(kColThreads, 2) k_msg_cols_tma(const MsgDesc *__restrict__ msgs,
-                                                              int R, int H, int W, int pady,
-                                                              int *err) {
-  const MsgDesc md = msgs[blockIdx.z];
+// One tile of the column pass: strip bx, (band, rotation) index by of
+// message *mdp (kTX columns x kCBand rows x one rotation); any multiple of
+// 32 threads up to 1024; sm: 128-byte aligned shared memory of
+// cols_tma_smem(pady) (less the alignment slack).  The barriers are
+// invalidated at the end, so that a persistent CTA can run tile after tile.
+__device__ __forceinline__ void cols_tile_tma(const MsgDesc *__restrict__ mdp, int R, int H, int W,
+                                              int pady, int bx, int by, int *err, float *sm) {
+  const MsgDesc md = *mdp;
   if (md.full || md.tc) return;
-  const int r = blockIdx.y % R;
-  const int y0 = (blockIdx.y / R) * kCBand, y1 = min(H, y0 + kCBand);
-  const int x0 = blockIdx.x * kTX, x1 = min(W, x0 + kTX);
-  const bool first_block = blockIdx.x == 0 && blockIdx.y == 0;
-  extern __shared__ __align__(16) float sm_raw[];
-  float *sm = smem_align128(sm_raw);
+  const int r = by % R;
+  const int y0 = (by / R) * kCBand, y1 = min(H, y0 + kCBand);
+  const int x0 = bx * kTX, x1 = min(W, x0 + kTX);
+  const bool first_block = bx == 0 && by == 0;
+  const int nw = blockDim.x >> 5;
   __shared__ int lim[4];
-  __shared__ int red[kColWarps];
-  __shared__ unsigned long long redu[kColWarps];
+  __shared__ int red[32];
+  __shared__ unsigned long long redu[32];
   __shared__ __align__(8) uint64_t bar, bar_src;
   const int4 dxo = md.sdesc[2 * R + r], dyo = md.sdesc[3 * R + r];
   if (!dxo.w || !dyo.w) {  // uniform for the CTA
@@ -712,11 +724,17 @@ __global__ void __launch_bounds__(kColThreads, 2) k_msg_cols_tma(const MsgDesc *
     }
   }
   __syncthreads();
-  if (!s_ok) return;
+  if (!s_ok) {
+    if (tid == 0 && tma_ok) {
+      tc::mbar_inval(&bar);
+      tc::mbar_inval(&bar_src);
+    }
+    return;
+  }
   // y pass: warp w, lane c -> column c, rows [w*kNO, w*kNO + kNO) and the
   // same rows + Dh
   const int ncol = xb - xa;
-  for (int t = warp; t * kNO < Dh; t += kColWarps) {
+  for (int t = warp; t * kNO < Dh; t += nw) {
     const int q0 = t * kNO;
     float2 acc[kNO];
 #pragma unroll
@@ -743,12 +761,23 @@ __global__ void __launch_bounds__(kColThreads, 2) k_msg_cols_tma(const MsgDesc *
       }
     }
   }
-  if (tid == 0 && !tc::mbar_wait_try(&bar_src, 0, err)) {
-    tc::mbar_wait_try(&bar_src, 0, err);  // once more for the copies in flight
-    s_ok = 0;
+  // a second word: a slow warp may still be reading s_ok from the first test
+  __shared__ int s_src_ok;
+  if (tid == 0) {
+    s_src_ok = 1;
+    if (!tc::mbar_wait_try(&bar_src, 0, err)) {
+      tc::mbar_wait_try(&bar_src, 0, err);  // once more for the copies in flight
+      s_src_ok = 0;
+    }
   }
   __syncthreads();
-  if (!s_ok) return;
+  if (!s_src_ok) {
+    if (tid == 0) {
+      tc::mbar_inval(&bar);
+      tc::mbar_inval(&bar_src);
+    }
+    return;
+  }
 
   // epilogue (msg_epilogue's arithmetic for plain shifts), inputs from S0 / S1
   const float M = fkey_decode(*md.in_max);
@@ -763,7 +792,7 @@ __global__ void __launch_bounds__(kColThreads, 2) k_msg_cols_tma(const MsgDesc *
   int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
   unsigned long long am = 0ull;
 #pragma unroll 4
-  for (int yy = y0 + warp; yy < y1; yy += kColWarps) {
+  for (int yy = y0 + warp; yy < y1; yy += nw) {
     if (!colin) continue;
     float m = kLogZero;
     if (colok && yy >= ya && yy < yb) m = __fadd_rn(log_or_zero(F[(yy - ya) * kFP + fc]), M);
@@ -796,11 +825,24 @@ __global__ void __launch_bounds__(kColThreads, 2) k_msg_cols_tma(const MsgDesc *
       __syncthreads();
       if (tid == 0) {
         unsigned long long bm = redu[0];
-        for (int w = 1; w < kColWarps; ++w) bm = redu[w] > bm ? redu[w] : bm;
+        for (int w = 1; w < nw; ++w) bm = redu[w] > bm ? redu[w] : bm;
         atomicMax(md.amax0, bm);
       }
     }
   }
+  __syncthreads();  // the reductions' shared words are read before the next tile
+  if (tid == 0) {
+    tc::mbar_inval(&bar);
+    tc::mbar_inval(&bar_src);
+  }
+}
+
+__global__ void __launch_bounds__(kColThreads, 2) k_msg_cols_tma(const MsgDesc *__restrict__ msgs,
+                                                              int R, int H, int W, int pady,
+                                                              int *err) {
+  extern __shared__ __align__(16) float sm_raw[];
+  cols_tile_tma(msgs + blockIdx.z, R, H, W, pady, (int)blockIdx.x, (int)blockIdx.y, err,
+                smem_align128(sm_raw));
 }
 
 // ---------------------------------------------------------------------------
@@ -1112,8 +1154,8 @@ int rows_chunk(int R, int W, int padx) {
 
 template <int RT>
 cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
-                          int *err, cudaStream_t s) {
-  const int cw = rows_chunk<RT>(R, W, padx);
+                          int *err, cudaStream_t s, int cw_force = 0) {
+  const int cw = cw_force > 0 ? cw_force : rows_chunk<RT>(R, W, padx);
   if (cw <= 0 || (int64_t)R * H * W >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
   const size_t smem = rows_smem<RT>(R, cw, padx);
   cudaFuncSetAttribute(k_msg_rows<RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1122,6 +1164,150 @@ cudaError_t launch_rows_t(const MsgDesc *msgs, int n_msgs, int R, int H, int W, 
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// k_ps_queue: message passing of many images (sizes and rotation counts may
+// differ) in one persistent launch.
+//
+// Every CTA takes the next tile index from a global head (atomicAdd), finds
+// its job (binary search over the jobs' first tiles), waits until the jobs
+// it depends on are complete, runs the tile, and counts it done.  The host
+// orders the jobs so that every dependency points to an earlier job: the
+// upward row and column jobs level by level (post-order), the root
+// combinations, then the downward ones (pre-order).  A CTA waits only for
+// tiles taken before its own, by CTAs that are running and wait only for
+// earlier tiles in turn, so the queue cannot deadlock whatever number of
+// CTAs is resident.  Waits are bounded in time (globaltimer): on expiry the
+// CTA sets status bit 1 and the whole launch stops taking tiles.
+//
+// Memory order: every thread fences its tile's writes before the barrier
+// that precedes the done-count; the waiting thread reads counts with
+// acquire semantics and orders them before the TMA loads of the next tile
+// (fence.proxy.async), which read the maps other CTAs wrote.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// The 48-rotation row tile holds a whole column of 48 values in registers;
+// kept out of line, its register spills stay inside its own tiles.
+__device__ __noinline__ void rows_tile_48(const MsgDesc *md, int H, int W, int padx, int cw, int y,
+                                          int chunk, int *err, float *sm) {
+  rows_tile<48>(md, 48, H, W, padx, cw, y, chunk, err, sm);
+}
+__device__ __noinline__ void rows_tile_any(const MsgDesc *md, int R, int H, int W, int padx,
+                                           int cw, int y, int chunk, int *err, float *sm) {
+  rows_tile<0>(md, R, H, W, padx, cw, y, chunk, err, sm);
+}
+
+__global__ void __launch_bounds__(kQThreads, 2)
+    k_ps_queue(const QJob *__restrict__ jobs, int n_jobs, long long n_items,
+               unsigned long long *head, int *done, int *status, int *err, long long wait_limit_ns) {
+  extern __shared__ __align__(16) float sm_raw[];
+  float *sm = smem_align128(sm_raw);
+  __shared__ long long s_item;
+  __shared__ int s_job, s_stop;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) {
+      s_stop = 0;
+      const long long it = (long long)atomicAdd(head, 1ull);
+      s_item = it;
+      if (it >= n_items || ld_acquire(status) != 0) {
+        s_stop = 1;
+      } else {
+        int lo = 0, hi = n_jobs - 1;  // last job with first <= it
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (jobs[mid].first <= it) lo = mid;
+          else hi = mid - 1;
+        }
+        s_job = lo;
+        const QJob &j = jobs[lo];
+        const unsigned long long t0 = globaltimer_ns();
+        for (int d = 0; d < kQMaxDeps && !s_stop; ++d) {
+          const int dj = j.dep[d];
+          if (dj < 0) continue;
+          const int need = jobs[dj].type == QJOB_GATE ? 1 : jobs[dj].n_items;
+          while (ld_acquire(done + dj) < need) {
+            if (ld_acquire(status) != 0) {
+              s_stop = 1;
+              break;
+            }
+            if ((long long)(globaltimer_ns() - t0) > wait_limit_ns) {
+              atomicOr(status, 1);
+              s_stop = 1;
+              break;
+            }
+            __nanosleep(500);
+          }
+        }
+        asm volatile("fence.proxy.async;" ::: "memory");
+      }
+    }
+    __syncthreads();
+    if (s_stop) break;
+    const QJob &j = jobs[s_job];
+    const int li = (int)(s_item - j.first);
+    if (j.type == QJOB_ROWS) {
+      const int y = li / j.nch, chunk = li - (li / j.nch) * j.nch;
+      switch (j.R) {
+        case 12: rows_tile<12>(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+        case 24: rows_tile<24>(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+        case 48: rows_tile_48(j.md, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+        default: rows_tile_any(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+      }
+    } else if (j.type == QJOB_COLS) {
+      cols_tile_tma(j.md, j.R, j.H, j.W, j.pad, li % j.nch, li / j.nch, err, sm);
+    } else if (j.type == QJOB_ROOT) {
+      const long long c0 = (long long)li * kQRootCells;
+      root_combine_cells(*j.rd, c0, min(j.cells, c0 + kQRootCells), blockDim.x);
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicAdd(done + s_job, 1);
+  }
+}
+
+}  // namespace
+
+size_t ps_queue_smem_rows(int R, int cw, int padx) {
+  switch (R) {
+    case 12: return rows_smem<12>(R, cw, padx) + kSmemAlign;
+    case 24: return rows_smem<24>(R, cw, padx) + kSmemAlign;
+    case 48: return rows_smem<48>(R, cw, padx) + kSmemAlign;
+    default: return rows_smem<0>(R, cw, padx) + kSmemAlign;
+  }
+}
+
+size_t ps_queue_smem_cols(int pady) { return cols_tma_smem(pady); }
+
+cudaError_t launch_ps_queue(const QJob *jobs, int n_jobs, long long n_items, unsigned long long *head,
+                            int *done, int *status, int *err, long long wait_limit_ns, size_t smem,
+                            int *ctas_launched, cudaStream_t s) {
+  if (smem > 227 * 1024 || n_jobs < 1) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_ps_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ps_queue, kQThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  long long grid = (long long)sms * per_sm;
+  if (grid > n_items) grid = n_items > 0 ? n_items : 1;
+  if (ctas_launched) *ctas_launched = (int)grid;
+  k_ps_queue<<<(unsigned)grid, kQThreads, smem, s>>>(jobs, n_jobs, n_items, head, done, status, err,
+                                                      wait_limit_ns);
+  return cudaGetLastError();
+}
+
+namespace {
 }  // namespace
 
 cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,
@@ -1139,6 +1325,17 @@ cudaError_t launch_msg_rows(const MsgDesc *msgs, int n_msgs, int R, int H, int W
     case 24: return launch_rows_t<24>(msgs, n_msgs, R, H, W, padx, err, s);
     case 48: return launch_rows_t<48>(msgs, n_msgs, R, H, W, padx, err, s);
     default: return launch_rows_t<0>(msgs, n_msgs, R, H, W, padx, err, s);
+  }
+}
+
+cudaError_t launch_msg_rows_cw(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
+                               int cw, int *err, cudaStream_t s) {
+  if (cw < 1 || ps_queue_smem_rows(R, cw, padx) > 227 * 1024) return cudaErrorInvalidValue;
+  switch (R) {
+    case 12: return launch_rows_t<12>(msgs, n_msgs, R, H, W, padx, err, s, cw);
+    case 24: return launch_rows_t<24>(msgs, n_msgs, R, H, W, padx, err, s, cw);
+    case 48: return launch_rows_t<48>(msgs, n_msgs, R, H, W, padx, err, s, cw);
+    default: return launch_rows_t<0>(msgs, n_msgs, R, H, W, padx, err, s, cw);
   }
 }
 

@@ -21,60 +21,8 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
 // root marginal (:261-277).
 __global__ void __launch_bounds__(kThreads) k_root_combine(const RootDesc *__restrict__ rds,
                                                            int64_t N) {
-  const RootDesc &rd = rds[blockIdx.y];
-  const int k = rd.k;
-  int keys[kMaxRootChildren];
-#pragma unroll
-  for (int c = 0; c < kMaxRootChildren; ++c) keys[c] = kFkeyNegInf;
-  unsigned long long am = 0ull;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float m[kMaxRootChildren];
-#pragma unroll
-    for (int c = 0; c < kMaxRootChildren; ++c)
-      if (c < k) m[c] = __ldg(rd.msg[c] + i);
-    const float u = __ldg(rd.unary + i);
-    float s = 0.f;
-#pragma unroll
-    for (int c = 0; c < kMaxRootChildren; ++c)
-      if (c < k) s = __fadd_rn(s, m[c]);
-    const float post = __fadd_rn(s, u);
-    rd.post[i] = post;
-    am = umax64(am, akey(post, (uint32_t)i));
-#pragma unroll
-    for (int j = 0; j < kMaxRootChildren; ++j) {
-      if (j >= k) break;
-      float fr = 0.f;
-#pragma unroll
-      for (int c = 0; c < kMaxRootChildren; ++c)
-        if (c < k && c != j) fr = __fadd_rn(fr, m[c]);
-      fr = __fadd_rn(fr, u);
-      rd.from_root[j][i] = fr;
-      keys[j] = max(keys[j], (fr == fr) ? fkey(fr) : kFkeyNegInf);
-    }
-  }
-  __shared__ int skeys[kThreads / 32][kMaxRootChildren];
-  __shared__ unsigned long long sam[kThreads / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < kMaxRootChildren; ++j) {
-    const int v = __reduce_max_sync(0xFFFFFFFFu, keys[j]);
-    if (lane == 0) skeys[warp][j] = v;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) am = umax64(am, __shfl_xor_sync(0xFFFFFFFFu, am, o));
-  if (lane == 0) sam[warp] = am;
-  __syncthreads();
-  if (threadIdx.x < k) {
-    int v = kFkeyNegInf;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = max(v, skeys[w][threadIdx.x]);
-    atomicMax(rd.fr_max[threadIdx.x], v);
-  }
-  if (threadIdx.x == 0 && rd.amax) {
-    unsigned long long b = 0ull;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b = umax64(b, sam[w]);
-    atomicMax(rd.amax, b);
-  }
+  root_combine_cells(rds[blockIdx.y], (int64_t)blockIdx.x * blockDim.x, N,
+                     (int64_t)gridDim.x * blockDim.x);
 }
 
 // Root posterior over the kept rotations (objectdetect_findrot.cpp:694-726):

@@ -90,6 +90,8 @@ struct pa_ctx {
   // run independent image groups of one pa_find_obj_multi call side by side
   static constexpr int kWorkers = 4;
   std::vector<pa_ctx *> workers;
+  // pa_find_obj_queue: measured row-tile width per shape class (R, W, kx)
+  std::map<std::tuple<int, int, int>, int> row_tile;
 };
 
 namespace {
@@ -654,6 +656,8 @@ struct PsPlan {
     MsgDesc *msgs = nullptr;
     int n = 0, padx = 0, pady = 0;
     bool tma = false;  // every message of the phase has TMA maps for the column pass
+    // per message (host): image, child part, x / y kernel half-widths
+    std::vector<int> m_img, m_child, m_kx, m_ky;
     int n_full = 0, ohmax = 0, owmax = 0, kxf = 0, kyf = 0;  // full-covariance messages
     struct TcJob {
       void *eb, *xt, *tbx, *tby;
@@ -663,6 +667,8 @@ struct PsPlan {
     std::vector<TcJob> tc;  // tensor-core messages
   };
   bool tc_mode = false;  // diagonal-covariance messages on the tensor cores (H % 8 == 0)
+  bool own_e2 = false;   // every message its own e2 buffer (messages of different
+                         // phases in flight together: the persistent queue)
   bool sparse_up = false;  // bIsSparse of the upward messages
   // multi-scale computeRootPosteriorRot: batch entry i is scale img_scale[i]
   // (empty: every entry at scale 0)
@@ -769,8 +775,8 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
   size_t maxph = 0;
   for (auto &ph : upph) maxph = std::max(maxph, ph.size());
   for (auto &ph : dnph) maxph = std::max(maxph, ph.size());
-  std::vector<float *> e2(maxph);
-  for (size_t k = 0; k < maxph; ++k) e2[k] = b.scratch<float>(N);
+  std::vector<float *> e2(pl.own_e2 ? 0 : maxph);
+  for (size_t k = 0; k < e2.size(); ++k) e2[k] = b.scratch<float>(N);
   // message parameters; rotated-grid buffers of full-covariance messages are
   // shared by the messages that take slot k in their phase
   auto params_of = [&](const M &mm) {
@@ -836,6 +842,10 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
                          PsPlan::Phase &out) {
     std::vector<MsgDesc> descs(ph.size());
     out.n = (int)ph.size();
+    out.m_img.clear();
+    out.m_child.clear();
+    out.m_kx.clear();
+    out.m_ky.clear();
     out.padx = out.pady = 0;
     out.tc.clear();
     for (size_t k = 0; k < ph.size(); ++k) {
@@ -862,7 +872,11 @@ void plan_ps(Builder &b, PsPlan &pl, const pa_exp_param *e,
       d.rlen = mp.rlen;
       d.xlen = mp.xlen;
       d.ylen = mp.ylen;
-      d.e2 = e2[k];
+      d.e2 = pl.own_e2 ? b.scratch<float>(N) : e2[k];
+      out.m_img.push_back(mm.img);
+      out.m_child.push_back(c);
+      out.m_kx.push_back((mp.xlen - 1) / 2);
+      out.m_ky.push_back((mp.ylen - 1) / 2);
       if (mp.full) {
         d.full = 1;
         d.oh = mp.oh;
@@ -1033,6 +1047,8 @@ void plan_localmax(Builder &b, PsPlan &pl, const pa_exp_param *e, const pa_ps_ou
   pl.lm_scratch = sb ? (void *)b.scratch<char>(sb) : nullptr;
 }
 
+pa_status run_ps_tail(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl);
+
 pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   cudaStream_t st = ctx->stream;
   const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
@@ -1084,6 +1100,16 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
       if (!ph.n) continue;
       if (pa_status s2 = run_phase(ph)) return s2;
     }
+  }
+  return run_ps_tail(ctx, e, pl);
+}
+
+// The PS after the messages: root rotation marginalisation (or the argmax of
+// the unaries without pairwise terms), log-partition, local maxima.
+pa_status run_ps_tail(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
+  cudaStream_t st = ctx->stream;
+  const int B = pl.B, P = pl.P, R = pl.R, H = pl.H, W = pl.W;
+  if (e->use_pairwise) {
     PA_LAUNCH("root_posterior", launch_root_posterior(pl.post_root_ptrs, pl.root_post_ptrs, pl.keep, pl.n_keep, B,
                                     R, H, W, st));
     // leaves without a downward message (a root without children) keep the
@@ -1977,6 +2003,354 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
 // ==========================================================================
 // C-ABI
 // ==========================================================================
+// ------------------------------------------------------------------------
+// pa_find_obj_queue: waves of images, the message passing of a wave in one
+// persistent launch (k_ps_queue).
+// ------------------------------------------------------------------------
+namespace {
+
+struct QGroup {
+  std::vector<int> idx;  // images of the call
+  std::vector<pa_tree> trees;
+  std::vector<pa_ps_outputs> outs;
+  std::vector<const float *> desc;
+  std::vector<std::vector<Joint>> joints;
+  std::vector<float *> marg_out, rp_out;
+  const pa_image *f = nullptr;
+  PsPlan pl;  // the plan of the current pass
+  StumpPart *sp = nullptr;
+  const float *const *fields = nullptr;
+  bool fields_al = true;
+  float *scores = nullptr;
+  UnaryMap *umaps = nullptr;
+  int usep = 0;
+};
+
+// Plans one group (images of one shape) into b; `proto` carries the sizes
+// and flags between the dry and the real pass.
+pa_status plan_queue_group(pa_ctx *ctx, Builder &b, QGroup &g, const PsPlan &proto,
+                           const pa_classifier *const *cls, int n_cls) {
+  const pa_image &f = *g.f;
+  const pa_exp_param *e = f.ep;
+  const int n = (int)g.idx.size(), R = e->num_rotation_steps, P = proto.P;
+  const int64_t G = (int64_t)f.ny * f.nx, n_fields = (int64_t)n * R;
+  g.pl = proto;
+  g.sp = plan_stumps(b, cls, n_cls);
+  std::vector<const float *> fptr;
+  g.fields_al = true;
+  for (int i = 0; i < n; ++i)
+    for (int r = 0; r < R; ++r) {
+      fptr.push_back(g.desc[i] + (size_t)r * G * f.dim);
+      g.fields_al = g.fields_al && ((uintptr_t)fptr.back() & 15) == 0;
+    }
+  g.fields = b.param(fptr.data(), fptr.size());
+  g.scores = b.scratch<float>((size_t)n_cls * n_fields * G);
+  plan_ps(b, g.pl, e, g.joints, g.marg_out.data(), g.rp_out.data());
+  plan_marg_ptrs(b, g.pl);
+  plan_localmax(b, g.pl, e, g.outs.data());
+  std::vector<std::vector<float *>> uouts(n, std::vector<float *>(P, nullptr));
+  for (int i = 0; i < n && !b.dry; ++i)
+    for (int p = 0; p < P; ++p) uouts[i][p] = g.pl.im[i].U[p];
+  return plan_unary(ctx, b, f.Tig, f.tig_shared, n, P, R, f.ny, f.nx, f.H, f.W, !e->interpolate,
+                    g.scores, n_fields, uouts, g.pl.sc.upright, g.pl.sc.root,
+                    e->strip_border_detections, g.pl.umax, e, &g.umaps, 1, &g.usep);
+}
+
+constexpr size_t kQSmemTwo = 112 * 1024;  // two queue CTAs per SM (228 KB less 1 KB each)
+
+// Largest row-tile width (W itself, else a multiple of 352 outputs) whose
+// layout fits `lim` bytes; 0 if none.
+int queue_row_width(int R, int W, int kx, size_t lim) {
+  if (ps_queue_smem_rows(R, W, kx) <= lim) return W;
+  int best = 0;
+  for (int c = 352; c < W; c += 352)
+    if (ps_queue_smem_rows(R, c, kx) <= lim) best = c;
+  return best;
+}
+
+// One wave.  PA_ERR_UNSUPPORTED: a message of the wave needs a path the
+// queue does not run (the caller falls back to grouped launches).
+pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifier *const *cls,
+                     int n_cls, const pa_queue_opts &o) {
+  cudaStream_t s = ctx->stream;
+  std::vector<PsPlan> proto(groups.size());
+  size_t n_jobs_max = 1;  // the gate
+  for (size_t k = 0; k < groups.size(); ++k) {
+    QGroup &g = groups[k];
+    const pa_exp_param *e = g.f->ep;
+    if (!e->use_pairwise) return PA_ERR_UNSUPPORTED;
+    PsPlan &pl = proto[k];
+    pl.tc_mode = false;
+    pl.sparse_up = true;  // findObjectImageRotJoints passes bIsSparse = true
+    pl.own_e2 = true;
+    if (pa_status st = build_sched(ctx, &g.trees[0], pl.sc)) return st;
+    if (pl.sc.ch[pl.sc.root].size() > (size_t)kQMaxDeps) return PA_ERR_UNSUPPORTED;
+    for (size_t i = 1; i < g.trees.size(); ++i)
+      if (!same_topology(&g.trees[0], &g.trees[i]))
+        return fail(ctx, PA_ERR_INVALID, "image %d: tree topology differs", g.idx[i]);
+    pl.B = (int)g.idx.size();
+    pl.P = pl.sc.P;
+    pl.R = e->num_rotation_steps;
+    pl.H = g.f->H;
+    pl.W = g.f->W;
+    pl.N = (int64_t)pl.R * pl.H * pl.W;
+    g.joints.assign(pl.B, {});
+    for (int i = 0; i < pl.B; ++i)
+      if (pa_status st = load_joints(ctx, &g.trees[i], g.f->flip, g.joints[i])) return st;
+    if (n_cls < pl.P) return fail(ctx, PA_ERR_INVALID, "need at least n_parts classifiers");
+    if (pa_status st = check_classifiers(ctx, cls, n_cls, g.f->dim)) return st;
+    n_jobs_max += (size_t)pl.B * (4 * (pl.P - 1) + 1);
+  }
+  // pass 1 (dry), pass 2 (real): every group, then the queue's own words
+  Builder b1;
+  for (size_t k = 0; k < groups.size(); ++k)
+    if (pa_status st = plan_queue_group(ctx, b1, groups[k], proto[k], cls, n_cls)) return st;
+  b1.scratch<QJob>(n_jobs_max);
+  b1.scratch<int>(n_jobs_max);
+  b1.scratch<unsigned long long>(1);
+  b1.scratch<int>(2);
+  if (pa_status st = ensure_arena(ctx, b1.total())) return st;
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  b.base = ctx->arena;
+  for (size_t k = 0; k < groups.size(); ++k)
+    if (pa_status st = plan_queue_group(ctx, b, groups[k], proto[k], cls, n_cls)) return st;
+  QJob *d_jobs = b.scratch<QJob>(n_jobs_max);
+  int *d_done = b.scratch<int>(n_jobs_max);
+  unsigned long long *d_head = b.scratch<unsigned long long>(1);
+  int *d_status = b.scratch<int>(2);
+  if (b.blob.size() != b1.blob.size() || b.scratch_off != b1.scratch_off)
+    return fail(ctx, PA_ERR_INVALID, "internal: plan size mismatch");
+  for (QGroup &g : groups)
+    for (auto *phs : {&g.pl.up, &g.pl.down})
+      for (const PsPlan::Phase &ph : *phs)
+        if (ph.n && (!ph.tma || ph.n_full || !ph.tc.empty())) return PA_ERR_UNSUPPORTED;
+
+  // the jobs, in tree order: upward levels (rows, then columns), the roots,
+  // downward levels
+  std::vector<QJob> jobs;
+  auto blank = []() {
+    QJob j{};
+    for (int d = 0; d < kQMaxDeps; ++d) j.dep[d] = -1;
+    return j;
+  };
+  {
+    QJob gate = blank();
+    gate.type = QJOB_GATE;
+    jobs.push_back(gate);
+  }
+  // key (group, image, child part, 0 up / 1 down, 0 rows / 1 cols) -> job
+  std::map<std::tuple<int, int, int, int, int>, int> job_of;
+  std::map<std::pair<int, int>, int> root_of;
+  int maxd = 0;
+  for (QGroup &g : groups) maxd = std::max(maxd, g.pl.sc.maxdepth);
+  std::vector<std::pair<int, int>> tune_need;  // rows jobs whose width is still to choose
+  auto emit_phase_jobs = [&](bool up, int depth, int kind) {
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      QGroup &g = groups[gi];
+      const PsPlan &pl = g.pl;
+      const auto &phs = up ? pl.up : pl.down;
+      const int k = up ? pl.sc.maxdepth - depth : depth - 1;
+      if (k < 0 || k >= (int)phs.size()) continue;
+      const PsPlan::Phase &ph = phs[k];
+      for (int q = 0; q < ph.n; ++q) {
+        QJob j = blank();
+        j.type = kind == 0 ? QJOB_ROWS : QJOB_COLS;
+        j.md = ph.msgs + q;
+        j.R = pl.R;
+        j.H = pl.H;
+        j.W = pl.W;
+        if (kind == 0) {
+          j.pad = ph.m_kx[q];
+          j.cw = 0;  // chosen below
+        } else {
+          j.pad = ph.m_ky[q];
+          j.nch = (pl.W + kColTileCols - 1) / kColTileCols;
+          j.n_items = j.nch * pl.R * ((pl.H + kColBandRows - 1) / kColBandRows);
+        }
+        job_of[std::make_tuple((int)gi, ph.m_img[q], ph.m_child[q], up ? 0 : 1, kind)] =
+            (int)jobs.size();
+        jobs.push_back(j);
+      }
+    }
+  };
+  for (int d = maxd; d >= 1; --d) {
+    emit_phase_jobs(true, d, 0);
+    emit_phase_jobs(true, d, 1);
+  }
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const PsPlan &pl = groups[gi].pl;
+    for (int i = 0; i < pl.B; ++i) {
+      QJob j = blank();
+      j.type = QJOB_ROOT;
+      j.rd = pl.roots + i;
+      j.cells = pl.N;
+      j.n_items = (int)((pl.N + kQRootCells - 1) / kQRootCells);
+      root_of[{(int)gi, i}] = (int)jobs.size();
+      jobs.push_back(j);
+    }
+  }
+  for (int d = 1; d <= maxd; ++d) {
+    emit_phase_jobs(false, d, 0);
+    emit_phase_jobs(false, d, 1);
+  }
+  // dependencies
+  for (auto &kv : job_of) {
+    const int gi = std::get<0>(kv.first), i = std::get<1>(kv.first), c = std::get<2>(kv.first);
+    const bool up = std::get<3>(kv.first) == 0;
+    const int kind = std::get<4>(kv.first);
+    const Sched &sc = groups[gi].pl.sc;
+    QJob &j = jobs[kv.second];
+    if (kind == 1) {  // columns after the message's rows
+      j.dep[0] = job_of.at(std::make_tuple(gi, i, c, up ? 0 : 1, 0));
+    } else if (up) {  // rows of c -> parent after c's belief is complete
+      if (sc.ch[c].empty()) j.dep[0] = 0;
+      else
+        for (size_t k = 0; k < sc.ch[c].size() && k < (size_t)kQMaxDeps; ++k)
+          j.dep[k] = job_of.at(std::make_tuple(gi, i, sc.ch[c][k], 0, 1));
+    } else {  // rows of parent -> c after the parent's from-root belief
+      int par = -1;
+      for (int p = 0; p < sc.P; ++p)
+        for (int ch : sc.ch[p])
+          if (ch == c) par = p;
+      j.dep[0] = par == sc.root ? root_of.at({gi, i})
+                                : job_of.at(std::make_tuple(gi, i, par, 1, 1));
+    }
+  }
+  for (auto &kv : root_of) {
+    const Sched &sc = groups[kv.first.first].pl.sc;
+    QJob &j = jobs[kv.second];
+    if (sc.ch[sc.root].empty()) j.dep[0] = 0;
+    for (size_t k = 0; k < sc.ch[sc.root].size(); ++k)
+      j.dep[k] = job_of.at(std::make_tuple(kv.first.first, kv.first.second, sc.ch[sc.root][k], 0, 1));
+  }
+
+  // unaries of every group (the inputs of the first messages)
+  if (pa_status st = upload_blob(ctx, b)) return st;
+  for (QGroup &g : groups) {
+    const pa_image &f = *g.f;
+    const int n = (int)g.idx.size(), R = g.pl.R;
+    const int64_t G = (int64_t)f.ny * f.nx, n_fields = (int64_t)n * R;
+    if (pa_status st = init_slots(ctx, g.pl)) return st;
+    const std::vector<char> ff = fast_flags(cls, n_cls);
+    const std::vector<int> ns = stump_counts(cls, n_cls);
+    PA_LAUNCH("score_grids", launch_score_grids(g.sp, (const bool *)ff.data(), ns.data(), n_cls,
+                                                g.desc[0], g.fields, g.fields_al, G, (int)n_fields,
+                                                f.dim, 1, g.scores, s));
+    PA_LAUNCH_N("unary_maps", f.ep->interpolate ? 1 : 2,
+                launch_unary_maps(g.umaps, n * g.pl.P * R, f.ny, f.nx, f.H, f.W,
+                                  !f.ep->interpolate, g.usep, s));
+    if (g.pl.n_msgs_total > 0)
+      PA_LAUNCH_N("shift_tables", 2,
+                  launch_shift_tables(g.pl.shifts, g.pl.n_msgs_total, R, f.H, f.W, g.pl.tables,
+                                      g.pl.sdesc, s));
+  }
+
+  // row-tile widths: measured once per shape class (R, W, kx) on a message
+  // whose input (a leaf's unary) is ready, among the widths that fit
+  std::vector<std::pair<int, int>> cls_job;  // first leaf-upward rows job of each new class
+  for (auto &kv : job_of) {
+    if (std::get<4>(kv.first) != 0) continue;
+    QJob &j = jobs[kv.second];
+    const auto key = std::make_tuple(j.R, j.W, j.pad);
+    auto it = ctx->row_tile.find(key);
+    if (it != ctx->row_tile.end()) {
+      j.cw = it->second;
+      continue;
+    }
+    const bool leaf_up = std::get<3>(kv.first) == 0 && j.dep[0] == 0;
+    if (o.autotune && leaf_up) {
+      bool have = false;
+      for (auto &cj : cls_job)
+        if (jobs[cj.second].R == j.R && jobs[cj.second].W == j.W && jobs[cj.second].pad == j.pad) have = true;
+      if (!have) cls_job.push_back({0, kv.second});
+    }
+  }
+  cudaEvent_t t0 = take_event(ctx), t1 = take_event(ctx);
+  for (auto &cj : cls_job) {
+    const QJob &j = jobs[cj.second];
+    std::vector<int> cand;
+    for (size_t lim : {kQSmemTwo, (size_t)227 * 1024}) {
+      for (int c : {j.W, 704, 352})
+        if (c <= j.W && ps_queue_smem_rows(j.R, c, j.pad) <= lim &&
+            std::find(cand.begin(), cand.end(), c) == cand.end())
+          cand.push_back(c);
+      if (!cand.empty()) break;
+    }
+    int best = 0;
+    float best_ms = 0.f;
+    for (int c : cand) {
+      for (int rep = 0; rep < 2; ++rep) {
+        PA_CK(cudaEventRecord(t0, s));
+        PA_CK(launch_msg_rows_cw(j.md, 1, j.R, j.H, j.W, j.pad, c, groups[0].pl.err, s));
+        PA_CK(cudaEventRecord(t1, s));
+      }
+      PA_CK(cudaEventSynchronize(t1));
+      float ms = 0.f;
+      PA_CK(cudaEventElapsedTime(&ms, t0, t1));
+      if (!best || ms < best_ms) {
+        best = c;
+        best_ms = ms;
+      }
+    }
+    if (best) ctx->row_tile[std::make_tuple(j.R, j.W, j.pad)] = best;
+  }
+  ctx->pool.push_back(t0);
+  ctx->pool.push_back(t1);
+  size_t smem = 0;
+  for (auto &kv : job_of) {
+    QJob &j = jobs[kv.second];
+    if (std::get<4>(kv.first) == 0) {
+      if (!j.cw) {
+        auto it = ctx->row_tile.find(std::make_tuple(j.R, j.W, j.pad));
+        j.cw = it != ctx->row_tile.end() ? it->second : queue_row_width(j.R, j.W, j.pad, kQSmemTwo);
+        if (!j.cw) j.cw = queue_row_width(j.R, j.W, j.pad, (size_t)227 * 1024);
+        if (!j.cw) return PA_ERR_UNSUPPORTED;
+      }
+      j.nch = (j.W + j.cw - 1) / j.cw;
+      j.n_items = j.H * j.nch;
+      smem = std::max(smem, ps_queue_smem_rows(j.R, j.cw, j.pad));
+    } else {
+      smem = std::max(smem, ps_queue_smem_cols(j.pad));
+    }
+  }
+  long long n_items = 0;
+  for (QJob &j : jobs) {
+    j.first = n_items;
+    n_items += j.n_items;
+  }
+  if (jobs.size() > n_jobs_max) return fail(ctx, PA_ERR_INVALID, "internal: job count");
+  if (pa_status st = upload_to(ctx, d_jobs, jobs.data(), jobs.size() * sizeof(QJob))) return st;
+  PA_CK(cudaMemsetAsync(d_done, 0, jobs.size() * sizeof(int), s));
+  PA_CK(cudaMemsetAsync(d_head, 0, sizeof(unsigned long long), s));
+  PA_CK(cudaMemsetAsync(d_status, 0, 2 * sizeof(int), s));
+  // the host opens the start gate (the jobs of the leaves wait for it)
+  if (!o.hold_start) PA_LAUNCH("fill", launch_fill_int(d_done, 1, 1, s));
+  const long long wait_ns =
+      (long long)((o.wait_timeout_ms > 0 ? o.wait_timeout_ms : 20000.0) * 1e6);
+  int ctas = 0;
+  PA_LAUNCH("ps_queue", launch_ps_queue(d_jobs, (int)jobs.size(), n_items, d_head, d_done, d_status,
+                                        groups[0].pl.err, wait_ns, smem, &ctas, s));
+  int status = 0;
+  PA_CK(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PA_CK(cudaStreamSynchronize(s));
+  if (status & 1) return fail(ctx, PA_ERR_TIMEOUT, "a queue dependency wait ran out (%.0f ms)",
+                              o.wait_timeout_ms > 0 ? o.wait_timeout_ms : 20000.0);
+  // a tile's error bits went to the first group's word: carry them to all
+  int err0 = 0;
+  PA_CK(cudaMemcpyAsync(&err0, groups[0].pl.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PA_CK(cudaStreamSynchronize(s));
+  for (QGroup &g : groups) {
+    if (err0 && &g != &groups[0]) PA_LAUNCH("fill", launch_fill_int(g.pl.err, err0, 1, s));
+    if (pa_status st = run_ps_tail(ctx, g.f->ep, g.pl)) return st;
+    if (pa_status st = finish_ps(ctx, g.f->ep, g.pl, g.outs.data(), PA_MEM_DEVICE)) return st;
+  }
+  return PA_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *pa_status_string(pa_status s) {
@@ -1987,6 +2361,7 @@ const char *pa_status_string(pa_status s) {
     case PA_ERR_CUDA: return "CUDA error";
     case PA_ERR_NOMEM: return "out of memory";
     case PA_ERR_NUMERIC: return "numeric overflow";
+    case PA_ERR_TIMEOUT: return "device wait timed out";
     default: return "unknown status";
   }
 }
@@ -3383,6 +3758,80 @@ pa_status pa_find_obj_multi(pa_ctx *ctx, int n_images, const pa_image *imgs,
                          (int64_t)n * f.ep->num_rotation_steps, outs.data(), mem);
     if (st && st != PA_ERR_NUMERIC) return st;
     if (st) result = st;
+  }
+  return result;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
+}
+
+void pa_queue_opts_default(pa_queue_opts *o) {
+  if (!o) return;
+  o->images_per_wave = 32;
+  o->wait_timeout_ms = 20000.0;
+  o->autotune = 1;
+  o->hold_start = 0;
+}
+
+pa_status pa_find_obj_queue(pa_ctx *ctx, int n_images, const pa_image *imgs,
+                            const pa_classifier *const *cls, int n_cls,
+                            const pa_queue_opts *opts) try {
+  if (!ctx) return PA_ERR_INVALID;
+  if (n_images < 0 || (n_images > 0 && (!imgs || !cls || n_cls < 1)))
+    return fail(ctx, PA_ERR_INVALID, "invalid image list");
+  pa_queue_opts o;
+  pa_queue_opts_default(&o);
+  if (opts) o = *opts;
+  if (o.images_per_wave < 1) o.images_per_wave = 32;
+  for (int i = 0; i < n_images; ++i) {
+    const pa_image &im = imgs[i];
+    if (!im.ep || !exp_ok(im.ep) || !im.tree || !im.desc || !im.Tig || !im.out || im.ny < 1 ||
+        im.nx < 1 || im.dim < 1 || im.H < 1 || im.W < 1 || im.H > 32767 || im.W > 32767)
+      return fail(ctx, PA_ERR_INVALID, "image %d: invalid sizes, parameters or NULL input", i);
+    if (n_scales(im.ep) != 1)
+      return fail(ctx, PA_ERR_UNSUPPORTED, "image %d: one scale of descriptors per image", i);
+  }
+  auto same = [&](const pa_image &a, const pa_image &b) {
+    if (std::memcmp(a.ep, b.ep, sizeof(pa_exp_param)) != 0) return false;
+    if (a.flip != b.flip || a.ny != b.ny || a.nx != b.nx || a.dim != b.dim || a.H != b.H ||
+        a.W != b.W || !a.tig_shared || !b.tig_shared)
+      return false;
+    return std::memcmp(a.Tig, b.Tig, 9 * sizeof(double)) == 0 && same_topology(a.tree, b.tree);
+  };
+  DeviceGuard dg(ctx->device);
+  pa_status result = PA_OK;
+  for (int w0 = 0; w0 < n_images; w0 += o.images_per_wave) {
+    const int w1 = std::min(n_images, w0 + o.images_per_wave);
+    std::vector<QGroup> groups;
+    std::vector<int> grp(w1 - w0, -1);
+    for (int i = w0; i < w1; ++i) {
+      if (grp[i - w0] >= 0) continue;
+      grp[i - w0] = (int)groups.size();
+      groups.emplace_back();
+      for (int j = i + 1; j < w1; ++j)
+        if (grp[j - w0] < 0 && same(imgs[i], imgs[j])) grp[j - w0] = grp[i - w0];
+    }
+    for (int i = w0; i < w1; ++i) {
+      QGroup &g = groups[grp[i - w0]];
+      if (!g.f) g.f = &imgs[i];
+      g.idx.push_back(i);
+      g.trees.push_back(*imgs[i].tree);
+      g.outs.push_back(*imgs[i].out);
+      g.desc.push_back(imgs[i].desc);
+      g.marg_out.push_back(imgs[i].out->log_marg);
+      g.rp_out.push_back(imgs[i].out->root_post);
+    }
+    pa_status st = queue_wave(ctx, groups, cls, n_cls, o);
+    if (st == PA_ERR_UNSUPPORTED) {
+      // a path the queue does not run: this wave as pa_find_obj_multi does it
+      st = pa_find_obj_multi(ctx, w1 - w0, imgs + w0, cls, n_cls, PA_MEM_DEVICE);
+    }
+    if (st == PA_ERR_NUMERIC) {
+      result = st;
+      continue;
+    }
+    if (st) return st;
   }
   return result;
 } catch (const std::bad_alloc &) {

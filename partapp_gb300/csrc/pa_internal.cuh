@@ -190,6 +190,112 @@ struct RootDesc {
   unsigned long long *amax;
 };
 
+// Root of the tree.  In computeRootPosteriorRot (libPictStruct/
+// objectdetect_findrot.cpp:630-654) every message from a root child is added
+// into post[root] and into log_from_root of every *other* root child, in
+// joint order, starting from zero-initialised grids; then the root unary is
+// added to post[root], and computePartMarginals (:163-165) adds it to each
+// log_from_root.  This performs those sums element-wise in that order on the
+// cells first + threadIdx.x + k * stride < N of one block, and folds the
+// maxima that the downward messages need and the argmax of the root marginal
+// (:261-277) into the descriptor's words (one atomic per block and word).
+__device__ __forceinline__ void root_combine_cells(const RootDesc &rd, int64_t first, int64_t N,
+                                                   int64_t stride) {
+  const int k = rd.k;
+  int keys[kMaxRootChildren];
+#pragma unroll
+  for (int c = 0; c < kMaxRootChildren; ++c) keys[c] = kFkeyNegInf;
+  unsigned long long am = 0ull;
+  for (int64_t i = first + threadIdx.x; i < N; i += stride) {
+    float m[kMaxRootChildren];
+#pragma unroll
+    for (int c = 0; c < kMaxRootChildren; ++c)
+      if (c < k) m[c] = __ldg(rd.msg[c] + i);
+    const float u = __ldg(rd.unary + i);
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kMaxRootChildren; ++c)
+      if (c < k) s = __fadd_rn(s, m[c]);
+    const float post = __fadd_rn(s, u);
+    rd.post[i] = post;
+    const unsigned long long ak = akey(post, (uint32_t)i);
+    am = ak > am ? ak : am;
+#pragma unroll
+    for (int j = 0; j < kMaxRootChildren; ++j) {
+      if (j >= k) break;
+      float fr = 0.f;
+#pragma unroll
+      for (int c = 0; c < kMaxRootChildren; ++c)
+        if (c < k && c != j) fr = __fadd_rn(fr, m[c]);
+      fr = __fadd_rn(fr, u);
+      rd.from_root[j][i] = fr;
+      keys[j] = max(keys[j], (fr == fr) ? fkey(fr) : kFkeyNegInf);
+    }
+  }
+  __shared__ int skeys[32][kMaxRootChildren];
+  __shared__ unsigned long long sam[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int j = 0; j < kMaxRootChildren; ++j) {
+    const int v = __reduce_max_sync(0xFFFFFFFFu, keys[j]);
+    if (lane == 0) skeys[warp][j] = v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xFFFFFFFFu, am, o);
+    am = w > am ? w : am;
+  }
+  if (lane == 0) sam[warp] = am;
+  __syncthreads();
+  if ((int)threadIdx.x < k) {
+    int v = kFkeyNegInf;
+    for (int w = 0; w < nw; ++w) v = max(v, skeys[w][threadIdx.x]);
+    atomicMax(rd.fr_max[threadIdx.x], v);
+  }
+  if (threadIdx.x == 0 && rd.amax) {
+    unsigned long long b = 0ull;
+    for (int w = 0; w < nw; ++w) b = sam[w] > b ? sam[w] : b;
+    atomicMax(rd.amax, b);
+  }
+  __syncthreads();  // the shared words are read before they are reused
+}
+
+// ---------------------------------------------------------------------------
+// Persistent message passing (k_ps_queue, k_msg.cu): the row and column
+// tiles of every message and the root combinations of many images, drained
+// from one device work queue.  A job is a set of independent tiles; a job
+// may start when each job in `dep` has completed all its tiles.
+// ---------------------------------------------------------------------------
+enum QJobType { QJOB_ROWS = 0, QJOB_COLS = 1, QJOB_ROOT = 2, QJOB_GATE = 3 };
+constexpr int kQMaxDeps = 8;
+struct QJob {
+  int type;
+  int n_items;               // tiles (0 for the gate: it is opened by the host)
+  int dep[kQMaxDeps];        // job indices, -1: none
+  const MsgDesc *md;         // rows / cols
+  const RootDesc *rd;        // root
+  int R, H, W;
+  int pad;                   // rows: padx of the tile layout; cols: pady
+  int cw;                    // rows: column chunk width
+  int nch;                   // rows: column chunks per image row; cols: strips
+  long long cells;           // root: N; its tiles cover kQRootCells cells each
+  long long first;           // global index of the job's first tile
+};
+constexpr int kQRootCells = 384 * 64;
+constexpr int kColBandRows = 176;  // rows of one column-pass tile (kTX columns x one rotation)
+constexpr int kColTileCols = 32;
+// The row pass with a given column chunk width (the queue's autotuner).
+cudaError_t launch_msg_rows_cw(const MsgDesc *msgs, int n_msgs, int R, int H, int W, int padx,
+                               int cw, int *err, cudaStream_t s);
+constexpr int kQThreads = 384;
+// status bits of k_ps_queue: 1 = a dependency wait ran out (the queue was
+// abandoned)
+size_t ps_queue_smem_rows(int R, int cw, int padx);
+size_t ps_queue_smem_cols(int pady);
+cudaError_t launch_ps_queue(const QJob *jobs, int n_jobs, long long n_items, unsigned long long *head,
+                            int *done, int *status, int *err, long long wait_limit_ns, size_t smem,
+                            int *ctas_launched, cudaStream_t s);
+
 // Host-side parameters of one computeRotJointMarginal(child -> parent,
 // offset_c_10 = oc, offset_p_01 = op, rot_mean, rot_sigma): rotation-mean bin
 // shift, clipped rotation taps, spatial taps and the per-rotation shift

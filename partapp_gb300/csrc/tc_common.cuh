@@ -21,6 +21,12 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
                : "memory");
 }
 
+// Ends the barrier's life (no thread may still wait on it); the memory can
+// then hold a new barrier.
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
