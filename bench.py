@@ -56,6 +56,10 @@ def parse():
                          "sigma 4-24 px), FP32 and BF16 tensor-core message arithmetic; "
                          "uneven: images of random sizes (200-640 px) and rotation counts "
                          "(12/24/48) through pa_find_obj_multi, throughput and latency spread")
+    ap.add_argument("--uneven-images", type=int, default=256,
+                    help="uneven: images per call")
+    ap.add_argument("--images-per-wave", type=int, default=32,
+                    help="uneven: images per persistent message-passing launch")
     ap.add_argument("--learned", type=int, default=1,
                     help="find_obj: add the learned-vs-plain comparison (320x240, R=24)")
     ap.add_argument("--train-fields", type=int, default=20000)
@@ -563,8 +567,16 @@ def run_uneven(args):
     """find_obj over images of uneven sizes and rotation counts: heights and
     widths ~ U{200..640} rounded to multiples of 4, R in {12, 24, 48}, 10
     classifiers of 500 stumps over 960-d descriptors at stride 4, per-image
-    pairwise terms.  Throughput of one pa_find_obj_multi call over all images
-    (descriptors resident in HBM) and the latency spread of one-image calls."""
+    pairwise terms (offsets U(10, 60) px, sigma U(2, 12) px).
+
+    Calls of --uneven-images images (256) with the descriptors resident in
+    HBM, timed call by call: through pa_find_obj_queue (the message passing of
+    each wave of --images-per-wave images in one persistent launch) and through
+    pa_find_obj_multi (one launch per message group).  256 such images would
+    need ~300 GB of descriptors side by side, so each image's descriptors are
+    a view at a seeded offset into one 12 GB pool of Gamma(0.5, 1) rows,
+    L2-normalised per location (the inputs are larger than L2).  Also the
+    latency spread of one-image calls over the first 32 images."""
     import torch
 
     import partapp_gb300 as pa
@@ -575,36 +587,54 @@ def run_uneven(args):
     ctx = pa.Context(0)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
-    n = max(4, 8 * args.batch)
+    n = max(1, args.uneven_images)
     rng = np.random.default_rng(args.seed)
     models = synth.make_models(rng, n_parts=P, n_stumps=N_STUMPS, D=D)
     cls = ctx.classifiers(models)
     g = torch.Generator(device=dev)
     g.manual_seed(args.seed)
+    pool_rows = 3 << 20
+    pool = torch.empty((pool_rows, D), device=dev)
+    for r0 in range(0, pool_rows, 1 << 18):
+        z = pool[r0:r0 + (1 << 18)]
+        z.normal_(generator=g)
+        z.mul_(z).mul_(0.5)
+        z.div_(torch.linalg.vector_norm(z, dim=-1, keepdim=True))
     images = []
     for i in range(n):
         Hi = int(rng.integers(200, 641)) // 4 * 4
         Wi = int(rng.integers(200, 641)) // 4 * 4
         Ri = int(rng.choice([12, 24, 48]))
-        z = torch.randn((Ri, Hi // STRIDE, Wi // STRIDE, D), generator=g, device=dev)
-        z.mul_(z).mul_(0.5)
-        z.div_(torch.linalg.vector_norm(z, dim=-1, keepdim=True))
+        rows = Ri * (Hi // STRIDE) * (Wi // STRIDE)
+        off = int(rng.integers(0, pool_rows - rows + 1))
+        desc = pool[off:off + rows].view(Ri, Hi // STRIDE, Wi // STRIDE, D)
         tree = synth.make_tree(rng, R=Ri, offset_range=(10.0, 60.0), sigma_range=(2.0, 12.0))
-        images.append(dict(exp=pa.exp_param(R=Ri, interpolate=True), tree=tree, desc=z,
+        images.append(dict(exp=pa.exp_param(R=Ri, interpolate=True), tree=tree, desc=desc,
                            Tig=synth.grid_to_image(STRIDE), H=Hi, W=Wi))
-    for _ in range(max(1, min(args.warmup, 2))):
-        ctx.find_obj_multi(images, cls)
-    torch.cuda.synchronize(dev)
-    steps = max(1, args.steps // 10)
-    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for _ in range(steps):
-        ctx.find_obj_multi(images, cls)
-    t1.record(stream)
-    torch.cuda.synchronize(dev)
-    ms = t0.elapsed_time(t1) / steps
+    calls = max(5, args.steps // 4)
+
+    def timed(fn):
+        for _ in range(max(1, min(args.warmup, 3))):
+            fn()
+        torch.cuda.synchronize(dev)
+        ms = []
+        for _ in range(calls):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms.append(a.elapsed_time(b))
+        ms = np.array(ms)
+        return {"images_per_s": n / (ms.mean() / 1e3), "ms_per_call_mean": float(ms.mean()),
+                "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                "max_ms": float(ms.max()), "calls": calls}
+
+    with ClockSampler(0) as clk_q:
+        queue = timed(lambda: ctx.find_obj_queue(images, cls, images_per_wave=args.images_per_wave))
+    grouped = timed(lambda: ctx.find_obj_multi(images, cls))
     lat = []
-    for im in images:
+    for im in images[:32]:
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         ctx.find_obj(im["exp"], im["tree"], cls, im["desc"], im["Tig"], im["H"], im["W"])
@@ -612,16 +642,24 @@ def run_uneven(args):
         torch.cuda.synchronize(dev)
         lat.append(a.elapsed_time(b))
     lat = np.array(lat)
-    pix = [im["H"] * im["W"] * im["exp"].num_rotation_steps for im in images]
+    cells = [im["H"] * im["W"] * im["exp"].num_rotation_steps for im in images]
     line = {"metric": "images/s (uneven sizes and rotation counts)", "unit": "images/s",
-            "value": n / (ms / 1e3), "ms_per_call": ms, "images_per_call": n, "n_gpus": 1,
-            "steps": steps, "higher_is_better": True, "data": "synthetic", "dtype": "f32",
-            "config": {"workload": "find_obj, H, W ~ U{200..640}/4*4, R in {12,24,48}, "
-                                   "10 classifiers x 500 stumps, 960-d, 10-part PS"},
+            "value": queue["images_per_s"], "ms_per_step": queue["ms_per_call_mean"],
+            "images_per_call": n, "n_gpus": 1, "steps": calls, "warmup": max(1, min(args.warmup, 3)),
+            "higher_is_better": True, "scaling": "replicas only", "vs_baseline": None,
+            "data": "synthetic", "dtype": "f32",
+            "config": {"workload": f"find_obj, {n} images per call, H, W ~ U{{200..640}}/4*4, "
+                                   "R in {12,24,48}, 10 classifiers x 500 stumps, 960-d, 10-part PS",
+                       "images_per_wave": args.images_per_wave,
+                       "l2": "inputs larger than L2 (12 GB descriptor pool)"},
+            "queue": queue, "grouped_launches": grouped,
             "latency_ms_one_image": {"p50": float(np.percentile(lat, 50)),
-                                     "p90": float(np.percentile(lat, 90)),
-                                     "max": float(lat.max()), "min": float(lat.min())},
-            "cells_per_image": {"min": int(min(pix)), "max": int(max(pix))}}
+                                     "p99": float(np.percentile(lat, 99)),
+                                     "max": float(lat.max()), "min": float(lat.min()),
+                                     "images": int(lat.size)},
+            "cells_per_image": {"min": int(min(cells)), "max": int(max(cells)),
+                                "mean": float(np.mean(cells))},
+            "clocks": clk_q.summary()}
     print(json.dumps(line), flush=True)
     ctx.close()
 

@@ -1206,72 +1206,116 @@ __device__ __noinline__ void rows_tile_any(const MsgDesc *md, int R, int H, int 
   rows_tile<0>(md, R, H, W, padx, cw, y, chunk, err, sm);
 }
 
+__device__ __forceinline__ int ld_relaxed(const int *p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// One tile t of job j.
+__device__ __forceinline__ void ps_queue_tile(const QJob &j, int t, int *err, float *sm) {
+  if (j.type == QJOB_ROWS) {
+    const int y = t / j.nch, chunk = t - (t / j.nch) * j.nch;
+    switch (j.R) {
+      case 12: rows_tile<12>(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+      case 24: rows_tile<24>(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+      case 48: rows_tile_48(j.md, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+      default: rows_tile_any(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
+    }
+  } else if (j.type == QJOB_COLS) {
+    cols_tile_tma(j.md, j.R, j.H, j.W, j.pad, t % j.nch, t / j.nch, err, sm);
+  } else if (j.type == QJOB_ROOT) {
+    const long long c0 = (long long)t * kQRootCells;
+    root_combine_cells<kQMaxDeps, 4>(*j.rd, c0, min(j.cells, c0 + kQRootCells), blockDim.x);
+  }
+}
+
 __global__ void __launch_bounds__(kQThreads, 2)
     k_ps_queue(const QJob *__restrict__ jobs, int n_jobs, long long n_items,
-               unsigned long long *head, int *done, int *status, int *err, long long wait_limit_ns) {
+               unsigned long long *head, int *done, int *status, int *err, long long wait_limit_ns,
+               unsigned long long *stats) {
   extern __shared__ __align__(16) float sm_raw[];
   float *sm = smem_align128(sm_raw);
   __shared__ long long s_item;
   __shared__ int s_job, s_stop;
   const int tid = threadIdx.x;
+  // thread 0's state: the job of its last item (a CTA's items only grow, so
+  // the next job is found by a short forward scan) and the last job whose
+  // dependencies it saw complete (completion is never undone)
+  int last_job = 0, ready_job = -1;
+  unsigned long long t_take = 0, t_found = 0, t_ready = 0;
   for (;;) {
     if (tid == 0) {
       s_stop = 0;
+      if (stats) t_take = globaltimer_ns();
+      const int st0 = ld_relaxed(status);
       const long long it = (long long)atomicAdd(head, 1ull);
       s_item = it;
-      if (it >= n_items || ld_acquire(status) != 0) {
+      if (it >= n_items || st0 != 0) {
         s_stop = 1;
       } else {
-        int lo = 0, hi = n_jobs - 1;  // last job with first <= it
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (jobs[mid].first <= it) lo = mid;
-          else hi = mid - 1;
-        }
-        s_job = lo;
-        const QJob &j = jobs[lo];
-        const unsigned long long t0 = globaltimer_ns();
-        for (int d = 0; d < kQMaxDeps && !s_stop; ++d) {
-          const int dj = j.dep[d];
-          if (dj < 0) continue;
-          const int need = jobs[dj].type == QJOB_GATE ? 1 : jobs[dj].n_items;
-          while (ld_acquire(done + dj) < need) {
-            if (ld_acquire(status) != 0) {
-              s_stop = 1;
-              break;
-            }
-            if ((long long)(globaltimer_ns() - t0) > wait_limit_ns) {
-              atomicOr(status, 1);
-              s_stop = 1;
-              break;
-            }
-            __nanosleep(500);
+        int lo = last_job;
+        for (int k = 0; k < 8 && lo + 1 < n_jobs && jobs[lo + 1].first <= it; ++k) ++lo;
+        if (lo + 1 < n_jobs && jobs[lo + 1].first <= it) {  // far ahead: bisect
+          int hi = n_jobs - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (jobs[mid].first <= it) lo = mid;
+            else hi = mid - 1;
           }
         }
-        asm volatile("fence.proxy.async;" ::: "memory");
+        last_job = lo;
+        s_job = lo;
+        if (stats) t_found = globaltimer_ns();
+        if (lo != ready_job) {
+          const QJob &j = jobs[lo];
+          const unsigned long long t0 = globaltimer_ns();
+          for (int d = 0; d < kQMaxDeps && !s_stop; ++d) {
+            const int dj = j.dep[d];
+            if (dj < 0) continue;
+            const int need = jobs[dj].type == QJOB_GATE ? 1 : jobs[dj].n_items;
+            while (ld_acquire(done + dj) < need) {
+              if (ld_acquire(status) != 0) {
+                s_stop = 1;
+                break;
+              }
+              if ((long long)(globaltimer_ns() - t0) > wait_limit_ns) {
+                atomicOr(status, 1);
+                s_stop = 1;
+                break;
+              }
+              __nanosleep(256);
+            }
+          }
+          asm volatile("fence.proxy.async;" ::: "memory");
+          if (!s_stop) ready_job = lo;
+        }
+        if (stats) t_ready = globaltimer_ns();
       }
     }
     __syncthreads();
     if (s_stop) break;
     const QJob &j = jobs[s_job];
-    const int li = (int)(s_item - j.first);
-    if (j.type == QJOB_ROWS) {
-      const int y = li / j.nch, chunk = li - (li / j.nch) * j.nch;
-      switch (j.R) {
-        case 12: rows_tile<12>(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
-        case 24: rows_tile<24>(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
-        case 48: rows_tile_48(j.md, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
-        default: rows_tile_any(j.md, j.R, j.H, j.W, j.pad, j.cw, y, chunk, err, sm); break;
-      }
-    } else if (j.type == QJOB_COLS) {
-      cols_tile_tma(j.md, j.R, j.H, j.W, j.pad, li % j.nch, li / j.nch, err, sm);
-    } else if (j.type == QJOB_ROOT) {
-      const long long c0 = (long long)li * kQRootCells;
-      root_combine_cells(*j.rd, c0, min(j.cells, c0 + kQRootCells), blockDim.x);
+    const int c = (int)(s_item - j.first);
+    const int t1 = min(j.tiles, (c + 1) * j.per);
+    for (int t = c * j.per; t < t1; ++t) {
+      ps_queue_tile(j, t, err, sm);
+      __syncthreads();  // the tile's shared memory is read before the next one writes it
     }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) atomicAdd(done + s_job, 1);
+    // release: the barrier above orders every thread's writes before thread
+    // 0's fence and count (the pattern of a grid-wide barrier)
+    if (tid == 0) {
+      __threadfence();
+      atomicAdd(done + s_job, 1);
+      if (stats) {  // per job type (slot 3: rows of 48 rotations): take + find, wait, run, tiles
+        unsigned long long *st = stats + 4 * (j.type == QJOB_ROWS && j.R == 48 ? 3 : j.type);
+        const unsigned long long t_end = globaltimer_ns();
+        atomicAdd(st + 0, t_found - t_take);
+        atomicAdd(st + 1, t_ready - t_found);
+        atomicAdd(st + 2, t_end - t_ready);
+        atomicAdd(st + 3, (unsigned long long)(t1 - c * j.per));
+      }
+    }
   }
 }
 
@@ -1290,7 +1334,7 @@ size_t ps_queue_smem_cols(int pady) { return cols_tma_smem(pady); }
 
 cudaError_t launch_ps_queue(const QJob *jobs, int n_jobs, long long n_items, unsigned long long *head,
                             int *done, int *status, int *err, long long wait_limit_ns, size_t smem,
-                            int *ctas_launched, cudaStream_t s) {
+                            int *ctas_launched, unsigned long long *stats, cudaStream_t s) {
   if (smem > 227 * 1024 || n_jobs < 1) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_ps_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -1303,7 +1347,7 @@ cudaError_t launch_ps_queue(const QJob *jobs, int n_jobs, long long n_items, uns
   if (grid > n_items) grid = n_items > 0 ? n_items : 1;
   if (ctas_launched) *ctas_launched = (int)grid;
   k_ps_queue<<<(unsigned)grid, kQThreads, smem, s>>>(jobs, n_jobs, n_items, head, done, status, err,
-                                                      wait_limit_ns);
+                                                      wait_limit_ns, stats);
   return cudaGetLastError();
 }
 

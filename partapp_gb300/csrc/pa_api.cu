@@ -62,7 +62,9 @@ struct pa_ctx {
     size_t cap = 0;
   };
   static constexpr int kLandings = 3;
-  Landing land[kLandings];
+  std::vector<Landing> land = std::vector<Landing>(kLandings);  // grown by pa_find_obj_queue
+  // pa_find_obj_queue: side streams of the per-image work around the queue
+  std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> ring_done;  // per ring slot: the slot's image is computed
   // host-input ring: descriptor slots filled on copy_stream while the main
   // stream computes on the previous slot
@@ -2109,6 +2111,7 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
   b1.scratch<int>(n_jobs_max);
   b1.scratch<unsigned long long>(1);
   b1.scratch<int>(2);
+  b1.scratch<unsigned long long>(16);
   if (pa_status st = ensure_arena(ctx, b1.total())) return st;
   Builder b;
   b.dry = false;
@@ -2120,6 +2123,7 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
   int *d_done = b.scratch<int>(n_jobs_max);
   unsigned long long *d_head = b.scratch<unsigned long long>(1);
   int *d_status = b.scratch<int>(2);
+  unsigned long long *d_stats = b.scratch<unsigned long long>(16);
   if (b.blob.size() != b1.blob.size() || b.scratch_off != b1.scratch_off)
     return fail(ctx, PA_ERR_INVALID, "internal: plan size mismatch");
   for (QGroup &g : groups)
@@ -2143,6 +2147,11 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
   // key (group, image, child part, 0 up / 1 down, 0 rows / 1 cols) -> job
   std::map<std::tuple<int, int, int, int, int>, int> job_of;
   std::map<std::pair<int, int>, int> root_of;
+  // tiles per queue item: one for a wave of few images (the tree's levels
+  // leave most of the GPU to fill), up to four when many images overlap
+  int wave_images = 0;
+  for (QGroup &g : groups) wave_images += (int)g.idx.size();
+  const int per = std::max(1, std::min(4, wave_images / 4));
   int maxd = 0;
   for (QGroup &g : groups) maxd = std::max(maxd, g.pl.sc.maxdepth);
   std::vector<std::pair<int, int>> tune_need;  // rows jobs whose width is still to choose
@@ -2167,7 +2176,9 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
         } else {
           j.pad = ph.m_ky[q];
           j.nch = (pl.W + kColTileCols - 1) / kColTileCols;
-          j.n_items = j.nch * pl.R * ((pl.H + kColBandRows - 1) / kColBandRows);
+          j.tiles = j.nch * pl.R * ((pl.H + kColBandRows - 1) / kColBandRows);
+          j.per = per;
+          j.n_items = (j.tiles + per - 1) / per;
         }
         job_of[std::make_tuple((int)gi, ph.m_img[q], ph.m_child[q], up ? 0 : 1, kind)] =
             (int)jobs.size();
@@ -2186,7 +2197,9 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
       j.type = QJOB_ROOT;
       j.rd = pl.roots + i;
       j.cells = pl.N;
-      j.n_items = (int)((pl.N + kQRootCells - 1) / kQRootCells);
+      j.tiles = (int)((pl.N + kQRootCells - 1) / kQRootCells);
+      j.per = 1;
+      j.n_items = j.tiles;
       root_of[{(int)gi, i}] = (int)jobs.size();
       jobs.push_back(j);
     }
@@ -2226,26 +2239,66 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
       j.dep[k] = job_of.at(std::make_tuple(kv.first.first, kv.first.second, sc.ch[sc.root][k], 0, 1));
   }
 
+  // The per-group work before and after the queue (unaries; root marginal,
+  // log-partition, local maxima and result copies) runs on up to kWorkers
+  // side streams forked from the caller's stream and joined back into it.
+  const int NS = std::min((int)groups.size(), pa_ctx::kWorkers);
+  while ((int)ctx->side.size() < NS) {
+    cudaStream_t st = nullptr;
+    PA_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    ctx->side.push_back(st);
+  }
+  struct OnStream {  // ctx->stream set to a side stream for one group's launches
+    pa_ctx *c;
+    cudaStream_t keep;
+    OnStream(pa_ctx *c_, cudaStream_t st) : c(c_), keep(c_->stream) { c->stream = st; }
+    ~OnStream() { c->stream = keep; }
+  };
+  auto fork = [&]() -> pa_status {
+    cudaEvent_t ev = take_event(ctx);
+    PA_CK(cudaEventRecord(ev, s));
+    for (int k = 0; k < NS; ++k) PA_CK(cudaStreamWaitEvent(ctx->side[k], ev, 0));
+    ctx->pool.push_back(ev);  // a wait binds the record made before it
+    return PA_OK;
+  };
+  auto join = [&]() -> pa_status {
+    for (int k = 0; k < NS; ++k) {
+      cudaEvent_t ev = take_event(ctx);
+      PA_CK(cudaEventRecord(ev, ctx->side[k]));
+      PA_CK(cudaStreamWaitEvent(s, ev, 0));
+      ctx->pool.push_back(ev);
+    }
+    return PA_OK;
+  };
+
   // unaries of every group (the inputs of the first messages)
   if (pa_status st = upload_blob(ctx, b)) return st;
-  for (QGroup &g : groups) {
-    const pa_image &f = *g.f;
-    const int n = (int)g.idx.size(), R = g.pl.R;
-    const int64_t G = (int64_t)f.ny * f.nx, n_fields = (int64_t)n * R;
+  for (QGroup &g : groups)
     if (pa_status st = init_slots(ctx, g.pl)) return st;
+  if (pa_status st = fork()) return st;
+  {
     const std::vector<char> ff = fast_flags(cls, n_cls);
     const std::vector<int> ns = stump_counts(cls, n_cls);
-    PA_LAUNCH("score_grids", launch_score_grids(g.sp, (const bool *)ff.data(), ns.data(), n_cls,
-                                                g.desc[0], g.fields, g.fields_al, G, (int)n_fields,
-                                                f.dim, 1, g.scores, s));
-    PA_LAUNCH_N("unary_maps", f.ep->interpolate ? 1 : 2,
-                launch_unary_maps(g.umaps, n * g.pl.P * R, f.ny, f.nx, f.H, f.W,
-                                  !f.ep->interpolate, g.usep, s));
-    if (g.pl.n_msgs_total > 0)
-      PA_LAUNCH_N("shift_tables", 2,
-                  launch_shift_tables(g.pl.shifts, g.pl.n_msgs_total, R, f.H, f.W, g.pl.tables,
-                                      g.pl.sdesc, s));
+    for (size_t k = 0; k < groups.size(); ++k) {
+      QGroup &g = groups[k];
+      const pa_image &f = *g.f;
+      const int n = (int)g.idx.size(), R = g.pl.R;
+      const int64_t G = (int64_t)f.ny * f.nx, n_fields = (int64_t)n * R;
+      OnStream on(ctx, ctx->side[k % NS]);
+      cudaStream_t gs = ctx->stream;
+      PA_LAUNCH("score_grids", launch_score_grids(g.sp, (const bool *)ff.data(), ns.data(), n_cls,
+                                                  g.desc[0], g.fields, g.fields_al, G,
+                                                  (int)n_fields, f.dim, 1, g.scores, gs));
+      PA_LAUNCH_N("unary_maps", f.ep->interpolate ? 1 : 2,
+                  launch_unary_maps(g.umaps, n * g.pl.P * R, f.ny, f.nx, f.H, f.W,
+                                    !f.ep->interpolate, g.usep, gs));
+      if (g.pl.n_msgs_total > 0)
+        PA_LAUNCH_N("shift_tables", 2,
+                    launch_shift_tables(g.pl.shifts, g.pl.n_msgs_total, R, f.H, f.W, g.pl.tables,
+                                        g.pl.sdesc, gs));
+    }
   }
+  if (pa_status st = join()) return st;
 
   // row-tile widths: measured once per shape class (R, W, kx) on a message
   // whose input (a leaf's unary) is ready, among the widths that fit
@@ -2309,7 +2362,9 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
         if (!j.cw) return PA_ERR_UNSUPPORTED;
       }
       j.nch = (j.W + j.cw - 1) / j.cw;
-      j.n_items = j.H * j.nch;
+      j.tiles = j.H * j.nch;
+      j.per = per;
+      j.n_items = (j.tiles + per - 1) / per;
       smem = std::max(smem, ps_queue_smem_rows(j.R, j.cw, j.pad));
     } else {
       smem = std::max(smem, ps_queue_smem_cols(j.pad));
@@ -2330,23 +2385,56 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
   const long long wait_ns =
       (long long)((o.wait_timeout_ms > 0 ? o.wait_timeout_ms : 20000.0) * 1e6);
   int ctas = 0;
+  // PA_QUEUE_STATS=1: per job type, time taking tiles, waiting and running
+  // them (summed over CTAs), printed to stderr after each wave
+  const char *want_stats = std::getenv("PA_QUEUE_STATS");
+  const bool stats = want_stats && want_stats[0] == '1';
+  if (stats) PA_CK(cudaMemsetAsync(d_stats, 0, 16 * sizeof(unsigned long long), s));
   PA_LAUNCH("ps_queue", launch_ps_queue(d_jobs, (int)jobs.size(), n_items, d_head, d_done, d_status,
-                                        groups[0].pl.err, wait_ns, smem, &ctas, s));
+                                        groups[0].pl.err, wait_ns, smem, &ctas,
+                                        stats ? d_stats : nullptr, s));
   int status = 0;
   PA_CK(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
   PA_CK(cudaStreamSynchronize(s));
+  if (stats) {
+    unsigned long long h[16];
+    PA_CK(cudaMemcpy(h, d_stats, sizeof h, cudaMemcpyDeviceToHost));
+    static const char *names[4] = {"rows", "cols", "root", "rows48"};
+    std::fprintf(stderr, "ps_queue: %d CTAs, %zu jobs, %lld items of %d tiles, smem %zu\n", ctas, jobs.size(),
+                 n_items, per, smem);
+    for (int t = 0; t < 4; ++t)
+      if (h[4 * t + 3])
+        std::fprintf(stderr, "  %-4s tiles %8llu  take %7.2f us  wait %7.2f us  run %7.2f us\n",
+                     names[t], h[4 * t + 3], 1e-3 * h[4 * t] / h[4 * t + 3],
+                     1e-3 * h[4 * t + 1] / h[4 * t + 3], 1e-3 * h[4 * t + 2] / h[4 * t + 3]);
+  }
   if (status & 1) return fail(ctx, PA_ERR_TIMEOUT, "a queue dependency wait ran out (%.0f ms)",
                               o.wait_timeout_ms > 0 ? o.wait_timeout_ms : 20000.0);
   // a tile's error bits went to the first group's word: carry them to all
   int err0 = 0;
   PA_CK(cudaMemcpyAsync(&err0, groups[0].pl.err, sizeof(int), cudaMemcpyDeviceToHost, s));
   PA_CK(cudaStreamSynchronize(s));
-  for (QGroup &g : groups) {
-    if (err0 && &g != &groups[0]) PA_LAUNCH("fill", launch_fill_int(g.pl.err, err0, 1, s));
+  // tails: each group's results land in its own pinned block; one sync
+  if (ctx->land.size() < groups.size()) ctx->land.resize(groups.size());
+  std::vector<Readback> rb(groups.size());
+  if (pa_status st = fork()) return st;
+  for (size_t k = 0; k < groups.size(); ++k) {
+    QGroup &g = groups[k];
+    OnStream on(ctx, ctx->side[k % NS]);
+    if (err0 && k > 0) PA_LAUNCH("fill", launch_fill_int(g.pl.err, err0, 1, ctx->stream));
     if (pa_status st = run_ps_tail(ctx, g.f->ep, g.pl)) return st;
-    if (pa_status st = finish_ps(ctx, g.f->ep, g.pl, g.outs.data(), PA_MEM_DEVICE)) return st;
+    if (pa_status st = finish_enqueue(ctx, g.f->ep, g.pl, g.outs.data(), PA_MEM_DEVICE, (int)k, rb[k]))
+      return st;
   }
-  return PA_OK;
+  if (pa_status st = join()) return st;
+  if (pa_status st = sync_ctx(ctx)) return st;
+  pa_status result = PA_OK;
+  for (size_t k = 0; k < groups.size(); ++k) {
+    const pa_status st = finish_complete(ctx, groups[k].f->ep, groups[k].pl, groups[k].outs.data(), rb[k]);
+    if (st == PA_ERR_NUMERIC) result = st;
+    else if (st) return st;
+  }
+  return result;
 }
 
 }  // namespace
@@ -2421,6 +2509,10 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) try {
     for (auto &ld : ctx->land)
       if (ld.p) cudaFreeHost(ld.p);
     for (cudaEvent_t e : ctx->ring_done) cudaEventDestroy(e);
+    for (cudaStream_t st : ctx->side) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
     if (ctx->copy_stream) {
       cudaStreamSynchronize(ctx->copy_stream);
       cudaStreamDestroy(ctx->copy_stream);

@@ -199,44 +199,60 @@ struct RootDesc {
 // cells first + threadIdx.x + k * stride < N of one block, and folds the
 // maxima that the downward messages need and the argmax of the root marginal
 // (:261-277) into the descriptor's words (one atomic per block and word).
+// KC: the most root children the caller allows (rd.k <= KC); U: cells per
+// thread and step, their loads issued together.
+template <int KC = kMaxRootChildren, int U = 1>
 __device__ __forceinline__ void root_combine_cells(const RootDesc &rd, int64_t first, int64_t N,
                                                    int64_t stride) {
+  static_assert(KC <= kMaxRootChildren, "root children");
   const int k = rd.k;
-  int keys[kMaxRootChildren];
+  int keys[KC];
 #pragma unroll
-  for (int c = 0; c < kMaxRootChildren; ++c) keys[c] = kFkeyNegInf;
+  for (int c = 0; c < KC; ++c) keys[c] = kFkeyNegInf;
   unsigned long long am = 0ull;
-  for (int64_t i = first + threadIdx.x; i < N; i += stride) {
-    float m[kMaxRootChildren];
+  // plain loads: inside the persistent queue the messages are written by
+  // the same launch
+  for (int64_t i0 = first + threadIdx.x; i0 < N; i0 += U * stride) {
+    float m[U][KC], u[U];
 #pragma unroll
-    for (int c = 0; c < kMaxRootChildren; ++c)
-      if (c < k) m[c] = __ldg(rd.msg[c] + i);
-    const float u = __ldg(rd.unary + i);
-    float s = 0.f;
+    for (int q = 0; q < U; ++q) {
+      const int64_t i = i0 + q * stride;
+      const bool in = i < N;
 #pragma unroll
-    for (int c = 0; c < kMaxRootChildren; ++c)
-      if (c < k) s = __fadd_rn(s, m[c]);
-    const float post = __fadd_rn(s, u);
-    rd.post[i] = post;
-    const unsigned long long ak = akey(post, (uint32_t)i);
-    am = ak > am ? ak : am;
+      for (int c = 0; c < KC; ++c)
+        if (c < k) m[q][c] = in ? rd.msg[c][i] : 0.f;
+      u[q] = in ? rd.unary[i] : 0.f;
+    }
 #pragma unroll
-    for (int j = 0; j < kMaxRootChildren; ++j) {
-      if (j >= k) break;
-      float fr = 0.f;
+    for (int q = 0; q < U; ++q) {
+      const int64_t i = i0 + q * stride;
+      if (i >= N) break;
+      float s = 0.f;
 #pragma unroll
-      for (int c = 0; c < kMaxRootChildren; ++c)
-        if (c < k && c != j) fr = __fadd_rn(fr, m[c]);
-      fr = __fadd_rn(fr, u);
-      rd.from_root[j][i] = fr;
-      keys[j] = max(keys[j], (fr == fr) ? fkey(fr) : kFkeyNegInf);
+      for (int c = 0; c < KC; ++c)
+        if (c < k) s = __fadd_rn(s, m[q][c]);
+      const float post = __fadd_rn(s, u[q]);
+      rd.post[i] = post;
+      const unsigned long long ak = akey(post, (uint32_t)i);
+      am = ak > am ? ak : am;
+#pragma unroll
+      for (int j = 0; j < KC; ++j) {
+        if (j >= k) break;
+        float fr = 0.f;
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+          if (c < k && c != j) fr = __fadd_rn(fr, m[q][c]);
+        fr = __fadd_rn(fr, u[q]);
+        rd.from_root[j][i] = fr;
+        keys[j] = max(keys[j], (fr == fr) ? fkey(fr) : kFkeyNegInf);
+      }
     }
   }
   __shared__ int skeys[32][kMaxRootChildren];
   __shared__ unsigned long long sam[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int j = 0; j < kMaxRootChildren; ++j) {
+  for (int j = 0; j < KC; ++j) {
     const int v = __reduce_max_sync(0xFFFFFFFFu, keys[j]);
     if (lane == 0) skeys[warp][j] = v;
   }
@@ -263,14 +279,17 @@ __device__ __forceinline__ void root_combine_cells(const RootDesc &rd, int64_t f
 // ---------------------------------------------------------------------------
 // Persistent message passing (k_ps_queue, k_msg.cu): the row and column
 // tiles of every message and the root combinations of many images, drained
-// from one device work queue.  A job is a set of independent tiles; a job
-// may start when each job in `dep` has completed all its tiles.
+// from one device work queue.  A job is a set of independent tiles, taken
+// `per` at a time (one queue item); a job may start when each job in `dep`
+// has completed all its items.
 // ---------------------------------------------------------------------------
 enum QJobType { QJOB_ROWS = 0, QJOB_COLS = 1, QJOB_ROOT = 2, QJOB_GATE = 3 };
 constexpr int kQMaxDeps = 8;
 struct QJob {
   int type;
-  int n_items;               // tiles (0 for the gate: it is opened by the host)
+  int n_items;               // items, ceil(tiles / per) (0 for the gate: the host opens it)
+  int tiles;                 // tiles of the job
+  int per;                   // tiles per item
   int dep[kQMaxDeps];        // job indices, -1: none
   const MsgDesc *md;         // rows / cols
   const RootDesc *rd;        // root
@@ -279,7 +298,7 @@ struct QJob {
   int cw;                    // rows: column chunk width
   int nch;                   // rows: column chunks per image row; cols: strips
   long long cells;           // root: N; its tiles cover kQRootCells cells each
-  long long first;           // global index of the job's first tile
+  long long first;           // queue index of the job's first item
 };
 constexpr int kQRootCells = 384 * 64;
 constexpr int kColBandRows = 176;  // rows of one column-pass tile (kTX columns x one rotation)
@@ -289,12 +308,14 @@ cudaError_t launch_msg_rows_cw(const MsgDesc *msgs, int n_msgs, int R, int H, in
                                int cw, int *err, cudaStream_t s);
 constexpr int kQThreads = 384;
 // status bits of k_ps_queue: 1 = a dependency wait ran out (the queue was
-// abandoned)
+// abandoned).  stats (optional, [4][4] words: rows, cols, root, rows of 48
+// rotations): nanoseconds spent taking and finding items, waiting for
+// dependencies, running tiles, and the tile count.
 size_t ps_queue_smem_rows(int R, int cw, int padx);
 size_t ps_queue_smem_cols(int pady);
 cudaError_t launch_ps_queue(const QJob *jobs, int n_jobs, long long n_items, unsigned long long *head,
                             int *done, int *status, int *err, long long wait_limit_ns, size_t smem,
-                            int *ctas_launched, cudaStream_t s);
+                            int *ctas_launched, unsigned long long *stats, cudaStream_t s);
 
 // Host-side parameters of one computeRotJointMarginal(child -> parent,
 // offset_c_10 = oc, offset_p_01 = op, rot_mean, rot_sigma): rotation-mean bin
