@@ -196,6 +196,72 @@ def algorithmic_bytes(trees, batch):
     }
 
 
+def with_unary_total(kt):
+    """kernel_times() with "score_grids" = the whole AdaBoost unary stage: the
+    float kernel, or the rank form's two kernels (stump_ranks + stump_votes)."""
+    kt = dict(kt)
+    if "stump_ranks" in kt or "stump_votes" in kt:
+        a, b = kt.get("stump_ranks", (0.0, 0)), kt.get("stump_votes", (0.0, 0))
+        f = kt.get("score_grids", (0.0, 0))
+        kt["score_grids"] = (a[0] + b[0] + f[0], a[1] + b[1] + f[1])
+    return kt
+
+
+def gaussian_len(sigma):
+    """Taps of get_gaussian_filter(sigma): 2 * floor(3 sigma + 0.5) + 1."""
+    return 2 * int(np.floor(3.0 * sigma + 0.5)) + 1
+
+
+def algorithmic_ops(trees, batch):
+    """Algorithmic operation counts of one step (one batch of images).
+    score_grids: warp-level stump evaluations (32 locations of one classifier
+        and one stump); the irreducible per-evaluation work is 4 warp
+        instructions (shared load of the feature value, compare, select, add)
+        and 1 shared-memory wavefront (the 32 feature values).
+    msg_rows / msg_cols: FP32 FMAs, per message and cell the taps of the x
+        filter plus the rotation filter (rows) and of the y filter (cols)."""
+    from partapp_gb300 import synth
+
+    step = synth.rot_step_rad(R)
+    N = R * H * W
+    rows = cols = 0
+    for t in trees[:batch]:
+        for j in range(len(t["child"])):
+            xl = gaussian_len(np.sqrt(t["C"][j][0]))
+            yl = gaussian_len(np.sqrt(t["C"][j][3]))
+            rl = gaussian_len(t["rot_sigma"][j] / step)
+            if rl >= R:
+                rl = R - 2 if R % 2 else R - 1
+            rows += 2 * N * (xl + rl)  # upward and downward message of the joint
+            cols += 2 * N * yl
+    return {"score_grids_warp_evals": batch * R * NY * NX * N_CLS * N_STUMPS / 32,
+            "msg_rows_fma": rows, "msg_cols_fma": cols}
+
+
+def compute_rooflines(kernels, ops, steps, sm_mhz, n_sm):
+    """Issue / shared-memory / FP32-pipe fractions next to the HBM ones:
+    achieved = algorithmic operations / the kernel's measured time, peak =
+    n_sm x per-SM rate x the SM clock sampled during the timed region."""
+    if not sm_mhz:
+        return
+    hz = sm_mhz * 1e6
+    if "score_grids" in kernels:
+        t = kernels["score_grids"]["ms_per_step"] / 1e3
+        ev = ops["score_grids_warp_evals"]
+        kernels["score_grids"]["issue"] = {
+            "achieved_warp_instr_per_s": 4 * ev / t, "peak": n_sm * 4 * hz,
+            "frac": 4 * ev / t / (n_sm * 4 * hz), "alg_warp_instr_per_eval": 4}
+        kernels["score_grids"]["smem"] = {
+            "achieved_wavefronts_per_s": ev / t, "peak": n_sm * hz,
+            "frac": ev / t / (n_sm * hz), "alg_wavefronts_per_eval": 1}
+    for k in ("msg_rows", "msg_cols"):
+        if k in kernels:
+            t = kernels[k]["ms_per_step"] / 1e3
+            f = ops[k + "_fma"]
+            kernels[k]["fp32_pipe_frac"] = f / t / (n_sm * 128 * hz)
+            kernels[k]["fma_per_s"] = f / t
+
+
 def traffic_from_profiles(kernel):
     """dram read+write bytes per launch of `kernel` from the committed ncu
     summary, if present (profiles/traffic.json)."""
@@ -380,7 +446,7 @@ def run_ours(args):
     ctx.enable_timing(False)
     launches = ctx.kernel_launches - l0
     ms = replicas.max_over_ranks(t_start.elapsed_time(t_end), dist, dev)
-    ktimes = ctx.kernel_times()
+    ktimes = with_unary_total(ctx.kernel_times())
     images = replicas.sum_over_ranks(B * args.steps, dist, dev)
     value = replicas.throughput(images, ms)
 
@@ -403,6 +469,8 @@ def run_ours(args):
     for k in kernels:
         if k in alg:
             kernels[k]["GB/s"] = alg[k] / (ktimes[k][0] / args.steps / 1e3) / 1e9
+    compute_rooflines(kernels, algorithmic_ops(trees, B), args.steps, clk.summary()["sm_mhz"],
+                      torch.cuda.get_device_properties(dev).multi_processor_count)
 
     # end to end through the same C-ABI call with pinned host buffers
     Be = args.e2e_batch
@@ -976,7 +1044,7 @@ def learned_vs_plain(ctx, dev, stream, args, steps=10, B=8):
         torch.cuda.synchronize(dev)
         ctx.enable_timing(False)
         ms = a.elapsed_time(b) / steps
-        kt = ctx.kernel_times()
+        kt = with_unary_total(ctx.kernel_times())
         out[name] = {"images_per_s": B * 1e3 / ms, "ms_per_step": ms,
                      "unary_ms_per_image": sum(v[0] for k, v in kt.items()
                                                if k.startswith("net_") or k == "score_grids")

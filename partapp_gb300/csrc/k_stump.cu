@@ -14,6 +14,7 @@
 // part w of the CTA's part group, lane l evaluates location l, so the stump
 // record a warp reads is uniform (broadcast load).
 #include "pa_internal.cuh"
+#include "tc_common.cuh"
 
 namespace pa {
 namespace {
@@ -284,6 +285,195 @@ __global__ void __launch_bounds__(32 * kMaxWarps, 1) k_score_grids_pipe(
   }
 }
 
+// ---------------------------------------------------------------------------
+// Rank form of the stump test (classifier sets with unit polarities).
+//
+// For a feature f let U_f = {u_0 < u_1 < ... < u_{m-1}} be the distinct
+// thresholds t (of the sign-folded records above) that the set's stumps put
+// on f.  The rank of a value v is b(v) = #{u in U_f : u <= v} (a NaN ranks
+// above every threshold).  A stump (f, t = u_k) has v < t exactly when
+// b(v) <= k, so with m <= 127 every test is a byte comparison:
+//
+// k_rank_buckets: every descriptor value -> its rank byte by a d-step search
+//   of the feature's thresholds, stored in Eytzinger order (shared memory).
+//   Output: tiles of kRankLoc = 128 locations of one field, word (f, g) of a
+//   tile = the ranks of locations 4g .. 4g+3 (byte j = location 4g + j).
+// k_rank_votes: one warp per classifier walks its stumps in order over a
+//   tile bulk-copied into shared memory.  One 32-bit load gives lane g the
+//   ranks of four locations and one subtraction tests all four:
+//     d = (0x80 + k) * 0x01010101 - ranks,  bit 7 of byte j set <=> b_j <= k
+//   (0x80 + k - b lies in [1, 254]: no borrow crosses a byte; the record
+//   keeps 0x80 + k in its top byte, replicated by one byte permute).  The
+//   vote is -a with its sign bit flipped when the test holds.  Each
+//   location's votes are summed in stump order, as in the float kernels, so
+//   the scores are the same bits.  Padding records (k = 127, -a = -0) vote
+//   +0.
+// NaN descriptor values rank above every threshold: their test is false, as
+// v < t is.
+// ---------------------------------------------------------------------------
+constexpr int kRankLoc = 128;       // locations per tile
+constexpr int kRankSlab = 8;        // feature groups of 32 per k_rank_buckets CTA
+constexpr int kRankWarps1 = 16;     // k_rank_buckets
+constexpr int kRankMaxWarps = 32;   // k_rank_votes: one warp per classifier
+
+// A CTA serves one slab of 256 features (kRankSlab groups of 32) for a
+// strided set of tiles.  Lane g of a warp reads the slab of one location as
+// two float4 (features 128c + 4g .. 128c + 4g + 3, c = 0, 1): value u = 4c + j
+// of lane g is local feature fl(u, g) = 128c + 4g + j.  Shared tables and
+// output rows are kept in (u, g) order so that every access is one bank per
+// lane: thresholds as [u][entry][g], output rows r = 32u + g (stride 33).
+template <int D, bool VEC>
+__global__ void __launch_bounds__(32 * kRankWarps1) k_rank_buckets(
+    const float *__restrict__ eyt, int dim, const float *__restrict__ desc,
+    const float *const *__restrict__ fields, int64_t n_loc, int n_fields,
+    uint32_t *__restrict__ ranks) {
+  extern __shared__ __align__(16) float sm[];
+  constexpr int S = (1 << D) + 1;  // row stride of the global table
+  constexpr int T = 1 << D;        // entries per feature in shared memory
+  constexpr int SLAB = kRankSlab * 32;
+  const int n_slabs = (dim + SLAB - 1) / SLAB;
+  const int slab = blockIdx.x % n_slabs;
+  const int cta = blockIdx.x / n_slabs, n_cta = gridDim.x / n_slabs;
+  const int f0 = slab * SLAB, nf = min(dim, f0 + SLAB) - f0;  // nf: a multiple of 4
+  float *tab = sm;                                                     // [8][T][32]
+  uint32_t *os = reinterpret_cast<uint32_t *>(sm + (size_t)kRankSlab * T * 32);  // [8 * 32][33]
+  unsigned char *osb = reinterpret_cast<unsigned char *>(os);
+  for (int i = threadIdx.x; i < kRankSlab * T * 32; i += blockDim.x) {
+    const int u = i / (T * 32), e = (i / 32) % T, g = i & 31;
+    const int fl = (u >> 2) * 128 + 4 * g + (u & 3);
+    tab[i] = fl < nf ? __ldg(eyt + (size_t)(f0 + fl) * S + e) : INFINITY;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t tiles_per_field = (n_loc + kRankLoc - 1) / kRankLoc;
+  const int64_t n_tiles = tiles_per_field * n_fields;
+  const bool in0 = 4 * lane < nf, in1 = 128 + 4 * lane < nf;
+  // one location per warp at a time, the next one's loads in flight while
+  // this one is searched
+  auto load = [&](const float *p, bool ok, float *v4) {
+    if (VEC) {
+      const float4 x = ok ? __ldg(reinterpret_cast<const float4 *>(p)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      v4[0] = x.x, v4[1] = x.y, v4[2] = x.z, v4[3] = x.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v4[j] = ok ? __ldg(p + j) : 0.f;
+    }
+  };
+  for (int64_t t = cta; t < n_tiles; t += n_cta) {
+    const int field = (int)(t / tiles_per_field);
+    const int64_t loc0 = (t - (int64_t)field * tiles_per_field) * kRankLoc;
+    const float *fb = (fields ? fields[field] : desc + (int64_t)field * n_loc * dim) + f0 + 4 * lane;
+    float v[8], vn[8];
+    {
+      const int64_t loc = loc0 + warp;
+      load(fb + loc * dim, in0 && loc < n_loc, v);
+      load(fb + loc * dim + 128, in1 && loc < n_loc, v + 4);
+    }
+    for (int l = warp; l < kRankLoc; l += nw) {
+      const int64_t locn = loc0 + l + nw;
+      const bool more = l + nw < kRankLoc && locn < n_loc;
+      load(fb + locn * dim, in0 && more, vn);
+      load(fb + locn * dim + 128, in1 && more, vn + 4);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        // step right unless v < entry: "v >= entry or unordered", so a NaN
+        // takes the last leaf, rank 2^D - 1, above every threshold index
+        const float *col = tab + u * T * 32 + lane;
+        int i = 1;
+#pragma unroll
+        for (int st = 0; st < D; ++st) {
+          uint32_t m;
+          asm("set.geu.u32.f32 %0, %1, %2;" : "=r"(m) : "f"(v[u]), "f"(col[i * 32]));
+          i = 2 * i - (int)m;
+        }
+        osb[((size_t)(u * 32 + lane) * 33 + (l >> 2)) * 4 + (l & 3)] =
+            (unsigned char)(i - (1 << D));
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = vn[u];
+    }
+    __syncthreads();
+    // rows back in feature order: feature fl sits in row 32 * (4c + j) + g
+    uint32_t *dst = ranks + ((size_t)t * dim + f0) * 32;
+    for (int i = threadIdx.x; i < nf * 32; i += blockDim.x) {
+      const int fl = i >> 5;
+      const int r = ((fl >> 7) * 4 + (fl & 3)) * 32 + ((fl >> 2) & 31);
+      dst[i] = os[r * 33 + (i & 31)];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(32 * kRankMaxWarps, 1) k_rank_votes(
+    const uint2 *__restrict__ rec, const float *__restrict__ sum_alpha, int n_cls, int npad,
+    int dim, const uint32_t *__restrict__ ranks, int64_t n_loc, int n_fields, int normalize,
+    float *__restrict__ scores, int *err) {
+  extern __shared__ __align__(16) unsigned char smr[];
+  // tile [dim][32] words at the first 128-byte boundary, then the records
+  unsigned char *base =
+      smr + ((128 - (tc::smem_u32(smr) & 127u)) & 127u);
+  uint32_t *tile = reinterpret_cast<uint32_t *>(base);
+  uint2 *srec = reinterpret_cast<uint2 *>(base + (size_t)dim * 128);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_ok;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < n_cls * npad; i += blockDim.x) srec[i] = rec[i];
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int64_t tiles_per_field = (n_loc + kRankLoc - 1) / kRankLoc;
+  const int64_t n_tiles = tiles_per_field * n_fields;
+  const uint32_t tile_bytes = (uint32_t)dim * 128u, chunk = tile_bytes / 4u;  // dim * 32: 16-byte multiple
+  uint32_t phase = 0;
+  for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x, phase ^= 1u) {
+    if (tid == 0) {
+      const unsigned char *src = reinterpret_cast<const unsigned char *>(ranks) + (size_t)t * tile_bytes;
+      tc::mbar_arrive_expect_tx(&bar, tile_bytes);
+      for (int c = 0; c < 4; ++c) tc::bulk_load(base + c * chunk, src + c * chunk, chunk, &bar);
+      if (t + gridDim.x < n_tiles) tc::bulk_prefetch_l2(src + (size_t)gridDim.x * tile_bytes, tile_bytes);
+      s_ok = tc::mbar_wait_try(&bar, phase, err) ? 1 : 0;
+      if (!s_ok) tc::mbar_wait_try(&bar, phase, err);  // once more for the copies in flight
+    }
+    __syncthreads();
+    if (!s_ok) break;
+    if (warp < n_cls) {
+      const int field = (int)(t / tiles_per_field);
+      const int64_t loc0 = (t - (int64_t)field * tiles_per_field) * kRankLoc;
+      const uint2 *r = srec + (size_t)warp * npad;
+      const unsigned char *lane_base = base + lane * 4;
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll 4
+      for (int i = 0; i < npad; ++i) {
+        const uint2 q = r[i];
+        const uint32_t w = *reinterpret_cast<const uint32_t *>(lane_base + (q.x & 0x1FFFFu));
+        const uint32_t d = __byte_perm(q.x, 0u, 0x3333u) - w;
+        s0 += __uint_as_float(q.y ^ ((d << 24) & 0x80000000u));
+        s1 += __uint_as_float(q.y ^ ((d << 16) & 0x80000000u));
+        s2 += __uint_as_float(q.y ^ ((d << 8) & 0x80000000u));
+        s3 += __uint_as_float(q.y ^ (d & 0x80000000u));
+      }
+      if (normalize) {
+        const float sa = sum_alpha[warp];
+        s0 = __fdiv_rn(s0, sa);
+        s1 = __fdiv_rn(s1, sa);
+        s2 = __fdiv_rn(s2, sa);
+        s3 = __fdiv_rn(s3, sa);
+      }
+      float *o = scores + ((int64_t)warp * n_fields + field) * n_loc + loc0 + 4 * lane;
+      const int64_t left = n_loc - (loc0 + 4 * lane);
+      if (left > 0) o[0] = s0;
+      if (left > 1) o[1] = s1;
+      if (left > 2) o[2] = s2;
+      if (left > 3) o[3] = s3;
+    }
+    __syncthreads();  // the tile is read before the next copy overwrites it
+  }
+  __syncthreads();
+  if (tid == 0) tc::mbar_inval(&bar);
+}
+
 }  // namespace
 
 cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
@@ -335,6 +525,77 @@ cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
             (unsigned)((n_parts + gw - 1) / gw));
   k_score_grids<<<grid, 32 * gw, smem, s>>>(parts_dev, n_parts, desc, fields, n_loc, dim, dp, normalize,
                                             scores, n_fields);
+  return cudaGetLastError();
+}
+
+size_t rank_bytes(int dim, int64_t n_loc, int n_fields) {
+  return (size_t)((n_loc + kRankLoc - 1) / kRankLoc) * n_fields * dim * 128;
+}
+
+size_t rank_votes_smem(int dim, int n_cls, int npad) {
+  return 128 + (size_t)dim * 128 + (size_t)n_cls * npad * sizeof(uint2);
+}
+
+cudaError_t launch_rank_buckets(const RankTables &rt, const float *desc,
+                                const float *const *fields, bool aligned, int64_t n_loc,
+                                int n_fields, uint32_t *ranks, cudaStream_t s) {
+  if (rt.d < 1 || rt.d > 7 || rt.n_cls < 1 || rt.n_cls > kRankMaxWarps || rt.dim > 1023 ||
+      rt.dim % 4 || rank_votes_smem(rt.dim, rt.n_cls, rt.npad) > 227 * 1024)
+    return cudaErrorInvalidValue;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int n_slabs = (rt.dim + kRankSlab * 32 - 1) / (kRankSlab * 32);
+  const size_t smem1 = (size_t)kRankSlab * 32 * (((size_t)1 << rt.d) + 33) * sizeof(float);
+  const int64_t n_tiles = ((n_loc + kRankLoc - 1) / kRankLoc) * n_fields;
+  auto go1 = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+    if (e != cudaSuccess) return e;
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kRankWarps1, smem1);
+    if (per_sm < 1) per_sm = 1;
+    int64_t per_slab = ((int64_t)sms * per_sm + n_slabs - 1) / n_slabs;
+    if (per_slab > n_tiles) per_slab = n_tiles;
+    kern<<<(unsigned)(per_slab * n_slabs), 32 * kRankWarps1, smem1, s>>>(rt.eyt, rt.dim, desc, fields,
+                                                                         n_loc, n_fields, ranks);
+    return cudaGetLastError();
+  };
+  cudaError_t e = cudaSuccess;
+  switch (rt.d * 2 + (aligned ? 1 : 0)) {
+    case 2: e = go1(k_rank_buckets<1, false>); break;
+    case 3: e = go1(k_rank_buckets<1, true>); break;
+    case 4: e = go1(k_rank_buckets<2, false>); break;
+    case 5: e = go1(k_rank_buckets<2, true>); break;
+    case 6: e = go1(k_rank_buckets<3, false>); break;
+    case 7: e = go1(k_rank_buckets<3, true>); break;
+    case 8: e = go1(k_rank_buckets<4, false>); break;
+    case 9: e = go1(k_rank_buckets<4, true>); break;
+    case 10: e = go1(k_rank_buckets<5, false>); break;
+    case 11: e = go1(k_rank_buckets<5, true>); break;
+    case 12: e = go1(k_rank_buckets<6, false>); break;
+    case 13: e = go1(k_rank_buckets<6, true>); break;
+    case 14: e = go1(k_rank_buckets<7, false>); break;
+    default: e = go1(k_rank_buckets<7, true>); break;
+  }
+  return e;
+}
+
+cudaError_t launch_rank_votes(const RankTables &rt, int64_t n_loc, int n_fields, int normalize,
+                              float *scores, const uint32_t *ranks, int *err, cudaStream_t s) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t n_tiles = ((n_loc + kRankLoc - 1) / kRankLoc) * n_fields;
+  const size_t smem2 = rank_votes_smem(rt.dim, rt.n_cls, rt.npad);
+  cudaError_t e;
+  e = cudaFuncSetAttribute(k_rank_votes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+  if (e != cudaSuccess) return e;
+  const int warps = rt.n_cls < 8 ? 8 : rt.n_cls;
+  int64_t grid = sms;
+  if (grid > n_tiles) grid = n_tiles;
+  k_rank_votes<<<(unsigned)grid, 32 * warps, smem2, s>>>(rt.rec, rt.sum_alpha, rt.n_cls, rt.npad,
+                                                         rt.dim, ranks, n_loc, n_fields, normalize,
+                                                         scores, err);
   return cudaGetLastError();
 }
 

@@ -9,6 +9,8 @@
 // operations in the same order; this file is compiled with FMA contraction
 // off so the host rounds exactly as the reference did.
 #include <algorithm>
+#include <atomic>
+#include <functional>
 #include <cmath>
 #include <map>
 #include <cstdarg>
@@ -35,6 +37,8 @@ struct pa_classifier {
   float4 *d = nullptr;     // {f, p, theta*p, alpha}
   float4 *fast = nullptr;  // {f, t, p*alpha, 0}, only when every p is +1 or -1
   char *packed = nullptr;  // f8[npad/8] (uint4) then ta2[npad/2] (float4)
+  std::vector<float4> fast_h;  // host copy of `fast` (rank tables of classifier sets)
+  uint64_t id = 0;             // process-unique: the key of cached per-set tables
 };
 
 struct pa_ctx {
@@ -94,6 +98,13 @@ struct pa_ctx {
   std::vector<pa_ctx *> workers;
   // pa_find_obj_queue: measured row-tile width per shape class (R, W, kx)
   std::map<std::tuple<int, int, int>, int> row_tile;
+  // rank tables of the classifier sets seen (key: the classifiers' ids)
+  struct RankEntry {
+    bool ok = false;  // false: the set does not qualify (float kernels)
+    char *mem = nullptr;
+    pa::RankTables rt{};
+  };
+  std::map<std::vector<uint64_t>, RankEntry> rank_sets;
 };
 
 namespace {
@@ -1429,6 +1440,102 @@ pa_status check_classifiers(pa_ctx *ctx, const pa_classifier *const *cls, int n_
   return PA_OK;
 }
 
+// Rank tables of a classifier set (the rank form of k_stump.cu), built once
+// per set and context.  nullptr when the set does not qualify: a polarity
+// other than +-1, more than 127 distinct thresholds on one feature, dim >
+// 1023 or not a multiple of 4, more than 32 classifiers, or tables beyond
+// shared memory.
+const RankTables *rank_tables(pa_ctx *ctx, const pa_classifier *const *cls, int n) {
+  std::vector<uint64_t> key(n);
+  for (int c = 0; c < n; ++c) key[c] = cls[c]->id;
+  auto it = ctx->rank_sets.find(key);
+  if (it != ctx->rank_sets.end()) return it->second.ok ? &it->second.rt : nullptr;
+  pa_ctx::RankEntry &ent = ctx->rank_sets[key];
+  const int dim = cls[0]->dim;
+  if (n < 1 || n > 32 || dim > 1023 || dim % 4) return nullptr;
+  int nmax = 0;
+  for (int c = 0; c < n; ++c) {
+    if (cls[c]->dim != dim || cls[c]->fast_h.empty()) return nullptr;
+    nmax = std::max(nmax, cls[c]->n);
+  }
+  const int npad = (nmax + 3) / 4 * 4;
+  if (rank_votes_smem(dim, n, npad) > 227 * 1024) return nullptr;
+  // distinct thresholds per feature, ascending (-0 and +0 are one value)
+  std::vector<std::vector<float>> U(dim);
+  for (int c = 0; c < n; ++c)
+    for (const float4 &q : cls[c]->fast_h) {
+      int f;
+      std::memcpy(&f, &q.x, 4);
+      U[f].push_back(q.y);
+    }
+  size_t mmax = 0;
+  for (auto &u : U) {
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end(), [](float a, float b) { return a == b; }), u.end());
+    mmax = std::max(mmax, u.size());
+  }
+  if (mmax > 127) return nullptr;
+  int d = 1;
+  while (((size_t)1 << d) - 1 < mmax) ++d;
+  const int S = (1 << d) + 1, top = 1 << d;
+  // Eytzinger order: e[1] the root, children of e[i] at 2i and 2i + 1 (an
+  // in-order walk of that tree visits the sorted thresholds, +inf padded)
+  std::vector<float> eyt((size_t)dim * S, INFINITY);
+  for (int f = 0; f < dim; ++f) {
+    size_t next = 0;
+    float *row = eyt.data() + (size_t)f * S;
+    std::function<void(int)> fill = [&](int i) {
+      if (i >= top) return;
+      fill(2 * i);
+      row[i] = next < U[f].size() ? U[f][next] : INFINITY;
+      ++next;
+      fill(2 * i + 1);
+    };
+    fill(1);
+  }
+  std::vector<uint2> rec((size_t)n * npad, make_uint2(0xFFu << 24, 0x80000000u));
+  std::vector<float> sa(n);
+  for (int c = 0; c < n; ++c) {
+    sa[c] = cls[c]->sum_alpha;
+    for (int i = 0; i < cls[c]->n; ++i) {
+      const float4 &q = cls[c]->fast_h[i];
+      int f;
+      std::memcpy(&f, &q.x, 4);
+      const auto &u = U[f];
+      const uint32_t k = (uint32_t)(std::lower_bound(u.begin(), u.end(), q.y) - u.begin());
+      const float na = -q.z;
+      uint32_t nab;
+      std::memcpy(&nab, &na, 4);
+      rec[(size_t)c * npad + i] = make_uint2((uint32_t)f * 128u | ((0x80u + k) << 24), nab);
+    }
+  }
+  const size_t b_eyt = eyt.size() * sizeof(float), b_rec = rec.size() * sizeof(uint2);
+  const size_t o_rec = (b_eyt + 255) / 256 * 256, o_sa = o_rec + (b_rec + 255) / 256 * 256;
+  char *mem = nullptr;
+  if (cudaMalloc(&mem, o_sa + sa.size() * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemcpy(mem, eyt.data(), b_eyt, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(mem + o_rec, rec.data(), b_rec, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(mem + o_sa, sa.data(), sa.size() * sizeof(float), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(mem);
+    return nullptr;
+  }
+  ent.mem = mem;
+  ent.rt.eyt = reinterpret_cast<const float *>(mem);
+  ent.rt.rec = reinterpret_cast<const uint2 *>(mem + o_rec);
+  ent.rt.sum_alpha = reinterpret_cast<const float *>(mem + o_sa);
+  ent.rt.d = d;
+  ent.rt.dim = dim;
+  ent.rt.n_cls = n;
+  ent.rt.npad = npad;
+  ent.ok = true;
+  return &ent.rt;
+}
+
 StumpPart *plan_stumps(Builder &b, const pa_classifier *const *cls, int n_parts) {
   std::vector<StumpPart> sp(n_parts);
   for (int p = 0; p < n_parts; ++p) {
@@ -1750,6 +1857,9 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   const bool scores_dev_out =
       (mem == PA_MEM_DEVICE && scores_out && scores_field0 == 0 && scores_fields == n_fields);
   StumpPart *sp = ada ? plan_stumps(b1, run_cls, n_run) : nullptr;
+  // rank form of the stump test when the classifier set qualifies
+  const RankTables *rk = (!lu) ? rank_tables(ctx, cls, n_cls) : nullptr;
+  uint32_t *ranks = rk ? b1.scratch<uint32_t>(rank_bytes(dim, G, (int)n_fields) / 4) : nullptr;
   const float *desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b1.scratch<float>(n_fields * G * dim);
   // scores of the AdaBoost parts when the net writes the others
   const bool split_scores = lu && lu->any_ada && lu->any_net;
@@ -1785,6 +1895,7 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   b.base = ctx->arena;
   PsPlan pl2 = pl;
   sp = ada ? plan_stumps(b, run_cls, n_run) : nullptr;
+  ranks = rk ? b.scratch<uint32_t>(rank_bytes(dim, G, (int)n_fields) / 4) : nullptr;
   desc_dev = (in_mem == PA_MEM_DEVICE) ? desc : b.scratch<float>(n_fields * G * dim);
   ada_scores = split_scores ? b.scratch<float>((size_t)n_run * n_fields * G) : nullptr;
   fields_dev = img_desc ? b.param(fptr.data(), fptr.size()) : nullptr;
@@ -1810,7 +1921,11 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   st = init_slots(ctx, pl2);
   if (st) return st;
   cudaStream_t s = ctx->stream;
-  if (!lu) {
+  if (rk) {
+    const bool al = fields_dev ? fields_al : ((uintptr_t)desc_dev & 15) == 0;
+    PA_LAUNCH("stump_ranks", launch_rank_buckets(*rk, desc_dev, fields_dev, al, G, (int)n_fields, ranks, s));
+    PA_LAUNCH("stump_votes", launch_rank_votes(*rk, G, (int)n_fields, 1, scores, ranks, pl2.err, s));
+  } else if (!lu) {
     const std::vector<char> ff = fast_flags(cls, n_cls);
     const std::vector<int> ns = stump_counts(cls, n_cls);
     PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_cls, desc_dev, fields_dev, fields_al, G,
@@ -2024,6 +2139,8 @@ struct QGroup {
   const float *const *fields = nullptr;
   bool fields_al = true;
   float *scores = nullptr;
+  const RankTables *rk = nullptr;  // rank form of the stump test, if the set qualifies
+  uint32_t *ranks = nullptr;
   UnaryMap *umaps = nullptr;
   int usep = 0;
 };
@@ -2047,6 +2164,8 @@ pa_status plan_queue_group(pa_ctx *ctx, Builder &b, QGroup &g, const PsPlan &pro
     }
   g.fields = b.param(fptr.data(), fptr.size());
   g.scores = b.scratch<float>((size_t)n_cls * n_fields * G);
+  g.rk = rank_tables(ctx, cls, n_cls);
+  g.ranks = g.rk ? b.scratch<uint32_t>(rank_bytes(f.dim, G, (int)n_fields) / 4) : nullptr;
   plan_ps(b, g.pl, e, g.joints, g.marg_out.data(), g.rp_out.data());
   plan_marg_ptrs(b, g.pl);
   plan_localmax(b, g.pl, e, g.outs.data());
@@ -2286,9 +2405,16 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
       const int64_t G = (int64_t)f.ny * f.nx, n_fields = (int64_t)n * R;
       OnStream on(ctx, ctx->side[k % NS]);
       cudaStream_t gs = ctx->stream;
-      PA_LAUNCH("score_grids", launch_score_grids(g.sp, (const bool *)ff.data(), ns.data(), n_cls,
-                                                  g.desc[0], g.fields, g.fields_al, G,
-                                                  (int)n_fields, f.dim, 1, g.scores, gs));
+      if (g.rk)
+      {
+        PA_LAUNCH("stump_ranks", launch_rank_buckets(*g.rk, g.desc[0], g.fields, g.fields_al, G,
+                                                     (int)n_fields, g.ranks, gs));
+        PA_LAUNCH("stump_votes", launch_rank_votes(*g.rk, G, (int)n_fields, 1, g.scores, g.ranks,
+                                                   g.pl.err, gs));
+      } else
+        PA_LAUNCH("score_grids", launch_score_grids(g.sp, (const bool *)ff.data(), ns.data(), n_cls,
+                                                    g.desc[0], g.fields, g.fields_al, G,
+                                                    (int)n_fields, f.dim, 1, g.scores, gs));
       PA_LAUNCH_N("unary_maps", f.ep->interpolate ? 1 : 2,
                   launch_unary_maps(g.umaps, n * g.pl.P * R, f.ny, f.nx, f.H, f.W,
                                     !f.ep->interpolate, g.usep, gs));
@@ -2513,6 +2639,8 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) try {
       cudaStreamSynchronize(st);
       cudaStreamDestroy(st);
     }
+    for (auto &kv : ctx->rank_sets)
+      if (kv.second.mem) cudaFree(kv.second.mem);
     if (ctx->copy_stream) {
       cudaStreamSynchronize(ctx->copy_stream);
       cudaStreamDestroy(ctx->copy_stream);
@@ -2644,6 +2772,8 @@ pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int
   }
   DeviceGuard dg(ctx->device);
   std::unique_ptr<pa_classifier> c(new pa_classifier);
+  static std::atomic<uint64_t> next_id{1};
+  c->id = next_id.fetch_add(1);
   c->dim = dim;
   c->n = n_stumps;
   c->sum_alpha = sum_alpha;
@@ -2659,6 +2789,7 @@ pa_status pa_classifier_create(pa_ctx *ctx, int dim, const pa_stump *stumps, int
       return fail(ctx, PA_ERR_NOMEM, "cannot allocate stump table");
     }
     PA_CK(cudaMemcpy(c->fast, fast.data(), sizeof(float4) * n_stumps, cudaMemcpyHostToDevice));
+    c->fast_h = fast;
     // packed copy; stumps past n are {t = -inf, a = +0}: their vote -0 leaves
     // the running sum (which starts at +0 and is never -0) unchanged
     if (dim <= 65536) {
@@ -2778,11 +2909,16 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
   DeviceGuard dg(ctx->device);
   const int64_t G = (int64_t)ny * nx;
   const size_t din = (size_t)n_fields * G * dim, dout = (size_t)n_parts * n_fields * G;
+  const RankTables *rk = rank_tables(ctx, cls, n_parts);
   Builder b1;
   plan_stumps(b1, cls, n_parts);
   if (mem == PA_MEM_HOST) {
     b1.scratch<float>(din);
     b1.scratch<float>(dout);
+  }
+  if (rk) {
+    b1.scratch<uint32_t>(rank_bytes(dim, G, n_fields) / 4);
+    b1.scratch<int>(1);
   }
   Builder b;
   b.dry = false;
@@ -2797,19 +2933,34 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
     d_in = b.scratch<float>(din);
     d_out = b.scratch<float>(dout);
   }
+  uint32_t *ranks = rk ? b.scratch<uint32_t>(rank_bytes(dim, G, n_fields) / 4) : nullptr;
+  int *d_err = rk ? b.scratch<int>(1) : nullptr;
   st = upload_blob(ctx, b);
   if (st) return st;
   if (mem == PA_MEM_HOST) {
     st = copy_in(ctx, (void *)d_in, desc, din * sizeof(float), mem);
     if (st) return st;
   }
-  const std::vector<char> ff = fast_flags(cls, n_parts);
-  const std::vector<int> ns = stump_counts(cls, n_parts);
-  PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, d_in, nullptr, false, G,
-                                              n_fields, dim, normalize, d_out, ctx->stream));
+  int errflag = 0;
+  if (rk) {
+    PA_CK(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+    PA_LAUNCH("stump_ranks", launch_rank_buckets(*rk, d_in, nullptr, ((uintptr_t)d_in & 15) == 0, G,
+                                                 n_fields, ranks, ctx->stream));
+    PA_LAUNCH("stump_votes", launch_rank_votes(*rk, G, n_fields, normalize, d_out, ranks, d_err,
+                                               ctx->stream));
+    PA_CK(cudaMemcpyAsync(&errflag, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    const std::vector<char> ff = fast_flags(cls, n_parts);
+    const std::vector<int> ns = stump_counts(cls, n_parts);
+    PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, d_in, nullptr, false, G,
+                                                n_fields, dim, normalize, d_out, ctx->stream));
+  }
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-  return sync_ctx(ctx);
+  st = sync_ctx(ctx);
+  if (st) return st;
+  if (errflag) return fail(ctx, PA_ERR_CUDA, "rank tile copy did not complete (error bits %d)", errflag);
+  return PA_OK;
 } catch (const std::bad_alloc &) {
   return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
 } catch (const std::exception &exc) {

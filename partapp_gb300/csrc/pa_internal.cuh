@@ -339,6 +339,26 @@ void msg_params(const pa_exp_param *e, double scale, const double *oc, const dou
 // Score grids read field f at fields[f] (a device array) when given, else at
 // desc + f * n_loc * dim; fields_aligned: every field pointer is 16-byte
 // aligned.
+// Rank form of the stump test (k_stump.cu): device tables of one classifier
+// set with unit polarities, at most 127 distinct thresholds per feature.
+struct RankTables {
+  const float *eyt;        // [dim][2^d + 1] per feature: the thresholds in
+                           // Eytzinger order at 1 .. 2^d - 1, +inf padded
+  const uint2 *rec;        // [n_cls][npad] {f * 128 | (0x80 + k) << 24, bits of -a}
+  const float *sum_alpha;  // [n_cls]
+  int d, dim, n_cls, npad;
+};
+size_t rank_bytes(int dim, int64_t n_loc, int n_fields);  // rank tiles of a call
+size_t rank_votes_smem(int dim, int n_cls, int npad);
+// k_rank_buckets: the rank tiles of the call's descriptors
+// (aligned: every field starts on a 16-byte boundary)
+cudaError_t launch_rank_buckets(const RankTables &rt, const float *desc,
+                                const float *const *fields, bool aligned, int64_t n_loc,
+                                int n_fields, uint32_t *ranks, cudaStream_t s);
+// k_rank_votes: the score grids from the rank tiles; err bit 8: a tile copy
+// did not complete
+cudaError_t launch_rank_votes(const RankTables &rt, int64_t n_loc, int n_fields, int normalize,
+                              float *scores, const uint32_t *ranks, int *err, cudaStream_t s);
 cudaError_t launch_score_grids(const StumpPart *parts_dev, const bool *fast_ok,
                                const int *n_stumps, int n_parts, const float *desc,
                                const float *const *fields, bool fields_aligned,
