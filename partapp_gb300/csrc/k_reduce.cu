@@ -19,10 +19,12 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
 // log_from_root.  This kernel performs those sums element-wise in that order
 // and folds the maxima that the downward messages need and the argmax of the
 // root marginal (:261-277).
+// KC: the most root children of the images; U: cells per thread and step.
+template <int KC, int U>
 __global__ void __launch_bounds__(kThreads) k_root_combine(const RootDesc *__restrict__ rds,
                                                            int64_t N) {
-  root_combine_cells(rds[blockIdx.y], (int64_t)blockIdx.x * blockDim.x, N,
-                     (int64_t)gridDim.x * blockDim.x);
+  root_combine_cells<KC, U>(rds[blockIdx.y], (int64_t)blockIdx.x * blockDim.x, N,
+                            (int64_t)gridDim.x * blockDim.x);
 }
 
 // Root posterior over the kept rotations (objectdetect_findrot.cpp:694-726):
@@ -196,11 +198,15 @@ cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
   return cudaGetLastError();
 }
 
-cudaError_t launch_root_combine(const RootDesc *rd, int n_roots, int64_t N, cudaStream_t s) {
+cudaError_t launch_root_combine(const RootDesc *rd, int n_roots, int64_t N, int max_k,
+                                cudaStream_t s) {
   int blocks = (int)((N + kThreads - 1) / kThreads);
   if (blocks > 152 * 4) blocks = 152 * 4;
   dim3 grid((unsigned)blocks, (unsigned)n_roots);
-  k_root_combine<<<grid, kThreads, 0, s>>>(rd, N);
+  if (max_k <= 8)  // four cells per thread and step, their loads in flight together
+    k_root_combine<8, 4><<<grid, kThreads, 0, s>>>(rd, N);
+  else
+    k_root_combine<kMaxRootChildren, 1><<<grid, kThreads, 0, s>>>(rd, N);
   return cudaGetLastError();
 }
 

@@ -359,21 +359,32 @@ __global__ void __launch_bounds__(32 * kRankWarps1) k_rank_buckets(
       for (int j = 0; j < 4; ++j) v4[j] = ok ? __ldg(p + j) : 0.f;
     }
   };
-  for (int64_t t = cta; t < n_tiles; t += n_cta) {
+  // slab base of tile t's field and the tile's first location
+  auto tile_src = [&](int64_t t, int64_t &loc0) {
     const int field = (int)(t / tiles_per_field);
-    const int64_t loc0 = (t - (int64_t)field * tiles_per_field) * kRankLoc;
-    const float *fb = (fields ? fields[field] : desc + (int64_t)field * n_loc * dim) + f0 + 4 * lane;
-    float v[8], vn[8];
-    {
-      const int64_t loc = loc0 + warp;
-      load(fb + loc * dim, in0 && loc < n_loc, v);
-      load(fb + loc * dim + 128, in1 && loc < n_loc, v + 4);
-    }
+    loc0 = (t - (int64_t)field * tiles_per_field) * kRankLoc;
+    return (fields ? fields[field] : desc + (int64_t)field * n_loc * dim) + f0 + 4 * lane;
+  };
+  float v[8], vn[8];
+  if (cta < n_tiles) {
+    int64_t loc0;
+    const float *fb = tile_src(cta, loc0);
+    const int64_t loc = loc0 + warp;
+    load(fb + loc * dim, in0 && loc < n_loc, v);
+    load(fb + loc * dim + 128, in1 && loc < n_loc, v + 4);
+  }
+  for (int64_t t = cta; t < n_tiles; t += n_cta) {
+    int64_t loc0, loc0n = 0;
+    const float *fb = tile_src(t, loc0);
+    // the location after the last one of this tile: the next tile's first
+    const float *fbn = t + n_cta < n_tiles ? tile_src(t + n_cta, loc0n) : fb;
     for (int l = warp; l < kRankLoc; l += nw) {
-      const int64_t locn = loc0 + l + nw;
-      const bool more = l + nw < kRankLoc && locn < n_loc;
-      load(fb + locn * dim, in0 && more, vn);
-      load(fb + locn * dim + 128, in1 && more, vn + 4);
+      const bool here = l + nw < kRankLoc;
+      const int64_t locn = here ? loc0 + l + nw : loc0n + warp;
+      const float *src = here ? fb : fbn;
+      const bool more = (here || t + n_cta < n_tiles) && locn < n_loc;
+      load(src + locn * dim, in0 && more, vn);
+      load(src + locn * dim + 128, in1 && more, vn + 4);
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         // step right unless v < entry: "v >= entry or unordered", so a NaN

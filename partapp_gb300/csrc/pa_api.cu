@@ -1108,7 +1108,8 @@ pa_status run_ps(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
       if (!ph.n) continue;
       if (pa_status s2 = run_phase(ph)) return s2;
     }
-    PA_LAUNCH("root_combine", launch_root_combine(pl.roots, B, pl.N, st));
+    PA_LAUNCH("root_combine", launch_root_combine(pl.roots, B, pl.N,
+                                                  (int)pl.sc.ch[pl.sc.root].size(), st));
     for (auto &ph : pl.down) {
       if (!ph.n) continue;
       if (pa_status s2 = run_phase(ph)) return s2;

@@ -415,7 +415,9 @@ cudaError_t launch_msg_cols(const MsgDesc *msgs, int n_msgs, int R, int H, int W
 bool make_e2_map(CUtensorMap *m, const float *e2, int R, int H, int W);
 // Column-pass TMA map of an epilogue input (src0 / src1) [R][H][W].
 bool make_src_map(CUtensorMap *m, const float *src, int R, int H, int W);
-cudaError_t launch_root_combine(const RootDesc *rd, int n_roots, int64_t N, cudaStream_t s);
+// max_k: the most root children among the descriptors (rd.k <= max_k)
+cudaError_t launch_root_combine(const RootDesc *rd, int n_roots, int64_t N, int max_k,
+                                cudaStream_t s);
 cudaError_t launch_root_posterior(const float *const *post_root, float *const *root_post,
                                   const int *keep, int n_keep, int n_images, int R, int H, int W,
                                   cudaStream_t s);
