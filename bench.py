@@ -60,6 +60,8 @@ def parse():
                     help="uneven: images per call")
     ap.add_argument("--images-per-wave", type=int, default=32,
                     help="uneven: images per persistent message-passing launch")
+    ap.add_argument("--pool-gb", type=float, default=12.0,
+                    help="uneven: size of the descriptor pool the images view")
     ap.add_argument("--learned", type=int, default=1,
                     help="find_obj: add the learned-vs-plain comparison (320x240, R=24)")
     ap.add_argument("--train-fields", type=int, default=20000)
@@ -642,7 +644,7 @@ def run_uneven(args):
     each wave of --images-per-wave images in one persistent launch) and through
     pa_find_obj_multi (one launch per message group).  256 such images would
     need ~300 GB of descriptors side by side, so each image's descriptors are
-    a view at a seeded offset into one 12 GB pool of Gamma(0.5, 1) rows,
+    a view at a seeded offset into one pool (--pool-gb, 12 GB) of Gamma(0.5, 1) rows,
     L2-normalised per location (the inputs are larger than L2).  Also the
     latency spread of one-image calls over the first 32 images."""
     import torch
@@ -661,7 +663,8 @@ def run_uneven(args):
     cls = ctx.classifiers(models)
     g = torch.Generator(device=dev)
     g.manual_seed(args.seed)
-    pool_rows = 3 << 20
+    # rows of the largest image the generator can draw: 48 x 160 x 160
+    pool_rows = max(48 * 160 * 160, int(args.pool_gb * 2**30) // (4 * D))
     pool = torch.empty((pool_rows, D), device=dev)
     for r0 in range(0, pool_rows, 1 << 18):
         z = pool[r0:r0 + (1 << 18)]
@@ -719,7 +722,7 @@ def run_uneven(args):
             "config": {"workload": f"find_obj, {n} images per call, H, W ~ U{{200..640}}/4*4, "
                                    "R in {12,24,48}, 10 classifiers x 500 stumps, 960-d, 10-part PS",
                        "images_per_wave": args.images_per_wave,
-                       "l2": "inputs larger than L2 (12 GB descriptor pool)"},
+                       "l2": f"inputs larger than L2 ({args.pool_gb:g} GB descriptor pool)"},
             "queue": queue, "grouped_launches": grouped,
             "latency_ms_one_image": {"p50": float(np.percentile(lat, 50)),
                                      "p99": float(np.percentile(lat, 99)),
