@@ -67,8 +67,10 @@ struct pa_ctx {
   };
   static constexpr int kLandings = 3;
   std::vector<Landing> land = std::vector<Landing>(kLandings);  // grown by pa_find_obj_queue
-  // pa_find_obj_queue: side streams of the per-image work around the queue
+  // pa_find_obj_queue: side streams of the per-image work around the queue,
+  // pinned status words of the wave in flight
   std::vector<cudaStream_t> side;
+  int *qwords = nullptr;
   std::vector<cudaEvent_t> ring_done;  // per ring slot: the slot's image is computed
   // host-input ring: descriptor slots filled on copy_stream while the main
   // stream computes on the previous slot
@@ -2144,6 +2146,7 @@ struct QGroup {
   uint32_t *ranks = nullptr;
   UnaryMap *umaps = nullptr;
   int usep = 0;
+  Readback rb;  // where the group's small results land
 };
 
 // Plans one group (images of one shape) into b; `proto` carries the sizes
@@ -2520,10 +2523,18 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
   PA_LAUNCH("ps_queue", launch_ps_queue(d_jobs, (int)jobs.size(), n_items, d_head, d_done, d_status,
                                         groups[0].pl.err, wait_ns, smem, &ctas,
                                         stats ? d_stats : nullptr, s));
-  int status = 0;
-  PA_CK(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
-  PA_CK(cudaStreamSynchronize(s));
+  // the status word and the first group's error word (the tiles' error
+  // bits) land in pinned memory, read when the wave is finished
+  if (!ctx->qwords) {
+    if (cudaMallocHost(&ctx->qwords, 4 * sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_NOMEM, "cannot allocate pinned status words");
+    }
+  }
+  PA_CK(cudaMemcpyAsync(ctx->qwords, d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PA_CK(cudaMemcpyAsync(ctx->qwords + 1, groups[0].pl.err, sizeof(int), cudaMemcpyDeviceToHost, s));
   if (stats) {
+    PA_CK(cudaStreamSynchronize(s));
     unsigned long long h[16];
     PA_CK(cudaMemcpy(h, d_stats, sizeof h, cudaMemcpyDeviceToHost));
     static const char *names[4] = {"rows", "cols", "root", "rows48"};
@@ -2535,29 +2546,33 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
                      names[t], h[4 * t + 3], 1e-3 * h[4 * t] / h[4 * t + 3],
                      1e-3 * h[4 * t + 1] / h[4 * t + 3], 1e-3 * h[4 * t + 2] / h[4 * t + 3]);
   }
-  if (status & 1) return fail(ctx, PA_ERR_TIMEOUT, "a queue dependency wait ran out (%.0f ms)",
-                              o.wait_timeout_ms > 0 ? o.wait_timeout_ms : 20000.0);
-  // a tile's error bits went to the first group's word: carry them to all
-  int err0 = 0;
-  PA_CK(cudaMemcpyAsync(&err0, groups[0].pl.err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  PA_CK(cudaStreamSynchronize(s));
-  // tails: each group's results land in its own pinned block; one sync
+  // tails: each group's results land in its own pinned block (read by
+  // queue_wave_finish after one sync)
   if (ctx->land.size() < groups.size()) ctx->land.resize(groups.size());
-  std::vector<Readback> rb(groups.size());
   if (pa_status st = fork()) return st;
   for (size_t k = 0; k < groups.size(); ++k) {
     QGroup &g = groups[k];
     OnStream on(ctx, ctx->side[k % NS]);
-    if (err0 && k > 0) PA_LAUNCH("fill", launch_fill_int(g.pl.err, err0, 1, ctx->stream));
     if (pa_status st = run_ps_tail(ctx, g.f->ep, g.pl)) return st;
-    if (pa_status st = finish_enqueue(ctx, g.f->ep, g.pl, g.outs.data(), PA_MEM_DEVICE, (int)k, rb[k]))
+    if (pa_status st = finish_enqueue(ctx, g.f->ep, g.pl, g.outs.data(), PA_MEM_DEVICE, (int)k, g.rb))
       return st;
   }
-  if (pa_status st = join()) return st;
+  return join();
+}
+
+// Waits for a wave queued by queue_wave on ctx and decodes its results.
+pa_status queue_wave_finish(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_queue_opts &o) {
   if (pa_status st = sync_ctx(ctx)) return st;
+  if (ctx->qwords[0] & 1)
+    return fail(ctx, PA_ERR_TIMEOUT, "a queue dependency wait ran out (%.0f ms)",
+                o.wait_timeout_ms > 0 ? o.wait_timeout_ms : 20000.0);
+  // a tile's error bits went to the first group's word: they count for all
+  const int err0 = ctx->qwords[1];
   pa_status result = PA_OK;
   for (size_t k = 0; k < groups.size(); ++k) {
-    const pa_status st = finish_complete(ctx, groups[k].f->ep, groups[k].pl, groups[k].outs.data(), rb[k]);
+    QGroup &g = groups[k];
+    if (k > 0) *g.rb.err |= err0;
+    const pa_status st = finish_complete(ctx, g.f->ep, g.pl, g.outs.data(), g.rb);
     if (st == PA_ERR_NUMERIC) result = st;
     else if (st) return st;
   }
@@ -2642,6 +2657,7 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) try {
     }
     for (auto &kv : ctx->rank_sets)
       if (kv.second.mem) cudaFree(kv.second.mem);
+    if (ctx->qwords) cudaFreeHost(ctx->qwords);
     if (ctx->copy_stream) {
       cudaStreamSynchronize(ctx->copy_stream);
       cudaStreamDestroy(ctx->copy_stream);
@@ -4045,9 +4061,60 @@ pa_status pa_find_obj_queue(pa_ctx *ctx, int n_images, const pa_image *imgs,
   };
   DeviceGuard dg(ctx->device);
   pa_status result = PA_OK;
-  for (int w0 = 0; w0 < n_images; w0 += o.images_per_wave) {
+  // Waves alternate between two contexts (the caller's and a worker, each
+  // with its own workspace, streams and landing blocks), so that the host
+  // plans and queues wave k + 1 while the GPU runs wave k; a context's wave
+  // is finished before the context takes the next one.
+  const int n_waves = (n_images + o.images_per_wave - 1) / o.images_per_wave;
+  pa_ctx *wc[2] = {ctx, nullptr};
+  if (n_waves > 1) {
+    if (ctx->workers.empty()) {
+      pa_ctx *w = nullptr;
+      if (pa_ctx_create(ctx->device, &w) != PA_OK)
+        return fail(ctx, PA_ERR_CUDA, "cannot create a worker context");
+      ctx->workers.push_back(w);
+    }
+    wc[1] = ctx->workers[0];
+    wc[1]->msg_math = ctx->msg_math;
+    wc[1]->timing = ctx->timing;
+    if (wc[1]->row_tile.empty()) wc[1]->row_tile = ctx->row_tile;
+    while (ctx->ring_done.empty()) {
+      cudaEvent_t ev;
+      PA_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      ctx->ring_done.push_back(ev);
+    }
+    // the worker starts behind everything queued on the caller's stream
+    PA_CK(cudaEventRecord(ctx->ring_done[0], ctx->stream));
+    PA_CK(cudaStreamWaitEvent(wc[1]->stream, ctx->ring_done[0], 0));
+  }
+  std::vector<QGroup> pend[2];
+  bool busy[2] = {false, false};
+  auto finish = [&](int k) -> pa_status {
+    if (!busy[k]) return PA_OK;
+    busy[k] = false;
+    pa_status st = queue_wave_finish(wc[k], pend[k], o);
+    if (st && wc[k] != ctx) ctx->err = wc[k]->err;
+    return st;
+  };
+  auto finish_all = [&]() -> pa_status {
+    pa_status st0 = finish(0), st1 = finish(1);
+    if (st0 == PA_ERR_NUMERIC) result = st0, st0 = PA_OK;
+    if (st1 == PA_ERR_NUMERIC) result = st1, st1 = PA_OK;
+    return st0 ? st0 : st1;
+  };
+  int wave = 0;
+  for (int w0 = 0; w0 < n_images; w0 += o.images_per_wave, ++wave) {
     const int w1 = std::min(n_images, w0 + o.images_per_wave);
-    std::vector<QGroup> groups;
+    const int slot = wave & 1;
+    if (pa_status st = finish(slot)) {
+      if (st != PA_ERR_NUMERIC) {
+        finish_all();
+        return st;
+      }
+      result = st;
+    }
+    std::vector<QGroup> &groups = pend[slot];
+    groups.clear();
     std::vector<int> grp(w1 - w0, -1);
     for (int i = w0; i < w1; ++i) {
       if (grp[i - w0] >= 0) continue;
@@ -4066,7 +4133,18 @@ pa_status pa_find_obj_queue(pa_ctx *ctx, int n_images, const pa_image *imgs,
       g.marg_out.push_back(imgs[i].out->log_marg);
       g.rp_out.push_back(imgs[i].out->root_post);
     }
-    pa_status st = queue_wave(ctx, groups, cls, n_cls, o);
+    pa_status st = queue_wave(wc[slot], groups, cls, n_cls, o);
+    if (st == PA_OK) {
+      busy[slot] = true;
+      continue;
+    }
+    if (wc[slot] != ctx) ctx->err = wc[slot]->err;
+    // the wave stopped part way (kernels of its unaries may be queued):
+    // drain its context, then the other's wave
+    cudaStreamSynchronize(wc[slot]->stream);
+    for (cudaStream_t ss : wc[slot]->side) cudaStreamSynchronize(ss);
+    cudaGetLastError();
+    if (pa_status st2 = finish_all()) return st2;
     if (st == PA_ERR_UNSUPPORTED) {
       // a path the queue does not run: this wave as pa_find_obj_multi does it
       st = pa_find_obj_multi(ctx, w1 - w0, imgs + w0, cls, n_cls, PA_MEM_DEVICE);
@@ -4077,6 +4155,7 @@ pa_status pa_find_obj_queue(pa_ctx *ctx, int n_images, const pa_image *imgs,
     }
     if (st) return st;
   }
+  if (pa_status st = finish_all()) return st;
   return result;
 } catch (const std::bad_alloc &) {
   return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
