@@ -118,7 +118,7 @@ def trained(ctx, cls, models, train_fields, eval_fields, eval_scores, widths=(64
             ye = torch.cat([net(xe[i:i + 65536]).T for i in range(0, xe.shape[0], 65536)], 1)
         r = _summary(_errors(ye, te, me))
         r["train_s"] = round(time.time() - t0, 1)
-        r["final_loss"] = float(loss)
+        r["final_loss"] = float(loss.detach())
         res[f"H {H}"] = r
     return res
 
