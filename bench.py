@@ -199,9 +199,13 @@ def algorithmic_bytes(trees, batch):
 
 
 def with_unary_total(kt):
-    """kernel_times() with "score_grids" = the whole AdaBoost unary stage: the
-    float kernel, or the rank form's two kernels (stump_ranks + stump_votes)."""
+    """kernel_times() with "score_grids" = the whole AdaBoost unary stage (the
+    float kernel, or the rank form's stump_ranks + stump_votes) and
+    "local_max" = its three stages (lm_cand, lm_select, lm_final)."""
     kt = dict(kt)
+    if any(k in kt for k in ("lm_cand", "lm_select", "lm_final")):
+        parts = [kt.get(k, (0.0, 0)) for k in ("lm_cand", "lm_select", "lm_final")]
+        kt["local_max"] = (sum(p[0] for p in parts), sum(p[1] for p in parts))
     if "stump_ranks" in kt or "stump_votes" in kt:
         a, b = kt.get("stump_ranks", (0.0, 0)), kt.get("stump_votes", (0.0, 0))
         f = kt.get("score_grids", (0.0, 0))

@@ -311,10 +311,11 @@ struct LmLayout {
 constexpr int kRadixPasses = 8;  // 8-bit digits of the 64-bit keys
 constexpr int kRadixCtas = 8;    // CTAs per map in a histogram pass
 
-int local_max_kernels(int64_t cells, int k) {
+int local_max_kernels(int64_t cells, int k, int stages) {
   (void)cells;
   (void)k;
-  return 3 + kRadixPasses;  // counts, init, candidates + passes + final
+  return ((stages & LM_CAND) ? 2 : 0) + ((stages & LM_SELECT) ? kRadixPasses : 0) +
+         ((stages & LM_FINAL) ? 1 : 0);  // init + candidates, passes, final
 }
 
 size_t local_max_scratch_bytes(int n_maps, int64_t cells, int k) {
@@ -329,7 +330,7 @@ size_t local_max_scratch_bytes(int n_maps, int64_t cells, int k) {
 
 cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H, int W, int k,
                              void *scratch, float *hyps, int *n_hyps, cudaStream_t s,
-                             int *n_kernels) {
+                             int *n_kernels, int stages) {
   if (k < 1 || k > kChunk / 2) return cudaErrorInvalidValue;
   const int64_t cells = (int64_t)S * H * W;
   if (cells > 0xFFFFFFFFll) return cudaErrorInvalidValue;  // 32-bit enumeration index
@@ -341,22 +342,32 @@ cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H,
       reinterpret_cast<unsigned int *>(base + L.take((size_t)n_maps * 256 * sizeof(unsigned int)));
   unsigned long long *keys =
       reinterpret_cast<unsigned long long *>(base + L.take((size_t)n_maps * cells * 8));
-  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * n_maps, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * 256 * n_maps, s);
-  if (e != cudaSuccess) return e;
-  k_lm_init<<<(n_maps + 127) / 128, 128, 0, s>>>(state, n_maps, k);
-  const int rows_per_cta = kLmWarps * kLmRows;
   if (n_maps > 65535) return cudaErrorInvalidValue;
-  k_lm_cand<<<dim3((unsigned)((W + kLmCols - 1) / kLmCols),
-                   (unsigned)((H + rows_per_cta - 1) / rows_per_cta), (unsigned)n_maps),
-              32 * kLmWarps, 0, s>>>(maps, S, H, W, keys, cells, counts);
-  const int room = kChunk - k;
-  for (int pass = 0; pass < kRadixPasses; ++pass)
-    k_lm_radix<<<dim3(kRadixCtas, (unsigned)n_maps), 256, 0, s>>>(keys, counts, cells, pass, room,
-                                                                   hist, state);
-  k_lm_final<<<(unsigned)n_maps, kThreads, 0, s>>>(keys, counts, cells, state, k, S, H, W, hyps,
-                                                   n_hyps);
-  if (n_kernels) *n_kernels = 3 + kRadixPasses;
+  int nk = 0;
+  if (stages & LM_CAND) {
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * n_maps, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * 256 * n_maps, s);
+    if (e != cudaSuccess) return e;
+    k_lm_init<<<(n_maps + 127) / 128, 128, 0, s>>>(state, n_maps, k);
+    const int rows_per_cta = kLmWarps * kLmRows;
+    k_lm_cand<<<dim3((unsigned)((W + kLmCols - 1) / kLmCols),
+                     (unsigned)((H + rows_per_cta - 1) / rows_per_cta), (unsigned)n_maps),
+                32 * kLmWarps, 0, s>>>(maps, S, H, W, keys, cells, counts);
+    nk += 2;
+  }
+  if (stages & LM_SELECT) {
+    const int room = kChunk - k;
+    for (int pass = 0; pass < kRadixPasses; ++pass)
+      k_lm_radix<<<dim3(kRadixCtas, (unsigned)n_maps), 256, 0, s>>>(keys, counts, cells, pass,
+                                                                     room, hist, state);
+    nk += kRadixPasses;
+  }
+  if (stages & LM_FINAL) {
+    k_lm_final<<<(unsigned)n_maps, kThreads, 0, s>>>(keys, counts, cells, state, k, S, H, W, hyps,
+                                                     n_hyps);
+    nk += 1;
+  }
+  if (n_kernels) *n_kernels = nk;
   return cudaGetLastError();
 }
 

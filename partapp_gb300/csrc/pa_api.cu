@@ -1137,18 +1137,22 @@ pa_status run_ps_tail(pa_ctx *ctx, const pa_exp_param *e, PsPlan &pl) {
   if (pl.want_part_hyps) {
     const int first = pl.hyp_img >= 0 ? pl.hyp_img * P : 0;
     const int n_maps = pl.hyp_img >= 0 ? P : B * P;
-    PA_LAUNCH_N("local_max", local_max_kernels(pl.N, pl.hyp_k),
-                launch_local_max(pl.marg_ptrs + first, n_maps, R, H, W, pl.hyp_k, pl.lm_scratch,
-                                 pl.part_hyps, pl.n_part_hyps, st, nullptr));
+    static const char *names[3] = {"lm_cand", "lm_select", "lm_final"};
+    for (int g = 0; g < 3; ++g)
+      PA_LAUNCH_N(names[g], local_max_kernels(pl.N, pl.hyp_k, 1 << g),
+                  launch_local_max(pl.marg_ptrs + first, n_maps, R, H, W, pl.hyp_k, pl.lm_scratch,
+                                   pl.part_hyps, pl.n_part_hyps, st, nullptr, 1 << g));
   }
   if (pl.want_root_hyps) {
     // one [S][H][W] grid with scale neighbours (objectdetect_aux.cpp:193-236) when
     // the entries are the scales of one image, else one [1][H][W] grid per image
     const int n_maps = pl.root_joint ? 1 : B, S = pl.root_joint ? B : 1;
-    PA_LAUNCH_N("local_max", local_max_kernels((int64_t)S * H * W, kRootHyps),
-                launch_local_max(reinterpret_cast<const float *const *>(pl.root_post_ptrs), n_maps,
-                                 S, H, W, kRootHyps, pl.lm_scratch, pl.root_hyps, pl.n_root_hyps,
-                                 st, nullptr));
+    static const char *names[3] = {"lm_cand", "lm_select", "lm_final"};
+    for (int g = 0; g < 3; ++g)
+      PA_LAUNCH_N(names[g], local_max_kernels((int64_t)S * H * W, kRootHyps, 1 << g),
+                  launch_local_max(reinterpret_cast<const float *const *>(pl.root_post_ptrs),
+                                   n_maps, S, H, W, kRootHyps, pl.lm_scratch, pl.root_hyps,
+                                   pl.n_root_hyps, st, nullptr, 1 << g));
   }
   return PA_OK;
 }

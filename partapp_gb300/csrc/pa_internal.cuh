@@ -428,10 +428,14 @@ cudaError_t launch_map_max(const float *x, int64_t N, int *max_slot, cudaStream_
 // findLocalMax of n_maps [S][H][W] grids: up to k (1..2048) maxima per map as
 // (s, x, y, value) rows in hyps[map][k][4], their number in n_hyps[map].
 size_t local_max_scratch_bytes(int n_maps, int64_t cells, int k);
-int local_max_kernels(int64_t cells, int k);
+// findLocalMax in three stages that run in this order on one stream:
+// candidates (with the scratch's counters reset), the radix selection, the
+// final gather and sort; `stages` is a mask of them.
+enum { LM_CAND = 1, LM_SELECT = 2, LM_FINAL = 4, LM_ALL = 7 };
+int local_max_kernels(int64_t cells, int k, int stages = LM_ALL);
 cudaError_t launch_local_max(const float *const *maps, int n_maps, int S, int H, int W, int k,
                              void *scratch, float *hyps, int *n_hyps, cudaStream_t s,
-                             int *n_kernels);
+                             int *n_kernels, int stages = LM_ALL);
 cudaError_t launch_argmax(const float *const *maps, int n_maps, int64_t N,
                           unsigned long long *amax, cudaStream_t s);
 // log Z of each map in double (float-float partial sums, FP64 total);
