@@ -343,6 +343,13 @@ double rot_step_rad(const pa_exp_param *e) {
 
 // get_gaussian_filter, boost_math.cpp:104-117 (unnormalised)
 std::vector<double> gaussian_taps(double sigma) {
+  // the same sigmas recur across the images and calls of a model: the taps
+  // are kept per host thread, keyed by sigma's bits (cleared past 4096)
+  thread_local std::map<uint64_t, std::vector<double>> memo;
+  uint64_t key;
+  std::memcpy(&key, &sigma, sizeof key);
+  auto it = memo.find(key);
+  if (it != memo.end()) return it->second;
   int ksize = (int)std::floor(3 * sigma + 0.5);
   std::vector<double> f(2 * ksize + 1);
   f[ksize] = 1.0;
@@ -350,14 +357,36 @@ std::vector<double> gaussian_taps(double sigma) {
     f[ksize + i] = std::exp(-i * i / (2 * sigma * sigma));
     f[ksize - i] = f[ksize + i];
   }
+  if (memo.size() >= 4096) memo.clear();
+  memo.emplace(key, f);
   return f;
 }
 
 // prod(prod(R(alpha), S(scale)), (ox, oy, 0)), objectdetect_findrot.cpp:348-351
+// cos and sin of the float angle of every rotation bin, kept per host thread
+// for the last rotation set seen (a plan rotates two offsets per message and
+// rotation bin: ~7000 pairs for 4 images at R = 24).
+const std::vector<std::pair<double, double>> &rotation_trig(const pa_exp_param *e) {
+  thread_local int n = -1;
+  thread_local float lo = 0.f, hi = 0.f;
+  thread_local std::vector<std::pair<double, double>> tab;
+  if (n != e->num_rotation_steps || lo != e->min_part_rotation || hi != e->max_part_rotation) {
+    n = e->num_rotation_steps;
+    lo = e->min_part_rotation;
+    hi = e->max_part_rotation;
+    tab.resize(n > 0 ? n : 0);
+    for (int r = 0; r < n; ++r) {
+      const float alpha = (float)(rot_from_index(e, r) * M_PI / 180.0);
+      tab[r] = {std::cos((double)alpha), std::sin((double)alpha)};
+    }
+  }
+  return tab;
+}
+
 void rotate_offset(const pa_exp_param *e, int r, double scale, const double *o, double &dx,
                    double &dy) {
-  float alpha = (float)(rot_from_index(e, r) * M_PI / 180.0);
-  double ca = std::cos((double)alpha), sa = std::sin((double)alpha);
+  const auto &cs = rotation_trig(e)[r];
+  const double ca = cs.first, sa = cs.second;
   double t00 = ca * scale, t01 = (-sa) * scale;
   double t10 = sa * scale, t11 = ca * scale;
   dx = t00 * o[0] + t01 * o[1];
