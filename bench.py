@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=4, help="images per step")
+    ap.add_argument("--batch", type=int, default=16, help="images per step")
     ap.add_argument("--e2e-batch", type=int, default=8,
                     help="images per end-to-end call (host descriptors through the copy ring)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
@@ -268,14 +268,15 @@ def compute_rooflines(kernels, ops, steps, sm_mhz, n_sm):
             kernels[k]["fma_per_s"] = f / t
 
 
-def traffic_from_profiles(kernel):
-    """dram read+write bytes per launch of `kernel` from the committed ncu
-    summary, if present (profiles/traffic.json)."""
+def traffic_from_profiles(kernel, images, launches):
+    """dram read+write bytes per launch of `kernel`: the committed ncu
+    capture's bytes per image (profiles/traffic.json), times the images of a
+    step, over the step's launches of the kernel."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             d = json.load(f)
         v = d.get(kernel)
-        return None if v is None else float(v["bytes_per_launch"])
+        return None if v is None else float(v["bytes_per_image"]) * images / launches
     except (OSError, ValueError, KeyError):
         return None
 
@@ -468,7 +469,8 @@ def run_ours(args):
         achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
-                "traffic": traffic_from_profiles(dom), "alg_bytes_per_launch": per_launch_bytes,
+                "traffic": traffic_from_profiles(dom, B, dom_n / args.steps),
+                "alg_bytes_per_launch": per_launch_bytes,
                 "avg_launch_ms": avg_ms}
     kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps}
                for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][0])}
