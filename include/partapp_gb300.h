@@ -493,6 +493,28 @@ pa_status pa_nms_recursive(pa_ctx *ctx, int n, const float *x, const float *y, c
                            const float *score, double train_object_width,
                            double train_object_height, int *suppressed, int mem);
 
+/* nms_recursive of libNms, rectangle form (libNms/nms.cpp:132-225): n
+ * rectangles as corners rects[n][4][2] (x, y; double), sorted by descending
+ * score; suppressed[j] = 1 when an earlier rectangle i has
+ * dx^2 / e1 + dy^2 / e2 < ellipse_size^2, with e1 = |r1 - r0|^2,
+ * e2 = |r1 - r2|^2 of rectangle i, (dx, dy) the offset of j's centre from
+ * i's (centres: the mean of the four corners) projected on i's unit edges
+ * (r1 - r0) / sqrt(e1) and (r1 - r2) / sqrt(e2), every step in double.  The
+ * hypothesis-list form (:58-84) is pa_rect_from_hyp per hypothesis, then
+ * this call; the reference's default ellipse_size is 0.5 (:45-56).  Scores
+ * out of descending order are PA_ERR_INVALID; n <= PA_NMS_MAX_HYPS; `mem`
+ * tells where rects, score and suppressed lie. */
+pa_status pa_nms_rects(pa_ctx *ctx, int n, const double *rects, const double *score,
+                       double ellipse_size, int *suppressed, int mem);
+
+/* rect_from_hyp (libNms/nms.cpp:23-56): the upright rectangle of a
+ * hypothesis (x, y, scale as stored, float), height (int)(scale *
+ * reference_height) and width (int)(scale * reference_width) pixels,
+ * corners rect[4][2] = centre -+ half width, -+ half height in the
+ * reference's order.  Host memory; no context. */
+void pa_rect_from_hyp(float x, float y, float scale, double reference_height,
+                      double reference_width, double *rect);
+
 /* ---------------------------------------------------- learned unary */
 
 /* No counterpart in the reference: a convolutional network that maps a

@@ -140,6 +140,10 @@ def _declare(L):
     L.orc_nms_recursive.argtypes = [C.c_int, fp, fp, fp, fp, C.c_double, C.c_double,
                                     C.POINTER(C.c_int)]
     L.orc_nms_recursive.restype = C.c_int
+    L.orc_rect_from_hyp.argtypes = [C.c_float, C.c_float, C.c_float, C.c_double, C.c_double, dp]
+    L.orc_rect_from_hyp.restype = None
+    L.orc_nms_rects.argtypes = [C.c_int, dp, dp, C.c_double, C.POINTER(C.c_int)]
+    L.orc_nms_rects.restype = C.c_int
     L.orc_find_obj_f32.argtypes = [C.POINTER(OrcExp), C.POINTER(OrcTree), C.POINTER(OrcModels), fp,
                                    C.c_int, C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, fp, fp,
                                    fp, fp, fp, ip, fp, ip]
@@ -408,6 +412,27 @@ def nms_recursive(x, y, scale, score, train_w, train_h):
                                  float(train_h), _p(out, C.c_int))
     if rc:
         raise ValueError(f"orc_nms_recursive failed: {rc}")
+    return out[:n].astype(bool)
+
+
+def rect_from_hyp(x, y, scale, reference_height, reference_width):
+    """libNms rect_from_hyp: corners [4][2] (double) of one hypothesis."""
+    out = np.zeros(8, np.float64)
+    lib().orc_rect_from_hyp(float(np.float32(x)), float(np.float32(y)), float(np.float32(scale)),
+                            float(reference_height), float(reference_width), _p(out, C.c_double))
+    return out.reshape(4, 2)
+
+
+def nms_rects(rects, scores, ellipse_size=0.5):
+    """libNms nms_recursive on rectangles [n][4][2]: suppressed flags (bool [n])."""
+    r = np.ascontiguousarray(rects, dtype=np.float64).reshape(-1, 8)
+    sc = np.ascontiguousarray(scores, dtype=np.float64)
+    n = len(sc)
+    out = np.zeros(max(n, 1), np.int32)
+    rc = lib().orc_nms_rects(n, _p(r, C.c_double), _p(sc, C.c_double), float(ellipse_size),
+                             _p(out, C.c_int))
+    if rc:
+        raise ValueError(f"orc_nms_rects failed: {rc}")
     return out[:n].astype(bool)
 
 

@@ -918,6 +918,61 @@ int orc_nms_recursive(int n, const float *x, const float *y, const float *scale,
   return 0;
 }
 
+/* rect_from_hyp, libNms/nms.cpp:23-56: the upright rectangle (c = 1, s = 0)
+ * of a hypothesis, (int)(scale * reference) pixels high and wide, corners
+ * p - v1 - v2, p + v1 - v2, p + v1 + v2, p - v1 + v2 in QPointF (double)
+ * arithmetic. */
+void orc_rect_from_hyp(float x, float y, float scale, double reference_height,
+                       double reference_width, double *rect) {
+  const int nRectHeight = (int)(scale * reference_height);
+  const int nRectWidth = (int)(scale * reference_width);
+  const double c = 1, s = 0;
+  const double v1x = c * nRectWidth / 2, v1y = s * nRectWidth / 2;
+  const double v2x = -s * nRectHeight / 2, v2y = c * nRectHeight / 2;
+  const double px = x, py = y;
+  rect[0] = px - v1x - v2x, rect[1] = py - v1y - v2y;
+  rect[2] = px + v1x - v2x, rect[3] = py + v1y - v2y;
+  rect[4] = px + v1x + v2x, rect[5] = py + v1y + v2y;
+  rect[6] = px - v1x + v2x, rect[7] = py - v1y + v2y;
+}
+
+/* nms_recursive(rects, rect_scores, nms, ellipse_size), libNms/nms.cpp:
+ * 132-225 (get_rect_center :126-131): rects [n][4][2], scores descending
+ * (returns 2 when not, where the reference asserts); dist_threshold 1.0. */
+int orc_nms_rects(int n, const double *rects, const double *scores, double ellipse_size,
+                  int *nms) {
+  const double dist_threshold = 1.0;
+  if (n < 0) return 1;
+  for (int i = 0; i < n; ++i) nms[i] = 0;
+  auto center = [&](int k, double &cx, double &cy) {
+    const double *r = rects + 8 * (size_t)k;
+    cx = 0.25 * (r[0] + r[2] + r[4] + r[6]);
+    cy = 0.25 * (r[1] + r[3] + r[5] + r[7]);
+  };
+  for (int i = 0; i < n; ++i) {
+    if (i != n - 1 && scores[i] < scores[i + 1]) return 2;
+    const double *r = rects + 8 * (size_t)i;
+    double v1x = r[2] - r[0], v1y = r[3] - r[1];
+    double v2x = r[2] - r[4], v2y = r[3] - r[5];
+    const double e1 = v1x * v1x + v1y * v1y;
+    const double e2 = v2x * v2x + v2y * v2y;
+    const double n1 = std::sqrt(e1), n2 = std::sqrt(e2);
+    v1x /= n1, v1y /= n1;
+    v2x /= n2, v2y /= n2;
+    double c1x, c1y;
+    center(i, c1x, c1y);
+    for (int j = i + 1; j < n; ++j) {
+      double c2x, c2y;
+      center(j, c2x, c2y);
+      const double px = c2x - c1x, py = c2y - c1y;
+      const double dx = v1x * px + v1y * py;
+      const double dy = v2x * px + v2y * py;
+      if (dx * dx / e1 + dy * dy / e2 < ellipse_size * ellipse_size * dist_threshold) nms[j] = 1;
+    }
+  }
+  return 0;
+}
+
 int orc_squeeze_bbox(const float *grid, int ny, int nx, int *bbox) {
   int minx = nx, maxx = -1, miny = ny, maxy = -1;
   for (int ix = 0; ix < nx; ++ix)

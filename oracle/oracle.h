@@ -264,6 +264,13 @@ int orc_nms_recursive(int n, const float *x, const float *y, const float *scale,
                       const float *score, double train_object_width,
                       double train_object_height, int *nms);
 
+/* libNms: rect_from_hyp (corners rect[4][2]) and the rectangle form of
+ * nms_recursive (rects [n][4][2], scores descending; 2 when not sorted). */
+void orc_rect_from_hyp(float x, float y, float scale, double reference_height,
+                       double reference_width, double *rect);
+int orc_nms_rects(int n, const double *rects, const double *scores, double ellipse_size,
+                  int *nms);
+
 int orc_dpm_score(const orc_exp *e, int P, int root, float torso_weight, const float *torso,
                   float head_weight, int head_part, const float *head, float unary_weight,
                   int unary_rot, const float *unary, const int *is_detect, float *lu, int S,

@@ -54,7 +54,8 @@ EXPORTS = (
     "pa_unary_net_create", "pa_unary_net_destroy", "pa_unary_net_get_params",
     "pa_unary_net_set_params", "pa_unary_net_forward", "pa_unary_net_backward",
     "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries", "pa_add_dpm_scores",
-    "pa_nms_recursive", "pa_queue_opts_default", "pa_find_obj_queue",
+    "pa_nms_recursive", "pa_queue_opts_default", "pa_find_obj_queue", "pa_nms_rects",
+    "pa_rect_from_hyp",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
@@ -196,6 +197,9 @@ def load_library():
     L.pa_add_extra_unaries.argtypes = [vp, P(ExpParam), P(ExtraUnary), ip, ip, vp, ip, ip, ip]
     L.pa_add_dpm_scores.argtypes = [vp, P(ExpParam), P(DpmTerms), ip, ip, vp, ip, ip, ip]
     L.pa_nms_recursive.argtypes = [vp, ip, vp, vp, vp, vp, dp, dp, vp, ip]
+    L.pa_nms_rects.argtypes = [vp, ip, vp, vp, dp, vp, ip]
+    L.pa_rect_from_hyp.argtypes = [C.c_float, C.c_float, C.c_float, dp, dp, vp]
+    L.pa_rect_from_hyp.restype = None
     L.pa_unary_net_create.argtypes = [vp, ip, ip, C.c_uint64, P(vp)]
     L.pa_unary_net_destroy.argtypes = [vp, vp]
     L.pa_unary_net_get_params.argtypes = [vp, vp, vp, P(C.c_int64)]
@@ -220,6 +224,15 @@ def exp_param(R=24, min_rot=-180.0, max_rot=180.0, scale=1.0, strip=0.0, local_m
                     int(n_scales))
 
 
+def rect_from_hyp(x, y, scale, reference_height, reference_width) -> np.ndarray:
+    """libNms rect_from_hyp: the corners [4][2] (double) of the upright
+    rectangle of a hypothesis (x, y, scale as stored, float)."""
+    out = np.zeros(8, np.float64)
+    load_library().pa_rect_from_hyp(float(x), float(y), float(scale), float(reference_height),
+                                    float(reference_width), out.ctypes.data)
+    return out.reshape(4, 2)
+
+
 def _is_torch(a):
     return type(a).__module__.startswith("torch")
 
@@ -231,7 +244,7 @@ class _Buf:
         if _is_torch(a):
             import torch
 
-            tdt = {np.float32: torch.float32, np.uint8: torch.uint8}[dtype]
+            tdt = {np.float32: torch.float32, np.float64: torch.float64, np.uint8: torch.uint8}[dtype]
             if not a.is_cuda:
                 raise ValueError("torch tensors must live on the GPU")
             if a.dtype != tdt or not a.is_contiguous():
@@ -686,6 +699,26 @@ class Context:
                                             float(train_object_width), float(train_object_height),
                                             ptr, bufs[0].mem))
         return out if bufs[0].mem == PA_MEM_DEVICE else out.astype(bool)
+
+    def nms_rects(self, rects, scores, ellipse_size=0.5):
+        """libNms nms_recursive on rectangles [n][4][2] (double corners) sorted
+        by descending score (numpy arrays or CUDA tensors, alike): suppressed
+        flags, bool [n] (int32 CUDA tensor for tensor input)."""
+        r = _Buf(rects, np.float64)
+        sc = _Buf(scores, np.float64)
+        n = int(sc.arr.shape[0])
+        if tuple(r.arr.shape) != (n, 4, 2) or r.mem != sc.mem:
+            raise ValueError("rects [n][4][2] and scores [n] must be alike")
+        if sc.mem == PA_MEM_DEVICE:
+            import torch
+
+            out = torch.zeros(n, dtype=torch.int32, device=scores.device)
+            ptr = out.data_ptr()
+        else:
+            out = np.zeros(n, np.int32)
+            ptr = out.ctypes.data
+        self._check(self.L.pa_nms_rects(self.h, n, r.ptr, sc.ptr, float(ellipse_size), ptr, sc.mem))
+        return out if sc.mem == PA_MEM_DEVICE else out.astype(bool)
 
     def compute_root_posterior_rot(self, exp: ExpParam, tree, log_unary, flip=False,
                                    want_marg=True, is_sparse=False):

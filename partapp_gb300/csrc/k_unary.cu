@@ -470,6 +470,68 @@ __global__ void __launch_bounds__(kNmsTile) k_nms(const float *__restrict__ x, c
   if (live) out[j] = sup ? 1 : 0;
 }
 
+// nms_recursive of libNms, rectangle form (libNms/nms.cpp:132-225): rectangle
+// i suppresses every later rectangle j whose centre, projected on i's unit
+// edges v1 = r1 - r0 and v2 = r1 - r2, has dx^2 / e1 + dy^2 / e2 < thr with
+// e1 = |r1 - r0|^2, e2 = |r1 - r2|^2 (all in double, each operation rounded
+// as the reference's QPointF arithmetic rounds it).  One thread per j;
+// earlier rectangles staged in 256-wide shared tiles.
+__device__ __forceinline__ void rect_center(const double *r, double &cx, double &cy) {
+  cx = __dmul_rn(0.25, __dadd_rn(__dadd_rn(__dadd_rn(r[0], r[2]), r[4]), r[6]));
+  cy = __dmul_rn(0.25, __dadd_rn(__dadd_rn(__dadd_rn(r[1], r[3]), r[5]), r[7]));
+}
+
+__global__ void __launch_bounds__(kNmsTile) k_nms_rects(const double *__restrict__ rects,
+                                                       const double *__restrict__ score, int n,
+                                                       double thr, int *__restrict__ out,
+                                                       int *__restrict__ err) {
+  __shared__ double sc[2][kNmsTile], sv[4][kNmsTile], se[2][kNmsTile];
+  const int j = blockIdx.x * kNmsTile + threadIdx.x;
+  const bool live = j < n;
+  double cxj = 0.0, cyj = 0.0;
+  if (live) rect_center(rects + (int64_t)8 * j, cxj, cyj);
+  if (live && j + 1 < n && score[j] < score[j + 1]) atomicOr(err, 1);
+  bool sup = false;
+  const int i_end = min(n, (int)(blockIdx.x + 1) * kNmsTile);  // the block's last j + 1
+  for (int t0 = 0; t0 < i_end; t0 += kNmsTile) {
+    __syncthreads();
+    const int i = t0 + threadIdx.x;
+    if (i < n) {
+      const double *r = rects + (int64_t)8 * i;
+      const double v1x = __dsub_rn(r[2], r[0]), v1y = __dsub_rn(r[3], r[1]);
+      const double v2x = __dsub_rn(r[2], r[4]), v2y = __dsub_rn(r[3], r[5]);
+      const double e1 = __dadd_rn(__dmul_rn(v1x, v1x), __dmul_rn(v1y, v1y));
+      const double e2 = __dadd_rn(__dmul_rn(v2x, v2x), __dmul_rn(v2y, v2y));
+      const double n1 = __dsqrt_rn(e1), n2 = __dsqrt_rn(e2);
+      sv[0][threadIdx.x] = __ddiv_rn(v1x, n1);
+      sv[1][threadIdx.x] = __ddiv_rn(v1y, n1);
+      sv[2][threadIdx.x] = __ddiv_rn(v2x, n2);
+      sv[3][threadIdx.x] = __ddiv_rn(v2y, n2);
+      se[0][threadIdx.x] = e1;
+      se[1][threadIdx.x] = e2;
+      rect_center(r, sc[0][threadIdx.x], sc[1][threadIdx.x]);
+    }
+    __syncthreads();
+    const int m = min(kNmsTile, j - t0);  // earlier rectangles of this tile
+    for (int k = 0; k < m && !sup; ++k) {
+      const double px = __dsub_rn(cxj, sc[0][k]), py = __dsub_rn(cyj, sc[1][k]);
+      const double dx = __dadd_rn(__dmul_rn(sv[0][k], px), __dmul_rn(sv[1][k], py));
+      const double dy = __dadd_rn(__dmul_rn(sv[2][k], px), __dmul_rn(sv[3][k], py));
+      const double q =
+          __dadd_rn(__ddiv_rn(__dmul_rn(dx, dx), se[0][k]), __ddiv_rn(__dmul_rn(dy, dy), se[1][k]));
+      sup = q < thr;
+    }
+  }
+  if (live) out[j] = sup ? 1 : 0;
+}
+
+cudaError_t launch_nms_rects(const double *rects, const double *score, int n, double thr, int *out,
+                             int *err, cudaStream_t s) {
+  if (n < 1) return cudaSuccess;
+  k_nms_rects<<<(n + kNmsTile - 1) / kNmsTile, kNmsTile, 0, s>>>(rects, score, n, thr, out, err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_nms(const float *x, const float *y, const float *scale, const float *score, int n,
                        double train_w, double train_h, int *out, int *err, cudaStream_t s) {
   if (n < 1) return cudaSuccess;

@@ -4352,6 +4352,75 @@ pa_status pa_add_dpm_scores(pa_ctx *ctx, const pa_exp_param *ep, const pa_dpm_te
   return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
+pa_status pa_nms_rects(pa_ctx *ctx, int n, const double *rects, const double *score,
+                       double ellipse_size, int *suppressed, int mem) try {
+  if (!ctx) return PA_ERR_INVALID;
+  if (n < 0 || n > PA_NMS_MAX_HYPS || (n > 0 && (!rects || !score || !suppressed)))
+    return fail(ctx, PA_ERR_INVALID, "invalid rectangle count or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  if (n == 0) return PA_OK;
+  DeviceGuard dg(ctx->device);
+  Builder b1;
+  b1.scratch<int>(1);
+  if (mem == PA_MEM_HOST) {
+    b1.scratch<double>((size_t)9 * n);
+    b1.scratch<int>(n);
+  }
+  pa_status st = ensure_arena(ctx, b1.total());
+  if (st) return st;
+  Builder b;
+  b.dry = false;
+  b.blob_size = b1.blob.size();
+  b.base = ctx->arena;
+  int *err = b.scratch<int>(1);
+  cudaStream_t s = ctx->stream;
+  const double *dr = rects, *dsc = score;
+  int *dout = suppressed;
+  if (mem == PA_MEM_HOST) {
+    double *h = b.scratch<double>((size_t)9 * n);
+    dout = b.scratch<int>(n);
+    PA_CK(cudaMemcpyAsync(h, rects, (size_t)8 * n * sizeof(double), cudaMemcpyHostToDevice, s));
+    PA_CK(cudaMemcpyAsync(h + (size_t)8 * n, score, (size_t)n * sizeof(double),
+                          cudaMemcpyHostToDevice, s));
+    dr = h;
+    dsc = h + (size_t)8 * n;
+  }
+  // square(ellipse_size) * dist_threshold, dist_threshold = 1 (nms.cpp:135-158)
+  const double thr = (ellipse_size * ellipse_size) * 1.0;
+  PA_CK(cudaMemsetAsync(err, 0, sizeof(int), s));
+  PA_LAUNCH("nms", launch_nms_rects(dr, dsc, n, thr, dout, err, s));
+  int flag = 0;
+  PA_CK(cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (mem == PA_MEM_HOST)
+    PA_CK(cudaMemcpyAsync(suppressed, dout, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  if (pa_status ss = sync_ctx(ctx)) return ss;
+  if (flag) return fail(ctx, PA_ERR_INVALID, "unsorted hypothesis vector");
+  return PA_OK;
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
+}
+
+void pa_rect_from_hyp(float x, float y, float scale, double reference_height,
+                      double reference_width, double *rect) {
+  if (!rect) return;
+  const int h = (int)((double)scale * reference_height);
+  const int w = (int)((double)scale * reference_width);
+  const double c = 1.0, sn = 0.0;  // upright rectangles only, as the reference
+  const double v1x = c * w / 2, v1y = sn * w / 2;
+  const double v2x = -sn * h / 2, v2y = c * h / 2;
+  const double px = (double)x, py = (double)y;
+  const double pts[4][2] = {{(px - v1x) - v2x, (py - v1y) - v2y},
+                            {(px + v1x) - v2x, (py + v1y) - v2y},
+                            {(px + v1x) + v2x, (py + v1y) + v2y},
+                            {(px - v1x) + v2x, (py - v1y) + v2y}};
+  for (int k = 0; k < 4; ++k) {
+    rect[2 * k] = pts[k][0];
+    rect[2 * k + 1] = pts[k][1];
+  }
+}
+
 pa_status pa_nms_recursive(pa_ctx *ctx, int n, const float *x, const float *y, const float *scale,
                            const float *score, double train_object_width,
                            double train_object_height, int *suppressed, int mem) try {

@@ -472,6 +472,10 @@ struct DpmTerms {
 };
 cudaError_t launch_dpm_score(const DpmTerms &dt, float *lu, int P, int S, int R, int H, int W,
                              cudaStream_t s);
+// libNms's rectangle form of nms_recursive: rects [n][4][2] corners, scores
+// descending; thr = ellipse_size^2 (err bit 1: scores out of order).
+cudaError_t launch_nms_rects(const double *rects, const double *score, int n, double thr, int *out,
+                             int *err, cudaStream_t s);
 cudaError_t launch_nms(const float *x, const float *y, const float *scale, const float *score, int n,
                        double train_w, double train_h, int *out, int *err, cudaStream_t s);
 
