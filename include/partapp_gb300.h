@@ -171,6 +171,24 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
                              const double *x_axis, const double *y_axis, double desc_step,
                              int desc_size, float *cells, uint8_t *valid, int mem);
 
+/* computeDescriptorGrid(image, grid, "SHAPEv5", detection_mask, roi)
+ * (libPartDetect/partdetect_aux.cpp:77-160; the detection-mask and ROI
+ * overloads of partdetect.h:137-141): pa_descriptor_grid, except that a
+ * position inside the image also gets no descriptor (valid 0, cell zero)
+ *   - when detection_mask [img_h][img_w] (same memory as image; NULL: none)
+ *     is 0 at the position's truncated image coordinates, or
+ *   - when it lies outside roi = {x, y, width, height}, the rectangle
+ *     QRect(x, y, width, height) spans (inclusive right edge x + width - 1).
+ *     NULL stands for the default QRect(0, 0, img_w - 1, img_h - 1) of the
+ *     reference's other overloads, which excludes the last column and row:
+ *     with desc_size = 0 that removes positions past img_w - 2 / img_h - 2;
+ *     pa_descriptor_grid applies the same default. */
+pa_status pa_descriptor_grid_masked(pa_ctx *ctx, const float *image, int img_h, int img_w,
+                                    const double *x_axis, const double *y_axis,
+                                    double desc_step, int desc_size,
+                                    const float *detection_mask, const int *roi, float *cells,
+                                    uint8_t *valid, int mem);
+
 /* AbcDetectorParam fields of the dense part detector
  * (libPartDetect/AbcDetectorParam.proto:2-12). */
 typedef struct {
@@ -209,6 +227,20 @@ pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
                         int img_w, int flip, const pa_classifier *const *cls, int n_cls,
                         const pa_part_window *windows, const pa_abc_param *abc,
                         float *log_unary, int mem);
+
+/* pa_partdetect with the detection masks of partdetect_dense
+ * (partdetect_test.cpp:86-99: exp_param.detection_masks_dir's per-image
+ * FloatGrid3 "detection_mask"): detection_mask [S][img_h][img_w] (same
+ * memory as image), one mask per scale.  Each scale's mask is read as if
+ * placed in a zero array the size of the bordered image (:135-146), so a
+ * descriptor position in the mirrored border, or where the mask is 0, gets
+ * no descriptor; windows touching one score NO_CLASS_VALUE, and a grid with
+ * no scored window is not squeezed (:436-449).  NULL: pa_partdetect. */
+pa_status pa_partdetect_masked(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
+                               int img_h, int img_w, int flip, const pa_classifier *const *cls,
+                               int n_cls, const pa_part_window *windows,
+                               const pa_abc_param *abc, const float *detection_mask,
+                               float *log_unary, int mem);
 
 /* computeScoreGrid over a grid of per-cell descriptors: each window vector is
  * the reverse-order concatenation of gx*gy cell descriptors taken every

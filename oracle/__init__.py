@@ -519,6 +519,9 @@ def _desc_decl(L):
     L.orc_descriptor_grid.argtypes = [fp, C.c_int, C.c_int, dp, dp, C.c_double, C.c_int, fp,
                                       C.POINTER(C.c_uint8)]
     L.orc_descriptor_grid.restype = C.c_int
+    L.orc_descriptor_grid_ex.argtypes = [fp, C.c_int, C.c_int, dp, dp, C.c_double, C.c_int, fp,
+                                         ip, fp, C.POINTER(C.c_uint8)]
+    L.orc_descriptor_grid_ex.restype = C.c_int
     L.orc_smooth.argtypes = [fp, C.c_int, C.c_int, C.c_float, fp]
     L.orc_smooth.restype = C.c_int
     L.orc_add_border.argtypes = [fp, C.c_int, C.c_int, C.c_int, fp]
@@ -526,6 +529,9 @@ def _desc_decl(L):
     L.orc_partdetect.argtypes = [C.c_void_p, C.c_void_p, ip, dp, C.c_int, C.c_int, C.c_double,
                                  fp, C.c_int, C.c_int, C.c_int, fp]
     L.orc_partdetect.restype = C.c_int
+    L.orc_partdetect_masked.argtypes = [C.c_void_p, C.c_void_p, ip, dp, C.c_int, C.c_int,
+                                        C.c_double, fp, C.c_int, C.c_int, C.c_int, fp, fp]
+    L.orc_partdetect_masked.restype = C.c_int
     L._desc_declared = True
     return L
 
@@ -565,8 +571,10 @@ def feature_grid(img_w, img_h, x_axis, y_axis, desc_step):
     return rect, nx.value, ny.value
 
 
-def descriptor_grid(image, x_axis, y_axis, desc_step, desc_size):
-    """computeDescriptorGrid (SHAPEv5): (cells [ny][nx][96] f32, valid [ny][nx] u8)."""
+def descriptor_grid(image, x_axis, y_axis, desc_step, desc_size, mask=None, roi=None):
+    """computeDescriptorGrid (SHAPEv5): (cells [ny][nx][96] f32, valid [ny][nx] u8).
+    mask: detection mask [h][w] or None; roi: (x, y, width, height) as
+    QRect(x, y, width, height), or None for QRect(0, 0, w - 1, h - 1)."""
     L = _desc_decl(lib())
     img = np.ascontiguousarray(image, dtype=np.float32)
     h, w = img.shape
@@ -574,9 +582,15 @@ def descriptor_grid(image, x_axis, y_axis, desc_step, desc_size):
     ax, ay = _axes(x_axis, y_axis)
     cells = np.zeros((ny, nx, SHAPE_DIM), np.float32)
     valid = np.zeros((ny, nx), np.uint8)
-    rc = L.orc_descriptor_grid(_p(img, C.c_float), h, w, _p(ax, C.c_double), _p(ay, C.c_double),
-                               float(desc_step), int(desc_size), _p(cells, C.c_float),
-                               _p(valid, C.c_uint8))
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+    if mk is not None and mk.shape != (h, w):
+        raise ValueError("the detection mask must have the image's shape")
+    rr = None if roi is None else np.ascontiguousarray(roi, dtype=np.int32)
+    rc = L.orc_descriptor_grid_ex(_p(img, C.c_float), h, w, _p(ax, C.c_double),
+                                  _p(ay, C.c_double), float(desc_step), int(desc_size),
+                                  None if mk is None else _p(mk, C.c_float),
+                                  None if rr is None else _p(rr, C.c_int), _p(cells, C.c_float),
+                                  _p(valid, C.c_uint8))
     if rc:
         raise ValueError(f"orc_descriptor_grid failed: {rc}")
     return cells, valid
@@ -604,11 +618,12 @@ def add_border(image, b):
     return out, used
 
 
-def partdetect(exp: OrcExp, models, windows, desc_step, desc_size, ratio, image, flip=False):
+def partdetect(exp: OrcExp, models, windows, desc_step, desc_size, ratio, image, flip=False,
+               mask=None):
     """partdetect_dense (one image, in-memory path) + clip/log: windows =
     [(window_size_x, window_size_y, pos_offset_x, pos_offset_y)] per
-    classifier; returns log unaries [n][R][h][w], or [n][S][R][h][w] for
-    num_scale_steps = S > 1."""
+    classifier; mask: detection masks [S][h][w] or None; returns log
+    unaries [n][R][h][w], or [n][S][R][h][w] for num_scale_steps = S > 1."""
     L = _desc_decl(lib())
     mh = _ModelsHolder(models)
     n = mh.s.n_parts
@@ -618,9 +633,13 @@ def partdetect(exp: OrcExp, models, windows, desc_step, desc_size, ratio, image,
     po = np.ascontiguousarray([[float(a[2]), float(a[3])] for a in windows], dtype=np.float64)
     S = max(1, exp.num_scale_steps)
     out = np.zeros((n, S, exp.num_rotation_steps, h, w), np.float32)
-    rc = L.orc_partdetect(C.addressof(exp), C.addressof(mh.s), _p(ws, C.c_int),
-                          _p(po, C.c_double), int(desc_step), int(desc_size), float(ratio),
-                          _p(img, C.c_float), h, w, int(bool(flip)), _p(out, C.c_float))
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+    if mk is not None and mk.shape != (S, h, w):
+        raise ValueError("detection masks must be [S][h][w]")
+    rc = L.orc_partdetect_masked(C.addressof(exp), C.addressof(mh.s), _p(ws, C.c_int),
+                                 _p(po, C.c_double), int(desc_step), int(desc_size),
+                                 float(ratio), _p(img, C.c_float), h, w, int(bool(flip)),
+                                 None if mk is None else _p(mk, C.c_float), _p(out, C.c_float))
     if rc:
         raise ValueError(f"orc_partdetect failed: {rc}")
     return out if S > 1 else out[:, 0]

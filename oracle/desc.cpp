@@ -419,9 +419,10 @@ void orc_feature_grid(int img_w, int img_h, const double *ax, const double *ay, 
   *ny = (int)std::floor(((mxy - mny + 1) / desc_step)) + 1;
 }
 
-int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *ax,
-                        const double *ay, double desc_step, int desc_size, float *cells,
-                        uint8_t *valid) {
+int orc_descriptor_grid_ex(const float *image, int img_h, int img_w, const double *ax,
+                           const double *ay, double desc_step, int desc_size,
+                           const float *detection_mask, const int *roi, float *cells,
+                           uint8_t *valid) {
   double rect[4];
   int nx = 0, ny = 0;
   orc_feature_grid(img_w, img_h, ax, ay, desc_step, rect, &nx, &ny);
@@ -436,6 +437,13 @@ int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *
     if (orc_smooth(image, img_h, img_w, (float)patch_scale, smoothed.data())) return -2;
   }
   const Img src{img_w, img_h, patch_scale > 1.0 ? smoothed.data() : image};
+  /* the ROI as QRect(x, y, width, height) holds it: right() = x + width - 1;
+   * the default is QRect(0, 0, x() - 1, y() - 1) (partdetect_aux.cpp:44-55),
+   * whose right() is x() - 2, so the reference tests it (:113-118) */
+  const int rl = roi ? roi[0] : 0, rt = roi ? roi[1] : 0;
+  const int rr = roi ? roi[0] + roi[2] - 1 : img_w - 2, rb = roi ? roi[1] + roi[3] - 1 : img_h - 2;
+  const bool test_roi = !(rl == 0 && rr == img_w - 1 && rt == 0 && rb == img_h - 1);
+  const unsigned uw = (unsigned)img_w, uh = (unsigned)img_h, ud = (unsigned)(desc_size + 1);
   float patch[kPatch * kPatch];
   for (int iy = 0; iy < ny; ++iy)
     for (int ix = 0; ix < nx; ++ix) {
@@ -445,9 +453,15 @@ int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *
       const double x2 = rect[0] + ix * desc_step, y2 = rect[2] + iy * desc_step;
       const double px = (0.0 + x2 * ax[0]) + y2 * ay[0];
       const double py = (0.0 + x2 * ax[1]) + y2 * ay[1];
-      if (!(px >= desc_size + 1 && px <= img_w - (desc_size + 1) && py >= desc_size + 1 &&
-            py <= img_h - (desc_size + 1)))
+      /* x() - (desc_size + 1) in the unsigned arithmetic of x() */
+      if (!(px >= desc_size + 1 && px <= (double)(uw - ud) && py >= desc_size + 1 &&
+            py <= (double)(uh - ud)))
         continue;
+      /* detection_mask[imgpos(1)][imgpos(0)] == 0 skips the position (:132-138);
+       * the double indices truncate */
+      if (detection_mask && detection_mask[(size_t)(long)py * img_w + (size_t)(long)px] == 0)
+        continue;
+      if (test_roi && !(px >= rl && px <= rr && py >= rt && py <= rb)) continue;
       interpolate(src, (float)px, (float)py, (float)(patch_scale * ax[0]),
                   (float)(patch_scale * ay[0]), (float)(patch_scale * ax[1]),
                   (float)(patch_scale * ay[1]), patch);
@@ -456,6 +470,13 @@ int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *
       valid[cell] = 1;
     }
   return 0;
+}
+
+int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *ax,
+                        const double *ay, double desc_step, int desc_size, float *cells,
+                        uint8_t *valid) {
+  return orc_descriptor_grid_ex(image, img_h, img_w, ax, ay, desc_step, desc_size, nullptr,
+                                nullptr, cells, valid);
 }
 
 /* add_image_border2 (libKMA2/ImageContent/ImageContent.cpp:937-999): a
@@ -501,7 +522,8 @@ void hc_inv(const double *T, double *I) {
 }
 int partdetect_scale(const orc_exp *e, int si, const orc_models *m, const int *window_size,
                      const double *pos_offset, int desc_step0, int desc_size0, double ratio,
-                     const float *image, int h, int w, int flip, float *log_unary);
+                     const float *image, int h, int w, int flip, const float *mask,
+                     float *log_unary);
 
 void mul3(const double *A, const double *B, double *Cm) {
   for (int i = 0; i < 3; ++i)
@@ -519,17 +541,27 @@ extern "C" {
 /* partdetect_dense for one image, one scale, in-memory path
  * (libPartDetect/partdetect_test.cpp:53-294) followed by clip_scores_fill +
  * computeLogGrid (objectdetect_findrot.cpp:834-845): see oracle.h. */
-int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size,
-                   const double *pos_offset, int desc_step0, int desc_size0, double ratio,
-                   const float *image, int h, int w, int flip, float *log_unary) {
+int orc_partdetect_masked(const orc_exp *e, const orc_models *m, const int *window_size,
+                          const double *pos_offset, int desc_step0, int desc_size0, double ratio,
+                          const float *image, int h, int w, int flip,
+                          const float *detection_mask, float *log_unary) {
   const int S = n_scales_desc(e);
   if (S > 1 && e->min_object_scale == e->max_object_scale) return -1;
   for (int si = 0; si < S; ++si) {
     const int rc = partdetect_scale(e, si, m, window_size, pos_offset, desc_step0, desc_size0,
-                                    ratio, image, h, w, flip, log_unary);
+                                    ratio, image, h, w, flip,
+                                    detection_mask ? detection_mask + (size_t)si * h * w : nullptr,
+                                    log_unary);
     if (rc) return rc;
   }
   return 0;
+}
+
+int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size,
+                   const double *pos_offset, int desc_step0, int desc_size0, double ratio,
+                   const float *image, int h, int w, int flip, float *log_unary) {
+  return orc_partdetect_masked(e, m, window_size, pos_offset, desc_step0, desc_size0, ratio,
+                               image, h, w, flip, nullptr, log_unary);
 }
 
 }  // extern "C"
@@ -540,7 +572,8 @@ namespace {
  * log_unary [n][S][R][h][w] */
 int partdetect_scale(const orc_exp *e, int si, const orc_models *m, const int *window_size,
                      const double *pos_offset, int desc_step0, int desc_size0, double ratio,
-                     const float *image, int h, int w, int flip, float *log_unary) {
+                     const float *image, int h, int w, int flip, const float *mask,
+                     float *log_unary) {
   const int S = n_scales_desc(e);
   const double scale = scale_value(e, si);
   const int R = e->num_rotation_steps, n = m->n_parts;
@@ -557,6 +590,15 @@ int partdetect_scale(const orc_exp *e, int si, const orc_models *m, const int *w
   const int eh = h + 2 * b, ew = w + 2 * b;
   std::vector<float> ext((size_t)eh * ew);
   orc_add_border(image, h, w, b, ext.data());
+  /* this scale's detection mask placed in a zero array of the bordered
+   * image's size (partdetect_test.cpp:135-146) */
+  std::vector<float> ext_mask;
+  if (mask) {
+    ext_mask.assign((size_t)eh * ew, 0.f);
+    for (int y = 0; y < h; ++y)
+      std::memcpy(ext_mask.data() + (size_t)(y + b) * ew + b, mask + (size_t)y * w,
+                  (size_t)w * sizeof(float));
+  }
   double window_step = ratio * desc_step;
   if (window_step < 1) window_step = 1;
   const double grid_step = desc_step / window_step;
@@ -575,8 +617,9 @@ int partdetect_scale(const orc_exp *e, int si, const orc_models *m, const int *w
     orc_feature_grid(ew, eh, ax, ay, window_step, rect, &nx, &ny);
     std::vector<float> cells((size_t)nx * ny * kShape);
     std::vector<uint8_t> valid((size_t)nx * ny);
-    if (orc_descriptor_grid(ext.data(), eh, ew, ax, ay, window_step, desc_size, cells.data(),
-                            valid.data()))
+    if (orc_descriptor_grid_ex(ext.data(), eh, ew, ax, ay, window_step, desc_size,
+                               mask ? ext_mask.data() : nullptr, nullptr, cells.data(),
+                               valid.data()))
       return -2;
     const double T32[9] = {1, 0, -rect[0], 0, 1, -rect[2], 0, 0, 1};
     double T23[9];

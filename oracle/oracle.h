@@ -233,6 +233,16 @@ int orc_descriptor_grid(const float *image, int img_h, int img_w, const double *
                         const double *y_axis, double desc_step, int desc_size, float *cells,
                         uint8_t *valid);
 
+/* computeDescriptorGrid with a detection mask and a region of interest
+ * (partdetect_aux.cpp:77-160): detection_mask [img_h][img_w] or NULL (a
+ * position whose mask value, at the truncated image coordinates, is 0 gets
+ * no descriptor); roi = {x, y, width, height} as QRect(x, y, width, height)
+ * holds it, or NULL for the default QRect(0, 0, img_w - 1, img_h - 1). */
+int orc_descriptor_grid_ex(const float *image, int img_h, int img_w, const double *x_axis,
+                           const double *y_axis, double desc_step, int desc_size,
+                           const float *detection_mask, const int *roi, float *cells,
+                           uint8_t *valid);
+
 /* add_image_border2 (libKMA2/ImageContent/ImageContent.cpp:937-999): out is
  * [h + 2b][w + 2b]; returns the border used (b, or min(w, h) - 1). */
 int orc_add_border(const float *in, int h, int w, int b, float *out);
@@ -248,6 +258,14 @@ int orc_add_border(const float *in, int h, int w, int b, float *out);
 int orc_partdetect(const orc_exp *e, const orc_models *m, const int *window_size,
                    const double *pos_offset, int desc_step, int desc_size, double ratio,
                    const float *image, int h, int w, int flip, float *log_unary);
+
+/* orc_partdetect with the per-scale detection masks of partdetect_dense
+ * (partdetect_test.cpp:86-99, 135-146): detection_mask [S][h][w], each scale's
+ * mask placed in a zero array the size of the bordered image. */
+int orc_partdetect_masked(const orc_exp *e, const orc_models *m, const int *window_size,
+                          const double *pos_offset, int desc_step, int desc_size, double ratio,
+                          const float *image, int h, int w, int flip,
+                          const float *detection_mask, float *log_unary);
 
 /* extra unary terms of findObjectImageRotJoints (objectdetect_findrot.cpp:915-948) */
 int orc_extra_unary(const orc_exp *e, int P, int root, float rot_weight, const double *rot_params,

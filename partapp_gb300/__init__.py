@@ -55,7 +55,7 @@ EXPORTS = (
     "pa_unary_net_set_params", "pa_unary_net_forward", "pa_unary_net_backward",
     "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries", "pa_add_dpm_scores",
     "pa_nms_recursive", "pa_queue_opts_default", "pa_find_obj_queue", "pa_nms_rects",
-    "pa_rect_from_hyp",
+    "pa_rect_from_hyp", "pa_descriptor_grid_masked", "pa_partdetect_masked",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
@@ -180,6 +180,10 @@ def load_library():
     L.pa_descriptor_grid.argtypes = [vp, vp, ip, ip, P(dp), P(dp), dp, ip, vp, vp, ip]
     L.pa_partdetect.argtypes = [vp, P(ExpParam), vp, ip, ip, ip, vp, ip, P(PartWindow),
                                 P(AbcParam), vp, ip]
+    L.pa_descriptor_grid_masked.argtypes = [vp, vp, ip, ip, P(dp), P(dp), dp, ip, vp, P(ip), vp,
+                                            vp, ip]
+    L.pa_partdetect_masked.argtypes = [vp, P(ExpParam), vp, ip, ip, ip, vp, ip, P(PartWindow),
+                                       P(AbcParam), vp, vp, ip]
     L.pa_rot_joint_marginal.argtypes = [vp, P(ExpParam), vp, vp, ip, ip, ip, P(dp), P(dp), P(dp),
                                         dp, dp, dp, ip, ip]
     L.pa_gemm_bf16.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, ip, ip, ip, ip]
@@ -253,6 +257,26 @@ class _Buf:
         else:
             arr = np.ascontiguousarray(a, dtype=dtype)
             self.arr, self.ptr, self.mem = arr, arr.ctypes.data, PA_MEM_HOST
+
+
+def _mask_buf(mask, like: _Buf, shape):
+    """A float32 detection mask in the memory space of `like`, checked for shape."""
+    if mask is None:
+        return None
+    if like.mem == PA_MEM_DEVICE and not _is_torch(mask):
+        import torch
+
+        mask = torch.as_tensor(np.ascontiguousarray(mask, dtype=np.float32), device=like.arr.device)
+    elif like.mem == PA_MEM_HOST and _is_torch(mask):
+        mask = mask.detach().cpu().numpy()
+    if _is_torch(mask):
+        import torch
+
+        mask = mask.to(torch.float32).contiguous()
+    m = _Buf(mask, np.float32)
+    if tuple(m.arr.shape) != tuple(shape):
+        raise ValueError(f"detection mask must be {tuple(shape)}, got {tuple(m.arr.shape)}")
+    return m
 
 
 def _empty_like_space(shape, mem, like=None):
@@ -431,10 +455,12 @@ class Context:
         return out
 
     # ------------------------------------------------------ descriptors
-    def descriptor_grid(self, image, x_axis, y_axis, desc_step, desc_size):
+    def descriptor_grid(self, image, x_axis, y_axis, desc_step, desc_size, mask=None, roi=None):
         """computeDescriptorGrid with SHAPEv5 on a grey image [h][w] (numpy or
         CUDA tensor): returns (cells [ny][nx][96] f32, valid [ny][nx] u8) in
-        the image's memory space."""
+        the image's memory space.  mask: detection mask [h][w] (0: no
+        descriptor there) or None; roi: (x, y, width, height) as QRect(x, y,
+        width, height), or None for the default QRect(0, 0, w - 1, h - 1)."""
         im = _Buf(image, np.float32)
         h, w = im.arr.shape
         ax = np.ascontiguousarray(x_axis, dtype=np.float64).reshape(2)
@@ -451,16 +477,19 @@ class Context:
         else:
             valid = np.empty((ny.value, nx.value), np.uint8)
             vptr = valid.ctypes.data
-        self._check(self.L.pa_descriptor_grid(self.h, im.ptr, h, w, pd(ax), pd(ay),
-                                              float(desc_step), int(desc_size),
-                                              _Buf(cells, np.float32).ptr, vptr, im.mem))
+        mk = _mask_buf(mask, im, (h, w))
+        rr = None if roi is None else (C.c_int * 4)(*[int(v) for v in roi])
+        self._check(self.L.pa_descriptor_grid_masked(
+            self.h, im.ptr, h, w, pd(ax), pd(ay), float(desc_step), int(desc_size),
+            None if mk is None else mk.ptr, rr, _Buf(cells, np.float32).ptr, vptr, im.mem))
         return cells, valid
 
     def partdetect(self, exp: ExpParam, image, cls_list, windows, desc_step, desc_size,
-                   ratio=1.0, flip=False):
+                   ratio=1.0, flip=False, mask=None):
         """partdetect_dense + clip/log on one grey image [h][w] (numpy or CUDA
         tensor): windows = [(window_size_x, window_size_y, pos_offset_x,
-        pos_offset_y)] per classifier; returns log unaries [n][R][h][w], or
+        pos_offset_y)] per classifier; mask: detection masks [S][h][w] (one
+        per scale) or None; returns log unaries [n][R][h][w], or
         [n][S][R][h][w] for num_scale_steps = S > 1."""
         im = _Buf(image, np.float32)
         h, w = im.arr.shape
@@ -471,9 +500,11 @@ class Context:
                                   for a in windows])
         abc = AbcParam(int(desc_step), int(desc_size), float(ratio))
         out = _empty_like_space((n, S, R, h, w) if S > 1 else (n, R, h, w), im.mem, im.arr)
-        self._check(self.L.pa_partdetect(self.h, C.byref(exp), im.ptr, h, w, int(bool(flip)),
-                                         self._cls_array(cls_list), n, wins, C.byref(abc),
-                                         _Buf(out, np.float32).ptr, im.mem))
+        mk = _mask_buf(mask, im, (S, h, w))
+        self._check(self.L.pa_partdetect_masked(
+            self.h, C.byref(exp), im.ptr, h, w, int(bool(flip)), self._cls_array(cls_list), n,
+            wins, C.byref(abc), None if mk is None else mk.ptr, _Buf(out, np.float32).ptr,
+            im.mem))
         return out
 
     # ---------------------------------------------------------- messages

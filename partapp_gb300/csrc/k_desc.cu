@@ -294,7 +294,15 @@ __global__ void __launch_bounds__(32 * kDescWarps, 5) k_shape_grid(
   const double y2 = dadd(g.min_y, dmul((double)iy, g.step));
   const double px = dadd(dadd(0.0, dmul(x2, g.ax0)), dmul(y2, g.ay0));
   const double py = dadd(dadd(0.0, dmul(x2, g.ax1)), dmul(y2, g.ay1));
-  if (!(px >= g.lo && px <= g.hi_x && py >= g.lo && py <= g.hi_y)) {
+  bool skip = !(px >= g.lo_x && px <= g.hi_x && py >= g.lo_y && py <= g.hi_y);
+  if (!skip && g.mask) {
+    // detection_mask[imgpos(1)][imgpos(0)] == 0 (partdetect_aux.cpp:132-138);
+    // px, py >= 1 here, so the truncation is a floor
+    const long long mx = (long long)px - g.mask_ox, my = (long long)py - g.mask_oy;
+    skip = mx < 0 || my < 0 || mx >= g.mask_w || my >= g.mask_h ||
+           g.mask[my * g.mask_w + mx] == 0.f;
+  }
+  if (skip) {
     for (int k = lane; k < kShape; k += 32) out[k] = 0.f;
     if (lane == 0) valid[cell] = 0;
     return;

@@ -161,14 +161,23 @@ __global__ void __launch_bounds__(kThreads) k_unary_direct_fill(const UnaryMap *
   const int y0 = blockIdx.y * rows_per_cta;
   const int y1e = min(H, y0 + rows_per_cta);
   const int npix = (y1e - y0) * W;
+  if (m.order) {  // ordered map: the gather pass writes every pixel
+    int *ord = m.order + (int64_t)y0 * W;
+    for (int i = threadIdx.x; i < npix; i += blockDim.x) ord[i] = -1;
+    return;
+  }
   float *out = m.out + (int64_t)y0 * W;
   for (int i = threadIdx.x; i < npix; i += blockDim.x) out[i] = kLogZero;
   if (m.max_slot && blockIdx.y == 0) block_max_commit(fkey(kLogZero), m.max_slot);
 }
 
 // TM_DIRECT, pass 2: forward-map every grid cell != NO_CLASS_VALUE
-// (multi_array_transform.hpp:173-193).  The host guarantees the map is
-// injective, so the reference's "last write wins" order never matters.
+// (multi_array_transform.hpp:173-193).  An injective map writes the pixel
+// directly.  Where two cells may land on one pixel the reference keeps the
+// last one its loop (x1 outer, y1 inner) writes: the cell's position in that
+// loop, x1 * ny + y1, goes to the pixel by atomicMax and pass 3 reads the
+// winner.  A squeezed grid's loop runs over a sub-box of the same cells in
+// the same (x1, y1) order, so the full grid's index orders it too.
 __global__ void __launch_bounds__(kThreads) k_unary_direct_scatter(const UnaryMap *__restrict__ maps,
                                                                    int ny, int nx, int H, int W) {
   const UnaryMap m = maps[blockIdx.x];
@@ -189,9 +198,41 @@ __global__ void __launch_bounds__(kThreads) k_unary_direct_scatter(const UnaryMa
       iy3 = (int)floor(__dadd_rn(y3, 0.5));
     }
     if (ix3 < 0 || ix3 >= W || iy3 < 0 || iy3 >= H) continue;
+    if (m.order) {
+      atomicMax(m.order + (int64_t)iy3 * W + ix3, x1 * ny + y1);
+      continue;
+    }
     float o = clip_log(v);
     if (m.masked_all || (m.strip > 0 && (ix3 < m.strip || ix3 >= W - m.strip))) o = kLogZero;
     m.out[(int64_t)iy3 * W + ix3] = o;
+    kmax = max(kmax, key_of(o));
+  }
+  if (m.max_slot && !m.order) block_max_commit(kmax, m.max_slot);
+}
+
+// TM_DIRECT, pass 3 of an ordered map: each pixel takes its last writer's
+// value (NO_CLASS_VALUE -> LOG_ZERO where no cell landed).
+__global__ void __launch_bounds__(kThreads) k_unary_direct_gather(const UnaryMap *__restrict__ maps,
+                                                                  int ny, int nx, int H, int W,
+                                                                  int rows_per_cta) {
+  const UnaryMap m = maps[blockIdx.x];
+  if (!m.order) return;
+  const int y0 = blockIdx.y * rows_per_cta;
+  const int y1e = min(H, y0 + rows_per_cta);
+  const int npix = (y1e - y0) * W;
+  const int *ord = m.order + (int64_t)y0 * W;
+  float *out = m.out + (int64_t)y0 * W;
+  int kmax = kFkeyNegInf;
+  for (int i = threadIdx.x; i < npix; i += blockDim.x) {
+    const int k = ord[i];
+    float o = kLogZero;
+    if (k >= 0) {
+      const int x1 = k / ny, y1 = k - x1 * ny;
+      const int x3 = i % W;
+      o = clip_log(__ldg(m.grid + (int64_t)y1 * nx + x1));
+      if (m.masked_all || (m.strip > 0 && (x3 < m.strip || x3 >= W - m.strip))) o = kLogZero;
+    }
+    out[i] = o;
     kmax = max(kmax, key_of(o));
   }
   if (m.max_slot) block_max_commit(kmax, m.max_slot);
@@ -245,7 +286,7 @@ __global__ void k_fill_int(int *p, int v, int64_t n) {
 }  // namespace
 
 cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, int H, int W,
-                              int direct, int separable, cudaStream_t s) {
+                              int direct, int separable, int ordered, cudaStream_t s) {
   const int rows = 16;
   dim3 grid((unsigned)n_maps, (unsigned)((H + rows - 1) / rows));
   if (!direct) {
@@ -265,6 +306,7 @@ cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, 
     if (chunks > 64) chunks = 64;
     k_unary_direct_scatter<<<dim3((unsigned)n_maps, (unsigned)chunks), kThreads, 0, s>>>(
         maps, ny, nx, H, W);
+    if (ordered) k_unary_direct_gather<<<grid, kThreads, 0, s>>>(maps, ny, nx, H, W, rows);
   }
   return cudaGetLastError();
 }

@@ -1355,8 +1355,16 @@ struct UnaryTables {
   std::vector<int> colx, rowy;
   std::vector<float> cola, rowb;
   bool separable = false;
+  bool collide = false;  // TM_DIRECT: two grid cells may round to one pixel
   double T13[9], T31[9];
 };
+
+// plan_unary's flags: every map takes the separable bilinear kernel; some
+// direct map keeps a last-writer scratch (a third launch)
+constexpr int kUnarySeparable = 1, kUnaryOrdered = 2;
+int unary_launches(int direct, int flags) {
+  return !direct ? 1 : (flags & kUnaryOrdered) ? 3 : 2;
+}
 
 pa_status unary_tables(pa_ctx *ctx, const double *Tig, int ny, int nx, int H, int W, int direct,
                        UnaryTables &t) {
@@ -1393,19 +1401,18 @@ pa_status unary_tables(pa_ctx *ctx, const double *Tig, int ny, int nx, int H, in
       t.rowy.resize(ny);
       for (int x1 = 0; x1 < nx; ++x1) t.colx[x1] = (int)std::floor(Tig[0] * x1 + Tig[2] + 0.5);
       for (int y1 = 0; y1 < ny; ++y1) t.rowy[y1] = (int)std::floor(Tig[4] * y1 + Tig[5] + 0.5);
-      for (int x1 = 1; x1 < nx; ++x1)
-        if (t.colx[x1] == t.colx[x1 - 1])
-          return fail(ctx, PA_ERR_UNSUPPORTED, "TM_DIRECT map is not injective (grid step < 1)");
-      for (int y1 = 1; y1 < ny; ++y1)
-        if (t.rowy[y1] == t.rowy[y1 - 1])
-          return fail(ctx, PA_ERR_UNSUPPORTED, "TM_DIRECT map is not injective (grid step < 1)");
+      std::vector<int> cx(t.colx), ry(t.rowy);
+      std::sort(cx.begin(), cx.end());
+      std::sort(ry.begin(), ry.end());
+      t.collide = std::adjacent_find(cx.begin(), cx.end()) != cx.end() ||
+                  std::adjacent_find(ry.begin(), ry.end()) != ry.end();
     } else {
-      // smallest singular value of the linear part must exceed sqrt(2)
+      // cells one grid step apart land more than sqrt 2 apart, so never on one
+      // pixel, when the smallest singular value of the linear part exceeds sqrt 2
       const double a = Tig[0], b = Tig[1], c = Tig[3], d = Tig[4];
       const double s1 = a * a + b * b + c * c + d * d, det = std::fabs(a * d - b * c);
       const double smin2 = 0.5 * (s1 - std::sqrt(std::max(0.0, s1 * s1 - 4 * det * det)));
-      if (smin2 <= 2.0)
-        return fail(ctx, PA_ERR_UNSUPPORTED, "rotated TM_DIRECT map may collide (scale < sqrt 2)");
+      t.collide = !(smin2 > 2.0);
     }
   }
   return PA_OK;
@@ -1416,7 +1423,7 @@ pa_status plan_unary(pa_ctx *ctx, Builder &b, const double *Tig, int tig_shared,
                      int64_t scores_field_stride, const std::vector<std::vector<float *>> &outs,
                      const std::vector<int> &upright, int root, float strip_frac, int *umax,
                      const pa_exp_param *e, UnaryMap **maps_dev, int apply_masks,
-                     int *all_separable) {
+                     int *flags) {
   const int n_tig = tig_shared ? 1 : P * R;
   std::vector<UnaryTables> tabs(n_tig);
   std::vector<const int *> dcolx(n_tig), drowy(n_tig);
@@ -1434,9 +1441,15 @@ pa_status plan_unary(pa_ctx *ctx, Builder &b, const double *Tig, int tig_shared,
     }
   }
   const int strip = (int)(strip_frac * W);
-  *all_separable = 1;
-  for (int k = 0; k < n_tig; ++k)
-    if (!tabs[k].separable || std::fabs(tabs[k].T13[4]) > 1.0) *all_separable = 0;
+  *flags = kUnarySeparable;
+  bool any_collide = false;
+  for (int k = 0; k < n_tig; ++k) {
+    if (!tabs[k].separable || std::fabs(tabs[k].T13[4]) > 1.0) *flags = 0;
+    any_collide = any_collide || (direct && tabs[k].collide);
+  }
+  // last-writer scratch for the maps whose cells may share a pixel
+  int *order = any_collide ? b.scratch<int>((size_t)n_img * P * R * H * W) : nullptr;
+  if (any_collide) *flags |= kUnaryOrdered;
   std::vector<UnaryMap> maps((size_t)n_img * P * R);
   for (int i = 0; i < n_img; ++i)
     for (int p = 0; p < P; ++p)
@@ -1460,6 +1473,8 @@ pa_status plan_unary(pa_ctx *ctx, Builder &b, const double *Tig, int tig_shared,
           m.strip = (p == root) ? strip : 0;
         }
         m.max_slot = (b.dry || !umax) ? nullptr : umax + i * P + p;
+        m.order = (order && tabs[k].collide) ? order + (((size_t)i * P + p) * R + r) * H * W
+                                             : nullptr;
       }
   *maps_dev = b.param(maps.data(), maps.size());
   return PA_OK;
@@ -1996,7 +2011,9 @@ pa_status find_obj_core(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
                             (size_t)n_fields * G * sizeof(float), (size_t)n_cls,
                             mem == PA_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
                             s));
-  PA_LAUNCH_N("unary_maps", e->interpolate ? 1 : 2, launch_unary_maps(umaps, n_img * P * R, ny, nx, H, W, !e->interpolate, usep, s));
+  PA_LAUNCH_N("unary_maps", unary_launches(!e->interpolate, usep),
+              launch_unary_maps(umaps, n_img * P * R, ny, nx, H, W, !e->interpolate,
+                                usep & kUnarySeparable, usep & kUnaryOrdered, s));
   if (!e->use_pairwise) {
     // getMaxStates: the marginals are the masked unaries
     for (int i = 0; i < n_img; ++i)
@@ -2452,9 +2469,10 @@ pa_status queue_wave(pa_ctx *ctx, std::vector<QGroup> &groups, const pa_classifi
         PA_LAUNCH("score_grids", launch_score_grids(g.sp, (const bool *)ff.data(), ns.data(), n_cls,
                                                     g.desc[0], g.fields, g.fields_al, G,
                                                     (int)n_fields, f.dim, 1, g.scores, gs));
-      PA_LAUNCH_N("unary_maps", f.ep->interpolate ? 1 : 2,
+      PA_LAUNCH_N("unary_maps", unary_launches(!f.ep->interpolate, g.usep),
                   launch_unary_maps(g.umaps, n * g.pl.P * R, f.ny, f.nx, f.H, f.W,
-                                    !f.ep->interpolate, g.usep, gs));
+                                    !f.ep->interpolate, g.usep & kUnarySeparable,
+                                    g.usep & kUnaryOrdered, gs));
       if (g.pl.n_msgs_total > 0)
         PA_LAUNCH_N("shift_tables", 2,
                     launch_shift_tables(g.pl.shifts, g.pl.n_msgs_total, R, f.H, f.W, g.pl.tables,
@@ -3119,6 +3137,32 @@ void smooth_coefficients(float sigma, float *coefs) {
 
 }  // namespace
 
+namespace {
+
+// The inside test of computeDescriptorGrid (partdetect_aux.cpp:128-130:
+// imgpos >= desc_size + 1, imgpos <= x() - (desc_size + 1) in x()'s unsigned
+// arithmetic) intersected with its region-of-interest test (:113-118,
+// 140-145).  roi = {x, y, width, height} as QRect(x, y, width, height) holds
+// it (right() = x + width - 1), or null for the QRect(0, 0, x() - 1, y() - 1)
+// every default entry builds (:44-55), whose right() is x() - 2: that one is
+// tested too, and bites when desc_size is 0.  Both tests skip a position the
+// same way, so one box holds both.
+void desc_bounds(DescGrid &g, int w, int h, int desc_size, const int *roi) {
+  g.lo_x = g.lo_y = (double)(desc_size + 1);
+  g.hi_x = (double)((unsigned)w - (unsigned)(desc_size + 1));
+  g.hi_y = (double)((unsigned)h - (unsigned)(desc_size + 1));
+  const long long l = roi ? roi[0] : 0, t = roi ? roi[1] : 0;
+  const long long r = roi ? (long long)roi[0] + roi[2] - 1 : (long long)w - 2;
+  const long long b = roi ? (long long)roi[1] + roi[3] - 1 : (long long)h - 2;
+  if (l == 0 && r == (long long)w - 1 && t == 0 && b == (long long)h - 1) return;  // bTestRoi false
+  g.lo_x = std::max(g.lo_x, (double)l);
+  g.lo_y = std::max(g.lo_y, (double)t);
+  g.hi_x = std::min(g.hi_x, (double)r);
+  g.hi_y = std::min(g.hi_y, (double)b);
+}
+
+}  // namespace
+
 pa_status pa_feature_grid_size(int img_w, int img_h, const double *x_axis, const double *y_axis,
                                double desc_step, int *nx, int *ny) try {
   if (img_w < 1 || img_h < 1 || !x_axis || !y_axis || !nx || !ny || !(desc_step > 0))
@@ -3134,7 +3178,16 @@ pa_status pa_feature_grid_size(int img_w, int img_h, const double *x_axis, const
 
 pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img_w,
                              const double *x_axis, const double *y_axis, double desc_step,
-                             int desc_size, float *cells, uint8_t *valid, int mem) try {
+                             int desc_size, float *cells, uint8_t *valid, int mem) {
+  return pa_descriptor_grid_masked(ctx, image, img_h, img_w, x_axis, y_axis, desc_step,
+                                   desc_size, nullptr, nullptr, cells, valid, mem);
+}
+
+pa_status pa_descriptor_grid_masked(pa_ctx *ctx, const float *image, int img_h, int img_w,
+                                    const double *x_axis, const double *y_axis,
+                                    double desc_step, int desc_size,
+                                    const float *detection_mask, const int *roi, float *cells,
+                                    uint8_t *valid, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!image || !cells || !valid || !x_axis || !y_axis || img_h < 2 || img_w < 2 ||
       !(desc_step > 0) || desc_size < 0 || img_h > 65535 || img_w > 65535)
@@ -3160,10 +3213,11 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
   g.ax1 = x_axis[1];
   g.ay0 = y_axis[0];
   g.ay1 = y_axis[1];
-  // imgpos >= desc_size + 1 and imgpos <= x() - (desc_size + 1) in unsigned arithmetic
-  g.lo = (double)(desc_size + 1);
-  g.hi_x = (double)((unsigned)img_w - (unsigned)(desc_size + 1));
-  g.hi_y = (double)((unsigned)img_h - (unsigned)(desc_size + 1));
+  desc_bounds(g, img_w, img_h, desc_size, roi);
+  g.mask = nullptr;
+  g.mask_w = img_w;
+  g.mask_h = img_h;
+  g.mask_ox = g.mask_oy = 0;
   g.v0x = (float)(patch_scale * x_axis[0]);
   g.v0y = (float)(patch_scale * y_axis[0]);
   g.v1x = (float)(patch_scale * x_axis[1]);
@@ -3177,6 +3231,7 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
                   uint8_t **vout) {
     *t = b.param(&tabs, 1);
     *din = mem == PA_MEM_HOST ? b.scratch<float>(npx) : image;
+    if (detection_mask) g.mask = mem == PA_MEM_HOST ? b.scratch<float>(npx) : detection_mask;
     *dout = mem == PA_MEM_HOST ? b.scratch<float>(ncell * 96) : cells;
     *vout = mem == PA_MEM_HOST ? b.scratch<uint8_t>(ncell) : valid;
     sm_tmp = smooth ? b.scratch<float>(npx) : nullptr;
@@ -3196,8 +3251,12 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
   b.base = ctx->arena;
   plan(b, &t, &din, &dout, &vout);
   if ((st = upload_blob(ctx, b))) return st;
-  if (mem == PA_MEM_HOST)
+  if (mem == PA_MEM_HOST) {
     if ((st = copy_in(ctx, (void *)din, image, npx * sizeof(float), mem))) return st;
+    if (detection_mask &&
+        (st = copy_in(ctx, (void *)g.mask, detection_mask, npx * sizeof(float), mem)))
+      return st;
+  }
   if (smooth) {
     PA_LAUNCH_N("smooth", 2, launch_smooth(din, sm_tmp, sm_out, img_h, img_w, cf, ctx->stream));
     din = sm_out;
@@ -3222,7 +3281,7 @@ namespace {
 pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const float *image,
                            int img_h, int img_w, int flip, const pa_classifier *const *cls,
                            int n_cls, const pa_part_window *windows, const pa_abc_param *abc,
-                           float *log_unary, int mem) {
+                           const float *detection_mask, float *log_unary, int mem) {
   const int R = ep->num_rotation_steps, S = n_scales(ep);
   const double scale = scale_from_index(ep, si);
   const double desc_step = scale * abc->desc_step;
@@ -3250,12 +3309,10 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
   double window_step = abc->window_desc_step_ratio * desc_step;
   if (window_step < 1) window_step = 1;
   const double grid_step = desc_step / window_step;
-  // TM_DIRECT of a rotated grid into the image keeps the reference's result only
-  // when no two cells round to one pixel ("last write wins" has no parallel
-  // order); cells window_step apart never share a pixel when window_step > sqrt 2
-  if (!(window_step * window_step > 2.0))
-    return fail(ctx, PA_ERR_UNSUPPORTED,
-                "window step %.3f px: the rotated grid -> image map may collide", window_step);
+  // cells window_step apart never share a pixel of the TM_DIRECT map when
+  // window_step > sqrt 2; closer grids keep the reference's last writer per
+  // pixel in a scratch (k_unary_direct_gather)
+  const bool ordered = !(window_step * window_step > 2.0);
   // the rotated grids (partdetect_test.cpp:171-185)
   struct Rot {
     double ax[2], ay[2], rect[4];
@@ -3311,18 +3368,23 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
   struct Dev {
     const DescTables *tabs;
     StumpPart *sp;
-    const float *img;
+    const float *img, *mask;
     float *ext, *sm_tmp, *sm_out, *cells, *dense, *scores, *out;
     uint8_t *valid, *ok;
     int4 *bbox;
     const float **grid_ptrs;
     UnaryMap *maps;
+    int *order;
   } d{};
   std::vector<const float *> grid_ptrs((size_t)R * n_cls);
   auto plan = [&](Builder &b) {
     d.tabs = b.param(&tabs, 1);
     d.sp = plan_stumps(b, cls_sorted.data(), n_cls);
     d.img = mem == PA_MEM_HOST ? b.scratch<float>(npx) : image;
+    // this scale's detection mask [img_h][img_w]
+    d.mask = !detection_mask ? nullptr
+             : mem == PA_MEM_HOST ? b.scratch<float>(npx)
+                                  : detection_mask + (size_t)si * npx;
     d.ext = b.scratch<float>(nepx);
     d.sm_tmp = smooth ? b.scratch<float>(nepx) : nullptr;
     d.sm_out = smooth ? b.scratch<float>(nepx) : nullptr;
@@ -3338,6 +3400,8 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
             b.dry ? nullptr : d.scores + score_off[r] + (size_t)k * rots[r].nx * rots[r].ny;
     d.grid_ptrs = b.param(grid_ptrs.data(), grid_ptrs.size());
     d.maps = b.scratch<UnaryMap>((size_t)R * n_cls + 1);  // + 1: the 16-byte copy tail
+    // one rotation's last writers, reused by the next (stream order)
+    d.order = ordered ? b.scratch<int>((size_t)n_cls * npx) : nullptr;
     // host memory: this scale's [n_cls][R][img_h][img_w] block, copied out below
     d.out = mem == PA_MEM_HOST ? b.scratch<float>((size_t)n_cls * R * npx) : log_unary;
   };
@@ -3354,8 +3418,12 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
   plan(b);
   if ((st = upload_blob(ctx, b))) return st;
   cudaStream_t s = ctx->stream;
-  if (mem == PA_MEM_HOST)
+  if (mem == PA_MEM_HOST) {
     if ((st = copy_in(ctx, (void *)d.img, image, npx * sizeof(float), mem))) return st;
+    if (d.mask && (st = copy_in(ctx, (void *)d.mask, detection_mask + (size_t)si * npx,
+                                npx * sizeof(float), mem)))
+      return st;
+  }
   PA_LAUNCH_N("border", border > 0 ? 2 : 1, launch_mirror_border(d.img, img_h, img_w, border, d.ext, s));
   const float *src = d.ext;
   if (smooth) {
@@ -3374,9 +3442,13 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
     g.ax1 = q.ax[1];
     g.ay0 = q.ay[0];
     g.ay1 = q.ay[1];
-    g.lo = (double)(desc_size + 1);
-    g.hi_x = (double)((unsigned)ew - (unsigned)(desc_size + 1));
-    g.hi_y = (double)((unsigned)eh - (unsigned)(desc_size + 1));
+    desc_bounds(g, ew, eh, desc_size, nullptr);
+    // the mask sits in a zero array the size of the bordered image, at
+    // (border, border) (partdetect_test.cpp:135-146)
+    g.mask = d.mask;
+    g.mask_w = img_w;
+    g.mask_h = img_h;
+    g.mask_ox = g.mask_oy = border;
     g.v0x = (float)(patch_scale * q.ax[0]);
     g.v0y = (float)(patch_scale * q.ay[0]);
     g.v1x = (float)(patch_scale * q.ax[1]);
@@ -3441,12 +3513,14 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
       for (int t = 0; t < 6; ++t) m.T31[t] = Tig[t];
       m.ox = ox;
       m.oy = oy;
+      m.order = ordered ? d.order + (size_t)k * npx : nullptr;
     }
   }
   if ((st = upload_to(ctx, d.maps, maps.data(), maps.size() * sizeof(UnaryMap)))) return st;
   for (int r = 0; r < R; ++r)
-    PA_LAUNCH_N("unary_maps", 2, launch_unary_maps(d.maps + (size_t)r * n_cls, n_cls, rots[r].ny,
-                                                   rots[r].nx, img_h, img_w, 1, 0, s));
+    PA_LAUNCH_N("unary_maps", ordered ? 3 : 2,
+                launch_unary_maps(d.maps + (size_t)r * n_cls, n_cls, rots[r].ny, rots[r].nx,
+                                  img_h, img_w, 1, 0, ordered, s));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpy2DAsync(log_unary + (size_t)si * R * npx, (size_t)S * R * npx * sizeof(float),
                             d.out, (size_t)R * npx * sizeof(float), (size_t)R * npx * sizeof(float),
@@ -3459,7 +3533,16 @@ pa_status partdetect_scale(pa_ctx *ctx, const pa_exp_param *ep, int si, const fl
 pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image, int img_h,
                         int img_w, int flip, const pa_classifier *const *cls, int n_cls,
                         const pa_part_window *windows, const pa_abc_param *abc,
-                        float *log_unary, int mem) try {
+                        float *log_unary, int mem) {
+  return pa_partdetect_masked(ctx, ep, image, img_h, img_w, flip, cls, n_cls, windows, abc,
+                              nullptr, log_unary, mem);
+}
+
+pa_status pa_partdetect_masked(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
+                               int img_h, int img_w, int flip, const pa_classifier *const *cls,
+                               int n_cls, const pa_part_window *windows,
+                               const pa_abc_param *abc, const float *detection_mask,
+                               float *log_unary, int mem) try {
   if (!ctx) return PA_ERR_INVALID;
   if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
   if (!image || !log_unary || !windows || !abc || img_h < 5 || img_w < 5 || img_h > 16384 ||
@@ -3472,7 +3555,7 @@ pa_status pa_partdetect(pa_ctx *ctx, const pa_exp_param *ep, const float *image,
   // its own descriptor step and size, border, grids and windows
   for (int si = 0; si < n_scales(ep); ++si)
     if (pa_status st = partdetect_scale(ctx, ep, si, image, img_h, img_w, flip, cls, n_cls,
-                                        windows, abc, log_unary, mem))
+                                        windows, abc, detection_mask, log_unary, mem))
       return st;
   return PA_OK;
 } catch (const std::bad_alloc &) {
@@ -3588,7 +3671,9 @@ pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, in
   if ((st = upload_blob(ctx, b))) return st;
   if (mem == PA_MEM_HOST)
     if ((st = copy_in(ctx, (void *)d_in, scores, nin * sizeof(float), mem))) return st;
-  PA_LAUNCH_N("unary_maps", interpolate ? 1 : 2, launch_unary_maps(maps, n_parts * R, ny, nx, H, W, !interpolate, usep, ctx->stream));
+  PA_LAUNCH_N("unary_maps", unary_launches(!interpolate, usep),
+              launch_unary_maps(maps, n_parts * R, ny, nx, H, W, !interpolate,
+                                usep & kUnarySeparable, usep & kUnaryOrdered, ctx->stream));
   if (mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(log_unary, d_out, nout * sizeof(float), cudaMemcpyDeviceToHost,
                           ctx->stream));

@@ -81,9 +81,13 @@ struct DescTables {
 struct DescGrid {
   double min_x, min_y, step;            // rect.min_proj_x / min_proj_y, desc_step
   double ax0, ax1, ay0, ay1;            // x_axis, y_axis
-  double lo, hi_x, hi_y;                // inside test bounds
+  double lo_x, lo_y, hi_x, hi_y;        // inside test and region of interest, intersected
   float v0x, v0y, v1x, v1y;             // patch_scale * axes, as float
   int nx, ny;
+  // detection mask [mask_h][mask_w] or null: image position (x, y) reads
+  // mask[(long)y - mask_oy][(long)x - mask_ox], 0 outside the array
+  const float *mask;
+  int mask_w, mask_h, mask_ox, mask_oy;
 };
 struct IirCoefs {
   float c[17];  // set_smooth_coefficients order (gauss_iir.cpp:77-120)
@@ -118,6 +122,9 @@ struct UnaryMap {
   int strip;             // root border strip width in pixels (0 if none)
   int *max_slot;         // fkey of max over the part's masked map
   int ox, oy;            // general DIRECT path: T31 applies to (x1 - ox, y1 - oy)
+  // DIRECT maps that may send two cells to one pixel: [H][W] scratch holding
+  // the reference's last writer per pixel (null: the map is injective)
+  int *order;
 };
 
 // ---------------------------------------------------------------------------
@@ -371,8 +378,9 @@ cudaError_t launch_mask_no_class(float *scores, const uint8_t *ok, int n_parts, 
                                  cudaStream_t s);
 // separable != 0 promises every map uses the column/row tables and that a
 // band of 16 image rows reads at most 18 grid rows (|Tig y scale| >= 1).
+// ordered: some direct map carries an `order` scratch (a third, gather pass)
 cudaError_t launch_unary_maps(const UnaryMap *maps, int n_maps, int ny, int nx, int H, int W,
-                              int direct, int separable, cudaStream_t s);
+                              int direct, int separable, int ordered, cudaStream_t s);
 cudaError_t launch_prepare_unary(const float *in, float *out, const int *masked_rot, int strip,
                                  int R, int H, int W, int *max_slot, cudaStream_t s);
 cudaError_t launch_shift_tables(const double *shifts, int n_msgs, int R, int H, int W,

@@ -21,8 +21,12 @@
 //   windows.txt    one line per classifier: window_size_x window_size_y
 //                  pos_offset_x pos_offset_y (PartWindowParam)
 //   exp.txt        additionally desc_step, desc_size, window_desc_step_ratio
-//                  (AbcDetectorParam); height, width, grid_*, dim and tig.txt
-//                  are not used
+//                  (AbcDetectorParam) and, for several scales, num_scale_steps,
+//                  min_object_scale, max_object_scale (in place of
+//                  object_scale); height, width, grid_*, dim and tig.txt are
+//                  not used
+//   --detection_masks_dir DIR   DIR/detection_mask_imgidx<NNNNN>.mat per image
+//                  (exp_param.detection_masks_dir, partdetect_test.cpp:89-99)
 //
 // With --scoregrid_dir DIR the unaries come from the score grids the
 // reference's part detector saved (the default branch of findObjectDataset,
@@ -258,7 +262,8 @@ void dump_array(const MatArray &a, const std::string &indent) {
 void usage() {
   std::cout << "usage: partapp_find_obj --find_obj --expdir DIR [--outdir DIR] [--first i]\n"
                "                        [--numimgs n] [--batch b] [--flip] [--device d]\n"
-               "                        [--save_marginals] [--from_images | --scoregrid_dir DIR]\n"
+               "                        [--save_marginals] [--from_images [--detection_masks_dir DIR]\n"
+               "                         | --scoregrid_dir DIR]\n"
                "                        [--pred_dir DIR --pred_rot_weight w --pred_pos_weight w\n"
                "                         --torso_det_dir DIR --rootidx_det k]\n"
                "                        [--torso_prior FILE --torso_prior_weight w]\n"
@@ -274,7 +279,7 @@ void usage() {
 }  // namespace
 
 int main(int argc, char **argv) {
-  std::string expdir, outdir, scoregrid_dir, pred_dir, torso_det_dir, torso_prior;
+  std::string expdir, outdir, scoregrid_dir, pred_dir, torso_det_dir, torso_prior, masks_dir;
   float rot_w = 0.f, pos_w = 0.f, torso_w = 0.f;
   int rootidx_det = -1;
   DpmOptions dpm;
@@ -298,6 +303,7 @@ int main(int argc, char **argv) {
     else if (a == "--save_marginals") save_marg = true;
     else if (a == "--from_images") from_images = true;
     else if (a == "--scoregrid_dir") scoregrid_dir = next();
+    else if (a == "--detection_masks_dir") masks_dir = next();
     else if (a == "--part_conf") jsrc.part_conf = next();
     else if (a == "--spatial_dir") jsrc.spatial_dir = next();
     else if (a == "--joints_dump") joints_dump = true;
@@ -355,7 +361,8 @@ int main(int argc, char **argv) {
     e.num_rotation_steps = (int)need(kv, "num_rotation_steps");
     e.min_part_rotation = (float)need(kv, "min_part_rotation");
     e.max_part_rotation = (float)need(kv, "max_part_rotation");
-    e.min_object_scale = e.max_object_scale = (float)need(kv, "object_scale");
+    if (!(from_images && kv.count("num_scale_steps")))
+      e.min_object_scale = e.max_object_scale = (float)need(kv, "object_scale");
     e.strip_border_detections = (float)need(kv, "strip_border_detections");
     e.roi_save_num_samples = (int)need(kv, "roi_save_num_samples");
     e.use_pairwise = need(kv, "use_pairwise") != 0;
@@ -370,6 +377,11 @@ int main(int argc, char **argv) {
       app.m_abc_param.desc_step = (int)need(kv, "desc_step");
       app.m_abc_param.desc_size = (int)need(kv, "desc_size");
       app.m_abc_param.window_desc_step_ratio = need(kv, "window_desc_step_ratio");
+      if (kv.count("num_scale_steps")) {  // several scales (partdetect_test.cpp:116)
+        e.num_scale_steps = (int)need(kv, "num_scale_steps");
+        e.min_object_scale = (float)need(kv, "min_object_scale");
+        e.max_object_scale = (float)need(kv, "max_object_scale");
+      }
       std::istringstream win(read_file(expdir + "/windows.txt"));
       for (int c = 0; c < n_cls; ++c) {
         PartWindow pw;
@@ -394,6 +406,11 @@ int main(int argc, char **argv) {
         loadDpmScores(extra, i, app.m_part_conf.part_size(), app.m_exp_param.c().num_rotation_steps,
                       h, w, dpm);
         app.m_extra = &extra;
+        std::vector<float> mask;
+        if (!masks_dir.empty())
+          mask = loadDetectionMask(masks_dir, i, std::max(1, app.m_exp_param.num_scale_steps), h,
+                                   w);
+        app.m_detection_mask = masks_dir.empty() ? nullptr : &mask;
         const FindObjResult r = findObjectImageFromImage(ctx, app, flip, joints, img.data(), h, w,
                                                          save_marg);
         write_outputs(outdir, i, flip, r);

@@ -272,9 +272,12 @@ std::vector<float> partdetect_raw(Context &ctx, const PartApp &part_app, const f
   const pa_abc_param abc = {part_app.m_abc_param.desc_step, part_app.m_abc_param.desc_size,
                             part_app.m_abc_param.window_desc_step_ratio};
   const int S = std::max(1, e.num_scale_steps), R = e.num_rotation_steps;
+  const std::vector<float> *mask = part_app.m_detection_mask;
+  require(!mask || mask->size() == (size_t)S * img_h * img_w, "detection masks: [S][H][W]");
   std::vector<float> lu((size_t)n * S * R * img_h * img_w);
-  ctx.check(pa_partdetect(ctx.get(), &e, image, img_h, img_w, flip ? 1 : 0, cls.data(), n,
-                          wins.data(), &abc, lu.data(), PA_MEM_HOST));
+  ctx.check(pa_partdetect_masked(ctx.get(), &e, image, img_h, img_w, flip ? 1 : 0, cls.data(),
+                                 n, wins.data(), &abc, mask ? mask->data() : nullptr, lu.data(),
+                                 PA_MEM_HOST));
   return lu;
 }
 
@@ -450,6 +453,25 @@ void dpm_cell(const std::string &path, int Rd, int H, int W, float *dst) {
 }
 
 }  // namespace
+
+std::vector<float> loadDetectionMask(const std::string &dir, int imgidx, int S, int H, int W) {
+  char name[64];
+  std::snprintf(name, sizeof name, "/detection_mask_imgidx%05d.mat", imgidx + 1);
+  const std::string path = dir + name;
+  const auto v = mat_read(path);
+  const MatArray &a = mat_find(v, "detection_mask");
+  // mat_load_multi_array keeps MATLAB's dims: element (s, y, x)
+  require(!a.is_cell() && a.dims.size() == 3 && (int)a.dims[0] >= S && (int)a.dims[1] == H &&
+              (int)a.dims[2] == W,
+          path + ": detection_mask is not [>=" + std::to_string(S) + "][" + std::to_string(H) +
+              "][" + std::to_string(W) + "]");
+  std::vector<float> m((size_t)S * H * W);
+  for (int s = 0; s < S; ++s)
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x)
+        m[((size_t)s * H + y) * W + x] = (float)mat_at(a, {(size_t)s, (size_t)y, (size_t)x});
+  return m;
+}
 
 void loadDpmScores(ExtraUnaryParams &x, int imgidx, int n_parts, int R, int H, int W,
                    const DpmOptions &o) {

@@ -225,6 +225,12 @@ struct DpmOptions {
 void loadDpmScores(ExtraUnaryParams &x, int imgidx, int n_parts, int R, int H, int W,
                    const DpmOptions &o);
 
+// The detection masks of image imgidx as partdetect_dense loads them
+// (libPartDetect/partdetect_test.cpp:89-99): <dir>/detection_mask_imgidx<NNNNN>.mat
+// (NNNNN = imgidx + 1, five digits), variable "detection_mask" [S'][H][W]
+// with S' >= S; returns the first S masks as [S][H][W] floats.
+std::vector<float> loadDetectionMask(const std::string &dir, int imgidx, int S, int H, int W);
+
 // Reads the reference's prediction files for image imgidx:
 //   rot:   <pred_dir>/testlist_params_rot_imgidx<i>.mat, "rot_test" [P][2+]
 //          (mean, deviation -> variance = deviation^2), getRotParams :193-226
@@ -293,6 +299,8 @@ struct PartApp {
   AbcDetectorParam m_abc_param;                   // for detection from images
   std::vector<PartWindow> m_window_param;         // one per classifier in m_abc
   const ExtraUnaryParams *m_extra = nullptr;       // extra unary terms, if any
+  // the image's detection masks [S][H][W] (exp_param.detection_masks_dir), if any
+  const std::vector<float> *m_detection_mask = nullptr;
 };
 
 // computeRotJointMarginal (objectdetect_findrot.cpp:292-456): child ->
@@ -355,6 +363,7 @@ std::vector<FindObjResult> findObjectDataset(Context &ctx, const PartApp &part_a
 // partdetect (libPartDetect/partdetect_test.cpp:296-341 -> partdetect_dense)
 // on a grey image [img_h][img_w] followed by clip_scores_fill + computeLogGrid:
 // log_part_detections[classifier][scale] = FloatGrid3(R, img_h, img_w).
+// part_app.m_detection_mask, when set, restricts the descriptor positions.
 void partdetect(Context &ctx, const PartApp &part_app, const float *image, int img_h,
                 int img_w, bool flip, std::vector<std::vector<FloatGrid3>> &log_part_detections);
 

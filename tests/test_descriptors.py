@@ -299,13 +299,21 @@ def test_partdetect_matches_oracle(ctx, orc, pa, R, flip, ratio):
 
 
 @pytest.mark.gpu
-def test_partdetect_rejects_colliding_maps(ctx, pa):
-    m, dims = _pd_models(1, WINDOWS[:1])
-    cls = [pa.Classifier.from_stumps(ctx, m["f"][0], m["p"][0], m["theta"][0], m["alpha"][0],
-                                     dims[0])]
-    with pytest.raises(pa.PaError) as ei:  # window step 1 px < sqrt 2
-        ctx.partdetect(pa.exp_param(R=2), grey_image(1, 40, 48), cls, WINDOWS[:1], 4, 10, 0.25)
-    assert ei.value.status == pa.PA_ERR_UNSUPPORTED
+@pytest.mark.parametrize("ratio,flip", [(0.25, False), (0.3, True)])
+def test_partdetect_small_window_step(ctx, orc, pa, ratio, flip):
+    """Window steps of 1 and 1.2 px (<= sqrt 2): rotated grid cells share
+    pixels of the TM_DIRECT map and the reference's last writer wins."""
+    img = grey_image(11, 40, 48)
+    wins = WINDOWS[:2]
+    m, dims = _pd_models(1, wins)
+    cls = [pa.Classifier.from_stumps(ctx, m["f"][i], m["p"][i], m["theta"][i], m["alpha"][i],
+                                     dims[i]) for i in range(len(wins))]
+    want = orc.partdetect(orc.make_exp(R=3), m, wins, 4, 10, ratio, img, flip)
+    got = ctx.partdetect(pa.exp_param(R=3), img, cls, wins, 4, 10, ratio, flip)
+    z = want == np.float32(-1e6)
+    assert np.array_equal(got == np.float32(-1e6), z)
+    off = np.abs(got[~z] - want[~z]) > 4e-7 * np.maximum(1.0, np.abs(want[~z]))
+    assert off.mean() <= 1e-3 and (~z).sum() > 1000
 
 
 def _maxnorm(a, b):
@@ -344,3 +352,142 @@ def test_find_obj_from_image_two_scales(ctx, orc, pa):
         for s in range(2):
             assert _maxnorm(got["log_marg"][p, s], want["log_marg"][p, s]) <= 1e-4, (p, s)
     assert np.array_equal(got["best_conf"][:, [0, 2, 4, 5]], want["best_conf"][:, [0, 2, 4, 5]])
+
+
+# ------------------------------------------- detection masks and the ROI
+def _positions(orc, w, h, deg, step, flip=False):
+    ax, ay = axes(deg, flip)
+    rect, nx, ny = orc.feature_grid(w, h, ax, ay, step)
+    iy, ix = np.mgrid[0:ny, 0:nx]
+    x2, y2 = rect[0] + ix * step, rect[2] + iy * step
+    return ax, ay, (0.0 + x2 * ax[0]) + y2 * ay[0], (0.0 + x2 * ax[1]) + y2 * ay[1]
+
+
+def blob_mask(seed, h, w, frac=0.5):
+    """A detection mask of a few rectangles of ones (values 1 or 0.25) on zeros."""
+    rng = np.random.default_rng(seed)
+    m = np.zeros((h, w), np.float32)
+    while (m != 0).mean() < frac:
+        y0, x0 = rng.integers(0, h - 4), rng.integers(0, w - 4)
+        m[y0:y0 + rng.integers(4, h // 2), x0:x0 + rng.integers(4, w // 2)] = rng.choice([1.0, 0.25])
+    return m
+
+
+def test_descriptor_grid_mask_and_roi_pins(orc):
+    """partdetect_aux.cpp:128-145: after the inside test a position is skipped
+    when detection_mask[(long) y][(long) x] == 0, then when it lies outside the
+    ROI; the descriptors that remain are those of the unmasked grid."""
+    img = grey_image(5, 64, 80)
+    ds, step = 10, 4.0
+    mask = blob_mask(6, 64, 80)
+    for deg in (0.0, 37.0):
+        ax, ay, px, py = _positions(orc, 80, 64, deg, step)
+        full, vf = orc.descriptor_grid(img, ax, ay, step, ds)
+        cells, valid = orc.descriptor_grid(img, ax, ay, step, ds, mask=mask)
+        inside = vf.astype(bool)
+        on = np.zeros_like(inside)
+        on[inside] = mask[py[inside].astype(np.int64), px[inside].astype(np.int64)] != 0
+        assert np.array_equal(valid.astype(bool), on)
+        assert np.array_equal(cells[on], full[on]) and (cells[~on] == 0).all()
+        assert 0 < on.sum() < inside.sum()
+        roi = (20, 14, 41, 30)  # QRect(20, 14, 41, 30): x in [20, 60], y in [14, 43]
+        cells, valid = orc.descriptor_grid(img, ax, ay, step, ds, roi=roi)
+        want = inside & (px >= 20) & (px <= 60) & (py >= 14) & (py <= 43)
+        assert np.array_equal(valid.astype(bool), want)
+        assert np.array_equal(cells[want], full[want])
+        # the whole image as the ROI tests nothing
+        _, valid = orc.descriptor_grid(img, ax, ay, step, ds, roi=(0, 0, 80, 64))
+        assert np.array_equal(valid, vf)
+
+
+def test_default_roi_drops_last_column_when_desc_size_is_zero(orc):
+    """The default QRect(0, 0, x() - 1, y() - 1) has right() = x() - 2: with
+    desc_size 0 the inside test alone would admit x up to x() - 1."""
+    img = grey_image(7, 40, 48)
+    ax, ay, px, py = _positions(orc, 48, 40, 0.0, 1.0)
+    _, valid = orc.descriptor_grid(img, ax, ay, 1.0, 0)
+    want = (px >= 1) & (px <= 46) & (py >= 1) & (py <= 38)
+    assert np.array_equal(valid.astype(bool), want)
+    _, valid = orc.descriptor_grid(img, ax, ay, 1.0, 0, roi=(0, 0, 48, 40))
+    assert valid.astype(bool)[(px == 47) & (py == 20)].all()
+
+
+def test_partdetect_mask_restricts_scored_cells(orc):
+    """partdetect_test.cpp:135-146: each scale's mask sits in a zero array the
+    size of the bordered image, so an all-ones mask only drops windows that
+    reach into the mirrored border; a zero mask leaves every grid empty
+    (not squeezed, :436-449) and every unary LOG_ZERO."""
+    img = grey_image(8, 48, 64)
+    wins = WINDOWS[:2]
+    m, _ = _pd_models(4, wins)
+    e = orc.make_exp(R=3)
+    full = orc.partdetect(e, m, wins, 4, 10, 1.0, img)
+    ones = orc.partdetect(e, m, wins, 4, 10, 1.0, img, mask=np.ones((1, 48, 64), np.float32))
+    z = np.float32(-1e6)
+    assert ((ones == full) | (ones == z)).all()
+    assert (ones == z).sum() > (full == z).sum() and (ones != z).sum() > 100
+    none = orc.partdetect(e, m, wins, 4, 10, 1.0, img, mask=np.zeros((1, 48, 64), np.float32))
+    assert (none == z).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("deg,flip", [(0.0, False), (-67.5, True)])
+def test_descriptor_grid_masked_matches_oracle(ctx, orc, deg, flip):
+    import torch
+
+    img = grey_image(60, 80, 112)
+    mask = blob_mask(61, 80, 112)
+    ax, ay = axes(deg, flip)
+    for kw in (dict(mask=mask), dict(roi=(9, 17, 70, 45)), dict(mask=mask, roi=(30, 0, 82, 80))):
+        want, vw = orc.descriptor_grid(img, ax, ay, 4.0, 10, **kw)
+        got, vg = ctx.descriptor_grid(img, ax, ay, 4.0, 10, **kw)
+        frac, worst = _compare(got, want, vg, vw)
+        assert frac <= ATAN2_FRAC and worst <= 2 and vw.sum() > 20, kw
+        assert (got[~vw.astype(bool)] == 0).all()
+    dimg, dmask = torch.from_numpy(img).cuda(), torch.from_numpy(mask).cuda()
+    got, vg = ctx.descriptor_grid(dimg, ax, ay, 4.0, 10, mask=dmask, roi=(9, 17, 70, 45))
+    want, vw = orc.descriptor_grid(img, ax, ay, 4.0, 10, mask=mask, roi=(9, 17, 70, 45))
+    frac, worst = _compare(got.cpu().numpy(), want, vg.cpu().numpy(), vw)
+    assert frac <= ATAN2_FRAC and worst <= 2
+
+
+@pytest.mark.gpu
+def test_descriptor_grid_desc_size_zero(ctx, orc):
+    """desc_size 0: the default ROI (right() = x() - 2) decides the last column."""
+    img = grey_image(62, 40, 48)
+    for deg in (0.0, 30.0):
+        ax, ay = axes(deg)
+        want, vw = orc.descriptor_grid(img, ax, ay, 1.0, 0)
+        got, vg = ctx.descriptor_grid(img, ax, ay, 1.0, 0)
+        frac, worst = _compare(got, want, vg, vw)
+        assert frac <= ATAN2_FRAC and worst <= 2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_scales", [1, 2])
+def test_partdetect_masked_matches_oracle(ctx, orc, pa, n_scales):
+    """pa_partdetect_masked: per-scale masks read at the border offset; an
+    all-zero mask (scale 1 of the two-scale case) empties every grid."""
+    import torch
+
+    img = grey_image(63, 64, 88)
+    m, dims = _pd_models(5, WINDOWS)
+    cls = [pa.Classifier.from_stumps(ctx, m["f"][i], m["p"][i], m["theta"][i], m["alpha"][i],
+                                     dims[i]) for i in range(len(dims))]
+    kw = dict(n_scales=2, scale_range=(0.875, 1.125)) if n_scales == 2 else {}
+    masks = np.stack([blob_mask(64 + s, 64, 88, 0.6) for s in range(n_scales)])
+    if n_scales == 2:
+        masks[1] = 0
+    want = orc.partdetect(orc.make_exp(R=4, **kw), m, WINDOWS, 4, 10, 1.0, img, mask=masks)
+    for dev in (False, True):
+        args = (torch.from_numpy(img).cuda(), torch.from_numpy(masks).cuda()) if dev else (img, masks)
+        got = ctx.partdetect(pa.exp_param(R=4, **kw), args[0], cls, WINDOWS, 4, 10, 1.0,
+                             mask=args[1])
+        got = got.cpu().numpy() if dev else got
+        assert got.shape == want.shape
+        z = want == np.float32(-1e6)
+        assert np.array_equal(got == np.float32(-1e6), z)
+        off = np.abs(got[~z] - want[~z]) > 4e-7 * np.maximum(1.0, np.abs(want[~z]))
+        assert off.mean() <= 1e-3 and (~z).sum() > 100
+    if n_scales == 2:
+        assert z[:, 1].all()

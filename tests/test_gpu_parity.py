@@ -189,6 +189,32 @@ def test_unary_maps_rotated_grid(ctx, orc):
         assert np.max(np.abs(got[0, r][~z] - want[~z])) <= 4e-6
 
 
+@pytest.mark.parametrize("Tig", [
+    synth.grid_to_image(0.75, 3.0, 2.0),                       # separable, grid step < 1 px
+    np.array([[0.9 * math.cos(0.4), -0.9 * math.sin(0.4), 20.0],
+              [0.9 * math.sin(0.4), 0.9 * math.cos(0.4), 4.0], [0, 0, 1]]),  # rotated, < sqrt 2
+    np.array([[-1.3 * math.cos(1.1), -1.3 * math.sin(1.1), 60.0],
+              [-1.3 * math.sin(1.1), 1.3 * math.cos(1.1), 30.0], [0, 0, 1]]),  # flipped
+])
+def test_unary_maps_direct_colliding(ctx, orc, Tig):
+    """TM_DIRECT maps that send several cells to one pixel keep the
+    reference's last writer (x1 outer, y1 inner loop): bit-exact cells and
+    zero pattern against the oracle's transform_grid_fixed_size."""
+    rng = np.random.default_rng(9)
+    P, R, ny, nx, H, W = 2, 2, 41, 57, 48, 64
+    s = rng.uniform(-1, 1, (P, R, ny, nx)).astype(np.float32)
+    s[:, :, ::7, ::5] = 0.0  # NO_CLASS_VALUE cells never write
+    got = ctx.unary_maps(s, Tig, H, W, interpolate=False)
+    for p in range(P):
+        for r in range(R):
+            want = orc.clip_log(orc.transform_grid(s[p, r], (H, W), Tig, 0.0, 2))
+            z = want == LOG_ZERO
+            assert np.array_equal(got[p, r] == LOG_ZERO, z)
+            d = np.abs(got[p, r][~z] - want[~z])
+            assert np.all(d <= 4e-7 * np.maximum(1.0, np.abs(want[~z])))
+            assert (~z).sum() > 200
+
+
 # ---------------------------------------------------------------- messages
 @pytest.mark.parametrize("R", [24, 12, 8, 48])
 def test_rot_joint_marginal(ctx, orc, R):

@@ -192,6 +192,70 @@ def test_cli_find_obj_from_images(tmp_path, ctx):
         assert np.array_equal(got, ref["best_conf"]), i
 
 
+@pytest.mark.gpu
+def test_cli_from_images_masks_and_two_scales(tmp_path, ctx):
+    """`--from_images --detection_masks_dir DIR` at two scales: the masks
+    come from detection_mask_imgidx<NNNNN>.mat ([S][H][W], as
+    partdetect_dense loads them) and best_conf equals pa_partdetect_masked +
+    pa_ps_infer through the Python mirror."""
+    sio = pytest.importorskip("scipy.io")
+    import partapp_gb300 as pa
+
+    rng = np.random.default_rng(18)
+    Rr, h, w, n_cls = 4, 56, 72, 10
+    windows = [(4, 16, 2.0, 8.0)] * n_cls
+    models = dict(f=rng.integers(0, 960, (n_cls, 80)).astype(np.int32),
+                  p=np.where(rng.random((n_cls, 80)) < 0.5, -1.0, 1.0).astype(np.float32),
+                  theta=rng.uniform(0, 60, (n_cls, 80)).astype(np.float32),
+                  alpha=rng.uniform(0, 1, (n_cls, 80)).astype(np.float32), D=960)
+    tree = synth.make_tree(rng, R=Rr, offset_range=(3.0, 8.0), sigma_range=(1.0, 2.5))
+    d = str(tmp_path)
+    masks_dir = os.path.join(d, "masks")
+    os.makedirs(masks_dir)
+    g = np.clip(rng.uniform(0, 255, (h, w)), 0, 255)
+    k = np.ones(5) / 5.0
+    g = np.apply_along_axis(lambda v: np.convolve(v, k, mode="same"), 0, g)
+    g = np.apply_along_axis(lambda v: np.convolve(v, k, mode="same"), 1, g)
+    g[h // 3:, :] += 60.0
+    img = np.clip(g, 0, 255).astype(np.uint8)
+    with open(os.path.join(d, "img_0.pgm"), "wb") as fh:
+        fh.write(f"P5\n{w} {h}\n255\n".encode())
+        fh.write(img.tobytes())
+    mask = np.zeros((3, h, w), np.float32)  # one more scale than used: the first two are read
+    mask[0, 6:50, 10:60] = 1.0
+    mask[1, :, 20:] = 0.5
+    mask[2] = 1.0
+    sio.savemat(os.path.join(masks_dir, "detection_mask_imgidx00001.mat"), {"detection_mask": mask})
+    with open(os.path.join(d, "exp.txt"), "w") as fh:
+        for k_, v in (("num_rotation_steps", Rr), ("min_part_rotation", -180),
+                      ("max_part_rotation", 180), ("num_scale_steps", 2),
+                      ("min_object_scale", 0.875), ("max_object_scale", 1.125),
+                      ("strip_border_detections", 0), ("roi_save_num_samples", 50),
+                      ("use_pairwise", 1), ("interpolate", 0), ("n_classifiers", n_cls),
+                      ("n_images", 1), ("desc_step", 4), ("desc_size", 10),
+                      ("window_desc_step_ratio", 1)):
+            fh.write(f"{k_} {v}\n")
+    with open(os.path.join(d, "windows.txt"), "w") as fh:
+        for wx, wy, ox, oy in windows:
+            fh.write(f"{wx} {wy} {ox} {oy}\n")
+    write_joints(os.path.join(d, "joints.txt"), tree)
+    for c in range(n_cls):
+        write_classifier(os.path.join(d, f"class_{c}.txt"), models, c)
+    r = subprocess.run([cli(), "--find_obj", "--from_images", "--expdir", d,
+                        "--detection_masks_dir", masks_dir], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    cls = ctx.classifiers(models)
+    e = pa.exp_param(R=Rr, local_max=50, interpolate=False, n_scales=2,
+                     scale_range=(0.875, 1.125))
+    lu = ctx.partdetect(e, img.astype(np.float32), cls, windows, 4, 10, 1.0, mask=mask[:2])
+    full = ctx.partdetect(e, img.astype(np.float32), cls, windows, 4, 10, 1.0)
+    assert not np.array_equal(lu, full)  # the masks removed detections
+    ref = ctx.compute_root_posterior_rot(e, tree, lu[:10], is_sparse=True)
+    got = np.loadtxt(os.path.join(d, "best_conf_0.txt"), dtype=np.float64).astype(np.float32)
+    assert np.array_equal(got, ref["best_conf"])
+
+
 # ------------------------------------------- the reference's joint files
 def write_part_conf(path, tree, n_joint_types=1):
     """PartConfig (libPartDetect/PartConfig.proto) in protobuf text format,
