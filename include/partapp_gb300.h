@@ -399,11 +399,34 @@ pa_status pa_gemm_bf16(pa_ctx *ctx, const void *A, int64_t lda, const void *B, i
  * uses.
  *   desc       [R][ny][nx][dim]
  *   Tig        as pa_unary_maps for the first n_parts classifiers
- *   scores_out [n_cls][R][ny][nx] score grids (may be NULL), in `mem` */
+ *   scores_out [n_cls][R][ny][nx] score grids (may be NULL), in `mem`
+ * One scale (num_scale_steps <= 1; several: pa_find_obj_scales). */
 pa_status pa_find_obj(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
                       const pa_classifier *const *cls, int n_cls, const float *desc, int ny,
                       int nx, int dim, const double *Tig, int tig_shared, int H, int W,
                       float *scores_out, const pa_ps_outputs *out, int mem);
+
+/* One scale's descriptor fields for pa_find_obj_scales. */
+typedef struct {
+  const float *desc;  /* [R][ny][nx][dim], in the call's `mem` space */
+  int ny, nx, dim;
+  const double *Tig;  /* as pa_find_obj: [n_parts][R][9], or one [9] if tig_shared */
+  int tig_shared;
+} pa_scale_fields;
+
+/* pa_find_obj at num_scale_steps = S scales (the scale loop of
+ * partdetect_dense, partdetect_test.cpp:116, and of computeRootPosteriorRot,
+ * objectdetect_findrot.cpp:503-678): fields[s] holds scale s's descriptors
+ * (their grid size and Tig differ per scale); each scale's normalised score
+ * grids of the first tree->n_parts classifiers go through pa_unary_maps into
+ * the [P][S][R][H][W] log unaries, then pa_ps_infer with bIsSparse.  Outputs
+ * as pa_ps_infer's for S scales; with S = 1 the results equal pa_find_obj's.
+ * Keeps one device block of P * (S + 1) * R * H * W floats (plus one scale's
+ * scores) in the context between calls. */
+pa_status pa_find_obj_scales(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                             const pa_classifier *const *cls, int n_cls,
+                             const pa_scale_fields *fields, int H, int W,
+                             const pa_ps_outputs *out, int mem);
 
 /* A batch of images sharing sizes and classifiers, each with its own tree
  * parameters (the per-image pairwise terms of poselet-conditioned models),

@@ -56,6 +56,7 @@ EXPORTS = (
     "pa_unary_net_adam", "pa_find_obj_batch_learned", "pa_add_extra_unaries", "pa_add_dpm_scores",
     "pa_nms_recursive", "pa_queue_opts_default", "pa_find_obj_queue", "pa_nms_rects",
     "pa_rect_from_hyp", "pa_descriptor_grid_masked", "pa_partdetect_masked",
+    "pa_find_obj_scales",
 )
 PA_MSG_FP32, PA_MSG_BF16_TENSOR = 0, 1
 
@@ -70,6 +71,12 @@ class Image(C.Structure):
     _fields_ = [("ep", C.c_void_p), ("tree", C.c_void_p), ("flip", C.c_int), ("desc", C.c_void_p),
                 ("ny", C.c_int), ("nx", C.c_int), ("dim", C.c_int), ("Tig", C.c_void_p),
                 ("tig_shared", C.c_int), ("H", C.c_int), ("W", C.c_int), ("out", C.c_void_p)]
+
+
+class ScaleFields(C.Structure):
+    """pa_scale_fields."""
+    _fields_ = [("desc", C.c_void_p), ("ny", C.c_int), ("nx", C.c_int), ("dim", C.c_int),
+                ("Tig", C.c_void_p), ("tig_shared", C.c_int)]
 
 
 class PaError(RuntimeError):
@@ -198,6 +205,8 @@ def load_library():
                               ip, ip, vp, P(PsOutputs), ip]
     L.pa_find_obj_batch.argtypes = [vp, P(ExpParam), ip, P(Tree), ip, P(vp), ip, vp, ip, ip, ip,
                                     P(dp), ip, ip, ip, vp, P(PsOutputs), ip]
+    L.pa_find_obj_scales.argtypes = [vp, P(ExpParam), P(Tree), ip, P(vp), ip, P(ScaleFields), ip,
+                                     ip, P(PsOutputs), ip]
     L.pa_add_extra_unaries.argtypes = [vp, P(ExpParam), P(ExtraUnary), ip, ip, vp, ip, ip, ip]
     L.pa_add_dpm_scores.argtypes = [vp, P(ExpParam), P(DpmTerms), ip, ip, vp, ip, ip, ip]
     L.pa_nms_recursive.argtypes = [vp, ip, vp, vp, vp, vp, dp, dp, vp, ip]
@@ -785,6 +794,34 @@ class Context:
                                        self._cls_array(cls_list), len(cls_list), d.ptr, ny, nx,
                                        dim, T.ctypes.data_as(C.POINTER(C.c_double)),
                                        int(T.size == 9), H, W, None, C.byref(o), d.mem))
+        return self._finish(res, P)
+
+    def find_obj_scales(self, exp: ExpParam, tree, cls_list, descs, Tigs, H, W, flip=False,
+                        want_marg=True):
+        """descs: one [R][ny][nx][dim] array per scale (grid sizes may differ),
+        Tigs: one grid -> image transform per scale ([9] or [P][R][9]); the
+        maps come back as [P][S][R][H][W] / [S][H][W], log_z as [S][P]."""
+        S = max(1, exp.num_scale_steps)
+        if len(descs) != S or len(Tigs) != S:
+            raise ValueError("one descriptor array and one Tig per scale")
+        bufs = [_Buf(d, np.float32) for d in descs]
+        if len({b.mem for b in bufs}) != 1:
+            raise ValueError("all scales' descriptors in one memory space")
+        th = _TreeHolder(tree)
+        P = th.s.n_parts
+        R = bufs[0].arr.shape[0]
+        Ts = [np.ascontiguousarray(T, dtype=np.float64).reshape(-1) for T in Tigs]
+        fields = (ScaleFields * S)(*[
+            ScaleFields(b.ptr, b.arr.shape[1], b.arr.shape[2], b.arr.shape[3], T.ctypes.data,
+                        int(T.size == 9)) for b, T in zip(bufs, Ts)])
+        res, o = self._outputs(P, R, H, W, exp.roi_save_num_samples, bufs[0].mem, bufs[0].arr,
+                               want_marg, S=S if S > 1 else 0)
+        self._check(self.L.pa_find_obj_scales(self.h, C.byref(exp), C.byref(th.s), int(flip),
+                                              self._cls_array(cls_list), len(cls_list), fields,
+                                              H, W, C.byref(o), bufs[0].mem))
+        if S > 1:
+            res["log_z"] = res["log_z"].reshape(S, P)
+            res["msg_max"] = res["msg_max"].reshape(S, -1)
         return self._finish(res, P)
 
     def find_obj_batch(self, exp: ExpParam, trees, cls_list, desc, Tig, H, W, flip=False,

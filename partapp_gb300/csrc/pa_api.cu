@@ -49,6 +49,10 @@ struct pa_ctx {
   uint64_t launches = 0;
   char *arena = nullptr;
   size_t arena_cap = 0;
+  // pa_find_obj_scales: every scale's unaries [P][S][R][H][W] and one scale's
+  // scores and unary maps, kept across the calls that fill the arena
+  char *scales_buf = nullptr;
+  size_t scales_cap = 0;
   // pinned staging of plan blobs, used round-robin: a buffer is rewritten
   // only after the upload kernel that last read it has run, so a call can
   // plan the next image while the GPU still works on the previous one
@@ -2155,7 +2159,7 @@ pa_status find_obj_impl(pa_ctx *ctx, const pa_exp_param *e, int n_img, const pa_
   if (!exp_ok(e)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
   if (n_scales(e) != 1)
     return fail(ctx, PA_ERR_UNSUPPORTED,
-                "the descriptors are one scale; run pa_ps_infer on per-scale unaries");
+                "the descriptors are one scale; pa_find_obj_scales takes several");
   if (n_img < 1 || !trees || !desc || !Tig || !outs || ny < 1 || nx < 1 || dim < 1 || H < 1 ||
       W < 1 || H > 32767 || W > 32767)
     return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
@@ -2695,6 +2699,7 @@ pa_status pa_ctx_destroy(pa_ctx *ctx) try {
     resolve_timing(ctx);
     for (cudaEvent_t e : ctx->pool) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->scales_buf) cudaFree(ctx->scales_buf);
     for (auto &sg : ctx->stage) {
       if (sg.p) cudaFreeHost(sg.p);
       if (sg.done) cudaEventDestroy(sg.done);
@@ -2965,13 +2970,12 @@ pa_status pa_classifier_info(const pa_classifier *cls, int *dim, int *n_stumps, 
   return PA_ERR_INVALID;
 }
 
-pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
-                         const float *desc, int n_fields, int ny, int nx, int dim, int normalize,
-                         float *scores, int mem) try {
-  if (!ctx) return PA_ERR_INVALID;
-  if (!desc || !scores || n_fields < 1 || ny < 1 || nx < 1 || dim < 1)
-    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
-  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+namespace {
+
+// pa_score_grids with the descriptors in in_mem and the scores in out_mem.
+pa_status score_grids_impl(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
+                           const float *desc, int in_mem, int n_fields, int ny, int nx, int dim,
+                           int normalize, float *scores, int out_mem) {
   pa_status st = check_classifiers(ctx, cls, n_parts, dim);
   if (st) return st;
   DeviceGuard dg(ctx->device);
@@ -2980,10 +2984,8 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
   const RankTables *rk = rank_tables(ctx, cls, n_parts);
   Builder b1;
   plan_stumps(b1, cls, n_parts);
-  if (mem == PA_MEM_HOST) {
-    b1.scratch<float>(din);
-    b1.scratch<float>(dout);
-  }
+  if (in_mem == PA_MEM_HOST) b1.scratch<float>(din);
+  if (out_mem == PA_MEM_HOST) b1.scratch<float>(dout);
   if (rk) {
     b1.scratch<uint32_t>(rank_bytes(dim, G, n_fields) / 4);
     b1.scratch<int>(1);
@@ -2995,18 +2997,14 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
   if (st) return st;
   b.base = ctx->arena;
   StumpPart *sp = plan_stumps(b, cls, n_parts);
-  const float *d_in = desc;
-  float *d_out = scores;
-  if (mem == PA_MEM_HOST) {
-    d_in = b.scratch<float>(din);
-    d_out = b.scratch<float>(dout);
-  }
+  const float *d_in = in_mem == PA_MEM_HOST ? b.scratch<float>(din) : desc;
+  float *d_out = out_mem == PA_MEM_HOST ? b.scratch<float>(dout) : scores;
   uint32_t *ranks = rk ? b.scratch<uint32_t>(rank_bytes(dim, G, n_fields) / 4) : nullptr;
   int *d_err = rk ? b.scratch<int>(1) : nullptr;
   st = upload_blob(ctx, b);
   if (st) return st;
-  if (mem == PA_MEM_HOST) {
-    st = copy_in(ctx, (void *)d_in, desc, din * sizeof(float), mem);
+  if (in_mem == PA_MEM_HOST) {
+    st = copy_in(ctx, (void *)d_in, desc, din * sizeof(float), in_mem);
     if (st) return st;
   }
   int errflag = 0;
@@ -3023,12 +3021,25 @@ pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_par
     PA_LAUNCH("score_grids", launch_score_grids(sp, (const bool *)ff.data(), ns.data(), n_parts, d_in, nullptr, false, G,
                                                 n_fields, dim, normalize, d_out, ctx->stream));
   }
-  if (mem == PA_MEM_HOST)
+  if (out_mem == PA_MEM_HOST)
     PA_CK(cudaMemcpyAsync(scores, d_out, dout * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
   st = sync_ctx(ctx);
   if (st) return st;
   if (errflag) return fail(ctx, PA_ERR_CUDA, "rank tile copy did not complete (error bits %d)", errflag);
   return PA_OK;
+}
+
+}  // namespace
+
+pa_status pa_score_grids(pa_ctx *ctx, const pa_classifier *const *cls, int n_parts,
+                         const float *desc, int n_fields, int ny, int nx, int dim, int normalize,
+                         float *scores, int mem) try {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!desc || !scores || n_fields < 1 || ny < 1 || nx < 1 || dim < 1)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  return score_grids_impl(ctx, cls, n_parts, desc, mem, n_fields, ny, nx, dim, normalize, scores,
+                          mem);
 } catch (const std::bad_alloc &) {
   return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
 } catch (const std::exception &exc) {
@@ -3684,14 +3695,12 @@ pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, in
   return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
 }
 
-pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
-                      int is_sparse, const float *log_unary, int H, int W,
-                      const pa_ps_outputs *out, int mem) try {
-  if (!ctx) return PA_ERR_INVALID;
-  if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
-  if (!tree || !log_unary || !out || H < 1 || W < 1 || H > 32767 || W > 32767)
-    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
-  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+namespace {
+
+// pa_ps_infer with the log unaries in unary_mem and the outputs in mem.
+pa_status ps_infer_impl(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                        int is_sparse, const float *log_unary, int unary_mem, int H, int W,
+                        const pa_ps_outputs *out, int mem) {
   PsPlan pl;
   pl.tc_mode = ctx->msg_math == PA_MSG_BF16_TENSOR;
   pl.sparse_up = is_sparse != 0;
@@ -3745,7 +3754,7 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
       for (int r = 0; r < R; ++r) masked[(size_t)p * R + r] = !(std::fabs(rot_from_index(ep, r)) < 15.0);
   auto plan = [&](Builder &b, PsPlan &p2, int **masked_dev, const float **unary_dev) {
     *masked_dev = b.param(masked.data(), masked.size());
-    *unary_dev = (mem == PA_MEM_HOST) ? b.scratch<float>((size_t)P * S * pl.N) : log_unary;
+    *unary_dev = (unary_mem == PA_MEM_HOST) ? b.scratch<float>((size_t)P * S * pl.N) : log_unary;
     std::vector<float *> rp = rp_out;
     if (S > 1 && !rp[0]) {  // the scales' root posteriors form one [S][H][W] grid
       float *g = b.scratch<float>((size_t)S * HW);
@@ -3768,8 +3777,8 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
   PsPlan pl2 = pl;
   plan(b, pl2, &mk, &ud);
   if ((st = upload_blob(ctx, b))) return st;
-  if (mem == PA_MEM_HOST)
-    if ((st = copy_in(ctx, (void *)ud, log_unary, (size_t)P * S * pl.N * sizeof(float), mem)))
+  if (unary_mem == PA_MEM_HOST)
+    if ((st = copy_in(ctx, (void *)ud, log_unary, (size_t)P * S * pl.N * sizeof(float), unary_mem)))
       return st;
   if ((st = init_slots(ctx, pl2))) return st;
   cudaStream_t s = ctx->stream;
@@ -3785,6 +3794,19 @@ pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, 
     }
   if ((st = run_ps(ctx, ep, pl2))) return st;
   return finish_ps(ctx, ep, pl2, outs.data(), mem);
+}
+
+}  // namespace
+
+pa_status pa_ps_infer(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                      int is_sparse, const float *log_unary, int H, int W,
+                      const pa_ps_outputs *out, int mem) try {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (!tree || !log_unary || !out || H < 1 || W < 1 || H > 32767 || W > 32767)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  return ps_infer_impl(ctx, ep, tree, flip, is_sparse, log_unary, mem, H, W, out, mem);
 } catch (const std::bad_alloc &) {
   return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
 } catch (const std::exception &exc) {
@@ -3949,6 +3971,67 @@ pa_status pa_find_obj_batch(pa_ctx *ctx, const pa_exp_param *ep, int n_images,
   if (!ctx) return PA_ERR_INVALID;
   return find_obj_impl(ctx, ep, n_images, trees, flip, cls, n_cls, desc, ny, nx, dim, Tig,
                        tig_shared, H, W, scores_out, out, mem);
+} catch (const std::bad_alloc &) {
+  return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
+} catch (const std::exception &exc) {
+  return fail(ctx, PA_ERR_INVALID, "%s", exc.what());
+}
+
+pa_status pa_find_obj_scales(pa_ctx *ctx, const pa_exp_param *ep, const pa_tree *tree, int flip,
+                             const pa_classifier *const *cls, int n_cls,
+                             const pa_scale_fields *fields, int H, int W,
+                             const pa_ps_outputs *out, int mem) try {
+  if (!ctx) return PA_ERR_INVALID;
+  if (!ep || !exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
+  if (!tree || !cls || !fields || !out || H < 1 || W < 1 || H > 32767 || W > 32767)
+    return fail(ctx, PA_ERR_INVALID, "invalid sizes or NULL input");
+  if (mem != PA_MEM_DEVICE && mem != PA_MEM_HOST) return fail(ctx, PA_ERR_INVALID, "bad mem");
+  const int S = n_scales(ep), R = ep->num_rotation_steps, P = tree->n_parts;
+  if (P < 1 || n_cls < P) return fail(ctx, PA_ERR_INVALID, "fewer classifiers than parts");
+  size_t max_scores = 0;
+  for (int sc = 0; sc < S; ++sc) {
+    const pa_scale_fields &f = fields[sc];
+    if (!f.desc || !f.Tig || f.ny < 1 || f.nx < 1 || f.dim < 1)
+      return fail(ctx, PA_ERR_INVALID, "scale %d: invalid fields", sc);
+    max_scores = std::max(max_scores, (size_t)P * R * f.ny * f.nx);
+  }
+  DeviceGuard dg(ctx->device);
+  // one device block outlives the arena-using calls below: the unaries of
+  // every scale, then one scale's scores and unary maps
+  const size_t N = (size_t)R * H * W;
+  const size_t n_lu = (size_t)P * S * N, n_map = (size_t)P * N;
+  const size_t need = (n_lu + n_map + max_scores) * sizeof(float) + 512;
+  if (ctx->scales_cap < need) {
+    PA_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->scales_buf) cudaFree(ctx->scales_buf);
+    ctx->scales_buf = nullptr;
+    ctx->scales_cap = 0;
+    if (cudaMalloc(&ctx->scales_buf, need) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, PA_ERR_NOMEM, "device memory exhausted (%zu bytes)", need);
+    }
+    ctx->scales_cap = need;
+  }
+  float *lu = reinterpret_cast<float *>(ctx->scales_buf);
+  float *maps = lu + n_lu;
+  float *scores = reinterpret_cast<float *>(
+      (reinterpret_cast<uintptr_t>(maps + n_map) + 255) & ~(uintptr_t)255);
+  // per scale: partdetect_dense's score grids with normalised votes, the
+  // grid -> image maps, clip + log (objectdetect_findrot.cpp:834-845), into
+  // the [P][S][R][H][W] block computeRootPosteriorRot reads
+  for (int sc = 0; sc < S; ++sc) {
+    const pa_scale_fields &f = fields[sc];
+    pa_status st = score_grids_impl(ctx, cls, P, f.desc, mem, R, f.ny, f.nx, f.dim, 1, scores,
+                                    PA_MEM_DEVICE);
+    if (st) return st;
+    if ((st = pa_unary_maps(ctx, scores, P, R, f.ny, f.nx, f.Tig, f.tig_shared, ep->interpolate,
+                            H, W, maps, PA_MEM_DEVICE)))
+      return st;
+    PA_CK(cudaMemcpy2DAsync(lu + (size_t)sc * N, S * N * sizeof(float), maps, N * sizeof(float),
+                            N * sizeof(float), (size_t)P, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  // findObjectImageRotJoints passes bIsSparse = true (objectdetect_findrot.cpp:740)
+  return ps_infer_impl(ctx, ep, tree, flip, 1, lu, PA_MEM_DEVICE, H, W, out, mem);
 } catch (const std::bad_alloc &) {
   return fail(ctx, PA_ERR_NOMEM, "host memory exhausted");
 } catch (const std::exception &exc) {
@@ -4751,7 +4834,7 @@ pa_status pa_find_obj_batch_learned(pa_ctx *ctx, const pa_exp_param *ep, int n_i
   if (!ep || !exp_ok(ep)) return fail(ctx, PA_ERR_INVALID, "invalid experiment parameters");
   if (n_scales(ep) != 1)
     return fail(ctx, PA_ERR_UNSUPPORTED,
-                "the descriptors are one scale; run pa_ps_infer on per-scale unaries");
+                "the descriptors are one scale; pa_find_obj_scales takes several");
   if (!net || n_images < 1 || !trees || !Tig || !out || ny < 1 || nx < 1 || dim != net->dim ||
       H < 1 || W < 1 || H > 32767 || W > 32767 || trees[0].n_parts != net->P)
     return fail(ctx, PA_ERR_INVALID, "invalid sizes, NULL input, or a net of another shape");

@@ -469,6 +469,43 @@ def test_find_obj_batch_device_resident(ctx, orc):
         assert maxnorm_err(got[i]["root_post"].cpu().numpy(), want["root_post"]) <= TOL_F32
 
 
+def test_find_obj_scales(ctx, orc):
+    """pa_find_obj_scales: with one scale it is pa_find_obj bit for bit; with
+    two (grids of stride 4 and 5, their own Tig) it matches the oracle's
+    per-scale unaries followed by computeRootPosteriorRot over both scales."""
+    import torch
+
+    R, H, W = 8, 48, 64
+    img = synth.make_image(201, R=R, H=H, W=W, n_stumps=60, D=96, offset_range=(3, 8),
+                           sigma_range=(1, 2.5))
+    tree, models = img["tree"], img["models"]
+    rng = np.random.default_rng(202)
+    descs = [img["desc"], synth.make_descriptors(rng, R, 9, 12, 96)]
+    tigs = [img["Tig"], synth.grid_to_image(5.0, 1.0, 2.0)]
+    cls = ctx.classifiers(models)
+    one = ctx.find_obj_scales(_pa_exp(R), tree, cls, descs[:1], tigs[:1], H, W)
+    ref = ctx.find_obj(_pa_exp(R), tree, cls, descs[0], tigs[0], H, W)
+    assert np.array_equal(one["log_marg"], ref["log_marg"])
+    assert np.array_equal(one["best_conf"], ref["best_conf"])
+    assert np.array_equal(one["root_post"], ref["root_post"])
+    kw = dict(n_scales=2, scale_range=(0.8, 1.25))
+    lu = np.stack([orc.find_obj(orc.make_exp(R=R), tree, models, d, T, H, W)["log_unary"]
+                   for d, T in zip(descs, tigs)], axis=1)
+    want = orc.ps_infer(orc.make_exp(R=R, sparse=True, **kw), tree, lu)
+    for dev in (False, True):
+        ds = [torch.from_numpy(d).cuda() for d in descs] if dev else descs
+        got = ctx.find_obj_scales(_pa_exp(R, **kw), tree, cls, ds, tigs, H, W)
+        marg = got["log_marg"].cpu().numpy() if dev else got["log_marg"]
+        assert marg.shape == (10, 2, R, H, W)
+        for p in range(10):
+            for sc in range(2):
+                assert maxnorm_err(marg[p, sc], want["log_marg"][p, sc]) <= TOL_F32, (p, sc)
+        assert np.array_equal(got["best_conf"][:, [0, 2, 4, 5]], want["best_conf"][:, [0, 2, 4, 5]])
+        # the same unaries through pa_ps_infer give the same marginals
+        ps = ctx.compute_root_posterior_rot(_pa_exp(R, **kw), tree, lu, is_sparse=True)
+        assert maxnorm_err(ps["log_marg"], marg) <= 1e-6
+
+
 def test_find_obj_batch_host_ring_matches_device(ctx):
     """Host descriptors go through the copy/compute ring one image at a time;
     results (and the strided score-grid output) must equal the batched
