@@ -193,28 +193,43 @@ __device__ __forceinline__ void rows_tile(const MsgDesc *__restrict__ mdp, int R
     // Raw child values of the shifted rows land in E by asynchronous copies
     // (all of a thread's copies in flight at once).  Cells without a source
     // get LOG_ZERO, the dummy rotation of an odd R gets -inf (exp -> 0); the
-    // exp is taken when the rotation filter reads the column.  Thread tid
-    // stages word h = tid & 1 of pair-cells (p, gx), walking the pair-cells
-    // in steps of blockDim.x / 2.
+    // exp is taken when the rotation filter reads the column.  A rotation
+    // pair p belongs to wpp warps; lane l stages word h = l & 1 (rotation
+    // 2p + h) of the pair-cells l >> 1, + 16, ... of its warp's columns, so
+    // a warp writes consecutive words and reads the row's shift once.
     float *Ef = reinterpret_cast<float *>(E);
-    const int h = tid & 1, step = blockDim.x >> 1;
-    int p = (tid >> 1) / gw, c = (tid >> 1) - ((tid >> 1) / gw) * gw;
-    while (p < RP) {
-      const int r = 2 * p + h;
-      const int gx = gx0 + c;
-      float *dst = Ef + (p * WP + lg0 + c) * 2 + h;
-      if (r >= R) {
-        *dst = -INFINITY;
-      } else {
-        const int ro = rowoff[r];
-        const int sx = ro >= 0 ? shift_src(sdesc[r], md.tx_in + r * W, gx) : -1;
-        if (sx >= 0) cp_async4(dst, md.in + (int64_t)ro + sx, true);
-        else *dst = kLogZero;
-      }
-      c += step;
-      while (c >= gw) {
-        c -= gw;
-        ++p;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int h = lane & 1;
+    const int wpp = RP >= nwarps ? 1 : nwarps / RP;  // warps per rotation pair
+    const int groups = nwarps / wpp;                 // pairs staged at a time
+    const int cstep = 16 * wpp;
+    if (warp < groups * wpp) {
+      for (int p = warp / wpp; p < RP; p += groups) {
+        const int r = 2 * p + h;
+        float *dst = Ef + ((size_t)p * WP + lg0) * 2 + h;  // pair-cell c at dst[2 c]
+        int c = (warp % wpp) * 16 + (lane >> 1);
+        const int ro = r < R ? rowoff[r] : -1;
+        if (ro < 0) {
+          const float fillv = r >= R ? -INFINITY : kLogZero;
+          for (; c < gw; c += cstep) dst[2 * c] = fillv;
+          continue;
+        }
+        const int4 d = sdesc[r];
+        const float *src = md.in + (int64_t)ro;
+        if (d.w) {  // the plain shift gx -> gx + d.x on [d.y, d.z)
+          for (; c < gw; c += cstep) {
+            const int gx = gx0 + c;
+            if (gx >= d.y && gx < d.z) cp_async4(dst + 2 * c, src + gx + d.x, true);
+            else dst[2 * c] = kLogZero;
+          }
+        } else {
+          const int16_t *tab = md.tx_in + r * W;
+          for (; c < gw; c += cstep) {
+            const int sx = tab[gx0 + c];
+            if (sx >= 0) cp_async4(dst + 2 * c, src + sx, true);
+            else dst[2 * c] = kLogZero;
+          }
+        }
       }
     }
     cp_async_wait_all();
