@@ -806,28 +806,52 @@ __device__ __forceinline__ void cols_tile_tma(const MsgDesc *__restrict__ mdp, i
   float *dst0 = md.dst0, *dst1 = md.dst1;
   int k0 = kFkeyNegInf, k1 = kFkeyNegInf;
   unsigned long long am = 0ull;
-#pragma unroll 4
-  for (int yy = y0 + warp; yy < y1; yy += nw) {
-    if (!colin) continue;
-    float m = kLogZero;
-    if (colok && yy >= ya && yy < yb) m = __fadd_rn(log_or_zero(F[(yy - ya) * kFP + fc]), M);
-    const int idx = r * HW + yy * W + xx;
-    const int si = (yy - y0) * kTX + lane;
+  // One loop per mode (uniform for the CTA).  The running maxima are keyed
+  // as before; a cell below the current maximum as a float (never true for
+  // NaN) cannot change its key and skips the key arithmetic.
+  if (colin) {
+    auto mval = [&](int yy) {
+      return (colok && yy >= ya && yy < yb) ? __fadd_rn(log_or_zero(F[(yy - ya) * kFP + fc]), M)
+                                            : kLogZero;
+    };
+    const int didx = nw * W, dsi = nw * kTX;
+    int idx = r * HW + (y0 + warp) * W + xx, si = warp * kTX + lane;
     if (mode == EPI_STORE) {
-      dst0[idx] = m;
+#pragma unroll 4
+      for (int yy = y0 + warp; yy < y1; yy += nw, idx += didx) dst0[idx] = mval(yy);
     } else if (mode == EPI_ADD) {
-      const float ov = __fadd_rn(m, S0[si]);
-      dst0[idx] = ov;
-      k0 = max(k0, (ov == ov) ? fkey(ov) : kFkeyNegInf);
+      float b0 = -INFINITY;
+#pragma unroll 4
+      for (int yy = y0 + warp; yy < y1; yy += nw, idx += didx, si += dsi) {
+        const float ov = __fadd_rn(mval(yy), S0[si]);
+        dst0[idx] = ov;
+        if (!(ov < b0)) {
+          const int k = (ov == ov) ? fkey(ov) : kFkeyNegInf;
+          if (k > k0) k0 = k, b0 = ov;
+        }
+      }
     } else {
-      const float ov = __fadd_rn(S0[si], m);
-      dst0[idx] = ov;
-      const unsigned long long k = akey(ov, (uint32_t)idx);
-      am = k > am ? k : am;
-      if (dst1) {
-        const float o1 = __fadd_rn(S1[si], m);
-        dst1[idx] = o1;
-        k1 = max(k1, (o1 == o1) ? fkey(o1) : kFkeyNegInf);
+      float ba = -INFINITY, b1 = -INFINITY;
+#pragma unroll 4
+      for (int yy = y0 + warp; yy < y1; yy += nw, idx += didx, si += dsi) {
+        const float m = mval(yy);
+        const float ov = __fadd_rn(S0[si], m);
+        dst0[idx] = ov;
+        if (!(ov < ba)) {
+          const unsigned long long k = akey(ov, (uint32_t)idx);
+          if (k > am) {
+            am = k;
+            if (ov == ov) ba = ov;  // a NaN's key is the lowest: it never raises the filter
+          }
+        }
+        if (dst1) {
+          const float o1 = __fadd_rn(S1[si], m);
+          dst1[idx] = o1;
+          if (!(o1 < b1)) {
+            const int k = (o1 == o1) ? fkey(o1) : kFkeyNegInf;
+            if (k > k1) k1 = k, b1 = o1;
+          }
+        }
       }
     }
   }
