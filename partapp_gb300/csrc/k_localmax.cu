@@ -79,19 +79,19 @@ __global__ void __launch_bounds__(32 * kLmWarps, 3) k_lm_cand(const float *const
   lm_load_slice(C, g + HW, ya, H, W, x, S > 1);
   for (int s = 0; s < S; ++s) {
     lm_load_slice(D, g + (int64_t)(s + 2) * HW, ya, H, W, x, s + 2 < S);
-    float bl[kLmR], br[kLmR];
+    // "no neighbour is greater" against row maxima: fmaxf skips NaN
+    // neighbours, which never compare greater, so the test is unchanged
+    float ml[kLmR], mh[kLmR];  // max of left/right; of left/centre/right
 #pragma unroll
     for (int j = 0; j < kLmR; ++j) {
-      bl[j] = __shfl_up_sync(0xFFFFFFFFu, B[j], 1);
-      br[j] = __shfl_down_sync(0xFFFFFFFFu, B[j], 1);
+      ml[j] = fmaxf(__shfl_up_sync(0xFFFFFFFFu, B[j], 1), __shfl_down_sync(0xFFFFFFFFu, B[j], 1));
+      mh[j] = fmaxf(ml[j], B[j]);
     }
 #pragma unroll
     for (int j = 1; j <= kLmRows; ++j) {
       const int y = ya - 1 + j;
       const float v = B[j];
-      bool lm = out_lane && y < H && !(B[j - 1] > v) && !(bl[j - 1] > v) && !(br[j - 1] > v) &&
-                !(bl[j] > v) && !(br[j] > v) && !(B[j + 1] > v) && !(bl[j + 1] > v) &&
-                !(br[j + 1] > v);
+      bool lm = out_lane && y < H && !(mh[j - 1] > v) && !(ml[j] > v) && !(mh[j + 1] > v);
       if (s > 0) lm = lm && A[j] < v;
       if (s < S - 1) lm = lm && C[j] < v;
       unsigned long long key = 0ull;

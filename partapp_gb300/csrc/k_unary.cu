@@ -107,6 +107,11 @@ __global__ void __launch_bounds__(kThreads) k_unary_bilinear_sep(const UnaryMap 
   const int y0 = blockIdx.y * rows_per_cta;
   const int y1e = min(H, y0 + rows_per_cta);
   const float eps10 = 10.0f * 1.1920928955078125e-07f;  // 10 * FLT_EPSILON
+  if (masked_all) {  // every output is LOG_ZERO (uniform for the CTA)
+    for (int i = threadIdx.x; i < (y1e - y0) * W; i += blockDim.x) out[(int64_t)y0 * W + i] = kLogZero;
+    if (max_slot) block_max_commit(fkey(kLogZero), max_slot);
+    return;
+  }
   int *sx = reinterpret_cast<int *>(sm);          // [W] ix1
   float *sa = sm + W;                             // [W] a
   float *sg = sm + 2 * W;                         // [nrows][nx] grid rows
@@ -146,7 +151,7 @@ __global__ void __launch_bounds__(kThreads) k_unary_bilinear_sep(const UnaryMap 
         }
       }
       float o = clip_log(v);
-      if (masked_all || (strip > 0 && (x3 < strip || x3 >= W - strip))) o = kLogZero;
+      if (strip > 0 && (x3 < strip || x3 >= W - strip)) o = kLogZero;
       out[(int64_t)y3 * W + x3] = o;
       kmax = max(kmax, key_of(o));
     }
