@@ -454,17 +454,23 @@ __global__ void __launch_bounds__(32 * kRankMaxWarps, 1) k_rank_votes(
       const int64_t loc0 = (t - (int64_t)field * tiles_per_field) * kRankLoc;
       const uint2 *r = srec + (size_t)warp * npad;
       const unsigned char *lane_base = base + lane * 4;
-      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+      // locations 0, 1 and 2, 3 summed in pairs by packed adds (two IEEE
+      // float adds each, the same order as scalar sums)
+      unsigned long long s01 = 0ull, s23 = 0ull;
 #pragma unroll 4
       for (int i = 0; i < npad; ++i) {
         const uint2 q = r[i];
         const uint32_t w = *reinterpret_cast<const uint32_t *>(lane_base + (q.x & 0x1FFFFu));
         const uint32_t d = __byte_perm(q.x, 0u, 0x3333u) - w;
-        s0 += __uint_as_float(q.y ^ ((d << 24) & 0x80000000u));
-        s1 += __uint_as_float(q.y ^ ((d << 16) & 0x80000000u));
-        s2 += __uint_as_float(q.y ^ ((d << 8) & 0x80000000u));
-        s3 += __uint_as_float(q.y ^ (d & 0x80000000u));
+        const uint32_t v0 = q.y ^ ((d << 24) & 0x80000000u), v1 = q.y ^ ((d << 16) & 0x80000000u);
+        const uint32_t v2 = q.y ^ ((d << 8) & 0x80000000u), v3 = q.y ^ (d & 0x80000000u);
+        const unsigned long long a01 = ((unsigned long long)v1 << 32) | v0;
+        const unsigned long long a23 = ((unsigned long long)v3 << 32) | v2;
+        asm("add.rn.f32x2 %0, %0, %1;" : "+l"(s01) : "l"(a01));
+        asm("add.rn.f32x2 %0, %0, %1;" : "+l"(s23) : "l"(a23));
       }
+      float s0 = __uint_as_float((uint32_t)s01), s1 = __uint_as_float((uint32_t)(s01 >> 32));
+      float s2 = __uint_as_float((uint32_t)s23), s3 = __uint_as_float((uint32_t)(s23 >> 32));
       if (normalize) {
         const float sa = sum_alpha[warp];
         s0 = __fdiv_rn(s0, sa);
