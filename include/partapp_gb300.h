@@ -177,8 +177,10 @@ pa_status pa_descriptor_grid(pa_ctx *ctx, const float *image, int img_h, int img
  * position inside the image also gets no descriptor (valid 0, cell zero)
  *   - when detection_mask [img_h][img_w] (same memory as image; NULL: none)
  *     is 0 at the position's truncated image coordinates, or
- *   - when it lies outside roi = {x, y, width, height}, the rectangle
- *     QRect(x, y, width, height) spans (inclusive right edge x + width - 1).
+ *   - when it lies outside roi = {x, y, width, height} (a host array), the
+ *     rectangle QRect(x, y, width, height) spans (inclusive right edge
+ *     x + width - 1).  Only a mask value equal to 0 removes a position
+ *     (NaN does not, as in the reference's == 0 test).
  *     NULL stands for the default QRect(0, 0, img_w - 1, img_h - 1) of the
  *     reference's other overloads, which excludes the last column and row:
  *     with desc_size = 0 that removes positions past img_w - 2 / img_h - 2;

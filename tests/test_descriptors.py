@@ -398,6 +398,12 @@ def test_descriptor_grid_mask_and_roi_pins(orc):
         # the whole image as the ROI tests nothing
         _, valid = orc.descriptor_grid(img, ax, ay, step, ds, roi=(0, 0, 80, 64))
         assert np.array_equal(valid, vf)
+        # only a mask value equal to 0 removes a position: -0 does, NaN does not
+        odd = np.where(mask == 0, np.float32(np.nan), np.float32(-0.0))
+        _, valid = orc.descriptor_grid(img, ax, ay, step, ds, mask=odd)
+        want = np.zeros_like(inside)
+        want[inside] = np.isnan(odd[py[inside].astype(np.int64), px[inside].astype(np.int64)])
+        assert np.array_equal(valid.astype(bool), want) and want.any()
 
 
 def test_default_roi_drops_last_column_when_desc_size_is_zero(orc):
