@@ -84,40 +84,56 @@ __device__ __forceinline__ int shift_src(int4 d, const int16_t *tab, int pos) {
 __device__ __forceinline__ float log_or_zero(float f) { return f == 0.f ? kLogZero : logf(f); }
 
 // ---------------------------------------------------------------------------
-// Rotation filter on one column held in registers: out[r] = sum_j t[j] *
+// Rotation filter on columns held in registers: out[r] = sum_j t[j] *
 // e[(r - NR + j) mod R] (grid_filter_1d_blas_wraparound,
 // libMultiArray/multi_array_filter.hpp:116-155).
+// E = exp(J10 - M) and the filter for the columns [x0, x1) of the staged
+// pairs E (stride WP), a column per thread at a time; the taps (2 NR + 1)
+// stay in registers for all of a thread's columns.  Returns whether an exp
+// overflowed.
 // ---------------------------------------------------------------------------
 template <int R, int NR>
-__device__ __forceinline__ void rot_filter_fixed(const float (&e)[R], float2 *out, int stride,
-                                                 const float *t) {
+__device__ __forceinline__ bool rot_filter_columns(float2 *E, int WP, int x0, int x1,
+                                                   float negM, const float *t) {
   static_assert(R % 2 == 0, "rotation pairs");
   float tv[2 * NR + 1];
 #pragma unroll
   for (int j = 0; j < 2 * NR + 1; ++j) tv[j] = t[j];
+  float emax = 0.f;
+  for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+    float e[R];
 #pragma unroll
-  for (int q = 0; q < R / 2; ++q) {
-    float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-    for (int j = 0; j < 2 * NR + 1; ++j) {
-      a0 = fmaf(tv[j], e[((2 * q - NR + j) % R + R) % R], a0);
-      a1 = fmaf(tv[j], e[((2 * q + 1 - NR + j) % R + R) % R], a1);
+    for (int p = 0; p < R / 2; ++p) {
+      const float2 v = E[p * WP + x];
+      e[2 * p] = expf(__fadd_rn(v.x, negM));
+      e[2 * p + 1] = expf(__fadd_rn(v.y, negM));
+      emax = fmaxf(emax, fmaxf(e[2 * p], e[2 * p + 1]));  // fmaxf skips NaN, as == INF does
     }
-    out[q * stride] = make_float2(a0, a1);
+    float2 *out = E + x;
+#pragma unroll
+    for (int q = 0; q < R / 2; ++q) {
+      float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+      for (int j = 0; j < 2 * NR + 1; ++j) {
+        a0 = fmaf(tv[j], e[((2 * q - NR + j) % R + R) % R], a0);
+        a1 = fmaf(tv[j], e[((2 * q + 1 - NR + j) % R + R) % R], a1);
+      }
+      out[q * WP] = make_float2(a0, a1);
+    }
   }
+  return emax == INFINITY;
 }
 
+// rot_filter_columns for the runtime half-width nr (one dispatch per tile);
+// status bit 1: an exp overflowed, bit 2: nr beyond the specialisations.
 template <int R, int NR>
-__device__ __forceinline__ bool rot_filter_dispatch(int nr, const float (&e)[R], float2 *out,
-                                                    int stride, const float *t) {
+__device__ __forceinline__ int rot_filter_dispatch(int nr, float2 *E, int WP, int x0, int x1,
+                                                   float negM, const float *t) {
   if constexpr (NR < 0) {
-    return false;
+    return 2;
   } else {
-    if (nr == NR) {
-      rot_filter_fixed<R, NR>(e, out, stride, t);
-      return true;
-    }
-    return rot_filter_dispatch<R, NR - 1>(nr, e, out, stride, t);
+    if (nr == NR) return rot_filter_columns<R, NR>(E, WP, x0, x1, negM, t) ? 1 : 0;
+    return rot_filter_dispatch<R, NR - 1>(nr, E, WP, x0, x1, negM, t);
   }
 }
 
@@ -250,19 +266,8 @@ __device__ __forceinline__ void rows_tile(const MsgDesc *__restrict__ mdp, int R
   if (md.rlen > 0) {
     const int nr = (md.rlen - 1) / 2;
     if constexpr (RT > 0) {
-      for (int x = lg0 + tid; x < lg1; x += blockDim.x) {
-        float e[RT];
-        bool inf = false;
-#pragma unroll
-        for (int p = 0; p < RT / 2; ++p) {
-          const float2 v = E[p * WP + x];
-          e[2 * p] = expf(__fadd_rn(v.x, negM));
-          e[2 * p + 1] = expf(__fadd_rn(v.y, negM));
-          inf = inf || e[2 * p] == INFINITY || e[2 * p + 1] == INFINITY;
-        }
-        if (inf) atomicOr(err, 1);
-        if (!rot_filter_dispatch<RT, (RT - 1) / 2>(nr, e, E + x, WP, tr)) atomicOr(err, 2);
-      }
+      const int bits = rot_filter_dispatch<RT, (RT - 1) / 2>(nr, E, WP, lg0, lg1, negM, tr);
+      if (bits) atomicOr(err, bits);
     } else {
       float *col = tr + kMaxRot;  // [blockDim.x][R] scratch
       float *Ef = reinterpret_cast<float *>(E);
