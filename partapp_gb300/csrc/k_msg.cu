@@ -342,16 +342,27 @@ __device__ __forceinline__ void rows_tile(const MsgDesc *__restrict__ mdp, int R
     }
     const int nx = min(32 * kNO, ncw - xs);
     float *o = e2 + (int64_t)(2 * p) * HW + (int64_t)y * W + xc0 + xs;
+    // the staged row goes out in 16-byte words when W is a multiple of 4
+    // (then o, HW and nx are too: the chunk and strip starts are multiples of 4)
+    auto copy_out = [&](float *dst) {
+      if ((W & 3) == 0) {
+        const float4 *src4 = reinterpret_cast<const float4 *>(ws);
+        float4 *dst4 = reinterpret_cast<float4 *>(dst);
+        for (int j = lane; j < (nx >> 2); j += 32) dst4[j] = src4[j];
+      } else {
+        for (int j = lane; j < nx; j += 32) dst[j] = ws[j];
+      }
+    };
 #pragma unroll
     for (int i = 0; i < kNO; ++i) ws[lane * kNO + i] = acc[i].x;  // odd kNO: conflict-free
     __syncwarp();
-    for (int j = lane; j < nx; j += 32) o[j] = ws[j];
+    copy_out(o);
     __syncwarp();
     if (2 * p + 1 < R) {
 #pragma unroll
       for (int i = 0; i < kNO; ++i) ws[lane * kNO + i] = acc[i].y;
       __syncwarp();
-      for (int j = lane; j < nx; j += 32) o[HW + j] = ws[j];
+      copy_out(o + HW);
       __syncwarp();
     }
   }
