@@ -127,7 +127,10 @@ __global__ void __launch_bounds__(kThreads) k_unary_bilinear_sep(const UnaryMap 
   }
   for (int i = threadIdx.x; i < nrows * nx; i += blockDim.x) sg[i] = __ldg(grid + (int64_t)rlo * nx + i);
   __syncthreads();
-  int kmax = kFkeyNegInf;
+  // running maximum as a float: fmaxf skips NaN (key_of's -inf) and the
+  // outputs are never -0 (logf gives +0 at 1), so key_of(omax) is the
+  // maximum of the outputs' keys
+  float omax = -INFINITY;
   for (int y3 = y0; y3 < y1e; ++y3) {
     const int iy1 = rowy[y3];
     const float b = rowb[y3];
@@ -153,10 +156,10 @@ __global__ void __launch_bounds__(kThreads) k_unary_bilinear_sep(const UnaryMap 
       float o = clip_log(v);
       if (strip > 0 && (x3 < strip || x3 >= W - strip)) o = kLogZero;
       out[(int64_t)y3 * W + x3] = o;
-      kmax = max(kmax, key_of(o));
+      omax = fmaxf(omax, o);
     }
   }
-  if (max_slot) block_max_commit(kmax, max_slot);
+  if (max_slot) block_max_commit(key_of(omax), max_slot);
 }
 
 // TM_DIRECT, pass 1: every pixel starts at NO_CLASS_VALUE -> LOG_ZERO.
