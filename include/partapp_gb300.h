@@ -217,7 +217,9 @@ typedef struct {
  * bSqueeze and normalised votes: grid_x_count = window_size_x / desc_step +
  * 1, likewise in y; grid_step = desc_step / window_step), the squeeze to the
  * non-empty box, the TM_DIRECT map into the image by Tig = (Ti_ei Ti2)(T2g
- * Tg4), then clip_scores_fill + computeLogGrid.  Every one of the
+ * Tg4) (where cells share a pixel, window steps <= sqrt 2 px, the last one
+ * in the reference's x-outer, y-inner loop wins), then clip_scores_fill +
+ * computeLogGrid.  Every one of the
  * num_scale_steps = S scales has its own descriptor step and size
  * (scale * desc_step, round(scale * desc_size)), border and grids (the scale
  * loop, :116); the result feeds pa_ps_infer unchanged.  `flip` negates the
@@ -262,7 +264,9 @@ pa_status pa_score_grids_window(pa_ctx *ctx, const pa_classifier *const *cls,
  * (libPartApp/partapp.cpp:876-899) / partdetect_dense
  * (partdetect_test.cpp:268-292), then clip_scores_fill + computeLogGrid
  * (objectdetect_findrot.cpp:834-845).  Tig is [n_parts][R][9] (row-major
- * 3x3, grid -> image), or one shared [9] matrix if tig_shared.
+ * 3x3, grid -> image), or one shared [9] matrix if tig_shared.  With
+ * interpolate = 0 (TM_DIRECT) cells that round to one pixel leave the value
+ * of the last of them in the reference's loop (x1 outer, y1 inner).
  *   scores    [n_parts][R][ny][nx]
  *   log_unary [n_parts][R][H][W] */
 pa_status pa_unary_maps(pa_ctx *ctx, const float *scores, int n_parts, int R, int ny,
