@@ -52,3 +52,29 @@ def test_null_context_is_rejected(lib):
     # no GPU work: every entry point validates its context first
     assert lib.pa_ctx_synchronize(None) == 1
     assert lib.pa_score_grids(None, None, 0, None, 0, 0, 0, 0, 0, None, 0) == 1
+
+
+def test_null_context_is_rejected_by_the_image_entries(lib):
+    # the descriptor, detection and multi-scale entries check the context
+    # before anything else (no GPU is touched)
+    assert lib.pa_descriptor_grid_masked(None, None, 0, 0, None, None, 0.0, 0, None, None, None,
+                                         None, 0) == 1
+    assert lib.pa_partdetect_masked(None, None, None, 0, 0, 0, None, 0, None, None, None, None,
+                                    0) == 1
+    assert lib.pa_find_obj_scales(None, None, None, 0, None, 0, None, 0, 0, None, 0) == 1
+    assert lib.pa_nms_rects(None, 0, None, None, 0.5, None, 0) == 1
+
+
+def test_mask_buffers_follow_the_image(lib):
+    """A numpy detection mask beside a host image stays a host buffer of the
+    checked shape; a wrong shape is refused before any call."""
+    import numpy as np
+
+    import partapp_gb300 as pa
+
+    img = pa._Buf(np.zeros((6, 8), np.float32), np.float32)
+    m = pa._mask_buf(np.ones((6, 8), np.float64), img, (6, 8))
+    assert m.mem == pa.PA_MEM_HOST and m.arr.dtype == np.float32 and m.arr.shape == (6, 8)
+    assert pa._mask_buf(None, img, (6, 8)) is None
+    with pytest.raises(ValueError):
+        pa._mask_buf(np.ones((2, 6, 8), np.float32), img, (6, 8))
