@@ -56,6 +56,8 @@
 // mixtures of pairwise terms (num_joint_types > 1), --pred_dir DIR
 // (testlist_pred_pwise_imgidx_<i>.mat, clusidx_test -> joint_<c>_<p>_tidx_<t>.mat).
 // --joints_dump prints the joints as loaded (no GPU needed).
+// --mask_dump S H W (with --detection_masks_dir DIR --first i) prints image i's
+// detection masks as loaded for S scales of H x W (no GPU needed).
 //
 // --mat_dump FILE prints every variable of a MAT-file (name, class, dims and
 // values in MATLAB's column-major order, cells one by one).
@@ -271,6 +273,7 @@ void usage() {
                "                        [--dpm_unary_dir DIR --use_dpm_head --dpm_head_weight w\n"
                "                         --use_dpm_unary --dpm_unary_weight w --dpm_rot]\n"
                "                        [--part_conf FILE --spatial_dir DIR [--pred_dir DIR]]\n"
+               "       partapp_find_obj --mask_dump S H W --detection_masks_dir DIR [--first i]\n"
                "       partapp_find_obj --joints_dump [--expdir DIR | --part_conf FILE\n"
                "                        --spatial_dir DIR [--pred_dir DIR]] [--first i --numimgs n]\n"
                "       partapp_find_obj --mat_dump FILE\n";
@@ -285,6 +288,8 @@ int main(int argc, char **argv) {
   DpmOptions dpm;
   int first = 0, numimgs = -1, batch = 1, device = 0;
   bool find_obj = false, flip = false, save_marg = false, from_images = false, joints_dump = false;
+  bool mask_dump = false;
+  int mask_dims[3] = {0, 0, 0};
   JointSource jsrc;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
@@ -307,6 +312,12 @@ int main(int argc, char **argv) {
     else if (a == "--part_conf") jsrc.part_conf = next();
     else if (a == "--spatial_dir") jsrc.spatial_dir = next();
     else if (a == "--joints_dump") joints_dump = true;
+    else if (a == "--mask_dump") {
+      mask_dims[0] = std::atoi(next().c_str());
+      mask_dims[1] = std::atoi(next().c_str());
+      mask_dims[2] = std::atoi(next().c_str());
+      mask_dump = true;
+    }
     else if (a == "--pred_dir") jsrc.pred_dir = pred_dir = next();
     else if (a == "--pred_rot_weight") rot_w = (float)std::atof(next().c_str());
     else if (a == "--pred_pos_weight") pos_w = (float)std::atof(next().c_str());
@@ -333,6 +344,26 @@ int main(int argc, char **argv) {
     }
     else if (a == "--help" || a == "-h") { usage(); return 0; }
     else { std::cerr << "unknown option " << a << "\n"; usage(); return 2; }
+  }
+  if (mask_dump) {
+    try {
+      const int S = mask_dims[0], H = mask_dims[1], W = mask_dims[2];
+      if (S < 1 || H < 1 || W < 1 || masks_dir.empty())
+        throw std::runtime_error("--mask_dump needs S H W >= 1 and --detection_masks_dir");
+      const std::vector<float> m = loadDetectionMask(masks_dir, first, S, H, W);
+      for (int sc = 0; sc < S; ++sc) {
+        std::printf("scale %d\n", sc);
+        for (int y = 0; y < H; ++y) {
+          for (int x = 0; x < W; ++x)
+            std::printf(x ? " %.9g" : "%.9g", (double)m[((size_t)sc * H + y) * W + x]);
+          std::printf("\n");
+        }
+      }
+    } catch (const std::exception &ex) {
+      std::cerr << "partapp_find_obj: " << ex.what() << "\n";
+      return 1;
+    }
+    return 0;
   }
   if (joints_dump) {
     try {

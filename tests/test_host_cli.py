@@ -81,6 +81,35 @@ def test_cli_builds_and_prints_usage():
     assert r.returncode == 0 and "--find_obj" in r.stdout
 
 
+def test_detection_masks_load_as_the_reference_reads_them(tmp_path):
+    """detection_mask_imgidx<NNNNN>.mat (NNNNN = imgidx + 1), variable
+    detection_mask [S'][H][W] (mat_load_multi_array keeps MATLAB's dims):
+    the first S scales come back as [S][H][W]; a file of another image size
+    is refused."""
+    sio = pytest.importorskip("scipy.io")
+    rng = np.random.default_rng(4)
+    S, H, W = 3, 5, 7
+    mask = rng.integers(0, 3, (S + 1, H, W)).astype(np.float32) * 0.5
+    sio.savemat(str(tmp_path / "detection_mask_imgidx00003.mat"), {"detection_mask": mask})
+    r = subprocess.run([cli(), "--mask_dump", str(S), str(H), str(W), "--detection_masks_dir",
+                        str(tmp_path), "--first", "2"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got, cur = [], None
+    for line in r.stdout.splitlines():
+        if line.startswith("scale"):
+            cur = []
+            got.append(cur)
+        else:
+            cur.append([float(v) for v in line.split()])
+    assert np.array_equal(np.array(got, np.float32), mask[:S])
+    r = subprocess.run([cli(), "--mask_dump", str(S), str(H + 1), str(W), "--detection_masks_dir",
+                        str(tmp_path), "--first", "2"], capture_output=True, text=True)
+    assert r.returncode == 1 and "detection_mask is not" in r.stderr
+    r = subprocess.run([cli(), "--mask_dump", str(S), str(H), str(W), "--detection_masks_dir",
+                        str(tmp_path), "--first", "0"], capture_output=True, text=True)
+    assert r.returncode == 1  # no file for image 0
+
+
 def test_cli_reports_a_missing_experiment(tmp_path):
     r = subprocess.run([cli(), "--find_obj", "--expdir", str(tmp_path / "none")],
                        capture_output=True, text=True)
