@@ -195,6 +195,26 @@ def test_bilinear_exact_hit_and_edge(orc):
     assert outd[4, 6] == g[2, 3]
 
 
+def test_direct_transform_last_writer_wins(orc):
+    """TM_DIRECT (multi_array_transform.hpp:173-193) loops x1 outer, y1 inner and
+    writes every cell != default: where a half-pixel grid puts several cells on
+    one pixel, the last of them in that loop order stays."""
+    g = np.arange(1, 1 + 4 * 5, dtype=np.float32).reshape(4, 5)  # [ny][nx], no zeros
+    T = np.array([[0.5, 0.0, 0.0], [0.0, 0.5, 0.0], [0, 0, 1]])
+    out = orc.transform_grid(g, (3, 3), T, 0.0, 2)
+    want = np.zeros((3, 3), np.float32)
+    for x1 in range(5):
+        for y1 in range(4):
+            x3, y3 = math.floor(0.5 * x1 + 0.5), math.floor(0.5 * y1 + 0.5)
+            if x3 < 3 and y3 < 3:
+                want[y3, x3] = g[y1, x1]
+    assert np.array_equal(out, want)
+    assert out[1, 1] == g[2, 2]  # cells (1, 1), (1, 2), (2, 1), (2, 2) land on (1, 1)
+    g[2, 2] = 0.0  # a default cell writes nothing: the previous writer stays
+    out = orc.transform_grid(g, (3, 3), T, 0.0, 2)
+    assert out[1, 1] == g[1, 2]
+
+
 def test_clip_log(orc):
     g = np.array([-0.5, 0.0, 0.25, 1.0], dtype=np.float32)
     out = orc.clip_log(g)
